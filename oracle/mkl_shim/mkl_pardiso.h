@@ -1,0 +1,2 @@
+/* MKL-API shim (oracle test infrastructure): everything lives in mkl.h. */
+#include "mkl.h"

@@ -1,0 +1,104 @@
+"""Workload definitions shared by the golden-vector generator, the tests and bench.py.
+
+Each case names a lattice, its material and its load schedule in the terms the
+LPM-C reference uses (src/lpmc_project.c:75-335): lattice id, particle radius,
+box (createCuboid input), per-type elastic constants, J2 parameters and
+per-step displacement boundary conditions given as (type, axis, step).
+
+Rigid-body pin: the SC cases fix only z on the bottom face, which leaves x/y
+translation and z-rotation free (a singular stiffness).  Two bottom particles
+are additionally pinned (one in x and y, one in y), removing exactly those
+three modes without loading the specimen.
+"""
+import numpy as np
+
+# particle types (reference convention: type selects BCs and Ce rows)
+T_INTERIOR, T_TOP, T_BOTTOM, T_FULL, T_PIN_XY, T_PIN_Y = 0, 1, 2, 3, 4, 5
+NTYPE = 6
+
+
+def iso_cubic(E, nu):
+    """C11, C12, C44 of an isotropic solid (src/lpmc_project.c:188-190)."""
+    C11 = E * (1.0 - nu) / (1.0 + nu) / (1.0 - 2.0 * nu)
+    C12 = E * nu / (1.0 + nu) / (1.0 - 2.0 * nu)
+    C44 = E / 2.0 / (1.0 + nu)
+    return C11, C12, C44
+
+
+def sc_box(nx, ny, nz, radius):
+    """Box for createCuboid (lattice 2) that holds exactly nx*ny*nz particles.
+
+    x starts at box[0]; y and z start at -|box diagonal| (src/initialization.c:247-282),
+    so the y/z boxes are widened by half a spacing on both sides to capture
+    exactly ny/nz grid lines whatever their offset.
+    """
+    h = 2.0 * radius
+    return [0.0, (nx - 1) * h + 0.5 * h, -0.5 * h, (ny - 1) * h + 0.5 * h,
+            -0.5 * h, (nz - 1) * h + 0.5 * h]
+
+
+def sc_types(xyz, nb, radius, nneighbors=18):
+    """Types: top/bottom layers, full-neighbour interior, and the two pins."""
+    n = xyz.shape[0]
+    t = np.full(n, T_INTERIOR, dtype=np.int32)
+    zmax, zmin = xyz[:, 2].max(), xyz[:, 2].min()
+    top = xyz[:, 2] >= zmax - 1.2 * radius
+    bot = xyz[:, 2] <= zmin + 1.2 * radius
+    t[top] = T_TOP
+    t[bot] = T_BOTTOM
+    t[nb == nneighbors] = T_FULL
+    bidx = np.nonzero(bot)[0]
+    p1 = bidx[np.lexsort((xyz[bidx, 0], xyz[bidx, 1]))[0]]          # min y, then min x
+    cand = bidx[np.isclose(xyz[bidx, 1], xyz[p1, 1])]
+    p2 = cand[np.argmax(xyz[cand, 0])]                               # same row, max x
+    t[p1] = T_PIN_XY
+    t[p2] = T_PIN_Y
+    return t
+
+
+def sc_bcs(step_z):
+    """Per-step BCs: bottom z fixed, pins, top z displaced by step_z."""
+    return [(T_BOTTOM, "z", 0.0), (T_PIN_XY, "x", 0.0), (T_PIN_XY, "y", 0.0),
+            (T_PIN_XY, "z", 0.0), (T_PIN_Y, "y", 0.0), (T_PIN_Y, "z", 0.0),
+            (T_TOP, "z", step_z)]
+
+
+def cyclic_schedule(amplitude, steps_per_quarter, cycles):
+    """Increments 0->+A->0->-A->0 per cycle, steps_per_quarter equal steps each."""
+    inc = amplitude / steps_per_quarter
+    one = [inc] * steps_per_quarter + [-inc] * (2 * steps_per_quarter) + [inc] * steps_per_quarter
+    return one * cycles
+
+
+class SCCase:
+    """SC elastoplastic cyclic case (C1 at n=10, C2 at n=100)."""
+
+    def __init__(self, n=10, radius=0.1, E=200e3, nu=0.3, sigmay=250.0, H=2000.0,
+                 strain=0.002, steps_per_quarter=20, cycles=2, newton_tol=1e-8,
+                 e_noise=0.0, seed=1):
+        self.n = n
+        self.radius = radius
+        self.lattice = 2
+        self.box = sc_box(n, n, n, radius)
+        self.E, self.nu, self.sigmay, self.H = E, nu, sigmay, H
+        self.height = (n - 1) * 2.0 * radius
+        self.schedule = cyclic_schedule(strain * self.height, steps_per_quarter, cycles)
+        self.newton_tol = newton_tol
+        self.e_noise = e_noise
+        self.seed = seed
+
+    def ce_per_type(self):
+        return np.tile(iso_cubic(self.E, self.nu), (NTYPE, 1))
+
+
+def splitmix64_uniform(seed, count):
+    """Counter-based uniform doubles in [0,1): splitmix64(seed*2^32 + k) >> 11 * 2^-53."""
+    out = np.empty(count, dtype=np.float64)
+    mask = (1 << 64) - 1
+    for k in range(count):
+        z = ((seed << 32) + k + 0x9E3779B97F4A7C15) & mask
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & mask
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & mask
+        z = z ^ (z >> 31)
+        out[k] = (z >> 11) * (1.0 / 9007199254740992.0)
+    return out

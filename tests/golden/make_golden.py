@@ -1,0 +1,123 @@
+"""Generate the golden vectors under tests/golden/ from the LPM-C reference itself.
+
+Runs the reference's own C sources (built by oracle/build_ref.sh into
+oracle/_ref/libref_lpm.so, MKL replaced by the public-API shim) on the SC
+cyclic case at 10x10x10 (C1) and a small FCC crystal-plasticity case, and
+stores inputs and outputs as compressed .npz fixtures.  The reference runs
+single-threaded (its OpenMP loops race, see src/constitutive.c:95 with
+:495-515,625-645), so the fixtures are deterministic.
+
+    python tests/golden/make_golden.py [--steps N]
+
+Reference CG tolerances are overridden to |r|^2 <= 1e-20 |r0|^2 (1e-10 on the
+norm, absolute 0) because the hard-coded 1e-8 / 1e-12 (src/solver.c:221-222)
+makes a Newton tolerance of 1e-8 unreachable at these force levels.
+"""
+import argparse
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, HERE)
+
+import refdrv as R  # noqa: E402
+import cases  # noqa: E402
+
+
+def snapshot(n, nn):
+    """State the reference keeps after a converged step (slot 1 = converged)."""
+    return dict(
+        xyz=R.get_d2("xyz", n, 3),
+        F=R.get_d2("F", n, nn),
+        csx=R.get_d2("csx", n, nn), csy=R.get_d2("csy", n, nn), csz=R.get_d2("csz", n, nn),
+        dLp=R.get_d3("dLp", n, nn, 1),
+        alpha=R.get_d2("J2_alpha", n, 3)[:, 1],
+        beta=R.get_d3("J2_beta", n, 6, 1),
+        Pin=R.get_d1("Pin", 3 * n),
+        Pex=R.get_d1("Pex", 3 * n),
+        stress=R.get_d2("stress_tensor", n, 6),
+    )
+
+
+def sc_case(out, nsteps, tag="sc10"):
+    case = cases.SCCase(n=10)
+    t0 = time.time()
+    n = R.setup(case.lattice, case.radius, case.box)
+    nn = R.gint("nneighbors")
+    xyz0 = R.get_d2("xyz", n, 3)
+    nb = R.get_i1("nb", n)
+    types = cases.sc_types(xyz0, nb, case.radius)
+    R.set_types(types, cases.NTYPE)
+    R.material(case.ce_per_type(), 0, np.full(n, case.sigmay), 0.0, case.H)
+    R.init_state()
+    R.set_cg_tol(1e-20, 0.0)
+    kp = R.get_i2("K_pointer", n + 1, 2)
+    nnz = int(kp[n, 1])
+    setup = dict(
+        box=np.array(case.box), radius=case.radius, types=types, xyz=xyz0,
+        neighbors=R.get_i2("neighbors", n, nn), nsign=R.get_i2("nsign", n, nn), nb=nb,
+        distance_initial=R.get_d2("distance_initial", n, nn),
+        csx_initial=R.get_d2("csx_initial", n, nn), csy_initial=R.get_d2("csy_initial", n, nn),
+        csz_initial=R.get_d2("csz_initial", n, nn),
+        conn=R.get_i2("conn", n, R.gint("nneighbors_AFEM") + 1), nb_conn=R.get_i1("nb_conn", n),
+        K_pointer=kp, Kn=R.get_d2("Kn", n, nn), Tv=R.get_d2("Tv", n, nn),
+    )
+    np.savez_compressed(os.path.join(out, f"{tag}_setup.npz"), **setup)
+
+    sched = case.schedule[:nsteps]
+    rec = {k: [] for k in ("iters", "nres0", "nreac0", "nres", "cg", "disp_top", "react_top")}
+    snaps = {}
+    snap_steps = {1, 13, 14, 20, 40, len(sched)}
+    for s, stp in enumerate(sched, start=1):
+        if s == 1 or s == 14:
+            # stiffness at the converged state entering this step (FD, upper CSR)
+            state_in = snapshot(n, nn)
+            with R.quiet():
+                R.lib().calcStiffness3DFiniteDifference(6)
+            K = R.get_d1("K_global", nnz)
+            IK = R.get_i1("IK", 3 * n + 1)
+            JK = R.get_i1("JK", nnz)
+            np.savez_compressed(os.path.join(out, f"{tag}_K_step{s}.npz"), K_global=K, IK=IK, JK=JK,
+                                **{"in_" + k: v for k, v in state_in.items()})
+        with R.quiet():
+            st = R.load_step(cases.sc_bcs(stp), [], case.newton_tol)
+        xyz = R.get_d2("xyz", n, 3)
+        F = R.get_d2("F", n, nn)
+        csz = R.get_d2("csz", n, nn)
+        top = types == cases.T_TOP
+        rec["iters"].append(st[0])
+        rec["nres0"].append(st[1])
+        rec["nreac0"].append(st[2])
+        rec["nres"].append(st[3])
+        rec["cg"].append(st[4])
+        rec["disp_top"].append((xyz[top, 2].sum() - xyz0[top, 2].sum()) / top.sum())
+        rec["react_top"].append(np.sum(-csz[top] * F[top]))
+        if s in snap_steps:
+            snaps[s] = snapshot(n, nn)
+        print(f"{tag} step {s}: iters {int(st[0])} res {st[3]:.3e} t={time.time() - t0:.1f}s", flush=True)
+    arrs = {k: np.array(v) for k, v in rec.items()}
+    arrs["schedule"] = np.array(sched)
+    for s, d in snaps.items():
+        for k, v in d.items():
+            arrs[f"s{s}_{k}"] = v
+    arrs["snap_steps"] = np.array(sorted(snaps))
+    np.savez_compressed(os.path.join(out, f"{tag}_cyclic.npz"), **arrs)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--out", default=HERE)
+    args = ap.parse_args()
+    if not R.available():
+        sys.exit("oracle/_ref/libref_lpm.so missing: run oracle/build_ref.sh first")
+    sc_case(args.out, args.steps)
+
+
+if __name__ == "__main__":
+    main()
