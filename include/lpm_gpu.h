@@ -1,0 +1,180 @@
+/*
+ * lpm_gpu.h - C ABI of the GB300 (sm_103a) implementation of the LPM-C
+ * quasi-static solve path.
+ *
+ * One context owns one lattice specimen resident on one GPU: particle
+ * positions, bond lists, the fixed block-CSR stiffness pattern, material,
+ * state variables and solver work space.  All entry points return LPM_OK (0)
+ * or a negative LPM_ERR_* code; lpm_last_error() gives the message.  A
+ * context is not thread-safe; use one host thread per context.
+ *
+ * Each entry point replaces one function (or a fixed sequence) of the
+ * reference, cited as file:line of ymlasu/LPM-C.  The reference-named
+ * drop-in symbols operating on the include/lpm.h globals are declared in
+ * lpm_legacy.h.
+ */
+#ifndef LPM_GPU_H
+#define LPM_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LPM_OK 0
+#define LPM_ERR_ARG (-1)      /* bad argument or call order */
+#define LPM_ERR_CUDA (-2)     /* CUDA runtime failure */
+#define LPM_ERR_NOMEM (-3)    /* device or host allocation failed */
+#define LPM_ERR_DEVICE (-4)   /* a device-side check failed (status word) */
+
+/* step status bits (lpm_step_stats.status); the step still completes */
+#define LPM_STATUS_NEWTON_MAXIT 1 /* Newton loop stopped at maxiter (reference: MAXITER) */
+#define LPM_STATUS_CG_MAXIT 2     /* a linear solve stopped at its iteration cap */
+#define LPM_STATUS_NAN 4          /* a residual norm was not finite */
+#define LPM_STATUS_CP_SINGULAR 8  /* singular slip-system Jacobian (reference exits) */
+
+#define LPM_PREC_FP64 0  /* FP64 stiffness, SpMV and PCG */
+#define LPM_PREC_MIXED 1 /* FP32 stiffness/SpMV/PCG inside FP64 iterative refinement */
+
+/* constitutive modes (plmode, src/constitutive.c:88-146) */
+#define LPM_PL_J2 0        /* J2 mixed linear hardening */
+#define LPM_PL_CP 1        /* crystal plasticity (Miehe) */
+#define LPM_PL_PREDICTOR 4 /* elastic incremental predictor */
+#define LPM_PL_ELASTIC 6   /* elastic */
+
+typedef struct lpm_ctx lpm_ctx;
+
+/* same layout as struct dispBCPara (include/lpm.h:83-88) */
+typedef struct {
+    int type;
+    char flag; /* 'x', 'y' or 'z' */
+    double step;
+} lpm_disp_bc;
+
+/* same layout as struct forceBCPara (include/lpm.h:90-99) */
+typedef struct {
+    int type;
+    char flag1;
+    double step1;
+    char flag2;
+    double step2;
+    char flag3;
+    double step3;
+} lpm_force_bc;
+
+typedef struct {
+    int precision;      /* LPM_PREC_FP64 or LPM_PREC_MIXED */
+    double newton_tol;  /* stop when |r| <= tol * max(|r0|, |reaction0|) (TOLITER, include/lpm.h:41) */
+    int newton_maxiter; /* MAXITER (include/lpm.h:39) */
+    double cg_rtol;     /* linear solve: |b - K x| <= cg_rtol * |b| */
+    int cg_maxiter;     /* cap on PCG iterations per solve (FP64) or per inner solve (mixed) */
+    double inner_rtol;  /* mixed: relative tolerance of each FP32 inner PCG solve */
+    int refine_maxiter; /* mixed: cap on FP64 refinement sweeps */
+    int check_every;    /* PCG iterations between host convergence checks (graph chunk) */
+    int use_graphs;     /* capture PCG chunks as CUDA graphs */
+    int spmv_variant;   /* 0 = default; others select alternative SpMV kernels (tuning) */
+} lpm_solver_opts;
+
+typedef struct {
+    int newton_iters;
+    int cg_iters;      /* PCG iterations summed over the step (inner iterations for mixed) */
+    int refine_iters;  /* FP64 refinement sweeps summed over the step */
+    int spmv_calls;
+    int status;        /* LPM_STATUS_* bits */
+    double res0, reac0, res_final;
+    double ms_stiffness, ms_solve, ms_force;
+} lpm_step_stats;
+
+/* ---- context ------------------------------------------------------------ */
+int lpm_create(lpm_ctx **ctx, int device);
+void lpm_destroy(lpm_ctx *ctx);
+const char *lpm_last_error(void);
+/* Launch everything on the given cudaStream_t (NULL = the context's own stream). */
+int lpm_set_stream(lpm_ctx *ctx, void *stream);
+void lpm_default_solver_opts(lpm_solver_opts *opts);
+int lpm_set_solver(lpm_ctx *ctx, const lpm_solver_opts *opts);
+
+/* ---- setup -------------------------------------------------------------- */
+/* createCuboid (src/initialization.c:6-459, lattice 2 = SC, 3 = FCC, no
+ * rotation) + initMatrices + searchNormalNeighbor (src/neighbor.c:9-46) +
+ * searchAFEMNeighbor (src/neighbor.c:49-141).  Returns the particle count
+ * (>0) or an error code. */
+int lpm_setup_lattice(lpm_ctx *ctx, int lattice, double radius, const double box[6]);
+/* Same, with caller-supplied positions (n x 3, row-major). */
+int lpm_setup_particles(lpm_ctx *ctx, int lattice, double radius, int n, const double *xyz);
+int lpm_nparticle(const lpm_ctx *ctx);
+/* particle type: selects boundary conditions as in setDispBC/setForceBC */
+int lpm_set_types(lpm_ctx *ctx, const int *type);
+/* calcKnTv (src/stiffness.c:145-235) with per-particle C11, C12, C44, plus
+ * per-particle yield stress and hardening modulus (sigmay, J2_H) and the
+ * kinematic share J2_xi; plmode selects the constitutive law. */
+int lpm_set_material(lpm_ctx *ctx, const double *c11, const double *c12, const double *c44,
+                     const double *sigmay, const double *hardening, double xi, int plmode);
+/* crystal plasticity constants: tau0, taus, h0, p, q, eta, maxloop, dtime
+ * (cp_tau0, cp_taus, cp_h0, cp_p, cp_q, cp_eta, cp_maxloop, dtime of include/lpm.h) */
+int lpm_set_cp(lpm_ctx *ctx, const double cp[8]);
+/* computedL (src/lpm_basic.c:252-291), slipSysDefine3D
+ * (src/initialization.c:563-638) and computeCab (src/constitutive.c:1864-1917);
+ * resets the state variables to zero. */
+int lpm_init_state(lpm_ctx *ctx);
+
+/* ---- the hot path -------------------------------------------------------- */
+/* One load step: src/lpmc_project.c:385-471 (stiffness, displacement and force
+ * BCs, elastic predictor, Newton loop of PCG solve + bond force update +
+ * residual, state commit).  Damage is not modelled. */
+int lpm_load_step(lpm_ctx *ctx, int nbd, const lpm_disp_bc *dbc, int nbf, const lpm_force_bc *fbc,
+                  lpm_step_stats *stats);
+/* calcStiffness3DFiniteDifference (src/stiffness.c:384-516): the elastic
+ * tangent at the current configuration, computed analytically, symmetrised
+ * as the reference does, into the device block-CSR. */
+int lpm_assemble_stiffness(lpm_ctx *ctx);
+/* setDispBC / setForceBC (src/boundary.c:12-70) on the device state. */
+int lpm_apply_bc(lpm_ctx *ctx, int nbd, const lpm_disp_bc *dbc, int nbf, const lpm_force_bc *fbc);
+/* computeBondForceGeneral (src/constitutive.c:88-146) for plmode 0, 1, 4, 6,
+ * including computeStress and switchStateV(2), then updateRR
+ * (src/stiffness.c:519-534).  norms (may be NULL): |residual|, |reaction|. */
+int lpm_compute_force(lpm_ctx *ctx, int plmode, double norms[2]);
+/* switchStateV (src/constitutive.c:10-85): 0 = converged -> current,
+ * 1 = current -> converged. */
+int lpm_switch_state(lpm_ctx *ctx, int flag);
+/* solverCG (src/solver.c:188-270) with setDispBC_stiffnessUpdate3D
+ * (src/boundary.c:159-281) folded in: solve K du = residual on the
+ * unconstrained DOFs, then xyz += du. */
+int lpm_solve(lpm_ctx *ctx, lpm_step_stats *stats);
+/* Start-of-step bookkeeping of src/lpmc_project.c:387-389: remember xyz and
+ * the bond forces for the elastic predictor. */
+int lpm_begin_step(lpm_ctx *ctx);
+
+/* ---- data exchange --------------------------------------------------------- */
+/* Copy a named array between host and device.  Names and shapes (n = particles,
+ * nn = bond slots per particle, row-major like the reference's [i][j]):
+ *   xyz, xyz_initial, xyz_temp (n x 3), Pin, Pex, residual, disp (3n),
+ *   F, dL, csx, csy, csz, Kn, Tv, distance_initial (n x nn),
+ *   dLp (n x nn, converged), dLp_trial, J2_alpha (n, converged), J2_beta (n x 6),
+ *   stress_tensor (n x 6), neighbors, nsign (n x nn, int32), nb (n, int32),
+ *   dispBC_index (3n, int32), type (n, int32), conn (n x 61, int32), nb_conn (n),
+ *   cp_gy (n x nslip), cp_A (n), cp_A_single (n x nslip), J2_dlambda (n). */
+int lpm_get(lpm_ctx *ctx, const char *name, void *dst, size_t bytes);
+int lpm_set(lpm_ctx *ctx, const char *name, const void *src, size_t bytes);
+int lpm_get_sizes(const lpm_ctx *ctx, int *n, int *nn, int *nslip, long long *nnz_blocks);
+/* The current stiffness in the reference's layout: 1-based upper-triangular
+ * scalar CSR (K_global, IK, JK of calcStiffness3DFiniteDifference).  Any
+ * pointer may be NULL; *nnz receives the entry count. */
+int lpm_export_upper_csr(lpm_ctx *ctx, double *K_global, int *IK, int *JK, long long *nnz);
+/* y = K x on the full (unmodified) block-CSR; x, y host arrays of 3n. */
+int lpm_spmv(lpm_ctx *ctx, const double *x, double *y);
+/* Solve K x = b (with the BC mask) for a host right-hand side; no xyz update. */
+int lpm_solve_rhs(lpm_ctx *ctx, const double *b, double *x, lpm_step_stats *stats);
+/* Average duration (ms) of the SpMV kernel launches since the last reset,
+ * measured with CUDA events on the context's stream, and their count. */
+int lpm_spmv_timing(lpm_ctx *ctx, double *avg_ms, long long *count, int reset);
+/* Block-CSR byte count of one SpMV (values + column indices + vectors),
+ * for the given precision, unpadded (algorithmic). */
+double lpm_spmv_bytes(const lpm_ctx *ctx, int precision);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,1256 @@
+// C ABI of the library (include/lpm_gpu.h): context lifetime, specimen setup,
+// data exchange, and the host side of the load-step loop
+// (src/lpmc_project.c:382-471) that sequences the device kernels.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include "lpm_internal.h"
+
+namespace lpm {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg)
+{
+    g_err = msg;
+    return code;
+}
+
+template <typename T>
+static int dalloc(T *&p, size_t count)
+{
+    if (p)
+        cudaFree(p);
+    p = nullptr;
+    if (count == 0)
+        count = 1;
+    cudaError_t e = cudaMalloc((void **)&p, count * sizeof(T));
+    if (e != cudaSuccess) {
+        p = nullptr;
+        return fail(LPM_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    cudaMemset(p, 0, count * sizeof(T));
+    return LPM_OK;
+}
+
+template <typename T>
+static void dfree(T *&p)
+{
+    if (p)
+        cudaFree(p);
+    p = nullptr;
+}
+
+Ctx::~Ctx()
+{
+    cudaSetDevice(device);
+    void **all[] = {(void **)&xyz, (void **)&xyz0, (void **)&xyz_temp, (void **)&Pin, (void **)&Pex,
+                    (void **)&res, (void **)&du, (void **)&mask, (void **)&type, (void **)&G, (void **)&sy,
+                    (void **)&Hh, (void **)&stress, (void **)&dlambda, (void **)&nbr, (void **)&shell,
+                    (void **)&rev, (void **)&nbv, (void **)&nconn_d, (void **)&L0, (void **)&Kn, (void **)&Tv,
+                    (void **)&oppv, (void **)&dL, (void **)&csx, (void **)&csy, (void **)&csz, (void **)&F,
+                    (void **)&F_prev, (void **)&S, (void **)&T, (void **)&ddL, (void **)&dS, (void **)&dT,
+                    (void **)&Cab, (void **)&sch, (void **)&jact, (void **)&U, (void **)&W,
+                    (void **)&rowoff, (void **)&npad, (void **)&cols, (void **)&Kd, (void **)&Kf,
+                    (void **)&Pinv_d, (void **)&Pinv_f, (void **)&x_d, (void **)&r_d, (void **)&p_d,
+                    (void **)&q_d, (void **)&z_d, (void **)&x_f, (void **)&r_f, (void **)&p_f, (void **)&q_f,
+                    (void **)&z_f, (void **)&b_d, (void **)&sc, (void **)&partials, (void **)&counter,
+                    (void **)&norms, (void **)&status};
+    for (void **p : all)
+        if (*p) {
+            cudaFree(*p);
+            *p = nullptr;
+        }
+    for (int s = 0; s < 3; s++) {
+        double **st[] = {&dLp[s], &alpha[s], &beta[s], &gy[s], &As[s], &A[s]};
+        for (double **p : st)
+            if (*p) {
+                cudaFree(*p);
+                *p = nullptr;
+            }
+    }
+    if (sc_host)
+        cudaFreeHost(sc_host);
+    if (norms_host)
+        cudaFreeHost(norms_host);
+    if (status_host)
+        cudaFreeHost(status_host);
+    if (graph_fp64)
+        cudaGraphExecDestroy(graph_fp64);
+    if (graph_fp32)
+        cudaGraphExecDestroy(graph_fp32);
+    if (ev_a)
+        cudaEventDestroy(ev_a);
+    if (ev_b)
+        cudaEventDestroy(ev_b);
+    if (own_stream && stream)
+        cudaStreamDestroy(stream);
+}
+
+// ---- helpers -----------------------------------------------------------------
+
+static int sync(Ctx &c)
+{
+    cudaError_t e = cudaStreamSynchronize(c.stream);
+    if (e != cudaSuccess)
+        return fail(LPM_ERR_CUDA, std::string("kernel execution: ") + cudaGetErrorString(e));
+    e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return fail(LPM_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    return LPM_OK;
+}
+
+// read the residual / reaction norms written by the last force kernel
+static int read_norms(Ctx &c, double &res, double &reac)
+{
+    LPM_CUDA(cudaMemcpyAsync(c.norms_host, c.norms, 4 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    int rc = sync(c);
+    if (rc)
+        return rc;
+    res = std::sqrt(c.norms_host[0]);
+    reac = std::sqrt(c.norms_host[1]);
+    return LPM_OK;
+}
+
+static void copy_state(Ctx &c, int to, int from)
+{
+    const size_t n = c.n;
+    cudaMemcpyAsync(c.dLp[to], c.dLp[from], n * LPM_NN * sizeof(double), cudaMemcpyDeviceToDevice, c.stream);
+    cudaMemcpyAsync(c.alpha[to], c.alpha[from], n * sizeof(double), cudaMemcpyDeviceToDevice, c.stream);
+    cudaMemcpyAsync(c.beta[to], c.beta[from], 6 * n * sizeof(double), cudaMemcpyDeviceToDevice, c.stream);
+    if (c.nslip) {
+        cudaMemcpyAsync(c.gy[to], c.gy[from], n * c.nslip * sizeof(double), cudaMemcpyDeviceToDevice, c.stream);
+        cudaMemcpyAsync(c.As[to], c.As[from], n * c.nslip * sizeof(double), cudaMemcpyDeviceToDevice, c.stream);
+        cudaMemcpyAsync(c.A[to], c.A[from], n * sizeof(double), cudaMemcpyDeviceToDevice, c.stream);
+    }
+}
+
+// switchStateV (src/constitutive.c:10-85)
+static void switch_state(Ctx &c, int flag)
+{
+    if (flag == 0)
+        copy_state(c, 0, 1);
+    else if (flag == 1)
+        copy_state(c, 1, 0);
+    else
+        copy_state(c, 0, 2);
+}
+
+// transposes between host row-major [n][k] and device [k][n]
+template <typename T>
+static void to_slot_major(const T *src, T *dst, int n, int k)
+{
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < k; j++)
+            dst[(size_t)j * n + i] = src[(size_t)i * k + j];
+}
+
+template <typename T>
+static void from_slot_major(const T *src, T *dst, int n, int k)
+{
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < k; j++)
+            dst[(size_t)i * k + j] = src[(size_t)j * n + i];
+}
+
+static int upload_particles(Ctx &c, dvec4 *dst, const double *src3)
+{
+    LPM_CUDA(cudaStreamSynchronize(c.stream));
+    std::vector<dvec4> t(c.n);
+    for (int i = 0; i < c.n; i++)
+        t[i] = make_dvec4(src3[3 * i], src3[3 * i + 1], src3[3 * i + 2], 0.0);
+    LPM_CUDA(cudaMemcpy(dst, t.data(), sizeof(dvec4) * c.n, cudaMemcpyHostToDevice));
+    return LPM_OK;
+}
+
+static int download_particles(Ctx &c, const dvec4 *src, double *dst3)
+{
+    std::vector<dvec4> t(c.n);
+    LPM_CUDA(cudaMemcpyAsync(t.data(), src, sizeof(dvec4) * c.n, cudaMemcpyDeviceToHost, c.stream));
+    int rc = sync(c);
+    if (rc)
+        return rc;
+    for (int i = 0; i < c.n; i++) {
+        dst3[3 * i] = t[i].x;
+        dst3[3 * i + 1] = t[i].y;
+        dst3[3 * i + 2] = t[i].z;
+    }
+    return LPM_OK;
+}
+
+// ---- device allocation for a specimen ----------------------------------------
+
+static int alloc_specimen(Ctx &c)
+{
+    const size_t n = c.n, nb = n * LPM_NN;
+    int rc = 0;
+#define A_(p, cnt)            \
+    if ((rc = dalloc(p, cnt))) \
+        return rc;
+    A_(c.xyz, n) A_(c.xyz0, n) A_(c.xyz_temp, n) A_(c.Pin, n) A_(c.Pex, n) A_(c.res, n) A_(c.du, n)
+    A_(c.mask, n) A_(c.type, n) A_(c.G, n) A_(c.sy, n) A_(c.Hh, n) A_(c.stress, 6 * n) A_(c.dlambda, n)
+    A_(c.nbr, nb) A_(c.shell, nb) A_(c.rev, nb) A_(c.nbv, n) A_(c.nconn_d, n) A_(c.L0, nb) A_(c.Kn, nb)
+    A_(c.Tv, nb) A_(c.oppv, nb) A_(c.dL, nb) A_(c.csx, nb) A_(c.csy, nb) A_(c.csz, nb) A_(c.F, nb)
+    A_(c.F_prev, nb) A_(c.S, n) A_(c.T, n) A_(c.ddL, nb) A_(c.dS, n) A_(c.dT, n) A_(c.U, 6 * n)
+    A_(c.W, 6 * n) A_(c.Pinv_d, 9 * n) A_(c.Pinv_f, 9 * n)
+    A_(c.x_d, n) A_(c.r_d, n) A_(c.p_d, n) A_(c.q_d, n) A_(c.z_d, n) A_(c.b_d, n)
+    A_(c.x_f, n) A_(c.r_f, n) A_(c.p_f, n) A_(c.q_f, n) A_(c.z_f, n)
+    for (int s = 0; s < 3; s++) {
+        A_(c.dLp[s], nb) A_(c.alpha[s], n) A_(c.beta[s], 6 * n)
+    }
+    A_(c.sc, 1) A_(c.norms, 4) A_(c.status, 1) A_(c.counter, 1)
+    const size_t red = std::max<size_t>((n + 63) / 64 + 64, (size_t)red_grid(c) + 64);
+    A_(c.partials, 4 * red)
+    // block-CSR pattern
+    const HostSetup &h = c.hs;
+    c.nblk = h.rowoff[n];
+    c.nblk_real = 0;
+    for (int i = 0; i < c.n; i++)
+        c.nblk_real += h.nconn[i];
+    A_(c.rowoff, n + 1) A_(c.npad, n) A_(c.cols, (size_t)c.nblk)
+#undef A_
+    LPM_CUDA(cudaMemcpy(c.rowoff, h.rowoff.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice));
+    LPM_CUDA(cudaMemcpy(c.npad, h.npad.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    LPM_CUDA(cudaMemcpy(c.cols, h.cols.data(), sizeof(int) * c.nblk, cudaMemcpyHostToDevice));
+    if (!c.sc_host) {
+        LPM_CUDA(cudaMallocHost((void **)&c.sc_host, sizeof(CgScalars)));
+        LPM_CUDA(cudaMallocHost((void **)&c.norms_host, 4 * sizeof(double)));
+        LPM_CUDA(cudaMallocHost((void **)&c.status_host, sizeof(int)));
+    }
+    return LPM_OK;
+}
+
+static int upload_setup(Ctx &c)
+{
+    const HostSetup &h = c.hs;
+    const int n = c.n;
+    const size_t nb = (size_t)n * LPM_NN;
+    int rc = upload_particles(c, c.xyz, h.xyz.data());
+    if (rc)
+        return rc;
+    rc = upload_particles(c, c.xyz0, h.xyz.data());
+    if (rc)
+        return rc;
+    rc = upload_particles(c, c.xyz_temp, h.xyz.data());
+    if (rc)
+        return rc;
+    std::vector<int> ti(nb);
+    std::vector<int8_t> t8(nb);
+    std::vector<double> td(nb);
+    to_slot_major(h.nbr.data(), ti.data(), n, LPM_NN);
+    LPM_CUDA(cudaMemcpy(c.nbr, ti.data(), nb * sizeof(int), cudaMemcpyHostToDevice));
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < LPM_NN; j++) {
+            t8[(size_t)j * n + i] = (int8_t)h.shell[(size_t)i * LPM_NN + j];
+        }
+    LPM_CUDA(cudaMemcpy(c.shell, t8.data(), nb, cudaMemcpyHostToDevice));
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < LPM_NN; j++)
+            t8[(size_t)j * n + i] = (int8_t)h.rev[(size_t)i * LPM_NN + j];
+    LPM_CUDA(cudaMemcpy(c.rev, t8.data(), nb, cudaMemcpyHostToDevice));
+    std::vector<int8_t> v8(n);
+    for (int i = 0; i < n; i++)
+        v8[i] = (int8_t)h.nb[i];
+    LPM_CUDA(cudaMemcpy(c.nbv, v8.data(), n, cudaMemcpyHostToDevice));
+    for (int i = 0; i < n; i++)
+        v8[i] = (int8_t)h.nconn[i];
+    LPM_CUDA(cudaMemcpy(c.nconn_d, v8.data(), n, cudaMemcpyHostToDevice));
+    to_slot_major(h.L0.data(), td.data(), n, LPM_NN);
+    LPM_CUDA(cudaMemcpy(c.L0, td.data(), nb * sizeof(double), cudaMemcpyHostToDevice));
+    to_slot_major(h.oppv.data(), td.data(), n, LPM_NN);
+    LPM_CUDA(cudaMemcpy(c.oppv, td.data(), nb * sizeof(double), cudaMemcpyHostToDevice));
+    std::vector<uint8_t> m(n, 7);
+    LPM_CUDA(cudaMemcpy(c.mask, m.data(), n, cudaMemcpyHostToDevice));
+    return LPM_OK;
+}
+
+static int setup_common(Ctx &c)
+{
+    HostSetup &h = c.hs;
+    build_neighbors(h);
+    build_afem(h);
+    build_bond_tables(h);
+    build_block_pattern(h);
+    c.n = h.n;
+    c.ready = false;
+    c.have_K = false;
+    c.nslip = 0;
+    int rc = alloc_specimen(c);
+    if (rc)
+        return rc;
+    rc = upload_setup(c);
+    if (rc)
+        return rc;
+    return c.n;
+}
+
+}  // namespace lpm
+
+using namespace lpm;
+
+// ---- C ABI -------------------------------------------------------------------
+
+extern "C" {
+
+const char *lpm_last_error(void) { return g_err.c_str(); }
+
+void lpm_default_solver_opts(lpm_solver_opts *o)
+{
+    o->precision = LPM_PREC_FP64;
+    o->newton_tol = 1e-8;
+    o->newton_maxiter = 100;
+    o->cg_rtol = 1e-10;
+    o->cg_maxiter = 20000;
+    o->inner_rtol = 1e-4;
+    o->refine_maxiter = 40;
+    o->check_every = 16;
+    o->use_graphs = 1;
+    o->spmv_variant = 0;
+}
+
+int lpm_create(lpm_ctx **out, int device)
+{
+    if (!out)
+        return fail(LPM_ERR_ARG, "null output pointer");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0)
+        return fail(LPM_ERR_CUDA, "no CUDA device available");
+    if (device < 0 || device >= ndev)
+        return fail(LPM_ERR_ARG, "device index out of range");
+    lpm_ctx *x = new (std::nothrow) lpm_ctx;
+    if (!x)
+        return fail(LPM_ERR_NOMEM, "host allocation failed");
+    Ctx &c = x->c;
+    c.device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete x;
+        return fail(LPM_ERR_CUDA, "stream creation failed");
+    }
+    c.own_stream = true;
+    cudaEventCreate(&c.ev_a);
+    cudaEventCreate(&c.ev_b);
+    lpm_default_solver_opts(&c.opts);
+    *out = x;
+    return LPM_OK;
+}
+
+void lpm_destroy(lpm_ctx *ctx) { delete ctx; }
+
+int lpm_set_stream(lpm_ctx *ctx, void *stream)
+{
+    if (!ctx)
+        return fail(LPM_ERR_ARG, "null context");
+    Ctx &c = ctx->c;
+    if (c.graph_fp64) {
+        cudaGraphExecDestroy(c.graph_fp64);
+        c.graph_fp64 = nullptr;
+    }
+    if (c.graph_fp32) {
+        cudaGraphExecDestroy(c.graph_fp32);
+        c.graph_fp32 = nullptr;
+    }
+    if (stream) {
+        if (c.own_stream && c.stream)
+            cudaStreamDestroy(c.stream);
+        c.stream = (cudaStream_t)stream;
+        c.own_stream = false;
+    } else if (!c.own_stream) {
+        cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking);
+        c.own_stream = true;
+    }
+    return LPM_OK;
+}
+
+int lpm_set_solver(lpm_ctx *ctx, const lpm_solver_opts *o)
+{
+    if (!ctx || !o)
+        return fail(LPM_ERR_ARG, "null argument");
+    if (o->precision != LPM_PREC_FP64 && o->precision != LPM_PREC_MIXED)
+        return fail(LPM_ERR_ARG, "unknown precision");
+    if (!(o->cg_rtol > 0) || o->cg_maxiter <= 0 || o->newton_maxiter < 0 || o->check_every <= 0)
+        return fail(LPM_ERR_ARG, "invalid solver options");
+    Ctx &c = ctx->c;
+    const bool prec_change = c.opts.precision != o->precision;
+    c.opts = *o;
+    if (prec_change)
+        c.have_K = false;
+    if (c.graph_fp64) {
+        cudaGraphExecDestroy(c.graph_fp64);
+        c.graph_fp64 = nullptr;
+    }
+    if (c.graph_fp32) {
+        cudaGraphExecDestroy(c.graph_fp32);
+        c.graph_fp32 = nullptr;
+    }
+    return LPM_OK;
+}
+
+int lpm_setup_lattice(lpm_ctx *ctx, int lattice, double radius, const double box[6])
+{
+    if (!ctx || !box)
+        return fail(LPM_ERR_ARG, "null argument");
+    Ctx &c = ctx->c;
+    cudaSetDevice(c.device);
+    c.hs = HostSetup();
+    int rc = build_lattice(c.hs, lattice, radius, box);
+    if (rc < 0)
+        return rc;
+    return setup_common(c);
+}
+
+int lpm_setup_particles(lpm_ctx *ctx, int lattice, double radius, int n, const double *xyz)
+{
+    if (!ctx)
+        return fail(LPM_ERR_ARG, "null context");
+    Ctx &c = ctx->c;
+    cudaSetDevice(c.device);
+    c.hs = HostSetup();
+    int rc = build_particles(c.hs, lattice, radius, n, xyz);
+    if (rc < 0)
+        return rc;
+    return setup_common(c);
+}
+
+int lpm_nparticle(const lpm_ctx *ctx) { return ctx ? ctx->c.n : 0; }
+
+int lpm_get_sizes(const lpm_ctx *ctx, int *n, int *nn, int *nslip, long long *nnzb)
+{
+    if (!ctx)
+        return fail(LPM_ERR_ARG, "null context");
+    if (n)
+        *n = ctx->c.n;
+    if (nn)
+        *nn = LPM_NN;
+    if (nslip)
+        *nslip = ctx->c.nslip;
+    if (nnzb)
+        *nnzb = ctx->c.nblk_real;
+    return LPM_OK;
+}
+
+int lpm_set_types(lpm_ctx *ctx, const int *type)
+{
+    if (!ctx || !type || ctx->c.n <= 0)
+        return fail(LPM_ERR_ARG, "set up the specimen before its types");
+    LPM_CUDA(cudaMemcpy(ctx->c.type, type, sizeof(int) * ctx->c.n, cudaMemcpyHostToDevice));
+    return LPM_OK;
+}
+
+int lpm_set_material(lpm_ctx *ctx, const double *c11, const double *c12, const double *c44,
+                     const double *sigmay, const double *hardening, double xi, int plmode)
+{
+    if (!ctx || !c11 || !c12 || !c44 || ctx->c.n <= 0)
+        return fail(LPM_ERR_ARG, "set up the specimen and pass C11, C12, C44 per particle");
+    Ctx &c = ctx->c;
+    LPM_CUDA(cudaStreamSynchronize(c.stream));
+    if (plmode != LPM_PL_J2 && plmode != LPM_PL_CP && plmode != LPM_PL_ELASTIC)
+        return fail(LPM_ERR_ARG, "plmode must be 0 (J2), 1 (crystal plasticity) or 6 (elastic)");
+    if (plmode == LPM_PL_CP && c.hs.lattice != 3)
+        return fail(LPM_ERR_ARG, "crystal plasticity needs the FCC lattice (3)");
+    const int n = c.n;
+    const HostSetup &h = c.hs;
+    std::vector<double> knt(3 * (size_t)n);
+    kntv_per_particle(h.lattice, h.radius, c11, c12, c44, n, knt.data());
+    std::vector<double> kn((size_t)n * LPM_NN, 0.0), tv((size_t)n * LPM_NN, 0.0);
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < h.nb[i]; j++) {
+            const size_t b = (size_t)i * LPM_NN + j;
+            const int p = h.nbr[b], s = h.shell[b];
+            if (h.lattice == 2) {  // src/stiffness.c:192-200, averaged over the bond ends
+                kn[b] = 0.5 * (knt[3 * i + s] + knt[3 * p + s]);
+                tv[b] = 0.5 * (knt[3 * i + 2] + knt[3 * p + 2]);
+            } else {               // src/stiffness.c:223-232, the particle's own values
+                kn[b] = knt[3 * i + s];
+                tv[b] = knt[3 * i + 2];
+            }
+        }
+    std::vector<double> t((size_t)n * LPM_NN);
+    to_slot_major(kn.data(), t.data(), n, LPM_NN);
+    LPM_CUDA(cudaMemcpy(c.Kn, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice));
+    to_slot_major(tv.data(), t.data(), n, LPM_NN);
+    LPM_CUDA(cudaMemcpy(c.Tv, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice));
+    LPM_CUDA(cudaMemcpy(c.G, c44, sizeof(double) * n, cudaMemcpyHostToDevice));
+    std::vector<double> z(n, 0.0);
+    LPM_CUDA(cudaMemcpy(c.sy, sigmay ? sigmay : z.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    LPM_CUDA(cudaMemcpy(c.Hh, hardening ? hardening : z.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    c.xi = xi;
+    c.plmode = plmode;
+    c.have_K = false;
+    return LPM_OK;
+}
+
+int lpm_set_cp(lpm_ctx *ctx, const double cp[8])
+{
+    if (!ctx || !cp)
+        return fail(LPM_ERR_ARG, "null argument");
+    if (!(cp[3] > 0) || !(cp[7] > 0) || !(cp[1] > cp[0]))
+        return fail(LPM_ERR_ARG, "crystal plasticity needs p > 0, dtime > 0 and taus > tau0");
+    std::memcpy(ctx->c.cp, cp, sizeof(ctx->c.cp));
+    return LPM_OK;
+}
+
+int lpm_init_state(lpm_ctx *ctx)
+{
+    if (!ctx || ctx->c.n <= 0)
+        return fail(LPM_ERR_ARG, "set up the specimen first");
+    Ctx &c = ctx->c;
+    const size_t n = c.n, nb = n * LPM_NN;
+    for (int s = 0; s < 3; s++) {
+        LPM_CUDA(cudaMemsetAsync(c.dLp[s], 0, nb * sizeof(double), c.stream));
+        LPM_CUDA(cudaMemsetAsync(c.alpha[s], 0, n * sizeof(double), c.stream));
+        LPM_CUDA(cudaMemsetAsync(c.beta[s], 0, 6 * n * sizeof(double), c.stream));
+    }
+    LPM_CUDA(cudaMemsetAsync(c.F, 0, nb * sizeof(double), c.stream));
+    LPM_CUDA(cudaMemsetAsync(c.F_prev, 0, nb * sizeof(double), c.stream));
+    LPM_CUDA(cudaMemsetAsync(c.Pex, 0, n * sizeof(dvec4), c.stream));
+    LPM_CUDA(cudaMemsetAsync(c.Pin, 0, n * sizeof(dvec4), c.stream));
+    LPM_CUDA(cudaMemsetAsync(c.status, 0, sizeof(int), c.stream));
+    LPM_CUDA(cudaMemcpyAsync(c.xyz, c.xyz0, n * sizeof(dvec4), cudaMemcpyDeviceToDevice, c.stream));
+    std::vector<uint8_t> m(n, 7);
+    LPM_CUDA(cudaMemcpy(c.mask, m.data(), n, cudaMemcpyHostToDevice));
+    // computedL (src/lpm_basic.c:252-291): stretches and unit vectors at rest
+    launch_stretch(c, c.dLp[0], true);
+    if (c.hs.lattice == 3 && c.plmode == LPM_PL_CP) {
+        // slipSysDefine3D (src/initialization.c:565-637): 24 signed {111}<110>
+        static const int pl[4][3] = {{1, 1, 1}, {-1, 1, 1}, {1, -1, 1}, {-1, -1, 1}};
+        static const int dir[4][6][3] = {
+            {{1, -1, 0}, {-1, 1, 0}, {-1, 0, 1}, {1, 0, -1}, {0, 1, -1}, {0, -1, 1}},
+            {{1, 0, 1}, {-1, 0, -1}, {-1, -1, 0}, {1, 1, 0}, {0, 1, -1}, {0, -1, 1}},
+            {{-1, 0, 1}, {1, 0, -1}, {0, -1, -1}, {0, 1, 1}, {1, 1, 0}, {-1, -1, 0}},
+            {{-1, 1, 0}, {1, -1, 0}, {1, 0, 1}, {-1, 0, -1}, {0, -1, -1}, {0, 1, 1}}};
+        const double a3 = 1 / std::sqrt(3.0), a2 = 1 / std::sqrt(2.0);
+        std::vector<double> sch(6 * LPM_NSLIP);
+        int m2 = 0;
+        for (int p = 0; p < 4; p++)
+            for (int d = 0; d < 6; d++, m2++) {
+                double nv[3], sv[3];
+                for (int k = 0; k < 3; k++) {
+                    nv[k] = pl[p][k] * a3;
+                    sv[k] = dir[p][d][k] * a2;
+                }
+                double *s = &sch[6 * m2];
+                s[0] = nv[0] * sv[0];
+                s[1] = nv[1] * sv[1];
+                s[2] = nv[2] * sv[2];
+                s[3] = nv[1] * sv[2] + nv[2] * sv[1];
+                s[4] = nv[0] * sv[2] + nv[2] * sv[0];
+                s[5] = nv[0] * sv[1] + nv[1] * sv[0];
+            }
+        c.nslip = LPM_NSLIP;
+        int rc = 0;
+        for (int s = 0; s < 3; s++) {
+            if ((rc = dalloc(c.gy[s], n * LPM_NSLIP)) || (rc = dalloc(c.As[s], n * LPM_NSLIP)) ||
+                (rc = dalloc(c.A[s], n)))
+                return rc;
+            std::vector<double> g0(n * LPM_NSLIP, c.cp[0]);  // cp_gy = tau0 (src/initialization.c:570)
+            LPM_CUDA(cudaMemcpy(c.gy[s], g0.data(), g0.size() * sizeof(double), cudaMemcpyHostToDevice));
+        }
+        if ((rc = dalloc(c.Cab, n * LPM_NSLIP * LPM_NSLIP)) || (rc = dalloc(c.sch, 6 * LPM_NSLIP)) ||
+            (rc = dalloc(c.jact, n)))
+            return rc;
+        LPM_CUDA(cudaMemcpy(c.sch, sch.data(), sch.size() * sizeof(double), cudaMemcpyHostToDevice));
+        launch_cab(c);  // computeCab (src/constitutive.c:1864-1917)
+    }
+    c.ready = true;
+    c.have_K = false;
+    return sync(c);
+}
+
+}  // extern "C"
+
+// ---- solver ------------------------------------------------------------------
+
+namespace lpm {
+
+// Run PCG iterations until the device marks the solve done; the host checks
+// every opts.check_every iterations (one CUDA graph per chunk when enabled).
+static int run_pcg(Ctx &c, bool fp32, int &iters, int &status)
+{
+    const int chunk = c.opts.check_every;
+    cudaGraphExec_t &ge = fp32 ? c.graph_fp32 : c.graph_fp64;
+    bool use_graph = c.opts.use_graphs != 0;
+    if (use_graph && ge && c.graph_timed != c.time_spmv) {
+        cudaGraphExecDestroy(c.graph_fp64 ? c.graph_fp64 : c.graph_fp32);
+        if (c.graph_fp64 && c.graph_fp32)
+            cudaGraphExecDestroy(c.graph_fp32);
+        c.graph_fp64 = c.graph_fp32 = nullptr;
+    }
+    if (use_graph && (!ge || c.graph_chunk != chunk)) {
+        if (ge) {
+            cudaGraphExecDestroy(ge);
+            ge = nullptr;
+        }
+        cudaGraph_t g;
+        if (cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            use_graph = false;
+        } else {
+            for (int k = 0; k < chunk; k++) {
+                if (fp32)
+                    launch_cg_iter_f(c);
+                else
+                    launch_cg_iter_d(c);
+            }
+            if (cudaStreamEndCapture(c.stream, &g) != cudaSuccess) {
+                use_graph = false;
+            } else {
+                if (cudaGraphInstantiate(&ge, g, 0) != cudaSuccess) {
+                    ge = nullptr;
+                    use_graph = false;
+                }
+                cudaGraphDestroy(g);
+                c.graph_chunk = chunk;
+                c.graph_timed = c.time_spmv;
+            }
+        }
+        cudaGetLastError();
+    }
+    for (;;) {
+        if (use_graph) {
+            LPM_CUDA(cudaGraphLaunch(ge, c.stream));
+        } else {
+            for (int k = 0; k < chunk; k++) {
+                if (fp32)
+                    launch_cg_iter_f(c);
+                else
+                    launch_cg_iter_d(c);
+            }
+        }
+        LPM_CUDA(cudaMemcpyAsync(c.sc_host, c.sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, c.stream));
+        if (c.time_spmv) {
+            // one sampled SpMV launch per chunk (the last one issued)
+            int rc = sync(c);
+            if (rc)
+                return rc;
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, c.ev_a, c.ev_b) == cudaSuccess) {
+                c.spmv_ms_sum += ms;
+                c.spmv_count++;
+            }
+        } else {
+            int rc = sync(c);
+            if (rc)
+                return rc;
+        }
+        if (c.sc_host->done)
+            break;
+    }
+    iters = c.sc_host->it;
+    status = c.sc_host->done;
+    return LPM_OK;
+}
+
+// Solve K x = b (b device, masked); x written to c.du.  FP64 PCG, or FP32 PCG
+// inside FP64 iterative refinement.
+static int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
+{
+    int rc;
+    if (c.opts.precision == LPM_PREC_FP64) {
+        launch_cg_init_d(c, b);
+        int it = 0, done = 0;
+        if ((rc = run_pcg(c, false, it, done)))
+            return rc;
+        if (st) {
+            st->cg_iters += it;
+            st->spmv_calls += it;
+            if (done == 2)
+                st->status |= LPM_STATUS_CG_MAXIT;
+            if (done == 3)
+                st->status |= LPM_STATUS_NAN;
+        }
+        LPM_CUDA(cudaMemcpyAsync(c.du, c.x_d, sizeof(dvec4) * c.n, cudaMemcpyDeviceToDevice, c.stream));
+        return LPM_OK;
+    }
+    // mixed: x = 0, r = b; repeat: inner FP32 PCG on r/|r|, x += d|r|, r = b - K32 x
+    LPM_CUDA(cudaMemsetAsync(c.x_d, 0, sizeof(dvec4) * c.n, c.stream));
+    launch_norm2(c, b, 2);
+    double bn = 0, rn = 0;
+    {
+        LPM_CUDA(cudaMemcpyAsync(c.norms_host, c.norms, 4 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        if ((rc = sync(c)))
+            return rc;
+        bn = std::sqrt(c.norms_host[2]);
+    }
+    rn = bn;
+    const dvec4 *r = b;
+    int sweeps = 0;
+    while (rn > c.opts.cg_rtol * bn && sweeps < c.opts.refine_maxiter && rn > 0 && std::isfinite(rn)) {
+        const double scale = 1.0 / rn;
+        launch_cg_init_f(c, r, scale);
+        int it = 0, done = 0;
+        if ((rc = run_pcg(c, true, it, done)))
+            return rc;
+        launch_axpy_refine(c, scale);
+        launch_refine_residual(c, c.x_d, b, c.r_d);
+        r = c.r_d;
+        LPM_CUDA(cudaMemcpyAsync(c.norms_host, c.norms, 4 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        if ((rc = sync(c)))
+            return rc;
+        rn = std::sqrt(c.norms_host[2]);
+        sweeps++;
+        if (st) {
+            st->cg_iters += it;
+            st->spmv_calls += it + 1;
+            st->refine_iters += 1;
+            if (done == 3)
+                st->status |= LPM_STATUS_NAN;
+        }
+    }
+    if (st && rn > c.opts.cg_rtol * bn)
+        st->status |= std::isfinite(rn) ? LPM_STATUS_CG_MAXIT : LPM_STATUS_NAN;
+    LPM_CUDA(cudaMemcpyAsync(c.du, c.x_d, sizeof(dvec4) * c.n, cudaMemcpyDeviceToDevice, c.stream));
+    return LPM_OK;
+}
+
+static int assemble(Ctx &c)
+{
+    const bool fp32 = c.opts.precision == LPM_PREC_MIXED;
+    int rc;
+    if (fp32 && !c.Kf && (rc = dalloc(c.Kf, 9 * (size_t)c.nblk)))
+        return rc;
+    if (!fp32 && !c.Kd && (rc = dalloc(c.Kd, 9 * (size_t)c.nblk)))
+        return rc;
+    launch_tangent_geometry(c);
+    launch_assemble(c, fp32);
+    c.have_K = true;
+    return LPM_OK;
+}
+
+static int prepare_preconditioner(Ctx &c)
+{
+    launch_block_jacobi(c, c.opts.precision == LPM_PREC_MIXED);
+    return LPM_OK;
+}
+
+static int force_eval(Ctx &c, int plmode)
+{
+    switch (plmode) {
+    case LPM_PL_PREDICTOR:
+        launch_predictor(c);
+        break;
+    case LPM_PL_ELASTIC:
+        launch_elastic_force(c);
+        copy_state(c, 2, 0);
+        break;
+    case LPM_PL_J2:
+        launch_j2(c);
+        launch_final_force(c);
+        break;
+    case LPM_PL_CP:
+        if (!c.Cab)
+            return fail(LPM_ERR_ARG, "crystal plasticity state not initialised");
+        launch_cp(c);
+        launch_final_force(c);
+        break;
+    default:
+        return fail(LPM_ERR_ARG, "unsupported plmode");
+    }
+    switch_state(c, 2);
+    return LPM_OK;
+}
+
+static int apply_bc(Ctx &c, int nbd, const lpm_disp_bc *dbc, int nbf, const lpm_force_bc *fbc)
+{
+    if (nbd > 0) {
+        if (!dbc)
+            return fail(LPM_ERR_ARG, "null displacement BC array");
+        launch_apply_disp_bc(c, nbd, dbc);
+    }
+    if (nbf > 0) {
+        if (!fbc)
+            return fail(LPM_ERR_ARG, "null force BC array");
+        // particle counts per BC type (src/boundary.c:53-58)
+        std::vector<int> types(c.n), counts(nbf, 0);
+        LPM_CUDA(cudaMemcpyAsync(types.data(), c.type, sizeof(int) * c.n, cudaMemcpyDeviceToHost, c.stream));
+        int rc = sync(c);
+        if (rc)
+            return rc;
+        for (int k = 0; k < nbf; k++)
+            for (int i = 0; i < c.n; i++)
+                counts[k] += (types[i] == fbc[k].type);
+        launch_apply_force_bc(c, nbf, fbc, counts.data());
+    }
+    return LPM_OK;
+}
+
+struct Timer {
+    cudaEvent_t a, b;
+    cudaStream_t s;
+    Timer(cudaStream_t st) : s(st)
+    {
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, s);
+    }
+    double stop()
+    {
+        float ms = 0.f;
+        cudaEventRecord(b, s);
+        cudaEventSynchronize(b);
+        cudaEventElapsedTime(&ms, a, b);
+        return ms;
+    }
+    ~Timer()
+    {
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+    }
+};
+
+}  // namespace lpm
+
+extern "C" {
+
+int lpm_begin_step(lpm_ctx *ctx)
+{
+    if (!ctx || !ctx->c.ready)
+        return fail(LPM_ERR_ARG, "call lpm_init_state first");
+    Ctx &c = ctx->c;
+    // src/lpmc_project.c:387-389: xyz_temp = xyz, F_temp = F
+    LPM_CUDA(cudaMemcpyAsync(c.xyz_temp, c.xyz, sizeof(dvec4) * c.n, cudaMemcpyDeviceToDevice, c.stream));
+    LPM_CUDA(cudaMemcpyAsync(c.F_prev, c.F, sizeof(double) * LPM_NN * c.n, cudaMemcpyDeviceToDevice, c.stream));
+    return LPM_OK;
+}
+
+int lpm_assemble_stiffness(lpm_ctx *ctx)
+{
+    if (!ctx || !ctx->c.ready)
+        return fail(LPM_ERR_ARG, "call lpm_init_state first");
+    int rc = assemble(ctx->c);
+    if (rc)
+        return rc;
+    return sync(ctx->c);
+}
+
+int lpm_apply_bc(lpm_ctx *ctx, int nbd, const lpm_disp_bc *dbc, int nbf, const lpm_force_bc *fbc)
+{
+    if (!ctx || !ctx->c.ready)
+        return fail(LPM_ERR_ARG, "call lpm_init_state first");
+    int rc = apply_bc(ctx->c, nbd, dbc, nbf, fbc);
+    if (rc)
+        return rc;
+    return sync(ctx->c);
+}
+
+int lpm_compute_force(lpm_ctx *ctx, int plmode, double norms[2])
+{
+    if (!ctx || !ctx->c.ready)
+        return fail(LPM_ERR_ARG, "call lpm_init_state first");
+    Ctx &c = ctx->c;
+    int rc = force_eval(c, plmode);
+    if (rc)
+        return rc;
+    double a = 0, b = 0;
+    if ((rc = read_norms(c, a, b)))
+        return rc;
+    if (norms) {
+        norms[0] = a;
+        norms[1] = b;
+    }
+    return LPM_OK;
+}
+
+int lpm_switch_state(lpm_ctx *ctx, int flag)
+{
+    if (!ctx || !ctx->c.ready || flag < 0 || flag > 2)
+        return fail(LPM_ERR_ARG, "bad switchStateV flag or uninitialised context");
+    switch_state(ctx->c, flag);
+    return sync(ctx->c);
+}
+
+int lpm_solve(lpm_ctx *ctx, lpm_step_stats *st)
+{
+    if (!ctx || !ctx->c.ready || !ctx->c.have_K)
+        return fail(LPM_ERR_ARG, "assemble the stiffness first");
+    Ctx &c = ctx->c;
+    int rc = prepare_preconditioner(c);
+    if (rc)
+        return rc;
+    if ((rc = solve_device(c, c.res, st)))
+        return rc;
+    launch_add_du(c);
+    return sync(c);
+}
+
+int lpm_solve_rhs(lpm_ctx *ctx, const double *b, double *x, lpm_step_stats *st)
+{
+    if (!ctx || !ctx->c.ready || !ctx->c.have_K || !b || !x)
+        return fail(LPM_ERR_ARG, "assemble the stiffness first; b and x must be non-null");
+    Ctx &c = ctx->c;
+    int rc = upload_particles(c, c.b_d, b);
+    if (rc)
+        return rc;
+    if ((rc = prepare_preconditioner(c)) || (rc = solve_device(c, c.b_d, st)))
+        return rc;
+    return download_particles(c, c.du, x);
+}
+
+int lpm_load_step(lpm_ctx *ctx, int nbd, const lpm_disp_bc *dbc, int nbf, const lpm_force_bc *fbc,
+                  lpm_step_stats *stats)
+{
+    if (!ctx || !ctx->c.ready)
+        return fail(LPM_ERR_ARG, "call lpm_init_state first");
+    Ctx &c = ctx->c;
+    lpm_step_stats st;
+    std::memset(&st, 0, sizeof(st));
+    int rc = lpm_begin_step(ctx);
+    if (rc)
+        return rc;
+    {
+        Timer t(c.stream);
+        if ((rc = assemble(c)))  // calcStiffness3DFiniteDifference (src/lpmc_project.c:396)
+            return rc;
+        st.ms_stiffness = t.stop();
+    }
+    if ((rc = apply_bc(c, nbd, dbc, nbf, fbc)))  // setDispBC / setForceBC (:402-403)
+        return rc;
+    if ((rc = prepare_preconditioner(c)))  // BC-modified block diagonal (:440)
+        return rc;
+    double res = 0, reac = 0;
+    {
+        Timer t(c.stream);
+        if ((rc = force_eval(c, LPM_PL_PREDICTOR)) || (rc = read_norms(c, res, reac)))  // :405-414
+            return rc;
+        st.ms_force += t.stop();
+    }
+    const double tolm = std::max(res, reac);
+    st.res0 = res;
+    st.reac0 = reac;
+    int ni = 0;
+    while (res > c.opts.newton_tol * tolm && ni < c.opts.newton_maxiter) {  // :424
+        if (!std::isfinite(res)) {
+            st.status |= LPM_STATUS_NAN;
+            break;
+        }
+        switch_state(c, 0);  // :428
+        {
+            Timer t(c.stream);
+            if ((rc = solve_device(c, c.res, &st)))  // :449 solverCG
+                return rc;
+            launch_add_du(c);
+            st.ms_solve += t.stop();
+        }
+        {
+            Timer t(c.stream);
+            if ((rc = force_eval(c, c.plmode)) || (rc = read_norms(c, res, reac)))  // :454-463
+                return rc;
+            st.ms_force += t.stop();
+        }
+        ni++;
+    }
+    if (ni >= c.opts.newton_maxiter && res > c.opts.newton_tol * tolm)
+        st.status |= LPM_STATUS_NEWTON_MAXIT;
+    switch_state(c, 1);  // :471
+    LPM_CUDA(cudaMemcpyAsync(c.status_host, c.status, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    if ((rc = sync(c)))
+        return rc;
+    st.status |= *c.status_host;
+    st.newton_iters = ni;
+    st.res_final = res;
+    if (stats)
+        *stats = st;
+    return LPM_OK;
+}
+
+// ---- data exchange -------------------------------------------------------------
+
+int lpm_get(lpm_ctx *ctx, const char *name, void *dst, size_t bytes)
+{
+    if (!ctx || !name || !dst)
+        return fail(LPM_ERR_ARG, "null argument");
+    Ctx &c = ctx->c;
+    const int n = c.n;
+    const size_t nb = (size_t)n * LPM_NN;
+    std::string nm(name);
+    auto need = [&](size_t b) { return bytes >= b; };
+    auto particles = [&](const dvec4 *src) -> int {
+        if (!need(3 * n * sizeof(double)))
+            return fail(LPM_ERR_ARG, nm + ": buffer too small");
+        return download_particles(c, src, (double *)dst);
+    };
+    auto bond_d = [&](const double *src) -> int {
+        if (!need(nb * sizeof(double)))
+            return fail(LPM_ERR_ARG, nm + ": buffer too small");
+        std::vector<double> t(nb);
+        LPM_CUDA(cudaMemcpy(t.data(), src, nb * sizeof(double), cudaMemcpyDeviceToHost));
+        from_slot_major(t.data(), (double *)dst, n, LPM_NN);
+        return LPM_OK;
+    };
+    auto rows_d = [&](const double *src, int k) -> int {
+        if (!need((size_t)k * n * sizeof(double)))
+            return fail(LPM_ERR_ARG, nm + ": buffer too small");
+        std::vector<double> t((size_t)k * n);
+        LPM_CUDA(cudaMemcpy(t.data(), src, t.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        from_slot_major(t.data(), (double *)dst, n, k);
+        return LPM_OK;
+    };
+    LPM_CUDA(cudaStreamSynchronize(c.stream));
+    if (nm == "xyz") return particles(c.xyz);
+    if (nm == "xyz_initial") return particles(c.xyz0);
+    if (nm == "xyz_temp") return particles(c.xyz_temp);
+    if (nm == "Pin") return particles(c.Pin);
+    if (nm == "Pex") return particles(c.Pex);
+    if (nm == "residual") return particles(c.res);
+    if (nm == "disp") return particles(c.du);
+    if (nm == "F") return bond_d(c.F);
+    if (nm == "F_temp") return bond_d(c.F_prev);
+    if (nm == "dL") return bond_d(c.dL);
+    if (nm == "csx") return bond_d(c.csx);
+    if (nm == "csy") return bond_d(c.csy);
+    if (nm == "csz") return bond_d(c.csz);
+    if (nm == "Kn") return bond_d(c.Kn);
+    if (nm == "Tv") return bond_d(c.Tv);
+    if (nm == "distance_initial") return bond_d(c.L0);
+    if (nm == "dLp") return bond_d(c.dLp[1]);
+    if (nm == "dLp0") return bond_d(c.dLp[0]);
+    if (nm == "dLp2" || nm == "dLp_trial") return bond_d(c.dLp[2]);
+    if (nm == "J2_alpha") return rows_d(c.alpha[1], 1);
+    if (nm == "J2_alpha0") return rows_d(c.alpha[0], 1);
+    if (nm == "J2_alpha2") return rows_d(c.alpha[2], 1);
+    if (nm == "J2_beta") return rows_d(c.beta[1], 6);
+    if (nm == "J2_beta2") return rows_d(c.beta[2], 6);
+    if (nm == "J2_dlambda") return rows_d(c.dlambda, 1);
+    if (nm == "stress_tensor") return rows_d(c.stress, 6);
+    if (nm == "cp_gy" && c.nslip) return rows_d(c.gy[1], c.nslip);
+    if (nm == "cp_gy2" && c.nslip) return rows_d(c.gy[2], c.nslip);
+    if (nm == "cp_A_single" && c.nslip) return rows_d(c.As[1], c.nslip);
+    if (nm == "cp_A_single2" && c.nslip) return rows_d(c.As[2], c.nslip);
+    if (nm == "cp_A" && c.nslip) return rows_d(c.A[1], 1);
+    if (nm == "cp_A2" && c.nslip) return rows_d(c.A[2], 1);
+    if (nm == "cp_Cab" && c.nslip) return rows_d(c.Cab, c.nslip * c.nslip);
+    if (nm == "neighbors" || nm == "nsign") {
+        if (!need(nb * sizeof(int)))
+            return fail(LPM_ERR_ARG, nm + ": buffer too small");
+        std::memcpy(dst, (nm == "neighbors" ? c.hs.nbr : c.hs.shell).data(), nb * sizeof(int));
+        return LPM_OK;
+    }
+    if (nm == "nb" || nm == "nb_conn") {
+        if (!need(n * sizeof(int)))
+            return fail(LPM_ERR_ARG, nm + ": buffer too small");
+        std::memcpy(dst, (nm == "nb" ? c.hs.nb : c.hs.nconn).data(), n * sizeof(int));
+        return LPM_OK;
+    }
+    if (nm == "conn") {
+        if (!need((size_t)n * 61 * sizeof(int)))
+            return fail(LPM_ERR_ARG, nm + ": buffer too small");
+        std::memcpy(dst, c.hs.conn.data(), (size_t)n * 61 * sizeof(int));
+        return LPM_OK;
+    }
+    if (nm == "K_pointer") {
+        if (!need((size_t)(n + 1) * 2 * sizeof(int)))
+            return fail(LPM_ERR_ARG, nm + ": buffer too small");
+        int *o = (int *)dst;
+        for (int i = 0; i <= n; i++) {
+            o[2 * i] = c.hs.kp0[i];
+            o[2 * i + 1] = c.hs.kp1[i];
+        }
+        return LPM_OK;
+    }
+    if (nm == "dispBC_index") {
+        if (!need(3 * (size_t)n * sizeof(int)))
+            return fail(LPM_ERR_ARG, nm + ": buffer too small");
+        std::vector<uint8_t> m(n);
+        LPM_CUDA(cudaMemcpy(m.data(), c.mask, n, cudaMemcpyDeviceToHost));
+        int *o = (int *)dst;
+        for (int i = 0; i < n; i++)
+            for (int d = 0; d < 3; d++)
+                o[3 * i + d] = (m[i] >> d) & 1;
+        return LPM_OK;
+    }
+    if (nm == "cs_initial") {
+        if (!need(nb * 3 * sizeof(double)))
+            return fail(LPM_ERR_ARG, nm + ": buffer too small");
+        std::memcpy(dst, c.hs.cs0.data(), nb * 3 * sizeof(double));
+        return LPM_OK;
+    }
+    return fail(LPM_ERR_ARG, "unknown array name: " + nm);
+}
+
+int lpm_set(lpm_ctx *ctx, const char *name, const void *src, size_t bytes)
+{
+    if (!ctx || !name || !src)
+        return fail(LPM_ERR_ARG, "null argument");
+    Ctx &c = ctx->c;
+    const int n = c.n;
+    const size_t nb = (size_t)n * LPM_NN;
+    std::string nm(name);
+    LPM_CUDA(cudaStreamSynchronize(c.stream));
+    auto particles = [&](dvec4 *d) -> int {
+        if (bytes < 3 * (size_t)n * sizeof(double))
+            return fail(LPM_ERR_ARG, nm + ": buffer too small");
+        return upload_particles(c, d, (const double *)src);
+    };
+    auto bond_d = [&](double *d) -> int {
+        if (bytes < nb * sizeof(double))
+            return fail(LPM_ERR_ARG, nm + ": buffer too small");
+        std::vector<double> t(nb);
+        to_slot_major((const double *)src, t.data(), n, LPM_NN);
+        LPM_CUDA(cudaMemcpy(d, t.data(), nb * sizeof(double), cudaMemcpyHostToDevice));
+        return LPM_OK;
+    };
+    auto rows_d = [&](double *d, int k) -> int {
+        if (bytes < (size_t)k * n * sizeof(double))
+            return fail(LPM_ERR_ARG, nm + ": buffer too small");
+        std::vector<double> t((size_t)k * n);
+        to_slot_major((const double *)src, t.data(), n, k);
+        LPM_CUDA(cudaMemcpy(d, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice));
+        return LPM_OK;
+    };
+    if (nm == "xyz") return particles(c.xyz);
+    if (nm == "xyz_temp") return particles(c.xyz_temp);
+    if (nm == "Pex") return particles(c.Pex);
+    if (nm == "residual") return particles(c.res);
+    if (nm == "F") return bond_d(c.F);
+    if (nm == "F_temp") return bond_d(c.F_prev);
+    if (nm == "csx") return bond_d(c.csx);
+    if (nm == "csy") return bond_d(c.csy);
+    if (nm == "csz") return bond_d(c.csz);
+    if (nm == "dLp0") return bond_d(c.dLp[0]);
+    if (nm == "dLp" || nm == "dLp1") return bond_d(c.dLp[1]);
+    if (nm == "J2_alpha0") return rows_d(c.alpha[0], 1);
+    if (nm == "J2_alpha" || nm == "J2_alpha1") return rows_d(c.alpha[1], 1);
+    if (nm == "J2_beta0") return rows_d(c.beta[0], 6);
+    if (nm == "J2_beta" || nm == "J2_beta1") return rows_d(c.beta[1], 6);
+    if (nm == "dispBC_index") {
+        if (bytes < 3 * (size_t)n * sizeof(int))
+            return fail(LPM_ERR_ARG, nm + ": buffer too small");
+        const int *m = (const int *)src;
+        std::vector<uint8_t> t(n);
+        for (int i = 0; i < n; i++)
+            t[i] = (uint8_t)((m[3 * i] ? 1 : 0) | (m[3 * i + 1] ? 2 : 0) | (m[3 * i + 2] ? 4 : 0));
+        LPM_CUDA(cudaMemcpy(c.mask, t.data(), n, cudaMemcpyHostToDevice));
+        return LPM_OK;
+    }
+    return fail(LPM_ERR_ARG, "unknown or read-only array name: " + nm);
+}
+
+int lpm_export_upper_csr(lpm_ctx *ctx, double *Kg, int *IK, int *JK, long long *nnz)
+{
+    if (!ctx)
+        return fail(LPM_ERR_ARG, "null context");
+    Ctx &c = ctx->c;
+    const HostSetup &h = c.hs;
+    const int n = c.n, w = 61;
+    if (nnz)
+        *nnz = h.kp1[n];
+    if (!Kg && !IK && !JK)
+        return LPM_OK;
+    std::vector<double> val;
+    if (Kg) {
+        if (!c.have_K)
+            return fail(LPM_ERR_ARG, "no stiffness assembled");
+        val.resize(9 * (size_t)c.nblk);
+        if (c.opts.precision == LPM_PREC_FP64) {
+            LPM_CUDA(cudaMemcpy(val.data(), c.Kd, val.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        } else {
+            std::vector<float> vf(val.size());
+            LPM_CUDA(cudaMemcpy(vf.data(), c.Kf, vf.size() * sizeof(float), cudaMemcpyDeviceToHost));
+            for (size_t k = 0; k < vf.size(); k++)
+                val[k] = vf[k];
+        }
+    }
+    // layout of calcStiffness3DFiniteDifference (src/stiffness.c:431-515)
+    for (int i = 0; i < n; i++) {
+        const int base = h.kp1[i], k0 = h.kp0[i], np = h.npad[i];
+        const long long off = h.rowoff[i];
+        int num1 = 0;
+        for (int jid = 0; jid < h.nconn[i]; jid++) {
+            const int jj = h.conn[(size_t)i * w + jid];
+            auto V = [&](int r, int q) { return val[9 * off + (size_t)(3 * r + q) * np + jid]; };
+            if (jj == i) {
+                const int pos[6] = {base, base + 1, base + 2, base + 3 * k0, base + 3 * k0 + 1, base + 6 * k0 - 1};
+                const int rq[6][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
+                const int col[6] = {3 * (jj + 1) - 2, 3 * (jj + 1) - 1, 3 * (jj + 1), 3 * (jj + 1) - 1,
+                                    3 * (jj + 1), 3 * (jj + 1)};
+                for (int k = 0; k < 6; k++) {
+                    if (Kg)
+                        Kg[pos[k]] = V(rq[k][0], rq[k][1]);
+                    if (JK)
+                        JK[pos[k]] = col[k];
+                }
+            } else if (jj > i) {
+                num1++;
+                const int rowstart[3] = {base + 3 * num1, base + 3 * k0 + 3 * num1 - 1, base + 6 * k0 + 3 * num1 - 3};
+                for (int r = 0; r < 3; r++)
+                    for (int q = 0; q < 3; q++) {
+                        if (Kg)
+                            Kg[rowstart[r] + q] = V(r, q);
+                        if (JK)
+                            JK[rowstart[r] + q] = 3 * (jj + 1) - 2 + q;
+                    }
+            }
+        }
+        if (IK) {
+            IK[3 * i] = base + 1;
+            IK[3 * i + 1] = base + 3 * k0 + 1;
+            IK[3 * i + 2] = base + 6 * k0;
+        }
+    }
+    if (IK)
+        IK[3 * n] = h.kp1[n] + 1;
+    return LPM_OK;
+}
+
+int lpm_spmv(lpm_ctx *ctx, const double *x, double *y)
+{
+    if (!ctx || !ctx->c.have_K || !x || !y)
+        return fail(LPM_ERR_ARG, "assemble the stiffness first; x and y must be non-null");
+    Ctx &c = ctx->c;
+    int rc = upload_particles(c, c.b_d, x);
+    if (rc)
+        return rc;
+    if (c.opts.precision == LPM_PREC_FP64) {
+        launch_spmv_d(c, c.b_d, c.q_d, false, false);
+        return download_particles(c, c.q_d, y);
+    }
+    // FP32 product of an FP32 copy of x
+    std::vector<float4> xf(c.n);
+    for (int i = 0; i < c.n; i++)
+        xf[i] = make_float4((float)x[3 * i], (float)x[3 * i + 1], (float)x[3 * i + 2], 0.f);
+    LPM_CUDA(cudaMemcpy(c.p_f, xf.data(), sizeof(float4) * c.n, cudaMemcpyHostToDevice));
+    launch_spmv_f(c, c.p_f, c.q_f, false, false);
+    LPM_CUDA(cudaMemcpyAsync(xf.data(), c.q_f, sizeof(float4) * c.n, cudaMemcpyDeviceToHost, c.stream));
+    if ((rc = sync(c)))
+        return rc;
+    for (int i = 0; i < c.n; i++) {
+        y[3 * i] = xf[i].x;
+        y[3 * i + 1] = xf[i].y;
+        y[3 * i + 2] = xf[i].z;
+    }
+    return LPM_OK;
+}
+
+int lpm_spmv_timing(lpm_ctx *ctx, double *avg_ms, long long *count, int reset)
+{
+    if (!ctx)
+        return fail(LPM_ERR_ARG, "null context");
+    Ctx &c = ctx->c;
+    if (avg_ms)
+        *avg_ms = c.spmv_count ? c.spmv_ms_sum / c.spmv_count : 0.0;
+    if (count)
+        *count = c.spmv_count;
+    if (reset) {
+        c.spmv_ms_sum = 0;
+        c.spmv_count = 0;
+    }
+    // reset > 1 also switches sampling on (reset == 2) or off (reset == 3)
+    if (reset == 2)
+        c.time_spmv = true;
+    if (reset == 3)
+        c.time_spmv = false;
+    return LPM_OK;
+}
+
+double lpm_spmv_bytes(const lpm_ctx *ctx, int precision)
+{
+    if (!ctx)
+        return 0.0;
+    const Ctx &c = ctx->c;
+    const double sv = precision == LPM_PREC_MIXED ? 4.0 : 8.0;
+    // nnzb (9 s_v + 4) + 4 (N_b + 1) + 2 * 3 N_b * s_x
+    return (double)c.nblk_real * (9.0 * sv + 4.0) + 4.0 * (c.n + 1) + 2.0 * 3.0 * c.n * sv;
+}
+
+}  // extern "C"

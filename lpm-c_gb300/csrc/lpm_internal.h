@@ -1,0 +1,193 @@
+// Internal declarations of the GB300 LPM library: the context, device
+// layouts and the kernel launchers.  Not part of the public C ABI.
+//
+// Device layouts (n particles, NN = 18 bond slots per particle):
+//   particle vectors      dvec4 / float4 per particle (x, y, z, 0)
+//   bond arrays           slot-major [NN][n] so that thread i of a warp reads
+//                         bond j of particle i coalesced
+//   stiffness             block-CSR over particles, 3x3 blocks; the blocks of
+//                         row i are padded to a multiple of 4 (npad_i) and
+//                         stored component-major: value (r,c) of block b is at
+//                         val[9*rowoff_i + (3r+c)*npad_i + b], so a lane can
+//                         read 4 consecutive blocks' component with one
+//                         128-bit load; cols[rowoff_i + b] (padding -> i, 0)
+#pragma once
+#include <cstdint>
+#include <cstddef>
+#include <string>
+#include <vector>
+#include <cuda_runtime.h>
+#include "../../include/lpm_gpu.h"
+
+#define LPM_NN 18     // bond slots per particle (SC and FCC: 2 shells)
+#define LPM_NSLIP 24  // FCC signed {111}<110> systems
+#define LPM_MAXCONN 64
+
+// 32-byte aligned FP64 4-vector (x, y, z, 0) of one particle
+typedef double4_32a dvec4;
+__host__ __device__ inline dvec4 make_dvec4(double x, double y, double z, double w)
+{
+    return make_double4_32a(x, y, z, w);
+}
+
+namespace lpm {
+
+extern thread_local std::string g_err;
+int fail(int code, const std::string &msg);
+
+#define LPM_CUDA(call)                                                                   \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess)                                                           \
+            return ::lpm::fail(LPM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// Host-side setup data (built once per specimen, see setup.cpp).
+struct HostSetup {
+    int lattice = 0, n = 0, nn1 = 0, nn2 = 0;
+    double radius = 0, vol = 0, cut1 = 0, cut2 = 0;
+    std::vector<double> xyz;          // n x 3
+    std::vector<int> nbr;             // n x NN (row-major), -1 padded
+    std::vector<int> shell;           // n x NN
+    std::vector<int> nb;              // n
+    std::vector<int> rev;             // n x NN: slot of the reverse bond
+    std::vector<double> L0, cs0;      // n x NN, n x NN x 3
+    std::vector<double> oppv;         // n x NN: opposite-bond weight / particle volume
+    std::vector<int> conn;            // n x 61 sorted, -1 padded (searchAFEMNeighbor)
+    std::vector<int> nconn;           // n
+    std::vector<int> kp0, kp1;        // K_pointer[i][0], K_pointer[i][1]
+    // block-CSR pattern
+    std::vector<long long> rowoff;    // n+1, in blocks (padded)
+    std::vector<int> npad;            // n
+    std::vector<int> cols;            // rowoff[n]
+};
+
+int build_lattice(HostSetup &h, int lattice, double radius, const double *box);
+int build_particles(HostSetup &h, int lattice, double radius, int n, const double *xyz);
+void build_neighbors(HostSetup &h);
+void build_afem(HostSetup &h);
+void build_bond_tables(HostSetup &h);
+void build_block_pattern(HostSetup &h);
+void kntv_per_particle(int lattice, double radius, const double *c11, const double *c12,
+                       const double *c44, int n, double *knt);
+
+// Device scalars used by the PCG (one 128-byte record).
+struct CgScalars {
+    double rz, rz_old, pq, rr, alpha, beta, bnorm2, tol2;
+    int it, done, maxit, pad;
+};
+
+struct Ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int n = 0, nslip = 0, plmode = 0;
+    HostSetup hs;
+    lpm_solver_opts opts{};
+    double xi = 0.0;
+    double cp[8] = {0};
+    bool ready = false;   // init_state done
+    bool have_K = false;
+
+    // ---- device: particles
+    dvec4 *xyz = nullptr, *xyz0 = nullptr, *xyz_temp = nullptr;
+    dvec4 *Pin = nullptr, *Pex = nullptr, *res = nullptr, *du = nullptr;
+    uint8_t *mask = nullptr;  // bit d set = DOF d free (dispBC_index == 1)
+    int *type = nullptr;
+    double *G = nullptr, *sy = nullptr, *Hh = nullptr;
+    double *stress = nullptr;  // [6][n]
+    double *dlambda = nullptr;
+    // ---- device: bonds [NN][n]
+    int *nbr = nullptr;
+    int8_t *shell = nullptr, *rev = nullptr;
+    int8_t *nbv = nullptr;     // nb per particle (int8)
+    int8_t *nconn_d = nullptr; // AFEM connectivity count per particle
+    double *L0 = nullptr, *Kn = nullptr, *Tv = nullptr, *oppv = nullptr;
+    double *dL = nullptr;      // elastic stretch after the last force evaluation
+    double *csx = nullptr, *csy = nullptr, *csz = nullptr;  // unit vectors of the last evaluation
+    double *F = nullptr, *F_prev = nullptr;
+    double2 *S = nullptr, *T = nullptr;  // shell sums (dL_total, TdL_total)
+    double *ddL = nullptr;     // predictor increments
+    double2 *dS = nullptr, *dT = nullptr;
+    // state variables in the reference's three slots (src/constitutive.c:10-85):
+    // [0] current (read by a force evaluation), [1] last converged,
+    // [2] freshly computed (written by a force evaluation)
+    double *dLp[3] = {nullptr, nullptr, nullptr};     // [NN][n]
+    double *alpha[3] = {nullptr, nullptr, nullptr};   // [n]
+    double *beta[3] = {nullptr, nullptr, nullptr};    // [6][n]
+    double *gy[3] = {nullptr, nullptr, nullptr};      // [nslip][n]
+    double *As[3] = {nullptr, nullptr, nullptr};      // [nslip][n]
+    double *A[3] = {nullptr, nullptr, nullptr};       // [n]
+    double *Cab = nullptr;    // [nslip*nslip][n]
+    double *sch = nullptr;    // [nslip][6]
+    int *jact = nullptr;      // active set bitmask per particle
+    // stiffness geometry (tangent assembly)
+    double *U = nullptr, *W = nullptr;  // [6][n]: shell-sums of unit vectors (U) and Tv-weighted (W)
+    // ---- device: block-CSR
+    long long nblk = 0;       // padded block count
+    long long nblk_real = 0;  // structural blocks
+    long long *rowoff = nullptr;
+    int *npad = nullptr;
+    int *cols = nullptr;
+    double *Kd = nullptr;     // FP64 values (9*nblk)
+    float *Kf = nullptr;      // FP32 values (9*nblk)
+    double *Pinv_d = nullptr; // block-Jacobi inverse, [9][n]
+    float *Pinv_f = nullptr;
+    // ---- solver vectors
+    dvec4 *x_d = nullptr, *r_d = nullptr, *p_d = nullptr, *q_d = nullptr, *z_d = nullptr;
+    float4 *x_f = nullptr, *r_f = nullptr, *p_f = nullptr, *q_f = nullptr, *z_f = nullptr;
+    dvec4 *b_d = nullptr;
+    CgScalars *sc = nullptr;     // device
+    CgScalars *sc_host = nullptr; // pinned mirror
+    double *partials = nullptr;  // reduction partials
+    unsigned *counter = nullptr; // last-block counters
+    double *norms = nullptr;     // device norms [4]
+    double *norms_host = nullptr;
+    int *status = nullptr, *status_host = nullptr;
+    int red_blocks = 0;
+    // timing of the SpMV launches
+    cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+    double spmv_ms_sum = 0;
+    long long spmv_count = 0;
+    bool time_spmv = false;
+    // CUDA graphs of PCG chunks
+    cudaGraphExec_t graph_fp64 = nullptr, graph_fp32 = nullptr;
+    int graph_chunk = 0;
+    bool graph_timed = false;
+    ~Ctx();
+};
+
+// ---- kernel launchers (stream-ordered, no synchronisation) ----
+// force path (k_force.cu, FP64, no FMA contraction)
+void launch_stretch(Ctx &c, const double *dLp, bool store_cs);
+void launch_elastic_force(Ctx &c);
+void launch_predictor(Ctx &c);
+void launch_j2(Ctx &c);
+void launch_cp(Ctx &c);
+void launch_final_force(Ctx &c);
+void launch_residual(Ctx &c);  // updateRR + norms into c.norms[0..1]
+void launch_add_du(Ctx &c);
+void launch_apply_disp_bc(Ctx &c, int nbd, const lpm_disp_bc *d);
+void launch_apply_force_bc(Ctx &c, int nbf, const lpm_force_bc *f, const int *counts);
+void launch_cab(Ctx &c);
+// stiffness (k_stiff.cu)
+void launch_tangent_geometry(Ctx &c);
+void launch_assemble(Ctx &c, bool fp32);
+void launch_block_jacobi(Ctx &c, bool fp32);
+// solver (k_solve.cu)
+void launch_spmv_d(Ctx &c, const dvec4 *x, dvec4 *y, bool masked, bool dot_pq);
+void launch_spmv_f(Ctx &c, const float4 *x, float4 *y, bool masked, bool dot_pq);
+void launch_refine_residual(Ctx &c, const dvec4 *x, const dvec4 *b, dvec4 *r);  // r = b - K32 x (FP64)
+void launch_cg_init_d(Ctx &c, const dvec4 *b);
+void launch_cg_init_f(Ctx &c, const dvec4 *r64, double scale);
+void launch_cg_iter_d(Ctx &c);
+void launch_cg_iter_f(Ctx &c);
+void launch_axpy_refine(Ctx &c, double scale);  // x_d += x_f / scale
+void launch_norm2(Ctx &c, const dvec4 *v, int slot);
+int red_grid(const Ctx &c);
+
+}  // namespace lpm
+
+struct lpm_ctx {
+    lpm::Ctx c;
+};

@@ -1,0 +1,313 @@
+// Host-side specimen setup: lattice generation, two-shell bond lists, AFEM
+// connectivity, bond tables and the block-CSR stiffness pattern.  This is the
+// once-per-specimen part of the reference (src/initialization.c,
+// src/neighbor.c, src/stiffness.c:145-235); its outputs must be bit-identical
+// to the reference's, so it is compiled without floating-point contraction
+// and evaluates every expression in the reference's order.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+#include "lpm_internal.h"
+
+namespace lpm {
+
+static void lattice_constants(HostSetup &h)
+{
+    const double r = h.radius;
+    h.cut1 = 2.0 * r;                 // neighbor1_cutoff
+    h.cut2 = 2.0 * std::sqrt(2.0) * r;  // neighbor2_cutoff
+    if (h.lattice == 2) {            // src/initialization.c:251-259
+        h.nn1 = 6;
+        h.nn2 = 12;
+        h.vol = std::pow(2 * r, 3);
+    } else {                         // src/initialization.c:336-345
+        h.nn1 = 12;
+        h.nn2 = 6;
+        h.vol = 4.0 * std::sqrt(2.0) * std::pow(r, 3);
+    }
+}
+
+// createCuboid for the identity orientation (all Euler angles zero): the
+// rotation of src/initialization.c:287-313 maps every point to itself.
+int build_lattice(HostSetup &h, int lattice, double radius, const double *box)
+{
+    if (lattice != 2 && lattice != 3)
+        return fail(LPM_ERR_ARG, "lattice must be 2 (simple cubic) or 3 (FCC)");
+    if (!(radius > 0.0))
+        return fail(LPM_ERR_ARG, "radius must be positive");
+    h.lattice = lattice;
+    h.radius = radius;
+    lattice_constants(h);
+    const double bx = box[1] - box[0], by = box[3] - box[2], bz = box[5] - box[4];
+    const double a = std::sqrt(bx * bx + by * by + bz * bz);
+    const double t0 = -a, t1 = a;
+    h.xyz.clear();
+    auto keep = [&](double x, double y, double z) {
+        if (x >= box[0] && x <= box[1] && y >= box[2] && y <= box[3] && z >= box[4] && z <= box[5]) {
+            h.xyz.push_back(x);
+            h.xyz.push_back(y);
+            h.xyz.push_back(z);
+        }
+    };
+    if (lattice == 2) {  // src/initialization.c:241-284
+        const double s = 2 * radius;
+        const int nx = 1 + (int)std::floor((t1 - t0) / s);
+        for (int k = 1; k <= nx; k++) {
+            const double z = t0 + s * (k - 1);
+            for (int j = 1; j <= nx; j++) {
+                const double y = t0 + s * (j - 1);
+                for (int i = 1; i <= nx; i++)
+                    keep(box[0] + s * (i - 1), y, z);
+            }
+        }
+    } else {  // src/initialization.c:326-426 (alternating full / shifted rows)
+        const double s = 4 * radius / std::sqrt(2.0);
+        const int nx = 1 + (int)std::floor((t1 - t0) / s);
+        const int ny = 1 + (int)std::floor((t1 - t0) / (s / 2.0));
+        for (int k = 1; k <= ny; k++) {
+            const double z = t0 + s / 2.0 * (k - 1);
+            for (int j = 1; j <= ny; j++) {
+                const double y = t0 + s / 2.0 * (j - 1);
+                if ((k % 2 == 1) == (j % 2 == 1)) {
+                    for (int i = 1; i <= nx; i++)
+                        keep(t0 + s * (i - 1), y, z);
+                } else {
+                    for (int i = 1; i <= nx - 1; i++)
+                        keep(t0 + s * (i - 1) + s / 2.0, y, z);
+                }
+            }
+        }
+    }
+    h.n = (int)(h.xyz.size() / 3);
+    if (h.n <= 0)
+        return fail(LPM_ERR_ARG, "the box holds no lattice site");
+    return h.n;
+}
+
+int build_particles(HostSetup &h, int lattice, double radius, int n, const double *xyz)
+{
+    if (lattice != 2 && lattice != 3)
+        return fail(LPM_ERR_ARG, "lattice must be 2 (simple cubic) or 3 (FCC)");
+    if (n <= 0 || !xyz)
+        return fail(LPM_ERR_ARG, "no particles");
+    h.lattice = lattice;
+    h.radius = radius;
+    lattice_constants(h);
+    h.xyz.assign(xyz, xyz + 3 * (size_t)n);
+    h.n = n;
+    return n;
+}
+
+// searchNormalNeighbor (src/neighbor.c:9-46).  A uniform cell grid replaces
+// the all-pairs loop; every candidate is tested with the reference's
+// distance expression and cut-offs, and bonds are kept in ascending j.
+void build_neighbors(HostSetup &h)
+{
+    const int n = h.n;
+    const double c1 = 1.01 * h.cut1, c2 = 1.01 * h.cut2;
+    double lo[3], hi[3];
+    for (int d = 0; d < 3; d++) {
+        lo[d] = hi[d] = h.xyz[d];
+    }
+    for (int i = 0; i < n; i++)
+        for (int d = 0; d < 3; d++) {
+            lo[d] = std::min(lo[d], h.xyz[3 * i + d]);
+            hi[d] = std::max(hi[d], h.xyz[3 * i + d]);
+        }
+    const double cs = c2 * 1.0001;
+    int g[3];
+    for (int d = 0; d < 3; d++)
+        g[d] = (int)((hi[d] - lo[d]) / cs) + 1;
+    const size_t ncell = (size_t)g[0] * g[1] * g[2];
+    std::vector<int> cell(n), start(ncell + 1, 0), order(n);
+    for (int i = 0; i < n; i++) {
+        int c[3];
+        for (int d = 0; d < 3; d++)
+            c[d] = std::min(g[d] - 1, (int)((h.xyz[3 * i + d] - lo[d]) / cs));
+        cell[i] = (c[2] * g[1] + c[1]) * g[0] + c[0];
+        start[cell[i] + 1]++;
+    }
+    for (size_t c = 0; c < ncell; c++)
+        start[c + 1] += start[c];
+    {
+        std::vector<int> fill(start.begin(), start.end() - 1);
+        for (int i = 0; i < n; i++)
+            order[fill[cell[i]]++] = i;
+    }
+    h.nbr.assign((size_t)n * LPM_NN, -1);
+    h.shell.assign((size_t)n * LPM_NN, -1);
+    h.nb.assign(n, 0);
+    h.L0.assign((size_t)n * LPM_NN, 0.0);
+    h.cs0.assign((size_t)n * LPM_NN * 3, 0.0);
+    const double *X = h.xyz.data();
+#pragma omp parallel for schedule(dynamic, 512)
+    for (int i = 0; i < n; i++) {
+        int cand[96];
+        double cd[96];
+        int nc = 0;
+        const int ci = cell[i];
+        const int cx = ci % g[0], cy = (ci / g[0]) % g[1], cz = ci / (g[0] * g[1]);
+        for (int dz = -1; dz <= 1; dz++)
+            for (int dy = -1; dy <= 1; dy++)
+                for (int dx = -1; dx <= 1; dx++) {
+                    const int x = cx + dx, y = cy + dy, z = cz + dz;
+                    if (x < 0 || y < 0 || z < 0 || x >= g[0] || y >= g[1] || z >= g[2])
+                        continue;
+                    const size_t c = ((size_t)z * g[1] + y) * g[0] + x;
+                    for (int q = start[c]; q < start[c + 1]; q++) {
+                        const int j = order[q];
+                        const double ex = X[3 * j] - X[3 * i], ey = X[3 * j + 1] - X[3 * i + 1],
+                                     ez = X[3 * j + 2] - X[3 * i + 2];
+                        const double dis = std::sqrt(ex * ex + ey * ey + ez * ez);
+                        if ((((dis < c1) && (j != i)) || ((dis > c1) && (dis < c2))) && nc < 96) {
+                            cand[nc] = j;
+                            cd[nc] = dis;
+                            nc++;
+                        }
+                    }
+                }
+        // ascending j (the reference scans j = 0..n-1)
+        for (int a = 1; a < nc; a++) {
+            const int v = cand[a];
+            const double dv = cd[a];
+            int b = a - 1;
+            while (b >= 0 && cand[b] > v) {
+                cand[b + 1] = cand[b];
+                cd[b + 1] = cd[b];
+                b--;
+            }
+            cand[b + 1] = v;
+            cd[b + 1] = dv;
+        }
+        const int m = std::min(nc, LPM_NN);
+        for (int q = 0; q < m; q++) {
+            const int j = cand[q];
+            const double dis = cd[q];
+            const size_t b = (size_t)i * LPM_NN + q;
+            h.nbr[b] = j;
+            h.shell[b] = ((dis < c1) && (j != i)) ? 0 : 1;
+            h.cs0[3 * b] = (X[3 * i] - X[3 * j]) / dis;
+            h.cs0[3 * b + 1] = (X[3 * i + 1] - X[3 * j + 1]) / dis;
+            h.cs0[3 * b + 2] = (X[3 * i + 2] - X[3 * j + 2]) / dis;
+            h.L0[b] = dis;
+        }
+        h.nb[i] = m;
+    }
+}
+
+// searchAFEMNeighbor (src/neighbor.c:49-141): conn[i] = sorted unique union,
+// over i's bonds, of the bond partner and that partner's neighbours of the
+// same shell; K_pointer[i] = {#conn >= i, start of row in the upper CSR}.
+void build_afem(HostSetup &h)
+{
+    const int n = h.n, w = 61;
+    h.conn.assign((size_t)n * w, -1);
+    h.nconn.assign(n, 0);
+#pragma omp parallel for schedule(dynamic, 512)
+    for (int i = 0; i < n; i++) {
+        int col[LPM_NN * (LPM_NN + 1)];
+        int nc = 0;
+        for (int j = 0; j < h.nb[i]; j++) {
+            const size_t b = (size_t)i * LPM_NN + j;
+            const int p = h.nbr[b], s = h.shell[b];
+            col[nc++] = p;
+            for (int k = 0; k < h.nb[p]; k++)
+                if (h.shell[(size_t)p * LPM_NN + k] == s)
+                    col[nc++] = h.nbr[(size_t)p * LPM_NN + k];
+        }
+        std::sort(col, col + nc);
+        const int m = (int)(std::unique(col, col + nc) - col);
+        const int mm = std::min(m, w);
+        for (int k = 0; k < mm; k++)
+            h.conn[(size_t)i * w + k] = col[k];
+        h.nconn[i] = mm;
+    }
+    h.kp0.assign(n + 1, 0);
+    h.kp1.assign(n + 1, 0);
+    for (int i = 0; i < n; i++) {
+        int c = 0;
+        for (int k = 0; k < h.nconn[i]; k++)
+            c += (h.conn[(size_t)i * w + k] >= i);
+        h.kp0[i] = c;
+        h.kp1[i + 1] = h.kp1[i] + 9 * c - 3;
+    }
+}
+
+// Reverse bond slot (src/constitutive.c:654-658) and the stress weight
+// opp_flag / particle_volume (src/constitutive.c:541-562, damage_broken = 1).
+void build_bond_tables(HostSetup &h)
+{
+    const int n = h.n;
+    const double eps = 1e-6;
+    h.rev.assign((size_t)n * LPM_NN, -1);
+    h.oppv.assign((size_t)n * LPM_NN, 0.0);
+#pragma omp parallel for
+    for (int i = 0; i < n; i++) {
+        for (int j = 0; j < h.nb[i]; j++) {
+            const size_t b = (size_t)i * LPM_NN + j;
+            const int p = h.nbr[b];
+            for (int q = 0; q < LPM_NN; q++)
+                if (h.nbr[(size_t)p * LPM_NN + q] == i)
+                    h.rev[b] = q;
+            double opp = 1.0;
+            if (h.nb[i] == LPM_NN) {
+                opp = 0.5;
+            } else {
+                for (int m = 0; m < h.nb[i]; m++) {
+                    const size_t c = (size_t)i * LPM_NN + m;
+                    if (std::fabs(h.cs0[3 * c] + h.cs0[3 * b]) < eps &&
+                        std::fabs(h.cs0[3 * c + 1] + h.cs0[3 * b + 1]) < eps &&
+                        std::fabs(h.cs0[3 * c + 2] + h.cs0[3 * b + 2]) < eps) {
+                        opp = 0.5;
+                        break;
+                    }
+                }
+            }
+            h.oppv[b] = opp / h.vol;
+        }
+    }
+}
+
+// Block-CSR: block row i holds the blocks of conn[i] (ascending particle
+// index, i included), padded to a multiple of 4 with zero blocks on column i.
+void build_block_pattern(HostSetup &h)
+{
+    const int n = h.n, w = 61;
+    h.npad.assign(n, 0);
+    h.rowoff.assign(n + 1, 0);
+    for (int i = 0; i < n; i++) {
+        h.npad[i] = (h.nconn[i] + 3) & ~3;
+        h.rowoff[i + 1] = h.rowoff[i] + h.npad[i];
+    }
+    h.cols.assign((size_t)h.rowoff[n], 0);
+#pragma omp parallel for
+    for (int i = 0; i < n; i++) {
+        int *c = h.cols.data() + h.rowoff[i];
+        for (int k = 0; k < h.npad[i]; k++)
+            c[k] = k < h.nconn[i] ? h.conn[(size_t)i * w + k] : i;
+    }
+}
+
+// calcKnTv's KnTve = radius * mapping * [C11, C12, C44] per particle
+// (src/stiffness.c:179-185 SC, :210-216 FCC), summed in the order of a
+// plain row-major matrix-vector product.
+void kntv_per_particle(int lattice, double radius, const double *c11, const double *c12,
+                       const double *c44, int n, double *knt)
+{
+    const double r2 = std::sqrt(2.0);
+    const double msc[9] = {1, -1, -1, 0, 0, 1, 0, 1.0 / 18.0, -1.0 / 18.0};
+    const double mfcc[9] = {0, 0, r2, r2 / 4.0, -r2 / 4.0, -r2 / 4.0, 0, r2 / 24.0, -r2 / 24.0};
+    const double *m = lattice == 2 ? msc : mfcc;
+    for (int i = 0; i < n; i++) {
+        const double ce[3] = {c11[i], c12[i], c44[i]};
+        for (int r = 0; r < 3; r++) {
+            double s = 0.0;
+            for (int l = 0; l < 3; l++)
+                s += m[3 * r + l] * ce[l];
+            knt[3 * i + r] = radius * s;
+        }
+    }
+}
+
+}  // namespace lpm

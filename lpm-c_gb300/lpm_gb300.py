@@ -1,0 +1,311 @@
+"""Python host binding of the GB300 LPM library (ctypes over include/lpm_gpu.h).
+
+Mirrors the reference's operator boundary for the quasi-static solve path:
+``Specimen.setup_lattice`` (createCuboid + neighbour search), ``set_material``
+(calcKnTv), ``init_state`` (computedL / computeCab), ``load_step`` (one load
+step of src/lpmc_project.c:385-471), and the single-function entry points
+``assemble_stiffness`` / ``compute_force`` / ``solve`` / ``switch_state``.
+Arrays come back in the reference's row-major [i][j] layout.
+
+The library is loaded from lpm-c_gb300/_build/liblpmgpu.so (built by
+build.py); there is no CPU fallback: if the shared object or a GPU is
+missing, calls raise.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liblpmgpu.so")
+
+PREC_FP64, PREC_MIXED = 0, 1
+PL_J2, PL_CP, PL_PREDICTOR, PL_ELASTIC = 0, 1, 4, 6
+STATUS_NEWTON_MAXIT, STATUS_CG_MAXIT, STATUS_NAN, STATUS_CP_SINGULAR = 1, 2, 4, 8
+
+# every symbol declared in include/lpm_gpu.h
+EXPORTED = [
+    "lpm_create", "lpm_destroy", "lpm_last_error", "lpm_set_stream", "lpm_default_solver_opts",
+    "lpm_set_solver", "lpm_setup_lattice", "lpm_setup_particles", "lpm_nparticle", "lpm_set_types",
+    "lpm_set_material", "lpm_set_cp", "lpm_init_state", "lpm_load_step", "lpm_assemble_stiffness",
+    "lpm_apply_bc", "lpm_compute_force", "lpm_switch_state", "lpm_solve", "lpm_begin_step", "lpm_get",
+    "lpm_set", "lpm_get_sizes", "lpm_export_upper_csr", "lpm_spmv", "lpm_solve_rhs", "lpm_spmv_timing",
+    "lpm_spmv_bytes",
+]
+
+
+class DispBC(C.Structure):
+    """lpm_disp_bc == struct dispBCPara (include/lpm.h:83-88)."""
+    _fields_ = [("type", C.c_int), ("flag", C.c_char), ("step", C.c_double)]
+
+
+class ForceBC(C.Structure):
+    """lpm_force_bc == struct forceBCPara (include/lpm.h:90-99)."""
+    _fields_ = [("type", C.c_int), ("flag1", C.c_char), ("step1", C.c_double),
+                ("flag2", C.c_char), ("step2", C.c_double), ("flag3", C.c_char), ("step3", C.c_double)]
+
+
+class SolverOpts(C.Structure):
+    _fields_ = [("precision", C.c_int), ("newton_tol", C.c_double), ("newton_maxiter", C.c_int),
+                ("cg_rtol", C.c_double), ("cg_maxiter", C.c_int), ("inner_rtol", C.c_double),
+                ("refine_maxiter", C.c_int), ("check_every", C.c_int), ("use_graphs", C.c_int),
+                ("spmv_variant", C.c_int)]
+
+
+class StepStats(C.Structure):
+    _fields_ = [("newton_iters", C.c_int), ("cg_iters", C.c_int), ("refine_iters", C.c_int),
+                ("spmv_calls", C.c_int), ("status", C.c_int), ("res0", C.c_double),
+                ("reac0", C.c_double), ("res_final", C.c_double), ("ms_stiffness", C.c_double),
+                ("ms_solve", C.c_double), ("ms_force", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class LPMError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load the CUDA library (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise LPMError(f"{path} not found: build the CUDA library first (lpm-c_gb300/build.py)")
+    L = C.CDLL(path)
+    vp, dp, ip = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int)
+    sig = {
+        "lpm_create": ([C.POINTER(vp), C.c_int], C.c_int),
+        "lpm_destroy": ([vp], None),
+        "lpm_last_error": ([], C.c_char_p),
+        "lpm_set_stream": ([vp, vp], C.c_int),
+        "lpm_default_solver_opts": ([C.POINTER(SolverOpts)], None),
+        "lpm_set_solver": ([vp, C.POINTER(SolverOpts)], C.c_int),
+        "lpm_setup_lattice": ([vp, C.c_int, C.c_double, dp], C.c_int),
+        "lpm_setup_particles": ([vp, C.c_int, C.c_double, C.c_int, dp], C.c_int),
+        "lpm_nparticle": ([vp], C.c_int),
+        "lpm_set_types": ([vp, ip], C.c_int),
+        "lpm_set_material": ([vp, dp, dp, dp, dp, dp, C.c_double, C.c_int], C.c_int),
+        "lpm_set_cp": ([vp, dp], C.c_int),
+        "lpm_init_state": ([vp], C.c_int),
+        "lpm_load_step": ([vp, C.c_int, C.POINTER(DispBC), C.c_int, C.POINTER(ForceBC),
+                           C.POINTER(StepStats)], C.c_int),
+        "lpm_assemble_stiffness": ([vp], C.c_int),
+        "lpm_apply_bc": ([vp, C.c_int, C.POINTER(DispBC), C.c_int, C.POINTER(ForceBC)], C.c_int),
+        "lpm_compute_force": ([vp, C.c_int, dp], C.c_int),
+        "lpm_switch_state": ([vp, C.c_int], C.c_int),
+        "lpm_solve": ([vp, C.POINTER(StepStats)], C.c_int),
+        "lpm_begin_step": ([vp], C.c_int),
+        "lpm_get": ([vp, C.c_char_p, vp, C.c_size_t], C.c_int),
+        "lpm_set": ([vp, C.c_char_p, vp, C.c_size_t], C.c_int),
+        "lpm_get_sizes": ([vp, ip, ip, ip, C.POINTER(C.c_longlong)], C.c_int),
+        "lpm_export_upper_csr": ([vp, dp, ip, ip, C.POINTER(C.c_longlong)], C.c_int),
+        "lpm_spmv": ([vp, dp, dp], C.c_int),
+        "lpm_solve_rhs": ([vp, dp, dp, C.POINTER(StepStats)], C.c_int),
+        "lpm_spmv_timing": ([vp, dp, C.POINTER(C.c_longlong), C.c_int], C.c_int),
+        "lpm_spmv_bytes": ([vp, C.c_int], C.c_double),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def bc_arrays(disp_bcs, force_bcs):
+    nd, nf = len(disp_bcs), len(force_bcs)
+    darr = (DispBC * max(nd, 1))()
+    for k, (t, f, s) in enumerate(disp_bcs):
+        darr[k] = DispBC(int(t), f.encode(), float(s))
+    farr = (ForceBC * max(nf, 1))()
+    for k, (t, fx, fy, fz) in enumerate(force_bcs):
+        farr[k] = ForceBC(int(t), b"x", float(fx), b"y", float(fy), b"z", float(fz))
+    return nd, darr, nf, farr
+
+
+def default_opts():
+    o = SolverOpts()
+    load().lpm_default_solver_opts(C.byref(o))
+    return o
+
+
+class Specimen:
+    """One lattice specimen resident on one GPU (an lpm_ctx)."""
+
+    def __init__(self, device=0):
+        self.L = load()
+        h = C.c_void_p()
+        self._check(self.L.lpm_create(C.byref(h), device))
+        self.h = h
+        self.n = 0
+        self.nn = 18
+        self.nslip = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.lpm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc):
+        if rc < 0:
+            raise LPMError(self.L.lpm_last_error().decode() or f"error {rc}")
+        return rc
+
+    # ---- setup
+    def setup_lattice(self, lattice, radius, box):
+        box = np.ascontiguousarray(box, dtype=np.float64)
+        self.n = self._check(self.L.lpm_setup_lattice(self.h, lattice, radius, _dp(box)))
+        return self.n
+
+    def setup_particles(self, lattice, radius, xyz):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        self.n = self._check(self.L.lpm_setup_particles(self.h, lattice, radius, xyz.shape[0], _dp(xyz)))
+        return self.n
+
+    def set_types(self, types):
+        t = np.ascontiguousarray(types, dtype=np.int32)
+        self._check(self.L.lpm_set_types(self.h, _ip(t)))
+
+    def set_material(self, c11, c12, c44, sigmay=0.0, hardening=0.0, xi=0.0, plmode=PL_J2):
+        arrs = [np.ascontiguousarray(np.broadcast_to(np.asarray(v, dtype=np.float64), (self.n,)))
+                for v in (c11, c12, c44, sigmay, hardening)]
+        self._check(self.L.lpm_set_material(self.h, *[_dp(a) for a in arrs], float(xi), int(plmode)))
+
+    def set_cp(self, tau0, taus, h0, p, q, eta, maxloop, dtime):
+        cp = np.array([tau0, taus, h0, p, q, eta, maxloop, dtime], dtype=np.float64)
+        self._check(self.L.lpm_set_cp(self.h, _dp(cp)))
+
+    def init_state(self):
+        self._check(self.L.lpm_init_state(self.h))
+        n, nn, ns = C.c_int(), C.c_int(), C.c_int()
+        self._check(self.L.lpm_get_sizes(self.h, C.byref(n), C.byref(nn), C.byref(ns), None))
+        self.nslip = ns.value
+
+    def set_solver(self, **kw):
+        o = default_opts()
+        for k, v in kw.items():
+            if not hasattr(o, k):
+                raise KeyError(k)
+            setattr(o, k, v)
+        self._check(self.L.lpm_set_solver(self.h, C.byref(o)))
+        return o
+
+    def set_stream(self, stream_ptr):
+        self._check(self.L.lpm_set_stream(self.h, C.c_void_p(stream_ptr)))
+
+    # ---- hot path
+    def load_step(self, disp_bcs, force_bcs=()):
+        nd, darr, nf, farr = bc_arrays(disp_bcs, list(force_bcs))
+        st = StepStats()
+        self._check(self.L.lpm_load_step(self.h, nd, darr, nf, farr, C.byref(st)))
+        return st.as_dict()
+
+    def begin_step(self):
+        self._check(self.L.lpm_begin_step(self.h))
+
+    def assemble_stiffness(self):
+        self._check(self.L.lpm_assemble_stiffness(self.h))
+
+    def apply_bc(self, disp_bcs, force_bcs=()):
+        nd, darr, nf, farr = bc_arrays(disp_bcs, list(force_bcs))
+        self._check(self.L.lpm_apply_bc(self.h, nd, darr, nf, farr))
+
+    def compute_force(self, plmode):
+        norms = np.zeros(2)
+        self._check(self.L.lpm_compute_force(self.h, plmode, _dp(norms)))
+        return norms
+
+    def switch_state(self, flag):
+        self._check(self.L.lpm_switch_state(self.h, flag))
+
+    def solve(self):
+        st = StepStats()
+        self._check(self.L.lpm_solve(self.h, C.byref(st)))
+        return st.as_dict()
+
+    def solve_rhs(self, b):
+        b = np.ascontiguousarray(b, dtype=np.float64).reshape(-1)
+        x = np.zeros_like(b)
+        st = StepStats()
+        self._check(self.L.lpm_solve_rhs(self.h, _dp(b), _dp(x), C.byref(st)))
+        return x, st.as_dict()
+
+    def spmv(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1)
+        y = np.zeros_like(x)
+        self._check(self.L.lpm_spmv(self.h, _dp(x), _dp(y)))
+        return y
+
+    # ---- data
+    _SHAPES = {
+        "xyz": ("p3", np.float64), "xyz_initial": ("p3", np.float64), "xyz_temp": ("p3", np.float64),
+        "Pin": ("p3", np.float64), "Pex": ("p3", np.float64), "residual": ("p3", np.float64),
+        "disp": ("p3", np.float64), "F": ("b", np.float64), "F_temp": ("b", np.float64),
+        "dL": ("b", np.float64), "csx": ("b", np.float64), "csy": ("b", np.float64),
+        "csz": ("b", np.float64), "Kn": ("b", np.float64), "Tv": ("b", np.float64),
+        "distance_initial": ("b", np.float64), "dLp": ("b", np.float64), "dLp0": ("b", np.float64),
+        "dLp2": ("b", np.float64), "J2_alpha": ("n1", np.float64), "J2_alpha0": ("n1", np.float64),
+        "J2_alpha2": ("n1", np.float64), "J2_beta": ("n6", np.float64), "J2_beta2": ("n6", np.float64),
+        "J2_dlambda": ("n1", np.float64), "stress_tensor": ("n6", np.float64),
+        "neighbors": ("b", np.int32), "nsign": ("b", np.int32), "nb": ("n1", np.int32),
+        "nb_conn": ("n1", np.int32), "conn": ("n61", np.int32), "K_pointer": ("kp", np.int32),
+        "dispBC_index": ("p3", np.int32), "cs_initial": ("b3", np.float64),
+        "cp_gy": ("ns", np.float64), "cp_gy2": ("ns", np.float64), "cp_A_single": ("ns", np.float64),
+        "cp_A_single2": ("ns", np.float64), "cp_A": ("n1", np.float64), "cp_A2": ("n1", np.float64),
+        "cp_Cab": ("nss", np.float64),
+    }
+
+    def _shape(self, kind):
+        n, nn, ns = self.n, self.nn, self.nslip
+        return {"p3": (n, 3), "b": (n, nn), "n1": (n,), "n6": (n, 6), "n61": (n, 61), "kp": (n + 1, 2),
+                "b3": (n, nn, 3), "ns": (n, ns), "nss": (n, ns * ns)}[kind]
+
+    def get(self, name):
+        kind, dt = self._SHAPES[name]
+        out = np.zeros(self._shape(kind), dtype=dt)
+        self._check(self.L.lpm_get(self.h, name.encode(), out.ctypes.data_as(C.c_void_p), out.nbytes))
+        return out
+
+    def set(self, name, arr):
+        alias = {"dLp1": "dLp", "J2_alpha1": "J2_alpha", "J2_beta0": "J2_beta2", "J2_beta1": "J2_beta"}
+        kind, dt = self._SHAPES.get(name, self._SHAPES.get(alias.get(name, ""), ("b", np.float64)))
+        a = np.ascontiguousarray(arr, dtype=dt)
+        self._check(self.L.lpm_set(self.h, name.encode(), a.ctypes.data_as(C.c_void_p), a.nbytes))
+
+    def export_upper_csr(self):
+        nnz = C.c_longlong()
+        self._check(self.L.lpm_export_upper_csr(self.h, None, None, None, C.byref(nnz)))
+        K = np.zeros(nnz.value)
+        IK = np.zeros(3 * self.n + 1, dtype=np.int32)
+        JK = np.zeros(nnz.value, dtype=np.int32)
+        self._check(self.L.lpm_export_upper_csr(self.h, _dp(K), _ip(IK), _ip(JK), C.byref(nnz)))
+        return K, IK, JK
+
+    def sizes(self):
+        n, nn, ns, nb = C.c_int(), C.c_int(), C.c_int(), C.c_longlong()
+        self._check(self.L.lpm_get_sizes(self.h, C.byref(n), C.byref(nn), C.byref(ns), C.byref(nb)))
+        return dict(n=n.value, nn=nn.value, nslip=ns.value, nnz_blocks=nb.value)
+
+    def spmv_timing(self, reset=0):
+        ms, cnt = C.c_double(), C.c_longlong()
+        self._check(self.L.lpm_spmv_timing(self.h, C.byref(ms), C.byref(cnt), int(reset)))
+        return ms.value, cnt.value
+
+    def spmv_bytes(self, precision):
+        return self.L.lpm_spmv_bytes(self.h, int(precision))
