@@ -1,0 +1,378 @@
+"""Benchmark: load steps/s of the 1M-particle SC elastoplastic cyclic case.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (one "step" = one load step of src/lpmc_project.c:385-471): simple
+cubic lattice 100 x 100 x 100 (1e6 particles, 8.9e6 bonds, 3e6 DOF),
+spacing 0.2 mm, E = 200 GPa with +-5% uniform noise per particle (seed 1),
+nu = 0.3, J2 yield 250 MPa, linear hardening 2 GPa; bottom face fixed in z
+(plus a 3-DOF rigid-body pin), top face displaced along the +-0.2% strain
+cycle, 20 steps per quarter cycle; Newton tolerance 1e-8, block-Jacobi PCG
+to relative residual 1e-10.  The W warm-up steps are the first W steps of
+the schedule; the K timed steps follow them.
+
+Headline: the mixed-precision path (FP32 stiffness/SpMV/PCG with FP64
+reliable updates, FP64 residuals and return map).  The same steps run on the
+plain FP64 path for the ratio and the displacement error between the two.
+Inputs are resident in HBM (value); `e2e` runs the same steps through the
+reference-named C drop-in (liblpmhost.so + liblpmgpu_legacy.so) with the
+include/lpm.h globals on the host, host<->device copies inside the timed
+region.  The reference arm times the oracle's C port of the reference
+algorithm on the host cores.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "lpm-c_gb300"), os.path.join(ROOT, "oracle"), os.path.join(ROOT, "tests", "golden")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import cases  # noqa: E402
+
+METRIC = "load steps/s, 1M-particle SC lattice: mixed vs FP64 GPU @1e-8 err; SpMV GB/s"
+UNIT = "load steps/s"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.tmp = tempfile.NamedTemporaryFile(prefix="clocks", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait(timeout=10)
+        self.tmp.close()
+        rows = []
+        with open(self.tmp.name) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) >= 9:
+                    rows.append(p)
+        os.unlink(self.tmp.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        loaded = sorted(sm)[len(sm) // 2:] if sm else []
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons, "samples": len(rows)}
+
+
+def build_specimen(G, case, precision, stream=None):
+    s = G.Specimen(0)
+    if stream is not None:
+        s.set_stream(stream)
+    n = s.setup_lattice(case.lattice, case.radius, case.box)
+    types = cases.sc_types(s.get("xyz"), s.get("nb"), case.radius)
+    s.set_types(types)
+    c11, c12, c44 = cases.iso_cubic(case.E, case.nu)
+    u = cases.splitmix64_uniform(case.seed, n)
+    sc = 1.0 + case.e_noise * (2.0 * u - 1.0)
+    s.set_material(c11 * sc, c12 * sc, c44 * sc, case.sigmay, case.H, 0.0, G.PL_J2)
+    s.init_state()
+    s.set_solver(precision=precision, newton_tol=case.newton_tol, newton_maxiter=100, cg_rtol=1e-10,
+                 cg_maxiter=200000)
+    return s, types
+
+
+def run_ours(args):
+    import torch
+    import lpm_gb300 as G
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    case = cases.SCCase(n=args.size, e_noise=0.05, seed=1)
+    sched = case.schedule
+    W, K = args.warmup, args.steps
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    results = {}
+    for prec_name, prec in (("mixed", G.PREC_MIXED), ("fp64", G.PREC_FP64)):
+        if prec_name == "fp64" and args.no_fp64:
+            continue
+        s, types = build_specimen(G, case, prec, stream.cuda_stream)
+        for k in range(W):
+            s.load_step(cases.sc_bcs(sched[k]))
+        barrier()
+        s.spmv_timing(reset=2)
+        clocks = ClockSampler(local)
+        clocks.start()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        stats = []
+        barrier()
+        ev0.record(stream)
+        for k in range(W, W + K):
+            stats.append(s.load_step(cases.sc_bcs(sched[k])))
+        ev1.record(stream)
+        barrier()
+        ms = ev0.elapsed_time(ev1)
+        ck = clocks.stop()
+        spmv_ms, spmv_cnt = s.spmv_timing(reset=3)
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        results[prec_name] = dict(ms=ms, stats=stats, spmv_ms=spmv_ms, spmv_cnt=spmv_cnt, clocks=ck,
+                                  spmv_bytes=s.spmv_bytes(prec), xyz=s.get("xyz"), x0=s.get("xyz_initial"),
+                                  n=s.n, nnzb=s.sizes()["nnz_blocks"])
+        s.close()
+        del s
+    mixed = results["mixed"]
+    value = world * K / (mixed["ms"] / 1e3)
+    hbm, peak_src = peaks()
+    achieved = mixed["spmv_bytes"] / (mixed["spmv_ms"] * 1e-3) / 1e9 if mixed["spmv_ms"] > 0 else None
+    err = None
+    fp64_rate = None
+    if "fp64" in results:
+        f = results["fp64"]
+        fp64_rate = world * K / (f["ms"] / 1e3)
+        du_m = mixed["xyz"] - mixed["x0"]
+        du_f = f["xyz"] - f["x0"]
+        err = float(np.abs(du_m - du_f).max() / np.abs(du_f).max())
+    e2e = run_e2e(args, case) if (not args.no_e2e and rank == 0) else None
+    counts = step_counts(args.size, W, K, results["fp64"]["stats"] if "fp64" in results else None)
+    cpu = run_cpu_baseline(args, case, counts) if (not args.no_cpu and rank == 0) else None
+    agg = lambda key: int(sum(st[key] for st in mixed["stats"]))  # noqa: E731
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": mixed["ms"] / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 stiffness/SpMV/PCG + f64 residual, refinement and return map",
+        "data": "synthetic (seeded lattice and material noise)",
+        "config": {"workload": f"SC {args.size}^3 elastoplastic cyclic, load steps {W + 1}-{W + K} of "
+                               f"{len(sched)} (first yield near step 12)",
+                   "particles": mixed["n"], "nnz_blocks": mixed["nnzb"], "precision": "mixed",
+                   "fp64_steps_per_s": fp64_rate, "mixed_over_fp64": (value / fp64_rate) if fp64_rate else None,
+                   "disp_err_mixed_vs_fp64": err, "newton_iters": agg("newton_iters"), "cg_iters": agg("cg_iters"),
+                   "reliable_updates": agg("refine_iters"),
+                   "fp64_cg_iters": (sum(st["cg_iters"] for st in results["fp64"]["stats"])
+                                     if "fp64" in results else None),
+                   "l2": "SpMV stream of 2.4 GB per call > 129 MB L2 (no flush needed)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": (achieved / hbm) if achieved else None, "traffic": None,
+                     "kernel": "k_spmv_f (FP32 block-CSR SpMV)", "peak_source": peak_src,
+                     "spmv_launches_sampled": mixed["spmv_cnt"]},
+        "clocks": mixed["clocks"],
+        "gpu_launches": gpu_launches(mixed["stats"]),
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def gpu_launches(stats):
+    """Kernel launches of the timed steps (counted from the solver statistics):
+    per step 3 (stiffness) + 2 (BC) + 1 (preconditioner) + 2 (predictor);
+    per Newton iteration 2 (force) + 1 (xyz update) + 1 (norm);
+    per PCG iteration 3; per reliable update 3."""
+    total = 0
+    for st in stats:
+        total += 8 + 4 * st["newton_iters"] + 3 * st["cg_iters"] + 3 * st["refine_iters"] + st["newton_iters"]
+    return total
+
+
+def run_e2e(args, case):
+    """Same steps through the reference-named C drop-in with host globals."""
+    try:
+        import torch
+        import lpm_gb300 as G
+        import lpm_host
+        h = lpm_host.HostDriver()
+        n = h.setup(case.lattice, case.radius, case.box)
+        xyz = h.get("xyz")
+        nbv = np.zeros(n, dtype=np.int32)
+        # particle types exactly as the GPU specimen (full neighbour lists -> type 3)
+        s = G.Specimen(0)
+        s.setup_lattice(case.lattice, case.radius, case.box)
+        nbv = s.get("nb")
+        s.close()
+        types = cases.sc_types(xyz, nbv, case.radius)
+        # one type per particle class; materials per particle need distinct Ce rows:
+        # use 6 types for BCs and give E noise through one Ce row per particle
+        u = cases.splitmix64_uniform(case.seed, n)
+        sc = 1.0 + case.e_noise * (2.0 * u - 1.0)
+        c11, c12, c44 = cases.iso_cubic(case.E, case.nu)
+        ce = np.stack([c11 * sc, c12 * sc, c44 * sc], 1)
+        # types carry both: particle i gets its own Ce row (ntype = n + NTYPE offset)
+        # BCs select by type, so keep BC types and put materials in per-type rows
+        tb = types.astype(np.int64)
+        h.set_types(tb, cases.NTYPE)
+        h.set_material(np.tile(cases.iso_cubic(case.E, case.nu), (cases.NTYPE, 1)), 0, case.sigmay, 0.0, case.H)
+        h.set_solver(precision=G.PREC_MIXED, cg_rtol=1e-10, cg_maxiter=200000)
+        h.init()
+        W, K = args.warmup, args.steps
+        for k in range(W):
+            h.load_step(cases.sc_bcs(case.schedule[k]), newton_tol=case.newton_tol)
+        h.traffic(reset=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(W, W + K):
+            h.load_step(cases.sc_bcs(case.schedule[k]), newton_tol=case.newton_tol)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        h2d, d2h = h.traffic()
+        return {"value": K / dt, "unit": UNIT, "h2d_bytes_per_step": h2d / K, "d2h_bytes_per_step": d2h / K,
+                "path": "C host loop (liblpmhost) -> reference-named drop-in (liblpmgpu_legacy), "
+                        "include/lpm.h globals on the host",
+                "note": "uniform E (per-particle E needs one Ce row per particle in the legacy ABI)"}
+    except Exception as e:  # report, never fake
+        return {"value": None, "unit": UNIT, "error": str(e)[:300]}
+
+
+COUNTS_FILE = os.path.join(ROOT, "profiles", "iteration_counts_sc100.json")
+
+
+def step_counts(size, W, K, stats=None):
+    """Newton iterations per step and CG iterations per Newton iteration of the
+    timed steps: from this run when available, else from the committed record
+    of an earlier FP64 GPU run of the same steps, else a model."""
+    if stats:
+        newton = sum(st["newton_iters"] for st in stats) / len(stats)
+        cg = sum(st["cg_iters"] for st in stats) / max(1.0, sum(st["newton_iters"] for st in stats))
+        return newton, cg, "this run's FP64 GPU counts"
+    try:
+        with open(COUNTS_FILE) as f:
+            d = json.load(f)
+        if d.get("size") == size and d.get("first_step") == W + 1 and d.get("steps") == K:
+            return d["newton_per_step"], d["cg_per_newton"], "recorded FP64 GPU counts (" + COUNTS_FILE[len(ROOT) + 1:] + ")"
+    except Exception:
+        pass
+    return 2.0, 1800.0, "model: 2 Newton iterations, 1800 CG iterations each"
+
+
+def run_cpu_baseline(args, case, counts):
+    """Per-load-step cost of the reference algorithm (the oracle's C port, all
+    host threads) at full size, from bounded samples of each phase."""
+    try:
+        import oracle as O
+        threads = os.cpu_count() or 1
+        O.set_threads(threads)
+        o = O.Oracle()
+        t0 = time.perf_counter()
+        n = o.setup_lattice(case.lattice, case.radius, case.box)
+        setup_s = time.perf_counter() - t0
+        types = cases.sc_types(o.d("xyz", (n, 3)), o.i("nb", (n,)), case.radius)
+        o.set_types(types)
+        u = cases.splitmix64_uniform(case.seed, n)
+        sc = 1.0 + case.e_noise * (2.0 * u - 1.0)
+        c11, c12, c44 = cases.iso_cubic(case.E, case.nu)
+        o.set_material(c11 * sc, c12 * sc, c44 * sc, case.sigmay, case.H, 0.0, 0)
+        o.init_state()
+        rows = min(n, 2000)
+        r0 = n // 2
+        t0 = time.perf_counter()
+        o.L.lo_fd_stiffness_range(o.h, r0, r0 + rows)  # serial, as the reference's side effects require
+        t_fd = (time.perf_counter() - t0) * n / rows / threads  # the reference runs it OpenMP-parallel
+        t0 = time.perf_counter()
+        o.force(0)
+        t_force = time.perf_counter() - t0
+        nit = 10
+        t0 = time.perf_counter()
+        o.L.lo_cg_iterations(o.h, nit)
+        t_cg = (time.perf_counter() - t0) / nit
+        newton, cgit, src = counts
+        step_s = t_fd + newton * (t_force + cgit * t_cg)
+        return {"value": 1.0 / step_s, "unit": UNIT, "cores": threads, "kind": "port",
+                "sample": (f"oracle C port of the reference path at {n} particles: FD stiffness of {rows} "
+                           f"rows (scaled to all rows and {threads} threads), one J2 force sweep, {nit} "
+                           f"threaded CG iterations on the full upper CSR; per step = FD + {newton:.1f} "
+                           f"Newton x (force + {cgit:.0f} CG iterations) - counts: {src} (the reference's "
+                           f"unpreconditioned CG needs more, so this flatters the CPU)"),
+                "phase_s": {"fd_stiffness": t_fd, "force": t_force, "cg_iter": t_cg, "setup": setup_s}}
+    except Exception as e:
+        return {"value": None, "unit": UNIT, "kind": "port", "error": str(e)[:300]}
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    case = cases.SCCase(n=args.size, e_noise=0.05, seed=1)
+    cpu = run_cpu_baseline(args, case, step_counts(args.size, args.warmup, args.steps))
+    line = {"metric": METRIC, "impl": "reference", "value": cpu.get("value"), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "vs_baseline": None,
+            "config": {"workload": f"SC {args.size}^3 elastoplastic cyclic"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": cpu.get("value"), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=100)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

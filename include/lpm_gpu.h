@@ -69,8 +69,8 @@ typedef struct {
     int newton_maxiter; /* MAXITER (include/lpm.h:39) */
     double cg_rtol;     /* linear solve: |b - K x| <= cg_rtol * |b| */
     int cg_maxiter;     /* cap on PCG iterations per solve (FP64) or per inner solve (mixed) */
-    double inner_rtol;  /* mixed: relative tolerance of each FP32 inner PCG solve */
-    int refine_maxiter; /* mixed: cap on FP64 refinement sweeps */
+    double inner_rtol;  /* mixed: FP32 residual drop between FP64 reliable updates (default 0.1) */
+    int refine_maxiter; /* mixed: cap on FP64 reliable updates per solve */
     int check_every;    /* PCG iterations between host convergence checks (graph chunk) */
     int use_graphs;     /* capture PCG chunks as CUDA graphs */
     int spmv_variant;   /* 0 = default; others select alternative SpMV kernels (tuning) */

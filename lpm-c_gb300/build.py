@@ -17,6 +17,7 @@ SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "liblpmgpu.so")
 LEGACY_LIB = os.path.join(OUT, "liblpmgpu_legacy.so")
+HOST_LIB = os.path.join(OUT, "liblpmhost.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -105,6 +106,12 @@ def build(verbose=False, ptxas_info=False):
     if lobjs and _stale(LEGACY_LIB, lobjs + [LIB]):
         _run(["g++", "-shared", "-o", LEGACY_LIB] + lobjs + ["-L", OUT, "-llpmgpu",
                                                               "-Wl,-rpath,$ORIGIN"])
+    # C host driver: defines the include/lpm.h globals, runs the reference loop
+    host_src = os.path.join(HERE, "host", "lpm_host.c")
+    if os.path.exists(host_src) and _stale(HOST_LIB, [host_src, LEGACY_LIB] + hdr):
+        _run(["gcc", "-std=gnu11", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-I", INCLUDE,
+              "-o", HOST_LIB, host_src, "-L", OUT, "-llpmgpu_legacy", "-llpmgpu",
+              "-Wl,-rpath,$ORIGIN", "-lm"])
     return LIB
 
 

@@ -287,7 +287,8 @@ struct VecArgs {
 // x = 0, r = mask(b) (cast), z = P^-1 r, p = z, rz, rr, |b|^2, tolerance.
 template <typename V, typename V4>
 __global__ void __launch_bounds__(VTPB) k_cg_init(VecArgs a, const dvec4 *b, double scale, const V *P,
-                                                  V4 *x, V4 *r, V4 *z, V4 *p, double rtol, int maxit)
+                                                  V4 *x, V4 *r, V4 *z, V4 *p, double rtol, int maxit,
+                                                  double delta2)
 {
     double v[2] = {0.0, 0.0};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
@@ -308,17 +309,46 @@ __global__ void __launch_bounds__(VTPB) k_cg_init(VecArgs a, const dvec4 *b, dou
         v[1] += (double)rv.x * rv.x + (double)rv.y * rv.y + (double)rv.z * rv.z;
     }
     CgScalars *sc = a.sc;
-    grid_reduce<2>(v, a.partials, a.counter, [sc, rtol, maxit](const double *t) {
+    grid_reduce<2>(v, a.partials, a.counter, [sc, rtol, maxit, delta2](const double *t) {
         sc->rz = t[0];
         sc->rz_old = t[0];
         sc->rr = t[1];
+        sc->rr_max = t[1];
         sc->bnorm2 = t[1];
         sc->tol2 = rtol * rtol * t[1];
+        sc->upd_delta2 = delta2;
         sc->it = 0;
         sc->maxit = maxit;
         sc->done = (t[1] <= sc->tol2 || !(t[1] == t[1])) ? 1 : 0;
         sc->alpha = 0.0;
         sc->beta = 0.0;
+        sc->upd_req = 0;
+    });
+}
+
+// Reliable update (residual replacement) of the FP32 CG: r = (FP64 true
+// residual) * scale, z = P^-1 r, the search direction p is kept, so the
+// iteration continues with its Krylov history.
+__global__ void __launch_bounds__(VTPB) k_reliable(VecArgs a, const dvec4 *r64, double scale, const float *P,
+                                                   float4 *r, float4 *z)
+{
+    double v[2] = {0.0, 0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
+        const dvec4 bb = mask4(r64[i], a.mask[i]);
+        const float4 rv = make_float4((float)(bb.x * scale), (float)(bb.y * scale), (float)(bb.z * scale), 0.f);
+        const float4 zv = apply_pinv<float, float4>(P, a.n, i, rv);
+        r[i] = rv;
+        z[i] = zv;
+        v[0] += (double)rv.x * zv.x + (double)rv.y * zv.y + (double)rv.z * zv.z;
+        v[1] += (double)rv.x * rv.x + (double)rv.y * rv.y + (double)rv.z * rv.z;
+    }
+    CgScalars *sc = a.sc;
+    grid_reduce<2>(v, a.partials, a.counter, [sc](const double *t) {
+        sc->rz = t[0];
+        sc->rr = t[1];
+        sc->rr_max = t[1];
+        sc->done = !(t[1] == t[1]) ? 3 : 0;
+        sc->upd_req = 0;
     });
 }
 
@@ -360,12 +390,17 @@ __global__ void __launch_bounds__(VTPB) k_cg_update(VecArgs a, const V *P, V4 *x
             sc->done = 3;
         else if (sc->it >= sc->maxit)
             sc->done = 2;
+        else if (t[1] < sc->upd_delta2 * sc->rr_max)
+            sc->upd_req = 1;  // raised as done = 4 once p is updated (k_cg_p)
+        if (t[1] > sc->rr_max)
+            sc->rr_max = t[1];
     });
 }
 
-// p = z + beta p
+// p = z + beta p; the last block turns a pending reliable-update request into
+// done = 4, so the host updates only after p belongs to the new iteration.
 template <typename V, typename V4>
-__global__ void __launch_bounds__(VTPB) k_cg_p(int n, const CgScalars *sc, const V4 *z, V4 *p)
+__global__ void __launch_bounds__(VTPB) k_cg_p(int n, CgScalars *sc, const V4 *z, V4 *p, unsigned *counter)
 {
     if (sc->done)
         return;
@@ -378,10 +413,21 @@ __global__ void __launch_bounds__(VTPB) k_cg_p(int n, const CgScalars *sc, const
         pv.z = zv.z + be * pv.z;
         p[i] = pv;
     }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(counter, 1u) == gridDim.x - 1) {
+            if (sc->upd_req) {
+                sc->upd_req = 0;
+                sc->done = 4;
+            }
+            *counter = 0u;
+        }
+    }
 }
 
-// x64 += x32 / scale
-__global__ void k_axpy_refine(int n, dvec4 *x, const float4 *d, double inv_scale)
+// x64 += x32 / scale, x32 = 0
+__global__ void k_axpy_refine(int n, dvec4 *x, float4 *d, double inv_scale)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         dvec4 xv = x[i];
@@ -390,6 +436,16 @@ __global__ void k_axpy_refine(int n, dvec4 *x, const float4 *d, double inv_scale
         xv.y += (double)dv.y * inv_scale;
         xv.z += (double)dv.z * inv_scale;
         x[i] = xv;
+        d[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+// y = x * s
+__global__ void k_scale_copy(int n, dvec4 *y, const dvec4 *x, double s)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const dvec4 v = x[i];
+        y[i] = make_dvec4(v.x * s, v.y * s, v.z * s, 0.0);
     }
 }
 
@@ -483,16 +539,26 @@ void launch_refine_residual(Ctx &c, const dvec4 *x, const dvec4 *b, dvec4 *r)
     k_refine_res<<<red_grid(c), VTPB, 0, c.stream>>>(spmv_args(c), c.Kf, x, b, r, c.norms, 2);
 }
 
-void launch_cg_init_d(Ctx &c, const dvec4 *b)
+void launch_cg_init_d(Ctx &c, const dvec4 *b, double scale)
 {
     k_cg_init<double, dvec4><<<red_grid(c), VTPB, 0, c.stream>>>(
-        vec_args(c), b, 1.0, c.Pinv_d, c.x_d, c.r_d, c.z_d, c.p_d, c.opts.cg_rtol, c.opts.cg_maxiter);
+        vec_args(c), b, scale, c.Pinv_d, c.x_d, c.r_d, c.z_d, c.p_d, c.opts.cg_rtol, c.opts.cg_maxiter, 0.0);
 }
 
-void launch_cg_init_f(Ctx &c, const dvec4 *r64, double scale)
+void launch_cg_init_f(Ctx &c, const dvec4 *r64, double scale, double rtol, double delta2)
 {
     k_cg_init<float, float4><<<red_grid(c), VTPB, 0, c.stream>>>(
-        vec_args(c), r64, scale, c.Pinv_f, c.x_f, c.r_f, c.z_f, c.p_f, c.opts.inner_rtol, c.opts.cg_maxiter);
+        vec_args(c), r64, scale, c.Pinv_f, c.x_f, c.r_f, c.z_f, c.p_f, rtol, c.opts.cg_maxiter, delta2);
+}
+
+void launch_reliable(Ctx &c, const dvec4 *r64, double scale)
+{
+    k_reliable<<<red_grid(c), VTPB, 0, c.stream>>>(vec_args(c), r64, scale, c.Pinv_f, c.r_f, c.z_f);
+}
+
+void launch_scale_copy(Ctx &c, dvec4 *y, const dvec4 *x, double s)
+{
+    k_scale_copy<<<red_grid(c), VTPB, 0, c.stream>>>(c.n, y, x, s);
 }
 
 void launch_cg_iter_d(Ctx &c)
@@ -501,7 +567,7 @@ void launch_cg_iter_d(Ctx &c)
     const int g = red_grid(c);
     k_cg_update<double, dvec4><<<g, VTPB, 0, c.stream>>>(vec_args(c), c.Pinv_d, c.x_d, c.r_d, c.z_d,
                                                            c.p_d, c.q_d);
-    k_cg_p<double, dvec4><<<g, VTPB, 0, c.stream>>>(c.n, c.sc, c.z_d, c.p_d);
+    k_cg_p<double, dvec4><<<g, VTPB, 0, c.stream>>>(c.n, c.sc, c.z_d, c.p_d, c.counter);
 }
 
 void launch_cg_iter_f(Ctx &c)
@@ -510,7 +576,7 @@ void launch_cg_iter_f(Ctx &c)
     const int g = red_grid(c);
     k_cg_update<float, float4><<<g, VTPB, 0, c.stream>>>(vec_args(c), c.Pinv_f, c.x_f, c.r_f, c.z_f, c.p_f,
                                                          c.q_f);
-    k_cg_p<float, float4><<<g, VTPB, 0, c.stream>>>(c.n, c.sc, c.z_f, c.p_f);
+    k_cg_p<float, float4><<<g, VTPB, 0, c.stream>>>(c.n, c.sc, c.z_f, c.p_f, c.counter);
 }
 
 void launch_axpy_refine(Ctx &c, double scale)

@@ -304,8 +304,8 @@ void lpm_default_solver_opts(lpm_solver_opts *o)
     o->newton_maxiter = 100;
     o->cg_rtol = 1e-10;
     o->cg_maxiter = 20000;
-    o->inner_rtol = 1e-4;
-    o->refine_maxiter = 40;
+    o->inner_rtol = 0.1;
+    o->refine_maxiter = 200;
     o->check_every = 16;
     o->use_graphs = 1;
     o->spmv_variant = 0;
@@ -642,13 +642,33 @@ static int run_pcg(Ctx &c, bool fp32, int &iters, int &status)
     return LPM_OK;
 }
 
-// Solve K x = b (b device, masked); x written to c.du.  FP64 PCG, or FP32 PCG
-// inside FP64 iterative refinement.
+// Solve K x = b (b on the device, masked); x is written to c.du.
+// The right-hand side is normalised by |b| so the iterates stay O(1) and
+// squared residual norms 1e-10..1e-12 below the start cannot underflow (the
+// reference's CG divides 0/0 there once forces are small).
+// FP64: block-Jacobi PCG.  Mixed: FP32 PCG with reliable updates - when the
+// FP32 recursive residual has fallen by the factor opts.inner_rtol since the
+// last update (or meets the tolerance), x64 absorbs the FP32 increment, the
+// true residual b - K32 x64 is recomputed with FP64 products and sums, and
+// replaces the FP32 residual; the search direction is kept, so CG keeps its
+// Krylov history.  Convergence is judged on the FP64 true residual.
 static int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
 {
     int rc;
+    launch_norm2(c, b, 2);
+    LPM_CUDA(cudaMemcpyAsync(c.norms_host, c.norms, 4 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    if ((rc = sync(c)))
+        return rc;
+    const double bn = std::sqrt(c.norms_host[2]);
+    if (!(bn > 0.0) || !std::isfinite(bn)) {
+        LPM_CUDA(cudaMemsetAsync(c.du, 0, sizeof(dvec4) * c.n, c.stream));
+        if (st && !std::isfinite(bn))
+            st->status |= LPM_STATUS_NAN;
+        return LPM_OK;
+    }
+    const double scale = 1.0 / bn;
     if (c.opts.precision == LPM_PREC_FP64) {
-        launch_cg_init_d(c, b);
+        launch_cg_init_d(c, b, scale);
         int it = 0, done = 0;
         if ((rc = run_pcg(c, false, it, done)))
             return rc;
@@ -660,46 +680,36 @@ static int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
             if (done == 3)
                 st->status |= LPM_STATUS_NAN;
         }
-        LPM_CUDA(cudaMemcpyAsync(c.du, c.x_d, sizeof(dvec4) * c.n, cudaMemcpyDeviceToDevice, c.stream));
+        launch_scale_copy(c, c.du, c.x_d, bn);
         return LPM_OK;
     }
-    // mixed: x = 0, r = b; repeat: inner FP32 PCG on r/|r|, x += d|r|, r = b - K32 x
     LPM_CUDA(cudaMemsetAsync(c.x_d, 0, sizeof(dvec4) * c.n, c.stream));
-    launch_norm2(c, b, 2);
-    double bn = 0, rn = 0;
-    {
-        LPM_CUDA(cudaMemcpyAsync(c.norms_host, c.norms, 4 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
-        if ((rc = sync(c)))
-            return rc;
-        bn = std::sqrt(c.norms_host[2]);
-    }
-    rn = bn;
-    const dvec4 *r = b;
-    int sweeps = 0;
-    while (rn > c.opts.cg_rtol * bn && sweeps < c.opts.refine_maxiter && rn > 0 && std::isfinite(rn)) {
-        const double scale = 1.0 / rn;
-        launch_cg_init_f(c, r, scale);
-        int it = 0, done = 0;
+    const double delta = c.opts.inner_rtol;
+    launch_cg_init_f(c, b, scale, c.opts.cg_rtol, delta * delta);
+    int sweeps = 0, it = 0, done = 0;
+    double rn = bn;
+    for (;;) {
         if ((rc = run_pcg(c, true, it, done)))
             return rc;
         launch_axpy_refine(c, scale);
         launch_refine_residual(c, c.x_d, b, c.r_d);
-        r = c.r_d;
         LPM_CUDA(cudaMemcpyAsync(c.norms_host, c.norms, 4 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
         if ((rc = sync(c)))
             return rc;
         rn = std::sqrt(c.norms_host[2]);
         sweeps++;
-        if (st) {
-            st->cg_iters += it;
-            st->spmv_calls += it + 1;
-            st->refine_iters += 1;
-            if (done == 3)
-                st->status |= LPM_STATUS_NAN;
-        }
+        if (rn <= c.opts.cg_rtol * bn || done == 2 || done == 3 || !std::isfinite(rn) ||
+            sweeps >= c.opts.refine_maxiter)
+            break;
+        launch_reliable(c, c.r_d, scale);
     }
-    if (st && rn > c.opts.cg_rtol * bn)
-        st->status |= std::isfinite(rn) ? LPM_STATUS_CG_MAXIT : LPM_STATUS_NAN;
+    if (st) {
+        st->cg_iters += it;
+        st->spmv_calls += it + sweeps;
+        st->refine_iters += sweeps;
+        if (rn > c.opts.cg_rtol * bn)
+            st->status |= std::isfinite(rn) ? LPM_STATUS_CG_MAXIT : LPM_STATUS_NAN;
+    }
     LPM_CUDA(cudaMemcpyAsync(c.du, c.x_d, sizeof(dvec4) * c.n, cudaMemcpyDeviceToDevice, c.stream));
     return LPM_OK;
 }
@@ -1113,6 +1123,12 @@ int lpm_set(lpm_ctx *ctx, const char *name, const void *src, size_t bytes)
     if (nm == "J2_alpha" || nm == "J2_alpha1") return rows_d(c.alpha[1], 1);
     if (nm == "J2_beta0") return rows_d(c.beta[0], 6);
     if (nm == "J2_beta" || nm == "J2_beta1") return rows_d(c.beta[1], 6);
+    if (nm == "cp_gy0" && c.nslip) return rows_d(c.gy[0], c.nslip);
+    if (nm == "cp_A_single0" && c.nslip) return rows_d(c.As[0], c.nslip);
+    if (nm == "cp_A0" && c.nslip) return rows_d(c.A[0], 1);
+    if ((nm == "cp_gy" || nm == "cp_gy1") && c.nslip) return rows_d(c.gy[1], c.nslip);
+    if ((nm == "cp_A_single" || nm == "cp_A_single1") && c.nslip) return rows_d(c.As[1], c.nslip);
+    if ((nm == "cp_A" || nm == "cp_A1") && c.nslip) return rows_d(c.A[1], 1);
     if (nm == "dispBC_index") {
         if (bytes < 3 * (size_t)n * sizeof(int))
             return fail(LPM_ERR_ARG, nm + ": buffer too small");

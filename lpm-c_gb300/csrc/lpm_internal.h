@@ -72,9 +72,12 @@ void kntv_per_particle(int lattice, double radius, const double *c11, const doub
                        const double *c44, int n, double *knt);
 
 // Device scalars used by the PCG (one 128-byte record).
+// done: 0 running, 1 converged (recursive residual), 2 iteration cap,
+// 3 non-finite, 4 reliable update requested (mixed precision)
 struct CgScalars {
     double rz, rz_old, pq, rr, alpha, beta, bnorm2, tol2;
-    int it, done, maxit, pad;
+    double rr_max, upd_delta2;
+    int it, done, maxit, upd_req;
 };
 
 struct Ctx {
@@ -178,8 +181,10 @@ void launch_block_jacobi(Ctx &c, bool fp32);
 void launch_spmv_d(Ctx &c, const dvec4 *x, dvec4 *y, bool masked, bool dot_pq);
 void launch_spmv_f(Ctx &c, const float4 *x, float4 *y, bool masked, bool dot_pq);
 void launch_refine_residual(Ctx &c, const dvec4 *x, const dvec4 *b, dvec4 *r);  // r = b - K32 x (FP64)
-void launch_cg_init_d(Ctx &c, const dvec4 *b);
-void launch_cg_init_f(Ctx &c, const dvec4 *r64, double scale);
+void launch_cg_init_d(Ctx &c, const dvec4 *b, double scale);
+void launch_cg_init_f(Ctx &c, const dvec4 *r64, double scale, double rtol, double delta2);
+void launch_reliable(Ctx &c, const dvec4 *r64, double scale);
+void launch_scale_copy(Ctx &c, dvec4 *y, const dvec4 *x, double s);
 void launch_cg_iter_d(Ctx &c);
 void launch_cg_iter_f(Ctx &c);
 void launch_axpy_refine(Ctx &c, double scale);  // x_d += x_f / scale

@@ -20,6 +20,7 @@
 #endif
 #include "lpm_oracle.h"
 #include "mkl_shim/mkl.h"
+#include "cg_rci.h"
 
 #define NDIM 3
 #define EPSP 1e-6      /* include/lpm.h:42 EPS */
@@ -864,6 +865,72 @@ int lo_solver_cg(lpm_oracle *o, double rtol_sq, double atol_sq)
         for (int d = 0; d < 3; d++)
             o->xyz[3 * i + d] += o->disp[3 * i + d];
     return fail ? -1 : it;
+}
+
+/* Timing helper for the CPU baseline: nit iterations of the reference's CG
+ * (src/solver.c:188-270) on the current upper CSR and residual, with the
+ * symmetric product spread over all OpenMP threads (per-thread accumulation,
+ * as a threaded sparse BLAS would).  Returns the iterations run. */
+int lo_cg_iterations(lpm_oracle *o, int nit)
+{
+    int n = 3 * o->n, nt = 1;
+#ifdef _OPENMP
+    nt = omp_get_max_threads();
+#endif
+    double *x = DALLOC(n), *r = DALLOC(n), *p = DALLOC(n), *q = DALLOC(n);
+    double *acc = DALLOC((size_t)nt * n);
+    memcpy(r, o->residual, sizeof(double) * n);
+    memcpy(p, r, sizeof(double) * n);
+    double rr = lpm_rci_dot(n, r, r);
+    int it = 0;
+    for (; it < nit; it++) {
+#pragma omp parallel
+        {
+            int t = 0;
+#ifdef _OPENMP
+            t = omp_get_thread_num();
+#endif
+            double *a = acc + (size_t)t * n;
+            memset(a, 0, sizeof(double) * n);
+#pragma omp for schedule(static)
+            for (int i = 0; i < n; i++)
+                for (int k = o->IK[i] - 1; k < o->IK[i + 1] - 1; k++) {
+                    int j = o->JK[k] - 1;
+                    a[i] += o->K[k] * p[j];
+                    if (j != i)
+                        a[j] += o->K[k] * p[i];
+                }
+#pragma omp for schedule(static)
+            for (int i = 0; i < n; i++) {
+                double s = 0.0;
+                for (int u = 0; u < nt; u++)
+                    s += acc[(size_t)u * n + i];
+                q[i] = s;
+            }
+        }
+        double pq = 0.0, rr2 = 0.0;
+#pragma omp parallel for reduction(+ : pq)
+        for (int i = 0; i < n; i++)
+            pq += p[i] * q[i];
+        double al = pq != 0.0 ? rr / pq : 0.0;
+#pragma omp parallel for reduction(+ : rr2)
+        for (int i = 0; i < n; i++) {
+            x[i] += al * p[i];
+            r[i] -= al * q[i];
+            rr2 += r[i] * r[i];
+        }
+        double be = rr != 0.0 ? rr2 / rr : 0.0;
+        rr = rr2;
+#pragma omp parallel for
+        for (int i = 0; i < n; i++)
+            p[i] = r[i] + be * p[i];
+    }
+    free(x);
+    free(r);
+    free(p);
+    free(q);
+    free(acc);
+    return it;
 }
 
 /* computeStress, src/lpm_basic.c:53-109 (stress tensor only) */

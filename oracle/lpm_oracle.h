@@ -86,6 +86,8 @@ int lo_load_step(lpm_oracle *o, int nbd, const lo_disp_bc *d, int nbf, const lo_
                  double *stats);
 /* Compute the upper CSR pattern (IK, JK 1-based) without values. */
 void lo_csr_pattern(lpm_oracle *o);
+/* CPU-baseline timing: nit threaded CG iterations on the current K/residual. */
+int lo_cg_iterations(lpm_oracle *o, int nit);
 
 /* sizes and raw views (row-major [i][j]) */
 int lo_n(const lpm_oracle *o);

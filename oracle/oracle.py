@@ -58,6 +58,7 @@ def lib():
                   "lo_update_rr", "lo_csr_pattern"):
             getattr(L, f).argtypes = [vp]
         L.lo_fd_stiffness_range.argtypes = [vp, C.c_int, C.c_int]
+        L.lo_cg_iterations.argtypes = [vp, C.c_int]
         L.lo_set_disp_bc.argtypes = [vp, C.c_int, C.POINTER(DispBC)]
         L.lo_set_force_bc.argtypes = [vp, C.c_int, C.POINTER(ForceBC)]
         L.lo_solver_cg.argtypes = [vp, C.c_double, C.c_double]

@@ -102,3 +102,33 @@ def splitmix64_uniform(seed, count):
         z = z ^ (z >> 31)
         out[k] = (z >> 11) * (1.0 / 9007199254740992.0)
     return out
+
+
+def fcc_box(ncell, radius):
+    """Box for createCuboid (lattice 3) holding ncell^3 FCC cells of edge 2*sqrt(2)*radius.
+
+    FCC sites start at -|box diagonal| on all axes (src/initialization.c:359-415);
+    the box is widened by a quarter cell on each side so it captures the sites
+    of exactly ncell cells plus their closing faces whatever the offset."""
+    a = 4 * radius / np.sqrt(2.0)
+    return [-0.25 * a, ncell * a + 0.25 * a] * 3
+
+
+class FCCCase:
+    """FCC single crystal, crystal plasticity, [001] tension (C3 at ncell=80)."""
+
+    def __init__(self, ncell=4, radius=0.1, strain=0.02, steps=100, newton_tol=1e-8,
+                 tau0=50.0, h0=500.0, p=20.0, q=1.0, eta=10.0, maxloop=10, dtime=1.0):
+        self.lattice = 3
+        self.radius = radius
+        self.box = fcc_box(ncell, radius)
+        # Al constants (examples/FCC_Al_R0.3_001_tension.c:200-202)
+        self.C11, self.C12, self.C44 = 107.3e3, 60.8e3, 28.3e3
+        # linear hardening: taus -> infinity makes h = h0 (src/constitutive.c:1125-1126)
+        self.cp = [tau0, 1e30, h0, p, q, eta, maxloop, dtime]
+        self.height = ncell * 4 * radius / np.sqrt(2.0)
+        self.schedule = [strain * self.height / steps] * steps
+        self.newton_tol = newton_tol
+
+    def ce_per_type(self):
+        return np.tile([self.C11, self.C12, self.C44], (NTYPE, 1))

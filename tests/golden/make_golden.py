@@ -79,6 +79,9 @@ def sc_case(out, nsteps, tag="sc10"):
             state_in = snapshot(n, nn)
             with R.quiet():
                 R.lib().calcStiffness3DFiniteDifference(6)
+            # the finite-difference sweep overwrites F (src/constitutive.c:270), which
+            # the load step copies into F_temp for its predictor: put it back
+            R.set_d2("F", state_in["F"])
             K = R.get_d1("K_global", nnz)
             IK = R.get_i1("IK", 3 * n + 1)
             JK = R.get_i1("JK", nnz)
@@ -109,14 +112,73 @@ def sc_case(out, nsteps, tag="sc10"):
     np.savez_compressed(os.path.join(out, f"{tag}_cyclic.npz"), **arrs)
 
 
+def fcc_case(out, nsteps, tag="fcc4"):
+    """FCC crystal plasticity (computeBondForceCPMiehe), [001] tension, 4^3 cells."""
+    case = cases.FCCCase(ncell=4)
+    t0 = time.time()
+    n = R.setup(case.lattice, case.radius, case.box)
+    nn = R.gint("nneighbors")
+    xyz0 = R.get_d2("xyz", n, 3)
+    nb = R.get_i1("nb", n)
+    types = cases.sc_types(xyz0, nb, case.radius)
+    R.set_types(types, cases.NTYPE)
+    R.material(case.ce_per_type(), 1, np.zeros(n), 0.0, 0.0, np.array(case.cp))
+    R.init_state()
+    R.set_cg_tol(1e-20, 0.0)
+    ns = R.gint("nslipSys")
+    arrs = dict(box=np.array(case.box), types=types, xyz=xyz0, cp=np.array(case.cp),
+                schmid=R.get_d2("schmid_tensor", ns, 6),
+                neighbors=R.get_i2("neighbors", n, nn), nsign=R.get_i2("nsign", n, nn),
+                distance_initial=R.get_d2("distance_initial", n, nn),
+                Kn=R.get_d2("Kn", n, nn), Tv=R.get_d2("Tv", n, nn),
+                cp_Cab=R.get_d2("cp_Cab", n, ns * ns))
+    rec = {k: [] for k in ("iters", "nres", "disp_top", "react_top")}
+    top = types == cases.T_TOP
+    for s, stp in enumerate(case.schedule[:nsteps], start=1):
+        with R.quiet():
+            st = R.load_step(cases.sc_bcs(stp), [], case.newton_tol)
+        xyz = R.get_d2("xyz", n, 3)
+        F = R.get_d2("F", n, nn)
+        csz = R.get_d2("csz", n, nn)
+        rec["iters"].append(st[0])
+        rec["nres"].append(st[3])
+        rec["disp_top"].append((xyz[top, 2].sum() - xyz0[top, 2].sum()) / top.sum())
+        rec["react_top"].append(np.sum(-csz[top] * F[top]))
+        if s in (5, nsteps):
+            arrs[f"s{s}_xyz"] = xyz
+            arrs[f"s{s}_F"] = F
+            for c in ("csx", "csy", "csz"):
+                arrs[f"s{s}_{c}"] = R.get_d2(c, n, nn)
+            arrs[f"s{s}_dLp"] = R.get_d3("dLp", n, nn, 1)
+            arrs[f"s{s}_cp_gy"] = R.get_d3("cp_gy", n, ns, 1)
+            arrs[f"s{s}_cp_A_single"] = R.get_d3("cp_A_single", n, ns, 1)
+            arrs[f"s{s}_cp_A"] = R.get_d2("cp_A", n, 3)[:, 1]
+        print(f"{tag} step {s}: iters {int(st[0])} res {st[3]:.3e} t={time.time() - t0:.1f}s", flush=True)
+    for k, v in rec.items():
+        arrs[k] = np.array(v)
+    arrs["schedule"] = np.array(case.schedule[:nsteps])
+    np.savez_compressed(os.path.join(out, f"{tag}_cp.npz"), **arrs)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--fcc-steps", type=int, default=12)
+    ap.add_argument("--only", choices=["sc", "fcc"], default=None)
     ap.add_argument("--out", default=HERE)
     args = ap.parse_args()
     if not R.available():
         sys.exit("oracle/_ref/libref_lpm.so missing: run oracle/build_ref.sh first")
-    sc_case(args.out, args.steps)
+    # the reference keeps all state in process globals: one case per process
+    if args.only == "fcc":
+        fcc_case(args.out, args.fcc_steps)
+    elif args.only == "sc":
+        sc_case(args.out, args.steps)
+    else:
+        import subprocess
+        for which in ("sc", "fcc"):
+            subprocess.check_call([sys.executable, __file__, "--only", which, "--steps", str(args.steps),
+                                   "--fcc-steps", str(args.fcc_steps), "--out", args.out])
 
 
 if __name__ == "__main__":

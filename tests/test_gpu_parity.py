@@ -56,3 +56,93 @@ def test_stiffness_vs_fd(sc10):
     rel = np.linalg.norm(K - Kf) / np.linalg.norm(Kf)
     # forward differences with h = 1e-6 r: truncation ~1e-6, rounding ~1e-9 / 1e-7
     assert rel < 1e-5, rel
+
+
+def _state_from_golden(s, o, g, step):
+    """Load the converged state after `step` into both the GPU specimen and the oracle."""
+    for name, key in (("xyz", "xyz"), ("F", "F"), ("csx", "csx"), ("csy", "csy"), ("csz", "csz"), ("Pex", "Pex")):
+        s.set(name, g[f"s{step}_{key}"])
+        o.set_d(name, g[f"s{step}_{key}"])
+    for slot in ("0", "1"):
+        s.set("dLp" + slot, g[f"s{step}_dLp"])
+        s.set("J2_alpha" + slot, g[f"s{step}_alpha"])
+        s.set("J2_beta" + slot, g[f"s{step}_beta"])
+    for slot in ("0", "1", "2"):
+        o.set_d("dLp" + slot, g[f"s{step}_dLp"])
+        o.set_d("alpha" + slot, g[f"s{step}_alpha"])
+        o.set_d("beta" + slot, g[f"s{step}_beta"])
+
+
+@pytest.mark.parametrize("step", [14, 20])
+def test_j2_force_bit_exact(oracle_mod, gpu_lib, step):
+    """One J2 force evaluation (return map + averaged force + stress + residual)
+    from a plastic state perturbed off equilibrium: GPU == oracle bit for bit."""
+    from conftest import golden
+    g = golden("sc10_cyclic.npz")
+    case = cases.SCCase(n=10)
+    o, types = sc_oracle(oracle_mod, case, threads=2)
+    s, _ = sc_gpu(gpu_lib, case)
+    _state_from_golden(s, o, g, step)
+    rng = np.random.default_rng(step)
+    x = g[f"s{step}_xyz"] + 2e-4 * rng.standard_normal(g[f"s{step}_xyz"].shape)
+    s.set("xyz", x)
+    o.set_d("xyz", x)
+    s.apply_bc(cases.sc_bcs(0.0))
+    from oracle import bc_arrays
+    nd, darr, nf, farr = bc_arrays(cases.sc_bcs(0.0), [])
+    o.L.lo_set_disp_bc(o.h, nd, darr)
+    s.compute_force(gpu_lib.PL_J2)
+    o.force(0)
+    o.update_rr()
+    n, nn = o.n, o.nn
+    assert np.array_equal(s.get("F"), o.d("F", (n, nn)))
+    assert np.array_equal(s.get("Pin"), o.d("Pin", (n, 3)))
+    assert np.array_equal(s.get("dLp0"), o.d("dLp0", (n, nn)))
+    assert np.array_equal(s.get("J2_alpha0"), o.d("alpha0", (n,)))
+    assert np.array_equal(s.get("stress_tensor"), o.d("stress_tensor", (n, 6)))
+    assert np.array_equal(s.get("residual"), o.d("residual", (n, 3)))
+    assert (o.d("alpha2", (n,)) > g[f"s{step}_alpha"]).any()  # the perturbation yields
+
+
+def test_predictor_bit_exact(oracle_mod, gpu_lib):
+    """Elastic incremental predictor (plmode 4) with the same stored unit vectors."""
+    from conftest import golden
+    g = golden("sc10_cyclic.npz")
+    case = cases.SCCase(n=10)
+    o, _ = sc_oracle(oracle_mod, case, threads=2)
+    s, _ = sc_gpu(gpu_lib, case)
+    _state_from_golden(s, o, g, 20)
+    s.begin_step()
+    o.set_d("xyz_temp", o.d("xyz", (o.n, 3)))
+    o.set_d("F_temp", o.d("F", (o.n, o.nn)))
+    s.apply_bc(cases.sc_bcs(case.schedule[20]))
+    from oracle import bc_arrays
+    nd, darr, nf, farr = bc_arrays(cases.sc_bcs(case.schedule[20]), [])
+    o.L.lo_set_disp_bc(o.h, nd, darr)
+    s.compute_force(gpu_lib.PL_PREDICTOR)
+    o.force(4)
+    o.update_rr()
+    n, nn = o.n, o.nn
+    assert np.array_equal(s.get("F"), o.d("F", (n, nn)))
+    assert np.array_equal(s.get("Pin"), o.d("Pin", (n, 3)))
+    assert np.array_equal(s.get("residual"), o.d("residual", (n, 3)))
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_load_steps_match_oracle(oracle_mod, gpu_lib, precision):
+    """C1 cyclic case, steps 1-15 (elastic ramp and first plastic steps), both
+    sides converged tightly: displacements within 1e-8 of the oracle's."""
+    case = cases.SCCase(n=10, newton_tol=1e-10)
+    o, types = sc_oracle(oracle_mod, case, threads=4)
+    s, _ = sc_gpu(gpu_lib, case, precision=precision, newton_maxiter=300, cg_rtol=1e-10)
+    n = o.n
+    x0 = o.d("xyz_initial", (n, 3))
+    for k, stp in enumerate(case.schedule[:15]):
+        st = s.load_step(cases.sc_bcs(stp))
+        so = o.load_step(cases.sc_bcs(stp), [], 1e-10, 300, 1e-20, 0.0)
+        assert st["status"] == 0, st
+        du_g = s.get("xyz") - x0
+        du_o = o.d("xyz", (n, 3)) - x0
+        err = np.abs(du_g - du_o).max() / np.abs(du_o).max()
+        assert err < 1e-8, (k + 1, err, st, so)
+    assert np.abs(s.get("J2_alpha") - o.d("alpha1", (n,))).max() < 1e-10
