@@ -237,24 +237,13 @@ def run_e2e(args, case):
         import lpm_host
         h = lpm_host.HostDriver()
         n = h.setup(case.lattice, case.radius, case.box)
-        xyz = h.get("xyz")
-        nbv = np.zeros(n, dtype=np.int32)
-        # particle types exactly as the GPU specimen (full neighbour lists -> type 3)
+        # particle types as for the GPU specimen (the legacy ABI selects BCs by
+        # type and takes Ce per type, so this leg runs with uniform E)
         s = G.Specimen(0)
         s.setup_lattice(case.lattice, case.radius, case.box)
-        nbv = s.get("nb")
+        types = cases.sc_types(h.get("xyz"), s.get("nb"), case.radius)
         s.close()
-        types = cases.sc_types(xyz, nbv, case.radius)
-        # one type per particle class; materials per particle need distinct Ce rows:
-        # use 6 types for BCs and give E noise through one Ce row per particle
-        u = cases.splitmix64_uniform(case.seed, n)
-        sc = 1.0 + case.e_noise * (2.0 * u - 1.0)
-        c11, c12, c44 = cases.iso_cubic(case.E, case.nu)
-        ce = np.stack([c11 * sc, c12 * sc, c44 * sc], 1)
-        # types carry both: particle i gets its own Ce row (ntype = n + NTYPE offset)
-        # BCs select by type, so keep BC types and put materials in per-type rows
-        tb = types.astype(np.int64)
-        h.set_types(tb, cases.NTYPE)
+        h.set_types(types, cases.NTYPE)
         h.set_material(np.tile(cases.iso_cubic(case.E, case.nu), (cases.NTYPE, 1)), 0, case.sigmay, 0.0, case.H)
         h.set_solver(precision=G.PREC_MIXED, cg_rtol=1e-10, cg_maxiter=200000)
         h.init()

@@ -73,7 +73,7 @@ typedef struct {
     int refine_maxiter; /* mixed: cap on FP64 reliable updates per solve */
     int check_every;    /* PCG iterations between host convergence checks (graph chunk) */
     int use_graphs;     /* capture PCG chunks as CUDA graphs */
-    int spmv_variant;   /* 0 = default; others select alternative SpMV kernels (tuning) */
+    int mixed_vectors;  /* mixed: 32 = FP32 CG vectors, 64 = FP64 CG vectors (FP32 stiffness and products) */
 } lpm_solver_opts;
 
 typedef struct {

@@ -101,10 +101,46 @@ struct SpmvArgs {
     CgScalars *sc;
 };
 
-// y = K x (FP32).  DOT: accumulate x.y in FP64 and set alpha = rz / (x.y).
-template <bool MASK, bool DOT>
-__global__ void __launch_bounds__(VTPB) k_spmv_f(SpmvArgs a, const float *__restrict__ val,
-                                                 const float4 *__restrict__ x, float4 *__restrict__ y)
+// 4 consecutive stiffness values of one component: one 128-bit (FP32) or
+// 256-bit (FP64) streaming load.
+__device__ __forceinline__ float4 load_vals4(const float *p) { return __ldcs(reinterpret_cast<const float4 *>(p)); }
+__device__ __forceinline__ double4_32a load_vals4(const double *p)
+{
+    return *reinterpret_cast<const double4_32a *>(p);
+}
+template <typename A>
+__device__ __forceinline__ void xyz_of(const float4 &v, A &x, A &y, A &z)
+{
+    x = (A)v.x;
+    y = (A)v.y;
+    z = (A)v.z;
+}
+template <typename A>
+__device__ __forceinline__ void xyz_of(const dvec4 &v, A &x, A &y, A &z)
+{
+    x = (A)v.x;
+    y = (A)v.y;
+    z = (A)v.z;
+}
+// read-only gathers of one particle's vector entry
+__device__ __forceinline__ float4 ldx(const float4 *p) { return __ldg(p); }
+__device__ __forceinline__ dvec4 ldx(const dvec4 *p)
+{
+    const double2 a = __ldg(reinterpret_cast<const double2 *>(p));
+    const double2 b = __ldg(reinterpret_cast<const double2 *>(p) + 1);
+    return make_dvec4(a.x, a.y, b.x, b.y);
+}
+__device__ __forceinline__ void store3(float4 *p, float a, float b, float c) { *p = make_float4(a, b, c, 0.f); }
+__device__ __forceinline__ void store3(dvec4 *p, double a, double b, double c) { *p = make_dvec4(a, b, c, 0.0); }
+
+// y = K x with a half-warp per block row; each lane takes four consecutive
+// blocks of every 64-block chunk.  V: stiffness value type (products and
+// sums in V), X: vector element type (float4 or dvec4).  MASK zeroes the
+// constrained DOFs of y; DOT accumulates x.y in FP64 and sets
+// alpha = rz / (x.y) for the CG.
+template <typename V, typename X, bool MASK, bool DOT>
+__global__ void __launch_bounds__(VTPB) k_spmv(SpmvArgs a, const V *__restrict__ val, const X *__restrict__ x,
+                                               X *__restrict__ y)
 {
     if (DOT && a.sc->done)
         return;
@@ -116,27 +152,31 @@ __global__ void __launch_bounds__(VTPB) k_spmv_f(SpmvArgs a, const float *__rest
     for (int row = gw; row < a.n; row += nhw) {
         const long long off = a.rowoff[row];
         const int np = a.npad[row];
-        const float *vr = val + 9 * off;
-        float y0 = 0.f, y1 = 0.f, y2 = 0.f;
+        const V *vr = val + 9 * off;
+        V y0 = 0, y1 = 0, y2 = 0;
         for (int b0 = 4 * hl; b0 < np; b0 += 64) {
             const int4 c4 = __ldg(reinterpret_cast<const int4 *>(a.cols + off + b0));
-            float4 v[9];
+            decltype(load_vals4(vr)) v[9];
 #pragma unroll
             for (int k = 0; k < 9; k++)
-                v[k] = __ldcs(reinterpret_cast<const float4 *>(vr + (size_t)k * np + b0));
-            const float4 xa = __ldg(x + c4.x), xb = __ldg(x + c4.y), xc = __ldg(x + c4.z), xd = __ldg(x + c4.w);
-            y0 += v[0].x * xa.x + v[1].x * xa.y + v[2].x * xa.z;
-            y1 += v[3].x * xa.x + v[4].x * xa.y + v[5].x * xa.z;
-            y2 += v[6].x * xa.x + v[7].x * xa.y + v[8].x * xa.z;
-            y0 += v[0].y * xb.x + v[1].y * xb.y + v[2].y * xb.z;
-            y1 += v[3].y * xb.x + v[4].y * xb.y + v[5].y * xb.z;
-            y2 += v[6].y * xb.x + v[7].y * xb.y + v[8].y * xb.z;
-            y0 += v[0].z * xc.x + v[1].z * xc.y + v[2].z * xc.z;
-            y1 += v[3].z * xc.x + v[4].z * xc.y + v[5].z * xc.z;
-            y2 += v[6].z * xc.x + v[7].z * xc.y + v[8].z * xc.z;
-            y0 += v[0].w * xd.x + v[1].w * xd.y + v[2].w * xd.z;
-            y1 += v[3].w * xd.x + v[4].w * xd.y + v[5].w * xd.z;
-            y2 += v[6].w * xd.x + v[7].w * xd.y + v[8].w * xd.z;
+                v[k] = load_vals4(vr + (size_t)k * np + b0);
+            V ax, ay, az, bx, by, bz, cx, cy, cz, dx, dy, dz;
+            xyz_of<V>(ldx(x + c4.x), ax, ay, az);
+            xyz_of<V>(ldx(x + c4.y), bx, by, bz);
+            xyz_of<V>(ldx(x + c4.z), cx, cy, cz);
+            xyz_of<V>(ldx(x + c4.w), dx, dy, dz);
+            y0 += v[0].x * ax + v[1].x * ay + v[2].x * az;
+            y1 += v[3].x * ax + v[4].x * ay + v[5].x * az;
+            y2 += v[6].x * ax + v[7].x * ay + v[8].x * az;
+            y0 += v[0].y * bx + v[1].y * by + v[2].y * bz;
+            y1 += v[3].y * bx + v[4].y * by + v[5].y * bz;
+            y2 += v[6].y * bx + v[7].y * by + v[8].y * bz;
+            y0 += v[0].z * cx + v[1].z * cy + v[2].z * cz;
+            y1 += v[3].z * cx + v[4].z * cy + v[5].z * cz;
+            y2 += v[6].z * cx + v[7].z * cy + v[8].z * cz;
+            y0 += v[0].w * dx + v[1].w * dy + v[2].w * dz;
+            y1 += v[3].w * dx + v[4].w * dy + v[5].w * dz;
+            y2 += v[6].w * dx + v[7].w * dy + v[8].w * dz;
         }
 #pragma unroll
         for (int o = 8; o > 0; o >>= 1) {
@@ -145,67 +185,17 @@ __global__ void __launch_bounds__(VTPB) k_spmv_f(SpmvArgs a, const float *__rest
             y2 += __shfl_xor_sync(hmask, y2, o);
         }
         if (hl == 0) {
-            float4 out = make_float4(y0, y1, y2, 0.f);
-            if (MASK)
-                out = mask4(out, a.mask[row]);
-            y[row] = out;
-            if (DOT) {
-                const float4 pv = x[row];
-                dot += (double)pv.x * out.x + (double)pv.y * out.y + (double)pv.z * out.z;
+            if (MASK) {
+                const uint8_t m = a.mask[row];
+                y0 = (m & 1) ? y0 : V(0);
+                y1 = (m & 2) ? y1 : V(0);
+                y2 = (m & 4) ? y2 : V(0);
             }
-        }
-    }
-    if (DOT) {
-        double v[1] = {dot};
-        CgScalars *sc = a.sc;
-        grid_reduce<1>(v, a.partials, a.counter, [sc](const double *t) {
-            sc->pq = t[0];
-            sc->alpha = (t[0] != 0.0) ? sc->rz / t[0] : 0.0;
-        });
-    }
-}
-
-// y = K x (FP64), a warp per row, two blocks per lane.
-template <bool MASK, bool DOT>
-__global__ void __launch_bounds__(VTPB) k_spmv_d(SpmvArgs a, const double *__restrict__ val,
-                                                 const dvec4 *__restrict__ x, dvec4 *__restrict__ y)
-{
-    if (DOT && a.sc->done)
-        return;
-    const int lane = threadIdx.x & 31;
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
-    double dot = 0.0;
-    for (int row = gw; row < a.n; row += nw) {
-        const long long off = a.rowoff[row];
-        const int np = a.npad[row];
-        const double *vr = val + 9 * off;
-        double y0 = 0.0, y1 = 0.0, y2 = 0.0;
-        for (int b0 = 2 * lane; b0 < np; b0 += 64) {
-            const int2 c2 = __ldg(reinterpret_cast<const int2 *>(a.cols + off + b0));
-            double2 v[9];
-#pragma unroll
-            for (int k = 0; k < 9; k++)
-                v[k] = __ldcs(reinterpret_cast<const double2 *>(vr + (size_t)k * np + b0));
-            const dvec4 xa = x[c2.x], xb = x[c2.y];
-            y0 += v[0].x * xa.x + v[1].x * xa.y + v[2].x * xa.z;
-            y1 += v[3].x * xa.x + v[4].x * xa.y + v[5].x * xa.z;
-            y2 += v[6].x * xa.x + v[7].x * xa.y + v[8].x * xa.z;
-            y0 += v[0].y * xb.x + v[1].y * xb.y + v[2].y * xb.z;
-            y1 += v[3].y * xb.x + v[4].y * xb.y + v[5].y * xb.z;
-            y2 += v[6].y * xb.x + v[7].y * xb.y + v[8].y * xb.z;
-        }
-        y0 = warp_sum(y0);
-        y1 = warp_sum(y1);
-        y2 = warp_sum(y2);
-        if (lane == 0) {
-            dvec4 out = make_dvec4(y0, y1, y2, 0.0);
-            if (MASK)
-                out = mask4(out, a.mask[row]);
-            y[row] = out;
+            store3(y + row, y0, y1, y2);
             if (DOT) {
-                const dvec4 pv = x[row];
-                dot += pv.x * out.x + pv.y * out.y + pv.z * out.z;
+                double px, py, pz;
+                xyz_of<double>(x[row], px, py, pz);
+                dot += px * (double)y0 + py * (double)y1 + pz * (double)y2;
             }
         }
     }
@@ -224,7 +214,8 @@ __global__ void __launch_bounds__(VTPB) k_spmv_d(SpmvArgs a, const double *__res
 __global__ void __launch_bounds__(VTPB) k_refine_res(SpmvArgs a, const float *__restrict__ val,
                                                      const dvec4 *__restrict__ x,
                                                      const dvec4 *__restrict__ bvec,
-                                                     dvec4 *__restrict__ r, double *norms, int slot)
+                                                     dvec4 *__restrict__ r, double *norms, int slot,
+                                                     double bscale)
 {
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -254,7 +245,7 @@ __global__ void __launch_bounds__(VTPB) k_refine_res(SpmvArgs a, const float *__
         y2 = warp_sum(y2);
         if (lane == 0) {
             const dvec4 bb = bvec[row];
-            dvec4 out = make_dvec4(bb.x - y0, bb.y - y1, bb.z - y2, 0.0);
+            dvec4 out = make_dvec4(bb.x * bscale - y0, bb.y * bscale - y1, bb.z * bscale - y2, 0.0);
             out = mask4(out, a.mask[row]);
             r[row] = out;
             acc += out.x * out.x + out.y * out.y + out.z * out.z;
@@ -426,6 +417,30 @@ __global__ void __launch_bounds__(VTPB) k_cg_p(int n, CgScalars *sc, const V4 *z
     }
 }
 
+// Reliable update of the FP64-vector variant: r = true residual (already in
+// the scaled units of the iteration), z = P^-1 r; p is kept.
+__global__ void __launch_bounds__(VTPB) k_reliable_d(VecArgs a, const dvec4 *rtrue, const double *P, dvec4 *r,
+                                                     dvec4 *z)
+{
+    double v[2] = {0.0, 0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
+        const dvec4 rv = mask4(rtrue[i], a.mask[i]);
+        const dvec4 zv = apply_pinv<double, dvec4>(P, a.n, i, rv);
+        r[i] = rv;
+        z[i] = zv;
+        v[0] += rv.x * zv.x + rv.y * zv.y + rv.z * zv.z;
+        v[1] += rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
+    }
+    CgScalars *sc = a.sc;
+    grid_reduce<2>(v, a.partials, a.counter, [sc](const double *t) {
+        sc->rz = t[0];
+        sc->rr = t[1];
+        sc->rr_max = t[1];
+        sc->done = !(t[1] == t[1]) ? 3 : 0;
+        sc->upd_req = 0;
+    });
+}
+
 // x64 += x32 / scale, x32 = 0
 __global__ void k_axpy_refine(int n, dvec4 *x, float4 *d, double inv_scale)
 {
@@ -471,7 +486,7 @@ int red_grid(const Ctx &c)
 // external event nodes, so the last SpMV of each graph launch is timed.
 static void record_timing(Ctx &c, cudaEvent_t ev)
 {
-    if (!c.time_spmv)
+    if (!c.time_spmv || !c.time_this)
         return;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     cudaStreamIsCapturing(c.stream, &cs);
@@ -506,37 +521,62 @@ static VecArgs vec_args(Ctx &c)
     return a;
 }
 
-void launch_spmv_f(Ctx &c, const float4 *x, float4 *y, bool masked, bool dot)
+template <typename V, typename X>
+static void spmv_launch(Ctx &c, const V *val, const X *x, X *y, bool masked, bool dot)
 {
     SpmvArgs a = spmv_args(c);
     const int g = red_grid(c);
     record_timing(c, c.ev_a);
     if (masked && dot)
-        k_spmv_f<true, true><<<g, VTPB, 0, c.stream>>>(a, c.Kf, x, y);
+        k_spmv<V, X, true, true><<<g, VTPB, 0, c.stream>>>(a, val, x, y);
     else if (masked)
-        k_spmv_f<true, false><<<g, VTPB, 0, c.stream>>>(a, c.Kf, x, y);
+        k_spmv<V, X, true, false><<<g, VTPB, 0, c.stream>>>(a, val, x, y);
     else
-        k_spmv_f<false, false><<<g, VTPB, 0, c.stream>>>(a, c.Kf, x, y);
+        k_spmv<V, X, false, false><<<g, VTPB, 0, c.stream>>>(a, val, x, y);
     record_timing(c, c.ev_b);
+}
+
+void launch_spmv_f(Ctx &c, const float4 *x, float4 *y, bool masked, bool dot)
+{
+    spmv_launch<float, float4>(c, c.Kf, x, y, masked, dot);
 }
 
 void launch_spmv_d(Ctx &c, const dvec4 *x, dvec4 *y, bool masked, bool dot)
 {
-    SpmvArgs a = spmv_args(c);
-    const int g = red_grid(c);
-    record_timing(c, c.ev_a);
-    if (masked && dot)
-        k_spmv_d<true, true><<<g, VTPB, 0, c.stream>>>(a, c.Kd, x, y);
-    else if (masked)
-        k_spmv_d<true, false><<<g, VTPB, 0, c.stream>>>(a, c.Kd, x, y);
-    else
-        k_spmv_d<false, false><<<g, VTPB, 0, c.stream>>>(a, c.Kd, x, y);
-    record_timing(c, c.ev_b);
+    spmv_launch<double, dvec4>(c, c.Kd, x, y, masked, dot);
 }
 
-void launch_refine_residual(Ctx &c, const dvec4 *x, const dvec4 *b, dvec4 *r)
+void launch_spmv_fx(Ctx &c, const dvec4 *x, dvec4 *y, bool masked, bool dot)
 {
-    k_refine_res<<<red_grid(c), VTPB, 0, c.stream>>>(spmv_args(c), c.Kf, x, b, r, c.norms, 2);
+    spmv_launch<float, dvec4>(c, c.Kf, x, y, masked, dot);
+}
+
+void launch_refine_residual(Ctx &c, const dvec4 *x, const dvec4 *b, dvec4 *r, double bscale)
+{
+    k_refine_res<<<red_grid(c), VTPB, 0, c.stream>>>(spmv_args(c), c.Kf, x, b, r, c.norms, 2, bscale);
+}
+
+// mixed precision with FP64 CG vectors: FP32 stiffness, FP32 products and row
+// sums, FP64 search directions, residuals and dot products
+void launch_cg_init_fx(Ctx &c, const dvec4 *b, double scale, double delta2)
+{
+    k_cg_init<double, dvec4><<<red_grid(c), VTPB, 0, c.stream>>>(
+        vec_args(c), b, scale, c.Pinv_d, c.x_d, c.r_d, c.z_d, c.p_d, c.opts.cg_rtol, c.opts.cg_maxiter, delta2);
+}
+
+void launch_cg_iter_fx(Ctx &c)
+{
+    launch_spmv_fx(c, c.p_d, c.q_d, true, true);
+    const int g = red_grid(c);
+    k_cg_update<double, dvec4><<<g, VTPB, 0, c.stream>>>(vec_args(c), c.Pinv_d, c.x_d, c.r_d, c.z_d,
+                                                           c.p_d, c.q_d);
+    k_cg_p<double, dvec4><<<g, VTPB, 0, c.stream>>>(c.n, c.sc, c.z_d, c.p_d, c.counter);
+}
+
+// reliable update of the FP64-vector variant: r = (true residual), z = P^-1 r
+void launch_reliable_d(Ctx &c, const dvec4 *rtrue)
+{
+    k_reliable_d<<<red_grid(c), VTPB, 0, c.stream>>>(vec_args(c), rtrue, c.Pinv_d, c.r_d, c.z_d);
 }
 
 void launch_cg_init_d(Ctx &c, const dvec4 *b, double scale)

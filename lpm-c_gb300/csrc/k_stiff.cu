@@ -183,9 +183,9 @@ __global__ void __launch_bounds__(STPB) k_assemble(AsmArgs a, V *val)
 // Block-Jacobi: inverse of each 3x3 diagonal block with the constrained
 // DOFs' rows and columns replaced by the identity (setDispBC_stiffnessUpdate3D,
 // src/boundary.c:159-281, decouples them; their solution is zero).
-template <typename V>
+template <typename V, typename P>
 __global__ void k_jacobi(int n, const long long *rowoff, const int *npad, const int *cols,
-                         const int8_t *nconn, const V *val, const uint8_t *mask, V *Pinv)
+                         const int8_t *nconn, const V *val, const uint8_t *mask, P *Pinv)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
@@ -215,7 +215,7 @@ __global__ void k_jacobi(int n, const long long *rowoff, const int *npad, const 
     const double out[9] = {c00 * inv, c01 * inv, c02 * inv, c01 * inv, c11 * inv, c12 * inv,
                            c02 * inv, c12 * inv, c22 * inv};
     for (int k = 0; k < 9; k++)
-        Pinv[(size_t)k * n + i] = (V)out[k];
+        Pinv[(size_t)k * n + i] = (P)out[k];
 }
 
 void launch_tangent_geometry(Ctx &c)
@@ -258,12 +258,17 @@ void launch_assemble(Ctx &c, bool fp32)
 void launch_block_jacobi(Ctx &c, bool fp32)
 {
     const int g = (c.n + STPB - 1) / STPB;
-    if (fp32)
-        k_jacobi<float><<<g, STPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.nconn_d, c.Kf, c.mask,
-                                                  c.Pinv_f);
-    else
-        k_jacobi<double><<<g, STPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.nconn_d, c.Kd, c.mask,
-                                                   c.Pinv_d);
+    if (fp32) {
+        // FP32 inverse for FP32 CG vectors, FP64 inverse of the same FP32 blocks
+        // for the FP64-vector variant
+        k_jacobi<float, float><<<g, STPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.nconn_d, c.Kf,
+                                                         c.mask, c.Pinv_f);
+        k_jacobi<float, double><<<g, STPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.nconn_d, c.Kf,
+                                                          c.mask, c.Pinv_d);
+    } else {
+        k_jacobi<double, double><<<g, STPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.nconn_d, c.Kd,
+                                                           c.mask, c.Pinv_d);
+    }
 }
 
 }  // namespace lpm

@@ -308,7 +308,7 @@ void lpm_default_solver_opts(lpm_solver_opts *o)
     o->refine_maxiter = 200;
     o->check_every = 16;
     o->use_graphs = 1;
-    o->spmv_variant = 0;
+    o->mixed_vectors = 32;
 }
 
 int lpm_create(lpm_ctx **out, int device)
@@ -565,34 +565,42 @@ int lpm_init_state(lpm_ctx *ctx)
 
 namespace lpm {
 
+enum PcgMode { PCG_FP64 = 0, PCG_FP32 = 1, PCG_FP32_K_FP64_VEC = 2 };
+
+// One chunk of PCG iterations; the first SpMV of the chunk (which always does
+// work: a chunk is only launched while the solve is running) carries the
+// timing events when sampling is on.
+static void issue_chunk(Ctx &c, int mode, int chunk)
+{
+    for (int k = 0; k < chunk; k++) {
+        c.time_this = (k == 0);
+        if (mode == PCG_FP64)
+            launch_cg_iter_d(c);
+        else if (mode == PCG_FP32)
+            launch_cg_iter_f(c);
+        else
+            launch_cg_iter_fx(c);
+    }
+    c.time_this = false;
+}
+
 // Run PCG iterations until the device marks the solve done; the host checks
 // every opts.check_every iterations (one CUDA graph per chunk when enabled).
-static int run_pcg(Ctx &c, bool fp32, int &iters, int &status)
+static int run_pcg(Ctx &c, int mode, int &iters, int &status)
 {
     const int chunk = c.opts.check_every;
-    cudaGraphExec_t &ge = fp32 ? c.graph_fp32 : c.graph_fp64;
+    cudaGraphExec_t &ge = mode == PCG_FP64 ? c.graph_fp64 : c.graph_fp32;
     bool use_graph = c.opts.use_graphs != 0;
-    if (use_graph && ge && c.graph_timed != c.time_spmv) {
-        cudaGraphExecDestroy(c.graph_fp64 ? c.graph_fp64 : c.graph_fp32);
-        if (c.graph_fp64 && c.graph_fp32)
-            cudaGraphExecDestroy(c.graph_fp32);
-        c.graph_fp64 = c.graph_fp32 = nullptr;
+    if (ge && (c.graph_timed != c.time_spmv || c.graph_chunk != chunk || c.graph_mode != mode)) {
+        cudaGraphExecDestroy(ge);
+        ge = nullptr;
     }
-    if (use_graph && (!ge || c.graph_chunk != chunk)) {
-        if (ge) {
-            cudaGraphExecDestroy(ge);
-            ge = nullptr;
-        }
+    if (use_graph && !ge) {
         cudaGraph_t g;
         if (cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
             use_graph = false;
         } else {
-            for (int k = 0; k < chunk; k++) {
-                if (fp32)
-                    launch_cg_iter_f(c);
-                else
-                    launch_cg_iter_d(c);
-            }
+            issue_chunk(c, mode, chunk);
             if (cudaStreamEndCapture(c.stream, &g) != cudaSuccess) {
                 use_graph = false;
             } else {
@@ -603,6 +611,7 @@ static int run_pcg(Ctx &c, bool fp32, int &iters, int &status)
                 cudaGraphDestroy(g);
                 c.graph_chunk = chunk;
                 c.graph_timed = c.time_spmv;
+                c.graph_mode = mode;
             }
         }
         cudaGetLastError();
@@ -611,12 +620,7 @@ static int run_pcg(Ctx &c, bool fp32, int &iters, int &status)
         if (use_graph) {
             LPM_CUDA(cudaGraphLaunch(ge, c.stream));
         } else {
-            for (int k = 0; k < chunk; k++) {
-                if (fp32)
-                    launch_cg_iter_f(c);
-                else
-                    launch_cg_iter_d(c);
-            }
+            issue_chunk(c, mode, chunk);
         }
         LPM_CUDA(cudaMemcpyAsync(c.sc_host, c.sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, c.stream));
         if (c.time_spmv) {
@@ -667,10 +671,41 @@ static int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
         return LPM_OK;
     }
     const double scale = 1.0 / bn;
+    const double delta = c.opts.inner_rtol;
+    if (c.opts.precision == LPM_PREC_MIXED && c.opts.mixed_vectors == 64) {
+        // FP32 stiffness and products, FP64 vectors (x in units of |b|);
+        // reliable updates replace r by s b - K32 x computed with FP64 sums
+        launch_cg_init_fx(c, b, scale, delta * delta);
+        int sweeps = 0, it = 0, done = 0;
+        double rel = 1.0;
+        for (;;) {
+            if ((rc = run_pcg(c, PCG_FP32_K_FP64_VEC, it, done)))
+                return rc;
+            launch_refine_residual(c, c.x_d, b, c.q_d, scale);
+            LPM_CUDA(cudaMemcpyAsync(c.norms_host, c.norms, 4 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+            if ((rc = sync(c)))
+                return rc;
+            rel = std::sqrt(c.norms_host[2]);
+            sweeps++;
+            if (rel <= c.opts.cg_rtol || done == 2 || done == 3 || !std::isfinite(rel) ||
+                sweeps >= c.opts.refine_maxiter)
+                break;
+            launch_reliable_d(c, c.q_d);
+        }
+        if (st) {
+            st->cg_iters += it;
+            st->spmv_calls += it + sweeps;
+            st->refine_iters += sweeps;
+            if (rel > c.opts.cg_rtol)
+                st->status |= std::isfinite(rel) ? LPM_STATUS_CG_MAXIT : LPM_STATUS_NAN;
+        }
+        launch_scale_copy(c, c.du, c.x_d, bn);
+        return LPM_OK;
+    }
     if (c.opts.precision == LPM_PREC_FP64) {
         launch_cg_init_d(c, b, scale);
         int it = 0, done = 0;
-        if ((rc = run_pcg(c, false, it, done)))
+        if ((rc = run_pcg(c, PCG_FP64, it, done)))
             return rc;
         if (st) {
             st->cg_iters += it;
@@ -684,15 +719,14 @@ static int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
         return LPM_OK;
     }
     LPM_CUDA(cudaMemsetAsync(c.x_d, 0, sizeof(dvec4) * c.n, c.stream));
-    const double delta = c.opts.inner_rtol;
     launch_cg_init_f(c, b, scale, c.opts.cg_rtol, delta * delta);
     int sweeps = 0, it = 0, done = 0;
     double rn = bn;
     for (;;) {
-        if ((rc = run_pcg(c, true, it, done)))
+        if ((rc = run_pcg(c, PCG_FP32, it, done)))
             return rc;
         launch_axpy_refine(c, scale);
-        launch_refine_residual(c, c.x_d, b, c.r_d);
+        launch_refine_residual(c, c.x_d, b, c.r_d, 1.0);
         LPM_CUDA(cudaMemcpyAsync(c.norms_host, c.norms, 4 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
         if ((rc = sync(c)))
             return rc;

@@ -155,8 +155,9 @@ struct Ctx {
     bool time_spmv = false;
     // CUDA graphs of PCG chunks
     cudaGraphExec_t graph_fp64 = nullptr, graph_fp32 = nullptr;
-    int graph_chunk = 0;
+    int graph_chunk = 0, graph_mode = -1;
     bool graph_timed = false;
+    bool time_this = false;  // the next SpMV launch carries the timing events
     ~Ctx();
 };
 
@@ -180,7 +181,11 @@ void launch_block_jacobi(Ctx &c, bool fp32);
 // solver (k_solve.cu)
 void launch_spmv_d(Ctx &c, const dvec4 *x, dvec4 *y, bool masked, bool dot_pq);
 void launch_spmv_f(Ctx &c, const float4 *x, float4 *y, bool masked, bool dot_pq);
-void launch_refine_residual(Ctx &c, const dvec4 *x, const dvec4 *b, dvec4 *r);  // r = b - K32 x (FP64)
+void launch_refine_residual(Ctx &c, const dvec4 *x, const dvec4 *b, dvec4 *r, double bscale);  // r = s b - K32 x (FP64)
+void launch_spmv_fx(Ctx &c, const dvec4 *x, dvec4 *y, bool masked, bool dot);
+void launch_cg_init_fx(Ctx &c, const dvec4 *b, double scale, double delta2);
+void launch_cg_iter_fx(Ctx &c);
+void launch_reliable_d(Ctx &c, const dvec4 *rtrue);
 void launch_cg_init_d(Ctx &c, const dvec4 *b, double scale);
 void launch_cg_init_f(Ctx &c, const dvec4 *r64, double scale, double rtol, double delta2);
 void launch_reliable(Ctx &c, const dvec4 *r64, double scale);
