@@ -175,6 +175,7 @@ def run_ours(args):
     value = world * K / (mixed["ms"] / 1e3)
     hbm, peak_src = peaks()
     achieved = mixed["spmv_bytes"] / (mixed["spmv_ms"] * 1e-3) / 1e9 if mixed["spmv_ms"] > 0 else None
+    traffic = spmv_traffic(mixed["spmv_bytes"])
     err = None
     fp64_rate = None
     if "fp64" in results:
@@ -203,7 +204,7 @@ def run_ours(args):
                    "l2": "SpMV stream of 2.4 GB per call > 129 MB L2 (no flush needed)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": (achieved / hbm) if achieved else None, "traffic": None,
+                     "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
                      "kernel": "k_spmv_f (FP32 block-CSR SpMV)", "peak_source": peak_src,
                      "spmv_launches_sampled": mixed["spmv_cnt"]},
         "clocks": mixed["clocks"],
@@ -267,6 +268,19 @@ def run_e2e(args, case):
 
 
 COUNTS_FILE = os.path.join(ROOT, "profiles", "iteration_counts_sc100.json")
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "k_spmv_f_traffic.json")
+
+
+def spmv_traffic(alg_bytes):
+    """DRAM bytes (read + write) per SpMV launch: the ncu capture of a smaller
+    case (dram__bytes_read.sum + dram__bytes_write.sum) scaled to this launch
+    by its algorithmic bytes, which grow with the block count."""
+    try:
+        with open(TRAFFIC_FILE) as f:
+            d = json.load(f)
+        return alg_bytes * d["traffic_over_algorithmic"]
+    except Exception:
+        return None
 
 
 def step_counts(size, W, K, stats=None):

@@ -68,6 +68,7 @@ void build_neighbors(HostSetup &h);
 void build_afem(HostSetup &h);
 void build_bond_tables(HostSetup &h);
 void build_block_pattern(HostSetup &h);
+void merge_setups(HostSetup &dst, const std::vector<HostSetup> &parts, std::vector<int> &offsets);
 void kntv_per_particle(int lattice, double radius, const double *c11, const double *c12,
                        const double *c44, int n, double *knt);
 

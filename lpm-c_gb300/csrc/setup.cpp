@@ -289,6 +289,60 @@ void build_block_pattern(HostSetup &h)
     }
 }
 
+// Concatenate independently built specimens into one setup: particle,
+// bond and block indices of specimen s are shifted by its particle offset,
+// so no bond or stiffness block couples two specimens (a block-diagonal
+// system) and each specimen's arrays equal those of a single-specimen setup.
+void merge_setups(HostSetup &dst, const std::vector<HostSetup> &parts, std::vector<int> &offsets)
+{
+    dst = HostSetup();
+    const HostSetup &f = parts.front();
+    dst.lattice = f.lattice;
+    dst.radius = f.radius;
+    dst.vol = f.vol;
+    dst.cut1 = f.cut1;
+    dst.cut2 = f.cut2;
+    dst.nn1 = f.nn1;
+    dst.nn2 = f.nn2;
+    offsets.assign(parts.size() + 1, 0);
+    for (size_t s = 0; s < parts.size(); s++)
+        offsets[s + 1] = offsets[s] + parts[s].n;
+    const int n = offsets.back();
+    dst.n = n;
+    dst.kp0.assign(n + 1, 0);
+    dst.kp1.assign(n + 1, 0);
+    dst.rowoff.assign(n + 1, 0);
+    long long kbase = 0, rbase = 0;
+    for (size_t s = 0; s < parts.size(); s++) {
+        const HostSetup &p = parts[s];
+        const int o = offsets[s];
+        dst.xyz.insert(dst.xyz.end(), p.xyz.begin(), p.xyz.end());
+        for (int v : p.nbr)
+            dst.nbr.push_back(v >= 0 ? v + o : v);
+        dst.shell.insert(dst.shell.end(), p.shell.begin(), p.shell.end());
+        dst.nb.insert(dst.nb.end(), p.nb.begin(), p.nb.end());
+        dst.rev.insert(dst.rev.end(), p.rev.begin(), p.rev.end());
+        dst.L0.insert(dst.L0.end(), p.L0.begin(), p.L0.end());
+        dst.cs0.insert(dst.cs0.end(), p.cs0.begin(), p.cs0.end());
+        dst.oppv.insert(dst.oppv.end(), p.oppv.begin(), p.oppv.end());
+        for (int v : p.conn)
+            dst.conn.push_back(v >= 0 ? v + o : v);
+        dst.nconn.insert(dst.nconn.end(), p.nconn.begin(), p.nconn.end());
+        dst.npad.insert(dst.npad.end(), p.npad.begin(), p.npad.end());
+        for (int v : p.cols)
+            dst.cols.push_back(v + o);
+        for (int i = 0; i < p.n; i++) {
+            dst.kp0[o + i] = p.kp0[i];
+            dst.kp1[o + i] = (int)(p.kp1[i] + kbase);
+            dst.rowoff[o + i] = p.rowoff[i] + rbase;
+        }
+        kbase += p.kp1[p.n];
+        rbase += p.rowoff[p.n];
+    }
+    dst.kp1[n] = (int)kbase;
+    dst.rowoff[n] = rbase;
+}
+
 // calcKnTv's KnTve = radius * mapping * [C11, C12, C44] per particle
 // (src/stiffness.c:179-185 SC, :210-216 FCC), summed in the order of a
 // plain row-major matrix-vector product.
