@@ -173,6 +173,29 @@ int lpm_spmv_timing(lpm_ctx *ctx, double *avg_ms, long long *count, int reset);
  * for the given precision, unpadded (algorithmic). */
 double lpm_spmv_bytes(const lpm_ctx *ctx, int precision);
 
+/* ---- no-allocation entry point ----------------------------------------------- */
+/* No counterpart in the reference: an allocation-free form of the residual
+ * update for callers that cannot call cudaMalloc (their device memory comes
+ * from their own pool or a fixed budget, so a library may not allocate).
+ *
+ * residual[d] = dispBC_index[d] * (Pex[d] - Pin[d]) over the 3n DOFs, and
+ * norms = {|residual|, |Pin on the DOFs with dispBC_index == 0|} (the
+ * quantities lpm_compute_force reports).  Pin, Pex, dispBC_index and residual
+ * are DEVICE arrays of 3n entries on the current device, in the reference's
+ * per-particle (x, y, z) order; norms is a host array or NULL.  With norms the
+ * call waits for the stream; without, it only enqueues work on it.
+ *
+ * Allocates nothing: its only work space is a fixed 256 KB device array in
+ * the library (held on every GPU that loads the library until exit), shared by
+ * all calls on a device and keeping the last call's contents.  n beyond
+ * LPM_NOALLOC_MAX_PARTICLES is rejected with LPM_ERR_ARG.  The first call on
+ * each device looks up that array's device address; make that first call
+ * before any stream capture.  Calls whose kernels overlap on the GPU race on
+ * the shared array: order them on one stream. */
+#define LPM_NOALLOC_MAX_PARTICLES 4194304
+int lpm_update_rr_noalloc(int n, const double *Pin, const double *Pex, const int *dispBC_index,
+                          double *residual, double norms[2], void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -30,7 +30,7 @@ EXPORTED = [
     "lpm_set_material", "lpm_set_cp", "lpm_init_state", "lpm_load_step", "lpm_assemble_stiffness",
     "lpm_apply_bc", "lpm_compute_force", "lpm_switch_state", "lpm_solve", "lpm_begin_step", "lpm_get",
     "lpm_set", "lpm_get_sizes", "lpm_export_upper_csr", "lpm_spmv", "lpm_solve_rhs", "lpm_spmv_timing",
-    "lpm_spmv_bytes",
+    "lpm_spmv_bytes", "lpm_update_rr_noalloc",
 ]
 
 
@@ -108,6 +108,7 @@ def load(path=LIB_PATH):
         "lpm_solve_rhs": ([vp, dp, dp, C.POINTER(StepStats)], C.c_int),
         "lpm_spmv_timing": ([vp, dp, C.POINTER(C.c_longlong), C.c_int], C.c_int),
         "lpm_spmv_bytes": ([vp, C.c_int], C.c_double),
+        "lpm_update_rr_noalloc": ([C.c_int, vp, vp, vp, vp, dp, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
