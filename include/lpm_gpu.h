@@ -173,6 +173,31 @@ int lpm_spmv_timing(lpm_ctx *ctx, double *avg_ms, long long *count, int reset);
  * for the given precision, unpadded (algorithmic). */
 double lpm_spmv_bytes(const lpm_ctx *ctx, int precision);
 
+/* ---- batched specimens ------------------------------------------------------- */
+/* Many independent specimens of uneven size (parameter sweeps, random
+ * heterogeneity) in one context.  The reference runs one specimen per process
+ * (the main loop of src/lpmc_project.c:382-471); here the specimens'
+ * particles are concatenated (specimen s owns particles offsets[s] ..
+ * offsets[s+1]-1) and every kernel covers all of them in one launch.
+ *
+ * lpm_setup_batch: createCuboid + searchNormalNeighbor + searchAFEMNeighbor
+ * (src/initialization.c:241-284, src/neighbor.c:9-141) for nspec boxes
+ * (boxes[6 s .. 6 s + 5] as lpm_setup_lattice's box), one lattice and radius.
+ * Returns the total particle count.  Types, material (per particle, so per
+ * specimen) and lpm_init_state then act on the concatenated particles. */
+int lpm_setup_batch(lpm_ctx *ctx, int lattice, double radius, int nspec, const double *boxes);
+/* Specimen count; offsets (may be NULL) receives nspec + 1 particle offsets. */
+int lpm_batch_offsets(const lpm_ctx *ctx, int *offsets);
+/* One load step of src/lpmc_project.c:385-471 for every specimen at once:
+ * dbc holds nbd displacement BCs per specimen (nspec x nbd, specimen-major),
+ * stats (may be NULL) nspec records.  Each specimen runs its own Newton test
+ * and its own PCG scalars and convergence test (block-Jacobi PCG of all
+ * specimens in one launch per kernel, chunks of iterations as CUDA graphs).
+ * A specimen that has left the Newton loop keeps its configuration while the
+ * others iterate; its bond forces are re-evaluated at that configuration.
+ * Force BCs are not supported in a batch. */
+int lpm_batch_load_step(lpm_ctx *ctx, int nbd, const lpm_disp_bc *dbc, lpm_step_stats *stats);
+
 /* ---- no-allocation entry point ----------------------------------------------- */
 /* No counterpart in the reference: an allocation-free form of the residual
  * update for callers that cannot call cudaMalloc (their device memory comes

@@ -30,6 +30,7 @@ CU_UNITS = [
     ("k_stiff.cu", []),
     ("k_solve.cu", []),
     ("lpm_api.cu", []),
+    ("k_batch.cu", []),
     ("k_noalloc.cu", []),
 ]
 CPP_UNITS = [("setup.cpp", ["-ffp-contract=off", "-fopenmp"])]

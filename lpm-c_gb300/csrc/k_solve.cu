@@ -99,6 +99,10 @@ struct SpmvArgs {
     double *partials;
     unsigned *counter;
     CgScalars *sc;
+    // batched specimens: skip the whole launch when *stop is set, and the rows
+    // of specimens whose solve has stopped (spec_done[row_spec[row]] != 0)
+    const int *stop;
+    const int *row_spec, *spec_done, *spec_upd;
 };
 
 // 4 consecutive stiffness values of one component: one 128-bit (FP32) or
@@ -137,12 +141,15 @@ __device__ __forceinline__ void store3(dvec4 *p, double a, double b, double c) {
 // blocks of every 64-block chunk.  V: stiffness value type (products and
 // sums in V), X: vector element type (float4 or dvec4).  MASK zeroes the
 // constrained DOFs of y; DOT accumulates x.y in FP64 and sets
-// alpha = rz / (x.y) for the CG.
-template <typename V, typename X, bool MASK, bool DOT>
+// alpha = rz / (x.y) for the CG.  BATCH: rows of stopped specimens are
+// skipped (their y is left as it was).
+template <typename V, typename X, bool MASK, bool DOT, bool BATCH = false>
 __global__ void __launch_bounds__(VTPB) k_spmv(SpmvArgs a, const V *__restrict__ val, const X *__restrict__ x,
                                                X *__restrict__ y)
 {
     if (DOT && a.sc->done)
+        return;
+    if (BATCH && *a.stop)
         return;
     const int hl = threadIdx.x & 15;
     const unsigned hmask = (threadIdx.x & 16) ? 0xffff0000u : 0x0000ffffu;
@@ -150,6 +157,8 @@ __global__ void __launch_bounds__(VTPB) k_spmv(SpmvArgs a, const V *__restrict__
     const int nhw = (gridDim.x * blockDim.x) >> 4;
     double dot = 0.0;
     for (int row = gw; row < a.n; row += nhw) {
+        if (BATCH && a.spec_done[a.row_spec[row]])
+            continue;
         const long long off = a.rowoff[row];
         const int np = a.npad[row];
         const V *vr = val + 9 * off;
@@ -210,7 +219,9 @@ __global__ void __launch_bounds__(VTPB) k_spmv(SpmvArgs a, const V *__restrict__
 }
 
 // Refinement residual r = b - K32 x64 with FP64 products and sums (masked),
-// and |r|^2 into norms[slot].
+// and |r|^2 into norms[slot].  BATCH: only the rows of specimens due for a
+// reliable update (running with a request, or recursively converged).
+template <bool BATCH = false>
 __global__ void __launch_bounds__(VTPB) k_refine_res(SpmvArgs a, const float *__restrict__ val,
                                                      const dvec4 *__restrict__ x,
                                                      const dvec4 *__restrict__ bvec,
@@ -222,6 +233,12 @@ __global__ void __launch_bounds__(VTPB) k_refine_res(SpmvArgs a, const float *__
     const int nw = (gridDim.x * blockDim.x) >> 5;
     double acc = 0.0;
     for (int row = gw; row < a.n; row += nw) {
+        if (BATCH) {
+            const int s = a.row_spec[row];
+            const int d = a.spec_done[s];
+            if (!((d == 0 && a.spec_upd[s]) || d == 1))
+                continue;
+        }
         const long long off = a.rowoff[row];
         const int np = a.npad[row];
         const float *vr = val + 9 * off;
@@ -507,6 +524,10 @@ static SpmvArgs spmv_args(Ctx &c)
     a.partials = c.partials;
     a.counter = c.counter;
     a.sc = c.sc;
+    a.stop = nullptr;
+    a.row_spec = nullptr;
+    a.spec_done = nullptr;
+    a.spec_upd = nullptr;
     return a;
 }
 
@@ -551,9 +572,34 @@ void launch_spmv_fx(Ctx &c, const dvec4 *x, dvec4 *y, bool masked, bool dot)
     spmv_launch<float, dvec4>(c, c.Kf, x, y, masked, dot);
 }
 
+// masked y = K x over every specimen of a batch that is still running
+void launch_spmv_batch(Ctx &c, const dvec4 *x, dvec4 *y, bool k32)
+{
+    SpmvArgs a = spmv_args(c);
+    a.stop = c.bcg.all_done;
+    a.row_spec = c.bcg.spec_of;
+    a.spec_done = c.bcg.done;
+    const int g = red_grid(c);
+    record_timing(c, c.ev_a);
+    if (k32)
+        k_spmv<float, dvec4, true, false, true><<<g, VTPB, 0, c.stream>>>(a, c.Kf, x, y);
+    else
+        k_spmv<double, dvec4, true, false, true><<<g, VTPB, 0, c.stream>>>(a, c.Kd, x, y);
+    record_timing(c, c.ev_b);
+}
+
 void launch_refine_residual(Ctx &c, const dvec4 *x, const dvec4 *b, dvec4 *r, double bscale)
 {
     k_refine_res<<<red_grid(c), VTPB, 0, c.stream>>>(spmv_args(c), c.Kf, x, b, r, c.norms, 2, bscale);
+}
+
+void launch_refine_batch(Ctx &c, const dvec4 *x, const dvec4 *b, dvec4 *r)
+{
+    SpmvArgs a = spmv_args(c);
+    a.row_spec = c.bcg.spec_of;
+    a.spec_done = c.bcg.done;
+    a.spec_upd = c.bcg.upd;
+    k_refine_res<true><<<red_grid(c), VTPB, 0, c.stream>>>(a, c.Kf, x, b, r, c.norms, 3, 1.0);
 }
 
 // mixed precision with FP64 CG vectors: FP32 stiffness, FP32 products and row

@@ -44,9 +44,31 @@ static void dfree(T *&p)
     p = nullptr;
 }
 
+static void free_batch(Ctx &c)
+{
+    BatchCg &b = c.bcg;
+    void *dev[] = {(void *)b.spec_of, (void *)b.off, (void *)b.seg_base, b.rz, b.rz_old, b.rr, b.rr_max,
+                   b.tol2, b.alpha, b.beta, b.bscale, b.it, b.done, b.upd, b.nrel, b.active, b.partials,
+                   b.counter, b.all_done, c.bh.norms_d, c.bh.bs, c.bh.bc_d};
+    for (void *p : dev)
+        if (p)
+            cudaFree(p);
+    void *host[] = {c.bh.norms_h, c.bh.bscale_h, c.bh.active_h, c.bh.it_h, c.bh.done_h, c.bh.nrel_h,
+                    c.bh.all_done_h};
+    for (void *p : host)
+        if (p)
+            cudaFreeHost(p);
+    if (c.bh.graph)
+        cudaGraphExecDestroy(c.bh.graph);
+    c.bcg = BatchCg();
+    c.bh = BatchHost();
+    c.nspec = 0;
+}
+
 Ctx::~Ctx()
 {
     cudaSetDevice(device);
+    free_batch(*this);
     void **all[] = {(void **)&xyz, (void **)&xyz0, (void **)&xyz_temp, (void **)&Pin, (void **)&Pex,
                     (void **)&res, (void **)&du, (void **)&mask, (void **)&type, (void **)&G, (void **)&sy,
                     (void **)&Hh, (void **)&stress, (void **)&dlambda, (void **)&nbr, (void **)&shell,
@@ -267,13 +289,15 @@ static int upload_setup(Ctx &c)
     return LPM_OK;
 }
 
-static int setup_common(Ctx &c)
+static int setup_common(Ctx &c, bool built = false)
 {
     HostSetup &h = c.hs;
-    build_neighbors(h);
-    build_afem(h);
-    build_bond_tables(h);
-    build_block_pattern(h);
+    if (!built) {
+        build_neighbors(h);
+        build_afem(h);
+        build_bond_tables(h);
+        build_block_pattern(h);
+    }
     c.n = h.n;
     c.ready = false;
     c.have_K = false;
@@ -394,6 +418,7 @@ int lpm_setup_lattice(lpm_ctx *ctx, int lattice, double radius, const double box
         return fail(LPM_ERR_ARG, "null argument");
     Ctx &c = ctx->c;
     cudaSetDevice(c.device);
+    free_batch(c);
     c.hs = HostSetup();
     int rc = build_lattice(c.hs, lattice, radius, box);
     if (rc < 0)
@@ -407,6 +432,7 @@ int lpm_setup_particles(lpm_ctx *ctx, int lattice, double radius, int n, const d
         return fail(LPM_ERR_ARG, "null context");
     Ctx &c = ctx->c;
     cudaSetDevice(c.device);
+    free_batch(c);
     c.hs = HostSetup();
     int rc = build_particles(c.hs, lattice, radius, n, xyz);
     if (rc < 0)
@@ -998,6 +1024,295 @@ int lpm_load_step(lpm_ctx *ctx, int nbd, const lpm_disp_bc *dbc, int nbf, const 
     return LPM_OK;
 }
 
+}  // extern "C"
+
+// ---- batched specimens ---------------------------------------------------------
+
+namespace lpm {
+
+static int alloc_batch(Ctx &c, const std::vector<int> &off)
+{
+    const int ns = (int)off.size() - 1, n = c.n;
+    BatchCg &b = c.bcg;
+    b.n = n;
+    b.nspec = ns;
+    b.nchunk = (n + BATCH_TPB - 1) / BATCH_TPB;
+    std::vector<int> spec(n), seg(b.nchunk + 1, 0);
+    for (int s = 0; s < ns; s++)
+        for (int i = off[s]; i < off[s + 1]; i++)
+            spec[i] = s;
+    for (int ch = 0; ch < b.nchunk; ch++) {
+        const int first = ch * BATCH_TPB, last = std::min(n, first + BATCH_TPB) - 1;
+        seg[ch + 1] = seg[ch] + spec[last] - spec[first] + 1;
+    }
+    b.nseg = seg[b.nchunk];
+    int rc = 0;
+    int *spec_of = nullptr, *offd = nullptr, *segd = nullptr;
+#define A_(p, cnt)            \
+    if ((rc = dalloc(p, cnt))) \
+        return rc;
+    A_(spec_of, n) A_(offd, ns + 1) A_(segd, b.nchunk + 1)
+    A_(b.rz, ns) A_(b.rz_old, ns) A_(b.rr, ns) A_(b.rr_max, ns) A_(b.tol2, ns) A_(b.alpha, ns) A_(b.beta, ns)
+    A_(b.bscale, ns) A_(b.it, ns) A_(b.done, ns) A_(b.upd, ns) A_(b.nrel, ns) A_(b.active, ns)
+    A_(b.partials, 3 * (size_t)b.nseg) A_(b.counter, 1) A_(b.all_done, 1)
+    A_(c.bh.norms_d, 2 * ns) A_(c.bh.bs, n)
+#undef A_
+    b.spec_of = spec_of;
+    b.off = offd;
+    b.seg_base = segd;
+    LPM_CUDA(cudaMemcpy(spec_of, spec.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    LPM_CUDA(cudaMemcpy(offd, off.data(), sizeof(int) * (ns + 1), cudaMemcpyHostToDevice));
+    LPM_CUDA(cudaMemcpy(segd, seg.data(), sizeof(int) * (b.nchunk + 1), cudaMemcpyHostToDevice));
+    BatchHost &h = c.bh;
+    LPM_CUDA(cudaMallocHost((void **)&h.norms_h, 2 * ns * sizeof(double)));
+    LPM_CUDA(cudaMallocHost((void **)&h.bscale_h, ns * sizeof(double)));
+    LPM_CUDA(cudaMallocHost((void **)&h.active_h, ns * sizeof(int)));
+    LPM_CUDA(cudaMallocHost((void **)&h.it_h, ns * sizeof(int)));
+    LPM_CUDA(cudaMallocHost((void **)&h.done_h, ns * sizeof(int)));
+    LPM_CUDA(cudaMallocHost((void **)&h.nrel_h, ns * sizeof(int)));
+    LPM_CUDA(cudaMallocHost((void **)&h.all_done_h, sizeof(int)));
+    h.nspec = ns;
+    h.off = off;
+    c.nspec = ns;
+    return LPM_OK;
+}
+
+// per-specimen |residual| and |reaction| after a force evaluation
+static int read_batch_norms(Ctx &c, std::vector<double> &res, std::vector<double> &reac)
+{
+    launch_bnorm(c);
+    LPM_CUDA(cudaMemcpyAsync(c.bh.norms_h, c.bh.norms_d, 2 * c.nspec * sizeof(double), cudaMemcpyDeviceToHost,
+                             c.stream));
+    int rc = sync(c);
+    if (rc)
+        return rc;
+    for (int s = 0; s < c.nspec; s++) {
+        res[s] = std::sqrt(c.bh.norms_h[2 * s]);
+        reac[s] = std::sqrt(c.bh.norms_h[2 * s + 1]);
+    }
+    return LPM_OK;
+}
+
+static void issue_batch_chunk(Ctx &c, bool k32, int chunk)
+{
+    for (int k = 0; k < chunk; k++)
+        launch_bcg_iter(c, k32);
+    if (k32)
+        launch_bcg_reliable(c);
+}
+
+// One linear solve of every active specimen (bh.active_h, bh.bscale_h set by
+// the caller): K du = residual on each specimen's unconstrained DOFs, du = 0
+// for the others.  The iterations run as CUDA graphs of opts.check_every
+// iterations (plus the reliable-update step with an FP32 matrix); the host
+// reads one flag per graph launch.
+static int batch_solve(Ctx &c, std::vector<lpm_step_stats> &st)
+{
+    const bool k32 = c.opts.precision == LPM_PREC_MIXED;
+    const int ns = c.nspec, chunk = std::max(1, c.opts.check_every);
+    BatchCg &b = c.bcg;
+    BatchHost &h = c.bh;
+    const double d2 = k32 ? c.opts.inner_rtol * c.opts.inner_rtol : 0.0;
+    const bool same = b.maxit == c.opts.cg_maxiter && b.maxrel == c.opts.refine_maxiter && b.upd_delta2 == d2;
+    b.maxit = c.opts.cg_maxiter;
+    b.maxrel = c.opts.refine_maxiter;
+    b.upd_delta2 = d2;
+    LPM_CUDA(cudaMemcpyAsync(b.bscale, h.bscale_h, ns * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    LPM_CUDA(cudaMemcpyAsync(b.active, h.active_h, ns * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+    launch_bcg_init(c, c.res);
+    // the kernels take BatchCg by value: a graph is valid for the options it
+    // was captured with
+    if (h.graph && (!same || h.graph_chunk != chunk || h.graph_k32 != (int)k32)) {
+        cudaGraphExecDestroy(h.graph);
+        h.graph = nullptr;
+    }
+    bool use_graph = c.opts.use_graphs != 0;
+    if (use_graph && !h.graph) {
+        cudaGraph_t g;
+        if (cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            use_graph = false;
+        } else {
+            issue_batch_chunk(c, k32, chunk);
+            if (cudaStreamEndCapture(c.stream, &g) != cudaSuccess) {
+                use_graph = false;
+            } else {
+                if (cudaGraphInstantiate(&h.graph, g, 0) != cudaSuccess) {
+                    h.graph = nullptr;
+                    use_graph = false;
+                }
+                cudaGraphDestroy(g);
+                h.graph_chunk = chunk;
+                h.graph_k32 = (int)k32;
+            }
+        }
+        cudaGetLastError();
+    }
+    const long long max_chunks = (long long)c.opts.cg_maxiter / chunk + c.opts.refine_maxiter + 4;
+    long long chunks = 0;
+    for (;;) {
+        if (use_graph) {
+            LPM_CUDA(cudaGraphLaunch(h.graph, c.stream));
+        } else {
+            issue_batch_chunk(c, k32, chunk);
+        }
+        LPM_CUDA(cudaMemcpyAsync(h.all_done_h, b.all_done, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+        int rc = sync(c);
+        if (rc)
+            return rc;
+        chunks++;
+        if (*h.all_done_h || chunks >= max_chunks)
+            break;
+    }
+    launch_bcg_finish(c);
+    LPM_CUDA(cudaMemcpyAsync(h.it_h, b.it, ns * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    LPM_CUDA(cudaMemcpyAsync(h.done_h, b.done, ns * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    LPM_CUDA(cudaMemcpyAsync(h.nrel_h, b.nrel, ns * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    int rc = sync(c);
+    if (rc)
+        return rc;
+    for (int s = 0; s < ns; s++) {
+        if (!h.active_h[s])
+            continue;
+        st[s].cg_iters += h.it_h[s];
+        st[s].refine_iters += h.nrel_h[s];
+        st[s].spmv_calls += h.it_h[s] + h.nrel_h[s];
+        const int d = h.done_h[s];
+        if (d == 2 || d == 0 || (k32 && d == 1))
+            st[s].status |= LPM_STATUS_CG_MAXIT;
+        if (d == 3)
+            st[s].status |= LPM_STATUS_NAN;
+    }
+    return LPM_OK;
+}
+
+}  // namespace lpm
+
+extern "C" {
+
+int lpm_setup_batch(lpm_ctx *ctx, int lattice, double radius, int nspec, const double *boxes)
+{
+    if (!ctx || !boxes || nspec <= 0)
+        return fail(LPM_ERR_ARG, "lpm_setup_batch: null argument or no specimen");
+    Ctx &c = ctx->c;
+    cudaSetDevice(c.device);
+    free_batch(c);
+    c.hs = HostSetup();
+    std::vector<int> off;
+    int rc = build_batch(c.hs, lattice, radius, nspec, boxes, off);
+    if (rc < 0)
+        return rc;
+    rc = setup_common(c, true);
+    if (rc < 0)
+        return rc;
+    if ((rc = alloc_batch(c, off)))
+        return rc;
+    return c.n;
+}
+
+int lpm_batch_offsets(const lpm_ctx *ctx, int *offsets)
+{
+    if (!ctx)
+        return fail(LPM_ERR_ARG, "null context");
+    const Ctx &c = ctx->c;
+    if (offsets)
+        for (int s = 0; s <= c.nspec; s++)
+            offsets[s] = c.bh.off[s];
+    return c.nspec;
+}
+
+int lpm_batch_load_step(lpm_ctx *ctx, int nbd, const lpm_disp_bc *dbc, lpm_step_stats *stats)
+{
+    if (!ctx || !ctx->c.ready)
+        return fail(LPM_ERR_ARG, "call lpm_init_state first");
+    Ctx &c = ctx->c;
+    if (c.nspec <= 0)
+        return fail(LPM_ERR_ARG, "lpm_batch_load_step: the context holds no batch (lpm_setup_batch)");
+    if (nbd < 0 || (nbd > 0 && !dbc))
+        return fail(LPM_ERR_ARG, "lpm_batch_load_step: bad displacement BC list");
+    const int ns = c.nspec;
+    std::vector<lpm_step_stats> st(ns);
+    std::memset(st.data(), 0, sizeof(lpm_step_stats) * ns);
+    int rc = lpm_begin_step(ctx);
+    if (rc)
+        return rc;
+    double ms_stiff = 0, ms_solve = 0, ms_force = 0;
+    {
+        Timer t(c.stream);
+        if ((rc = assemble(c)))
+            return rc;
+        ms_stiff = t.stop();
+    }
+    if ((rc = launch_disp_bc_batch(c, nbd, dbc)))
+        return rc;
+    if ((rc = prepare_preconditioner(c)))
+        return rc;
+    std::vector<double> res(ns), reac(ns), tolm(ns);
+    std::vector<int> ni(ns, 0), live(ns, 1);
+    {
+        Timer t(c.stream);
+        if ((rc = force_eval(c, LPM_PL_PREDICTOR)) || (rc = read_batch_norms(c, res, reac)))
+            return rc;
+        ms_force += t.stop();
+    }
+    for (int s = 0; s < ns; s++) {
+        tolm[s] = std::max(res[s], reac[s]);
+        st[s].res0 = res[s];
+        st[s].reac0 = reac[s];
+    }
+    for (;;) {
+        // a specimen leaves the Newton loop for the rest of the step once its
+        // test of src/lpmc_project.c:424 fails
+        bool any = false;
+        for (int s = 0; s < ns; s++) {
+            if (live[s] && !std::isfinite(res[s])) {
+                st[s].status |= LPM_STATUS_NAN;
+                live[s] = 0;
+            }
+            if (live[s] && !(res[s] > c.opts.newton_tol * tolm[s] && ni[s] < c.opts.newton_maxiter))
+                live[s] = 0;
+            c.bh.active_h[s] = live[s];
+            c.bh.bscale_h[s] = live[s] ? 1.0 / res[s] : 0.0;
+            any = any || live[s];
+        }
+        if (!any)
+            break;
+        switch_state(c, 0);
+        {
+            Timer t(c.stream);
+            if ((rc = batch_solve(c, st)))
+                return rc;
+            launch_add_du(c);
+            ms_solve += t.stop();
+        }
+        {
+            Timer t(c.stream);
+            if ((rc = force_eval(c, c.plmode)) || (rc = read_batch_norms(c, res, reac)))
+                return rc;
+            ms_force += t.stop();
+        }
+        for (int s = 0; s < ns; s++)
+            if (live[s])
+                ni[s]++;
+    }
+    switch_state(c, 1);
+    LPM_CUDA(cudaMemcpyAsync(c.status_host, c.status, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    if ((rc = sync(c)))
+        return rc;
+    for (int s = 0; s < ns; s++) {
+        if (ni[s] >= c.opts.newton_maxiter && res[s] > c.opts.newton_tol * tolm[s])
+            st[s].status |= LPM_STATUS_NEWTON_MAXIT;
+        st[s].status |= *c.status_host;
+        st[s].newton_iters = ni[s];
+        st[s].res_final = res[s];
+        st[s].ms_stiffness = ms_stiff;
+        st[s].ms_solve = ms_solve;
+        st[s].ms_force = ms_force;
+    }
+    if (stats)
+        std::memcpy(stats, st.data(), sizeof(lpm_step_stats) * ns);
+    return LPM_OK;
+}
+
 // ---- data exchange -------------------------------------------------------------
 
 int lpm_get(lpm_ctx *ctx, const char *name, void *dst, size_t bytes)
@@ -1083,6 +1398,8 @@ int lpm_get(lpm_ctx *ctx, const char *name, void *dst, size_t bytes)
         return LPM_OK;
     }
     if (nm == "K_pointer") {
+        if (c.hs.kp1.empty())
+            return fail(LPM_ERR_ARG, "K_pointer: this batch exceeds the reference's int32 CSR offsets");
         if (!need((size_t)(n + 1) * 2 * sizeof(int)))
             return fail(LPM_ERR_ARG, nm + ": buffer too small");
         int *o = (int *)dst;
@@ -1183,6 +1500,8 @@ int lpm_export_upper_csr(lpm_ctx *ctx, double *Kg, int *IK, int *JK, long long *
     Ctx &c = ctx->c;
     const HostSetup &h = c.hs;
     const int n = c.n, w = 61;
+    if (h.kp1.empty())
+        return fail(LPM_ERR_ARG, "export_upper_csr: this batch exceeds the reference's int32 CSR offsets");
     if (nnz)
         *nnz = h.kp1[n];
     if (!Kg && !IK && !JK)

@@ -69,6 +69,8 @@ void build_afem(HostSetup &h);
 void build_bond_tables(HostSetup &h);
 void build_block_pattern(HostSetup &h);
 void merge_setups(HostSetup &dst, const std::vector<HostSetup> &parts, std::vector<int> &offsets);
+int build_batch(HostSetup &dst, int lattice, double radius, int nspec, const double *boxes,
+                std::vector<int> &offsets);
 void kntv_per_particle(int lattice, double radius, const double *c11, const double *c12,
                        const double *c44, int n, double *knt);
 
@@ -79,6 +81,41 @@ struct CgScalars {
     double rz, rz_old, pq, rr, alpha, beta, bnorm2, tol2;
     double rr_max, upd_delta2;
     int it, done, maxit, upd_req;
+};
+
+// Per-specimen PCG state of a batch (device pointers, passed by value).
+// done: 0 running, 1 recursive residual met the tolerance, 2 iteration cap,
+// 3 non-finite, 5 specimen inactive (its Newton loop has converged),
+// 6 true residual met the tolerance (mixed precision)
+struct BatchCg {
+    int n = 0, nspec = 0, nchunk = 0, nseg = 0, maxit = 0, maxrel = 0;
+    double upd_delta2 = 0.0;
+    const int *spec_of = nullptr;   // [n] specimen of each particle
+    const int *off = nullptr;       // [nspec + 1] first particle of each specimen
+    const int *seg_base = nullptr;  // [nchunk + 1] first reduction segment of each chunk
+    double *rz = nullptr, *rz_old = nullptr, *rr = nullptr, *rr_max = nullptr, *tol2 = nullptr;
+    double *alpha = nullptr, *beta = nullptr, *bscale = nullptr;
+    int *it = nullptr, *done = nullptr, *upd = nullptr, *nrel = nullptr, *active = nullptr;
+    double *partials = nullptr;     // [3][nseg]
+    unsigned *counter = nullptr;
+    int *all_done = nullptr;        // 1 once every specimen has stopped
+};
+
+// Host-side bookkeeping of a batch context.
+struct BatchHost {
+    int nspec = 0;
+    std::vector<int> off;            // [nspec + 1]
+    double *norms_d = nullptr;       // [2 nspec] squared |residual|, |reaction| per specimen
+    double *norms_h = nullptr;       // pinned mirror
+    double *bscale_h = nullptr;      // pinned [nspec]
+    int *active_h = nullptr;         // pinned [nspec]
+    int *it_h = nullptr, *done_h = nullptr, *nrel_h = nullptr;  // pinned [nspec]
+    int *all_done_h = nullptr;       // pinned
+    void *bc_d = nullptr;            // per-specimen displacement BC lists
+    size_t bc_cap = 0;
+    dvec4 *bs = nullptr;             // right-hand side scaled per specimen
+    cudaGraphExec_t graph = nullptr;
+    int graph_chunk = 0, graph_k32 = -1;
 };
 
 struct Ctx {
@@ -159,6 +196,10 @@ struct Ctx {
     int graph_chunk = 0, graph_mode = -1;
     bool graph_timed = false;
     bool time_this = false;  // the next SpMV launch carries the timing events
+    // batched specimens (lpm_setup_batch); nspec == 0 for a single specimen
+    int nspec = 0;
+    BatchCg bcg;
+    BatchHost bh;
     ~Ctx();
 };
 
@@ -196,6 +237,16 @@ void launch_cg_iter_f(Ctx &c);
 void launch_axpy_refine(Ctx &c, double scale);  // x_d += x_f / scale
 void launch_norm2(Ctx &c, const dvec4 *v, int slot);
 int red_grid(const Ctx &c);
+// batched specimens (k_batch.cu)
+constexpr int BATCH_TPB = 256;  // particles per reduction chunk
+void launch_spmv_batch(Ctx &c, const dvec4 *x, dvec4 *y, bool k32);  // k_solve.cu
+void launch_refine_batch(Ctx &c, const dvec4 *x, const dvec4 *b, dvec4 *r);  // k_solve.cu
+void launch_bnorm(Ctx &c);                       // per-specimen norms -> c.bh.norms_d
+void launch_bcg_init(Ctx &c, const dvec4 *b);   // per-specimen PCG start (uses bcg.active, bcg.bscale)
+void launch_bcg_iter(Ctx &c, bool k32);         // one PCG iteration of every running specimen
+void launch_bcg_reliable(Ctx &c);               // true residual + residual replacement (FP32 matrix)
+void launch_bcg_finish(Ctx &c);                 // du = x / bscale
+int launch_disp_bc_batch(Ctx &c, int nbd, const lpm_disp_bc *d);
 
 }  // namespace lpm
 

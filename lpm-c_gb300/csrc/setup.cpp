@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstring>
 #include <vector>
+#include <omp.h>
 #include "lpm_internal.h"
 
 namespace lpm {
@@ -341,6 +342,57 @@ void merge_setups(HostSetup &dst, const std::vector<HostSetup> &parts, std::vect
     }
     dst.kp1[n] = (int)kbase;
     dst.rowoff[n] = rbase;
+    // K_pointer is the reference's int32 offset into one specimen's upper
+    // CSR; a batch beyond 2^31 entries has no such layout
+    if (kbase > 2147483647LL) {
+        dst.kp0.clear();
+        dst.kp1.clear();
+    }
+}
+
+// Set up nspec specimens (one lattice box each) and concatenate them; the
+// specimens are independent, so they are built in parallel.
+int build_batch(HostSetup &dst, int lattice, double radius, int nspec, const double *boxes,
+                std::vector<int> &offsets)
+{
+    std::vector<HostSetup> parts(nspec);
+    std::vector<int> rcs(nspec, 0);
+    std::vector<std::string> errs(nspec);
+    auto one = [&](int s) {
+        int rc = build_lattice(parts[s], lattice, radius, boxes + 6 * (size_t)s);
+        if (rc < 0) {
+            rcs[s] = rc;
+            errs[s] = g_err;
+            return;
+        }
+        if (parts[s].n <= 0) {
+            rcs[s] = LPM_ERR_ARG;
+            errs[s] = "specimen " + std::to_string(s) + " holds no particle";
+            return;
+        }
+        build_neighbors(parts[s]);
+        build_afem(parts[s]);
+        build_bond_tables(parts[s]);
+        build_block_pattern(parts[s]);
+    };
+    if (nspec >= omp_get_max_threads()) {
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int s = 0; s < nspec; s++)
+            one(s);
+    } else {
+        for (int s = 0; s < nspec; s++)
+            one(s);
+    }
+    for (int s = 0; s < nspec; s++)
+        if (rcs[s] < 0)
+            return fail(rcs[s], "specimen " + std::to_string(s) + ": " + errs[s]);
+    long long total = 0;
+    for (int s = 0; s < nspec; s++)
+        total += parts[s].n;
+    if (total > 2147483647LL / 4)
+        return fail(LPM_ERR_ARG, "batch too large: " + std::to_string(total) + " particles");
+    merge_setups(dst, parts, offsets);
+    return dst.n;
 }
 
 // calcKnTv's KnTve = radius * mapping * [C11, C12, C44] per particle

@@ -30,7 +30,8 @@ EXPORTED = [
     "lpm_set_material", "lpm_set_cp", "lpm_init_state", "lpm_load_step", "lpm_assemble_stiffness",
     "lpm_apply_bc", "lpm_compute_force", "lpm_switch_state", "lpm_solve", "lpm_begin_step", "lpm_get",
     "lpm_set", "lpm_get_sizes", "lpm_export_upper_csr", "lpm_spmv", "lpm_solve_rhs", "lpm_spmv_timing",
-    "lpm_spmv_bytes", "lpm_update_rr_noalloc",
+    "lpm_spmv_bytes", "lpm_update_rr_noalloc", "lpm_setup_batch", "lpm_batch_offsets",
+    "lpm_batch_load_step",
 ]
 
 
@@ -109,6 +110,9 @@ def load(path=LIB_PATH):
         "lpm_spmv_timing": ([vp, dp, C.POINTER(C.c_longlong), C.c_int], C.c_int),
         "lpm_spmv_bytes": ([vp, C.c_int], C.c_double),
         "lpm_update_rr_noalloc": ([C.c_int, vp, vp, vp, vp, dp, vp], C.c_int),
+        "lpm_setup_batch": ([vp, C.c_int, C.c_double, C.c_int, dp], C.c_int),
+        "lpm_batch_offsets": ([vp, ip], C.c_int),
+        "lpm_batch_load_step": ([vp, C.c_int, C.POINTER(DispBC), C.POINTER(StepStats)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -173,6 +177,34 @@ class Specimen:
         box = np.ascontiguousarray(box, dtype=np.float64)
         self.n = self._check(self.L.lpm_setup_lattice(self.h, lattice, radius, _dp(box)))
         return self.n
+
+    def setup_batch(self, lattice, radius, boxes):
+        """Concatenate len(boxes) specimens (lpm_setup_batch); returns the
+        total particle count."""
+        boxes = np.ascontiguousarray(boxes, dtype=np.float64).reshape(-1, 6)
+        self.n = self._check(self.L.lpm_setup_batch(self.h, lattice, radius, len(boxes), _dp(boxes)))
+        return self.n
+
+    def batch_offsets(self):
+        ns = self._check(self.L.lpm_batch_offsets(self.h, None))
+        off = np.zeros(ns + 1, dtype=np.int32)
+        self._check(self.L.lpm_batch_offsets(self.h, _ip(off)))
+        return off
+
+    def batch_load_step(self, disp_bcs):
+        """disp_bcs: one list of (type, flag, step) per specimen, all of the
+        same length.  Returns one statistics dict per specimen."""
+        ns = len(disp_bcs)
+        nbd = len(disp_bcs[0]) if ns else 0
+        if any(len(b) != nbd for b in disp_bcs):
+            raise LPMError("every specimen needs the same number of displacement BCs")
+        arr = (DispBC * max(1, ns * nbd))()
+        for s, bl in enumerate(disp_bcs):
+            for k, (t, f, v) in enumerate(bl):
+                arr[s * nbd + k] = DispBC(int(t), f.encode() if isinstance(f, str) else f, float(v))
+        st = (StepStats * ns)()
+        self._check(self.L.lpm_batch_load_step(self.h, nbd, arr, st))
+        return [x.as_dict() for x in st]
 
     def setup_particles(self, lattice, radius, xyz):
         xyz = np.ascontiguousarray(xyz, dtype=np.float64)

@@ -37,6 +37,19 @@ def sc_box(nx, ny, nz, radius):
             -0.5 * h, (nz - 1) * h + 0.5 * h]
 
 
+def sc_box_exact(nx, ny, nz, radius):
+    """Box for createCuboid (lattice 2) holding exactly nx*ny*nz particles for
+    any edge lengths.  The generator's y/z grid lines sit at -a + 2r k with a
+    the box diagonal (src/initialization.c:241-284), and a depends only on the
+    box's edge lengths, so the y/z ranges are centred on grid lines: no line
+    falls on a face."""
+    h = 2.0 * radius
+    bx, by, bz = (nx - 1) * h + 0.5 * h, ny * h, nz * h
+    a = np.sqrt(bx * bx + by * by + bz * bz)
+    line0 = -a + h * np.ceil(a / h)  # first grid line at or above 0
+    return [0.0, bx, line0 - 0.5 * h, line0 - 0.5 * h + by, line0 - 0.5 * h, line0 - 0.5 * h + bz]
+
+
 def sc_types(xyz, nb, radius, nneighbors=18):
     """Types: top/bottom layers, full-neighbour interior, and the two pins."""
     n = xyz.shape[0]
@@ -132,3 +145,30 @@ class FCCCase:
 
     def ce_per_type(self):
         return np.tile([self.C11, self.C12, self.C44], (NTYPE, 1))
+
+
+class BatchCase:
+    """Batch of independent SC specimens of uneven size (C4 at nspec=256,
+    edges 20..60): each edge drawn independently from U{lo..hi}, per-specimen
+    E ~ U[180e3, 220e3], yield ~ U[200, 400], H = 2000; monotonic tension to
+    `strain` over `steps` equal steps (top layer displaced along z)."""
+
+    def __init__(self, nspec=256, edge_lo=20, edge_hi=60, radius=0.1, nu=0.3, H=2000.0,
+                 strain=0.01, steps=50, newton_tol=1e-8, seed=1):
+        self.nspec, self.radius, self.lattice = nspec, radius, 2
+        u = splitmix64_uniform(seed, 3 * nspec).reshape(nspec, 3)
+        self.edges = (edge_lo + np.floor(u * (edge_hi - edge_lo + 1))).astype(int)
+        self.E = 180e3 + 40e3 * splitmix64_uniform(seed + 1, nspec)
+        self.sigmay = 200.0 + 200.0 * splitmix64_uniform(seed + 2, nspec)
+        self.nu, self.H = nu, H
+        self.boxes = np.array([sc_box_exact(nx, ny, nz, radius) for nx, ny, nz in self.edges])
+        self.heights = (self.edges[:, 2] - 1) * 2.0 * radius
+        self.strain, self.steps = strain, steps
+        self.newton_tol = newton_tol
+
+    def particles(self):
+        return int(np.prod(self.edges, axis=1).sum())
+
+    def step_bcs(self):
+        """Per-specimen BC lists of one load step."""
+        return [sc_bcs(self.strain * h / self.steps) for h in self.heights]

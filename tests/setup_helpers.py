@@ -39,3 +39,35 @@ def material_arrays(case, n):
         scale = 1.0 + case.e_noise * (2.0 * u - 1.0)
         return c11 * scale, c12 * scale, c44 * scale
     return np.full(n, c11), np.full(n, c12), np.full(n, c44)
+
+
+def batch_gpu(G, case, precision=0, **solver):
+    """All specimens of a cases.BatchCase in one batch context."""
+    s = G.Specimen(0)
+    n = s.setup_batch(case.lattice, case.radius, case.boxes)
+    off = s.batch_offsets()
+    xyz, nb = s.get("xyz"), s.get("nb")
+    types = np.concatenate([cases.sc_types(xyz[off[k]:off[k + 1]], nb[off[k]:off[k + 1]], case.radius)
+                            for k in range(case.nspec)])
+    reps = np.diff(off)
+    E = np.repeat(case.E, reps)
+    c11, c12, c44 = cases.iso_cubic(E, case.nu)
+    s.set_types(types)
+    s.set_material(c11, c12, c44, np.repeat(case.sigmay, reps), np.full(n, case.H), 0.0, G.PL_J2)
+    s.init_state()
+    s.set_solver(precision=precision, newton_tol=case.newton_tol, **solver)
+    return s, off
+
+
+def single_of_batch(G, case, k, precision=0, **solver):
+    """Specimen k of a cases.BatchCase alone in its own context."""
+    s = G.Specimen(0)
+    n = s.setup_lattice(case.lattice, case.radius, case.boxes[k])
+    types = cases.sc_types(s.get("xyz"), s.get("nb"), case.radius)
+    c11, c12, c44 = cases.iso_cubic(case.E[k], case.nu)
+    s.set_types(types)
+    s.set_material(np.full(n, c11), np.full(n, c12), np.full(n, c44), np.full(n, case.sigmay[k]),
+                   np.full(n, case.H), 0.0, G.PL_J2)
+    s.init_state()
+    s.set_solver(precision=precision, newton_tol=case.newton_tol, **solver)
+    return s

@@ -1,0 +1,101 @@
+"""Batched specimens (lpm_setup_batch / lpm_batch_load_step) against a loop of
+single-specimen solves: every specimen of the batch must follow the same
+load path as the same specimen solved alone.
+
+Specimens of 64..729 particles make the 256-particle reduction chunks
+straddle several specimens, which exercises the segmented reductions."""
+import numpy as np
+import pytest
+
+import cases
+from setup_helpers import batch_gpu, single_of_batch
+
+pytestmark = pytest.mark.gpu
+
+DISP_RTOL = 1e-8   # displacement, relative to the specimen's largest |du|
+# modified Newton (elastic tangent) needs tens of iterations at the onset of
+# yield, hence the generous cap
+SOLVER = dict(newton_maxiter=300, cg_rtol=1e-11)
+
+
+def small_case(newton_tol=1e-8):
+    return cases.BatchCase(nspec=7, edge_lo=4, edge_hi=9, strain=0.004, steps=8, newton_tol=newton_tol, seed=3)
+
+
+def run_batch(G, case, nsteps, precision=0, **solver):
+    s, off = batch_gpu(G, case, precision=precision, **dict(SOLVER, **solver))
+    x0 = s.get("xyz_initial")
+    hist, stats = [], []
+    for _ in range(nsteps):
+        st = s.batch_load_step(case.step_bcs())
+        stats.append(st)
+        hist.append(s.get("xyz") - x0)
+    alpha = s.get("J2_alpha")
+    s.close()
+    return off, hist, stats, alpha
+
+
+def run_single(G, case, k, nsteps, precision=0):
+    s = single_of_batch(G, case, k, precision=precision, **SOLVER)
+    x0 = s.get("xyz_initial")
+    bcs = case.step_bcs()[k]
+    hist = []
+    for _ in range(nsteps):
+        st = s.load_step(bcs)
+        assert st["status"] == 0, st
+        hist.append(s.get("xyz") - x0)
+    alpha = s.get("J2_alpha")
+    s.close()
+    return hist, alpha
+
+
+@pytest.mark.parametrize("precision,graphs", [(0, 1), (0, 0), (1, 1)])
+def test_batch_matches_single_specimens(gpu_lib, precision, graphs):
+    G = gpu_lib
+    # the mixed batch is compared with FP64 single solves: both converged
+    # tightly so that their difference is the precision's, not Newton's
+    case = small_case(1e-8 if precision == 0 else 1e-10)
+    nsteps = 6
+    off, hist, stats, alpha = run_batch(G, case, nsteps, precision=precision, use_graphs=graphs)
+    assert len(off) == case.nspec + 1 and off[-1] == case.particles()
+    for step in stats:
+        for k, st in enumerate(step):
+            assert st["status"] == 0, (k, st)
+            assert st["newton_iters"] >= 1
+    assert alpha.max() > 0.0  # the path is plastic
+    for k in range(case.nspec):
+        ref_hist, ref_alpha = run_single(G, case, k, nsteps, precision=0)
+        sl = slice(off[k], off[k + 1])
+        for j in range(nsteps):
+            du, ref = hist[j][sl], ref_hist[j]
+            err = np.abs(du - ref).max() / np.abs(ref).max()
+            assert err < DISP_RTOL, (k, j, err)
+        am = max(ref_alpha.max(), 1e-30)
+        assert np.abs(alpha[sl] - ref_alpha).max() <= DISP_RTOL * am, k
+
+
+def test_batch_is_deterministic(gpu_lib):
+    """Two runs of the same batch give bit-identical displacements."""
+    case = small_case()
+    _, h1, s1, a1 = run_batch(gpu_lib, case, 3)
+    _, h2, s2, a2 = run_batch(gpu_lib, case, 3)
+    for a, b in zip(h1, h2):
+        assert np.array_equal(a, b)
+    assert np.array_equal(a1, a2)
+    assert [[st["cg_iters"] for st in step] for step in s1] == [[st["cg_iters"] for st in step] for step in s2]
+
+
+def test_batch_offsets_and_sizes(gpu_lib):
+    case = cases.BatchCase(nspec=5, edge_lo=3, edge_hi=7, seed=9)
+    s = gpu_lib.Specimen(0)
+    n = s.setup_batch(case.lattice, case.radius, case.boxes)
+    off = s.batch_offsets()
+    assert n == case.particles()
+    assert np.array_equal(np.diff(off), np.prod(case.edges, axis=1))
+    # each specimen's bond lists stay inside the specimen
+    nbr = s.get("neighbors")
+    for k in range(case.nspec):
+        blk = nbr[off[k]:off[k + 1]]
+        valid = blk[blk >= 0]
+        assert valid.min() >= off[k] and valid.max() < off[k + 1]
+    s.close()
