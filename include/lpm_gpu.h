@@ -173,6 +173,28 @@ int lpm_spmv_timing(lpm_ctx *ctx, double *avg_ms, long long *count, int reset);
  * for the given precision, unpadded (algorithmic). */
 double lpm_spmv_bytes(const lpm_ctx *ctx, int precision);
 
+/* ---- autotuner ------------------------------------------------------------------ */
+/* Launch shapes of the solve: the SpMV tile (lanes per block row x
+ * consecutive blocks per lane: variant 0 = 16 x 4, 1 = 8 x 4, 2 = 32 x 2,
+ * 3 = 4 x 4), its thread blocks per SM, and the thread blocks per SM of the
+ * PCG vector kernels.  No counterpart in the reference, whose solve is MKL's. */
+typedef struct lpm_tuning {
+    int spmv_variant;
+    int spmv_lanes;        /* output: lanes per block row */
+    int spmv_blocks;       /* output: consecutive blocks per lane */
+    int spmv_per_sm;
+    int cg_per_sm;
+    double spmv_ms;        /* lpm_autotune: time of the chosen SpMV shape */
+    double spmv_ms_default;/* lpm_autotune: time of the default shape (0, 8, 8) */
+} lpm_tuning;
+/* Time every SpMV shape (and vector-kernel grid) on the context's current
+ * stiffness with CUDA events and keep the fastest.  Needs an assembled
+ * stiffness (lpm_assemble_stiffness or a load step).  Different shapes sum a
+ * row in different orders, so results can change in the last bits. */
+int lpm_autotune(lpm_ctx *ctx, lpm_tuning *out);
+int lpm_set_tuning(lpm_ctx *ctx, const lpm_tuning *t);
+int lpm_get_tuning(const lpm_ctx *ctx, lpm_tuning *t);
+
 /* ---- batched specimens ------------------------------------------------------- */
 /* Many independent specimens of uneven size (parameter sweeps, random
  * heterogeneity) in one context.  The reference runs one specimen per process

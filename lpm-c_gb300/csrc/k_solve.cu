@@ -103,14 +103,57 @@ struct SpmvArgs {
     // of specimens whose solve has stopped (spec_done[row_spec[row]] != 0)
     const int *stop;
     const int *row_spec, *spec_done, *spec_upd;
+    const int *act_chunk, *n_act;  // batch: chunks of BATCH_TPB rows holding a running specimen
 };
 
-// 4 consecutive stiffness values of one component: one 128-bit (FP32) or
-// 256-bit (FP64) streaming load.
-__device__ __forceinline__ float4 load_vals4(const float *p) { return __ldcs(reinterpret_cast<const float4 *>(p)); }
-__device__ __forceinline__ double4_32a load_vals4(const double *p)
+// B consecutive stiffness values of one component: one 64/128-bit (FP32)
+// or 128/256-bit (FP64) streaming load.
+template <typename V, int B>
+struct VPack;
+template <>
+struct VPack<float, 4> {
+    typedef float4 T;
+};
+template <>
+struct VPack<float, 2> {
+    typedef float2 T;
+};
+template <>
+struct VPack<double, 4> {
+    typedef double4_32a T;
+};
+template <>
+struct VPack<double, 2> {
+    typedef double2 T;
+};
+__device__ __forceinline__ float4 ld_vals(const float4 *p) { return __ldcs(p); }
+__device__ __forceinline__ float2 ld_vals(const float2 *p) { return __ldcs(p); }
+__device__ __forceinline__ double2 ld_vals(const double2 *p) { return __ldcs(p); }
+__device__ __forceinline__ double4_32a ld_vals(const double4_32a *p) { return *p; }
+template <int B, typename T, typename A>
+__device__ __forceinline__ void unpack(const T &v, A (&o)[B])
 {
-    return *reinterpret_cast<const double4_32a *>(p);
+    o[0] = v.x;
+    o[1] = v.y;
+    if constexpr (B == 4) {
+        o[2] = v.z;
+        o[3] = v.w;
+    }
+}
+template <int B>
+__device__ __forceinline__ void load_cols(const int *p, int (&c)[B])
+{
+    if constexpr (B == 4) {
+        const int4 v = __ldg(reinterpret_cast<const int4 *>(p));
+        c[0] = v.x;
+        c[1] = v.y;
+        c[2] = v.z;
+        c[3] = v.w;
+    } else {
+        const int2 v = __ldg(reinterpret_cast<const int2 *>(p));
+        c[0] = v.x;
+        c[1] = v.y;
+    }
 }
 template <typename A>
 __device__ __forceinline__ void xyz_of(const float4 &v, A &x, A &y, A &z)
@@ -137,63 +180,68 @@ __device__ __forceinline__ dvec4 ldx(const dvec4 *p)
 __device__ __forceinline__ void store3(float4 *p, float a, float b, float c) { *p = make_float4(a, b, c, 0.f); }
 __device__ __forceinline__ void store3(dvec4 *p, double a, double b, double c) { *p = make_dvec4(a, b, c, 0.0); }
 
-// y = K x with a half-warp per block row; each lane takes four consecutive
-// blocks of every 64-block chunk.  V: stiffness value type (products and
-// sums in V), X: vector element type (float4 or dvec4).  MASK zeroes the
-// constrained DOFs of y; DOT accumulates x.y in FP64 and sets
-// alpha = rz / (x.y) for the CG.  BATCH: rows of stopped specimens are
-// skipped (their y is left as it was).
-template <typename V, typename X, bool MASK, bool DOT, bool BATCH = false>
+// y = K x with L lanes per block row; each lane takes B consecutive blocks
+// of every L*B-block chunk of its row (rows are padded to a multiple of 4
+// blocks, so B = 4 or 2 never crosses a row end).  The default L = 16, B = 4
+// gives one 128-bit value load per component and one int4 of columns per
+// lane for the 61-block rows of the interior; the autotuner picks among the
+// variants.  V: stiffness value type (products and sums in V), X: vector
+// element type (float4 or dvec4).  MASK zeroes the constrained DOFs of y;
+// DOT accumulates x.y in FP64 and sets alpha = rz / (x.y) for the CG.
+// BATCH: rows of stopped specimens are skipped (their y is left as it was).
+template <typename V, typename X, bool MASK, bool DOT, bool BATCH = false, int L = 16, int B = 4>
 __global__ void __launch_bounds__(VTPB) k_spmv(SpmvArgs a, const V *__restrict__ val, const X *__restrict__ x,
                                                X *__restrict__ y)
 {
+    static_assert(L == 4 || L == 8 || L == 16 || L == 32, "lanes per row");
+    static_assert(B == 2 || B == 4, "blocks per lane");
+    typedef typename VPack<V, B>::T P;
     if (DOT && a.sc->done)
         return;
     if (BATCH && *a.stop)
         return;
-    const int hl = threadIdx.x & 15;
-    const unsigned hmask = (threadIdx.x & 16) ? 0xffff0000u : 0x0000ffffu;
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 4;
-    const int nhw = (gridDim.x * blockDim.x) >> 4;
+    const int sub = threadIdx.x & (L - 1);
+    const unsigned gmask = (L == 32) ? 0xffffffffu : (((1u << L) - 1u) << ((threadIdx.x & 31) & ~(L - 1)));
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) / L;
+    const int nhw = (gridDim.x * blockDim.x) / L;
     double dot = 0.0;
-    for (int row = gw; row < a.n; row += nhw) {
-        if (BATCH && a.spec_done[a.row_spec[row]])
-            continue;
+    const int nrows = BATCH ? (*a.n_act) * BATCH_TPB : a.n;
+    for (int vrow = gw; vrow < nrows; vrow += nhw) {
+        int row = vrow;
+        if (BATCH) {
+            row = a.act_chunk[vrow / BATCH_TPB] * BATCH_TPB + vrow % BATCH_TPB;
+            if (row >= a.n || a.spec_done[a.row_spec[row]])
+                continue;
+        }
         const long long off = a.rowoff[row];
         const int np = a.npad[row];
         const V *vr = val + 9 * off;
         V y0 = 0, y1 = 0, y2 = 0;
-        for (int b0 = 4 * hl; b0 < np; b0 += 64) {
-            const int4 c4 = __ldg(reinterpret_cast<const int4 *>(a.cols + off + b0));
-            decltype(load_vals4(vr)) v[9];
+        for (int b0 = B * sub; b0 < np; b0 += B * L) {
+            int cc[B];
+            load_cols<B>(a.cols + off + b0, cc);
+            V v[9][B];
 #pragma unroll
             for (int k = 0; k < 9; k++)
-                v[k] = load_vals4(vr + (size_t)k * np + b0);
-            V ax, ay, az, bx, by, bz, cx, cy, cz, dx, dy, dz;
-            xyz_of<V>(ldx(x + c4.x), ax, ay, az);
-            xyz_of<V>(ldx(x + c4.y), bx, by, bz);
-            xyz_of<V>(ldx(x + c4.z), cx, cy, cz);
-            xyz_of<V>(ldx(x + c4.w), dx, dy, dz);
-            y0 += v[0].x * ax + v[1].x * ay + v[2].x * az;
-            y1 += v[3].x * ax + v[4].x * ay + v[5].x * az;
-            y2 += v[6].x * ax + v[7].x * ay + v[8].x * az;
-            y0 += v[0].y * bx + v[1].y * by + v[2].y * bz;
-            y1 += v[3].y * bx + v[4].y * by + v[5].y * bz;
-            y2 += v[6].y * bx + v[7].y * by + v[8].y * bz;
-            y0 += v[0].z * cx + v[1].z * cy + v[2].z * cz;
-            y1 += v[3].z * cx + v[4].z * cy + v[5].z * cz;
-            y2 += v[6].z * cx + v[7].z * cy + v[8].z * cz;
-            y0 += v[0].w * dx + v[1].w * dy + v[2].w * dz;
-            y1 += v[3].w * dx + v[4].w * dy + v[5].w * dz;
-            y2 += v[6].w * dx + v[7].w * dy + v[8].w * dz;
+                unpack<B>(ld_vals(reinterpret_cast<const P *>(vr + (size_t)k * np + b0)), v[k]);
+            V xs[B][3];
+#pragma unroll
+            for (int j = 0; j < B; j++)
+                xyz_of<V>(ldx(x + cc[j]), xs[j][0], xs[j][1], xs[j][2]);
+#pragma unroll
+            for (int j = 0; j < B; j++) {
+                y0 += v[0][j] * xs[j][0] + v[1][j] * xs[j][1] + v[2][j] * xs[j][2];
+                y1 += v[3][j] * xs[j][0] + v[4][j] * xs[j][1] + v[5][j] * xs[j][2];
+                y2 += v[6][j] * xs[j][0] + v[7][j] * xs[j][1] + v[8][j] * xs[j][2];
+            }
         }
 #pragma unroll
-        for (int o = 8; o > 0; o >>= 1) {
-            y0 += __shfl_xor_sync(hmask, y0, o);
-            y1 += __shfl_xor_sync(hmask, y1, o);
-            y2 += __shfl_xor_sync(hmask, y2, o);
+        for (int o = L / 2; o > 0; o >>= 1) {
+            y0 += __shfl_xor_sync(gmask, y0, o);
+            y1 += __shfl_xor_sync(gmask, y1, o);
+            y2 += __shfl_xor_sync(gmask, y2, o);
         }
-        if (hl == 0) {
+        if (sub == 0) {
             if (MASK) {
                 const uint8_t m = a.mask[row];
                 y0 = (m & 1) ? y0 : V(0);
@@ -492,12 +540,19 @@ __global__ void __launch_bounds__(VTPB) k_norm2(int n, const dvec4 *v, double *p
     grid_reduce<1>(s, partials, counter, [norms, slot](const double *t) { norms[slot] = t[0]; });
 }
 
-int red_grid(const Ctx &c)
+static int sm_count(const Ctx &c)
 {
+    if (c.tune.sms > 0)
+        return c.tune.sms;
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
-    return sms * 8;
+    return sms;
 }
+
+int red_grid(const Ctx &c) { return sm_count(c) * c.tune.vec_per_sm; }
+int spmv_grid(const Ctx &c) { return sm_count(c) * c.tune.spmv_per_sm; }
+int spmv_variant_lanes(int v) { return v == 1 ? 8 : (v == 2 ? 32 : (v == 3 ? 4 : 16)); }
+int spmv_variant_blocks(int v) { return v == 2 ? 2 : 4; }
 
 // Event pair around SpMV launches; inside a stream capture the records become
 // external event nodes, so the last SpMV of each graph launch is timed.
@@ -528,6 +583,8 @@ static SpmvArgs spmv_args(Ctx &c)
     a.row_spec = nullptr;
     a.spec_done = nullptr;
     a.spec_upd = nullptr;
+    a.act_chunk = nullptr;
+    a.n_act = nullptr;
     return a;
 }
 
@@ -542,18 +599,36 @@ static VecArgs vec_args(Ctx &c)
     return a;
 }
 
+template <typename V, typename X, bool MASK, bool DOT, bool BATCH>
+static void spmv_variant(const Ctx &c, const SpmvArgs &a, const V *val, const X *x, X *y)
+{
+    const int g = spmv_grid(c);
+    switch (c.tune.spmv_variant) {
+    case 1:
+        k_spmv<V, X, MASK, DOT, BATCH, 8, 4><<<g, VTPB, 0, c.stream>>>(a, val, x, y);
+        break;
+    case 2:
+        k_spmv<V, X, MASK, DOT, BATCH, 32, 2><<<g, VTPB, 0, c.stream>>>(a, val, x, y);
+        break;
+    case 3:
+        k_spmv<V, X, MASK, DOT, BATCH, 4, 4><<<g, VTPB, 0, c.stream>>>(a, val, x, y);
+        break;
+    default:
+        k_spmv<V, X, MASK, DOT, BATCH, 16, 4><<<g, VTPB, 0, c.stream>>>(a, val, x, y);
+    }
+}
+
 template <typename V, typename X>
 static void spmv_launch(Ctx &c, const V *val, const X *x, X *y, bool masked, bool dot)
 {
     SpmvArgs a = spmv_args(c);
-    const int g = red_grid(c);
     record_timing(c, c.ev_a);
     if (masked && dot)
-        k_spmv<V, X, true, true><<<g, VTPB, 0, c.stream>>>(a, val, x, y);
+        spmv_variant<V, X, true, true, false>(c, a, val, x, y);
     else if (masked)
-        k_spmv<V, X, true, false><<<g, VTPB, 0, c.stream>>>(a, val, x, y);
+        spmv_variant<V, X, true, false, false>(c, a, val, x, y);
     else
-        k_spmv<V, X, false, false><<<g, VTPB, 0, c.stream>>>(a, val, x, y);
+        spmv_variant<V, X, false, false, false>(c, a, val, x, y);
     record_timing(c, c.ev_b);
 }
 
@@ -579,12 +654,13 @@ void launch_spmv_batch(Ctx &c, const dvec4 *x, dvec4 *y, bool k32)
     a.stop = c.bcg.all_done;
     a.row_spec = c.bcg.spec_of;
     a.spec_done = c.bcg.done;
-    const int g = red_grid(c);
+    a.act_chunk = c.bcg.act_chunk;
+    a.n_act = c.bcg.n_act;
     record_timing(c, c.ev_a);
     if (k32)
-        k_spmv<float, dvec4, true, false, true><<<g, VTPB, 0, c.stream>>>(a, c.Kf, x, y);
+        spmv_variant<float, dvec4, true, false, true>(c, a, c.Kf, x, y);
     else
-        k_spmv<double, dvec4, true, false, true><<<g, VTPB, 0, c.stream>>>(a, c.Kd, x, y);
+        spmv_variant<double, dvec4, true, false, true>(c, a, c.Kd, x, y);
     record_timing(c, c.ev_b);
 }
 

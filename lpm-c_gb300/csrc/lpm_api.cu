@@ -49,7 +49,7 @@ static void free_batch(Ctx &c)
     BatchCg &b = c.bcg;
     void *dev[] = {(void *)b.spec_of, (void *)b.off, (void *)b.seg_base, b.rz, b.rz_old, b.rr, b.rr_max,
                    b.tol2, b.alpha, b.beta, b.bscale, b.it, b.done, b.upd, b.nrel, b.active, b.partials,
-                   b.counter, b.all_done, c.bh.norms_d, c.bh.bs, c.bh.bc_d};
+                   b.counter, b.all_done, b.act_chunk, b.n_act, c.bh.norms_d, c.bh.bs, c.bh.bc_d};
     for (void *p : dev)
         if (p)
             cudaFree(p);
@@ -224,7 +224,10 @@ static int alloc_specimen(Ctx &c)
         A_(c.dLp[s], nb) A_(c.alpha[s], n) A_(c.beta[s], 6 * n)
     }
     A_(c.sc, 1) A_(c.norms, 4) A_(c.status, 1) A_(c.counter, 1)
-    const size_t red = std::max<size_t>((n + 63) / 64 + 64, (size_t)red_grid(c) + 64);
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
+    c.tune.sms = sms;
+    const size_t red = std::max<size_t>((n + 63) / 64 + 64, (size_t)sms * TUNE_MAX_PER_SM + 64);
     A_(c.partials, 4 * red)
     // block-CSR pattern
     const HostSetup &h = c.hs;
@@ -1054,7 +1057,8 @@ static int alloc_batch(Ctx &c, const std::vector<int> &off)
     A_(spec_of, n) A_(offd, ns + 1) A_(segd, b.nchunk + 1)
     A_(b.rz, ns) A_(b.rz_old, ns) A_(b.rr, ns) A_(b.rr_max, ns) A_(b.tol2, ns) A_(b.alpha, ns) A_(b.beta, ns)
     A_(b.bscale, ns) A_(b.it, ns) A_(b.done, ns) A_(b.upd, ns) A_(b.nrel, ns) A_(b.active, ns)
-    A_(b.partials, 3 * (size_t)b.nseg) A_(b.counter, 1) A_(b.all_done, 1)
+    A_(b.partials, 3 * (size_t)b.nseg) A_(b.counter, 1) A_(b.all_done, 1) A_(b.act_chunk, b.nchunk)
+    A_(b.n_act, 1)
     A_(c.bh.norms_d, 2 * ns) A_(c.bh.bs, n)
 #undef A_
     b.spec_of = spec_of;
@@ -1095,6 +1099,7 @@ static int read_batch_norms(Ctx &c, std::vector<double> &res, std::vector<double
 
 static void issue_batch_chunk(Ctx &c, bool k32, int chunk)
 {
+    launch_bcg_compact(c);
     for (int k = 0; k < chunk; k++)
         launch_bcg_iter(c, k32);
     if (k32)
@@ -1589,6 +1594,147 @@ int lpm_spmv(lpm_ctx *ctx, const double *x, double *y)
         y[3 * i + 2] = xf[i].z;
     }
     return LPM_OK;
+}
+
+}  // extern "C"
+
+// ---- autotuner -----------------------------------------------------------------
+
+namespace lpm {
+
+// cached CUDA graphs hold launch shapes: drop them when the shapes change
+static void drop_graphs(Ctx &c)
+{
+    if (c.graph_fp64)
+        cudaGraphExecDestroy(c.graph_fp64);
+    if (c.graph_fp32)
+        cudaGraphExecDestroy(c.graph_fp32);
+    c.graph_fp64 = c.graph_fp32 = nullptr;
+    if (c.bh.graph)
+        cudaGraphExecDestroy(c.bh.graph);
+    c.bh.graph = nullptr;
+}
+
+static void fill_tuning(const Ctx &c, lpm_tuning *t)
+{
+    t->spmv_variant = c.tune.spmv_variant;
+    t->spmv_lanes = spmv_variant_lanes(c.tune.spmv_variant);
+    t->spmv_blocks = spmv_variant_blocks(c.tune.spmv_variant);
+    t->spmv_per_sm = c.tune.spmv_per_sm;
+    t->cg_per_sm = c.tune.vec_per_sm;
+}
+
+}  // namespace lpm
+
+extern "C" {
+
+int lpm_get_tuning(const lpm_ctx *ctx, lpm_tuning *t)
+{
+    if (!ctx || !t)
+        return fail(LPM_ERR_ARG, "null argument");
+    fill_tuning(ctx->c, t);
+    t->spmv_ms = t->spmv_ms_default = 0.0;
+    return LPM_OK;
+}
+
+int lpm_set_tuning(lpm_ctx *ctx, const lpm_tuning *t)
+{
+    if (!ctx || !t)
+        return fail(LPM_ERR_ARG, "null argument");
+    auto ok_grid = [](int v) { return v >= 1 && v <= TUNE_MAX_PER_SM; };
+    if (t->spmv_variant < 0 || t->spmv_variant > 3 || !ok_grid(t->spmv_per_sm) || !ok_grid(t->cg_per_sm))
+        return fail(LPM_ERR_ARG, "lpm_set_tuning: variant 0..3, blocks per SM 1.." +
+                                     std::to_string(TUNE_MAX_PER_SM));
+    Ctx &c = ctx->c;
+    c.tune.spmv_variant = t->spmv_variant;
+    c.tune.spmv_per_sm = t->spmv_per_sm;
+    c.tune.vec_per_sm = t->cg_per_sm;
+    drop_graphs(c);
+    return LPM_OK;
+}
+
+int lpm_autotune(lpm_ctx *ctx, lpm_tuning *out)
+{
+    if (!ctx || !ctx->c.have_K)
+        return fail(LPM_ERR_ARG, "lpm_autotune: assemble the stiffness first");
+    Ctx &c = ctx->c;
+    const bool k32 = c.opts.precision == LPM_PREC_MIXED;
+    const bool vec64 = !k32 || c.nspec > 0 || c.opts.mixed_vectors == 64;
+    const bool timed = c.time_spmv;
+    c.time_spmv = false;
+    auto spmv = [&]() {
+        if (!k32)
+            launch_spmv_d(c, c.p_d, c.q_d, true, false);
+        else if (vec64)
+            launch_spmv_fx(c, c.p_d, c.q_d, true, false);
+        else
+            launch_spmv_f(c, c.p_f, c.q_f, true, false);
+    };
+    cudaEvent_t a, b;
+    LPM_CUDA(cudaEventCreate(&a));
+    LPM_CUDA(cudaEventCreate(&b));
+    const int reps = 10;
+    auto time_it = [&](auto &&launch, double &ms) -> int {
+        for (int r = 0; r < 2; r++)
+            launch();
+        LPM_CUDA(cudaEventRecord(a, c.stream));
+        for (int r = 0; r < reps; r++)
+            launch();
+        LPM_CUDA(cudaEventRecord(b, c.stream));
+        LPM_CUDA(cudaEventSynchronize(b));
+        float f = 0.f;
+        LPM_CUDA(cudaEventElapsedTime(&f, a, b));
+        ms = f / reps;
+        return LPM_OK;
+    };
+    const Tune keep = c.tune;
+    const int grids[] = {2, 4, 8, 16};
+    Tune best = keep;
+    double best_ms = 1e30, def_ms = 0.0;
+    int rc = LPM_OK;
+    for (int v = 0; v < 4 && !rc; v++)
+        for (int g : grids) {
+            c.tune.spmv_variant = v;
+            c.tune.spmv_per_sm = g;
+            double ms = 0.0;
+            if ((rc = time_it(spmv, ms)))
+                break;
+            if (v == 0 && g == 8)
+                def_ms = ms;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best.spmv_variant = v;
+                best.spmv_per_sm = g;
+            }
+        }
+    double best_vec = 1e30;
+    for (int g : grids) {
+        if (rc)
+            break;
+        c.tune.vec_per_sm = g;
+        double ms = 0.0;
+        if ((rc = time_it([&]() { launch_norm2(c, c.p_d, 3); }, ms)))
+            break;
+        if (ms < best_vec) {
+            best_vec = ms;
+            best.vec_per_sm = g;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    c.time_spmv = timed;
+    if (rc) {
+        c.tune = keep;
+        return rc;
+    }
+    c.tune = best;
+    drop_graphs(c);
+    if (out) {
+        fill_tuning(c, out);
+        out->spmv_ms = best_ms;
+        out->spmv_ms_default = def_ms;
+    }
+    return sync(c);
 }
 
 int lpm_spmv_timing(lpm_ctx *ctx, double *avg_ms, long long *count, int reset)

@@ -99,6 +99,8 @@ struct BatchCg {
     double *partials = nullptr;     // [3][nseg]
     unsigned *counter = nullptr;
     int *all_done = nullptr;        // 1 once every specimen has stopped
+    int *act_chunk = nullptr;       // [nchunk] chunks holding a running specimen (any order)
+    int *n_act = nullptr;           // number of entries in act_chunk
 };
 
 // Host-side bookkeeping of a batch context.
@@ -118,8 +120,20 @@ struct BatchHost {
     int graph_chunk = 0, graph_k32 = -1;
 };
 
+// Launch shapes of the solver kernels, set by lpm_autotune or lpm_set_tuning.
+// spmv_variant: 0 = 16 lanes x 4 blocks per row chunk, 1 = 8 x 4, 2 = 32 x 2,
+// 3 = 4 x 4 (lanes per block row x consecutive blocks per lane).
+struct Tune {
+    int spmv_variant = 0;
+    int spmv_per_sm = 8;  // SpMV thread blocks per SM (grid-stride over rows)
+    int vec_per_sm = 8;   // PCG vector-kernel thread blocks per SM
+    int sms = 0;          // SM count of the device
+};
+constexpr int TUNE_MAX_PER_SM = 16;
+
 struct Ctx {
     int device = 0;
+    Tune tune;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int n = 0, nslip = 0, plmode = 0;
@@ -237,12 +251,16 @@ void launch_cg_iter_f(Ctx &c);
 void launch_axpy_refine(Ctx &c, double scale);  // x_d += x_f / scale
 void launch_norm2(Ctx &c, const dvec4 *v, int slot);
 int red_grid(const Ctx &c);
+int spmv_grid(const Ctx &c);
+int spmv_variant_lanes(int variant);
+int spmv_variant_blocks(int variant);
 // batched specimens (k_batch.cu)
 constexpr int BATCH_TPB = 256;  // particles per reduction chunk
 void launch_spmv_batch(Ctx &c, const dvec4 *x, dvec4 *y, bool k32);  // k_solve.cu
 void launch_refine_batch(Ctx &c, const dvec4 *x, const dvec4 *b, dvec4 *r);  // k_solve.cu
 void launch_bnorm(Ctx &c);                       // per-specimen norms -> c.bh.norms_d
 void launch_bcg_init(Ctx &c, const dvec4 *b);   // per-specimen PCG start (uses bcg.active, bcg.bscale)
+void launch_bcg_compact(Ctx &c);                // act_chunk = chunks of running specimens
 void launch_bcg_iter(Ctx &c, bool k32);         // one PCG iteration of every running specimen
 void launch_bcg_reliable(Ctx &c);               // true residual + residual replacement (FP32 matrix)
 void launch_bcg_finish(Ctx &c);                 // du = x / bscale

@@ -31,7 +31,7 @@ EXPORTED = [
     "lpm_apply_bc", "lpm_compute_force", "lpm_switch_state", "lpm_solve", "lpm_begin_step", "lpm_get",
     "lpm_set", "lpm_get_sizes", "lpm_export_upper_csr", "lpm_spmv", "lpm_solve_rhs", "lpm_spmv_timing",
     "lpm_spmv_bytes", "lpm_update_rr_noalloc", "lpm_setup_batch", "lpm_batch_offsets",
-    "lpm_batch_load_step",
+    "lpm_batch_load_step", "lpm_autotune", "lpm_set_tuning", "lpm_get_tuning",
 ]
 
 
@@ -51,6 +51,16 @@ class SolverOpts(C.Structure):
                 ("cg_rtol", C.c_double), ("cg_maxiter", C.c_int), ("inner_rtol", C.c_double),
                 ("refine_maxiter", C.c_int), ("check_every", C.c_int), ("use_graphs", C.c_int),
                 ("mixed_vectors", C.c_int)]
+
+
+class Tuning(C.Structure):
+    """lpm_tuning: launch shapes of the solve (include/lpm_gpu.h)."""
+    _fields_ = [("spmv_variant", C.c_int), ("spmv_lanes", C.c_int), ("spmv_blocks", C.c_int),
+                ("spmv_per_sm", C.c_int), ("cg_per_sm", C.c_int), ("spmv_ms", C.c_double),
+                ("spmv_ms_default", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class StepStats(C.Structure):
@@ -113,6 +123,9 @@ def load(path=LIB_PATH):
         "lpm_setup_batch": ([vp, C.c_int, C.c_double, C.c_int, dp], C.c_int),
         "lpm_batch_offsets": ([vp, ip], C.c_int),
         "lpm_batch_load_step": ([vp, C.c_int, C.POINTER(DispBC), C.POINTER(StepStats)], C.c_int),
+        "lpm_autotune": ([vp, C.POINTER(Tuning)], C.c_int),
+        "lpm_set_tuning": ([vp, C.POINTER(Tuning)], C.c_int),
+        "lpm_get_tuning": ([vp, C.POINTER(Tuning)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -205,6 +218,20 @@ class Specimen:
         st = (StepStats * ns)()
         self._check(self.L.lpm_batch_load_step(self.h, nbd, arr, st))
         return [x.as_dict() for x in st]
+
+    def autotune(self):
+        t = Tuning()
+        self._check(self.L.lpm_autotune(self.h, C.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, spmv_variant=0, spmv_per_sm=8, cg_per_sm=8):
+        t = Tuning(spmv_variant=spmv_variant, spmv_per_sm=spmv_per_sm, cg_per_sm=cg_per_sm)
+        self._check(self.L.lpm_set_tuning(self.h, C.byref(t)))
+
+    def get_tuning(self):
+        t = Tuning()
+        self._check(self.L.lpm_get_tuning(self.h, C.byref(t)))
+        return t.as_dict()
 
     def setup_particles(self, lattice, radius, xyz):
         xyz = np.ascontiguousarray(xyz, dtype=np.float64)
