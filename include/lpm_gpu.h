@@ -220,6 +220,52 @@ int lpm_batch_offsets(const lpm_ctx *ctx, int *offsets);
  * Force BCs are not supported in a batch. */
 int lpm_batch_load_step(lpm_ctx *ctx, int nbd, const lpm_disp_bc *dbc, lpm_step_stats *stats);
 
+/* ---- adjoint ------------------------------------------------------------------ */
+/* Gradients of a function of the reaction-force curve with respect to the
+ * per-particle material (E, nu, yield stress, hardening modulus) of a J2
+ * isotropic-hardening load path, as a forward/backward pair: forward runs the
+ * load steps and returns the curve, backward takes dL/dR per step and
+ * returns dL/d(material), like a torch.autograd.Function.  No counterpart in
+ * the reference (whose observable is writeReaction, src/data_handler.c:309-335:
+ * R_n = -sum over particles of type rtype of the internal force component
+ * rcomp after load step n). */
+typedef struct lpm_adjoint_opts {
+    int checkpoint_every; /* load steps between stored states (default 10); the
+                             backward run recomputes the steps in between */
+    int gmres_restart;    /* Krylov basis of the adjoint solve (default 30) */
+    int gmres_maxiter;    /* per load step (default 600) */
+    double gmres_rtol;    /* relative residual of the adjoint solve (default 1e-10) */
+} lpm_adjoint_opts;
+typedef struct lpm_adjoint_stats {
+    int steps, recomputed_steps, checkpoints;
+    int gmres_iters;       /* adjoint Krylov iterations of the backward run */
+    int cg_iters;          /* PCG iterations of the forward run */
+    int cg_iters_backward; /* PCG iterations of the backward run (preconditioner) */
+    int status;            /* LPM_STATUS_* bits of the forward run and the adjoint solves */
+    double ms_forward, ms_backward;
+} lpm_adjoint_stats;
+void lpm_default_adjoint_opts(lpm_adjoint_opts *opts);
+/* Sets the material from E, nu (C11, C12, C44 as src/lpmc_project.c:188-190),
+ * sigmay, H (n each; J2, isotropic hardening), initialises the state and runs
+ * nsteps load steps with bcs (nsteps x nbd, step-major).  R (may be NULL)
+ * receives the nsteps reactions.  The context's solver options apply; every
+ * step must take at least one Newton iteration. */
+int lpm_adjoint_forward(lpm_ctx *ctx, const double *E, const double *nu, const double *sigmay, const double *H,
+                        int nsteps, int nbd, const lpm_disp_bc *bcs, int rtype, int rcomp,
+                        const lpm_adjoint_opts *opts, double *R);
+/* dLdR: nsteps values.  Outputs (n each, any may be NULL): dL/dE, dL/dnu,
+ * dL/dsigmay, dL/dH.  The context is left at the end of the forward run. */
+int lpm_adjoint_backward(lpm_ctx *ctx, const double *dLdR, double *gE, double *gnu, double *gsy, double *gH,
+                         lpm_adjoint_stats *stats);
+/* Reverse mode of one J2 force evaluation (lpm_compute_force(ctx, LPM_PL_J2)
+ * made from the converged state, e.g. after lpm_switch_state(ctx, 0)):
+ * cotangents Pbar (3n) of the internal force, mu_dLp (n x nn) and mu_alpha (n)
+ * of the new plastic state (may be NULL) -> xbar (3n), dLp_bar (n x nn),
+ * alpha_bar (n), theta_bar (5 x n: C11, C12, C44, sigmay, H).  Outputs may be
+ * NULL.  Allocates its work space. */
+int lpm_force_vjp(lpm_ctx *ctx, const double *Pbar, const double *mu_dLp, const double *mu_alpha, double *xbar,
+                  double *dLp_bar, double *alpha_bar, double *theta_bar);
+
 /* ---- no-allocation entry point ----------------------------------------------- */
 /* No counterpart in the reference: an allocation-free form of the residual
  * update for callers that cannot call cudaMalloc (their device memory comes

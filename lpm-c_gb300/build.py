@@ -31,6 +31,8 @@ CU_UNITS = [
     ("k_solve.cu", []),
     ("lpm_api.cu", []),
     ("k_batch.cu", []),
+    ("k_adjoint.cu", ["-fmad=false"]),
+    ("adjoint.cu", []),
     ("k_noalloc.cu", []),
 ]
 CPP_UNITS = [("setup.cpp", ["-ffp-contract=off", "-fopenmp"])]

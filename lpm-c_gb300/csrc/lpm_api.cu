@@ -69,6 +69,7 @@ Ctx::~Ctx()
 {
     cudaSetDevice(device);
     free_batch(*this);
+    free_adjoint(*this);
     void **all[] = {(void **)&xyz, (void **)&xyz0, (void **)&xyz_temp, (void **)&Pin, (void **)&Pex,
                     (void **)&res, (void **)&du, (void **)&mask, (void **)&type, (void **)&G, (void **)&sy,
                     (void **)&Hh, (void **)&stress, (void **)&dlambda, (void **)&nbr, (void **)&shell,
@@ -114,7 +115,7 @@ Ctx::~Ctx()
 
 // ---- helpers -----------------------------------------------------------------
 
-static int sync(Ctx &c)
+int sync(Ctx &c)
 {
     cudaError_t e = cudaStreamSynchronize(c.stream);
     if (e != cudaSuccess)
@@ -151,7 +152,7 @@ static void copy_state(Ctx &c, int to, int from)
 }
 
 // switchStateV (src/constitutive.c:10-85)
-static void switch_state(Ctx &c, int flag)
+void switch_state(Ctx &c, int flag)
 {
     if (flag == 0)
         copy_state(c, 0, 1);
@@ -685,7 +686,7 @@ static int run_pcg(Ctx &c, int mode, int &iters, int &status)
 // true residual b - K32 x64 is recomputed with FP64 products and sums, and
 // replaces the FP32 residual; the search direction is kept, so CG keeps its
 // Krylov history.  Convergence is judged on the FP64 true residual.
-static int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
+int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
 {
     int rc;
     launch_norm2(c, b, 2);
@@ -777,7 +778,7 @@ static int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
     return LPM_OK;
 }
 
-static int assemble(Ctx &c)
+int assemble(Ctx &c)
 {
     const bool fp32 = c.opts.precision == LPM_PREC_MIXED;
     int rc;
@@ -791,13 +792,13 @@ static int assemble(Ctx &c)
     return LPM_OK;
 }
 
-static int prepare_preconditioner(Ctx &c)
+int prepare_preconditioner(Ctx &c)
 {
     launch_block_jacobi(c, c.opts.precision == LPM_PREC_MIXED);
     return LPM_OK;
 }
 
-static int force_eval(Ctx &c, int plmode)
+int force_eval(Ctx &c, int plmode)
 {
     switch (plmode) {
     case LPM_PL_PREDICTOR:

@@ -83,6 +83,8 @@ struct CgScalars {
     int it, done, maxit, upd_req;
 };
 
+struct AdjointState;
+
 // Per-specimen PCG state of a batch (device pointers, passed by value).
 // done: 0 running, 1 recursive residual met the tolerance, 2 iteration cap,
 // 3 non-finite, 5 specimen inactive (its Newton loop has converged),
@@ -214,6 +216,7 @@ struct Ctx {
     int nspec = 0;
     BatchCg bcg;
     BatchHost bh;
+    AdjointState *adj = nullptr;  // lpm_adjoint_forward / lpm_adjoint_backward
     ~Ctx();
 };
 
@@ -254,6 +257,37 @@ int red_grid(const Ctx &c);
 int spmv_grid(const Ctx &c);
 int spmv_variant_lanes(int variant);
 int spmv_variant_blocks(int variant);
+// host steps of the load-step loop (lpm_api.cu), shared with the adjoint
+int sync(Ctx &c);
+void switch_state(Ctx &c, int flag);
+int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st);  // K du = b (masked) -> c.du
+int assemble(Ctx &c);
+int prepare_preconditioner(Ctx &c);
+int force_eval(Ctx &c, int plmode);
+
+// adjoint (k_adjoint.cu): reverse mode of one J2 force evaluation
+struct AdjBuffers {
+    double *gx = nullptr, *gy = nullptr, *gz = nullptr;  // [NN][n] bond position cotangents
+    double *knbar = nullptr, *tvbar = nullptr;           // [NN][n]
+    double *Gbar = nullptr, *sybar = nullptr, *Hbar = nullptr;  // [n]
+    double *E = nullptr, *nu = nullptr;                  // [n] material of the forward run
+    double *gE = nullptr, *gnu = nullptr, *gsy = nullptr, *gH = nullptr;  // [n] accumulated
+    double *gC = nullptr;                                // [3][n] accumulated C11, C12, C44 (may be null)
+};
+struct AdjointState;
+void free_adjoint(Ctx &c);
+// reverse of the last J2 force evaluation (state read from slot 1, forward
+// results from F, dL, S, T): Pbar on the internal force, mu on the new state
+void adj_vjp(Ctx &c, const dvec4 *Pbar, const double *mu_dLp, const double *mu_alpha, double *dLp_bar,
+             double *alpha_bar, bool theta, AdjBuffers &w);
+// x-bar from the bond cotangents (masked: prescribed DOFs zeroed); theta:
+// add the material cotangents to w.gE .. w.gH
+void adj_gather(Ctx &c, dvec4 *xbar, bool masked, bool theta, AdjBuffers &w);
+void adj_dot(Ctx &c, const dvec4 *x, const dvec4 *y, double *out);          // out[0] = x.y
+void adj_axpby(Ctx &c, double alpha, const dvec4 *x, double beta, dvec4 *y); // y = a x + b y
+void adj_reaction(Ctx &c, int type, int comp, double *out);                   // -sum Pin over a type
+void adj_reaction_seed(Ctx &c, int type, int comp, double w, const dvec4 *lam, dvec4 *Pbar);
+
 // batched specimens (k_batch.cu)
 constexpr int BATCH_TPB = 256;  // particles per reduction chunk
 void launch_spmv_batch(Ctx &c, const dvec4 *x, dvec4 *y, bool k32);  // k_solve.cu

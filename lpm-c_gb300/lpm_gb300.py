@@ -32,6 +32,7 @@ EXPORTED = [
     "lpm_set", "lpm_get_sizes", "lpm_export_upper_csr", "lpm_spmv", "lpm_solve_rhs", "lpm_spmv_timing",
     "lpm_spmv_bytes", "lpm_update_rr_noalloc", "lpm_setup_batch", "lpm_batch_offsets",
     "lpm_batch_load_step", "lpm_autotune", "lpm_set_tuning", "lpm_get_tuning",
+    "lpm_default_adjoint_opts", "lpm_adjoint_forward", "lpm_adjoint_backward", "lpm_force_vjp",
 ]
 
 
@@ -58,6 +59,20 @@ class Tuning(C.Structure):
     _fields_ = [("spmv_variant", C.c_int), ("spmv_lanes", C.c_int), ("spmv_blocks", C.c_int),
                 ("spmv_per_sm", C.c_int), ("cg_per_sm", C.c_int), ("spmv_ms", C.c_double),
                 ("spmv_ms_default", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class AdjointOpts(C.Structure):
+    _fields_ = [("checkpoint_every", C.c_int), ("gmres_restart", C.c_int), ("gmres_maxiter", C.c_int),
+                ("gmres_rtol", C.c_double)]
+
+
+class AdjointStats(C.Structure):
+    _fields_ = [("steps", C.c_int), ("recomputed_steps", C.c_int), ("checkpoints", C.c_int),
+                ("gmres_iters", C.c_int), ("cg_iters", C.c_int), ("cg_iters_backward", C.c_int),
+                ("status", C.c_int), ("ms_forward", C.c_double), ("ms_backward", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -126,6 +141,11 @@ def load(path=LIB_PATH):
         "lpm_autotune": ([vp, C.POINTER(Tuning)], C.c_int),
         "lpm_set_tuning": ([vp, C.POINTER(Tuning)], C.c_int),
         "lpm_get_tuning": ([vp, C.POINTER(Tuning)], C.c_int),
+        "lpm_default_adjoint_opts": ([C.POINTER(AdjointOpts)], None),
+        "lpm_adjoint_forward": ([vp, dp, dp, dp, dp, C.c_int, C.c_int, C.POINTER(DispBC), C.c_int, C.c_int,
+                                 C.POINTER(AdjointOpts), dp], C.c_int),
+        "lpm_adjoint_backward": ([vp, dp, dp, dp, dp, dp, C.POINTER(AdjointStats)], C.c_int),
+        "lpm_force_vjp": ([vp, dp, dp, dp, dp, dp, dp, dp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -232,6 +252,45 @@ class Specimen:
         t = Tuning()
         self._check(self.L.lpm_get_tuning(self.h, C.byref(t)))
         return t.as_dict()
+
+    def adjoint_forward(self, E, nu, sigmay, H, step_bcs, rtype, rcomp, **opts):
+        """Run the load steps (one BC list per step) and return the reaction
+        curve; opts: checkpoint_every, gmres_restart, gmres_maxiter, gmres_rtol."""
+        o = AdjointOpts()
+        self.L.lpm_default_adjoint_opts(C.byref(o))
+        for k, v in opts.items():
+            setattr(o, k, v)
+        nsteps = len(step_bcs)
+        nbd = len(step_bcs[0]) if nsteps else 0
+        arr = (DispBC * max(1, nsteps * nbd))()
+        for s, bl in enumerate(step_bcs):
+            for k, (t, f, v) in enumerate(bl):
+                arr[s * nbd + k] = DispBC(int(t), f.encode() if isinstance(f, str) else f, float(v))
+        vals = [np.ascontiguousarray(np.broadcast_to(np.asarray(x, dtype=np.float64), (self.n,)))
+                for x in (E, nu, sigmay, H)]
+        R = np.zeros(nsteps)
+        comp = {"x": 0, "y": 1, "z": 2}.get(rcomp, rcomp)
+        self._check(self.L.lpm_adjoint_forward(self.h, *[_dp(v) for v in vals], nsteps, nbd, arr, int(rtype),
+                                               int(comp), C.byref(o), _dp(R)))
+        return R
+
+    def adjoint_backward(self, dLdR):
+        dLdR = np.ascontiguousarray(dLdR, dtype=np.float64)
+        out = [np.zeros(self.n) for _ in range(4)]
+        st = AdjointStats()
+        self._check(self.L.lpm_adjoint_backward(self.h, _dp(dLdR), *[_dp(o) for o in out], C.byref(st)))
+        return dict(E=out[0], nu=out[1], sigmay=out[2], H=out[3]), st.as_dict()
+
+    def force_vjp(self, Pbar, mu_dLp=None, mu_alpha=None):
+        Pbar = np.ascontiguousarray(Pbar, dtype=np.float64).reshape(-1)
+        mud = None if mu_dLp is None else _dp(np.ascontiguousarray(mu_dLp, dtype=np.float64))
+        mua = None if mu_alpha is None else _dp(np.ascontiguousarray(mu_alpha, dtype=np.float64))
+        xbar = np.zeros((self.n, 3))
+        dlp = np.zeros((self.n, self.nn))
+        ab = np.zeros(self.n)
+        th = np.zeros((5, self.n))
+        self._check(self.L.lpm_force_vjp(self.h, _dp(Pbar), mud, mua, _dp(xbar), _dp(dlp), _dp(ab), _dp(th)))
+        return xbar, dlp, ab, th
 
     def setup_particles(self, lattice, radius, xyz):
         xyz = np.ascontiguousarray(xyz, dtype=np.float64)

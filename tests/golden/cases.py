@@ -172,3 +172,78 @@ class BatchCase:
     def step_bcs(self):
         """Per-specimen BC lists of one load step."""
         return [sc_bcs(self.strain * h / self.steps) for h in self.heights]
+
+
+def splitmix64_uniform_np(seed, count):
+    """Vectorised splitmix64_uniform (same values)."""
+    k = np.arange(count, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        z = np.uint64((seed << 32) & ((1 << 64) - 1)) + k + np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return (z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+def gaussian_filter3(a, sigma):
+    """Separable Gaussian filter (truncated at 4 sigma, reflected edges)."""
+    r = int(4 * sigma + 0.5)
+    x = np.arange(-r, r + 1, dtype=np.float64)
+    k = np.exp(-0.5 * (x / sigma) ** 2)
+    k /= k.sum()
+    out = a
+    for ax in range(3):
+        pad = [(0, 0)] * 3
+        pad[ax] = (r, r)
+        p = np.pad(out, pad, mode="reflect")
+        acc = np.zeros_like(out)
+        for t in range(2 * r + 1):
+            sl = [slice(None)] * 3
+            sl[ax] = slice(t, t + out.shape[ax])
+            acc += k[t] * p[tuple(sl)]
+        out = acc
+    return out
+
+
+class NotchedPlate:
+    """SC notched plate (C5 at 200 x 10 x 200): loading along z, thickness
+    along y; a single-edge notch one particle layer wide at mid-height, cut
+    from the x = 0 edge `notch` particles deep through the thickness.
+    Per-particle E, nu, yield stress and H are smooth random fields
+    (Gaussian-filtered white noise, correlation length `corr` particles,
+    min-max scaled to +-amp about 200 GPa / 0.3 / 250 MPa / 2 GPa)."""
+
+    BASE = (200e3, 0.3, 250.0, 2000.0)
+
+    def __init__(self, nx=200, ny=10, nz=200, notch=40, radius=0.1, steps=60, strain=0.01, corr=10.0, amp=0.1,
+                 newton_tol=1e-8):
+        self.nx, self.ny, self.nz, self.notch = nx, ny, nz, notch
+        self.radius, self.lattice = radius, 2
+        h = 2.0 * radius
+        iz, iy, ix = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+        keep = ~((iz == nz // 2) & (ix < notch))
+        self.grid = np.stack([ix[keep], iy[keep], iz[keep]], axis=1)
+        self.xyz = self.grid.astype(np.float64) * h
+        self.height = (nz - 1) * h
+        self.steps, self.strain = steps, strain
+        self.schedule = [strain * self.height / steps] * steps
+        self.corr, self.amp = corr, amp
+        self.newton_tol = newton_tol
+
+    @property
+    def n(self):
+        return self.xyz.shape[0]
+
+    def fields(self, seed):
+        """E, nu, sigmay, H per particle for a seed."""
+        out = []
+        for k, base in enumerate(self.BASE):
+            w = splitmix64_uniform_np(seed * 16 + k, self.nx * self.ny * self.nz) - 0.5
+            g = gaussian_filter3(w.reshape(self.nz, self.ny, self.nx), self.corr)
+            g = 2.0 * (g - g.min()) / (g.max() - g.min()) - 1.0
+            v = g[self.grid[:, 2], self.grid[:, 1], self.grid[:, 0]]
+            out.append(base * (1.0 + self.amp * v))
+        return out
+
+    def step_bcs(self):
+        return [sc_bcs(s) for s in self.schedule]
