@@ -74,6 +74,8 @@ typedef struct {
     int check_every;    /* PCG iterations between host convergence checks (graph chunk) */
     int use_graphs;     /* capture PCG chunks as CUDA graphs */
     int mixed_vectors;  /* mixed: 32 = FP32 CG vectors, 64 = FP64 CG vectors (FP32 stiffness and products) */
+    int newton_accel;   /* 0: modified Newton as the reference (u += K^-1 r); m > 0: the same
+                           fixed-point iteration with Anderson acceleration of depth m (<= 16) */
 } lpm_solver_opts;
 
 typedef struct {

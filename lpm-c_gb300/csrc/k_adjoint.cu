@@ -1,5 +1,6 @@
 // Reverse mode of one J2 force evaluation (plmode 0 with isotropic hardening)
-// and the vector kernels of the adjoint solve.
+// and the vector kernels of the adjoint solve and of the Anderson-accelerated
+// Newton loop.
 //
 // The force evaluation maps (positions u, converged state q = (dLp, alpha),
 // material theta = per-particle C11, C12, C44 via Kn/Tv and G = C44, yield
@@ -418,6 +419,30 @@ __global__ void __launch_bounds__(RTPB) k_dot(int n, const dvec4 *x, const dvec4
     adj_grid_sum<1>(v, partials, counter, out);
 }
 
+// out[k] = <A_k, w> for k < K (K <= 16), one pass over w
+struct MultiDot {
+    const dvec4 *A[16];
+    int K;
+};
+__global__ void __launch_bounds__(RTPB) k_multidot(int n, MultiDot md, const dvec4 *w, double *partials,
+                                                   unsigned *counter, double *out)
+{
+    double v[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++)
+        v[k] = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const dvec4 b = w[i];
+#pragma unroll
+        for (int k = 0; k < 16; k++)
+            if (k < md.K) {
+                const dvec4 a = md.A[k][i];
+                v[k] += a.x * b.x + a.y * b.y + a.z * b.z;
+            }
+    }
+    adj_grid_sum<16>(v, partials, counter, out);
+}
+
 // y = a x + b y
 __global__ void k_axpby(int n, double alpha, const dvec4 *x, double beta, dvec4 *y)
 {
@@ -540,6 +565,17 @@ void adj_gather(Ctx &c, dvec4 *xbar, bool masked, bool theta, AdjBuffers &w)
 void adj_dot(Ctx &c, const dvec4 *x, const dvec4 *y, double *out)
 {
     k_dot<<<red_grid(c), RTPB, 0, c.stream>>>(c.n, x, y, c.partials, c.counter, out);
+}
+
+void adj_multidot(Ctx &c, int K, const dvec4 *const *A, const dvec4 *w, double *out)
+{
+    MultiDot md;
+    md.K = K;
+    for (int k = 0; k < 16; k++)
+        md.A[k] = k < K ? A[k] : w;
+    const int sms = c.tune.sms > 0 ? c.tune.sms : 152;
+    // 16 partials per block must fit the reduction buffer (sized for 16 blocks per SM x 4)
+    k_multidot<<<2 * sms, RTPB, 0, c.stream>>>(c.n, md, w, c.partials, c.counter, out);
 }
 
 void adj_axpby(Ctx &c, double alpha, const dvec4 *x, double beta, dvec4 *y)

@@ -65,11 +65,24 @@ static void free_batch(Ctx &c)
     c.nspec = 0;
 }
 
+static void free_anderson(Ctx &c)
+{
+    dfree(c.acc.dU);
+    dfree(c.acc.dF);
+    dfree(c.acc.u_prev);
+    dfree(c.acc.f_prev);
+    dfree(c.acc.dots);
+    if (c.acc.dots_h)
+        cudaFreeHost(c.acc.dots_h);
+    c.acc = Ctx::Anderson();
+}
+
 Ctx::~Ctx()
 {
     cudaSetDevice(device);
     free_batch(*this);
     free_adjoint(*this);
+    free_anderson(*this);
     void **all[] = {(void **)&xyz, (void **)&xyz0, (void **)&xyz_temp, (void **)&Pin, (void **)&Pex,
                     (void **)&res, (void **)&du, (void **)&mask, (void **)&type, (void **)&G, (void **)&sy,
                     (void **)&Hh, (void **)&stress, (void **)&dlambda, (void **)&nbr, (void **)&shell,
@@ -337,6 +350,7 @@ void lpm_default_solver_opts(lpm_solver_opts *o)
     o->check_every = 16;
     o->use_graphs = 1;
     o->mixed_vectors = 32;
+    o->newton_accel = 0;
 }
 
 int lpm_create(lpm_ctx **out, int device)
@@ -398,7 +412,8 @@ int lpm_set_solver(lpm_ctx *ctx, const lpm_solver_opts *o)
         return fail(LPM_ERR_ARG, "null argument");
     if (o->precision != LPM_PREC_FP64 && o->precision != LPM_PREC_MIXED)
         return fail(LPM_ERR_ARG, "unknown precision");
-    if (!(o->cg_rtol > 0) || o->cg_maxiter <= 0 || o->newton_maxiter < 0 || o->check_every <= 0)
+    if (!(o->cg_rtol > 0) || o->cg_maxiter <= 0 || o->newton_maxiter < 0 || o->check_every <= 0 ||
+        o->newton_accel < 0 || o->newton_accel > 16)
         return fail(LPM_ERR_ARG, "invalid solver options");
     Ctx &c = ctx->c;
     const bool prec_change = c.opts.precision != o->precision;
@@ -961,6 +976,134 @@ int lpm_solve_rhs(lpm_ctx *ctx, const double *b, double *x, lpm_step_stats *st)
     return download_particles(c, c.du, x);
 }
 
+}  // extern "C"
+
+namespace lpm {
+
+// Anderson acceleration of the modified-Newton fixed point u <- u + K^-1 r(u)
+// (Walker & Ni, SIAM J. Numer. Anal. 49 (2011), type II, mixing 1): with
+// f_k = K^-1 r(u_k) and the last h differences dF_j = f_{j+1} - f_j,
+// dU_j = u_{j+1} - u_j, gamma = argmin |f_k - dF gamma| and
+// u_{k+1} = u_k + f_k - sum_j gamma_j (dU_j + dF_j).
+struct AndersonRun {
+    int m = 0, hist = 0, head = 0;
+    bool have_prev = false;
+    std::vector<double> G;  // Gram matrix of the stored dF, m x m
+};
+
+static int anderson_prepare(Ctx &c, int m)
+{
+    Ctx::Anderson &A = c.acc;
+    if (A.m == m && A.dU)
+        return LPM_OK;
+    free_anderson(c);
+    int rc;
+    const size_t n = c.n;
+    if ((rc = dalloc(A.dU, m * n)) || (rc = dalloc(A.dF, m * n)) || (rc = dalloc(A.u_prev, n)) ||
+        (rc = dalloc(A.f_prev, n)) || (rc = dalloc(A.dots, 16)))
+        return rc;
+    LPM_CUDA(cudaMallocHost((void **)&A.dots_h, 16 * sizeof(double)));
+    A.m = m;
+    return LPM_OK;
+}
+
+// small SPD solve (Cholesky) of (G + reg I) x = b, h <= 16; false if not SPD
+static bool spd_solve(std::vector<double> G, int h, int ld, std::vector<double> &x)
+{
+    double dmax = 0.0;
+    for (int i = 0; i < h; i++)
+        dmax = std::max(dmax, G[(size_t)i * ld + i]);
+    if (!(dmax > 0.0))
+        return false;
+    for (int i = 0; i < h; i++)
+        G[(size_t)i * ld + i] += 1e-12 * dmax;
+    std::vector<double> L((size_t)h * h, 0.0);
+    for (int i = 0; i < h; i++)
+        for (int j = 0; j <= i; j++) {
+            double s = G[(size_t)i * ld + j];
+            for (int k = 0; k < j; k++)
+                s -= L[(size_t)i * h + k] * L[(size_t)j * h + k];
+            if (i == j) {
+                if (!(s > 0.0))
+                    return false;
+                L[(size_t)i * h + i] = std::sqrt(s);
+            } else {
+                L[(size_t)i * h + j] = s / L[(size_t)j * h + j];
+            }
+        }
+    for (int i = 0; i < h; i++) {
+        double s = x[i];
+        for (int k = 0; k < i; k++)
+            s -= L[(size_t)i * h + k] * x[k];
+        x[i] = s / L[(size_t)i * h + i];
+    }
+    for (int i = h - 1; i >= 0; i--) {
+        double s = x[i];
+        for (int k = i + 1; k < h; k++)
+            s -= L[(size_t)k * h + i] * x[k];
+        x[i] = s / L[(size_t)i * h + i];
+    }
+    return true;
+}
+
+// apply the step from c.du (= f_k) at c.xyz (= u_k)
+static int anderson_step(Ctx &c, AndersonRun &R)
+{
+    Ctx::Anderson &A = c.acc;
+    const size_t n = c.n;
+    const int m = R.m;
+    auto dU = [&](int j) { return A.dU + (size_t)j * n; };
+    auto dF = [&](int j) { return A.dF + (size_t)j * n; };
+    if (R.have_prev) {
+        const int slot = R.head;
+        R.head = (R.head + 1) % m;
+        R.hist = std::min(R.hist + 1, m);
+        LPM_CUDA(cudaMemcpyAsync(dF(slot), c.du, n * sizeof(dvec4), cudaMemcpyDeviceToDevice, c.stream));
+        adj_axpby(c, -1.0, A.f_prev, 1.0, dF(slot));
+        LPM_CUDA(cudaMemcpyAsync(dU(slot), c.xyz, n * sizeof(dvec4), cudaMemcpyDeviceToDevice, c.stream));
+        adj_axpby(c, -1.0, A.u_prev, 1.0, dU(slot));
+        std::vector<const dvec4 *> ptr(R.hist);
+        for (int j = 0; j < R.hist; j++)
+            ptr[j] = dF(j);
+        adj_multidot(c, R.hist, ptr.data(), dF(slot), A.dots);
+        LPM_CUDA(cudaMemcpyAsync(A.dots_h, A.dots, R.hist * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        int rc = sync(c);
+        if (rc)
+            return rc;
+        for (int j = 0; j < R.hist; j++)
+            R.G[(size_t)slot * m + j] = R.G[(size_t)j * m + slot] = A.dots_h[j];
+    }
+    LPM_CUDA(cudaMemcpyAsync(A.u_prev, c.xyz, n * sizeof(dvec4), cudaMemcpyDeviceToDevice, c.stream));
+    LPM_CUDA(cudaMemcpyAsync(A.f_prev, c.du, n * sizeof(dvec4), cudaMemcpyDeviceToDevice, c.stream));
+    R.have_prev = true;
+    adj_axpby(c, 1.0, c.du, 1.0, c.xyz);
+    if (R.hist == 0)
+        return LPM_OK;
+    std::vector<const dvec4 *> ptr(R.hist);
+    for (int j = 0; j < R.hist; j++)
+        ptr[j] = dF(j);
+    adj_multidot(c, R.hist, ptr.data(), c.du, A.dots);
+    LPM_CUDA(cudaMemcpyAsync(A.dots_h, A.dots, R.hist * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    int rc = sync(c);
+    if (rc)
+        return rc;
+    std::vector<double> g(A.dots_h, A.dots_h + R.hist);
+    if (!spd_solve(R.G, R.hist, m, g)) {  // degenerate history: plain step, restart
+        R.hist = 0;
+        R.head = 0;
+        return LPM_OK;
+    }
+    for (int j = 0; j < R.hist; j++) {
+        adj_axpby(c, -g[j], dU(j), 1.0, c.xyz);
+        adj_axpby(c, -g[j], dF(j), 1.0, c.xyz);
+    }
+    return LPM_OK;
+}
+
+}  // namespace lpm
+
+extern "C" {
+
 int lpm_load_step(lpm_ctx *ctx, int nbd, const lpm_disp_bc *dbc, int nbf, const lpm_force_bc *fbc,
                   lpm_step_stats *stats)
 {
@@ -993,6 +1136,14 @@ int lpm_load_step(lpm_ctx *ctx, int nbd, const lpm_disp_bc *dbc, int nbf, const 
     st.res0 = res;
     st.reac0 = reac;
     int ni = 0;
+    AndersonRun ar;
+    if (c.opts.newton_accel > 0) {
+        if ((rc = anderson_prepare(c, c.opts.newton_accel)))
+            return rc;
+        ar.m = c.opts.newton_accel;
+        ar.G.assign((size_t)ar.m * ar.m, 0.0);
+    }
+    double res_best = res;
     while (res > c.opts.newton_tol * tolm && ni < c.opts.newton_maxiter) {  // :424
         if (!std::isfinite(res)) {
             st.status |= LPM_STATUS_NAN;
@@ -1003,7 +1154,12 @@ int lpm_load_step(lpm_ctx *ctx, int nbd, const lpm_disp_bc *dbc, int nbf, const 
             Timer t(c.stream);
             if ((rc = solve_device(c, c.res, &st)))  // :449 solverCG
                 return rc;
-            launch_add_du(c);
+            if (ar.m > 0) {
+                if ((rc = anderson_step(c, ar)))
+                    return rc;
+            } else {
+                launch_add_du(c);
+            }
             st.ms_solve += t.stop();
         }
         {
@@ -1012,6 +1168,11 @@ int lpm_load_step(lpm_ctx *ctx, int nbd, const lpm_disp_bc *dbc, int nbf, const 
                 return rc;
             st.ms_force += t.stop();
         }
+        if (ar.m > 0 && res > 10.0 * res_best) {  // safeguard: drop the history
+            ar.hist = 0;
+            ar.head = 0;
+        }
+        res_best = std::min(res_best, res);
         ni++;
     }
     if (ni >= c.opts.newton_maxiter && res > c.opts.newton_tol * tolm)

@@ -217,6 +217,13 @@ struct Ctx {
     BatchCg bcg;
     BatchHost bh;
     AdjointState *adj = nullptr;  // lpm_adjoint_forward / lpm_adjoint_backward
+    // Anderson acceleration of the Newton loop (opts.newton_accel)
+    struct Anderson {
+        int m = 0;
+        dvec4 *dU = nullptr, *dF = nullptr;      // m difference vectors each
+        dvec4 *u_prev = nullptr, *f_prev = nullptr;
+        double *dots = nullptr, *dots_h = nullptr;
+    } acc;
     ~Ctx();
 };
 
@@ -285,6 +292,7 @@ void adj_vjp(Ctx &c, const dvec4 *Pbar, const double *mu_dLp, const double *mu_a
 void adj_gather(Ctx &c, dvec4 *xbar, bool masked, bool theta, AdjBuffers &w);
 void adj_dot(Ctx &c, const dvec4 *x, const dvec4 *y, double *out);          // out[0] = x.y
 void adj_axpby(Ctx &c, double alpha, const dvec4 *x, double beta, dvec4 *y); // y = a x + b y
+void adj_multidot(Ctx &c, int K, const dvec4 *const *A, const dvec4 *w, double *out);  // out[k] = A_k.w, K <= 16
 void adj_reaction(Ctx &c, int type, int comp, double *out);                   // -sum Pin over a type
 void adj_reaction_seed(Ctx &c, int type, int comp, double w, const dvec4 *lam, dvec4 *Pbar);
 
