@@ -456,6 +456,142 @@ def run_batch(args):
     print(json.dumps(line))
 
 
+def run_adjoint(args):
+    """Differentiation workload: SC notched plate nx x 10 x nz (200 x 10 x 200:
+    399,600 particles), single-edge notch 40 particles deep, smooth random
+    per-particle E, nu, yield stress and H (Gaussian-filtered noise,
+    correlation length 10 particles, +-10%, seed 1), 60 displacement steps to
+    1% strain; loss = sum_n (R_n - R*_n)^2 with R* from the seed-2 fields.
+    Times the forward run and the adjoint backward run (checkpoints every 10
+    steps, recomputed), FP64, and checks one directional derivative per field
+    against central differences (h = 1e-5 relative, two extra forward runs
+    each) when --adj-fd is given."""
+    import torch
+    import lpm_gb300 as G
+    torch.cuda.set_device(0)
+    plate = cases.NotchedPlate(nx=args.plate_n, ny=10, nz=args.plate_n, notch=max(1, args.plate_n // 5),
+                               steps=args.adj_steps, strain=args.adj_strain, corr=10.0)
+    solver = dict(precision=G.PREC_FP64, newton_tol=args.adj_newton_tol, newton_maxiter=2000, cg_rtol=1e-12,
+                  cg_maxiter=200000, newton_accel=8)
+    bcs = plate.step_bcs()
+
+    def specimen():
+        s = G.Specimen(0)
+        s.setup_particles(plate.lattice, plate.radius, plate.xyz)
+        s.set_types(cases.sc_types(s.get("xyz"), s.get("nb"), plate.radius))
+        s.set_solver(**solver)
+        return s
+
+    f1, f2 = plate.fields(1), plate.fields(2)
+    s = specimen()
+    target = s.adjoint_forward(*f2, bcs, cases.T_TOP, "z")
+    s.close()
+    s = specimen()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    t0 = time.perf_counter()
+    R = s.adjoint_forward(*f1, bcs, cases.T_TOP, "z", checkpoint_every=10)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    grads, st = s.adjoint_backward(2.0 * (R - target))
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    ck = clocks.stop()
+    s.close()
+    L = float(((R - target) ** 2).sum())
+    fd = {}
+    if args.adj_fd:
+        names = ["E", "nu", "sigmay", "H"]
+        for k in range(4):
+            d = f1[k] * plate.fields(7 + k)[k] / plate.BASE[k]
+            h = 1e-5
+            Ls = []
+            for sgn in (1.0, -1.0):
+                f = [x.copy() for x in f1]
+                f[k] = f1[k] + sgn * h * d
+                t = specimen()
+                Rp = t.adjoint_forward(*f, bcs, cases.T_TOP, "z")
+                t.close()
+                Ls.append(float(((Rp - target) ** 2).sum()))
+            g_fd = (Ls[0] - Ls[1]) / (2 * h)
+            g_ad = float((grads[names[k]] * d).sum())
+            fd[names[k]] = {"adjoint": g_ad, "central_fd": g_fd, "rel_err": abs(g_fd - g_ad) / abs(g_ad)}
+    line = {
+        "metric": "adjoint gradient of a reaction-misfit loss: forward + backward seconds",
+        "value": t2 - t0, "unit": "s", "n_gpus": 1, "steps": plate.steps, "warmup": 0,
+        "higher_is_better": False, "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random fields)",
+        "config": {"workload": f"SC notched plate {plate.nx}x{plate.ny}x{plate.nz}, notch {plate.notch}, "
+                               f"{plate.steps} steps to {100 * plate.strain:g}% strain, loss vs seed-2 curve",
+                   "particles": plate.n, "forward_s": t1 - t0, "backward_s": t2 - t1, "loss": L,
+                   "adjoint_stats": st, "newton_tol": args.adj_newton_tol, "newton_accel": 8,
+                   "checkpoint_every": 10, "fd_checks": fd},
+        "clocks": ck, "e2e": None, "cpu_baseline": None,
+    }
+    print(json.dumps(line))
+
+
+def run_fcc(args):
+    """Crystal plasticity: FCC single crystal ncell^3 cells (80^3: 2,048,000
+    particles), Al elastic constants, 24 signed {111}<110> systems, tau0 =
+    50 MPa, linear hardening h0 = 500 MPa, [001] tension to 2% in 100 steps.
+    Times load steps W+1..W+K on the mixed path and on the FP64 path and
+    reports the displacement difference between them."""
+    import torch
+    import lpm_gb300 as G
+    torch.cuda.set_device(0)
+    case = cases.FCCCase(ncell=args.fcc_cells)
+    W, K = args.fcc_warmup, args.steps
+    stream = torch.cuda.current_stream()
+    out = {}
+    for name, prec in (("mixed", G.PREC_MIXED), ("fp64", G.PREC_FP64)):
+        t0 = time.perf_counter()
+        s = G.Specimen(0)
+        s.set_stream(stream.cuda_stream)
+        n = s.setup_lattice(case.lattice, case.radius, case.box)
+        s.set_types(cases.sc_types(s.get("xyz"), s.get("nb"), case.radius))
+        s.set_cp(*case.cp)
+        s.set_material(case.C11, case.C12, case.C44, 0.0, 0.0, 0.0, G.PL_CP)
+        s.init_state()
+        s.set_solver(precision=prec, newton_tol=case.newton_tol, newton_maxiter=300, cg_rtol=1e-10,
+                     cg_maxiter=200000)
+        setup_s = time.perf_counter() - t0
+        for k in range(W):
+            s.load_step(cases.sc_bcs(case.schedule[k]))
+            if k == 0:
+                s.autotune()
+        torch.cuda.synchronize()
+        clocks = ClockSampler(0)
+        clocks.start()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        stats = [s.load_step(cases.sc_bcs(case.schedule[k])) for k in range(W, W + K)]
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        out[name] = dict(ms=ev0.elapsed_time(ev1), stats=stats, clocks=clocks.stop(), n=n, setup_s=setup_s,
+                         du=s.get("xyz") - s.get("xyz_initial"), A=s.get("cp_A"))
+        s.close()
+    m, f = out["mixed"], out["fp64"]
+    value = K / (m["ms"] / 1e3)
+    err = float(np.abs(m["du"] - f["du"]).max() / np.abs(f["du"]).max())
+    agg = lambda st, key: int(sum(x[key] for x in st))  # noqa: E731
+    line = {
+        "metric": "load steps/s, FCC crystal plasticity, mixed vs FP64 GPU",
+        "value": value, "unit": "load steps/s", "n_gpus": 1, "steps": K, "warmup": W, "ms_per_step": m["ms"] / K,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 stiffness/SpMV/PCG + f64 residual, reliable updates and CP return map",
+        "data": "synthetic (FCC lattice)",
+        "config": {"workload": f"FCC {args.fcc_cells}^3 cells CP [001] tension, load steps {W + 1}-{W + K} of 100",
+                   "particles": m["n"], "setup_s": m["setup_s"], "fp64_steps_per_s": K / (f["ms"] / 1e3),
+                   "mixed_over_fp64": f["ms"] / m["ms"], "disp_err_mixed_vs_fp64": err,
+                   "newton_iters": agg(m["stats"], "newton_iters"), "cg_iters": agg(m["stats"], "cg_iters"),
+                   "fp64_newton_iters": agg(f["stats"], "newton_iters"), "fp64_cg_iters": agg(f["stats"], "cg_iters"),
+                   "max_cp_A": float(m["A"].max())},
+        "clocks": m["clocks"], "e2e": None, "cpu_baseline": None,
+    }
+    print(json.dumps(line))
+
+
 def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
@@ -481,9 +617,18 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--workload", default="sc", choices=["sc", "batch"],
-                    help="sc: the 1M-particle SC cyclic case (default); batch: 256 specimens")
+    ap.add_argument("--workload", default="sc", choices=["sc", "batch", "adjoint", "fcc"],
+                    help="sc: the 1M-particle SC cyclic case (default); batch: 256 specimens; "
+                         "adjoint: gradients on the notched plate; fcc: crystal plasticity")
+    ap.add_argument("--fcc-cells", type=int, default=80)
+    ap.add_argument("--fcc-warmup", type=int, default=1,
+                    help="warm-up load steps of the fcc workload (its steps are long)")
+    ap.add_argument("--adj-strain", type=float, default=0.01)
     ap.add_argument("--nspec", type=int, default=256)
+    ap.add_argument("--plate-n", type=int, default=200)
+    ap.add_argument("--adj-steps", type=int, default=60)
+    ap.add_argument("--adj-newton-tol", type=float, default=1e-10)
+    ap.add_argument("--adj-fd", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -491,6 +636,10 @@ def main():
         run_reference(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "adjoint":
+        run_adjoint(args)
+    elif args.workload == "fcc":
+        run_fcc(args)
     else:
         run_ours(args)
 
