@@ -50,6 +50,20 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(value, device=None):
+    """Max of a per-rank float over the process group (identity on one rank)."""
+    try:
+        import torch
+        import torch.distributed as dist
+    except Exception:
+        return value
+    if not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+        return value
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -164,11 +178,7 @@ def run_ours(args):
         ms = ev0.elapsed_time(ev1)
         ck = clocks.stop()
         spmv_ms, spmv_cnt = s.spmv_timing(reset=3)
-        if world > 1:
-            import torch.distributed as dist
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(ms, device="cuda")
         results[prec_name] = dict(ms=ms, stats=stats, spmv_ms=spmv_ms, spmv_cnt=spmv_cnt, clocks=ck, tuning=tuning,
                                   spmv_bytes=s.spmv_bytes(prec), xyz=s.get("xyz"), x0=s.get("xyz_initial"),
                                   n=s.n, nnzb=s.sizes()["nnz_blocks"])
