@@ -73,7 +73,9 @@ typedef struct {
     int refine_maxiter; /* mixed: cap on FP64 reliable updates per solve */
     int check_every;    /* PCG iterations between host convergence checks (graph chunk) */
     int use_graphs;     /* capture PCG chunks as CUDA graphs */
-    int mixed_vectors;  /* mixed: 32 = FP32 CG vectors, 64 = FP64 CG vectors (FP32 stiffness and products) */
+    int mixed_vectors;  /* mixed: 32 = FP32 CG vectors, 64 = FP64 CG vectors (FP32 stiffness and products);
+                           with 32, a solve whose FP32 iteration stagnates is redone with FP64
+                           vectors, and so are the context's later solves */
     int newton_accel;   /* 0: modified Newton as the reference (u += K^-1 r); m > 0: the same
                            fixed-point iteration with Anderson acceleration of depth m (<= 16) */
 } lpm_solver_opts;

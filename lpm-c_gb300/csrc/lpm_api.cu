@@ -418,6 +418,7 @@ int lpm_set_solver(lpm_ctx *ctx, const lpm_solver_opts *o)
     Ctx &c = ctx->c;
     const bool prec_change = c.opts.precision != o->precision;
     c.opts = *o;
+    c.vec64_fallback = false;
     if (prec_change)
         c.have_K = false;
     if (c.graph_fp64) {
@@ -717,7 +718,7 @@ int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
     }
     const double scale = 1.0 / bn;
     const double delta = c.opts.inner_rtol;
-    if (c.opts.precision == LPM_PREC_MIXED && c.opts.mixed_vectors == 64) {
+    if (c.opts.precision == LPM_PREC_MIXED && (c.opts.mixed_vectors == 64 || c.vec64_fallback)) {
         // FP32 stiffness and products, FP64 vectors (x in units of |b|);
         // reliable updates replace r by s b - K32 x computed with FP64 sums
         launch_cg_init_fx(c, b, scale, delta * delta);
@@ -767,6 +768,8 @@ int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
     launch_cg_init_f(c, b, scale, c.opts.cg_rtol, delta * delta);
     int sweeps = 0, it = 0, done = 0;
     double rn = bn;
+    std::vector<double> hist;  // true residual after each reliable update
+    bool stagnated = false;
     for (;;) {
         if ((rc = run_pcg(c, PCG_FP32, it, done)))
             return rc;
@@ -777,18 +780,31 @@ int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
             return rc;
         rn = std::sqrt(c.norms_host[2]);
         sweeps++;
-        if (rn <= c.opts.cg_rtol * bn || done == 2 || done == 3 || !std::isfinite(rn) ||
-            sweeps >= c.opts.refine_maxiter)
+        hist.push_back(rn);
+        if (rn <= c.opts.cg_rtol * bn || done == 3 || !std::isfinite(rn) || sweeps >= c.opts.refine_maxiter)
             break;
+        // FP32 vectors stagnate on very ill-conditioned systems: a healthy
+        // sweep cuts the true residual by about inner_rtol, so three sweeps
+        // that do not halve it (or the FP32 iteration cap) mean stagnation
+        if (done == 2 || (sweeps > 3 && rn > 0.5 * hist[sweeps - 4])) {
+            stagnated = true;
+            break;
+        }
         launch_reliable(c, c.r_d, scale);
     }
     if (st) {
         st->cg_iters += it;
         st->spmv_calls += it + sweeps;
         st->refine_iters += sweeps;
-        if (rn > c.opts.cg_rtol * bn)
-            st->status |= std::isfinite(rn) ? LPM_STATUS_CG_MAXIT : LPM_STATUS_NAN;
     }
+    if (stagnated) {
+        // redo this solve, and the context's later ones, with FP64 vectors
+        // (the FP32 stiffness and products stay)
+        c.vec64_fallback = true;
+        return solve_device(c, b, st);
+    }
+    if (st && rn > c.opts.cg_rtol * bn)
+        st->status |= std::isfinite(rn) ? LPM_STATUS_CG_MAXIT : LPM_STATUS_NAN;
     LPM_CUDA(cudaMemcpyAsync(c.du, c.x_d, sizeof(dvec4) * c.n, cudaMemcpyDeviceToDevice, c.stream));
     return LPM_OK;
 }
@@ -1821,7 +1837,7 @@ int lpm_autotune(lpm_ctx *ctx, lpm_tuning *out)
         return fail(LPM_ERR_ARG, "lpm_autotune: assemble the stiffness first");
     Ctx &c = ctx->c;
     const bool k32 = c.opts.precision == LPM_PREC_MIXED;
-    const bool vec64 = !k32 || c.nspec > 0 || c.opts.mixed_vectors == 64;
+    const bool vec64 = !k32 || c.nspec > 0 || c.opts.mixed_vectors == 64 || c.vec64_fallback;
     const bool timed = c.time_spmv;
     c.time_spmv = false;
     auto spmv = [&]() {

@@ -212,6 +212,7 @@ struct Ctx {
     int graph_chunk = 0, graph_mode = -1;
     bool graph_timed = false;
     bool time_this = false;  // the next SpMV launch carries the timing events
+    bool vec64_fallback = false;  // mixed: FP32-vector PCG stagnated, use FP64 vectors
     // batched specimens (lpm_setup_batch); nspec == 0 for a single specimen
     int nspec = 0;
     BatchCg bcg;
