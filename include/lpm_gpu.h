@@ -270,6 +270,32 @@ int lpm_adjoint_backward(lpm_ctx *ctx, const double *dLdR, double *gE, double *g
 int lpm_force_vjp(lpm_ctx *ctx, const double *Pbar, const double *mu_dLp, const double *mu_alpha, double *xbar,
                   double *dLp_bar, double *alpha_bar, double *theta_bar);
 
+/* ---- output in the reference's file formats ---------------------------------- */
+/* writeDump (src/data_handler.c:42-85, LAMMPS dump; J2 or crystal-plasticity
+ * columns by the context's plmode; damage columns are 0), writeDisp (:278-306),
+ * writeReaction (:309-335), writeStress (:110-135): same text, byte for byte,
+ * for the same data.  flag 's' starts the dump file, anything else appends.
+ * lpm_write_dump copies the device arrays into pinned memory on the context's
+ * stream and writes the file on a host thread (the next load step may run
+ * meanwhile); lpm_write_wait joins it and reports its error.  The other
+ * writers are synchronous. */
+int lpm_write_dump(lpm_ctx *ctx, const char *path, int step, char flag, const double box[6]);
+int lpm_write_wait(lpm_ctx *ctx);
+int lpm_write_disp(lpm_ctx *ctx, const char *path, char c, int t1, int tstep);
+int lpm_write_reaction(lpm_ctx *ctx, const char *path, char c, int t1, int tstep);
+int lpm_write_stress(lpm_ctx *ctx, const char *path, int t1, int tstep);
+/* The same formats from host arrays in the reference's per-particle layout
+ * (xyz n x 3, stress n x 6 as s11 s22 s33 s23 s13 s12, bond arrays n x nn;
+ * plmode 1 reads cp_As (n x nslip) and cp_A, otherwise alpha). */
+int lpm_format_dump(const char *path, int step, char flag, int n, const double box[6], int plmode, const int *type,
+                    const double *xyz, const double *xyz0, const double *stress, const double *alpha,
+                    const int *pl_flag, const double *cp_As, int nslip, const double *cp_A);
+int lpm_format_disp(const char *path, char c, int t1, int tstep, int n, const int *type, const double *xyz,
+                    const double *xyz0);
+int lpm_format_reaction(const char *path, char c, int t1, int tstep, int n, int nn, const int *type, const int *nb,
+                        const double *csx, const double *csy, const double *csz, const double *F);
+int lpm_format_stress(const char *path, int t1, int tstep, int n, const int *type, const double *stress);
+
 /* ---- no-allocation entry point ----------------------------------------------- */
 /* No counterpart in the reference: an allocation-free form of the residual
  * update for callers that cannot call cudaMalloc (their device memory comes

@@ -35,7 +35,7 @@ CU_UNITS = [
     ("adjoint.cu", []),
     ("k_noalloc.cu", []),
 ]
-CPP_UNITS = [("setup.cpp", ["-ffp-contract=off", "-fopenmp"])]
+CPP_UNITS = [("setup.cpp", ["-ffp-contract=off", "-fopenmp"]), ("output.cpp", ["-ffp-contract=off"])]
 LEGACY_UNITS = [("legacy.cpp", [])]
 
 

@@ -32,6 +32,7 @@ struct CpArgs {
     int *jact;
     double tau0, taus, h0, p, q, eta, maxloop, dtime;
     int *status;
+    int *pl_flag;
 };
 
 __device__ __forceinline__ double proj6(const double *sc, double cx, double cy, double cz)
@@ -111,6 +112,7 @@ __global__ void __launch_bounds__(CTPB) k_cp(CpArgs a)
             tmax = yfn[m];
     }
     if (!(tmax <= 1e-6)) {
+        a.pl_flag[i] = 1;  // pl_flag (src/constitutive.c:1026)
         // active-set loop (src/constitutive.c:1024-1305)
         int nouter = 0;
         const double dts = a.taus - a.tau0;
@@ -374,6 +376,7 @@ void launch_cp(Ctx &c)
     a.Cab = c.Cab;
     a.sch = c.sch;
     a.jact = c.jact;
+    a.pl_flag = c.pl_flag;
     a.tau0 = c.cp[0];
     a.taus = c.cp[1];
     a.h0 = c.cp[2];

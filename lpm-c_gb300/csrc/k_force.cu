@@ -51,6 +51,7 @@ struct ForceArgs {
     const double *G, *sy, *H;
     double xi;
     int *status;
+    int *pl_flag;
 };
 
 static ForceArgs make_args(Ctx &c)
@@ -98,6 +99,7 @@ static ForceArgs make_args(Ctx &c)
     a.H = c.Hh;
     a.xi = c.xi;
     a.status = c.status;
+    a.pl_flag = c.pl_flag;
     return a;
 }
 
@@ -401,8 +403,10 @@ __global__ void __launch_bounds__(TPB) k_j2(ForceArgs a)
     double alpha = a.alpha_c[i], dlam = 0.0;
     const double Hh = a.H[i];
     const double yf = seq - (a.sy[i] + (1.0 - a.xi) * Hh * alpha);
-    if (yf > 0.0)
+    if (yf > 0.0) {
         dlam = yf / (3 * a.G[i] + Hh);
+        a.pl_flag[i] = 1;  // pl_flag (src/constitutive.c:594)
+    }
     alpha += dlam;
     double dpl[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll

@@ -80,6 +80,7 @@ static void free_anderson(Ctx &c)
 Ctx::~Ctx()
 {
     cudaSetDevice(device);
+    free_writer(*this);
     free_batch(*this);
     free_adjoint(*this);
     free_anderson(*this);
@@ -93,7 +94,7 @@ Ctx::~Ctx()
                     (void **)&rowoff, (void **)&npad, (void **)&cols, (void **)&Kd, (void **)&Kf,
                     (void **)&Pinv_d, (void **)&Pinv_f, (void **)&x_d, (void **)&r_d, (void **)&p_d,
                     (void **)&q_d, (void **)&z_d, (void **)&x_f, (void **)&r_f, (void **)&p_f, (void **)&q_f,
-                    (void **)&z_f, (void **)&b_d, (void **)&sc, (void **)&partials, (void **)&counter,
+                    (void **)&z_f, (void **)&pl_flag, (void **)&b_d, (void **)&sc, (void **)&partials, (void **)&counter,
                     (void **)&norms, (void **)&status};
     for (void **p : all)
         if (*p) {
@@ -227,7 +228,7 @@ static int alloc_specimen(Ctx &c)
     if ((rc = dalloc(p, cnt))) \
         return rc;
     A_(c.xyz, n) A_(c.xyz0, n) A_(c.xyz_temp, n) A_(c.Pin, n) A_(c.Pex, n) A_(c.res, n) A_(c.du, n)
-    A_(c.mask, n) A_(c.type, n) A_(c.G, n) A_(c.sy, n) A_(c.Hh, n) A_(c.stress, 6 * n) A_(c.dlambda, n)
+    A_(c.mask, n) A_(c.type, n) A_(c.pl_flag, n) A_(c.G, n) A_(c.sy, n) A_(c.Hh, n) A_(c.stress, 6 * n) A_(c.dlambda, n)
     A_(c.nbr, nb) A_(c.shell, nb) A_(c.rev, nb) A_(c.nbv, n) A_(c.nconn_d, n) A_(c.L0, nb) A_(c.Kn, nb)
     A_(c.Tv, nb) A_(c.oppv, nb) A_(c.dL, nb) A_(c.csx, nb) A_(c.csy, nb) A_(c.csz, nb) A_(c.F, nb)
     A_(c.F_prev, nb) A_(c.S, n) A_(c.T, n) A_(c.ddL, nb) A_(c.dS, n) A_(c.dT, n) A_(c.U, 6 * n)
@@ -554,6 +555,7 @@ int lpm_init_state(lpm_ctx *ctx)
     LPM_CUDA(cudaMemsetAsync(c.Pex, 0, n * sizeof(dvec4), c.stream));
     LPM_CUDA(cudaMemsetAsync(c.Pin, 0, n * sizeof(dvec4), c.stream));
     LPM_CUDA(cudaMemsetAsync(c.status, 0, sizeof(int), c.stream));
+    LPM_CUDA(cudaMemsetAsync(c.pl_flag, 0, n * sizeof(int), c.stream));
     LPM_CUDA(cudaMemcpyAsync(c.xyz, c.xyz0, n * sizeof(dvec4), cudaMemcpyDeviceToDevice, c.stream));
     std::vector<uint8_t> m(n, 7);
     LPM_CUDA(cudaMemcpy(c.mask, m.data(), n, cudaMemcpyHostToDevice));
@@ -1572,6 +1574,12 @@ int lpm_get(lpm_ctx *ctx, const char *name, void *dst, size_t bytes)
         if (!need(n * sizeof(int)))
             return fail(LPM_ERR_ARG, nm + ": buffer too small");
         std::memcpy(dst, (nm == "nb" ? c.hs.nb : c.hs.nconn).data(), n * sizeof(int));
+        return LPM_OK;
+    }
+    if (nm == "type" || nm == "pl_flag") {
+        if (!need(n * sizeof(int)))
+            return fail(LPM_ERR_ARG, nm + ": buffer too small");
+        LPM_CUDA(cudaMemcpy(dst, nm == "type" ? c.type : c.pl_flag, n * sizeof(int), cudaMemcpyDeviceToHost));
         return LPM_OK;
     }
     if (nm == "conn") {

@@ -84,6 +84,7 @@ struct CgScalars {
 };
 
 struct AdjointState;
+struct AsyncWriter;
 
 // Per-specimen PCG state of a batch (device pointers, passed by value).
 // done: 0 running, 1 recursive residual met the tolerance, 2 iteration cap,
@@ -218,6 +219,8 @@ struct Ctx {
     BatchCg bcg;
     BatchHost bh;
     AdjointState *adj = nullptr;  // lpm_adjoint_forward / lpm_adjoint_backward
+    AsyncWriter *writer = nullptr; // lpm_write_dump (output.cpp)
+    int *pl_flag = nullptr;        // [n] set once a particle's return map has yielded (pl_flag)
     // Anderson acceleration of the Newton loop (opts.newton_accel)
     struct Anderson {
         int m = 0;
@@ -284,6 +287,7 @@ struct AdjBuffers {
 };
 struct AdjointState;
 void free_adjoint(Ctx &c);
+void free_writer(Ctx &c);
 // reverse of the last J2 force evaluation (state read from slot 1, forward
 // results from F, dL, S, T): Pbar on the internal force, mu on the new state
 void adj_vjp(Ctx &c, const dvec4 *Pbar, const double *mu_dLp, const double *mu_alpha, double *dLp_bar,

@@ -33,6 +33,8 @@ EXPORTED = [
     "lpm_spmv_bytes", "lpm_update_rr_noalloc", "lpm_setup_batch", "lpm_batch_offsets",
     "lpm_batch_load_step", "lpm_autotune", "lpm_set_tuning", "lpm_get_tuning",
     "lpm_default_adjoint_opts", "lpm_adjoint_forward", "lpm_adjoint_backward", "lpm_force_vjp",
+    "lpm_write_dump", "lpm_write_wait", "lpm_write_disp", "lpm_write_reaction", "lpm_write_stress",
+    "lpm_format_dump", "lpm_format_disp", "lpm_format_reaction", "lpm_format_stress",
 ]
 
 
@@ -146,6 +148,17 @@ def load(path=LIB_PATH):
                                  C.POINTER(AdjointOpts), dp], C.c_int),
         "lpm_adjoint_backward": ([vp, dp, dp, dp, dp, dp, C.POINTER(AdjointStats)], C.c_int),
         "lpm_force_vjp": ([vp, dp, dp, dp, dp, dp, dp, dp], C.c_int),
+        "lpm_write_dump": ([vp, C.c_char_p, C.c_int, C.c_char, dp], C.c_int),
+        "lpm_write_wait": ([vp], C.c_int),
+        "lpm_write_disp": ([vp, C.c_char_p, C.c_char, C.c_int, C.c_int], C.c_int),
+        "lpm_write_reaction": ([vp, C.c_char_p, C.c_char, C.c_int, C.c_int], C.c_int),
+        "lpm_write_stress": ([vp, C.c_char_p, C.c_int, C.c_int], C.c_int),
+        "lpm_format_dump": ([C.c_char_p, C.c_int, C.c_char, C.c_int, dp, C.c_int, ip, dp, dp, dp, dp, ip, dp,
+                             C.c_int, dp], C.c_int),
+        "lpm_format_disp": ([C.c_char_p, C.c_char, C.c_int, C.c_int, C.c_int, ip, dp, dp], C.c_int),
+        "lpm_format_reaction": ([C.c_char_p, C.c_char, C.c_int, C.c_int, C.c_int, C.c_int, ip, ip, dp, dp, dp, dp],
+                                C.c_int),
+        "lpm_format_stress": ([C.c_char_p, C.c_int, C.c_int, C.c_int, ip, dp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -292,6 +305,23 @@ class Specimen:
         self._check(self.L.lpm_force_vjp(self.h, _dp(Pbar), mud, mua, _dp(xbar), _dp(dlp), _dp(ab), _dp(th)))
         return xbar, dlp, ab, th
 
+    # ---- output in the reference's formats
+    def write_dump(self, path, step, flag, box):
+        self._check(self.L.lpm_write_dump(self.h, path.encode(), int(step), flag.encode(),
+                                          _dp(np.ascontiguousarray(box, dtype=np.float64))))
+
+    def write_wait(self):
+        self._check(self.L.lpm_write_wait(self.h))
+
+    def write_disp(self, path, c, t1, tstep):
+        self._check(self.L.lpm_write_disp(self.h, path.encode(), c.encode(), int(t1), int(tstep)))
+
+    def write_reaction(self, path, c, t1, tstep):
+        self._check(self.L.lpm_write_reaction(self.h, path.encode(), c.encode(), int(t1), int(tstep)))
+
+    def write_stress(self, path, t1, tstep):
+        self._check(self.L.lpm_write_stress(self.h, path.encode(), int(t1), int(tstep)))
+
     def setup_particles(self, lattice, radius, xyz):
         xyz = np.ascontiguousarray(xyz, dtype=np.float64)
         self.n = self._check(self.L.lpm_setup_particles(self.h, lattice, radius, xyz.shape[0], _dp(xyz)))
@@ -385,6 +415,7 @@ class Specimen:
         "neighbors": ("b", np.int32), "nsign": ("b", np.int32), "nb": ("n1", np.int32),
         "nb_conn": ("n1", np.int32), "conn": ("n61", np.int32), "K_pointer": ("kp", np.int32),
         "dispBC_index": ("p3", np.int32), "cs_initial": ("b3", np.float64),
+        "type": ("n1", np.int32), "pl_flag": ("n1", np.int32),
         "cp_gy": ("ns", np.float64), "cp_gy2": ("ns", np.float64), "cp_A_single": ("ns", np.float64),
         "cp_A_single2": ("ns", np.float64), "cp_A": ("n1", np.float64), "cp_A2": ("n1", np.float64),
         "cp_Cab": ("nss", np.float64),
