@@ -139,6 +139,11 @@ int lpm_apply_bc(lpm_ctx *ctx, int nbd, const lpm_disp_bc *dbc, int nbf, const l
  * including computeStress and switchStateV(2), then updateRR
  * (src/stiffness.c:519-534).  norms (may be NULL): |residual|, |reaction|. */
 int lpm_compute_force(lpm_ctx *ctx, int plmode, double norms[2]);
+/* computeStrain (src/lpm_basic.c:127-249): weighted least-squares strain
+ * tensor of every particle from its bond stretches of the last force
+ * evaluation; read it as "strain_tensor" (n x 6, s11 s22 s33 s23 s13 s12
+ * order). */
+int lpm_compute_strain(lpm_ctx *ctx);
 /* switchStateV (src/constitutive.c:10-85): 0 = converged -> current,
  * 1 = current -> converged. */
 int lpm_switch_state(lpm_ctx *ctx, int flag);
@@ -156,7 +161,7 @@ int lpm_begin_step(lpm_ctx *ctx);
  *   xyz, xyz_initial, xyz_temp (n x 3), Pin, Pex, residual, disp (3n),
  *   F, dL, csx, csy, csz, Kn, Tv, distance_initial (n x nn),
  *   dLp (n x nn, converged), dLp_trial, J2_alpha (n, converged), J2_beta (n x 6),
- *   stress_tensor (n x 6), neighbors, nsign (n x nn, int32), nb (n, int32),
+ *   stress_tensor, strain_tensor (n x 6), neighbors, nsign (n x nn, int32), nb (n, int32),
  *   dispBC_index (3n, int32), type (n, int32), conn (n x 61, int32), nb_conn (n),
  *   cp_gy (n x nslip), cp_A (n), cp_A_single (n x nslip), J2_dlambda (n). */
 int lpm_get(lpm_ctx *ctx, const char *name, void *dst, size_t bytes);
@@ -284,6 +289,7 @@ int lpm_write_wait(lpm_ctx *ctx);
 int lpm_write_disp(lpm_ctx *ctx, const char *path, char c, int t1, int tstep);
 int lpm_write_reaction(lpm_ctx *ctx, const char *path, char c, int t1, int tstep);
 int lpm_write_stress(lpm_ctx *ctx, const char *path, int t1, int tstep);
+int lpm_write_strain(lpm_ctx *ctx, const char *path, int t1, int tstep);  /* after lpm_compute_strain */
 /* The same formats from host arrays in the reference's per-particle layout
  * (xyz n x 3, stress n x 6 as s11 s22 s33 s23 s13 s12, bond arrays n x nn;
  * plmode 1 reads cp_As (n x nslip) and cp_A, otherwise alpha). */
@@ -295,6 +301,7 @@ int lpm_format_disp(const char *path, char c, int t1, int tstep, int n, const in
 int lpm_format_reaction(const char *path, char c, int t1, int tstep, int n, int nn, const int *type, const int *nb,
                         const double *csx, const double *csy, const double *csz, const double *F);
 int lpm_format_stress(const char *path, int t1, int tstep, int n, const int *type, const double *stress);
+int lpm_format_strain(const char *path, int t1, int tstep, int n, const int *type, const double *strain);
 
 /* ---- no-allocation entry point ----------------------------------------------- */
 /* No counterpart in the reference: an allocation-free form of the residual

@@ -32,6 +32,7 @@ CU_UNITS = [
     ("lpm_api.cu", []),
     ("k_batch.cu", []),
     ("k_adjoint.cu", ["-fmad=false"]),
+    ("k_strain.cu", ["-fmad=false"]),
     ("adjoint.cu", []),
     ("k_noalloc.cu", []),
 ]

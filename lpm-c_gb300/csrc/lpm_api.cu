@@ -86,7 +86,7 @@ Ctx::~Ctx()
     free_anderson(*this);
     void **all[] = {(void **)&xyz, (void **)&xyz0, (void **)&xyz_temp, (void **)&Pin, (void **)&Pex,
                     (void **)&res, (void **)&du, (void **)&mask, (void **)&type, (void **)&G, (void **)&sy,
-                    (void **)&Hh, (void **)&stress, (void **)&dlambda, (void **)&nbr, (void **)&shell,
+                    (void **)&Hh, (void **)&stress, (void **)&strain, (void **)&dlambda, (void **)&nbr, (void **)&shell,
                     (void **)&rev, (void **)&nbv, (void **)&nconn_d, (void **)&L0, (void **)&Kn, (void **)&Tv,
                     (void **)&oppv, (void **)&dL, (void **)&csx, (void **)&csy, (void **)&csz, (void **)&F,
                     (void **)&F_prev, (void **)&S, (void **)&T, (void **)&ddL, (void **)&dS, (void **)&dT,
@@ -228,7 +228,7 @@ static int alloc_specimen(Ctx &c)
     if ((rc = dalloc(p, cnt))) \
         return rc;
     A_(c.xyz, n) A_(c.xyz0, n) A_(c.xyz_temp, n) A_(c.Pin, n) A_(c.Pex, n) A_(c.res, n) A_(c.du, n)
-    A_(c.mask, n) A_(c.type, n) A_(c.pl_flag, n) A_(c.G, n) A_(c.sy, n) A_(c.Hh, n) A_(c.stress, 6 * n) A_(c.dlambda, n)
+    A_(c.mask, n) A_(c.type, n) A_(c.pl_flag, n) A_(c.G, n) A_(c.sy, n) A_(c.Hh, n) A_(c.stress, 6 * n) A_(c.strain, 6 * n) A_(c.dlambda, n)
     A_(c.nbr, nb) A_(c.shell, nb) A_(c.rev, nb) A_(c.nbv, n) A_(c.nconn_d, n) A_(c.L0, nb) A_(c.Kn, nb)
     A_(c.Tv, nb) A_(c.oppv, nb) A_(c.dL, nb) A_(c.csx, nb) A_(c.csy, nb) A_(c.csz, nb) A_(c.F, nb)
     A_(c.F_prev, nb) A_(c.S, n) A_(c.T, n) A_(c.ddL, nb) A_(c.dS, n) A_(c.dT, n) A_(c.U, 6 * n)
@@ -959,6 +959,14 @@ int lpm_compute_force(lpm_ctx *ctx, int plmode, double norms[2])
     return LPM_OK;
 }
 
+int lpm_compute_strain(lpm_ctx *ctx)
+{
+    if (!ctx || !ctx->c.ready)
+        return fail(LPM_ERR_ARG, "call lpm_init_state first");
+    launch_strain(ctx->c);
+    return sync(ctx->c);
+}
+
 int lpm_switch_state(lpm_ctx *ctx, int flag)
 {
     if (!ctx || !ctx->c.ready || flag < 0 || flag > 2)
@@ -1557,6 +1565,7 @@ int lpm_get(lpm_ctx *ctx, const char *name, void *dst, size_t bytes)
     if (nm == "J2_beta2") return rows_d(c.beta[2], 6);
     if (nm == "J2_dlambda") return rows_d(c.dlambda, 1);
     if (nm == "stress_tensor") return rows_d(c.stress, 6);
+    if (nm == "strain_tensor") return rows_d(c.strain, 6);
     if (nm == "cp_gy" && c.nslip) return rows_d(c.gy[1], c.nslip);
     if (nm == "cp_gy2" && c.nslip) return rows_d(c.gy[2], c.nslip);
     if (nm == "cp_A_single" && c.nslip) return rows_d(c.As[1], c.nslip);
@@ -1654,6 +1663,7 @@ int lpm_set(lpm_ctx *ctx, const char *name, const void *src, size_t bytes)
     if (nm == "xyz_temp") return particles(c.xyz_temp);
     if (nm == "Pex") return particles(c.Pex);
     if (nm == "residual") return particles(c.res);
+    if (nm == "dL") return bond_d(c.dL);
     if (nm == "F") return bond_d(c.F);
     if (nm == "F_temp") return bond_d(c.F_prev);
     if (nm == "csx") return bond_d(c.csx);

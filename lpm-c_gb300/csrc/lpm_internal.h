@@ -154,6 +154,7 @@ struct Ctx {
     int *type = nullptr;
     double *G = nullptr, *sy = nullptr, *Hh = nullptr;
     double *stress = nullptr;  // [6][n]
+    double *strain = nullptr;  // [6][n] (computeStrain)
     double *dlambda = nullptr;
     // ---- device: bonds [NN][n]
     int *nbr = nullptr;
@@ -244,6 +245,7 @@ void launch_add_du(Ctx &c);
 void launch_apply_disp_bc(Ctx &c, int nbd, const lpm_disp_bc *d);
 void launch_apply_force_bc(Ctx &c, int nbf, const lpm_force_bc *f, const int *counts);
 void launch_cab(Ctx &c);
+void launch_strain(Ctx &c);  // k_strain.cu
 // stiffness (k_stiff.cu)
 void launch_tangent_geometry(Ctx &c);
 void launch_assemble(Ctx &c, bool fp32);

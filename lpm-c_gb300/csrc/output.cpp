@@ -1,6 +1,6 @@
 // Output writers in the reference's file formats (src/data_handler.c):
 // writeDump (LAMMPS dump, :42-85), writeDisp (:278-306), writeReaction
-// (:309-335) and writeStress (:110-135).
+// (:309-335), writeStress (:110-135) and writeStrain (:137-162).
 //
 // lpm_format_* write from host arrays in the reference's per-particle layout;
 // the lpm_write_* entry points take a context: writeDump copies the device
@@ -178,10 +178,8 @@ int lpm_format_reaction(const char *path, char c, int t1, int tstep, int n, int 
     return LPM_OK;
 }
 
-int lpm_format_stress(const char *path, int t1, int tstep, int n, const int *type, const double *stress)
+static int format_type_average(const char *path, int t1, int tstep, int n, const int *type, const double *v)
 {
-    if (!path || !type || !stress)
-        return fail(LPM_ERR_ARG, "lpm_format_stress: null argument");
     FILE *f = std::fopen(path, "a+");
     if (!f)
         return fail(LPM_ERR_ARG, std::string("cannot open ") + path);
@@ -191,7 +189,7 @@ int lpm_format_stress(const char *path, int t1, int tstep, int n, const int *typ
         if (type[i] == t1) {
             num++;
             for (int j = 0; j < 6; j++)
-                ave[j] += stress[6 * (size_t)i + j];
+                ave[j] += v[6 * (size_t)i + j];
         }
     std::fprintf(f, "%d ", tstep);
     for (int j = 0; j < 6; j++)
@@ -199,6 +197,21 @@ int lpm_format_stress(const char *path, int t1, int tstep, int n, const int *typ
     std::fprintf(f, "\n");
     std::fclose(f);
     return LPM_OK;
+}
+
+int lpm_format_stress(const char *path, int t1, int tstep, int n, const int *type, const double *stress)
+{
+    if (!path || !type || !stress)
+        return fail(LPM_ERR_ARG, "lpm_format_stress: null argument");
+    return format_type_average(path, t1, tstep, n, type, stress);
+}
+
+// writeStrain (src/data_handler.c:137-162): same layout as writeStress
+int lpm_format_strain(const char *path, int t1, int tstep, int n, const int *type, const double *strain)
+{
+    if (!path || !type || !strain)
+        return fail(LPM_ERR_ARG, "lpm_format_strain: null argument");
+    return format_type_average(path, t1, tstep, n, type, strain);
 }
 
 }  // extern "C"
@@ -392,6 +405,20 @@ int lpm_write_reaction(lpm_ctx *ctx, const char *path, char c, int t1, int tstep
     }
     return lpm_format_reaction(path, c, t1, tstep, n, nn, type.data(), nb.data(), cs[0].data(), cs[1].data(),
                                cs[2].data(), F.data());
+}
+
+int lpm_write_strain(lpm_ctx *ctx, const char *path, int t1, int tstep)
+{
+    if (!ctx || !ctx->c.ready)
+        return fail(LPM_ERR_ARG, "lpm_write_strain: uninitialised context");
+    const int n = ctx->c.n;
+    std::vector<int> type(n);
+    std::vector<double> e(6 * (size_t)n);
+    int rc;
+    if ((rc = lpm_get(ctx, "type", type.data(), type.size() * sizeof(int))) ||
+        (rc = lpm_get(ctx, "strain_tensor", e.data(), e.size() * sizeof(double))))
+        return rc;
+    return lpm_format_strain(path, t1, tstep, n, type.data(), e.data());
 }
 
 int lpm_write_stress(lpm_ctx *ctx, const char *path, int t1, int tstep)

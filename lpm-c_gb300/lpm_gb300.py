@@ -35,6 +35,7 @@ EXPORTED = [
     "lpm_default_adjoint_opts", "lpm_adjoint_forward", "lpm_adjoint_backward", "lpm_force_vjp",
     "lpm_write_dump", "lpm_write_wait", "lpm_write_disp", "lpm_write_reaction", "lpm_write_stress",
     "lpm_format_dump", "lpm_format_disp", "lpm_format_reaction", "lpm_format_stress",
+    "lpm_compute_strain", "lpm_write_strain", "lpm_format_strain",
 ]
 
 
@@ -159,6 +160,9 @@ def load(path=LIB_PATH):
         "lpm_format_reaction": ([C.c_char_p, C.c_char, C.c_int, C.c_int, C.c_int, C.c_int, ip, ip, dp, dp, dp, dp],
                                 C.c_int),
         "lpm_format_stress": ([C.c_char_p, C.c_int, C.c_int, C.c_int, ip, dp], C.c_int),
+        "lpm_compute_strain": ([vp], C.c_int),
+        "lpm_write_strain": ([vp, C.c_char_p, C.c_int, C.c_int], C.c_int),
+        "lpm_format_strain": ([C.c_char_p, C.c_int, C.c_int, C.c_int, ip, dp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -319,6 +323,13 @@ class Specimen:
     def write_reaction(self, path, c, t1, tstep):
         self._check(self.L.lpm_write_reaction(self.h, path.encode(), c.encode(), int(t1), int(tstep)))
 
+    def compute_strain(self):
+        self._check(self.L.lpm_compute_strain(self.h))
+        return self.get("strain_tensor")
+
+    def write_strain(self, path, t1, tstep):
+        self._check(self.L.lpm_write_strain(self.h, path.encode(), int(t1), int(tstep)))
+
     def write_stress(self, path, t1, tstep):
         self._check(self.L.lpm_write_stress(self.h, path.encode(), int(t1), int(tstep)))
 
@@ -412,6 +423,7 @@ class Specimen:
         "dLp2": ("b", np.float64), "J2_alpha": ("n1", np.float64), "J2_alpha0": ("n1", np.float64),
         "J2_alpha2": ("n1", np.float64), "J2_beta": ("n6", np.float64), "J2_beta2": ("n6", np.float64),
         "J2_dlambda": ("n1", np.float64), "stress_tensor": ("n6", np.float64),
+        "strain_tensor": ("n6", np.float64),
         "neighbors": ("b", np.int32), "nsign": ("b", np.int32), "nb": ("n1", np.int32),
         "nb_conn": ("n1", np.int32), "conn": ("n61", np.int32), "K_pointer": ("kp", np.int32),
         "dispBC_index": ("p3", np.int32), "cs_initial": ("b3", np.float64),

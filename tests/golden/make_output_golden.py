@@ -2,10 +2,10 @@
 
 Runs the LPM-C reference built from its own sources (oracle/_ref) into the
 plastic range and writes, with the reference's own writeDump, writeDisp,
-writeReaction and writeStress, the files its main loop writes
-(src/lpmc_project.c:504-515).  Stores those files' text together with the
-arrays the writers read, so the repository's writers can be checked byte for
-byte without the reference:
+writeReaction, writeStress and writeStrain (after computeStress and
+computeStrain), the files its main loop writes (src/lpmc_project.c:466-515).
+Stores those files' text together with the arrays the writers read, so the
+repository's writers can be checked byte for byte without the reference:
 
     python tests/golden/make_output_golden.py
 
@@ -32,15 +32,18 @@ import cases  # noqa: E402
 def write_all(tmp, t_disp, comp, step):
     L = R.lib()
     L.computeStress()
-    names = {k: os.path.join(tmp, k + ".txt") for k in ("dump", "disp", "reaction", "stress")}
+    L.computeStrain()
+    names = {k: os.path.join(tmp, k + ".txt") for k in ("dump", "disp", "reaction", "stress", "strain")}
     L.writeDump.argtypes = [C.c_char_p, C.c_int, C.c_char]
     L.writeDisp.argtypes = [C.c_char_p, C.c_char, C.c_int, C.c_int]
     L.writeReaction.argtypes = [C.c_char_p, C.c_char, C.c_int, C.c_int]
     L.writeStress.argtypes = [C.c_char_p, C.c_int, C.c_int]
+    L.writeStrain.argtypes = [C.c_char_p, C.c_int, C.c_int]
     L.writeDump(names["dump"].encode(), step, b"s")
     L.writeDisp(names["disp"].encode(), comp, t_disp, step)
     L.writeReaction(names["reaction"].encode(), comp, t_disp, step)
     L.writeStress(names["stress"].encode(), cases.T_INTERIOR, step)
+    L.writeStrain(names["strain"].encode(), cases.T_INTERIOR, step)
     return {k: open(v).read() for k, v in names.items()}
 
 
@@ -48,7 +51,8 @@ def arrays(n, nn, xyz0, types, box):
     return dict(
         box=np.array(box), type=types, xyz=R.get_d2("xyz", n, 3), xyz0=xyz0,
         stress=R.get_d2("stress_tensor", n, 6), pl_flag=R.get_i1("pl_flag", n), nb=R.get_i1("nb", n),
-        csx=R.get_d2("csx", n, nn), csy=R.get_d2("csy", n, nn), csz=R.get_d2("csz", n, nn), F=R.get_d2("F", n, nn))
+        csx=R.get_d2("csx", n, nn), csy=R.get_d2("csy", n, nn), csz=R.get_d2("csz", n, nn), F=R.get_d2("F", n, nn),
+        dL=R.get_d2("dL", n, nn), distance_initial=R.get_d2("distance_initial", n, nn))
 
 
 def sc_j2(tmp):
@@ -68,6 +72,7 @@ def sc_j2(tmp):
     out = arrays(n, nn, xyz0, types, case.box)
     out["alpha"] = R.get_d2("J2_alpha", n, 3)[:, 0]
     texts = write_all(tmp, cases.T_TOP, b"z", nsteps)
+    out["strain"] = R.get_d2("strain_tensor", n, 6)
     out.update({"text_" + k: np.frombuffer(v.encode(), dtype=np.uint8) for k, v in texts.items()})
     out["step"] = nsteps
     return out

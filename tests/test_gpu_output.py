@@ -60,6 +60,21 @@ def test_writers_match_reference_sc(gpu_lib, tmp_path):
     s.close()
 
 
+def test_strain_bit_exact(gpu_lib, tmp_path):
+    """computeStrain on the GPU from the reference's bond stretches equals the
+    reference's strain tensor bit for bit; writeStrain text too."""
+    G = gpu_lib
+    d = golden("output_sc6_j2.npz")
+    s, case = run_sc(G)
+    s.set("dL", d["dL"])
+    e = s.compute_strain()
+    assert np.array_equal(e, d["strain"])
+    path = str(tmp_path / "strain.txt")
+    s.write_strain(path, cases.T_INTERIOR, int(d["step"]))
+    assert open(path).read() == bytes(d["text_strain"]).decode()
+    s.close()
+
+
 def test_dump_cp_matches_host_formatter(gpu_lib, tmp_path):
     """Crystal plasticity (FCC 4^3 cells into the plastic range, the case of
     tests/test_gpu_cp.py): the asynchronous device dump equals the host

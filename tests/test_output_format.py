@@ -64,6 +64,10 @@ def test_formats_match_reference_writers(gpu_lib, tmp_path, fixture):
     p = str(tmp_path / "stress.txt").encode()
     assert L.lpm_format_stress(p, cases.T_INTERIOR, step, n, arr(d["type"], _ip), arr(d["stress"], _dp)) == 0
     assert open(p.decode()).read() == text(d, "stress")
+    if "strain" in d:
+        p = str(tmp_path / "strain.txt").encode()
+        assert L.lpm_format_strain(p, cases.T_INTERIOR, step, n, arr(d["type"], _ip), arr(d["strain"], _dp)) == 0
+        assert open(p.decode()).read() == text(d, "strain")
 
 
 def test_dump_appends(gpu_lib, tmp_path):
