@@ -307,8 +307,20 @@ static int upload_setup(Ctx &c)
     return LPM_OK;
 }
 
+static void drop_graphs(Ctx &c);
+
 static int setup_common(Ctx &c, bool built = false)
 {
+    // everything sized for, or captured with, the previous specimen's arrays
+    // (CUDA graphs hold the old device pointers) goes before reallocation
+    free_writer(c);
+    free_adjoint(c);
+    free_anderson(c);
+    drop_graphs(c);
+    dfree(c.Kf);
+    dfree(c.Kd);
+    c.kf_cap = c.kd_cap = 0;
+    c.vec64_fallback = false;
     HostSetup &h = c.hs;
     if (!built) {
         build_neighbors(h);
@@ -815,10 +827,16 @@ int assemble(Ctx &c)
 {
     const bool fp32 = c.opts.precision == LPM_PREC_MIXED;
     int rc;
-    if (fp32 && !c.Kf && (rc = dalloc(c.Kf, 9 * (size_t)c.nblk)))
-        return rc;
-    if (!fp32 && !c.Kd && (rc = dalloc(c.Kd, 9 * (size_t)c.nblk)))
-        return rc;
+    if (fp32 && (!c.Kf || c.kf_cap != c.nblk)) {
+        if ((rc = dalloc(c.Kf, 9 * (size_t)c.nblk)))
+            return rc;
+        c.kf_cap = c.nblk;
+    }
+    if (!fp32 && (!c.Kd || c.kd_cap != c.nblk)) {
+        if ((rc = dalloc(c.Kd, 9 * (size_t)c.nblk)))
+            return rc;
+        c.kd_cap = c.nblk;
+    }
     launch_tangent_geometry(c);
     launch_assemble(c, fp32);
     c.have_K = true;

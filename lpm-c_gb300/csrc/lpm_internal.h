@@ -190,6 +190,7 @@ struct Ctx {
     int *cols = nullptr;
     double *Kd = nullptr;     // FP64 values (9*nblk)
     float *Kf = nullptr;      // FP32 values (9*nblk)
+    long long kd_cap = 0, kf_cap = 0;  // blocks Kd / Kf were allocated for
     double *Pinv_d = nullptr; // block-Jacobi inverse, [9][n]
     float *Pinv_f = nullptr;
     // ---- solver vectors
