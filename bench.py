@@ -308,7 +308,9 @@ def step_counts(size, W, K, stats=None):
     try:
         with open(COUNTS_FILE) as f:
             d = json.load(f)
-        if d.get("size") == size and d.get("first_step") == W + 1 and d.get("steps") == K:
+        # per-step averages over the recorded steps (the elastic steps 4-8
+        # all take 3 Newton iterations), valid for timed runs starting there
+        if d.get("size") == size and d.get("first_step") == W + 1:
             return d["newton_per_step"], d["cg_per_newton"], "recorded FP64 GPU counts (" + COUNTS_FILE[len(ROOT) + 1:] + ")"
     except Exception:
         pass
