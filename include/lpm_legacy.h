@@ -32,6 +32,9 @@ struct forceBCPara;
 
 /* src/stiffness.c:11 (include/stiffness.h:5) */
 void calcKnTv(void);
+/* src/lpm_basic.c:127 (include/lpm_basic.h:13): strain_tensor from the bond
+ * stretches dL of the last force evaluation (weighted least squares). */
+void computeStrain(void);
 /* src/stiffness.c:519 (include/stiffness.h:6); called with an ignored
  * argument at src/lpmc_project.c:462, hence the unprototyped form. */
 void updateRR();

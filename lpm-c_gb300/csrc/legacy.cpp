@@ -25,7 +25,7 @@ extern double *K_global, *residual, *Pin, *Pex, *disp, *sigmay, *reaction_force;
 extern double *J2_dlambda, *J2_stresseq, *J2_stressm, *J2_triaxiality;
 extern double **xyz, **xyz_initial, **xyz_temp, **F, **F_temp, **csx, **csy, **csz, **Ce, **dL, **Kn, **Tv;
 extern double **stress_tensor, **bond_stress, **J2_alpha, **J2_beta_eq, **cp_A, **cp_Cab;
-extern double **damage_local, **damage_nonlocal;
+extern double **damage_local, **damage_nonlocal, **strain_tensor;
 extern double ***dLp, ***J2_beta, ***cp_gy, ***cp_A_single, ***damage_D;
 }
 
@@ -290,6 +290,14 @@ void calcKnTv(void)
 }
 
 // src/constitutive.c:1864-1917: the GPU computed Cab in calcKnTv; copy it out.
+void computeStrain(void)
+{
+    const int n = nparticle, nn = nneighbors;
+    put("dL", flat2(dL, n, nn));  // the host's dL, as the last force call wrote it back
+    check(lpm_compute_strain(ctx()), "computeStrain");
+    scatter2(strain_tensor, get("strain_tensor", 6 * (size_t)n), n, 6);
+}
+
 void computeCab(void)
 {
     if (g_plmode_dev != 1 || nslipSys <= 0 || !cp_Cab)

@@ -388,6 +388,12 @@ int lpmh_get(const char *name, double *out)
     } else if (!strcmp(name, "csz")) {
         for (int i = 0; i < n; i++)
             memcpy(out + (size_t)i * nn, csz[i], sizeof(double) * nn);
+    } else if (!strcmp(name, "dL")) {
+        for (int i = 0; i < n; i++)
+            memcpy(out + (size_t)i * nn, dL[i], sizeof(double) * nn);
+    } else if (!strcmp(name, "strain_tensor")) {
+        for (int i = 0; i < n; i++)
+            memcpy(out + 6 * (size_t)i, strain_tensor[i], sizeof(double) * 6);
     } else {
         return -1;
     }

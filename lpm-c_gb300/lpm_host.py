@@ -70,11 +70,17 @@ class HostDriver:
 
     def get(self, name):
         shape = {"xyz": (self.n, 3), "xyz_initial": (self.n, 3), "J2_alpha": (self.n,),
-                 "F": (self.n, 18), "csz": (self.n, 18)}[name]
+                 "F": (self.n, 18), "csz": (self.n, 18), "dL": (self.n, 18),
+                 "strain_tensor": (self.n, 6)}[name]
         out = np.zeros(shape)
         if self.L.lpmh_get(name.encode(), out.ctypes.data_as(C.POINTER(C.c_double))) != 0:
             raise KeyError(name)
         return out
+
+    def compute_strain(self):
+        """computeStrain through the reference-named drop-in."""
+        self.L.computeStrain()
+        return self.get("strain_tensor")
 
     def traffic(self, reset=False):
         a, b = C.c_longlong(), C.c_longlong()

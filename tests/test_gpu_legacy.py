@@ -37,3 +37,15 @@ def test_legacy_host_loop_matches_oracle(oracle_mod, gpu_lib):
     assert np.abs(h.get("J2_alpha") - o.d("alpha1", (n,))).max() < 1e-10
     h2d, d2h = h.traffic()
     assert h2d > 0 and d2h > 0
+    # computeStrain through the drop-in equals the context entry point on the same bond stretches
+    e_host = h.compute_strain()
+    s = gpu_lib.Specimen(0)
+    s.setup_lattice(case.lattice, case.radius, case.box)
+    s.set_types(types)
+    c11, c12, c44 = cases.iso_cubic(case.E, case.nu)
+    s.set_material(np.full(n, c11), np.full(n, c12), np.full(n, c44), case.sigmay, case.H, 0.0, gpu_lib.PL_J2)
+    s.init_state()
+    s.set("dL", h.get("dL"))
+    assert np.array_equal(e_host, s.compute_strain())
+    assert np.abs(e_host).max() > 0.0
+    s.close()
