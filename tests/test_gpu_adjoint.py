@@ -196,3 +196,48 @@ def test_checkpointed_recomputation_is_exact(gpu_lib):
     assert st_ck["checkpoints"] == 3 and st_ck["recomputed_steps"] == plate.steps
     for name in g_all:
         assert np.array_equal(g_all[name], g_ck[name]), name
+
+
+def test_adjoint_matches_cpu_reference_gradient(oracle_mod, gpu_lib):
+    """The GPU adjoint gradient against a reference gradient from the FP64 CPU
+    path: central differences of the loss computed by the oracle (the C
+    restatement of the reference, bit-exact with it), along a smooth direction
+    of each field."""
+    G = gpu_lib
+    # two steps into the plastic range (74 of 154 particles yield): the
+    # reference's plain modified Newton, run by the oracle, converges there
+    # to 1e-12 (it diverges on the third step of this plate)
+    plate = cases.NotchedPlate(nx=8, ny=2, nz=10, notch=3, steps=2, strain=0.002, corr=2.0)
+    f1, f2 = plate.fields(1), plate.fields(2)
+    s = plate_specimen(G, plate)
+    target = s.adjoint_forward(*f2, plate.step_bcs(), cases.T_TOP, "z")
+    s.close()
+    L_gpu, grads, st, _ = loss_and_grad(G, plate, f1, target)
+    assert st["status"] == 0
+
+    def oracle_loss(fields):
+        o = oracle_mod.Oracle()
+        n = o.setup_particles(plate.lattice, plate.radius, plate.xyz)
+        o.set_types(cases.sc_types(o.d("xyz", (n, 3)), o.i("nb", (n,)), plate.radius))
+        E, nu, sy, H = fields
+        c11, c12, c44 = cases.iso_cubic(E, nu)
+        o.set_material(c11, c12, c44, sy, H, 0.0, 0)
+        o.init_state()
+        top = o.i("type", (n,)) == cases.T_TOP
+        R = []
+        for b in plate.step_bcs():
+            o.load_step(b, [], 1e-12, 3000, 1e-20, 0.0)
+            R.append(-o.d("Pin", (n, 3))[top, 2].sum())
+        return float(((np.array(R) - target) ** 2).sum())
+
+    assert abs(oracle_loss(f1) - L_gpu) <= 1e-8 * L_gpu
+    for k, name in enumerate(["E", "nu", "sigmay", "H"]):
+        d = f1[k] * plate.fields(7 + k)[k] / plate.BASE[k]
+        h = 1e-5
+        fp = [x.copy() for x in f1]
+        fm = [x.copy() for x in f1]
+        fp[k] = f1[k] + h * d
+        fm[k] = f1[k] - h * d
+        fd = (oracle_loss(fp) - oracle_loss(fm)) / (2 * h)
+        ad = float((grads[name] * d).sum())
+        assert abs(fd - ad) <= 1e-5 * abs(ad), (name, fd, ad)
