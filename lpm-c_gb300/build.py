@@ -29,7 +29,7 @@ CU_UNITS = [
     ("k_cp.cu", ["-fmad=false"]),
     ("k_stiff.cu", []),
     ("k_solve.cu", []),
-    ("lpm_api.cu", []),
+    ("lpm_api.cu", ["-Xcompiler", "-fopenmp"]),
     ("k_batch.cu", []),
     ("k_adjoint.cu", ["-fmad=false"]),
     ("k_strain.cu", ["-fmad=false"]),

@@ -180,6 +180,7 @@ void switch_state(Ctx &c, int flag)
 template <typename T>
 static void to_slot_major(const T *src, T *dst, int n, int k)
 {
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < n; i++)
         for (int j = 0; j < k; j++)
             dst[(size_t)j * n + i] = src[(size_t)i * k + j];
@@ -196,9 +197,10 @@ static void from_slot_major(const T *src, T *dst, int n, int k)
 static int upload_particles(Ctx &c, dvec4 *dst, const double *src3)
 {
     LPM_CUDA(cudaStreamSynchronize(c.stream));
-    std::vector<dvec4> t(c.n);
+    hvec<dvec4> t(c.n);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < c.n; i++)
-        t[i] = make_dvec4(src3[3 * i], src3[3 * i + 1], src3[3 * i + 2], 0.0);
+        t[i] = make_dvec4(src3[3 * (size_t)i], src3[3 * (size_t)i + 1], src3[3 * (size_t)i + 2], 0.0);
     LPM_CUDA(cudaMemcpy(dst, t.data(), sizeof(dvec4) * c.n, cudaMemcpyHostToDevice));
     return LPM_OK;
 }
@@ -277,16 +279,18 @@ static int upload_setup(Ctx &c)
     rc = upload_particles(c, c.xyz_temp, h.xyz.data());
     if (rc)
         return rc;
-    std::vector<int> ti(nb);
-    std::vector<int8_t> t8(nb);
-    std::vector<double> td(nb);
+    hvec<int> ti(nb);
+    hvec<int8_t> t8(nb);
+    hvec<double> td(nb);
     to_slot_major(h.nbr.data(), ti.data(), n, LPM_NN);
     LPM_CUDA(cudaMemcpy(c.nbr, ti.data(), nb * sizeof(int), cudaMemcpyHostToDevice));
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < n; i++)
         for (int j = 0; j < LPM_NN; j++) {
             t8[(size_t)j * n + i] = (int8_t)h.shell[(size_t)i * LPM_NN + j];
         }
     LPM_CUDA(cudaMemcpy(c.shell, t8.data(), nb, cudaMemcpyHostToDevice));
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < n; i++)
         for (int j = 0; j < LPM_NN; j++)
             t8[(size_t)j * n + i] = (int8_t)h.rev[(size_t)i * LPM_NN + j];

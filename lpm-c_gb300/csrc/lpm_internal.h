@@ -15,6 +15,8 @@
 #include <cstdint>
 #include <cstddef>
 #include <string>
+#include <memory>
+#include <utility>
 #include <vector>
 #include <cuda_runtime.h>
 #include "../../include/lpm_gpu.h"
@@ -42,24 +44,52 @@ int fail(int code, const std::string &msg);
             return ::lpm::fail(LPM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
+// Allocator whose resize() leaves trivial elements uninitialised, so that
+// gigabyte-sized setup arrays are first written (and their pages first
+// touched) by the parallel loops that fill them, not by a serial zero fill.
+template <typename T>
+struct NoInitAlloc : std::allocator<T> {
+    template <typename U>
+    struct rebind {
+        typedef NoInitAlloc<U> other;
+    };
+    NoInitAlloc() = default;
+    template <typename U>
+    NoInitAlloc(const NoInitAlloc<U> &) noexcept
+    {
+    }
+    template <typename U>
+    void construct(U *p) noexcept
+    {
+        ::new (static_cast<void *>(p)) U;
+    }
+    template <typename U, typename... A>
+    void construct(U *p, A &&...a)
+    {
+        ::new (static_cast<void *>(p)) U(std::forward<A>(a)...);
+    }
+};
+template <typename T>
+using hvec = std::vector<T, NoInitAlloc<T>>;
+
 // Host-side setup data (built once per specimen, see setup.cpp).
 struct HostSetup {
     int lattice = 0, n = 0, nn1 = 0, nn2 = 0;
     double radius = 0, vol = 0, cut1 = 0, cut2 = 0;
-    std::vector<double> xyz;          // n x 3
-    std::vector<int> nbr;             // n x NN (row-major), -1 padded
-    std::vector<int> shell;           // n x NN
-    std::vector<int> nb;              // n
-    std::vector<int> rev;             // n x NN: slot of the reverse bond
-    std::vector<double> L0, cs0;      // n x NN, n x NN x 3
-    std::vector<double> oppv;         // n x NN: opposite-bond weight / particle volume
-    std::vector<int> conn;            // n x 61 sorted, -1 padded (searchAFEMNeighbor)
-    std::vector<int> nconn;           // n
-    std::vector<int> kp0, kp1;        // K_pointer[i][0], K_pointer[i][1]
+    hvec<double> xyz;          // n x 3
+    hvec<int> nbr;             // n x NN (row-major), -1 padded
+    hvec<int> shell;           // n x NN
+    hvec<int> nb;              // n
+    hvec<int> rev;             // n x NN: slot of the reverse bond
+    hvec<double> L0, cs0;      // n x NN, n x NN x 3
+    hvec<double> oppv;         // n x NN: opposite-bond weight / particle volume
+    hvec<int> conn;            // n x 61 sorted, -1 padded (searchAFEMNeighbor)
+    hvec<int> nconn;           // n
+    hvec<int> kp0, kp1;        // K_pointer[i][0], K_pointer[i][1]
     // block-CSR pattern
-    std::vector<long long> rowoff;    // n+1, in blocks (padded)
-    std::vector<int> npad;            // n
-    std::vector<int> cols;            // rowoff[n]
+    hvec<long long> rowoff;    // n+1, in blocks (padded)
+    hvec<int> npad;            // n
+    hvec<int> cols;            // rowoff[n]
 };
 
 int build_lattice(HostSetup &h, int lattice, double radius, const double *box);

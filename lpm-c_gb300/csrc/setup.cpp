@@ -136,11 +136,12 @@ void build_neighbors(HostSetup &h)
         for (int i = 0; i < n; i++)
             order[fill[cell[i]]++] = i;
     }
-    h.nbr.assign((size_t)n * LPM_NN, -1);
-    h.shell.assign((size_t)n * LPM_NN, -1);
-    h.nb.assign(n, 0);
-    h.L0.assign((size_t)n * LPM_NN, 0.0);
-    h.cs0.assign((size_t)n * LPM_NN * 3, 0.0);
+    // sized without a fill: the loop below writes every slot of its row
+    h.nbr.resize((size_t)n * LPM_NN);
+    h.shell.resize((size_t)n * LPM_NN);
+    h.nb.resize(n);
+    h.L0.resize((size_t)n * LPM_NN);
+    h.cs0.resize((size_t)n * LPM_NN * 3);
     const double *X = h.xyz.data();
 #pragma omp parallel for schedule(dynamic, 512)
     for (int i = 0; i < n; i++) {
@@ -193,6 +194,13 @@ void build_neighbors(HostSetup &h)
             h.cs0[3 * b + 2] = (X[3 * i + 2] - X[3 * j + 2]) / dis;
             h.L0[b] = dis;
         }
+        for (int q = m; q < LPM_NN; q++) {
+            const size_t b = (size_t)i * LPM_NN + q;
+            h.nbr[b] = -1;
+            h.shell[b] = -1;
+            h.cs0[3 * b] = h.cs0[3 * b + 1] = h.cs0[3 * b + 2] = 0.0;
+            h.L0[b] = 0.0;
+        }
         h.nb[i] = m;
     }
 }
@@ -203,8 +211,8 @@ void build_neighbors(HostSetup &h)
 void build_afem(HostSetup &h)
 {
     const int n = h.n, w = 61;
-    h.conn.assign((size_t)n * w, -1);
-    h.nconn.assign(n, 0);
+    h.conn.resize((size_t)n * w);
+    h.nconn.resize(n);
 #pragma omp parallel for schedule(dynamic, 512)
     for (int i = 0; i < n; i++) {
         int col[LPM_NN * (LPM_NN + 1)];
@@ -220,8 +228,8 @@ void build_afem(HostSetup &h)
         std::sort(col, col + nc);
         const int m = (int)(std::unique(col, col + nc) - col);
         const int mm = std::min(m, w);
-        for (int k = 0; k < mm; k++)
-            h.conn[(size_t)i * w + k] = col[k];
+        for (int k = 0; k < w; k++)
+            h.conn[(size_t)i * w + k] = k < mm ? col[k] : -1;
         h.nconn[i] = mm;
     }
     h.kp0.assign(n + 1, 0);
@@ -241,16 +249,22 @@ void build_bond_tables(HostSetup &h)
 {
     const int n = h.n;
     const double eps = 1e-6;
-    h.rev.assign((size_t)n * LPM_NN, -1);
-    h.oppv.assign((size_t)n * LPM_NN, 0.0);
+    h.rev.resize((size_t)n * LPM_NN);
+    h.oppv.resize((size_t)n * LPM_NN);
 #pragma omp parallel for
     for (int i = 0; i < n; i++) {
+        for (int j = h.nb[i]; j < LPM_NN; j++) {
+            h.rev[(size_t)i * LPM_NN + j] = -1;
+            h.oppv[(size_t)i * LPM_NN + j] = 0.0;
+        }
         for (int j = 0; j < h.nb[i]; j++) {
             const size_t b = (size_t)i * LPM_NN + j;
             const int p = h.nbr[b];
+            int rv = -1;
             for (int q = 0; q < LPM_NN; q++)
                 if (h.nbr[(size_t)p * LPM_NN + q] == i)
-                    h.rev[b] = q;
+                    rv = q;
+            h.rev[b] = rv;
             double opp = 1.0;
             if (h.nb[i] == LPM_NN) {
                 opp = 0.5;
@@ -281,7 +295,7 @@ void build_block_pattern(HostSetup &h)
         h.npad[i] = (h.nconn[i] + 3) & ~3;
         h.rowoff[i + 1] = h.rowoff[i] + h.npad[i];
     }
-    h.cols.assign((size_t)h.rowoff[n], 0);
+    h.cols.resize((size_t)h.rowoff[n]);  // every entry written below
 #pragma omp parallel for
     for (int i = 0; i < n; i++) {
         int *c = h.cols.data() + h.rowoff[i];
@@ -305,40 +319,69 @@ void merge_setups(HostSetup &dst, const std::vector<HostSetup> &parts, std::vect
     dst.cut2 = f.cut2;
     dst.nn1 = f.nn1;
     dst.nn2 = f.nn2;
-    offsets.assign(parts.size() + 1, 0);
-    for (size_t s = 0; s < parts.size(); s++)
+    const size_t ns = parts.size();
+    offsets.assign(ns + 1, 0);
+    std::vector<long long> kb(ns + 1, 0), rb(ns + 1, 0);
+    for (size_t s = 0; s < ns; s++) {
         offsets[s + 1] = offsets[s] + parts[s].n;
+        kb[s + 1] = kb[s] + parts[s].kp1[parts[s].n];
+        rb[s + 1] = rb[s] + parts[s].rowoff[parts[s].n];
+    }
     const int n = offsets.back();
+    const long long kbase = kb[ns], rbase = rb[ns];
+    const size_t w = 61;
     dst.n = n;
+    // every array sized once, then each specimen's particles copied in
+    // parallel (no reallocation; the result equals appending the parts)
+    dst.xyz.resize(3 * (size_t)n);
+    dst.nbr.resize((size_t)n * LPM_NN);
+    dst.shell.resize((size_t)n * LPM_NN);
+    dst.nb.resize(n);
+    dst.rev.resize((size_t)n * LPM_NN);
+    dst.L0.resize((size_t)n * LPM_NN);
+    dst.cs0.resize((size_t)n * LPM_NN * 3);
+    dst.oppv.resize((size_t)n * LPM_NN);
+    dst.conn.resize((size_t)n * w);
+    dst.nconn.resize(n);
+    dst.npad.resize(n);
+    dst.cols.resize((size_t)rbase);
     dst.kp0.assign(n + 1, 0);
     dst.kp1.assign(n + 1, 0);
     dst.rowoff.assign(n + 1, 0);
-    long long kbase = 0, rbase = 0;
-    for (size_t s = 0; s < parts.size(); s++) {
+    for (size_t s = 0; s < ns; s++) {
         const HostSetup &p = parts[s];
         const int o = offsets[s];
-        dst.xyz.insert(dst.xyz.end(), p.xyz.begin(), p.xyz.end());
-        for (int v : p.nbr)
-            dst.nbr.push_back(v >= 0 ? v + o : v);
-        dst.shell.insert(dst.shell.end(), p.shell.begin(), p.shell.end());
-        dst.nb.insert(dst.nb.end(), p.nb.begin(), p.nb.end());
-        dst.rev.insert(dst.rev.end(), p.rev.begin(), p.rev.end());
-        dst.L0.insert(dst.L0.end(), p.L0.begin(), p.L0.end());
-        dst.cs0.insert(dst.cs0.end(), p.cs0.begin(), p.cs0.end());
-        dst.oppv.insert(dst.oppv.end(), p.oppv.begin(), p.oppv.end());
-        for (int v : p.conn)
-            dst.conn.push_back(v >= 0 ? v + o : v);
-        dst.nconn.insert(dst.nconn.end(), p.nconn.begin(), p.nconn.end());
-        dst.npad.insert(dst.npad.end(), p.npad.begin(), p.npad.end());
-        for (int v : p.cols)
-            dst.cols.push_back(v + o);
+        const long long kbs = kb[s], rbs = rb[s];
+#pragma omp parallel for schedule(static)
         for (int i = 0; i < p.n; i++) {
-            dst.kp0[o + i] = p.kp0[i];
-            dst.kp1[o + i] = (int)(p.kp1[i] + kbase);
-            dst.rowoff[o + i] = p.rowoff[i] + rbase;
+            const size_t gi = (size_t)o + i;
+            for (int d = 0; d < 3; d++)
+                dst.xyz[3 * gi + d] = p.xyz[3 * (size_t)i + d];
+            for (int j = 0; j < LPM_NN; j++) {
+                const size_t a = (size_t)i * LPM_NN + j, g = gi * LPM_NN + j;
+                const int v = p.nbr[a];
+                dst.nbr[g] = v >= 0 ? v + o : v;
+                dst.shell[g] = p.shell[a];
+                dst.rev[g] = p.rev[a];
+                dst.L0[g] = p.L0[a];
+                dst.oppv[g] = p.oppv[a];
+                for (int d = 0; d < 3; d++)
+                    dst.cs0[3 * g + d] = p.cs0[3 * a + d];
+            }
+            dst.nb[gi] = p.nb[i];
+            for (size_t k = 0; k < w; k++) {
+                const int v = p.conn[(size_t)i * w + k];
+                dst.conn[gi * w + k] = v >= 0 ? v + o : v;
+            }
+            dst.nconn[gi] = p.nconn[i];
+            dst.npad[gi] = p.npad[i];
+            const long long r0 = p.rowoff[i], r1 = p.rowoff[i + 1];
+            for (long long k = r0; k < r1; k++)
+                dst.cols[(size_t)(rbs + k)] = p.cols[(size_t)k] + o;
+            dst.kp0[gi] = p.kp0[i];
+            dst.kp1[gi] = (int)(p.kp1[i] + kbs);
+            dst.rowoff[gi] = r0 + rbs;
         }
-        kbase += p.kp1[p.n];
-        rbase += p.rowoff[p.n];
     }
     dst.kp1[n] = (int)kbase;
     dst.rowoff[n] = rbase;
