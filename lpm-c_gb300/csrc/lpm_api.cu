@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -392,6 +393,8 @@ int lpm_create(lpm_ctx **out, int device)
     cudaEventCreate(&c.ev_a);
     cudaEventCreate(&c.ev_b);
     lpm_default_solver_opts(&c.opts);
+    const char *tr = std::getenv("LPM_TRACE");
+    c.trace = tr && tr[0] && std::strcmp(tr, "0") != 0;
     *out = x;
     return LPM_OK;
 }
@@ -763,6 +766,9 @@ int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
             if (rel > c.opts.cg_rtol)
                 st->status |= std::isfinite(rel) ? LPM_STATUS_CG_MAXIT : LPM_STATUS_NAN;
         }
+        if (c.trace)
+            std::fprintf(stderr, "lpm: solve fp32-K/fp64-vec |b| %.6e iters %d sweeps %d rel %.3e end %d\n", bn,
+                         it, sweeps, rel, done);
         launch_scale_copy(c, c.du, c.x_d, bn);
         return LPM_OK;
     }
@@ -779,6 +785,8 @@ int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
             if (done == 3)
                 st->status |= LPM_STATUS_NAN;
         }
+        if (c.trace)
+            std::fprintf(stderr, "lpm: solve fp64 |b| %.6e iters %d end %d\n", bn, it, done);
         launch_scale_copy(c, c.du, c.x_d, bn);
         return LPM_OK;
     }
@@ -815,6 +823,9 @@ int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
         st->spmv_calls += it + sweeps;
         st->refine_iters += sweeps;
     }
+    if (c.trace)
+        std::fprintf(stderr, "lpm: solve fp32 |b| %.6e iters %d sweeps %d rel %.3e end %d%s\n", bn, it, sweeps,
+                     rn / bn, done, stagnated ? " stagnated" : "");
     if (stagnated) {
         // redo this solve, and the context's later ones, with FP64 vectors
         // (the FP32 stiffness and products stay)
@@ -1183,6 +1194,10 @@ int lpm_load_step(lpm_ctx *ctx, int nbd, const lpm_disp_bc *dbc, int nbf, const 
     const double tolm = std::max(res, reac);
     st.res0 = res;
     st.reac0 = reac;
+    c.trace_step++;
+    if (c.trace)
+        std::fprintf(stderr, "lpm: step %lld res0 %.6e reac0 %.6e target %.6e stiffness %.1f ms\n", c.trace_step,
+                     res, reac, c.opts.newton_tol * tolm, st.ms_stiffness);
     int ni = 0;
     AndersonRun ar;
     if (c.opts.newton_accel > 0) {
@@ -1216,6 +1231,10 @@ int lpm_load_step(lpm_ctx *ctx, int nbd, const lpm_disp_bc *dbc, int nbf, const 
                 return rc;
             st.ms_force += t.stop();
         }
+        if (c.trace)
+            std::fprintf(stderr, "lpm: step %lld newton %d res %.6e ratio %.3e step totals: cg %d sweeps %d solve %.1f ms force %.1f ms\n",
+                         c.trace_step, ni + 1, res, res / std::max(res_best, 1e-300), st.cg_iters, st.refine_iters,
+                         st.ms_solve, st.ms_force);
         if (ar.m > 0 && res > 10.0 * res_best) {  // safeguard: drop the history
             ar.hist = 0;
             ar.head = 0;

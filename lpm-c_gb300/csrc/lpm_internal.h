@@ -246,6 +246,8 @@ struct Ctx {
     bool graph_timed = false;
     bool time_this = false;  // the next SpMV launch carries the timing events
     bool vec64_fallback = false;  // mixed: FP32-vector PCG stagnated, use FP64 vectors
+    bool trace = false;           // LPM_TRACE set: one stderr line per Newton iteration and solve
+    long long trace_step = 0;     // load steps run by this context (trace numbering)
     // batched specimens (lpm_setup_batch); nspec == 0 for a single specimen
     int nspec = 0;
     BatchCg bcg;

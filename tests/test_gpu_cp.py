@@ -67,3 +67,27 @@ def test_fcc_cp_steps_match_oracle(oracle_mod, gpu_lib, precision):
     assert np.abs(s.get("cp_A") - A_o).max() <= 1e-8 * A_o.max()
     gy_o = o.d("cp_gy1", (n, 24))
     assert np.abs(s.get("cp_gy") - gy_o).max() <= 1e-8 * np.abs(gy_o).max()
+
+
+@pytest.mark.parametrize("steps", [0, 3])
+def test_fcc_stiffness_vs_fd(oracle_mod, gpu_lib, steps):
+    """Analytic tangent vs the reference's forward-difference K on the FCC
+    lattice (calcStiffness3DFiniteDifference differentiates the elastic bond
+    force for every material model), at rest and after three [001] tension
+    steps, where the force-dependent (geometric) terms are non-zero."""
+    case = cases.FCCCase(ncell=4, newton_tol=1e-10)
+    s, _ = fcc_gpu(gpu_lib, case, newton_maxiter=300, cg_rtol=1e-11)
+    o, _ = fcc_oracle(oracle_mod, case)
+    for stp in case.schedule[:steps]:
+        assert s.load_step(cases.sc_bcs(stp))["status"] == 0
+        o.load_step(cases.sc_bcs(stp), [], 1e-10, 300, 1e-22, 0.0)
+    o.fd_stiffness()
+    s.assemble_stiffness()
+    K, IK, JK = s.export_upper_csr()
+    nnz = o.nnz
+    assert np.array_equal(IK, o.i("IK", (3 * o.n + 1,)))
+    assert np.array_equal(JK, o.i("JK", (nnz,)))
+    Kf = o.d("K_global", (nnz,))
+    rel = np.linalg.norm(K - Kf) / np.linalg.norm(Kf)
+    # forward differences with h = 1e-6 r: truncation ~1e-6 relative
+    assert rel < 1e-5, rel
