@@ -76,6 +76,38 @@ def sc_bcs(step_z):
             (T_TOP, "z", step_z)]
 
 
+def sc_force_bcs(fx, fz):
+    """Force-controlled variant (setForceBC, src/boundary.c:50-70): bottom z
+    fixed and the pins as in sc_bcs; the top layer carries the per-step force
+    increment (fx, 0, fz), shared equally by its particles.
+    Returns (displacement BCs, force BCs)."""
+    disp = [(T_BOTTOM, "z", 0.0), (T_PIN_XY, "x", 0.0), (T_PIN_XY, "y", 0.0),
+            (T_PIN_XY, "z", 0.0), (T_PIN_Y, "y", 0.0), (T_PIN_Y, "z", 0.0)]
+    return disp, [(T_TOP, fx, 0.0, fz)]
+
+
+class ForceCase:
+    """SC J2 specimen nx x ny x nz under a top-face force ramp: `steps` equal
+    increments of (fx, 0, fz) N.  Yield starts at step 4; the reference's
+    modified Newton converges through step 8 (96 iterations there) and not
+    beyond, where the force approaches the specimen's limit load."""
+
+    def __init__(self, nx=6, ny=6, nz=8, radius=0.1, E=200e3, nu=0.3, sigmay=150.0, H=2000.0,
+                 fz=20.0, fx=2.0, steps=8, newton_tol=1e-8):
+        self.lattice, self.radius = 2, radius
+        self.box = sc_box(nx, ny, nz, radius)
+        self.E, self.nu, self.sigmay, self.H = E, nu, sigmay, H
+        self.fz, self.fx, self.steps = fz, fx, steps
+        self.newton_tol = newton_tol
+        self.e_noise, self.seed = 0.0, 1
+
+    def ce_per_type(self):
+        return np.tile(iso_cubic(self.E, self.nu), (NTYPE, 1))
+
+    def bcs(self):
+        return sc_force_bcs(self.fx, self.fz)
+
+
 def cyclic_schedule(amplitude, steps_per_quarter, cycles):
     """Increments 0->+A->0->-A->0 per cycle, steps_per_quarter equal steps each."""
     inc = amplitude / steps_per_quarter

@@ -2,7 +2,8 @@
 
 Runs the reference's own C sources (built by oracle/build_ref.sh into
 oracle/_ref/libref_lpm.so, MKL replaced by the public-API shim) on the SC
-cyclic case at 10x10x10 (C1) and a small FCC crystal-plasticity case, and
+cyclic case at 10x10x10 (C1), a small FCC crystal-plasticity case and a
+force-controlled SC case (setForceBC), and
 stores inputs and outputs as compressed .npz fixtures.  The reference runs
 single-threaded (its OpenMP loops race, see src/constitutive.c:95 with
 :495-515,625-645), so the fixtures are deterministic.
@@ -160,11 +161,49 @@ def fcc_case(out, nsteps, tag="fcc4"):
     np.savez_compressed(os.path.join(out, f"{tag}_cp.npz"), **arrs)
 
 
+def force_case(out, tag="sc_force"):
+    """Force-controlled SC J2 case (setForceBC): top-face force ramp into the
+    plastic range, x and z components."""
+    case = cases.ForceCase()
+    t0 = time.time()
+    n = R.setup(case.lattice, case.radius, case.box)
+    nn = R.gint("nneighbors")
+    xyz0 = R.get_d2("xyz", n, 3)
+    types = cases.sc_types(xyz0, R.get_i1("nb", n), case.radius)
+    R.set_types(types, cases.NTYPE)
+    R.material(case.ce_per_type(), 0, np.full(n, case.sigmay), 0.0, case.H)
+    R.init_state()
+    R.set_cg_tol(1e-20, 0.0)
+    disp, force = case.bcs()
+    rec = {k: [] for k in ("iters", "nres0", "nreac0", "nres", "disp_top_x", "disp_top_z")}
+    top = types == cases.T_TOP
+    arrs = dict(box=np.array(case.box), types=types, xyz=xyz0)
+    for s in range(1, case.steps + 1):
+        with R.quiet():
+            st = R.load_step(disp, force, case.newton_tol)
+        xyz = R.get_d2("xyz", n, 3)
+        rec["iters"].append(st[0])
+        rec["nres0"].append(st[1])
+        rec["nreac0"].append(st[2])
+        rec["nres"].append(st[3])
+        rec["disp_top_x"].append((xyz[top, 0].sum() - xyz0[top, 0].sum()) / top.sum())
+        rec["disp_top_z"].append((xyz[top, 2].sum() - xyz0[top, 2].sum()) / top.sum())
+        print(f"{tag} step {s}: iters {int(st[0])} res {st[3]:.3e} t={time.time() - t0:.1f}s", flush=True)
+    for k, v in rec.items():
+        arrs[k] = np.array(v)
+    arrs["s_xyz"] = R.get_d2("xyz", n, 3)
+    arrs["s_alpha"] = R.get_d2("J2_alpha", n, 3)[:, 1]
+    arrs["s_dLp"] = R.get_d3("dLp", n, nn, 1)
+    arrs["s_Pex"] = R.get_d1("Pex", 3 * n)
+    arrs["s_F"] = R.get_d2("F", n, nn)
+    np.savez_compressed(os.path.join(out, f"{tag}.npz"), **arrs)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--fcc-steps", type=int, default=12)
-    ap.add_argument("--only", choices=["sc", "fcc"], default=None)
+    ap.add_argument("--only", choices=["sc", "fcc", "force"], default=None)
     ap.add_argument("--out", default=HERE)
     args = ap.parse_args()
     if not R.available():
@@ -172,11 +211,13 @@ def main():
     # the reference keeps all state in process globals: one case per process
     if args.only == "fcc":
         fcc_case(args.out, args.fcc_steps)
+    elif args.only == "force":
+        force_case(args.out)
     elif args.only == "sc":
         sc_case(args.out, args.steps)
     else:
         import subprocess
-        for which in ("sc", "fcc"):
+        for which in ("sc", "fcc", "force"):
             subprocess.check_call([sys.executable, __file__, "--only", which, "--steps", str(args.steps),
                                    "--fcc-steps", str(args.fcc_steps), "--out", args.out])
 

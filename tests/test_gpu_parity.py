@@ -146,3 +146,29 @@ def test_load_steps_match_oracle(oracle_mod, gpu_lib, precision):
         err = np.abs(du_g - du_o).max() / np.abs(du_o).max()
         assert err < 1e-8, (k + 1, err, st, so)
     assert np.abs(s.get("J2_alpha") - o.d("alpha1", (n,))).max() < 1e-10
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_force_bc_steps_match_oracle(oracle_mod, gpu_lib, precision):
+    """Force-controlled loading (setForceBC, src/boundary.c:50-70): the top
+    layer carries a growing (x, z) force, the bottom is held in z; 8 steps
+    into the plastic range, both sides converged to 1e-10.  External forces
+    bit-exact, displacements and plastic strain within 1e-8 of the oracle."""
+    case = cases.ForceCase(newton_tol=1e-10)
+    o, types = sc_oracle(oracle_mod, case, threads=4)
+    s, _ = sc_gpu(gpu_lib, case, precision=precision, newton_maxiter=300, cg_rtol=1e-10)
+    n = o.n
+    x0 = o.d("xyz_initial", (n, 3))
+    disp, force = case.bcs()
+    for k in range(case.steps):
+        st = s.load_step(disp, force)
+        o.load_step(disp, force, 1e-10, 300, 1e-20, 0.0)
+        assert st["status"] == 0, (k + 1, st)
+        assert np.array_equal(s.get("Pex"), o.d("Pex", (n, 3))), k + 1
+        du_g = s.get("xyz") - x0
+        du_o = o.d("xyz", (n, 3)) - x0
+        err = np.abs(du_g - du_o).max() / np.abs(du_o).max()
+        assert err < 1e-8, (k + 1, err, st)
+    a_o = o.d("alpha1", (n,))
+    assert a_o.max() > 0.0
+    assert np.abs(s.get("J2_alpha") - a_o).max() <= 1e-8 * a_o.max()

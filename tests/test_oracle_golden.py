@@ -206,3 +206,28 @@ def test_fcc_schmid_factors_001():
     assert np.sum(np.isclose(m, 1 / np.sqrt(6))) == 8
     assert np.sum(np.isclose(m, -1 / np.sqrt(6))) == 8
     assert np.sum(np.isclose(m, 0.0)) == 8
+
+
+def test_force_bc_bit_exact(oracle_mod):
+    """Force-controlled SC J2 case (setForceBC, src/boundary.c:50-70): a
+    top-face force ramp with x and z components into the plastic range."""
+    case = cases.ForceCase()
+    o, types = sc_oracle(oracle_mod, case, threads=1)
+    g = golden("sc_force.npz")
+    n = o.n
+    assert np.array_equal(types, g["types"])
+    x0 = o.d("xyz_initial", (n, 3))
+    top = types == cases.T_TOP
+    disp, force = case.bcs()
+    for k in range(case.steps):
+        st = o.load_step(disp, force, case.newton_tol, 100, 1e-20, 0.0)
+        assert st[0] == g["iters"][k], k
+        assert st[1] == g["nres0"][k] and st[2] == g["nreac0"][k], k
+        xyz = o.d("xyz", (n, 3))
+        assert (xyz[top, 0].sum() - x0[top, 0].sum()) / top.sum() == g["disp_top_x"][k], k
+        assert (xyz[top, 2].sum() - x0[top, 2].sum()) / top.sum() == g["disp_top_z"][k], k
+    assert np.array_equal(o.d("xyz", (n, 3)), g["s_xyz"])
+    assert np.array_equal(o.d("alpha1", (n,)), g["s_alpha"])
+    assert g["s_alpha"].max() > 0.0
+    assert np.array_equal(o.d("Pex", (3 * n,)), g["s_Pex"])
+    assert np.array_equal(o.d("F", (n, 18)), g["s_F"])
