@@ -60,6 +60,16 @@ struct lpm_oracle {
     double *Cab, *cp_RSS, *cp_dA, *cp_dgy, *cp_dAs;
     int *Jact;
     int error;
+    /* damage (src/constitutive.c:1399-1862): per bond damage_broken (brk),
+     * damage_w (dw), damage_D (dD, slots 0 and 1); per particle
+     * damage_nonlocal (dnl, slots 0 and 1), damage_visual (dvis), the current
+     * bond count nb (nbc; o->nb holds nb_initial) and fix_index (fix, per
+     * DOF); the damage parameters and the broken-bond log (pairs i, j). */
+    double *brk, *dw, *dD[2], *dnl[2], *dvis;
+    int *nbc, *fix;
+    double dmg_L, dmg_thr, dmg_cA, dmg_crit;
+    int dmg_nbreak;
+    int *blog, nblog, blog_cap;
 };
 
 static void *xcalloc(size_t n, size_t s)
@@ -95,7 +105,8 @@ void lo_free(lpm_oracle *o)
                     o->G, o->sy, o->H, o->dlambda, o->dL, o->Ssum, o->Tsum, o->csx, o->csy,
                     o->csz, o->F, o->F_temp, o->ddLp, o->ddL, o->ddS, o->ddT, o->Pin, o->Pex,
                     o->Pex_temp, o->residual, o->reaction, o->disp, o->stress, o->mask, o->Cab,
-                    o->cp_RSS, o->cp_dA, o->cp_dgy, o->cp_dAs, o->Jact};
+                    o->cp_RSS, o->cp_dA, o->cp_dgy, o->cp_dAs, o->Jact, o->brk, o->dw, o->dD[0],
+                    o->dD[1], o->dnl[0], o->dnl[1], o->dvis, o->nbc, o->fix, o->blog};
     for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); k++)
         free(ptrs[k]);
     for (int s = 0; s < 3; s++) {
@@ -449,6 +460,27 @@ static void alloc_state(lpm_oracle *o)
     o->mask = IALLOC(3 * n);
     for (int k = 0; k < 3 * n; k++)
         o->mask[k] = 1;
+    /* damage state as initMatrices leaves it (src/initialization.c:1120-1194):
+     * intact bonds, no damage, nothing fixed; parameters as the reference's
+     * main sets them (src/lpmc_project.c:239-244) */
+    o->brk = DALLOC(nb);
+    o->dw = DALLOC(nb);
+    for (size_t k = 0; k < nb; k++)
+        o->brk[k] = o->dw[k] = 1.0;
+    o->dD[0] = DALLOC(nb);
+    o->dD[1] = DALLOC(nb);
+    o->dnl[0] = DALLOC(n);
+    o->dnl[1] = DALLOC(n);
+    o->dvis = DALLOC(n);
+    o->nbc = IALLOC(n);
+    o->fix = IALLOC(3 * n);
+    for (int k = 0; k < 3 * n; k++)
+        o->fix[k] = 1;
+    o->dmg_L = 0.5;
+    o->dmg_thr = 0.9;
+    o->dmg_cA = 0.0;
+    o->dmg_crit = 1.0e-2;
+    o->dmg_nbreak = 20;
 }
 
 static int finish_setup(lpm_oracle *o)
@@ -457,6 +489,7 @@ static int finish_setup(lpm_oracle *o)
     alloc_state(o);
     memcpy(o->xyz0, o->xyz, sizeof(double) * 3 * o->n);
     search_neighbors(o);
+    memcpy(o->nbc, o->nb, sizeof(int) * o->n);
     search_afem(o);
     bond_tables(o);
     lo_csr_pattern(o);
@@ -541,7 +574,7 @@ static void stretch_one(lpm_oracle *o, int i, const double *plastic, double *dL,
         double dis = sqrt(dx * dx + dy * dy + dz * dz);
         double v = dis - o->L0[b];
         v -= plastic[b];
-        v *= 1.0; /* damage_broken */
+        v *= o->brk[b]; /* damage_broken */
         dL[j] = v;
         S[o->shell[b]] += v;
         T[o->shell[b]] += o->Tv[b] * v;
@@ -577,7 +610,7 @@ static void force_elastic_one(lpm_oracle *o, int ii)
     int list[19], nl = 1;
     list[0] = ii;
     for (int k = 0; k < nn; k++)
-        if (o->nbr[(size_t)ii * nn + k] != -1)
+        if (o->brk[(size_t)ii * nn + k] > EPSP && o->nbr[(size_t)ii * nn + k] != -1)
             list[nl++] = o->nbr[(size_t)ii * nn + k];
     for (int k = 0; k < nl; k++) {
         int i = list[k];
@@ -590,7 +623,7 @@ static void force_elastic_one(lpm_oracle *o, int ii)
         int p = o->nbr[b], s = o->shell[b];
         double f = 2.0 * o->Kn[b] * o->dL[b] + 0.5 * (o->Tsum[2 * i + s] + o->Tsum[2 * p + s]) +
                    0.5 * o->Tv[b] * (o->Ssum[2 * i + s] + o->Ssum[2 * p + s]);
-        f *= 1.0;
+        f *= o->brk[b]; /* damage_broken */
         o->F[b] = f;
         o->Pin[3 * i] += o->csx[b] * f;
         o->Pin[3 * i + 1] += o->csy[b] * f;
@@ -781,7 +814,7 @@ void lo_bc_stiffness_update(lpm_oracle *o)
     free(diag);
     for (int i = 0; i < n; i++) {
         for (int d = 0; d < 3; d++) {
-            if (o->mask[3 * i + d] != 0)
+            if (o->mask[3 * i + d] != 0 && o->fix[3 * i + d] != 0)
                 continue;
             for (int jc = 0; jc < o->nconn[i]; jc++) {
                 int c = o->conn[(size_t)i * w + jc];
@@ -933,6 +966,24 @@ int lo_cg_iterations(lpm_oracle *o, int nit)
     return it;
 }
 
+/* opp_flag of bond b of particle i as the force and stress routines compute
+ * it (src/constitutive.c:532-551, src/lpm_basic.c:70-90): 0.5 when i keeps
+ * all its bonds, else 0.5 if the bond has an opposite bond that is intact,
+ * 1.0 otherwise.  Equal to the setup table o->opp while no bond is broken. */
+static double opp_now(const lpm_oracle *o, int i, size_t b)
+{
+    int nn = o->nn;
+    if (o->nbc[i] == nn)
+        return 0.5;
+    for (int m = 0; m < o->nb[i]; m++) {
+        size_t c = (size_t)i * nn + m;
+        if (fabs(o->cs0x[c] + o->cs0x[b]) < EPSP && fabs(o->cs0y[c] + o->cs0y[b]) < EPSP &&
+            fabs(o->cs0z[c] + o->cs0z[b]) < EPSP)
+            return o->brk[c] <= EPSP ? 1.0 : 0.5;
+    }
+    return 1.0;
+}
+
 /* computeStress, src/lpm_basic.c:53-109 (stress tensor only) */
 static void stress_all(lpm_oracle *o)
 {
@@ -944,7 +995,7 @@ static void stress_all(lpm_oracle *o)
             st[k] = 0.0;
         for (int j = 0; j < o->nb[i]; j++) {
             size_t b = (size_t)i * nn + j;
-            double w = o->opp[b] / o->vol * o->L0[b] * o->F[b];
+            double w = opp_now(o, i, b) / o->vol * o->L0[b] * o->F[b];
             st[0] += w * o->csx[b] * o->csx[b];
             st[1] += w * o->csy[b] * o->csy[b];
             st[2] += w * o->csz[b] * o->csz[b];
@@ -974,7 +1025,7 @@ static void force_predictor(lpm_oracle *o)
                              (a0[2] - b0[2]) * (a0[2] - b0[2]));
             double d1 = sqrt((a1[0] - b1[0]) * (a1[0] - b1[0]) + (a1[1] - b1[1]) * (a1[1] - b1[1]) +
                              (a1[2] - b1[2]) * (a1[2] - b1[2]));
-            double v = 1.0 * (d1 - d0);
+            double v = o->brk[b] * (d1 - d0);
             o->ddL[b] = v;
             o->ddS[2 * i + o->shell[b]] += v;
             o->ddT[2 * i + o->shell[b]] += o->Tv[b] * v;
@@ -988,7 +1039,7 @@ static void force_predictor(lpm_oracle *o)
             int p = o->nbr[b], s = o->shell[b];
             double f = o->F_temp[b] + 2.0 * o->Kn[b] * o->ddL[b] + 0.5 * (o->ddT[2 * i + s] + o->ddT[2 * p + s]) +
                        0.5 * o->Tv[b] * (o->ddS[2 * i + s] + o->ddS[2 * p + s]);
-            f *= 1.0;
+            f *= o->brk[b]; /* damage_broken */
             o->F[b] = f;
             o->Pin[3 * i] += o->csx[b] * f;
             o->Pin[3 * i + 1] += o->csy[b] * f;
@@ -1010,8 +1061,8 @@ static void trial_stress(const lpm_oracle *o, int i, const double *dL, const dou
         size_t b = (size_t)i * nn + j;
         int s = o->shell[b];
         double fij = 2.0 * o->Kn[b] * dL[j] + T[s] + o->Tv[b] * S[s];
-        fij *= 1.0; /* damage_w */
-        double w = o->opp[b] / o->vol * o->L0[b] * fij;
+        fij *= o->dw[b]; /* damage_w */
+        double w = opp_now(o, i, b) / o->vol * o->L0[b] * fij;
         st[0] += w * cx[j] * cx[j];
         st[1] += w * cy[j] * cy[j];
         st[2] += w * cz[j] * cz[j];
@@ -1078,10 +1129,10 @@ static void j2_return_one(lpm_oracle *o, int i)
             add = o->L0[b] * (dpl[0] * cx[j] * cx[j] + dpl[1] * cy[j] * cy[j] + dpl[2] * cz[j] * cz[j] +
                               2 * dpl[3] * cy[j] * cz[j] + 2 * dpl[4] * cx[j] * cz[j] +
                               2 * dpl[5] * cx[j] * cy[j]);
-            add *= 1.0;
+            add *= o->brk[b]; /* damage_broken */
             o->ddLp[b] = add;
         }
-        o->dLp[2][b] = 1.0 * (o->dLp[0][b] + add);
+        o->dLp[2][b] = o->brk[b] * (o->dLp[0][b] + add);
     }
     for (int k = 0; k < 6; k++)
         o->beta[2][6 * i + k] = beta[k];
@@ -1231,7 +1282,7 @@ static void cp_return_one(lpm_oracle *o, int i)
                     size_t b = (size_t)i * nn + j;
                     double v = o->L0[b] * (dpl[0] * cx[j] * cx[j] + dpl[1] * cy[j] * cy[j] + dpl[2] * cz[j] * cz[j] +
                                            dpl[3] * cy[j] * cz[j] + dpl[4] * cx[j] * cz[j] + dpl[5] * cx[j] * cy[j]);
-                    v *= 1.0;
+                    v *= o->brk[b]; /* damage_broken */
                     ddlp[j] = v;
                     xdL[j] = dL[j] - v;
                     xS[o->shell[b]] += xdL[j];
@@ -1330,7 +1381,7 @@ static void cp_return_one(lpm_oracle *o, int i)
     }
     for (int j = 0; j < nn; j++) {
         size_t b = (size_t)i * nn + j;
-        o->dLp[2][b] = 1.0 * (o->dLp[0][b] + (j < nbi ? ddlp[j] : 0.0));
+        o->dLp[2][b] = o->brk[b] * (o->dLp[0][b] + (j < nbi ? ddlp[j] : 0.0));
     }
     for (int s = 0; s < ns; s++) {
         double das = J[s] * gamma[s];
@@ -1357,7 +1408,7 @@ static void final_forces(lpm_oracle *o)
             double dla = 0.5 * (o->dL[b] + o->dL[(size_t)p * nn + o->rev[b]]);
             double f = 2.0 * o->Kn[b] * dla + 0.5 * (o->Tsum[2 * i + s] + o->Tsum[2 * p + s]) +
                        0.5 * o->Tv[b] * (o->Ssum[2 * i + s] + o->Ssum[2 * p + s]);
-            f *= 1.0; /* damage_w */
+            f *= o->dw[b]; /* damage_w */
             o->F[b] = f;
             o->Pin[3 * i] += o->csx[b] * f;
             o->Pin[3 * i + 1] += o->csy[b] * f;
@@ -1378,6 +1429,10 @@ void lo_switch_state(lpm_oracle *o, int flag)
         memcpy(o->cp_gy[to], o->cp_gy[from], ns * sizeof(double));
         memcpy(o->cp_As[to], o->cp_As[from], ns * sizeof(double));
         memcpy(o->cp_A[to], o->cp_A[from], o->n * sizeof(double));
+    }
+    if (flag == 0 || flag == 1) { /* damage_D, damage_nonlocal: slots 0 and 1 only */
+        memcpy(o->dD[to], o->dD[from], nb * sizeof(double));
+        memcpy(o->dnl[to], o->dnl[from], o->n * sizeof(double));
     }
 }
 
@@ -1403,6 +1458,7 @@ void lo_force(lpm_oracle *o, int plmode)
                 int p = o->nbr[b], s = o->shell[b];
                 double f = 2.0 * o->Kn[b] * o->dL[b] + 0.5 * (o->Tsum[2 * i + s] + o->Tsum[2 * p + s]) +
                            0.5 * o->Tv[b] * (o->Ssum[2 * i + s] + o->Ssum[2 * p + s]);
+                f *= o->brk[b]; /* damage_broken */
                 o->F[b] = f;
                 o->Pin[3 * i] += o->csx[b] * f;
                 o->Pin[3 * i + 1] += o->csy[b] * f;
@@ -1498,6 +1554,269 @@ int lo_load_step(lpm_oracle *o, int nbd, const lo_disp_bc *d, int nbf, const lo_
 }
 
 /* ---------------------------------------------------------------------- */
+/* damage and bond breaking (src/constitutive.c:149-164, :1399-1862) */
+
+void lo_set_damage(lpm_oracle *o, double L, double threshold, double cA, double crit_bstrain, int nbreak)
+{
+    o->dmg_L = L;
+    o->dmg_thr = threshold;
+    o->dmg_cA = cA;
+    o->dmg_crit = crit_bstrain;
+    o->dmg_nbreak = nbreak;
+}
+
+static void log_bond(lpm_oracle *o, int i, int j)
+{
+    if (o->nblog == o->blog_cap) {
+        o->blog_cap = o->blog_cap ? 2 * o->blog_cap : 256;
+        o->blog = (int *)realloc(o->blog, sizeof(int) * 2 * (size_t)o->blog_cap);
+        if (!o->blog) {
+            fprintf(stderr, "lpm_oracle: out of memory\n");
+            abort();
+        }
+    }
+    o->blog[2 * o->nblog] = i;
+    o->blog[2 * o->nblog + 1] = j;
+    o->nblog++;
+}
+
+/* updateDuctileDamagePwiseNonlocal, src/constitutive.c:1757-1862: nonlocal
+ * damage rate of particle i = Gaussian-weighted (length L, cut at 3L)
+ * average over all particles j of dlambda_j (1 + A triaxiality_j) at the
+ * initial positions, summed in ascending j; particles past the threshold are
+ * clamped to 1 and lose every bond; intact bonds carry D = max of the two
+ * particles' damage and w = 1 - D.  J2_triaxiality is never assigned in the
+ * reference, so it is 0 here. */
+static int damage_ductile_nonlocal(lpm_oracle *o)
+{
+    int n = o->n, nn = o->nn;
+    const double L = o->dmg_L, thr = o->dmg_thr, cA = o->dmg_cA;
+    const double PI_ = 3.14159265358979323846; /* include/lpm.h:34 */
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int i = 0; i < n; i++) {
+        if (o->dnl[0][i] > thr) {
+            if (o->dnl[0][i] > 1.0)
+                o->dnl[0][i] = 1.0;
+            continue;
+        }
+        double Ddot = 0, A = 0;
+        for (int j = 0; j < n; j++) {
+            double DdotLocal = 0;
+            double ex = o->xyz0[3 * j] - o->xyz0[3 * i], ey = o->xyz0[3 * j + 1] - o->xyz0[3 * i + 1],
+                   ez = o->xyz0[3 * j + 2] - o->xyz0[3 * i + 2];
+            double dis = sqrt(ex * ex + ey * ey + ez * ez);
+            if (dis < 3 * L) {
+                double triax = 0.0;
+                double damage_f = (1.0 + cA * triax);
+                if (damage_f > 0.0)
+                    DdotLocal = o->dlambda[j] * (1.0 + cA * triax);
+                double phi = 1.0 / L / sqrt(2 * PI_) * exp(-0.5 * dis * dis / L / L);
+                Ddot += DdotLocal * phi * o->vol;
+                A += phi * o->vol;
+            }
+        }
+        if (Ddot > 0.0)
+            o->dnl[0][i] += 1.0 / A * Ddot;
+    }
+    int k = 0;
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < o->nb[i]; j++) {
+            size_t b = (size_t)i * nn + j;
+            int p = o->nbr[b];
+            if (o->dnl[0][i] > thr || o->dnl[0][p] > thr) {
+                if (fabs(o->brk[b]) > EPSP) {
+                    o->brk[b] = 0.0;
+                    o->dD[0][b] = 1.0;
+                    log_bond(o, i, p);
+                    k++;
+                }
+            }
+        }
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < o->nb[i]; j++) {
+            size_t b = (size_t)i * nn + j;
+            int p = o->nbr[b];
+            if (fabs(o->brk[b]) > EPSP)
+                o->dD[0][b] = o->dnl[0][i] > o->dnl[0][p] ? o->dnl[0][i] : o->dnl[0][p];
+            o->dw[b] = 1.0 - o->dD[0][b];
+        }
+    return k;
+}
+
+/* updateBrittleDamage, src/constitutive.c:1437-1527: bonds whose elastic
+ * stretch / initial length reaches critical_bstrain are candidates (scan
+ * order i, then j); at most nbreak of them break, the largest strains after
+ * the reference's ascending shell sort; returns the number of candidates. */
+static int damage_brittle(lpm_oracle *o)
+{
+    int n = o->n, nn = o->nn, nbreak = o->dmg_nbreak;
+    int cap = 64, k = 0;
+    int *bi = IALLOC(cap), *bj = IALLOC(cap);
+    double *bs = DALLOC(cap);
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < o->nb[i]; j++) {
+            size_t b = (size_t)i * nn + j;
+            double ave_bstrain = o->dL[b] / o->L0[b];
+            if (ave_bstrain >= o->dmg_crit) {
+                if (k == cap) {
+                    cap *= 2;
+                    bi = (int *)realloc(bi, sizeof(int) * cap);
+                    bj = (int *)realloc(bj, sizeof(int) * cap);
+                    bs = (double *)realloc(bs, sizeof(double) * cap);
+                    if (!bi || !bj || !bs) {
+                        fprintf(stderr, "lpm_oracle: out of memory\n");
+                        abort();
+                    }
+                }
+                bi[k] = i;
+                bj[k] = j;
+                bs[k] = ave_bstrain;
+                k++;
+            }
+        }
+    int first = 0;
+    if (k > nbreak) {
+        for (int r = k / 2; r >= 1; r = r / 2)
+            for (int i = r; i < k; ++i) {
+                int ti = bi[i], tj = bj[i];
+                double tb = bs[i];
+                int j = i - r;
+                while (j >= 0 && bs[j] > tb) {
+                    bs[j + r] = bs[j];
+                    bi[j + r] = bi[j];
+                    bj[j + r] = bj[j];
+                    j = j - r;
+                }
+                bs[j + r] = tb;
+                bi[j + r] = ti;
+                bj[j + r] = tj;
+            }
+        first = k - nbreak;
+    }
+    for (int q = first; q < k; q++) {
+        size_t b = (size_t)bi[q] * nn + bj[q];
+        o->dD[0][b] = 1.0;
+        o->dw[b] = 0.0;
+        o->brk[b] = 0.0;
+        log_bond(o, bi[q], o->nbr[b]);
+    }
+    free(bi);
+    free(bj);
+    free(bs);
+    return k;
+}
+
+/* updateDamageGeneral, src/constitutive.c:149-164 (plmode 0: ductile
+ * pointwise nonlocal; 6: brittle; others: none) */
+int lo_damage_update(lpm_oracle *o, int plmode)
+{
+    if (plmode == 0)
+        return damage_ductile_nonlocal(o);
+    if (plmode == 6)
+        return damage_brittle(o);
+    return 0;
+}
+
+/* updateCrack, src/constitutive.c:1399-1434: current bond counts, damage
+ * picture, F scaled by w and Pin re-summed, particles without bonds fixed */
+void lo_update_crack(lpm_oracle *o)
+{
+    int n = o->n, nn = o->nn;
+    for (int i = 0; i < n; i++) {
+        o->nbc[i] = o->nb[i];
+        o->dvis[i] = 0.0;
+        o->Pin[3 * i] = 0.0, o->Pin[3 * i + 1] = 0.0, o->Pin[3 * i + 2] = 0.0;
+        for (int j = 0; j < o->nb[i]; j++) {
+            size_t b = (size_t)i * nn + j;
+            if (o->brk[b] <= EPSP)
+                o->nbc[i] -= 1;
+            o->dvis[i] += o->brk[b];
+            o->F[b] *= o->dw[b];
+            o->Pin[3 * i] += o->csx[b] * o->F[b];
+            o->Pin[3 * i + 1] += o->csy[b] * o->F[b];
+            o->Pin[3 * i + 2] += o->csz[b] * o->F[b];
+        }
+        if (o->nbc[i] < 1) {
+            o->fix[3 * i] = 0;
+            o->fix[3 * i + 1] = 0;
+            o->fix[3 * i + 2] = 0;
+        }
+        o->dvis[i] = 1 - o->dvis[i] / o->nb[i];
+    }
+}
+
+int lo_broken_log(const lpm_oracle *o, int *pairs)
+{
+    if (pairs)
+        memcpy(pairs, o->blog, sizeof(int) * 2 * (size_t)o->nblog);
+    return o->nblog;
+}
+
+/* one load step of the reference's main with its damage stage
+ * (src/lpmc_project.c:385-471 and :528-546): after the Newton loop,
+ * updateDamageGeneral, updateCrack and switchStateV(1); when bonds broke,
+ * the stiffness is recomputed and the same load step re-enters the Newton
+ * loop at label_broken_bond, until a pass breaks nothing.  stats: [0] Newton
+ * iterations over all passes, [1] first |residual|, [2] first |reaction|,
+ * [3] final |residual|, [4] CG iterations, [5] passes, [6] bonds broken
+ * (candidates counted as the reference's return value does). */
+int lo_load_step_damage(lpm_oracle *o, int nbd, const lo_disp_bc *d, int nbf, const lo_force_bc *f,
+                        double newton_tol, int maxiter, double cg_rtol_sq, double cg_atol_sq, int max_passes,
+                        double *stats)
+{
+    int n = o->n;
+    memcpy(o->xyz_temp, o->xyz, sizeof(double) * 3 * n);
+    memcpy(o->F_temp, o->F, sizeof(double) * n * o->nn);
+    memcpy(o->Pex_temp, o->Pex, sizeof(double) * 3 * n);
+    lo_fd_stiffness(o);
+    lo_set_disp_bc(o, nbd, d);
+    lo_set_force_bc(o, nbf, f);
+    lo_force(o, 4);
+    int ni_tot = 0, cg = 0, passes = 0, broken_tot = 0;
+    double nr0 = 0, nreac0 = 0, nr = 0;
+    for (;;) {
+        lo_update_rr(o);
+        nr = cblas_dnrm2(3 * n, o->residual, 1);
+        double nreac = cblas_dnrm2(o->nreact, o->reaction, 1);
+        double tolm = nr > nreac ? nr : nreac;
+        if (passes == 0) {
+            nr0 = nr;
+            nreac0 = nreac;
+        }
+        int ni = 0;
+        while (nr > newton_tol * tolm && ni < maxiter) {
+            lo_switch_state(o, 0);
+            lo_bc_stiffness_update(o);
+            int it = lo_solver_cg(o, cg_rtol_sq, cg_atol_sq);
+            cg += it > 0 ? it : 0;
+            lo_force(o, o->plmode);
+            lo_update_rr(o);
+            ni++;
+            nr = cblas_dnrm2(3 * n, o->residual, 1);
+        }
+        ni_tot += ni;
+        passes++;
+        int broken = lo_damage_update(o, o->plmode);
+        broken_tot += broken;
+        lo_update_crack(o);
+        lo_switch_state(o, 1);
+        if (broken <= 0 || passes >= max_passes)
+            break;
+        lo_fd_stiffness(o);
+    }
+    if (stats) {
+        stats[0] = ni_tot;
+        stats[1] = nr0;
+        stats[2] = nreac0;
+        stats[3] = nr;
+        stats[4] = cg;
+        stats[5] = passes;
+        stats[6] = broken_tot;
+    }
+    return ni_tot;
+}
+
+/* ---------------------------------------------------------------------- */
 int lo_n(const lpm_oracle *o) { return o->n; }
 int lo_nn(const lpm_oracle *o) { return o->nn; }
 int lo_nnz(const lpm_oracle *o) { return o->nnz; }
@@ -1521,6 +1840,8 @@ double *lo_d(lpm_oracle *o, const char *nm)
     D_("cp_A1", o->cp_A[1]); D_("cp_As0", o->cp_As[0]); D_("cp_As1", o->cp_As[1]);
     D_("cp_Cab", o->Cab); D_("schmid", &o->sch[0][0]); D_("KnTve", o->knt); D_("distance", o->dist);
     D_("cp_RSS", o->cp_RSS);
+    D_("damage_broken", o->brk); D_("damage_w", o->dw); D_("damage_D0", o->dD[0]); D_("damage_D1", o->dD[1]);
+    D_("damage_nonlocal0", o->dnl[0]); D_("damage_nonlocal1", o->dnl[1]); D_("damage_visual", o->dvis);
     return NULL;
 #undef D_
 }
@@ -1532,6 +1853,7 @@ int *lo_i(lpm_oracle *o, const char *nm)
     I_("nb_conn", o->nconn); I_("kp0", o->kp0); I_("kp1", o->kp1); I_("IK", o->IK); I_("JK", o->JK);
     I_("type", o->type); I_("rev", o->rev); I_("dispBC_index", o->mask); I_("cp_Jact", o->Jact);
     I_("neighbors1", o->nbr1); I_("neighbors2", o->nbr2); I_("error", &o->error);
+    I_("nb_current", o->nbc); I_("fix_index", o->fix);
     return NULL;
 #undef I_
 }

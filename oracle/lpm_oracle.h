@@ -24,6 +24,10 @@
  *   switchStateV            src/constitutive.c:10-85
  *   updateRR                src/stiffness.c:519-534
  *   load-step Newton loop   src/lpmc_project.c:382-471
+ *   updateDamageGeneral     src/constitutive.c:149-164 (ductile pointwise
+ *                           nonlocal :1757-1862, brittle :1437-1527)
+ *   updateCrack             src/constitutive.c:1399-1434
+ *   main's damage stage and re-solve  src/lpmc_project.c:466-470, :528-546
  * Arithmetic follows the reference's operation order (compile with
  * -ffp-contract=off), and the BLAS/LAPACK/RCI-CG calls go through the same
  * MKL-API shim the reference is linked against, so results are bit-identical
@@ -78,6 +82,16 @@ void lo_set_force_bc(lpm_oracle *o, int n, const lo_force_bc *f);
 void lo_bc_stiffness_update(lpm_oracle *o);
 int lo_solver_cg(lpm_oracle *o, double rtol_sq, double atol_sq);
 void lo_force(lpm_oracle *o, int plmode);
+/* damage parameters (damage_L, damage_threshold, damagec_A,
+ * critical_bstrain, nbreak; defaults as src/lpmc_project.c:239-244) */
+void lo_set_damage(lpm_oracle *o, double L, double threshold, double cA, double crit_bstrain, int nbreak);
+int lo_damage_update(lpm_oracle *o, int plmode);
+void lo_update_crack(lpm_oracle *o);
+/* broken bonds logged so far as (i, neighbour) pairs; pairs may be NULL */
+int lo_broken_log(const lpm_oracle *o, int *pairs);
+int lo_load_step_damage(lpm_oracle *o, int nbd, const lo_disp_bc *d, int nbf, const lo_force_bc *f,
+                        double newton_tol, int maxiter, double cg_rtol_sq, double cg_atol_sq, int max_passes,
+                        double *stats);
 void lo_switch_state(lpm_oracle *o, int flag);
 void lo_update_rr(lpm_oracle *o);
 /* stats: iterations, |r0|, |reaction0|, |r| final, total CG iterations */

@@ -73,6 +73,12 @@ def lib():
         L.lo_i.argtypes = [vp, C.c_char_p]
         L.lo_i.restype = C.POINTER(C.c_int)
         L.lo_set_threads.argtypes = [C.c_int]
+        L.lo_set_damage.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]
+        L.lo_damage_update.argtypes = [vp, C.c_int]
+        L.lo_update_crack.argtypes = [vp]
+        L.lo_broken_log.argtypes = [vp, C.POINTER(C.c_int)]
+        L.lo_load_step_damage.argtypes = [vp, C.c_int, C.POINTER(DispBC), C.c_int, C.POINTER(ForceBC),
+                                          C.c_double, C.c_int, C.c_double, C.c_double, C.c_int, dp]
         _lib = L
     return _lib
 
@@ -180,6 +186,33 @@ class Oracle:
 
     def update_rr(self):
         self.L.lo_update_rr(self.h)
+
+    # ---- damage (updateDamageGeneral, updateCrack, main's re-solve)
+    def set_damage(self, L=0.5, threshold=0.9, cA=0.0, crit_bstrain=1e-2, nbreak=20):
+        self.L.lo_set_damage(self.h, L, threshold, cA, crit_bstrain, nbreak)
+
+    def damage_update(self, plmode):
+        return self.L.lo_damage_update(self.h, plmode)
+
+    def update_crack(self):
+        self.L.lo_update_crack(self.h)
+
+    def broken_log(self):
+        k = self.L.lo_broken_log(self.h, None)
+        out = np.zeros((k, 2), dtype=np.int32)
+        if k:
+            self.L.lo_broken_log(self.h, out.ctypes.data_as(C.POINTER(C.c_int)))
+        return out
+
+    def load_step_damage(self, disp_bcs, force_bcs, newton_tol, maxiter=100, cg_rtol_sq=1e-20,
+                         cg_atol_sq=0.0, max_passes=1000):
+        """stats: Newton iterations (all passes), |r0|, |reaction0|, final |r|, CG
+        iterations, passes, bonds broken."""
+        nd, darr, nf, farr = bc_arrays(disp_bcs, force_bcs)
+        stats = np.zeros(7)
+        self.L.lo_load_step_damage(self.h, nd, darr, nf, farr, newton_tol, maxiter, cg_rtol_sq,
+                                   cg_atol_sq, max_passes, _dp(stats))
+        return stats
 
     def load_step(self, disp_bcs, force_bcs, newton_tol, maxiter=100, cg_rtol_sq=1e-20,
                   cg_atol_sq=0.0):

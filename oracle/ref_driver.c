@@ -16,6 +16,8 @@
  *                      instead of TOLITER, damage/crack updates are skipped
  *                      (the configurations exercised have no damage) and
  *                      computeStrain (output only) is skipped.
+ *   refd_load_step_damage -> the same load step with main's damage stage
+ *                      and re-solve (src/lpmc_project.c:466-470, :528-546).
  * Displacement BCs use the reference's setDispBC/setForceBC on `type`, or,
  * when refd_set_bc_groups() was given a group array (materials per particle
  * need one type per particle), the same semantics restated over the groups.
@@ -190,6 +192,87 @@ int refd_load_step(int nbd, struct dispBCPara *dbp, int nbf, struct forceBCPara 
         stats[4] = cgtot;
     }
     return ni;
+}
+
+/* Damage parameters (the globals src/lpmc_project.c:239-244 sets in main). */
+void refd_set_damage(double L, double threshold, double cA, double crit_bstrain, int nbreak_)
+{
+    damage_L = L;
+    damage_threshold = threshold;
+    damagec_A = cA;
+    critical_bstrain = crit_bstrain;
+    nbreak = nbreak_;
+}
+
+/*
+ * One load step of main with its damage stage (src/lpmc_project.c:385-471
+ * and :528-546): the Newton loop, then computeStrain, updateDamageGeneral
+ * (broken bonds appended to `bondfile`), updateCrack and switchStateV(1);
+ * when bonds broke, calcStiffness3DFiniteDifference and back to
+ * label_broken_bond, until a pass breaks nothing (or max_passes).  stats:
+ * [0] Newton iterations over all passes, [1] first |residual|, [2] first
+ * |reaction|, [3] final |residual|, [4] CG iterations, [5] passes, [6] sum of
+ * updateDamageGeneral's return values.
+ */
+int refd_load_step_damage(int nbd, struct dispBCPara *dbp, int nbf, struct forceBCPara *fbp, int load_ind,
+                          double newton_tol, int maxiter, int max_passes, const char *bondfile, int step,
+                          double *stats)
+{
+    copyDouble2D(xyz_temp, xyz, nparticle, NDIM);
+    copyDouble2D(F_temp, F, nparticle, nneighbors);
+    copyDouble1D(Pex_temp, Pex, dim * nparticle);
+    calcStiffness3DFiniteDifference(6);
+    if (g_bcgroup) {
+        group_disp_bc(nbd, dbp);
+        group_force_bc(nbf, fbp);
+    } else {
+        setDispBC(nbd, dbp);
+        setForceBC(nbf, fbp);
+    }
+    computeBondForceGeneral(4, load_ind);
+    int ni_tot = 0, cgtot = 0, passes = 0, broken_tot = 0;
+    double nr0 = 0, nreac0 = 0, nr = 0;
+    for (;;) {
+        updateRR();
+        nr = cblas_dnrm2(dim * nparticle, residual, 1);
+        double nreac = cblas_dnrm2(countNEqual(dispBC_index, nparticle * dim, 1), reaction_force, 1);
+        double tolm = MAX(nr, nreac);
+        if (passes == 0) {
+            nr0 = nr;
+            nreac0 = nreac;
+        }
+        int ni = 0;
+        while (nr > newton_tol * tolm && ni < maxiter) {
+            switchStateV(0);
+            setDispBC_stiffnessUpdate3D();
+            solverCG();
+            cgtot += lpm_shim_last_cg_iters();
+            computeBondForceGeneral(plmode, load_ind);
+            updateRR();
+            nr = cblas_dnrm2(dim * nparticle, residual, 1);
+            ni++;
+        }
+        ni_tot += ni;
+        passes++;
+        computeStrain();
+        int broken = updateDamageGeneral(bondfile, step, plmode);
+        broken_tot += broken;
+        updateCrack();
+        switchStateV(1);
+        if (broken <= 0 || passes >= max_passes)
+            break;
+        calcStiffness3DFiniteDifference(6);
+    }
+    if (stats) {
+        stats[0] = ni_tot;
+        stats[1] = nr0;
+        stats[2] = nreac0;
+        stats[3] = nr;
+        stats[4] = cgtot;
+        stats[5] = passes;
+        stats[6] = broken_tot;
+    }
+    return ni_tot;
 }
 
 /* ---- flat accessors for the pointer-of-pointer globals ---------------- */

@@ -147,6 +147,33 @@ def load_step(disp_bcs, force_bcs, newton_tol, maxiter=100, load_ind=1):
     return stats
 
 
+def set_damage(L=0.5, threshold=0.9, cA=0.0, crit_bstrain=1e-2, nbreak=20):
+    """damage_L, damage_threshold, damagec_A, critical_bstrain, nbreak."""
+    L_ = lib()
+    L_.refd_set_damage.argtypes = [C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]
+    L_.refd_set_damage(L, threshold, cA, crit_bstrain, nbreak)
+
+
+def load_step_damage(disp_bcs, force_bcs, newton_tol, bondfile, step, maxiter=100, max_passes=1000,
+                     load_ind=1):
+    """One load step of main with the damage stage; broken bonds are appended
+    to `bondfile` by the reference.  Returns the 7 stats of refd_load_step_damage."""
+    nd, nf = len(disp_bcs), len(force_bcs)
+    darr = (DispBC * max(nd, 1))()
+    for k, (t, f, s) in enumerate(disp_bcs):
+        darr[k] = DispBC(t, f.encode(), s)
+    farr = (ForceBC * max(nf, 1))()
+    for k, (t, fx, fy, fz) in enumerate(force_bcs):
+        farr[k] = ForceBC(t, b"x", fx, b"y", fy, b"z", fz)
+    stats = np.zeros(7)
+    L_ = lib()
+    L_.refd_load_step_damage.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_double,
+                                         C.c_int, C.c_int, C.c_char_p, C.c_int, C.c_void_p]
+    L_.refd_load_step_damage(nd, darr, nf, farr, load_ind, newton_tol, maxiter, max_passes,
+                             bondfile.encode(), step, _dp(stats))
+    return stats
+
+
 def set_cg_tol(rtol_sq, atol_sq):
     """Override the reference's hard-coded dcg tolerances (squared norms)."""
     lib().refd_set_cg_tol(float(rtol_sq), float(atol_sq))

@@ -108,6 +108,61 @@ class ForceCase:
         return sc_force_bcs(self.fx, self.fz)
 
 
+class DuctileDamageCase:
+    """J2 with the reference main's ductile nonlocal damage
+    (updateDuctileDamagePwiseNonlocal): SC 8^3 in z tension, yield stress
+    400 MPa except 60 MPa within 0.25 mm of the centre, nonlocal length
+    0.15 mm, damage threshold 1e-3.  Damage accumulates around the weak zone
+    from step 1; step 6 breaks the first bonds (one re-solve pass), step 7
+    cascades over several passes."""
+
+    def __init__(self, n=8, radius=0.1, E=200e3, nu=0.3, H=2000.0, inc=0.0005, steps=7,
+                 L=0.15, threshold=1e-3, newton_tol=1e-8):
+        self.n, self.radius, self.lattice = n, radius, 2
+        self.box = sc_box(n, n, n, radius)
+        self.E, self.nu, self.H = E, nu, H
+        self.schedule = [inc] * steps
+        self.L, self.threshold = L, threshold
+        self.newton_tol = newton_tol
+        self.e_noise, self.seed = 0.0, 1
+
+    def sigmay(self, xyz0):
+        c = xyz0.mean(axis=0)
+        return np.where(np.linalg.norm(xyz0 - c, axis=1) < 0.25, 60.0, 400.0)
+
+    def ce_per_type(self):
+        return np.tile(iso_cubic(self.E, self.nu), (NTYPE, 1))
+
+
+T_PATCH = 6  # a loaded patch of the top face (brittle case)
+
+
+class BrittleCase:
+    """Elastic SC 8^3 with the reference's brittle bond breaking
+    (updateBrittleDamage): only a 3 x 3 corner patch of the top face is
+    pulled along z (type T_PATCH), the rest of the top is free; bonds break
+    at an elastic bond strain of 2e-3, at most 6 per pass.  Breaking starts at
+    step 3 and spreads under the patch, with up to 11 passes per step."""
+
+    def __init__(self, n=8, radius=0.1, E=200e3, nu=0.3, inc=0.0004, steps=12, crit=2e-3, nbreak=6,
+                 newton_tol=1e-8):
+        self.n, self.radius, self.lattice = n, radius, 2
+        self.box = sc_box(n, n, n, radius)
+        self.E, self.nu = E, nu
+        self.schedule = [inc] * steps
+        self.crit, self.nbreak = crit, nbreak
+        self.newton_tol = newton_tol
+
+    def types(self, xyz0, nb):
+        t = sc_types(xyz0, nb, self.radius)
+        patch = (t == T_TOP) & (xyz0[:, 0] < 0.5) & (xyz0[:, 1] < 0.5)
+        t[patch] = T_PATCH
+        return t
+
+    def bcs(self, inc):
+        return [b for b in sc_bcs(0.0) if b[0] != T_TOP] + [(T_PATCH, "z", inc)]
+
+
 def cyclic_schedule(amplitude, steps_per_quarter, cycles):
     """Increments 0->+A->0->-A->0 per cycle, steps_per_quarter equal steps each."""
     inc = amplitude / steps_per_quarter

@@ -2,8 +2,9 @@
 
 Runs the reference's own C sources (built by oracle/build_ref.sh into
 oracle/_ref/libref_lpm.so, MKL replaced by the public-API shim) on the SC
-cyclic case at 10x10x10 (C1), a small FCC crystal-plasticity case and a
-force-controlled SC case (setForceBC), and
+cyclic case at 10x10x10 (C1), a small FCC crystal-plasticity case, a
+force-controlled SC case (setForceBC) and two cases of the main loop's damage
+stage (ductile nonlocal for J2, brittle for elastic), and
 stores inputs and outputs as compressed .npz fixtures.  The reference runs
 single-threaded (its OpenMP loops race, see src/constitutive.c:95 with
 :495-515,625-645), so the fixtures are deterministic.
@@ -199,11 +200,77 @@ def force_case(out, tag="sc_force"):
     np.savez_compressed(os.path.join(out, f"{tag}.npz"), **arrs)
 
 
+def _damage_record(n, nn, bondfile):
+    """Arrays after a damaged load step and the broken pairs the reference
+    logged (TIMESTEP lines dropped)."""
+    pairs = [tuple(int(v) for v in line.split()) for line in open(bondfile).read().splitlines()
+             if line and not line.startswith("TIMESTEP")]
+    return dict(
+        xyz=R.get_d2("xyz", n, 3), F=R.get_d2("F", n, nn), Pin=R.get_d1("Pin", 3 * n),
+        brk=R.get_d2("damage_broken", n, nn), w=R.get_d2("damage_w", n, nn),
+        D=R.get_d3("damage_D", n, nn, 1), dnl=R.get_d2("damage_nonlocal", n, 2)[:, 1],
+        dvis=R.get_d1("damage_visual", n), nb=R.get_i1("nb", n), fix=R.get_i1("fix_index", 3 * n),
+        alpha=R.get_d2("J2_alpha", n, 3)[:, 1], dLp=R.get_d3("dLp", n, nn, 1),
+        pairs=np.array(pairs, dtype=np.int32).reshape(-1, 2))
+
+
+def damage_case(out, which):
+    """The reference's main loop with its damage stage: ductile nonlocal (J2)
+    or brittle (elastic); per step the stats, the broken-bond log and the
+    damage state."""
+    import tempfile
+    if which == "ductile":
+        case = cases.DuctileDamageCase()
+        n = R.setup(case.lattice, case.radius, case.box)
+        xyz0 = R.get_d2("xyz", n, 3)
+        types = cases.sc_types(xyz0, R.get_i1("nb", n), case.radius)
+        R.set_types(types, cases.NTYPE)
+        R.material(case.ce_per_type(), 0, case.sigmay(xyz0), 0.0, case.H)
+        R.init_state()
+        R.set_damage(L=case.L, threshold=case.threshold, cA=0.0)
+        step_bcs = [cases.sc_bcs(v) for v in case.schedule]
+        tag = "damage_ductile"
+        full_steps = {5, 6, 7}
+    else:
+        case = cases.BrittleCase()
+        n = R.setup(case.lattice, case.radius, case.box)
+        xyz0 = R.get_d2("xyz", n, 3)
+        types = case.types(xyz0, R.get_i1("nb", n))
+        R.set_types(types, cases.NTYPE + 1)
+        ce = np.tile(cases.iso_cubic(case.E, case.nu), (cases.NTYPE + 1, 1))
+        R.material(ce, 6, np.full(n, 1e30), 0.0, 0.0)
+        R.init_state()
+        R.set_damage(crit_bstrain=case.crit, nbreak=case.nbreak)
+        step_bcs = [case.bcs(v) for v in case.schedule]
+        tag = "damage_brittle"
+        full_steps = {3, 6, 12}
+    R.set_cg_tol(1e-20, 0.0)
+    nn = R.gint("nneighbors")
+    arrs = dict(types=types, xyz0=xyz0)
+    stats = []
+    t0 = time.time()
+    with tempfile.TemporaryDirectory() as tmp:
+        for s, bcs in enumerate(step_bcs, start=1):
+            bondfile = os.path.join(tmp, f"bonds{s}.txt")
+            with R.quiet():
+                st = R.load_step_damage(bcs, [], case.newton_tol, bondfile, s, maxiter=200, max_passes=50)
+            stats.append(st)
+            rec = _damage_record(n, nn, bondfile)
+            arrs[f"s{s}_pairs"] = rec.pop("pairs")
+            if s in full_steps:  # the whole state only where damage changes course
+                for k, v in rec.items():
+                    arrs[f"s{s}_{k}"] = v
+            print(f"{tag} step {s}: newton {int(st[0])} passes {int(st[5])} candidates {int(st[6])} "
+                  f"res {st[3]:.2e} t={time.time() - t0:.1f}s", flush=True)
+    arrs["stats"] = np.array(stats)
+    np.savez_compressed(os.path.join(out, f"{tag}.npz"), **arrs)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--fcc-steps", type=int, default=12)
-    ap.add_argument("--only", choices=["sc", "fcc", "force"], default=None)
+    ap.add_argument("--only", choices=["sc", "fcc", "force", "ductile", "brittle"], default=None)
     ap.add_argument("--out", default=HERE)
     args = ap.parse_args()
     if not R.available():
@@ -213,11 +280,13 @@ def main():
         fcc_case(args.out, args.fcc_steps)
     elif args.only == "force":
         force_case(args.out)
+    elif args.only in ("ductile", "brittle"):
+        damage_case(args.out, args.only)
     elif args.only == "sc":
         sc_case(args.out, args.steps)
     else:
         import subprocess
-        for which in ("sc", "fcc", "force"):
+        for which in ("sc", "fcc", "force", "ductile", "brittle"):
             subprocess.check_call([sys.executable, __file__, "--only", which, "--steps", str(args.steps),
                                    "--fcc-steps", str(args.fcc_steps), "--out", args.out])
 
