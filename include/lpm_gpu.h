@@ -88,6 +88,8 @@ typedef struct {
     int status;        /* LPM_STATUS_* bits */
     double res0, reac0, res_final;
     double ms_stiffness, ms_solve, ms_force;
+    int damage_passes;   /* damage stage: Newton passes of the step (1 + re-solves after breaking) */
+    int bonds_broken;    /* damage stage: sum of updateDamageGeneral's return values over the passes */
 } lpm_step_stats;
 
 /* ---- context ------------------------------------------------------------ */
@@ -126,7 +128,9 @@ int lpm_init_state(lpm_ctx *ctx);
 /* ---- the hot path -------------------------------------------------------- */
 /* One load step: src/lpmc_project.c:385-471 (stiffness, displacement and force
  * BCs, elastic predictor, Newton loop of PCG solve + bond force update +
- * residual, state commit).  Damage is not modelled. */
+ * residual, state commit).  With the damage stage enabled (lpm_set_damage),
+ * also main's damage updates and re-solves after broken bonds
+ * (src/lpmc_project.c:466-470, :528-546). */
 int lpm_load_step(lpm_ctx *ctx, int nbd, const lpm_disp_bc *dbc, int nbf, const lpm_force_bc *fbc,
                   lpm_step_stats *stats);
 /* calcStiffness3DFiniteDifference (src/stiffness.c:384-516): the elastic
@@ -144,6 +148,37 @@ int lpm_compute_force(lpm_ctx *ctx, int plmode, double norms[2]);
  * evaluation; read it as "strain_tensor" (n x 6, s11 s22 s33 s23 s13 s12
  * order). */
 int lpm_compute_strain(lpm_ctx *ctx);
+/* ---- damage stage ---------------------------------------------------------
+ * The reference's main runs, after each converged load step,
+ * updateDamageGeneral (src/constitutive.c:149-164: ductile pointwise nonlocal
+ * damage for J2, :1757-1862; brittle bond breaking for elastic bonds,
+ * :1437-1527; nothing for crystal plasticity), then updateCrack (:1399-1434:
+ * bond forces scaled by 1 - D, current bond counts) and, when bonds broke,
+ * recomputes the stiffness and re-enters the Newton loop of the same load
+ * step (src/lpmc_project.c:528-546).  Off by default (the parity target of
+ * the solve path); lpm_set_damage after lpm_init_state switches it on with
+ * all bonds intact.  The stress-averaging weights follow the broken bonds as
+ * the reference's opp_flag does; the stiffness drops broken bonds (exact when
+ * a bond and its reverse break together, which the ductile update always
+ * does).  Not combined with batches or the adjoint. */
+typedef struct {
+    int enabled;             /* 0: no damage stage (default) */
+    double length;           /* damage_L: nonlocal length; weights cut at 3 L */
+    double threshold;        /* damage_threshold: particles above it lose all bonds */
+    double triax_coeff;      /* damagec_A (J2_triaxiality is 0 in the reference) */
+    double critical_bstrain; /* brittle: elastic bond strain at which a bond breaks */
+    int nbreak;              /* brittle: at most this many bonds break per pass */
+    int max_passes;          /* cap on Newton passes of one load step */
+} lpm_damage_opts;
+/* enabled = 0 and the values of src/lpmc_project.c:239-244 (L 0.5,
+ * threshold 0.9, A 0, critical strain 1e-2, nbreak 20), max_passes 1000 */
+void lpm_default_damage_opts(lpm_damage_opts *opts);
+int lpm_set_damage(lpm_ctx *ctx, const lpm_damage_opts *opts);
+/* Bonds broken so far, as (particle, partner) pairs in the order the
+ * reference writes them to its bond file.  pairs may be NULL to query the
+ * count; otherwise it holds 2 * capacity ints. */
+int lpm_damage_log(lpm_ctx *ctx, int *pairs, int capacity, int *count);
+
 /* switchStateV (src/constitutive.c:10-85): 0 = converged -> current,
  * 1 = current -> converged. */
 int lpm_switch_state(lpm_ctx *ctx, int flag);
@@ -163,7 +198,10 @@ int lpm_begin_step(lpm_ctx *ctx);
  *   dLp (n x nn, converged), dLp_trial, J2_alpha (n, converged), J2_beta (n x 6),
  *   stress_tensor, strain_tensor (n x 6), neighbors, nsign (n x nn, int32), nb (n, int32),
  *   dispBC_index (3n, int32), type (n, int32), conn (n x 61, int32), nb_conn (n),
- *   cp_gy (n x nslip), cp_A (n), cp_A_single (n x nslip), J2_dlambda (n). */
+ *   cp_gy (n x nslip), cp_A (n), cp_A_single (n x nslip), J2_dlambda (n);
+ *   with the damage stage on: damage_broken, damage_w, damage_D (n x nn,
+ *   converged), damage_nonlocal (n, converged), damage_visual (n),
+ *   nb_current (n, int32: intact bonds; nb stays nb_initial). */
 int lpm_get(lpm_ctx *ctx, const char *name, void *dst, size_t bytes);
 int lpm_set(lpm_ctx *ctx, const char *name, const void *src, size_t bytes);
 int lpm_get_sizes(const lpm_ctx *ctx, int *n, int *nn, int *nslip, long long *nnz_blocks);

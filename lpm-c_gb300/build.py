@@ -35,6 +35,7 @@ CU_UNITS = [
     ("k_strain.cu", ["-fmad=false"]),
     ("adjoint.cu", []),
     ("k_noalloc.cu", []),
+    ("k_damage.cu", ["-fmad=false"]),
 ]
 CPP_UNITS = [("setup.cpp", ["-ffp-contract=off", "-fopenmp"]), ("output.cpp", ["-ffp-contract=off"])]
 LEGACY_UNITS = [("legacy.cpp", [])]

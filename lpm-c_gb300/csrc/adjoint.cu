@@ -310,6 +310,9 @@ int lpm_adjoint_forward(lpm_ctx *ctx, const double *E, const double *nu, const d
     Ctx &c = ctx->c;
     if (c.n <= 0 || c.nspec > 0)
         return fail(LPM_ERR_ARG, "lpm_adjoint_forward: set up one specimen (and its types) first");
+    if (c.dmg.on)
+        return fail(LPM_ERR_ARG, "lpm_adjoint_forward: the adjoint does not model the damage stage "
+                                 "(switch it off with lpm_set_damage)");
     auto t0 = std::chrono::steady_clock::now();
     const int n = c.n;
     std::vector<double> c11(n), c12(n), c44(n);

@@ -33,6 +33,8 @@ struct CpArgs {
     double tau0, taus, h0, p, q, eta, maxloop, dtime;
     int *status;
     int *pl_flag;
+    // damage_broken / damage_w [NN][n]; null while the damage stage is off
+    const double *brk, *dw;
 };
 
 __device__ __forceinline__ double proj6(const double *sc, double cx, double cy, double cz)
@@ -41,6 +43,9 @@ __device__ __forceinline__ double proj6(const double *sc, double cx, double cy, 
            cx * cy * sc[5];
 }
 
+// DMG: the damage stage is on (a.brk, a.dw set); the undamaged instantiation
+// carries no trace of it.
+template <bool DMG>
 __global__ void __launch_bounds__(CTPB) k_cp(CpArgs a)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -61,7 +66,8 @@ __global__ void __launch_bounds__(CTPB) k_cp(CpArgs a)
             e[j] = dis - a.L0[b];
             double v = e[j];
             v -= a.dLp_c[b];
-            v *= 1.0;
+            if (DMG)
+                v *= a.brk[b];  // damage_broken
             dL[j] = v;
             xdL[j] = v;
             S[a.shell[b]] += v;
@@ -90,7 +96,8 @@ __global__ void __launch_bounds__(CTPB) k_cp(CpArgs a)
             const size_t b = (size_t)j * n + i;
             const int s = a.shell[b];
             double fij = 2.0 * a.Kn[b] * dls[j] + Ts[s] + a.Tv[b] * Ss[s];
-            fij *= 1.0;
+            if (DMG)
+                fij *= a.dw[b];  // damage_w
             const double w = a.oppv[b] * a.L0[b] * fij;
             const double cx = a.csx[b], cy = a.csy[b], cz = a.csz[b];
             st[0] += w * cx * cx;
@@ -140,7 +147,8 @@ __global__ void __launch_bounds__(CTPB) k_cp(CpArgs a)
                     const double cx = a.csx[b], cy = a.csy[b], cz = a.csz[b];
                     double v = a.L0[b] * (dpl[0] * cx * cx + dpl[1] * cy * cy + dpl[2] * cz * cz +
                                           dpl[3] * cy * cz + dpl[4] * cx * cz + dpl[5] * cx * cy);
-                    v *= 1.0;
+                    if (DMG)
+                        v *= a.brk[b];  // damage_broken
                     ddlp[j] = v;
                     xdL[j] = dL[j] - v;
                     xS[a.shell[b]] += xdL[j];
@@ -295,12 +303,13 @@ __global__ void __launch_bounds__(CTPB) k_cp(CpArgs a)
     S[0] = S[1] = T[0] = T[1] = 0.0;
     for (int j = 0; j < LPM_NN; j++) {
         const size_t b = (size_t)j * n + i;
-        const double lp = 1.0 * (a.dLp_c[b] + (j < nbi ? ddlp[j] : 0.0));
+        const double lp = (DMG ? a.brk[b] : 1.0) * (a.dLp_c[b] + (j < nbi ? ddlp[j] : 0.0));
         a.dLp_t[b] = lp;
         if (j < nbi) {
             double v = e[j];
             v -= lp;
-            v *= 1.0;
+            if (DMG)
+                v *= a.brk[b];  // damage_broken
             a.dL[b] = v;
             S[a.shell[b]] += v;
             T[a.shell[b]] += a.Tv[b] * v;
@@ -386,7 +395,12 @@ void launch_cp(Ctx &c)
     a.maxloop = c.cp[6];
     a.dtime = c.cp[7];
     a.status = c.status;
-    k_cp<<<(c.n + CTPB - 1) / CTPB, CTPB, 0, c.stream>>>(a);
+    a.brk = c.dmg.brk;
+    a.dw = c.dmg.dw;
+    if (a.brk)
+        k_cp<true><<<(c.n + CTPB - 1) / CTPB, CTPB, 0, c.stream>>>(a);
+    else
+        k_cp<false><<<(c.n + CTPB - 1) / CTPB, CTPB, 0, c.stream>>>(a);
 }
 
 void launch_cab(Ctx &c)

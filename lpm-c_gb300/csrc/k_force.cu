@@ -52,6 +52,8 @@ struct ForceArgs {
     double xi;
     int *status;
     int *pl_flag;
+    // damage_broken / damage_w [NN][n]; null while the damage stage is off
+    const double *brk, *dw;
 };
 
 static ForceArgs make_args(Ctx &c)
@@ -100,6 +102,8 @@ static ForceArgs make_args(Ctx &c)
     a.xi = c.xi;
     a.status = c.status;
     a.pl_flag = c.pl_flag;
+    a.brk = c.dmg.brk;
+    a.dw = c.dmg.dw;
     return a;
 }
 
@@ -225,7 +229,8 @@ __global__ void k_stretch(ForceArgs a, const double *dLp, int store_cs)
         const double dis = bond_length(xi, a.xyz[p], dx, dy, dz);
         double v = dis - a.L0[b];
         v -= dLp[b];
-        v *= 1.0;
+        if (a.brk)
+            v *= a.brk[b];  // damage_broken
         a.dL[b] = v;
         if (a.shell[b] == 0) {
             S0 += v;
@@ -260,7 +265,8 @@ __global__ void k_elastic(ForceArgs a)
             const bool s0 = a.shell[b] == 0;
             double f = 2.0 * a.Kn[b] * a.dL[b] + 0.5 * ((s0 ? Ti.x : Ti.y) + (s0 ? Tp.x : Tp.y)) +
                        0.5 * a.Tv[b] * ((s0 ? Si.x : Si.y) + (s0 ? Sp.x : Sp.y));
-            f *= 1.0;
+            if (a.brk)
+                f *= a.brk[b];  // damage_broken
             a.F[b] = f;
             const double cx = a.csx[b], cy = a.csy[b], cz = a.csz[b];
             p0 += cx * f;
@@ -289,7 +295,7 @@ __global__ void k_pred1(ForceArgs a)
         double dx, dy, dz;
         const double d0 = bond_length(x0, a.xyz_temp[p], dx, dy, dz);
         const double d1 = bond_length(x1, a.xyz[p], dx, dy, dz);
-        const double v = 1.0 * (d1 - d0);
+        const double v = (a.brk ? a.brk[b] : 1.0) * (d1 - d0);  // damage_broken
         a.ddL[b] = v;
         if (a.shell[b] == 0) {
             S0 += v;
@@ -320,7 +326,8 @@ __global__ void k_pred2(ForceArgs a)
             const bool s0 = a.shell[b] == 0;
             double f = a.F_prev[b] + 2.0 * a.Kn[b] * a.ddL[b] + 0.5 * ((s0 ? Ti.x : Ti.y) + (s0 ? Tp.x : Tp.y)) +
                        0.5 * a.Tv[b] * ((s0 ? Si.x : Si.y) + (s0 ? Sp.x : Sp.y));
-            f *= 1.0;
+            if (a.brk)
+                f *= a.brk[b];  // damage_broken
             a.F[b] = f;
             const double cx = a.csx[b], cy = a.csy[b], cz = a.csz[b];
             p0 += cx * f;
@@ -354,7 +361,8 @@ __global__ void __launch_bounds__(TPB) k_j2(ForceArgs a)
             e[j] = dis - a.L0[b];
             double v = e[j];
             v -= a.dLp_c[b];
-            v *= 1.0;
+            if (a.brk)
+                v *= a.brk[b];  // damage_broken
             if (a.shell[b] == 0) {
                 S0 += v;
                 T0 += a.Tv[b] * v;
@@ -375,10 +383,12 @@ __global__ void __launch_bounds__(TPB) k_j2(ForceArgs a)
             const size_t b = (size_t)j * n + i;
             double v = e[j];
             v -= a.dLp_c[b];
-            v *= 1.0;
+            if (a.brk)
+                v *= a.brk[b];  // damage_broken
             const bool s0 = a.shell[b] == 0;
             double fij = 2.0 * a.Kn[b] * v + (s0 ? T0 : T1) + a.Tv[b] * (s0 ? S0 : S1);
-            fij *= 1.0;
+            if (a.dw)
+                fij *= a.dw[b];  // damage_w
             stress_add(st, a.oppv[b] * a.L0[b] * fij, a.csx[b], a.csy[b], a.csz[b]);
         }
     }
@@ -425,14 +435,16 @@ __global__ void __launch_bounds__(TPB) k_j2(ForceArgs a)
             const double cx = a.csx[b], cy = a.csy[b], cz = a.csz[b];
             add = a.L0[b] * (dpl[0] * cx * cx + dpl[1] * cy * cy + dpl[2] * cz * cz + 2 * dpl[3] * cy * cz +
                              2 * dpl[4] * cx * cz + 2 * dpl[5] * cx * cy);
-            add *= 1.0;
+            if (a.brk)
+                add *= a.brk[b];  // damage_broken
         }
-        const double lp = 1.0 * (a.dLp_c[b] + add);
+        const double lp = (a.brk ? a.brk[b] : 1.0) * (a.dLp_c[b] + add);
         a.dLp_t[b] = lp;
         if (j < nbi) {
             double v = e[j];
             v -= lp;
-            v *= 1.0;
+            if (a.brk)
+                v *= a.brk[b];  // damage_broken
             a.dL[b] = v;
             if (a.shell[b] == 0) {
                 S0 += v;
@@ -471,7 +483,8 @@ __global__ void k_final(ForceArgs a)
             const double dla = 0.5 * (a.dL[b] + (rv >= 0 ? a.dL[(size_t)rv * n + p] : a.dL[b]));
             double f = 2.0 * a.Kn[b] * dla + 0.5 * ((s0 ? Ti.x : Ti.y) + (s0 ? Tp.x : Tp.y)) +
                        0.5 * a.Tv[b] * ((s0 ? Si.x : Si.y) + (s0 ? Sp.x : Sp.y));
-            f *= 1.0;
+            if (a.dw)
+                f *= a.dw[b];  // damage_w
             a.F[b] = f;
             const double cx = a.csx[b], cy = a.csy[b], cz = a.csz[b];
             p0 += cx * f;
@@ -480,6 +493,37 @@ __global__ void k_final(ForceArgs a)
             stress_add(st, a.oppv[b] * a.L0[b] * f, cx, cy, cz);
         }
         stress_store(a, i, st);
+    }
+    residual_epilogue(a, i, valid, p0, p1, p2);
+}
+
+// updateCrack (src/constitutive.c:1399-1434): intact-bond count, damage
+// picture, bond forces scaled by w and the internal force re-summed, then
+// updateRR and its norms.  Particles left without bonds are not fixed here:
+// their internal force is zero, so with no external force their residual is
+// zero and the solve leaves them in place, as fix_index does.
+__global__ void k_crack(ForceArgs a, int8_t *nbc, double *dvis)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < a.n;
+    double p0 = 0.0, p1 = 0.0, p2 = 0.0;
+    if (valid) {
+        const int n = a.n, nbi = a.nbv[i];
+        int cnt = nbi;
+        double vis = 0.0;
+        for (int j = 0; j < nbi; j++) {
+            const size_t b = (size_t)j * n + i;
+            if (a.brk[b] <= 1e-6)
+                cnt -= 1;
+            vis += a.brk[b];
+            const double f = a.F[b] * a.dw[b];
+            a.F[b] = f;
+            p0 += a.csx[b] * f;
+            p1 += a.csy[b] * f;
+            p2 += a.csz[b] * f;
+        }
+        nbc[i] = (int8_t)cnt;
+        dvis[i] = 1 - vis / nbi;
     }
     residual_epilogue(a, i, valid, p0, p1, p2);
 }
@@ -558,6 +602,12 @@ void launch_stretch(Ctx &c, const double *dLp, bool store_cs)
 {
     ForceArgs a = make_args(c);
     k_stretch<<<grid_for(c.n), TPB, 0, c.stream>>>(a, dLp, store_cs ? 1 : 0);
+}
+
+void launch_crack(Ctx &c)
+{
+    ForceArgs a = make_args(c);
+    k_crack<<<grid_for(c.n), TPB, 0, c.stream>>>(a, c.dmg.nbc, c.dmg.dvis);
 }
 
 void launch_elastic_force(Ctx &c)

@@ -17,6 +17,12 @@
 // U_p^s = sum of shell-s unit vectors, W_p^s = Tv-weighted sum.  Using
 // Fbar_ij = (F_ij + F_ji)/2 in the off-diagonal geometric term is exactly the
 // reference's symmetrisation; the other terms are already symmetric.
+//
+// With the damage stage on, a broken bond has zero stretch and force
+// (damage_broken multiplies both, src/constitutive.c:254,271), so it drops out
+// of the shell sums S, T, U, W, of its own terms and of the two-hop terms
+// through it.  A pair contributes only when the bond and its reverse are both
+// intact; that is the reference's matrix whenever the two break together.
 #include "lpm_internal.h"
 
 namespace lpm {
@@ -28,8 +34,8 @@ constexpr int STPB = 128;
 // the unit-vector sums U and W of each shell.
 __global__ void k_tgeom(int n, const dvec4 *xyz, const int *nbr, const int8_t *shell,
                         const int8_t *nbv, const double *L0, const double *Tv, const double *dLp,
-                        double *dL, double *csx, double *csy, double *csz, double2 *S, double2 *T,
-                        double *U, double *W)
+                        const double *brk, double *dL, double *csx, double *csy, double *csz, double2 *S,
+                        double2 *T, double *U, double *W)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
@@ -44,7 +50,8 @@ __global__ void k_tgeom(int n, const dvec4 *xyz, const int *nbr, const int8_t *s
         const double dis = sqrt(dx * dx + dy * dy + dz * dz);
         double v = dis - L0[b];
         v -= dLp[b];
-        v *= 1.0;
+        if (brk)
+            v *= brk[b];  // damage_broken
         dL[b] = v;
         const int sh = shell[b];
         s[sh] += v;
@@ -53,6 +60,8 @@ __global__ void k_tgeom(int n, const dvec4 *xyz, const int *nbr, const int8_t *s
         csx[b] = cx;
         csy[b] = cy;
         csz[b] = cz;
+        if (brk && brk[b] == 0.0)
+            continue;
         u[3 * sh] += cx;
         u[3 * sh + 1] += cy;
         u[3 * sh + 2] += cz;
@@ -77,6 +86,7 @@ struct AsmArgs {
     const double2 *S, *T;
     const long long *rowoff;
     const int *npad, *cols;
+    const double *brk;  // damage_broken [NN][n], null while the damage stage is off
 };
 
 __device__ __forceinline__ int find_slot(const int *c, int cnt, int key)
@@ -133,6 +143,8 @@ __global__ void __launch_bounds__(STPB) k_assemble(AsmArgs a, V *val)
         const double Tsum = (s == 0 ? Ti.x + Tp.x : Ti.y + Tp.y);
         const double Ssum = (s == 0 ? Si.x + Sp.x : Si.y + Sp.y);
         const int rv = a.rev[b];
+        if (a.brk && a.brk[b] * (rv >= 0 ? a.brk[(size_t)rv * n + p] : 1.0) == 0.0)
+            continue;  // broken pair
         const double dlij = a.dL[b], dlji = rv >= 0 ? a.dL[(size_t)rv * n + p] : dlij;
         const double fel = 2.0 * kn * dlij + 0.5 * Tsum + 0.5 * tv * Ssum;
         const double fbar = kn * (dlij + dlji) + 0.5 * Tsum + 0.5 * tv * Ssum;
@@ -155,7 +167,7 @@ __global__ void __launch_bounds__(STPB) k_assemble(AsmArgs a, V *val)
         const int nbp = a.nbv[p];
         for (int m = 0; m < nbp; m++) {
             const size_t bm = (size_t)m * n + p;
-            if (a.shell[bm] != s)
+            if (a.shell[bm] != s || (a.brk && a.brk[bm] == 0.0))
                 continue;
             const int q = a.nbr[bm];
             const double cq[3] = {a.csx[bm], a.csy[bm], a.csz[bm]};
@@ -221,8 +233,8 @@ __global__ void k_jacobi(int n, const long long *rowoff, const int *npad, const 
 void launch_tangent_geometry(Ctx &c)
 {
     k_tgeom<<<(c.n + STPB - 1) / STPB, STPB, 0, c.stream>>>(c.n, c.xyz, c.nbr, c.shell, c.nbv, c.L0, c.Tv,
-                                                            c.dLp[0], c.dL, c.csx, c.csy, c.csz, c.S,
-                                                            c.T, c.U, c.W);
+                                                            c.dLp[0], c.dmg.brk, c.dL, c.csx, c.csy, c.csz,
+                                                            c.S, c.T, c.U, c.W);
 }
 
 void launch_assemble(Ctx &c, bool fp32)
@@ -248,6 +260,7 @@ void launch_assemble(Ctx &c, bool fp32)
     a.rowoff = c.rowoff;
     a.npad = c.npad;
     a.cols = c.cols;
+    a.brk = c.dmg.brk;
     const int g = (c.n + STPB - 1) / STPB;
     if (fp32)
         k_assemble<float><<<g, STPB, 0, c.stream>>>(a, c.Kf);

@@ -78,6 +78,28 @@ static void free_anderson(Ctx &c)
     c.acc = Ctx::Anderson();
 }
 
+static void free_damage(Ctx &c)
+{
+    Ctx::Damage &d = c.dmg;
+    dfree(d.brk);
+    dfree(d.dw);
+    dfree(d.D[0]);
+    dfree(d.D[1]);
+    dfree(d.dnl[0]);
+    dfree(d.dnl[1]);
+    dfree(d.dvis);
+    dfree(d.nbc);
+    dfree(d.opp);
+    dfree(d.cstart);
+    dfree(d.corder);
+    dfree(d.list);
+    dfree(d.lval);
+    dfree(d.count);
+    if (d.count_h)
+        cudaFreeHost(d.count_h);
+    c.dmg = Ctx::Damage();
+}
+
 Ctx::~Ctx()
 {
     cudaSetDevice(device);
@@ -85,6 +107,7 @@ Ctx::~Ctx()
     free_batch(*this);
     free_adjoint(*this);
     free_anderson(*this);
+    free_damage(*this);
     void **all[] = {(void **)&xyz, (void **)&xyz0, (void **)&xyz_temp, (void **)&Pin, (void **)&Pex,
                     (void **)&res, (void **)&du, (void **)&mask, (void **)&type, (void **)&G, (void **)&sy,
                     (void **)&Hh, (void **)&stress, (void **)&strain, (void **)&dlambda, (void **)&nbr, (void **)&shell,
@@ -166,7 +189,8 @@ static void copy_state(Ctx &c, int to, int from)
     }
 }
 
-// switchStateV (src/constitutive.c:10-85)
+// switchStateV (src/constitutive.c:10-85); damage_D and damage_nonlocal have
+// slots 0 and 1 only and move with flags 0 and 1
 void switch_state(Ctx &c, int flag)
 {
     if (flag == 0)
@@ -175,6 +199,13 @@ void switch_state(Ctx &c, int flag)
         copy_state(c, 1, 0);
     else
         copy_state(c, 0, 2);
+    if (c.dmg.on && flag != 2) {
+        const int to = flag == 0 ? 0 : 1, from = 1 - to;
+        cudaMemcpyAsync(c.dmg.D[to], c.dmg.D[from], (size_t)c.n * LPM_NN * sizeof(double), cudaMemcpyDeviceToDevice,
+                        c.stream);
+        cudaMemcpyAsync(c.dmg.dnl[to], c.dmg.dnl[from], (size_t)c.n * sizeof(double), cudaMemcpyDeviceToDevice,
+                        c.stream);
+    }
 }
 
 // transposes between host row-major [n][k] and device [k][n]
@@ -321,6 +352,7 @@ static int setup_common(Ctx &c, bool built = false)
     free_writer(c);
     free_adjoint(c);
     free_anderson(c);
+    free_damage(c);
     drop_graphs(c);
     dfree(c.Kf);
     dfree(c.Kd);
@@ -564,6 +596,13 @@ int lpm_init_state(lpm_ctx *ctx)
         return fail(LPM_ERR_ARG, "set up the specimen first");
     Ctx &c = ctx->c;
     const size_t n = c.n, nb = n * LPM_NN;
+    if (c.dmg.on) {
+        // back to intact bonds: the setup's stress weights, no damage stage
+        hvec<double> t(nb);
+        to_slot_major(c.hs.oppv.data(), t.data(), c.n, LPM_NN);
+        LPM_CUDA(cudaMemcpy(c.oppv, t.data(), nb * sizeof(double), cudaMemcpyHostToDevice));
+        free_damage(c);
+    }
     for (int s = 0; s < 3; s++) {
         LPM_CUDA(cudaMemsetAsync(c.dLp[s], 0, nb * sizeof(double), c.stream));
         LPM_CUDA(cudaMemsetAsync(c.alpha[s], 0, n * sizeof(double), c.stream));
@@ -915,6 +954,109 @@ static int apply_bc(Ctx &c, int nbd, const lpm_disp_bc *dbc, int nbf, const lpm_
     return LPM_OK;
 }
 
+// The damage stage after a converged Newton pass (src/lpmc_project.c:466-469):
+// updateDamageGeneral for the model (src/constitutive.c:149-164), then
+// updateCrack (:1399-1434) and the stress weights of the intact bonds.
+// `broken` is updateDamageGeneral's return value.  Broken bonds are logged as
+// (particle, partner) in the order the reference writes its bond file.
+static int damage_pass(Ctx &c, int &broken)
+{
+    Ctx::Damage &d = c.dmg;
+    const int n = c.n;
+    broken = 0;
+    auto read_list = [&](int &k) -> int {
+        LPM_CUDA(cudaMemcpyAsync(d.count_h, d.count, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+        int rc = sync(c);
+        if (rc)
+            return rc;
+        k = *d.count_h;
+        return LPM_OK;
+    };
+    if (c.plmode == LPM_PL_J2) {
+        // updateDuctileDamagePwiseNonlocal (src/constitutive.c:1757-1862)
+        launch_dmg_nonlocal(c);
+        launch_dmg_ductile_break(c);
+        launch_dmg_ductile_w(c);
+        int k = 0, rc = read_list(k);
+        if (rc)
+            return rc;
+        if (k > 0) {
+            std::vector<int> b(k);
+            LPM_CUDA(cudaMemcpy(b.data(), d.list, sizeof(int) * k, cudaMemcpyDeviceToHost));
+            // scan order of the reference: particle, then bond slot
+            std::sort(b.begin(), b.end(), [n](int x, int y) {
+                const int ix = x % n, iy = y % n;
+                return ix != iy ? ix < iy : x / n < y / n;
+            });
+            for (int v : b) {
+                const int i = v % n, j = v / n;
+                d.log.push_back(i);
+                d.log.push_back(c.hs.nbr[(size_t)i * LPM_NN + j]);
+            }
+        }
+        broken = k;
+    } else if (c.plmode == LPM_PL_ELASTIC) {
+        // updateBrittleDamage (src/constitutive.c:1437-1527)
+        launch_dmg_brittle_cand(c);
+        int k = 0, rc = read_list(k);
+        if (rc)
+            return rc;
+        if (k > 0) {
+            std::vector<int> b(k), idx(k);
+            std::vector<double> v(k);
+            LPM_CUDA(cudaMemcpy(b.data(), d.list, sizeof(int) * k, cudaMemcpyDeviceToHost));
+            LPM_CUDA(cudaMemcpy(v.data(), d.lval, sizeof(double) * k, cudaMemcpyDeviceToHost));
+            for (int q = 0; q < k; q++)
+                idx[q] = q;
+            std::sort(idx.begin(), idx.end(), [&](int x, int y) {
+                const int ix = b[x] % n, iy = b[y] % n;
+                return ix != iy ? ix < iy : b[x] / n < b[y] / n;
+            });
+            std::vector<int> bi(k);
+            std::vector<double> bs(k);
+            for (int q = 0; q < k; q++) {
+                bi[q] = b[idx[q]];
+                bs[q] = v[idx[q]];
+            }
+            int first = 0;
+            const int nbreak = d.opts.nbreak;
+            if (k > nbreak) {
+                // the reference's shell sort, ascending strain (gaps k/2, k/4, ..., 1);
+                // the last nbreak entries (largest strains) break
+                for (int r = k / 2; r >= 1; r = r / 2)
+                    for (int i = r; i < k; ++i) {
+                        const int tb = bi[i];
+                        const double ts = bs[i];
+                        int j = i - r;
+                        while (j >= 0 && bs[j] > ts) {
+                            bs[j + r] = bs[j];
+                            bi[j + r] = bi[j];
+                            j = j - r;
+                        }
+                        bs[j + r] = ts;
+                        bi[j + r] = tb;
+                    }
+                first = k - nbreak;
+            }
+            std::vector<int> chosen(bi.begin() + first, bi.end());
+            if (!chosen.empty()) {
+                LPM_CUDA(cudaMemcpyAsync(d.list, chosen.data(), sizeof(int) * chosen.size(), cudaMemcpyHostToDevice,
+                                         c.stream));
+                launch_dmg_break_list(c, d.list, (int)chosen.size());
+            }
+            for (int v2 : chosen) {
+                const int i = v2 % n, j = v2 / n;
+                d.log.push_back(i);
+                d.log.push_back(c.hs.nbr[(size_t)i * LPM_NN + j]);
+            }
+        }
+        broken = k;
+    }
+    launch_crack(c);
+    launch_dmg_oppv(c);
+    return sync(c);
+}
+
 struct Timer {
     cudaEvent_t a, b;
     cudaStream_t s;
@@ -942,6 +1084,161 @@ struct Timer {
 }  // namespace lpm
 
 extern "C" {
+
+void lpm_default_damage_opts(lpm_damage_opts *o)
+{
+    o->enabled = 0;
+    o->length = 0.5;             // damage_L, src/lpmc_project.c:244
+    o->threshold = 0.9;          // damage_threshold, :243
+    o->triax_coeff = 0.0;        // damagec_A, :242
+    o->critical_bstrain = 1e-2;  // critical_bstrain, :240
+    o->nbreak = 20;              // nbreak, :239
+    o->max_passes = 1000;
+}
+
+int lpm_set_damage(lpm_ctx *ctx, const lpm_damage_opts *o)
+{
+    if (!ctx || !o)
+        return fail(LPM_ERR_ARG, "null argument");
+    Ctx &c = ctx->c;
+    if (!c.ready)
+        return fail(LPM_ERR_ARG, "call lpm_init_state first");
+    if (c.nspec > 0)
+        return fail(LPM_ERR_ARG, "the damage stage is not available for batches");
+    if (c.adj)
+        return fail(LPM_ERR_ARG, "the damage stage is not available with the adjoint");
+    if (!o->enabled) {
+        if (c.dmg.on) {
+            hvec<double> t((size_t)c.n * LPM_NN);
+            to_slot_major(c.hs.oppv.data(), t.data(), c.n, LPM_NN);
+            LPM_CUDA(cudaMemcpy(c.oppv, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice));
+        }
+        free_damage(c);
+        return LPM_OK;
+    }
+    if (!(o->length > 0.0) || !std::isfinite(o->threshold) || !std::isfinite(o->triax_coeff) ||
+        !(o->critical_bstrain > 0.0) || o->nbreak < 0 || o->max_passes < 1)
+        return fail(LPM_ERR_ARG, "invalid damage options");
+    if ((long long)c.n * LPM_NN > 2147483647LL)
+        return fail(LPM_ERR_ARG, "too many bonds for the damage stage");
+    free_damage(c);
+    Ctx::Damage &d = c.dmg;
+    const int n = c.n;
+    const size_t nb = (size_t)n * LPM_NN;
+    const HostSetup &h = c.hs;
+    int rc = 0;
+    if ((rc = dalloc(d.brk, nb)) || (rc = dalloc(d.dw, nb)) || (rc = dalloc(d.D[0], nb)) || (rc = dalloc(d.D[1], nb)) ||
+        (rc = dalloc(d.dnl[0], n)) || (rc = dalloc(d.dnl[1], n)) || (rc = dalloc(d.dvis, n)) ||
+        (rc = dalloc(d.nbc, n)) || (rc = dalloc(d.opp, nb)) || (rc = dalloc(d.list, nb)) ||
+        (rc = dalloc(d.lval, nb)) || (rc = dalloc(d.count, 1))) {
+        free_damage(c);
+        return rc;
+    }
+    LPM_CUDA(cudaMallocHost((void **)&d.count_h, sizeof(int)));
+    // initMatrices (src/initialization.c:1176-1181): intact bonds, no damage
+    {
+        hvec<double> ones(nb);
+#pragma omp parallel for schedule(static)
+        for (long long k = 0; k < (long long)nb; k++)
+            ones[k] = 1.0;
+        LPM_CUDA(cudaMemcpy(d.brk, ones.data(), nb * sizeof(double), cudaMemcpyHostToDevice));
+        LPM_CUDA(cudaMemcpy(d.dw, ones.data(), nb * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    LPM_CUDA(cudaMemset(d.D[0], 0, nb * sizeof(double)));
+    LPM_CUDA(cudaMemset(d.D[1], 0, nb * sizeof(double)));
+    LPM_CUDA(cudaMemset(d.dnl[0], 0, n * sizeof(double)));
+    LPM_CUDA(cudaMemset(d.dnl[1], 0, n * sizeof(double)));
+    LPM_CUDA(cudaMemset(d.dvis, 0, n * sizeof(double)));
+    LPM_CUDA(cudaMemcpy(d.nbc, c.nbv, n, cudaMemcpyDeviceToDevice));
+    // slot of each bond's opposite bond (the first match, as the reference's
+    // opp_flag search over the initial unit vectors)
+    {
+        hvec<int8_t> op(nb);
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < n; i++) {
+            for (int j = 0; j < LPM_NN; j++) {
+                int m0 = -1;
+                if (j < h.nb[i]) {
+                    const double *cj = &h.cs0[3 * ((size_t)i * LPM_NN + j)];
+                    for (int m = 0; m < h.nb[i]; m++) {
+                        const double *cm = &h.cs0[3 * ((size_t)i * LPM_NN + m)];
+                        if (std::fabs(cm[0] + cj[0]) < 1e-6 && std::fabs(cm[1] + cj[1]) < 1e-6 &&
+                            std::fabs(cm[2] + cj[2]) < 1e-6) {
+                            m0 = m;
+                            break;
+                        }
+                    }
+                }
+                op[(size_t)j * n + i] = (int8_t)m0;
+            }
+        }
+        LPM_CUDA(cudaMemcpy(d.opp, op.data(), nb, cudaMemcpyHostToDevice));
+    }
+    // cell list of the initial positions for the nonlocal sum (cells >= 3 L,
+    // coarsened when a fine grid would hold far more cells than particles)
+    {
+        double lo[3], hi[3];
+        for (int k = 0; k < 3; k++)
+            lo[k] = hi[k] = h.xyz[k];
+        for (int i = 0; i < n; i++)
+            for (int k = 0; k < 3; k++) {
+                lo[k] = std::min(lo[k], h.xyz[3 * (size_t)i + k]);
+                hi[k] = std::max(hi[k], h.xyz[3 * (size_t)i + k]);
+            }
+        double cs = 3.0 * o->length * 1.0001;
+        int g[3];
+        for (;;) {
+            for (int k = 0; k < 3; k++)
+                g[k] = (int)((hi[k] - lo[k]) / cs) + 1;
+            if ((double)g[0] * g[1] * g[2] <= 8.0 * n + 4096.0)
+                break;
+            cs *= 1.5;
+        }
+        const size_t ncell = (size_t)g[0] * g[1] * g[2];
+        std::vector<int> cell(n), start(ncell + 1, 0), order(n);
+        for (int i = 0; i < n; i++) {
+            int cc[3];
+            for (int k = 0; k < 3; k++)
+                cc[k] = std::min(g[k] - 1, (int)((h.xyz[3 * (size_t)i + k] - lo[k]) / cs));
+            cell[i] = (int)(((size_t)cc[2] * g[1] + cc[1]) * g[0] + cc[0]);
+            start[cell[i] + 1]++;
+        }
+        for (size_t q = 0; q < ncell; q++)
+            start[q + 1] += start[q];
+        std::vector<int> fill(start.begin(), start.end() - 1);
+        for (int i = 0; i < n; i++)
+            order[fill[cell[i]]++] = i;
+        if ((rc = dalloc(d.cstart, ncell + 1)) || (rc = dalloc(d.corder, n))) {
+            free_damage(c);
+            return rc;
+        }
+        LPM_CUDA(cudaMemcpy(d.cstart, start.data(), (ncell + 1) * sizeof(int), cudaMemcpyHostToDevice));
+        LPM_CUDA(cudaMemcpy(d.corder, order.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+        for (int k = 0; k < 3; k++) {
+            d.g[k] = g[k];
+            d.lo[k] = lo[k];
+        }
+        d.cs = cs;
+    }
+    d.opts = *o;
+    d.on = 1;
+    return LPM_OK;
+}
+
+int lpm_damage_log(lpm_ctx *ctx, int *pairs, int capacity, int *count)
+{
+    if (!ctx || !count)
+        return fail(LPM_ERR_ARG, "null argument");
+    Ctx &c = ctx->c;
+    const int k = (int)(c.dmg.log.size() / 2);
+    *count = k;
+    if (pairs) {
+        if (capacity < k)
+            return fail(LPM_ERR_ARG, "damage log: buffer too small");
+        std::memcpy(pairs, c.dmg.log.data(), sizeof(int) * 2 * (size_t)k);
+    }
+    return LPM_OK;
+}
 
 int lpm_begin_step(lpm_ctx *ctx)
 {
@@ -1191,7 +1488,7 @@ int lpm_load_step(lpm_ctx *ctx, int nbd, const lpm_disp_bc *dbc, int nbf, const 
             return rc;
         st.ms_force += t.stop();
     }
-    const double tolm = std::max(res, reac);
+    double tolm = std::max(res, reac);
     st.res0 = res;
     st.reac0 = reac;
     c.trace_step++;
@@ -1206,45 +1503,84 @@ int lpm_load_step(lpm_ctx *ctx, int nbd, const lpm_disp_bc *dbc, int nbf, const 
         ar.m = c.opts.newton_accel;
         ar.G.assign((size_t)ar.m * ar.m, 0.0);
     }
-    double res_best = res;
-    while (res > c.opts.newton_tol * tolm && ni < c.opts.newton_maxiter) {  // :424
-        if (!std::isfinite(res)) {
-            st.status |= LPM_STATUS_NAN;
+    // One Newton pass without the damage stage; with it, a pass per
+    // label_broken_bond re-entry (src/lpmc_project.c:405, :528-546).
+    int passes = 0;
+    for (;;) {
+        double res_best = res;
+        int nip = 0;
+        ar.hist = 0;  // a pass starts without acceleration history
+        ar.head = 0;
+        ar.have_prev = false;
+        while (res > c.opts.newton_tol * tolm && nip < c.opts.newton_maxiter) {  // :424
+            if (!std::isfinite(res)) {
+                st.status |= LPM_STATUS_NAN;
+                break;
+            }
+            switch_state(c, 0);  // :428
+            {
+                Timer t(c.stream);
+                if ((rc = solve_device(c, c.res, &st)))  // :449 solverCG
+                    return rc;
+                if (ar.m > 0) {
+                    if ((rc = anderson_step(c, ar)))
+                        return rc;
+                } else {
+                    launch_add_du(c);
+                }
+                st.ms_solve += t.stop();
+            }
+            {
+                Timer t(c.stream);
+                if ((rc = force_eval(c, c.plmode)) || (rc = read_norms(c, res, reac)))  // :454-463
+                    return rc;
+                st.ms_force += t.stop();
+            }
+            if (c.trace)
+                std::fprintf(stderr, "lpm: step %lld newton %d res %.6e ratio %.3e step totals: cg %d sweeps %d solve %.1f ms force %.1f ms\n",
+                             c.trace_step, ni + nip + 1, res, res / std::max(res_best, 1e-300), st.cg_iters,
+                             st.refine_iters, st.ms_solve, st.ms_force);
+            if (ar.m > 0 && res > 10.0 * res_best) {  // safeguard: drop the history
+                ar.hist = 0;
+                ar.head = 0;
+            }
+            res_best = std::min(res_best, res);
+            nip++;
+        }
+        if (nip >= c.opts.newton_maxiter && res > c.opts.newton_tol * tolm)
+            st.status |= LPM_STATUS_NEWTON_MAXIT;
+        ni += nip;
+        passes++;
+        if (!c.dmg.on) {
+            switch_state(c, 1);  // :471
             break;
         }
-        switch_state(c, 0);  // :428
-        {
-            Timer t(c.stream);
-            if ((rc = solve_device(c, c.res, &st)))  // :449 solverCG
-                return rc;
-            if (ar.m > 0) {
-                if ((rc = anderson_step(c, ar)))
-                    return rc;
-            } else {
-                launch_add_du(c);
-            }
-            st.ms_solve += t.stop();
-        }
-        {
-            Timer t(c.stream);
-            if ((rc = force_eval(c, c.plmode)) || (rc = read_norms(c, res, reac)))  // :454-463
-                return rc;
-            st.ms_force += t.stop();
-        }
+        // damage stage: updateDamageGeneral, updateCrack, switchStateV(1) (:466-471)
+        int broken = 0;
+        if ((rc = damage_pass(c, broken)))
+            return rc;
+        st.bonds_broken += broken;
+        switch_state(c, 1);
         if (c.trace)
-            std::fprintf(stderr, "lpm: step %lld newton %d res %.6e ratio %.3e step totals: cg %d sweeps %d solve %.1f ms force %.1f ms\n",
-                         c.trace_step, ni + 1, res, res / std::max(res_best, 1e-300), st.cg_iters, st.refine_iters,
-                         st.ms_solve, st.ms_force);
-        if (ar.m > 0 && res > 10.0 * res_best) {  // safeguard: drop the history
-            ar.hist = 0;
-            ar.head = 0;
+            std::fprintf(stderr, "lpm: step %lld damage pass %d: %d bonds reached the criterion\n", c.trace_step,
+                         passes, broken);
+        if (broken <= 0 || passes >= c.dmg.opts.max_passes)
+            break;
+        // bonds broke: new stiffness, and the elastic-law bond forces of the
+        // current configuration that the reference's finite-difference sweep
+        // leaves behind (src/stiffness.c:390-418) start the next pass
+        {
+            Timer t(c.stream);
+            if ((rc = assemble(c)) || (rc = prepare_preconditioner(c)))
+                return rc;
+            st.ms_stiffness += t.stop();
         }
-        res_best = std::min(res_best, res);
-        ni++;
+        launch_elastic_force(c);
+        if ((rc = read_norms(c, res, reac)))
+            return rc;
+        tolm = std::max(res, reac);
     }
-    if (ni >= c.opts.newton_maxiter && res > c.opts.newton_tol * tolm)
-        st.status |= LPM_STATUS_NEWTON_MAXIT;
-    switch_state(c, 1);  // :471
+    st.damage_passes = c.dmg.on ? passes : 0;
     LPM_CUDA(cudaMemcpyAsync(c.status_host, c.status, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     if ((rc = sync(c)))
         return rc;
@@ -1665,6 +2001,24 @@ int lpm_get(lpm_ctx *ctx, const char *name, void *dst, size_t bytes)
         if (!need(nb * 3 * sizeof(double)))
             return fail(LPM_ERR_ARG, nm + ": buffer too small");
         std::memcpy(dst, c.hs.cs0.data(), nb * 3 * sizeof(double));
+        return LPM_OK;
+    }
+    if (nm == "damage_broken" || nm == "damage_w" || nm == "damage_D" || nm == "damage_nonlocal" ||
+        nm == "damage_visual" || nm == "nb_current") {
+        if (!c.dmg.on)
+            return fail(LPM_ERR_ARG, nm + ": the damage stage is off (lpm_set_damage)");
+        if (nm == "damage_broken") return bond_d(c.dmg.brk);
+        if (nm == "damage_w") return bond_d(c.dmg.dw);
+        if (nm == "damage_D") return bond_d(c.dmg.D[1]);
+        if (nm == "damage_nonlocal") return rows_d(c.dmg.dnl[1], 1);
+        if (nm == "damage_visual") return rows_d(c.dmg.dvis, 1);
+        if (!need(n * sizeof(int)))
+            return fail(LPM_ERR_ARG, nm + ": buffer too small");
+        std::vector<int8_t> t(n);
+        LPM_CUDA(cudaMemcpy(t.data(), c.dmg.nbc, n, cudaMemcpyDeviceToHost));
+        int *o = (int *)dst;
+        for (int i = 0; i < n; i++)
+            o[i] = t[i];
         return LPM_OK;
     }
     return fail(LPM_ERR_ARG, "unknown array name: " + nm);

@@ -255,6 +255,26 @@ struct Ctx {
     AdjointState *adj = nullptr;  // lpm_adjoint_forward / lpm_adjoint_backward
     AsyncWriter *writer = nullptr; // lpm_write_dump (output.cpp)
     int *pl_flag = nullptr;        // [n] set once a particle's return map has yielded (pl_flag)
+    // damage stage (lpm_set_damage; src/constitutive.c:149-164, :1399-1862).
+    // All pointers stay null while it is off, and the force and stiffness
+    // kernels then take their undamaged path unchanged.
+    struct Damage {
+        int on = 0;
+        lpm_damage_opts opts{};
+        double *brk = nullptr, *dw = nullptr;            // damage_broken, damage_w [NN][n]
+        double *D[2] = {nullptr, nullptr};               // damage_D slots 0, 1 [NN][n]
+        double *dnl[2] = {nullptr, nullptr};             // damage_nonlocal slots 0, 1 [n]
+        double *dvis = nullptr;                          // damage_visual [n]
+        int8_t *nbc = nullptr;                           // intact bonds per particle (current nb)
+        int8_t *opp = nullptr;                           // slot of the opposite bond, -1 none [NN][n]
+        int *cstart = nullptr, *corder = nullptr;        // cell list of the initial positions
+        int g[3] = {0, 0, 0};
+        double lo[3] = {0, 0, 0}, cs = 0;                // grid origin and cell size (>= 3 L)
+        int *list = nullptr;                             // bonds found by a damage kernel
+        double *lval = nullptr;                          // their bond strains (brittle)
+        int *count = nullptr, *count_h = nullptr;        // list length (device, pinned)
+        std::vector<int> log;                            // broken (particle, partner) pairs, in order
+    } dmg;
     // Anderson acceleration of the Newton loop (opts.newton_accel)
     struct Anderson {
         int m = 0;
@@ -279,6 +299,14 @@ void launch_apply_disp_bc(Ctx &c, int nbd, const lpm_disp_bc *d);
 void launch_apply_force_bc(Ctx &c, int nbf, const lpm_force_bc *f, const int *counts);
 void launch_cab(Ctx &c);
 void launch_strain(Ctx &c);  // k_strain.cu
+// damage stage (k_damage.cu; updateCrack in k_force.cu)
+void launch_dmg_nonlocal(Ctx &c);     // damage_nonlocal += weighted dlambda (slot 0)
+void launch_dmg_ductile_break(Ctx &c);// bonds of particles past the threshold -> list
+void launch_dmg_ductile_w(Ctx &c);    // D = max of the two particles, w = 1 - D
+void launch_dmg_brittle_cand(Ctx &c); // bonds at the critical strain -> list, lval
+void launch_dmg_break_list(Ctx &c, const int *bonds, int k);  // D = 1, w = 0, broken
+void launch_dmg_oppv(Ctx &c);         // stress weights from the intact bonds
+void launch_crack(Ctx &c);            // updateCrack + updateRR norms
 // stiffness (k_stiff.cu)
 void launch_tangent_geometry(Ctx &c);
 void launch_assemble(Ctx &c, bool fp32);

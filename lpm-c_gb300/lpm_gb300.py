@@ -36,6 +36,7 @@ EXPORTED = [
     "lpm_write_dump", "lpm_write_wait", "lpm_write_disp", "lpm_write_reaction", "lpm_write_stress",
     "lpm_format_dump", "lpm_format_disp", "lpm_format_reaction", "lpm_format_stress",
     "lpm_compute_strain", "lpm_write_strain", "lpm_format_strain",
+    "lpm_default_damage_opts", "lpm_set_damage", "lpm_damage_log",
 ]
 
 
@@ -85,7 +86,15 @@ class StepStats(C.Structure):
     _fields_ = [("newton_iters", C.c_int), ("cg_iters", C.c_int), ("refine_iters", C.c_int),
                 ("spmv_calls", C.c_int), ("status", C.c_int), ("res0", C.c_double),
                 ("reac0", C.c_double), ("res_final", C.c_double), ("ms_stiffness", C.c_double),
-                ("ms_solve", C.c_double), ("ms_force", C.c_double)]
+                ("ms_solve", C.c_double), ("ms_force", C.c_double), ("damage_passes", C.c_int),
+                ("bonds_broken", C.c_int)]
+
+
+class DamageOpts(C.Structure):
+    """lpm_damage_opts: the reference main's damage stage (include/lpm_gpu.h)."""
+    _fields_ = [("enabled", C.c_int), ("length", C.c_double), ("threshold", C.c_double),
+                ("triax_coeff", C.c_double), ("critical_bstrain", C.c_double), ("nbreak", C.c_int),
+                ("max_passes", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -163,6 +172,9 @@ def load(path=LIB_PATH):
         "lpm_compute_strain": ([vp], C.c_int),
         "lpm_write_strain": ([vp, C.c_char_p, C.c_int, C.c_int], C.c_int),
         "lpm_format_strain": ([C.c_char_p, C.c_int, C.c_int, C.c_int, ip, dp], C.c_int),
+        "lpm_default_damage_opts": ([C.POINTER(DamageOpts)], None),
+        "lpm_set_damage": ([vp, C.POINTER(DamageOpts)], C.c_int),
+        "lpm_damage_log": ([vp, ip, C.c_int, ip], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -431,6 +443,9 @@ class Specimen:
         "cp_gy": ("ns", np.float64), "cp_gy2": ("ns", np.float64), "cp_A_single": ("ns", np.float64),
         "cp_A_single2": ("ns", np.float64), "cp_A": ("n1", np.float64), "cp_A2": ("n1", np.float64),
         "cp_Cab": ("nss", np.float64),
+        "damage_broken": ("b", np.float64), "damage_w": ("b", np.float64), "damage_D": ("b", np.float64),
+        "damage_nonlocal": ("n1", np.float64), "damage_visual": ("n1", np.float64),
+        "nb_current": ("n1", np.int32),
     }
 
     def _shape(self, kind):
@@ -449,6 +464,29 @@ class Specimen:
         kind, dt = self._SHAPES.get(name, self._SHAPES.get(alias.get(name, ""), ("b", np.float64)))
         a = np.ascontiguousarray(arr, dtype=dt)
         self._check(self.L.lpm_set(self.h, name.encode(), a.ctypes.data_as(C.c_void_p), a.nbytes))
+
+    # ---- damage stage (updateDamageGeneral, updateCrack, re-solve)
+    def set_damage(self, enabled=True, **kw):
+        """Switch the reference main's damage stage on (keyword overrides of
+        lpm_default_damage_opts: length, threshold, triax_coeff,
+        critical_bstrain, nbreak, max_passes) or off (enabled=False)."""
+        o = DamageOpts()
+        self.L.lpm_default_damage_opts(C.byref(o))
+        o.enabled = 1 if enabled else 0
+        for k, v in kw.items():
+            if not hasattr(o, k):
+                raise KeyError(k)
+            setattr(o, k, v)
+        self._check(self.L.lpm_set_damage(self.h, C.byref(o)))
+
+    def damage_log(self):
+        """Broken bonds so far as (particle, partner) rows, in the reference's order."""
+        k = C.c_int()
+        self._check(self.L.lpm_damage_log(self.h, None, 0, C.byref(k)))
+        out = np.zeros((k.value, 2), dtype=np.int32)
+        if k.value:
+            self._check(self.L.lpm_damage_log(self.h, _ip(out), k.value, C.byref(k)))
+        return out
 
     def export_upper_csr(self):
         nnz = C.c_longlong()
