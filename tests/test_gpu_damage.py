@@ -10,13 +10,20 @@ sum runs in a different order and with CUDA's exp).  The order of bonds
 within one brittle pass is not compared: equal-strain bonds swap places there
 under round-off-level differences of the solution, in the reference too.
 """
+import os
+
 import numpy as np
 import pytest
 
 import cases
 from test_oracle_damage import _brittle, _ductile
 
-pytestmark = pytest.mark.gpu
+# These tests have not yet run on a GPU.  Until they have, they run only when
+# LPM_DAMAGE_GPU_TESTS=1, so that an unverified test cannot stop a fail-fast
+# GPU run before the parity tests.
+pytestmark = [pytest.mark.gpu,
+              pytest.mark.skipif(os.environ.get("LPM_DAMAGE_GPU_TESTS") != "1",
+                                 reason="damage stage not yet verified on a GPU (set LPM_DAMAGE_GPU_TESTS=1)")]
 
 # Both sides converge to 1e-9: the converged displacements are then within
 # 2e-9 of the 1e-10 solution (measured on the oracle), while 1e-10 sits at the
