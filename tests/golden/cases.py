@@ -163,6 +163,16 @@ class BrittleCase:
         return [b for b in sc_bcs(0.0) if b[0] != T_TOP] + [(T_PATCH, "z", inc)]
 
 
+# Setup-only shapes (lattice, radius, box) whose bond lists, AFEM
+# connectivity and CSR pattern are pinned against the reference: the 20^3
+# SC cube, a ragged SC box and a ragged FCC box.
+SETUP_SHAPES = {
+    "sc20": (2, 0.1, sc_box(20, 20, 20, 0.1)),
+    "sc7x3x11": (2, 0.1, sc_box_exact(7, 3, 11, 0.1)),
+    "fcc_ragged": (3, 0.1, [-0.07, 1.2, -0.07, 0.5, -0.07, 0.9]),
+}
+
+
 def cyclic_schedule(amplitude, steps_per_quarter, cycles):
     """Increments 0->+A->0->-A->0 per cycle, steps_per_quarter equal steps each."""
     inc = amplitude / steps_per_quarter

@@ -266,11 +266,30 @@ def damage_case(out, which):
     np.savez_compressed(os.path.join(out, f"{tag}.npz"), **arrs)
 
 
+def setup_case(out, name):
+    """Bond lists, AFEM connectivity and K_pointer of a setup-only shape
+    (searchNormalNeighbor, searchAFEMNeighbor), with the generated lattice."""
+    lattice, radius, box = cases.SETUP_SHAPES[name]
+    n = R.setup(lattice, radius, box)
+    nn = R.gint("nneighbors")
+    arrs = dict(
+        box=np.array(box), xyz=R.get_d2("xyz", n, 3),
+        neighbors=R.get_i2("neighbors", n, nn), nsign=R.get_i2("nsign", n, nn), nb=R.get_i1("nb", n),
+        distance_initial=R.get_d2("distance_initial", n, nn),
+        csx_initial=R.get_d2("csx_initial", n, nn), csy_initial=R.get_d2("csy_initial", n, nn),
+        csz_initial=R.get_d2("csz_initial", n, nn),
+        conn=R.get_i2("conn", n, R.gint("nneighbors_AFEM") + 1), nb_conn=R.get_i1("nb_conn", n),
+        K_pointer=R.get_i2("K_pointer", n + 1, 2))
+    np.savez_compressed(os.path.join(out, f"setup_{name}.npz"), **arrs)
+    print(f"setup {name}: {n} particles", flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--fcc-steps", type=int, default=12)
-    ap.add_argument("--only", choices=["sc", "fcc", "force", "ductile", "brittle"], default=None)
+    ap.add_argument("--only", choices=["sc", "fcc", "force", "ductile", "brittle"] +
+                    ["setup_" + k for k in cases.SETUP_SHAPES], default=None)
     ap.add_argument("--out", default=HERE)
     args = ap.parse_args()
     if not R.available():
@@ -282,11 +301,13 @@ def main():
         force_case(args.out)
     elif args.only in ("ductile", "brittle"):
         damage_case(args.out, args.only)
+    elif args.only and args.only.startswith("setup_"):
+        setup_case(args.out, args.only[len("setup_"):])
     elif args.only == "sc":
         sc_case(args.out, args.steps)
     else:
         import subprocess
-        for which in ("sc", "fcc", "force", "ductile", "brittle"):
+        for which in ["sc", "fcc", "force", "ductile", "brittle"] + ["setup_" + k for k in cases.SETUP_SHAPES]:
             subprocess.check_call([sys.executable, __file__, "--only", which, "--steps", str(args.steps),
                                    "--fcc-steps", str(args.fcc_steps), "--out", args.out])
 

@@ -172,3 +172,29 @@ def test_force_bc_steps_match_oracle(oracle_mod, gpu_lib, precision):
     a_o = o.d("alpha1", (n,))
     assert a_o.max() > 0.0
     assert np.abs(s.get("J2_alpha") - a_o).max() <= 1e-8 * a_o.max()
+
+
+@pytest.mark.parametrize("name", sorted(cases.SETUP_SHAPES))
+def test_setup_shapes_bit_exact(gpu_lib, name):
+    """GPU library setup (host cell-list search, device upload) against the
+    reference's own bond lists, AFEM connectivity and K_pointer for the 20^3
+    SC cube and ragged SC and FCC boxes (tests/golden/setup_*.npz)."""
+    from conftest import golden
+    lattice, radius, box = cases.SETUP_SHAPES[name]
+    g = golden(f"setup_{name}.npz")
+    s = gpu_lib.Specimen(0)
+    n = s.setup_lattice(lattice, radius, box)
+    assert n == g["xyz"].shape[0]
+    assert np.array_equal(s.get("xyz"), g["xyz"])
+    assert np.array_equal(s.get("neighbors"), g["neighbors"])
+    assert np.array_equal(s.get("nsign"), g["nsign"])
+    assert np.array_equal(s.get("nb"), g["nb"])
+    assert np.array_equal(s.get("distance_initial"), g["distance_initial"])
+    cs = s.get("cs_initial")
+    for k, c in enumerate(("x", "y", "z")):
+        assert np.array_equal(cs[:, :, k], g[f"cs{c}_initial"])
+    assert np.array_equal(s.get("conn"), g["conn"])
+    assert np.array_equal(s.get("nb_conn"), g["nb_conn"])
+    kp = s.get("K_pointer")
+    assert np.array_equal(kp[:n, 0], g["K_pointer"][:n, 0])
+    assert np.array_equal(kp[:, 1], g["K_pointer"][:, 1])

@@ -231,3 +231,28 @@ def test_force_bc_bit_exact(oracle_mod):
     assert g["s_alpha"].max() > 0.0
     assert np.array_equal(o.d("Pex", (3 * n,)), g["s_Pex"])
     assert np.array_equal(o.d("F", (n, 18)), g["s_F"])
+
+
+@pytest.mark.parametrize("name", sorted(cases.SETUP_SHAPES))
+def test_setup_shapes_bit_exact(oracle_mod, name):
+    """Bond lists, AFEM connectivity and K_pointer of the 20^3 SC cube and of
+    ragged SC and FCC boxes (searchNormalNeighbor, searchAFEMNeighbor)."""
+    lattice, radius, box = cases.SETUP_SHAPES[name]
+    g = golden(f"setup_{name}.npz")
+    o = oracle_mod.Oracle()
+    n = o.setup_lattice(lattice, radius, box)
+    nn = o.nn
+    assert n == g["xyz"].shape[0]
+    assert np.array_equal(o.d("xyz", (n, 3)), g["xyz"])
+    assert np.array_equal(o.i("neighbors", (n, nn)), g["neighbors"])
+    assert np.array_equal(o.i("nsign", (n, nn)), g["nsign"])
+    assert np.array_equal(o.i("nb", (n,)), g["nb"])
+    assert np.array_equal(o.d("distance_initial", (n, nn)), g["distance_initial"])
+    for k in ("x", "y", "z"):
+        assert np.array_equal(o.d(f"cs{k}_initial", (n, nn)), g[f"cs{k}_initial"])
+    w = g["conn"].shape[1]
+    assert np.array_equal(o.i("conn", (n, w)), g["conn"])
+    assert np.array_equal(o.i("nb_conn", (n,)), g["nb_conn"])
+    kp = g["K_pointer"]
+    assert np.array_equal(o.i("kp0", (n + 1,))[:n], kp[:n, 0])
+    assert np.array_equal(o.i("kp1", (n + 1,)), kp[:, 1])
