@@ -178,6 +178,13 @@ int lpm_set_damage(lpm_ctx *ctx, const lpm_damage_opts *opts);
  * reference writes them to its bond file.  pairs may be NULL to query the
  * count; otherwise it holds 2 * capacity ints. */
 int lpm_damage_log(lpm_ctx *ctx, int *pairs, int capacity, int *count);
+/* The brittle pass's choice (updateBrittleDamage, src/constitutive.c:1471-1520)
+ * among k candidate bonds b = slot * n + particle, given in any order with
+ * their bond strains: scan order, then, above nbreak candidates, the
+ * reference's shell sort and its last nbreak entries.  Host logic only (no
+ * context, no GPU); chosen receives up to k bonds, *nchosen their count. */
+int lpm_damage_brittle_select(const int *bonds, const double *strain, int k, int n, int nbreak, int *chosen,
+                              int *nchosen);
 
 /* switchStateV (src/constitutive.c:10-85): 0 = converged -> current,
  * 1 = current -> converged. */

@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 #include "lpm_internal.h"
+#include "damage_select.h"
 
 namespace lpm {
 
@@ -1002,43 +1003,11 @@ static int damage_pass(Ctx &c, int &broken)
         if (rc)
             return rc;
         if (k > 0) {
-            std::vector<int> b(k), idx(k);
+            std::vector<int> b(k);
             std::vector<double> v(k);
             LPM_CUDA(cudaMemcpy(b.data(), d.list, sizeof(int) * k, cudaMemcpyDeviceToHost));
             LPM_CUDA(cudaMemcpy(v.data(), d.lval, sizeof(double) * k, cudaMemcpyDeviceToHost));
-            for (int q = 0; q < k; q++)
-                idx[q] = q;
-            std::sort(idx.begin(), idx.end(), [&](int x, int y) {
-                const int ix = b[x] % n, iy = b[y] % n;
-                return ix != iy ? ix < iy : b[x] / n < b[y] / n;
-            });
-            std::vector<int> bi(k);
-            std::vector<double> bs(k);
-            for (int q = 0; q < k; q++) {
-                bi[q] = b[idx[q]];
-                bs[q] = v[idx[q]];
-            }
-            int first = 0;
-            const int nbreak = d.opts.nbreak;
-            if (k > nbreak) {
-                // the reference's shell sort, ascending strain (gaps k/2, k/4, ..., 1);
-                // the last nbreak entries (largest strains) break
-                for (int r = k / 2; r >= 1; r = r / 2)
-                    for (int i = r; i < k; ++i) {
-                        const int tb = bi[i];
-                        const double ts = bs[i];
-                        int j = i - r;
-                        while (j >= 0 && bs[j] > ts) {
-                            bs[j + r] = bs[j];
-                            bi[j + r] = bi[j];
-                            j = j - r;
-                        }
-                        bs[j + r] = ts;
-                        bi[j + r] = tb;
-                    }
-                first = k - nbreak;
-            }
-            std::vector<int> chosen(bi.begin() + first, bi.end());
+            const std::vector<int> chosen = brittle_select(b, v, n, d.opts.nbreak);
             if (!chosen.empty()) {
                 LPM_CUDA(cudaMemcpyAsync(d.list, chosen.data(), sizeof(int) * chosen.size(), cudaMemcpyHostToDevice,
                                          c.stream));
@@ -1237,6 +1206,18 @@ int lpm_damage_log(lpm_ctx *ctx, int *pairs, int capacity, int *count)
             return fail(LPM_ERR_ARG, "damage log: buffer too small");
         std::memcpy(pairs, c.dmg.log.data(), sizeof(int) * 2 * (size_t)k);
     }
+    return LPM_OK;
+}
+
+int lpm_damage_brittle_select(const int *bonds, const double *strain, int k, int n, int nbreak, int *chosen,
+                              int *nchosen)
+{
+    if (k < 0 || n <= 0 || nbreak < 0 || !nchosen || (k > 0 && (!bonds || !strain || !chosen)))
+        return fail(LPM_ERR_ARG, "lpm_damage_brittle_select: bad argument");
+    const std::vector<int> c = brittle_select(std::vector<int>(bonds, bonds + k),
+                                              std::vector<double>(strain, strain + k), n, nbreak);
+    std::copy(c.begin(), c.end(), chosen);
+    *nchosen = (int)c.size();
     return LPM_OK;
 }
 

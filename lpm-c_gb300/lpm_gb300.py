@@ -36,7 +36,7 @@ EXPORTED = [
     "lpm_write_dump", "lpm_write_wait", "lpm_write_disp", "lpm_write_reaction", "lpm_write_stress",
     "lpm_format_dump", "lpm_format_disp", "lpm_format_reaction", "lpm_format_stress",
     "lpm_compute_strain", "lpm_write_strain", "lpm_format_strain",
-    "lpm_default_damage_opts", "lpm_set_damage", "lpm_damage_log",
+    "lpm_default_damage_opts", "lpm_set_damage", "lpm_damage_log", "lpm_damage_brittle_select",
 ]
 
 
@@ -175,6 +175,7 @@ def load(path=LIB_PATH):
         "lpm_default_damage_opts": ([C.POINTER(DamageOpts)], None),
         "lpm_set_damage": ([vp, C.POINTER(DamageOpts)], C.c_int),
         "lpm_damage_log": ([vp, ip, C.c_int, ip], C.c_int),
+        "lpm_damage_brittle_select": ([ip, dp, C.c_int, C.c_int, C.c_int, ip, ip], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -207,6 +208,19 @@ def default_opts():
     o = SolverOpts()
     load().lpm_default_solver_opts(C.byref(o))
     return o
+
+
+def brittle_select(bonds, strain, n, nbreak):
+    """lpm_damage_brittle_select: the brittle pass's choice among candidate
+    bonds (b = slot * n + particle, any order); host logic, no GPU needed."""
+    L = load()
+    b = np.ascontiguousarray(bonds, dtype=np.int32)
+    v = np.ascontiguousarray(strain, dtype=np.float64)
+    out = np.zeros(max(len(b), 1), dtype=np.int32)
+    k = C.c_int()
+    if L.lpm_damage_brittle_select(_ip(b), _dp(v), len(b), int(n), int(nbreak), _ip(out), C.byref(k)) != 0:
+        raise LPMError(L.lpm_last_error().decode())
+    return out[:k.value]
 
 
 class Specimen:

@@ -1643,6 +1643,33 @@ static int damage_ductile_nonlocal(lpm_oracle *o)
     return k;
 }
 
+/* The choice of updateBrittleDamage (src/constitutive.c:1471-1520) among k
+ * candidates given in the reference's scan order: all of them when k <=
+ * nbreak, else the reference's ascending shell sort (gaps k/2, k/4, ..., 1)
+ * and the last nbreak.  Sorts (bi, bj, bs) in place and returns the index of
+ * the first chosen entry. */
+int lo_brittle_select(int *bi, int *bj, double *bs, int k, int nbreak)
+{
+    if (k <= nbreak)
+        return 0;
+    for (int r = k / 2; r >= 1; r = r / 2)
+        for (int i = r; i < k; ++i) {
+            int ti = bi[i], tj = bj[i];
+            double tb = bs[i];
+            int j = i - r;
+            while (j >= 0 && bs[j] > tb) {
+                bs[j + r] = bs[j];
+                bi[j + r] = bi[j];
+                bj[j + r] = bj[j];
+                j = j - r;
+            }
+            bs[j + r] = tb;
+            bi[j + r] = ti;
+            bj[j + r] = tj;
+        }
+    return k - nbreak;
+}
+
 /* updateBrittleDamage, src/constitutive.c:1437-1527: bonds whose elastic
  * stretch / initial length reaches critical_bstrain are candidates (scan
  * order i, then j); at most nbreak of them break, the largest strains after
@@ -1674,25 +1701,7 @@ static int damage_brittle(lpm_oracle *o)
                 k++;
             }
         }
-    int first = 0;
-    if (k > nbreak) {
-        for (int r = k / 2; r >= 1; r = r / 2)
-            for (int i = r; i < k; ++i) {
-                int ti = bi[i], tj = bj[i];
-                double tb = bs[i];
-                int j = i - r;
-                while (j >= 0 && bs[j] > tb) {
-                    bs[j + r] = bs[j];
-                    bi[j + r] = bi[j];
-                    bj[j + r] = bj[j];
-                    j = j - r;
-                }
-                bs[j + r] = tb;
-                bi[j + r] = ti;
-                bj[j + r] = tj;
-            }
-        first = k - nbreak;
-    }
+    int first = lo_brittle_select(bi, bj, bs, k, nbreak);
     for (int q = first; q < k; q++) {
         size_t b = (size_t)bi[q] * nn + bj[q];
         o->dD[0][b] = 1.0;

@@ -87,6 +87,9 @@ void lo_force(lpm_oracle *o, int plmode);
 void lo_set_damage(lpm_oracle *o, double L, double threshold, double cA, double crit_bstrain, int nbreak);
 int lo_damage_update(lpm_oracle *o, int plmode);
 void lo_update_crack(lpm_oracle *o);
+/* the brittle pass's choice among k candidates in scan order: sorts the
+ * arrays in place, returns the index of the first chosen entry */
+int lo_brittle_select(int *bi, int *bj, double *bs, int k, int nbreak);
 /* broken bonds logged so far as (i, neighbour) pairs; pairs may be NULL */
 int lo_broken_log(const lpm_oracle *o, int *pairs);
 int lo_load_step_damage(lpm_oracle *o, int nbd, const lo_disp_bc *d, int nbf, const lo_force_bc *f,

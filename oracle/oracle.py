@@ -77,6 +77,7 @@ def lib():
         L.lo_damage_update.argtypes = [vp, C.c_int]
         L.lo_update_crack.argtypes = [vp]
         L.lo_broken_log.argtypes = [vp, C.POINTER(C.c_int)]
+        L.lo_brittle_select.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_int), dp, C.c_int, C.c_int]
         L.lo_load_step_damage.argtypes = [vp, C.c_int, C.POINTER(DispBC), C.c_int, C.POINTER(ForceBC),
                                           C.c_double, C.c_int, C.c_double, C.c_double, C.c_int, dp]
         _lib = L
@@ -100,6 +101,17 @@ def bc_arrays(disp_bcs, force_bcs):
     for k, (t, fx, fy, fz) in enumerate(force_bcs):
         farr[k] = ForceBC(t, b"x", fx, b"y", fy, b"z", fz)
     return nd, darr, nf, farr
+
+
+def brittle_select(bi, bj, strain, nbreak):
+    """updateBrittleDamage's choice among candidates given in scan order:
+    the chosen (i, j) slots in the order they break."""
+    bi = np.ascontiguousarray(bi, dtype=np.int32).copy()
+    bj = np.ascontiguousarray(bj, dtype=np.int32).copy()
+    bs = np.ascontiguousarray(strain, dtype=np.float64).copy()
+    first = lib().lo_brittle_select(bi.ctypes.data_as(C.POINTER(C.c_int)), bj.ctypes.data_as(C.POINTER(C.c_int)),
+                                    _dp(bs), len(bs), int(nbreak))
+    return np.stack([bi[first:], bj[first:]], axis=1)
 
 
 class Oracle:
