@@ -78,6 +78,12 @@ typedef struct {
                            vectors, and so are the context's later solves */
     int newton_accel;   /* 0: modified Newton as the reference (u += K^-1 r); m > 0: the same
                            fixed-point iteration with Anderson acceleration of depth m (<= 16) */
+    double cg_forcing;  /* 0 (default): every linear solve to cg_rtol.  eta_max in (0, 1): inexact
+                           Newton, the k-th solve of a step only to eta_k = the Eisenstat-Walker
+                           choice 2 (0.9 (|r_k| / |r_k-1|)^2, safeguarded), capped at eta_max, never
+                           tighter than cg_rtol nor than half the Newton target over |r_k|.  The
+                           step converges to the same Newton tolerance with far fewer PCG
+                           iterations when modified Newton contracts slowly (plastic range). */
 } lpm_solver_opts;
 
 typedef struct {

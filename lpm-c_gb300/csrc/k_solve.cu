@@ -683,7 +683,7 @@ void launch_refine_batch(Ctx &c, const dvec4 *x, const dvec4 *b, dvec4 *r)
 void launch_cg_init_fx(Ctx &c, const dvec4 *b, double scale, double delta2)
 {
     k_cg_init<double, dvec4><<<red_grid(c), VTPB, 0, c.stream>>>(
-        vec_args(c), b, scale, c.Pinv_d, c.x_d, c.r_d, c.z_d, c.p_d, c.opts.cg_rtol, c.opts.cg_maxiter, delta2);
+        vec_args(c), b, scale, c.Pinv_d, c.x_d, c.r_d, c.z_d, c.p_d, solve_rtol(c), c.opts.cg_maxiter, delta2);
 }
 
 void launch_cg_iter_fx(Ctx &c)
@@ -704,7 +704,7 @@ void launch_reliable_d(Ctx &c, const dvec4 *rtrue)
 void launch_cg_init_d(Ctx &c, const dvec4 *b, double scale)
 {
     k_cg_init<double, dvec4><<<red_grid(c), VTPB, 0, c.stream>>>(
-        vec_args(c), b, scale, c.Pinv_d, c.x_d, c.r_d, c.z_d, c.p_d, c.opts.cg_rtol, c.opts.cg_maxiter, 0.0);
+        vec_args(c), b, scale, c.Pinv_d, c.x_d, c.r_d, c.z_d, c.p_d, solve_rtol(c), c.opts.cg_maxiter, 0.0);
 }
 
 void launch_cg_init_f(Ctx &c, const dvec4 *r64, double scale, double rtol, double delta2)

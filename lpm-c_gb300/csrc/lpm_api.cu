@@ -402,6 +402,7 @@ void lpm_default_solver_opts(lpm_solver_opts *o)
     o->use_graphs = 1;
     o->mixed_vectors = 32;
     o->newton_accel = 0;
+    o->cg_forcing = 0.0;
 }
 
 int lpm_create(lpm_ctx **out, int device)
@@ -466,7 +467,7 @@ int lpm_set_solver(lpm_ctx *ctx, const lpm_solver_opts *o)
     if (o->precision != LPM_PREC_FP64 && o->precision != LPM_PREC_MIXED)
         return fail(LPM_ERR_ARG, "unknown precision");
     if (!(o->cg_rtol > 0) || o->cg_maxiter <= 0 || o->newton_maxiter < 0 || o->check_every <= 0 ||
-        o->newton_accel < 0 || o->newton_accel > 16)
+        o->newton_accel < 0 || o->newton_accel > 16 || !(o->cg_forcing >= 0.0 && o->cg_forcing < 1.0))
         return fail(LPM_ERR_ARG, "invalid solver options");
     Ctx &c = ctx->c;
     const bool prec_change = c.opts.precision != o->precision;
@@ -794,7 +795,7 @@ int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
                 return rc;
             rel = std::sqrt(c.norms_host[2]);
             sweeps++;
-            if (rel <= c.opts.cg_rtol || done == 2 || done == 3 || !std::isfinite(rel) ||
+            if (rel <= solve_rtol(c) || done == 2 || done == 3 || !std::isfinite(rel) ||
                 sweeps >= c.opts.refine_maxiter)
                 break;
             launch_reliable_d(c, c.q_d);
@@ -803,7 +804,7 @@ int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
             st->cg_iters += it;
             st->spmv_calls += it + sweeps;
             st->refine_iters += sweeps;
-            if (rel > c.opts.cg_rtol)
+            if (rel > solve_rtol(c))
                 st->status |= std::isfinite(rel) ? LPM_STATUS_CG_MAXIT : LPM_STATUS_NAN;
         }
         if (c.trace)
@@ -831,7 +832,7 @@ int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
         return LPM_OK;
     }
     LPM_CUDA(cudaMemsetAsync(c.x_d, 0, sizeof(dvec4) * c.n, c.stream));
-    launch_cg_init_f(c, b, scale, c.opts.cg_rtol, delta * delta);
+    launch_cg_init_f(c, b, scale, solve_rtol(c), delta * delta);
     int sweeps = 0, it = 0, done = 0;
     double rn = bn;
     std::vector<double> hist;  // true residual after each reliable update
@@ -847,7 +848,7 @@ int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
         rn = std::sqrt(c.norms_host[2]);
         sweeps++;
         hist.push_back(rn);
-        if (rn <= c.opts.cg_rtol * bn || done == 3 || !std::isfinite(rn) || sweeps >= c.opts.refine_maxiter)
+        if (rn <= solve_rtol(c) * bn || done == 3 || !std::isfinite(rn) || sweeps >= c.opts.refine_maxiter)
             break;
         // FP32 vectors stagnate on very ill-conditioned systems: a healthy
         // sweep cuts the true residual by about inner_rtol, so three sweeps
@@ -872,7 +873,7 @@ int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
         c.vec64_fallback = true;
         return solve_device(c, b, st);
     }
-    if (st && rn > c.opts.cg_rtol * bn)
+    if (st && rn > solve_rtol(c) * bn)
         st->status |= std::isfinite(rn) ? LPM_STATUS_CG_MAXIT : LPM_STATUS_NAN;
     LPM_CUDA(cudaMemcpyAsync(c.du, c.x_d, sizeof(dvec4) * c.n, cudaMemcpyDeviceToDevice, c.stream));
     return LPM_OK;
@@ -1488,7 +1489,7 @@ int lpm_load_step(lpm_ctx *ctx, int nbd, const lpm_disp_bc *dbc, int nbf, const 
     // label_broken_bond re-entry (src/lpmc_project.c:405, :528-546).
     int passes = 0;
     for (;;) {
-        double res_best = res;
+        double res_best = res, res_prev = res, eta_prev = c.opts.cg_forcing;
         int nip = 0;
         ar.hist = 0;  // a pass starts without acceleration history
         ar.head = 0;
@@ -1499,9 +1500,28 @@ int lpm_load_step(lpm_ctx *ctx, int nbd, const lpm_disp_bc *dbc, int nbf, const 
                 break;
             }
             switch_state(c, 0);  // :428
+            if (c.opts.cg_forcing > 0.0) {
+                // inexact Newton (Eisenstat & Walker 1996, choice 2): solve only as
+                // far as the outer iteration can use
+                const double emax = c.opts.cg_forcing;
+                double eta = emax;
+                if (nip > 0) {
+                    const double q = res / res_prev;
+                    eta = 0.9 * q * q;
+                    if (0.9 * eta_prev * eta_prev > 0.1)
+                        eta = std::max(eta, 0.9 * eta_prev * eta_prev);
+                }
+                eta = std::max(eta, 0.5 * c.opts.newton_tol * tolm / res);
+                eta = std::min(std::max(eta, c.opts.cg_rtol), emax);
+                c.cg_rtol_now = eta;
+                eta_prev = eta;
+            }
+            res_prev = res;
             {
                 Timer t(c.stream);
-                if ((rc = solve_device(c, c.res, &st)))  // :449 solverCG
+                rc = solve_device(c, c.res, &st);  // :449 solverCG
+                c.cg_rtol_now = 0.0;
+                if (rc)
                     return rc;
                 if (ar.m > 0) {
                     if ((rc = anderson_step(c, ar)))

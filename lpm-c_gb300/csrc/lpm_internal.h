@@ -246,6 +246,7 @@ struct Ctx {
     bool graph_timed = false;
     bool time_this = false;  // the next SpMV launch carries the timing events
     bool vec64_fallback = false;  // mixed: FP32-vector PCG stagnated, use FP64 vectors
+    double cg_rtol_now = 0.0;     // relative tolerance of the current solve (0: opts.cg_rtol)
     bool trace = false;           // LPM_TRACE set: one stderr line per Newton iteration and solve
     long long trace_step = 0;     // load steps run by this context (trace numbering)
     // batched specimens (lpm_setup_batch); nspec == 0 for a single specimen
@@ -284,6 +285,9 @@ struct Ctx {
     } acc;
     ~Ctx();
 };
+
+// relative tolerance of the linear solve being run (inexact Newton sets it per solve)
+inline double solve_rtol(const Ctx &c) { return c.cg_rtol_now > 0.0 ? c.cg_rtol_now : c.opts.cg_rtol; }
 
 // ---- kernel launchers (stream-ordered, no synchronisation) ----
 // force path (k_force.cu, FP64, no FMA contraction)

@@ -55,7 +55,7 @@ class SolverOpts(C.Structure):
     _fields_ = [("precision", C.c_int), ("newton_tol", C.c_double), ("newton_maxiter", C.c_int),
                 ("cg_rtol", C.c_double), ("cg_maxiter", C.c_int), ("inner_rtol", C.c_double),
                 ("refine_maxiter", C.c_int), ("check_every", C.c_int), ("use_graphs", C.c_int),
-                ("mixed_vectors", C.c_int), ("newton_accel", C.c_int)]
+                ("mixed_vectors", C.c_int), ("newton_accel", C.c_int), ("cg_forcing", C.c_double)]
 
 
 class Tuning(C.Structure):
