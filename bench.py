@@ -484,7 +484,7 @@ def run_adjoint(args):
     plate = cases.NotchedPlate(nx=args.plate_n, ny=10, nz=args.plate_n, notch=max(1, args.plate_n // 5),
                                steps=args.adj_steps, strain=args.adj_strain, corr=10.0)
     solver = dict(precision=G.PREC_FP64, newton_tol=args.adj_newton_tol, newton_maxiter=2000, cg_rtol=1e-12,
-                  cg_maxiter=200000, newton_accel=8)
+                  cg_maxiter=200000, newton_accel=8, cg_forcing=args.adj_forcing)
     bcs = plate.step_bcs()
 
     def specimen():
@@ -537,6 +537,7 @@ def run_adjoint(args):
                                f"{plate.steps} steps to {100 * plate.strain:g}% strain, loss vs seed-2 curve",
                    "particles": plate.n, "forward_s": t1 - t0, "backward_s": t2 - t1, "loss": L,
                    "adjoint_stats": st, "newton_tol": args.adj_newton_tol, "newton_accel": 8,
+                   "cg_forcing": args.adj_forcing,
                    "checkpoint_every": 10, "fd_checks": fd},
         "clocks": ck, "e2e": None, "cpu_baseline": None,
     }
@@ -642,6 +643,8 @@ def main():
     ap.add_argument("--plate-n", type=int, default=200)
     ap.add_argument("--adj-steps", type=int, default=60)
     ap.add_argument("--adj-newton-tol", type=float, default=1e-10)
+    ap.add_argument("--adj-forcing", type=float, default=0.0,
+                    help="adjoint workload: inexact-Newton forcing cap (opts.cg_forcing; 0 = exact solves)")
     ap.add_argument("--adj-fd", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
