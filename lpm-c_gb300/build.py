@@ -38,7 +38,7 @@ CU_UNITS = [
     ("k_damage.cu", ["-fmad=false"]),
 ]
 CPP_UNITS = [("setup.cpp", ["-ffp-contract=off", "-fopenmp"]), ("output.cpp", ["-ffp-contract=off"])]
-LEGACY_UNITS = [("legacy.cpp", [])]
+LEGACY_UNITS = [("legacy.cpp", ["-fopenmp"])]
 
 
 def _nvcc():
@@ -110,8 +110,8 @@ def build(verbose=False, ptxas_info=False):
         if _stale(obj, [src] + hdr):
             _run(["g++", "-O2", "-std=c++17", "-fPIC", "-I", INCLUDE] + extra + ["-c", src, "-o", obj])
     if lobjs and _stale(LEGACY_LIB, lobjs + [LIB]):
-        _run(["g++", "-shared", "-o", LEGACY_LIB] + lobjs + ["-L", OUT, "-llpmgpu",
-                                                              "-Wl,-rpath,$ORIGIN"])
+        _run(["g++", "-shared", "-fopenmp", "-o", LEGACY_LIB] + lobjs + ["-L", OUT, "-llpmgpu",
+                                                                         "-Wl,-rpath,$ORIGIN"])
     # C host driver: defines the include/lpm.h globals, runs the reference loop
     host_src = os.path.join(HERE, "host", "lpm_host.c")
     if os.path.exists(host_src) and _stale(HOST_LIB, [host_src, LEGACY_LIB] + hdr):

@@ -9,6 +9,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
+#include <utility>
 #include <vector>
 #include "lpm_gpu.h"
 #include "lpm_legacy.h"
@@ -74,46 +76,76 @@ lpm_ctx *ctx()
     return g_ctx;
 }
 
-// flatten / scatter helpers for the pointer-of-pointer globals
-std::vector<double> flat2(double **a, int rows, int cols)
+// Host vectors whose resize() does not zero-fill: every element is written
+// by the parallel loop or the copy that fills it.
+template <typename T>
+struct NoInit : std::allocator<T> {
+    template <typename U>
+    struct rebind {
+        typedef NoInit<U> other;
+    };
+    NoInit() = default;
+    template <typename U>
+    NoInit(const NoInit<U> &) noexcept
+    {
+    }
+    template <typename U>
+    void construct(U *p) noexcept
+    {
+        ::new (static_cast<void *>(p)) U;
+    }
+    template <typename U, typename... A>
+    void construct(U *p, A &&...a)
+    {
+        ::new (static_cast<void *>(p)) U(std::forward<A>(a)...);
+    }
+};
+typedef std::vector<double, NoInit<double>> dvec;
+
+// flatten / scatter helpers for the pointer-of-pointer globals (rows in parallel)
+dvec flat2(double **a, int rows, int cols)
 {
-    std::vector<double> v((size_t)rows * cols);
+    dvec v((size_t)rows * cols);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < rows; i++)
         std::memcpy(&v[(size_t)i * cols], a[i], sizeof(double) * cols);
     return v;
 }
 
-void scatter2(double **a, const std::vector<double> &v, int rows, int cols)
+void scatter2(double **a, const dvec &v, int rows, int cols)
 {
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < rows; i++)
         std::memcpy(a[i], &v[(size_t)i * cols], sizeof(double) * cols);
 }
 
-std::vector<double> flat3(double ***a, int rows, int cols, int slot)
+dvec flat3(double ***a, int rows, int cols, int slot)
 {
-    std::vector<double> v((size_t)rows * cols);
+    dvec v((size_t)rows * cols);
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < rows; i++)
         for (int j = 0; j < cols; j++)
             v[(size_t)i * cols + j] = a[i][j][slot];
     return v;
 }
 
-void scatter3(double ***a, const std::vector<double> &v, int rows, int cols, int slot)
+void scatter3(double ***a, const dvec &v, int rows, int cols, int slot)
 {
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < rows; i++)
         for (int j = 0; j < cols; j++)
             a[i][j][slot] = v[(size_t)i * cols + j];
 }
 
-void put(const char *name, const std::vector<double> &v)
+void put(const char *name, const dvec &v)
 {
     check(lpm_set(ctx(), name, v.data(), v.size() * sizeof(double)), name);
     g_h2d += (long long)(v.size() * sizeof(double));
 }
 
-std::vector<double> get(const char *name, size_t count)
+dvec get(const char *name, size_t count)
 {
-    std::vector<double> v(count);
+    dvec v(count);
     check(lpm_get(ctx(), name, v.data(), v.size() * sizeof(double)), name);
     g_d2h += (long long)(v.size() * sizeof(double));
     return v;
@@ -131,6 +163,7 @@ void put_mask()
 // computeStress's derived outputs (src/lpm_basic.c:101-123) from the stress tensor
 void stress_derived()
 {
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < nparticle; i++) {
         double *s = stress_tensor[i];
         double q = 0.0;
@@ -153,7 +186,7 @@ void device_force(int pl, bool stress_outputs)
 {
     const int n = nparticle, nn = nneighbors;
     put("xyz", flat2(xyz, n, 3));
-    put("Pex", std::vector<double>(Pex, Pex + 3 * (size_t)n));
+    put("Pex", dvec(Pex, Pex + 3 * (size_t)n));
     put_mask();
     put("dLp0", flat3(dLp, n, nn, 0));
     if (pl == 4) {
@@ -164,7 +197,7 @@ void device_force(int pl, bool stress_outputs)
         put("csz", flat2(csz, n, nn));
     } else {
         put("J2_alpha0", [&] {
-            std::vector<double> a(n);
+            dvec a(n);
             for (int i = 0; i < n; i++)
                 a[i] = J2_alpha[i][0];
             return a;
@@ -173,7 +206,7 @@ void device_force(int pl, bool stress_outputs)
         if (pl == 1 && nslipSys > 0) {
             put("cp_gy0", flat3(cp_gy, n, nslipSys, 0));
             put("cp_A_single0", flat3(cp_A_single, n, nslipSys, 0));
-            std::vector<double> a(n);
+            dvec a(n);
             for (int i = 0; i < n; i++)
                 a[i] = cp_A[i][0];
             put("cp_A0", a);
@@ -182,7 +215,7 @@ void device_force(int pl, bool stress_outputs)
     double norms[2];
     check(lpm_compute_force(ctx(), pl, norms), "computeBondForceGeneral");
     scatter2(F, get("F", (size_t)n * nn), n, nn);
-    const std::vector<double> pin = get("Pin", 3 * (size_t)n);
+    const dvec pin = get("Pin", 3 * (size_t)n);
     std::memcpy(Pin, pin.data(), pin.size() * sizeof(double));
     if (pl != 4) {
         scatter2(csx, get("csx", (size_t)n * nn), n, nn);
@@ -192,17 +225,17 @@ void device_force(int pl, bool stress_outputs)
         scatter3(dLp, get("dLp2", (size_t)n * nn), n, nn, 2);
     }
     if (pl == 0) {
-        const std::vector<double> a = get("J2_alpha2", n);
+        const dvec a = get("J2_alpha2", n);
         for (int i = 0; i < n; i++)
             J2_alpha[i][2] = a[i];
         scatter3(J2_beta, get("J2_beta2", 6 * (size_t)n), n, 6, 2);
-        const std::vector<double> dl = get("J2_dlambda", n);
+        const dvec dl = get("J2_dlambda", n);
         std::memcpy(J2_dlambda, dl.data(), dl.size() * sizeof(double));
     }
     if (pl == 1 && nslipSys > 0) {
         scatter3(cp_gy, get("cp_gy2", (size_t)n * nslipSys), n, nslipSys, 2);
         scatter3(cp_A_single, get("cp_A_single2", (size_t)n * nslipSys), n, nslipSys, 2);
-        const std::vector<double> a = get("cp_A2", n);
+        const dvec a = get("cp_A2", n);
         for (int i = 0; i < n; i++)
             cp_A[i][2] = a[i];
     }
@@ -258,7 +291,7 @@ void calcKnTv(void)
     if (g_opts_set)
         check(lpm_set_solver(g_ctx, &g_opts), "lpm_set_solver");
     const int n = nparticle, nn = nneighbors;
-    std::vector<double> x0 = flat2(xyz_initial, n, 3);
+    dvec x0 = flat2(xyz_initial, n, 3);
     check(lpm_setup_particles(g_ctx, lattice, radius, n, x0.data()), "lpm_setup_particles");
     std::vector<int> nbr((size_t)n * 18);
     check(lpm_get(g_ctx, "neighbors", nbr.data(), nbr.size() * sizeof(int)), "neighbors");

@@ -46,6 +46,40 @@ static void dfree(T *&p)
     p = nullptr;
 }
 
+// Pinned host staging of at least `bytes`, grown when needed and kept by the
+// context; null when pinned memory cannot be had.
+static void *stage(Ctx &c, size_t bytes)
+{
+    if (bytes > c.stage_cap) {
+        if (c.stage_h)
+            cudaFreeHost(c.stage_h);
+        c.stage_h = nullptr;
+        c.stage_cap = 0;
+        if (cudaMallocHost(&c.stage_h, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            c.stage_h = nullptr;
+            return nullptr;
+        }
+        c.stage_cap = bytes;
+    }
+    return c.stage_h;
+}
+
+// A host buffer for one exchange: the context's pinned staging, or an
+// aligned pageable buffer of its own when pinning failed.
+struct Staging {
+    hvec<dvec4> own;
+    char *p;
+    Staging(Ctx &c, size_t bytes)
+    {
+        p = (char *)stage(c, bytes);
+        if (!p) {
+            own.resize((bytes + sizeof(dvec4) - 1) / sizeof(dvec4));
+            p = (char *)own.data();
+        }
+    }
+};
+
 static void free_batch(Ctx &c)
 {
     BatchCg &b = c.bcg;
@@ -136,6 +170,8 @@ Ctx::~Ctx()
     }
     if (sc_host)
         cudaFreeHost(sc_host);
+    if (stage_h)
+        cudaFreeHost(stage_h);
     if (norms_host)
         cudaFreeHost(norms_host);
     if (status_host)
@@ -222,6 +258,7 @@ static void to_slot_major(const T *src, T *dst, int n, int k)
 template <typename T>
 static void from_slot_major(const T *src, T *dst, int n, int k)
 {
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < n; i++)
         for (int j = 0; j < k; j++)
             dst[(size_t)i * k + j] = src[(size_t)j * n + i];
@@ -230,21 +267,24 @@ static void from_slot_major(const T *src, T *dst, int n, int k)
 static int upload_particles(Ctx &c, dvec4 *dst, const double *src3)
 {
     LPM_CUDA(cudaStreamSynchronize(c.stream));
-    hvec<dvec4> t(c.n);
+    Staging sb(c, sizeof(dvec4) * (size_t)c.n);
+    dvec4 *t = (dvec4 *)sb.p;
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < c.n; i++)
         t[i] = make_dvec4(src3[3 * (size_t)i], src3[3 * (size_t)i + 1], src3[3 * (size_t)i + 2], 0.0);
-    LPM_CUDA(cudaMemcpy(dst, t.data(), sizeof(dvec4) * c.n, cudaMemcpyHostToDevice));
+    LPM_CUDA(cudaMemcpy(dst, t, sizeof(dvec4) * c.n, cudaMemcpyHostToDevice));
     return LPM_OK;
 }
 
 static int download_particles(Ctx &c, const dvec4 *src, double *dst3)
 {
-    std::vector<dvec4> t(c.n);
-    LPM_CUDA(cudaMemcpyAsync(t.data(), src, sizeof(dvec4) * c.n, cudaMemcpyDeviceToHost, c.stream));
+    Staging sb(c, sizeof(dvec4) * (size_t)c.n);
+    const dvec4 *t = (const dvec4 *)sb.p;
+    LPM_CUDA(cudaMemcpyAsync(sb.p, src, sizeof(dvec4) * c.n, cudaMemcpyDeviceToHost, c.stream));
     int rc = sync(c);
     if (rc)
         return rc;
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < c.n; i++) {
         dst3[3 * i] = t[i].x;
         dst3[3 * i + 1] = t[i].y;
@@ -1903,17 +1943,17 @@ int lpm_get(lpm_ctx *ctx, const char *name, void *dst, size_t bytes)
     auto bond_d = [&](const double *src) -> int {
         if (!need(nb * sizeof(double)))
             return fail(LPM_ERR_ARG, nm + ": buffer too small");
-        std::vector<double> t(nb);
-        LPM_CUDA(cudaMemcpy(t.data(), src, nb * sizeof(double), cudaMemcpyDeviceToHost));
-        from_slot_major(t.data(), (double *)dst, n, LPM_NN);
+        Staging sb(c, nb * sizeof(double));
+        LPM_CUDA(cudaMemcpy(sb.p, src, nb * sizeof(double), cudaMemcpyDeviceToHost));
+        from_slot_major((const double *)sb.p, (double *)dst, n, LPM_NN);
         return LPM_OK;
     };
     auto rows_d = [&](const double *src, int k) -> int {
         if (!need((size_t)k * n * sizeof(double)))
             return fail(LPM_ERR_ARG, nm + ": buffer too small");
-        std::vector<double> t((size_t)k * n);
-        LPM_CUDA(cudaMemcpy(t.data(), src, t.size() * sizeof(double), cudaMemcpyDeviceToHost));
-        from_slot_major(t.data(), (double *)dst, n, k);
+        Staging sb(c, (size_t)k * n * sizeof(double));
+        LPM_CUDA(cudaMemcpy(sb.p, src, (size_t)k * n * sizeof(double), cudaMemcpyDeviceToHost));
+        from_slot_major((const double *)sb.p, (double *)dst, n, k);
         return LPM_OK;
     };
     LPM_CUDA(cudaStreamSynchronize(c.stream));
@@ -2042,17 +2082,17 @@ int lpm_set(lpm_ctx *ctx, const char *name, const void *src, size_t bytes)
     auto bond_d = [&](double *d) -> int {
         if (bytes < nb * sizeof(double))
             return fail(LPM_ERR_ARG, nm + ": buffer too small");
-        std::vector<double> t(nb);
-        to_slot_major((const double *)src, t.data(), n, LPM_NN);
-        LPM_CUDA(cudaMemcpy(d, t.data(), nb * sizeof(double), cudaMemcpyHostToDevice));
+        Staging sb(c, nb * sizeof(double));
+        to_slot_major((const double *)src, (double *)sb.p, n, LPM_NN);
+        LPM_CUDA(cudaMemcpy(d, sb.p, nb * sizeof(double), cudaMemcpyHostToDevice));
         return LPM_OK;
     };
     auto rows_d = [&](double *d, int k) -> int {
         if (bytes < (size_t)k * n * sizeof(double))
             return fail(LPM_ERR_ARG, nm + ": buffer too small");
-        std::vector<double> t((size_t)k * n);
-        to_slot_major((const double *)src, t.data(), n, k);
-        LPM_CUDA(cudaMemcpy(d, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice));
+        Staging sb(c, (size_t)k * n * sizeof(double));
+        to_slot_major((const double *)src, (double *)sb.p, n, k);
+        LPM_CUDA(cudaMemcpy(d, sb.p, (size_t)k * n * sizeof(double), cudaMemcpyHostToDevice));
         return LPM_OK;
     };
     if (nm == "xyz") return particles(c.xyz);
@@ -2096,66 +2136,31 @@ int lpm_export_upper_csr(lpm_ctx *ctx, double *Kg, int *IK, int *JK, long long *
         return fail(LPM_ERR_ARG, "null context");
     Ctx &c = ctx->c;
     const HostSetup &h = c.hs;
-    const int n = c.n, w = 61;
+    const int n = c.n;
     if (h.kp1.empty())
         return fail(LPM_ERR_ARG, "export_upper_csr: this batch exceeds the reference's int32 CSR offsets");
     if (nnz)
         *nnz = h.kp1[n];
     if (!Kg && !IK && !JK)
         return LPM_OK;
-    std::vector<double> val;
-    if (Kg) {
-        if (!c.have_K)
-            return fail(LPM_ERR_ARG, "no stiffness assembled");
-        val.resize(9 * (size_t)c.nblk);
-        if (c.opts.precision == LPM_PREC_FP64) {
-            LPM_CUDA(cudaMemcpy(val.data(), c.Kd, val.size() * sizeof(double), cudaMemcpyDeviceToHost));
-        } else {
-            std::vector<float> vf(val.size());
-            LPM_CUDA(cudaMemcpy(vf.data(), c.Kf, vf.size() * sizeof(float), cudaMemcpyDeviceToHost));
-            for (size_t k = 0; k < vf.size(); k++)
-                val[k] = vf[k];
-        }
-    }
     // layout of calcStiffness3DFiniteDifference (src/stiffness.c:431-515)
-    for (int i = 0; i < n; i++) {
-        const int base = h.kp1[i], k0 = h.kp0[i], np = h.npad[i];
-        const long long off = h.rowoff[i];
-        int num1 = 0;
-        for (int jid = 0; jid < h.nconn[i]; jid++) {
-            const int jj = h.conn[(size_t)i * w + jid];
-            auto V = [&](int r, int q) { return val[9 * off + (size_t)(3 * r + q) * np + jid]; };
-            if (jj == i) {
-                const int pos[6] = {base, base + 1, base + 2, base + 3 * k0, base + 3 * k0 + 1, base + 6 * k0 - 1};
-                const int rq[6][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
-                const int col[6] = {3 * (jj + 1) - 2, 3 * (jj + 1) - 1, 3 * (jj + 1), 3 * (jj + 1) - 1,
-                                    3 * (jj + 1), 3 * (jj + 1)};
-                for (int k = 0; k < 6; k++) {
-                    if (Kg)
-                        Kg[pos[k]] = V(rq[k][0], rq[k][1]);
-                    if (JK)
-                        JK[pos[k]] = col[k];
-                }
-            } else if (jj > i) {
-                num1++;
-                const int rowstart[3] = {base + 3 * num1, base + 3 * k0 + 3 * num1 - 1, base + 6 * k0 + 3 * num1 - 3};
-                for (int r = 0; r < 3; r++)
-                    for (int q = 0; q < 3; q++) {
-                        if (Kg)
-                            Kg[rowstart[r] + q] = V(r, q);
-                        if (JK)
-                            JK[rowstart[r] + q] = 3 * (jj + 1) - 2 + q;
-                    }
-            }
-        }
-        if (IK) {
-            IK[3 * i] = base + 1;
-            IK[3 * i + 1] = base + 3 * k0 + 1;
-            IK[3 * i + 2] = base + 6 * k0;
-        }
+    if (!Kg) {
+        export_upper_csr_host<double>(h, nullptr, Kg, IK, JK);
+        return LPM_OK;
     }
-    if (IK)
-        IK[3 * n] = h.kp1[n] + 1;
+    if (!c.have_K)
+        return fail(LPM_ERR_ARG, "no stiffness assembled");
+    const size_t cnt = 9 * (size_t)c.nblk;
+    if (c.opts.precision == LPM_PREC_FP64) {
+        Staging sb(c, cnt * sizeof(double));
+        LPM_CUDA(cudaMemcpy(sb.p, c.Kd, cnt * sizeof(double), cudaMemcpyDeviceToHost));
+        export_upper_csr_host<double>(h, (const double *)sb.p, Kg, IK, JK);
+    } else {
+        // FP32 values, widened exactly to double as they are written out
+        Staging sb(c, cnt * sizeof(float));
+        LPM_CUDA(cudaMemcpy(sb.p, c.Kf, cnt * sizeof(float), cudaMemcpyDeviceToHost));
+        export_upper_csr_host<float>(h, (const float *)sb.p, Kg, IK, JK);
+    }
     return LPM_OK;
 }
 

@@ -103,6 +103,8 @@ int build_batch(HostSetup &dst, int lattice, double radius, int nspec, const dou
                 std::vector<int> &offsets);
 void kntv_per_particle(int lattice, double radius, const double *c11, const double *c12,
                        const double *c44, int n, double *knt);
+template <typename T>  // T = double (FP64 stiffness) or float (FP32 values, widened exactly)
+void export_upper_csr_host(const HostSetup &h, const T *val, double *Kg, int *IK, int *JK);
 
 // Device scalars used by the PCG (one 128-byte record).
 // done: 0 running, 1 converged (recursive residual), 2 iteration cap,
@@ -247,6 +249,11 @@ struct Ctx {
     bool time_this = false;  // the next SpMV launch carries the timing events
     bool vec64_fallback = false;  // mixed: FP32-vector PCG stagnated, use FP64 vectors
     double cg_rtol_now = 0.0;     // relative tolerance of the current solve (0: opts.cg_rtol)
+    // pinned host staging of lpm_get / lpm_set / lpm_export_upper_csr copies,
+    // allocated on first use and kept, so repeated exchanges of the same
+    // arrays neither reallocate nor page-fault host memory
+    void *stage_h = nullptr;
+    size_t stage_cap = 0;
     bool trace = false;           // LPM_TRACE set: one stderr line per Newton iteration and solve
     long long trace_step = 0;     // load steps run by this context (trace numbering)
     // batched specimens (lpm_setup_batch); nspec == 0 for a single specimen

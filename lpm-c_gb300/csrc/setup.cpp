@@ -438,6 +438,59 @@ int build_batch(HostSetup &dst, int lattice, double radius, int nspec, const dou
     return dst.n;
 }
 
+// The block-CSR values (component-major rows, see lpm_internal.h) written in
+// the reference's 1-based upper-triangular scalar CSR, the layout of
+// calcStiffness3DFiniteDifference (src/stiffness.c:431-515): per particle the
+// upper part of its diagonal block, then for every connected particle jj > i
+// the full 3x3 block, in three scalar rows.  Any output may be null.  Rows
+// write disjoint ranges, so particles are converted in parallel.
+template <typename T>
+void export_upper_csr_host(const HostSetup &h, const T *val, double *Kg, int *IK, int *JK)
+{
+    const int n = h.n, w = 61;
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int i = 0; i < n; i++) {
+        const int base = h.kp1[i], k0 = h.kp0[i], np = h.npad[i];
+        const long long off = h.rowoff[i];
+        int num1 = 0;
+        for (int jid = 0; jid < h.nconn[i]; jid++) {
+            const int jj = h.conn[(size_t)i * w + jid];
+            auto V = [&](int r, int q) { return (double)val[9 * off + (size_t)(3 * r + q) * np + jid]; };
+            if (jj == i) {
+                const int pos[6] = {base, base + 1, base + 2, base + 3 * k0, base + 3 * k0 + 1, base + 6 * k0 - 1};
+                const int rq[6][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
+                const int col[6] = {3 * (jj + 1) - 2, 3 * (jj + 1) - 1, 3 * (jj + 1), 3 * (jj + 1) - 1,
+                                    3 * (jj + 1), 3 * (jj + 1)};
+                for (int k = 0; k < 6; k++) {
+                    if (Kg)
+                        Kg[pos[k]] = V(rq[k][0], rq[k][1]);
+                    if (JK)
+                        JK[pos[k]] = col[k];
+                }
+            } else if (jj > i) {
+                num1++;
+                const int rowstart[3] = {base + 3 * num1, base + 3 * k0 + 3 * num1 - 1, base + 6 * k0 + 3 * num1 - 3};
+                for (int r = 0; r < 3; r++)
+                    for (int q = 0; q < 3; q++) {
+                        if (Kg)
+                            Kg[rowstart[r] + q] = V(r, q);
+                        if (JK)
+                            JK[rowstart[r] + q] = 3 * (jj + 1) - 2 + q;
+                    }
+            }
+        }
+        if (IK) {
+            IK[3 * i] = base + 1;
+            IK[3 * i + 1] = base + 3 * k0 + 1;
+            IK[3 * i + 2] = base + 6 * k0;
+        }
+    }
+    if (IK)
+        IK[3 * n] = h.kp1[n] + 1;
+}
+template void export_upper_csr_host<double>(const HostSetup &, const double *, double *, int *, int *);
+template void export_upper_csr_host<float>(const HostSetup &, const float *, double *, int *, int *);
+
 // calcKnTv's KnTve = radius * mapping * [C11, C12, C44] per particle
 // (src/stiffness.c:179-185 SC, :210-216 FCC), summed in the order of a
 // plain row-major matrix-vector product.
