@@ -398,6 +398,7 @@ void solverPARDISO(void) { solverCG(); }
 void switchStateV(int f)
 {
     const int from = f == 0 ? 1 : (f == 1 ? 0 : 2), to = f == 1 ? 1 : 0;
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < nparticle; i++) {
         for (int j = 0; j < nneighbors; j++) {
             dLp[i][j][to] = dLp[i][j][from];
