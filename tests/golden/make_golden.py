@@ -284,11 +284,50 @@ def setup_case(out, name):
     print(f"setup {name}: {n} particles", flush=True)
 
 
+def noise_case(out, tag="sc8_enoise"):
+    """Per-particle moduli (the C2 material model at small size): E = 200 GPa
+    (1 + 0.05 U[-1, 1]) per particle, seed 1, as unique reference types (one
+    Ce row per particle) with the usual types as BC groups; bond Kn/Tv are the
+    two end particles' averages (src/stiffness.c:186-200).  14 cyclic steps
+    into the plastic range."""
+    case = cases.SCCase(n=8, sigmay=150.0, e_noise=0.05, seed=1)
+    n = R.setup(case.lattice, case.radius, case.box)
+    nn = R.gint("nneighbors")
+    xyz0 = R.get_d2("xyz", n, 3)
+    groups = cases.sc_types(xyz0, R.get_i1("nb", n), case.radius)
+    u = cases.splitmix64_uniform(case.seed, n)
+    scale = 1.0 + case.e_noise * (2.0 * u - 1.0)
+    c11, c12, c44 = cases.iso_cubic(case.E, case.nu)
+    ce = np.stack([c11 * scale, c12 * scale, c44 * scale], axis=1)
+    R.set_types(np.arange(n, dtype=np.int32), n)
+    R.set_bc_groups(groups)
+    R.material(ce, 0, np.full(n, case.sigmay), 0.0, case.H)
+    R.init_state()
+    R.set_cg_tol(1e-20, 0.0)
+    arrs = dict(groups=groups, xyz=xyz0, Kn=R.get_d2("Kn", n, nn), Tv=R.get_d2("Tv", n, nn))
+    top = groups == cases.T_TOP
+    rec = {k: [] for k in ("iters", "nres", "disp_top")}
+    for s_, stp in enumerate(case.schedule[:14], start=1):
+        with R.quiet():
+            st = R.load_step(cases.sc_bcs(stp), [], case.newton_tol)
+        xyz = R.get_d2("xyz", n, 3)
+        rec["iters"].append(st[0])
+        rec["nres"].append(st[3])
+        rec["disp_top"].append((xyz[top, 2].sum() - xyz0[top, 2].sum()) / top.sum())
+    for k, v in rec.items():
+        arrs[k] = np.array(v)
+    arrs["s_xyz"] = R.get_d2("xyz", n, 3)
+    arrs["s_alpha"] = R.get_d2("J2_alpha", n, 3)[:, 1]
+    arrs["s_F"] = R.get_d2("F", n, nn)
+    np.savez_compressed(os.path.join(out, f"{tag}.npz"), **arrs)
+    print(f"{tag}: {n} particles, alpha max {arrs['s_alpha'].max():.3e}", flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--fcc-steps", type=int, default=12)
-    ap.add_argument("--only", choices=["sc", "fcc", "force", "ductile", "brittle"] +
+    ap.add_argument("--only", choices=["sc", "fcc", "force", "ductile", "brittle", "enoise"] +
                     ["setup_" + k for k in cases.SETUP_SHAPES], default=None)
     ap.add_argument("--out", default=HERE)
     args = ap.parse_args()
@@ -299,6 +338,8 @@ def main():
         fcc_case(args.out, args.fcc_steps)
     elif args.only == "force":
         force_case(args.out)
+    elif args.only == "enoise":
+        noise_case(args.out)
     elif args.only in ("ductile", "brittle"):
         damage_case(args.out, args.only)
     elif args.only and args.only.startswith("setup_"):
@@ -307,7 +348,8 @@ def main():
         sc_case(args.out, args.steps)
     else:
         import subprocess
-        for which in ["sc", "fcc", "force", "ductile", "brittle"] + ["setup_" + k for k in cases.SETUP_SHAPES]:
+        for which in ["sc", "fcc", "force", "ductile", "brittle", "enoise"] + \
+                ["setup_" + k for k in cases.SETUP_SHAPES]:
             subprocess.check_call([sys.executable, __file__, "--only", which, "--steps", str(args.steps),
                                    "--fcc-steps", str(args.fcc_steps), "--out", args.out])
 

@@ -198,3 +198,30 @@ def test_setup_shapes_bit_exact(gpu_lib, name):
     kp = s.get("K_pointer")
     assert np.array_equal(kp[:n, 0], g["K_pointer"][:n, 0])
     assert np.array_equal(kp[:, 1], g["K_pointer"][:, 1])
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_per_particle_moduli_match_oracle(oracle_mod, gpu_lib, precision):
+    """The C2 material model (E +-5 % per particle) at 8^3: bond Kn/Tv
+    bit-exact with the reference (tests/golden/sc8_enoise.npz), then 14 cyclic
+    steps into the plastic range within 1e-8 of the oracle, both sides
+    converged to 1e-10."""
+    from conftest import golden
+    case = cases.SCCase(n=8, sigmay=150.0, e_noise=0.05, seed=1, newton_tol=1e-10)
+    g = golden("sc8_enoise.npz")
+    s, types = sc_gpu(gpu_lib, case, precision=precision, newton_maxiter=300, cg_rtol=1e-10)
+    o, _ = sc_oracle(oracle_mod, case, threads=4)
+    n = o.n
+    assert np.array_equal(s.get("Kn"), g["Kn"]) and np.array_equal(s.get("Tv"), g["Tv"])
+    x0 = o.d("xyz_initial", (n, 3))
+    for k, stp in enumerate(case.schedule[:14]):
+        st = s.load_step(cases.sc_bcs(stp))
+        o.load_step(cases.sc_bcs(stp), [], 1e-10, 300, 1e-20, 0.0)
+        assert st["status"] == 0, (k + 1, st)
+        du_g = s.get("xyz") - x0
+        du_o = o.d("xyz", (n, 3)) - x0
+        err = np.abs(du_g - du_o).max() / np.abs(du_o).max()
+        assert err < 1e-8, (k + 1, err)
+    a_o = o.d("alpha1", (n,))
+    assert a_o.max() > 0.0
+    assert np.abs(s.get("J2_alpha") - a_o).max() <= 1e-8 * a_o.max()

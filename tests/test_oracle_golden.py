@@ -256,3 +256,28 @@ def test_setup_shapes_bit_exact(oracle_mod, name):
     kp = g["K_pointer"]
     assert np.array_equal(o.i("kp0", (n + 1,))[:n], kp[:n, 0])
     assert np.array_equal(o.i("kp1", (n + 1,)), kp[:, 1])
+
+
+def test_per_particle_moduli_bit_exact(oracle_mod):
+    """Per-particle E (the C2 material model at 8^3): bond Kn/Tv as the
+    averages of the two end particles (src/stiffness.c:186-200), then 14 cyclic
+    steps into the plastic range.  The reference ran with one type per particle
+    and the usual types as BC groups; the oracle takes per-particle moduli."""
+    case = cases.SCCase(n=8, sigmay=150.0, e_noise=0.05, seed=1)
+    g = golden("sc8_enoise.npz")
+    o, types = sc_oracle(oracle_mod, case, threads=1)
+    n, nn = o.n, o.nn
+    assert np.array_equal(types, g["groups"])
+    assert np.array_equal(o.d("Kn", (n, nn)), g["Kn"])
+    assert np.array_equal(o.d("Tv", (n, nn)), g["Tv"])
+    x0 = o.d("xyz_initial", (n, 3))
+    top = types == cases.T_TOP
+    for k, stp in enumerate(case.schedule[:14]):
+        st = o.load_step(cases.sc_bcs(stp), [], case.newton_tol, 100, 1e-20, 0.0)
+        assert st[0] == g["iters"][k] and st[3] == g["nres"][k], k
+        xyz = o.d("xyz", (n, 3))
+        assert (xyz[top, 2].sum() - x0[top, 2].sum()) / top.sum() == g["disp_top"][k], k
+    assert np.array_equal(o.d("xyz", (n, 3)), g["s_xyz"])
+    assert np.array_equal(o.d("alpha1", (n,)), g["s_alpha"])
+    assert np.array_equal(o.d("F", (n, nn)), g["s_F"])
+    assert g["s_alpha"].max() > 0.0
