@@ -35,9 +35,12 @@ def _oracle_after_steps(O, case, steps, plmode):
     return o
 
 
-def analytic_tangent(o):
+def analytic_tangent(o, damaged=False):
     """Full (both triangles) 3n x 3n tangent, restricted to each row's AFEM
-    connectivity like the reference's pattern."""
+    connectivity like the reference's pattern.  damaged: weigh bonds by
+    damage_broken as k_stiff.cu does with the damage stage on (broken bonds
+    leave the shell sums, their own terms and the two-hop terms through
+    them; a pair counts only when both directions are intact)."""
     n, nn = o.n, o.nn
     xyz = o.d("xyz", (n, 3))
     nbr = o.i("neighbors", (n, nn))
@@ -47,6 +50,7 @@ def analytic_tangent(o):
     Kn = o.d("Kn", (n, nn))
     Tv = o.d("Tv", (n, nn))
     dLp = o.d("dLp0", (n, nn))  # plastic bond stretch, state slot 0
+    brk = o.d("damage_broken", (n, nn)) if damaged else np.ones((n, nn))
     conn = o.i("conn", (n, o.L.lo_nconn_max(o.h)))
     nconn = o.i("nb_conn", (n,))
     dL = np.zeros((n, nn))
@@ -61,13 +65,13 @@ def analytic_tangent(o):
             p = nbr[i, j]
             e = xyz[i] - xyz[p]
             dis = np.sqrt(e @ e)
-            dL[i, j] = dis - L0[i, j] - dLp[i, j]
+            dL[i, j] = (dis - L0[i, j] - dLp[i, j]) * brk[i, j]
             c[i, j] = e / dis
             s = sh[i, j]
             S[i, s] += dL[i, j]
             T[i, s] += Tv[i, j] * dL[i, j]
-            U[i, s] += c[i, j]
-            W[i, s] += Tv[i, j] * c[i, j]
+            U[i, s] += brk[i, j] * c[i, j]
+            W[i, s] += brk[i, j] * Tv[i, j] * c[i, j]
             hits = np.nonzero(nbr[p, :nb[p]] == i)[0]
             if hits.size:
                 rev[i, j] = hits[-1]
@@ -77,6 +81,8 @@ def analytic_tangent(o):
         kii = np.zeros((3, 3))
         for j in range(nb[i]):
             p, s, cc = nbr[i, j], sh[i, j], c[i, j]
+            if brk[i, j] * (brk[p, rev[i, j]] if rev[i, j] >= 0 else 1.0) == 0.0:
+                continue
             d = np.linalg.norm(xyz[i] - xyz[p])
             kn, tv = Kn[i, j], Tv[i, j]
             tsum, ssum = T[i, s] + T[p, s], S[i, s] + S[p, s]
@@ -91,7 +97,7 @@ def analytic_tangent(o):
                 K[3 * i:3 * i + 3, 3 * p:3 * p + 3] += (-fbar / d * proj - 2 * kn * np.outer(cc, cc)
                                                         + np.outer(cc, b) - np.outer(a, cc))
             for m in range(nb[p]):
-                if sh[p, m] != s:
+                if sh[p, m] != s or brk[p, m] == 0.0:
                     continue
                 q = nbr[p, m]
                 blk = -0.5 * (Tv[p, m] + tv) * np.outer(cc, c[p, m])
@@ -131,3 +137,26 @@ def test_analytic_tangent_matches_reference_fd(oracle_mod, lattice):
     o2 = _oracle_after_steps(oracle_mod, case, 0, plmode)
     o2.fd_stiffness()
     assert np.linalg.norm(o2.d("K_global", (nnz,)) - Kfd) > 100 * rel * np.linalg.norm(Kfd)
+
+
+@pytest.mark.parametrize("which,steps", [("ductile", 6), ("brittle", 6)])
+def test_damaged_tangent_matches_reference_fd(oracle_mod, which, steps):
+    """With broken bonds (the damage stage of the reference's main, restated by
+    the oracle): the tangent with the broken-bond weights against the FD
+    stiffness of the damaged state, and the undamaged formula far from it."""
+    from test_oracle_damage import _brittle, _ductile
+    o, _, step_bcs, tol = (_ductile if which == "ductile" else _brittle)(oracle_mod)
+    for bcs in step_bcs[:steps]:
+        o.load_step_damage(bcs, [], tol, 200, 1e-20, 0.0, 50)
+    n = o.n
+    assert (o.d("damage_broken", (n, o.nn)) == 0.0).sum() > 0
+    o.fd_stiffness()
+    nnz = o.nnz
+    IK = o.i("IK", (3 * n + 1,)) - 1
+    JK = o.i("JK", (nnz,)) - 1
+    Kfd = o.d("K_global", (nnz,))
+    rows = np.repeat(np.arange(3 * n), np.diff(IK))
+    rel = np.linalg.norm(analytic_tangent(o, damaged=True)[rows, JK] - Kfd) / np.linalg.norm(Kfd)
+    rel0 = np.linalg.norm(analytic_tangent(o)[rows, JK] - Kfd) / np.linalg.norm(Kfd)
+    assert rel < 1e-5, rel
+    assert rel0 > 1e-2, rel0
