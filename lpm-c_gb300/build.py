@@ -37,7 +37,8 @@ CU_UNITS = [
     ("k_noalloc.cu", []),
     ("k_damage.cu", ["-fmad=false"]),
 ]
-CPP_UNITS = [("setup.cpp", ["-ffp-contract=off", "-fopenmp"]), ("output.cpp", ["-ffp-contract=off"])]
+CPP_UNITS = [("setup.cpp", ["-ffp-contract=off", "-fopenmp"]), ("output.cpp", ["-ffp-contract=off"]),
+             ("amg_setup.cpp", ["-fopenmp"])]
 LEGACY_UNITS = [("legacy.cpp", ["-fopenmp"])]
 
 

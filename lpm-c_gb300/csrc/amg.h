@@ -1,0 +1,59 @@
+// Smoothed-aggregation multigrid hierarchy for the stiffness, built on the
+// host (amg_setup.cpp).  Plain C++ (no CUDA types), so that it can be built
+// and checked without a GPU.
+#pragma once
+#include <cstdint>
+#include <vector>
+
+namespace lpm {
+
+// scalar CSR, 0-based
+struct Csr {
+    int nrow = 0, ncol = 0;
+    std::vector<long long> ptr;
+    std::vector<int> col;
+    std::vector<double> val;
+};
+
+struct AmgLevel {
+    int nblock = 0;            // block rows: particles on level 0, aggregates above
+    int bs = 0;                // DOFs per block row: 3 on level 0, 6 above
+    Csr A;                     // operator of the level (constrained level-0 DOFs removed)
+    std::vector<double> Dinv;  // inverse of each bs x bs diagonal block
+    double omega = 1.0;        // smoother damping, 1 / rho(D^-1 A)
+    Csr P, Pt;                 // prolongation from the next level and its transpose
+};
+
+struct AmgHierarchy {
+    std::vector<AmgLevel> levels;     // finest first; the coarsest operator is coarse_A
+    Csr coarse_A;
+    int coarse_n = 0;
+    std::vector<double> coarse_chol;  // dense lower Cholesky factor of coarse_A, row-major
+};
+
+// The stiffness in the device's block-CSR layout: block row i holds npad[i]
+// blocks (nconn[i] real ones, then padding) at rowoff[i]; value (r, c) of
+// block b is val[9 * rowoff[i] + (3 r + c) * npad[i] + b]; mask bit d of
+// particle i set = DOF d free.
+struct AmgInput {
+    int n = 0;
+    const double *xyz = nullptr;      // initial positions, n x 3
+    const uint8_t *mask = nullptr;
+    const long long *rowoff = nullptr;
+    const int *npad = nullptr;
+    const int *nconn = nullptr;
+    const int *cols = nullptr;
+    const double *val = nullptr;
+};
+
+struct AmgOptions {
+    double agg_spacing = 0.6;  // edge of a level-0 aggregate box (3 SC spacings at radius 0.1)
+    int max_levels = 8;
+    int coarse_blocks = 150;   // stop coarsening at this many block rows
+};
+
+// Returns the number of levels above the coarsest, or -1 when the coarsest
+// operator is not positive definite.
+int amg_build(const AmgInput &in, AmgHierarchy &H, const AmgOptions &opt = AmgOptions());
+
+}  // namespace lpm

@@ -1,0 +1,85 @@
+// Test helper: runs lpm::amg_build on a stiffness given in the device
+// block-CSR layout (binary files in a directory) and writes the hierarchy
+// back as binary files, for tests/test_amg_setup.py.
+//   amg_harness DIR AGG_SPACING
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+#include <vector>
+#include "amg.h"
+
+template <typename T>
+static std::vector<T> rd(const std::string &path, size_t count)
+{
+    std::vector<T> v(count);
+    FILE *f = std::fopen(path.c_str(), "rb");
+    if (!f || std::fread(v.data(), sizeof(T), count, f) != count) {
+        std::fprintf(stderr, "cannot read %s\n", path.c_str());
+        std::exit(2);
+    }
+    std::fclose(f);
+    return v;
+}
+
+template <typename T>
+static void wr(const std::string &path, const std::vector<T> &v)
+{
+    FILE *f = std::fopen(path.c_str(), "wb");
+    std::fwrite(v.data(), sizeof(T), v.size(), f);
+    std::fclose(f);
+}
+
+static void wr_csr(const std::string &p, const lpm::Csr &A)
+{
+    wr(p + "_ptr.bin", A.ptr);
+    wr(p + "_col.bin", A.col);
+    wr(p + "_val.bin", A.val);
+}
+
+int main(int argc, char **argv)
+{
+    if (argc < 3)
+        return 2;
+    const std::string d(argv[1]);
+    int n = 0;
+    {
+        FILE *f = std::fopen((d + "/n.txt").c_str(), "r");
+        if (!f || std::fscanf(f, "%d", &n) != 1)
+            return 2;
+        std::fclose(f);
+    }
+    auto xyz = rd<double>(d + "/xyz.bin", 3 * (size_t)n);
+    auto mask = rd<uint8_t>(d + "/mask.bin", n);
+    auto rowoff = rd<long long>(d + "/rowoff.bin", (size_t)n + 1);
+    auto npad = rd<int>(d + "/npad.bin", n);
+    auto nconn = rd<int>(d + "/nconn.bin", n);
+    auto cols = rd<int>(d + "/cols.bin", (size_t)rowoff[n]);
+    auto val = rd<double>(d + "/val.bin", 9 * (size_t)rowoff[n]);
+    lpm::AmgInput in;
+    in.n = n;
+    in.xyz = xyz.data();
+    in.mask = mask.data();
+    in.rowoff = rowoff.data();
+    in.npad = npad.data();
+    in.nconn = nconn.data();
+    in.cols = cols.data();
+    in.val = val.data();
+    lpm::AmgOptions opt;
+    opt.agg_spacing = std::atof(argv[2]);
+    lpm::AmgHierarchy H;
+    const int L = lpm::amg_build(in, H, opt);
+    FILE *f = std::fopen((d + "/levels.txt").c_str(), "w");
+    std::fprintf(f, "%d %d\n", L, H.coarse_n);
+    for (size_t l = 0; l < H.levels.size(); l++) {
+        const lpm::AmgLevel &lv = H.levels[l];
+        std::fprintf(f, "%d %d %.17g %d %d\n", lv.nblock, lv.bs, lv.omega, lv.P.nrow, lv.P.ncol);
+        const std::string p = d + "/L" + std::to_string(l);
+        wr_csr(p + "_A", lv.A);
+        wr_csr(p + "_P", lv.P);
+        wr_csr(p + "_Pt", lv.Pt);
+        wr(p + "_Dinv.bin", lv.Dinv);
+    }
+    std::fclose(f);
+    wr(d + "/coarse_chol.bin", H.coarse_chol);
+    return L >= 0 ? 0 : 1;
+}

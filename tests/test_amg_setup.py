@@ -1,0 +1,161 @@
+"""The host-side smoothed-aggregation hierarchy (lpm-c_gb300/csrc/amg_setup.cpp)
+on the CPU: built from the oracle's stiffness (the reference's FD matrix with
+the boundary conditions of a load step) in the device block-CSR layout, then
+used as the preconditioner of a CG in numpy (V-cycle: two damped
+block-Jacobi sweeps before and after, Galerkin coarse operators, dense
+Cholesky on the coarsest level).  It must converge to 1e-10 in a small,
+size-independent number of iterations where block-Jacobi PCG needs hundreds.
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+import scipy.linalg as sla
+import scipy.sparse as sp
+
+import cases
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CSRC = os.path.join(ROOT, "lpm-c_gb300", "csrc")
+
+
+@pytest.fixture(scope="module")
+def harness(tmp_path_factory):
+    exe = str(tmp_path_factory.mktemp("amg") / "amg_harness")
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-fopenmp", "-I", CSRC, "-o", exe,
+                           os.path.join(ROOT, "tests", "amg_harness.cpp"), os.path.join(CSRC, "amg_setup.cpp")])
+    return exe
+
+
+def _system(O, lattice, size):
+    o = O.Oracle()
+    if lattice == 2:
+        case = cases.SCCase(n=size)
+        n = o.setup_lattice(case.lattice, case.radius, case.box)
+        o.set_types(cases.sc_types(o.d("xyz", (n, 3)), o.i("nb", (n,)), case.radius))
+        c11, c12, c44 = cases.iso_cubic(case.E, case.nu)
+        o.set_material(c11, c12, c44, case.sigmay, case.H, 0.0, 0)
+    else:
+        case = cases.FCCCase(ncell=size)
+        n = o.setup_lattice(case.lattice, case.radius, case.box)
+        o.set_types(cases.sc_types(o.d("xyz", (n, 3)), o.i("nb", (n,)), case.radius))
+        o.set_cp(*case.cp)
+        o.set_material(case.C11, case.C12, case.C44, 0.0, 0.0, 0.0, 1)
+    o.init_state()
+    o.load_step(cases.sc_bcs(case.schedule[0]), [], 1e30, maxiter=0)  # BCs, predictor, stiffness
+    nnz = o.nnz
+    IK = o.i("IK", (3 * n + 1,)) - 1
+    JK = o.i("JK", (nnz,)) - 1
+    U = sp.csr_matrix((o.d("K_global", (nnz,)), JK, IK), shape=(3 * n, 3 * n))
+    K = (U + sp.triu(U, 1).T).tocsr()
+    dofmask = o.i("dispBC_index", (3 * n,)).reshape(n, 3)
+    mask = (dofmask[:, 0] | (dofmask[:, 1] << 1) | (dofmask[:, 2] << 2)).astype(np.uint8)
+    w = o.L.lo_nconn_max(o.h)
+    conn, nconn = o.i("conn", (n, w)), o.i("nb_conn", (n,))
+    return o, K, o.d("residual", (3 * n,)), o.d("xyz", (n, 3)), mask, conn, nconn
+
+
+def _device_layout(K, conn, nconn):
+    """Block-CSR as on the device: rows padded to 4 blocks with column i,
+    values component-major per row."""
+    n = len(nconn)
+    npad = (nconn + 3) & ~3
+    rowoff = np.zeros(n + 1, dtype=np.int64)
+    rowoff[1:] = np.cumsum(npad)
+    cols = np.repeat(np.arange(n, dtype=np.int32), npad)
+    val = np.zeros(9 * rowoff[-1])
+    I = np.repeat(np.arange(n), nconn)
+    B = np.arange(len(I)) - np.repeat(np.cumsum(nconn) - nconn, nconn)
+    J = conn[I, B]
+    cols[rowoff[I] + B] = J
+    for r in range(3):
+        for c in range(3):
+            val[9 * rowoff[I] + (3 * r + c) * npad[I] + B] = np.asarray(K[3 * I + r, 3 * J + c]).ravel()
+    return rowoff, npad.astype(np.int32), cols, val
+
+
+def _load_hierarchy(d):
+    lines = open(os.path.join(d, "levels.txt")).read().split("\n")
+    L, nc = map(int, lines[0].split())
+    levels = []
+    rd = lambda name, dt: np.fromfile(os.path.join(d, name), dtype=dt)  # noqa: E731
+    for lev in range(L):
+        nblock, bs, omega, prow, pcol = lines[1 + lev].split()
+        nblock, bs, omega, prow, pcol = int(nblock), int(bs), float(omega), int(prow), int(pcol)
+
+        def csr(p, shape):
+            return sp.csr_matrix((rd(f"{p}_val.bin", np.float64), rd(f"{p}_col.bin", np.int32),
+                                  rd(f"{p}_ptr.bin", np.int64)), shape=shape)
+        nd = nblock * bs
+        levels.append(dict(A=csr(f"L{lev}_A", (nd, nd)), P=csr(f"L{lev}_P", (prow, pcol)),
+                           Pt=csr(f"L{lev}_Pt", (pcol, prow)), bs=bs, omega=omega,
+                           Dinv=rd(f"L{lev}_Dinv.bin", np.float64).reshape(nblock, bs, bs)))
+    chol = rd("coarse_chol.bin", np.float64).reshape(nc, nc)
+    return levels, chol
+
+
+def _vcycle(levels, chol):
+    def smooth(lv, x, b):
+        r = (b - lv["A"] @ x).reshape(-1, lv["bs"])
+        return x + lv["omega"] * np.einsum("nij,nj->ni", lv["Dinv"], r).ravel()
+
+    def V(l, b):
+        if l == len(levels):
+            return sla.cho_solve((chol, True), b)
+        lv = levels[l]
+        x = smooth(lv, np.zeros_like(b), b)
+        x = smooth(lv, x, b)
+        x = x + lv["P"] @ V(l + 1, lv["Pt"] @ (b - lv["A"] @ x))
+        x = smooth(lv, x, b)
+        return smooth(lv, x, b)
+    return lambda r: V(0, r)
+
+
+def _pcg(A, M, b, rtol=1e-10, maxit=5000):
+    x = np.zeros_like(b)
+    r = b.copy()
+    z = M(r)
+    p = z.copy()
+    rz = r @ z
+    bn = np.linalg.norm(b)
+    for it in range(maxit):
+        q = A @ p
+        al = rz / (p @ q)
+        x += al * p
+        r -= al * q
+        if np.linalg.norm(r) <= rtol * bn:
+            return x, it + 1
+        z = M(r)
+        rz_old, rz = rz, r @ z
+        p = z + (rz / rz_old) * p
+    return x, maxit
+
+
+@pytest.mark.parametrize("lattice,size", [(2, 10), (2, 16), (3, 6)])
+def test_hierarchy_preconditions_cg(oracle_mod, harness, tmp_path, lattice, size):
+    o, K, res, xyz, mask, conn, nconn = _system(oracle_mod, lattice, size)
+    n = len(nconn)
+    rowoff, npad, cols, val = _device_layout(K, conn, nconn)
+    d = str(tmp_path)
+    open(os.path.join(d, "n.txt"), "w").write(str(n))
+    for name, arr in (("xyz", xyz), ("mask", mask), ("rowoff", rowoff), ("npad", npad),
+                      ("nconn", nconn.astype(np.int32)), ("cols", cols), ("val", val)):
+        np.ascontiguousarray(arr).tofile(os.path.join(d, f"{name}.bin"))
+    subprocess.check_call([harness, d, "0.6"])
+    levels, chol = _load_hierarchy(d)
+    assert len(levels) >= 1
+    # the level-0 operator is the stiffness with the constrained DOFs removed
+    free = np.repeat(mask[:, None], 3, axis=1) >> np.arange(3) & 1
+    free = free.ravel().astype(bool)
+    A0 = levels[0]["A"]
+    Kf = K[free][:, free]
+    assert abs(A0[free][:, free] - Kf).max() == 0.0
+    assert A0[~free].nnz == 0 or abs(A0[~free]).max() == 0.0
+    b = res * free
+    x, it = _pcg(A0, _vcycle(levels, chol), b)
+    assert np.linalg.norm(Kf @ x[free] - b[free]) <= 1e-10 * np.linalg.norm(b)
+    # block-Jacobi PCG on the same system for reference
+    dinv = levels[0]["Dinv"]
+    _, it_bj = _pcg(A0, lambda r: np.einsum("nij,nj->ni", dinv, r.reshape(-1, 3)).ravel(), b)
+    assert it <= 30 and it * 5 < it_bj, (it, it_bj)
