@@ -38,7 +38,7 @@ CU_UNITS = [
     ("k_damage.cu", ["-fmad=false"]),
 ]
 CPP_UNITS = [("setup.cpp", ["-ffp-contract=off", "-fopenmp"]), ("output.cpp", ["-ffp-contract=off"]),
-             ("amg_setup.cpp", ["-fopenmp"])]
+             ("amg_setup.cpp", ["-O3", "-fopenmp"])]
 LEGACY_UNITS = [("legacy.cpp", ["-fopenmp"])]
 
 

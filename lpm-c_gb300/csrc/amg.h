@@ -7,9 +7,10 @@
 
 namespace lpm {
 
-// scalar CSR, 0-based
-struct Csr {
-    int nrow = 0, ncol = 0;
+// Block-CSR with R x C blocks, 0-based; block k is val[k*R*C ...], row-major.
+struct Bsr {
+    int nbr = 0, nbc = 0;  // block rows, block columns
+    int R = 0, C = 0;
     std::vector<long long> ptr;
     std::vector<int> col;
     std::vector<double> val;
@@ -18,23 +19,26 @@ struct Csr {
 struct AmgLevel {
     int nblock = 0;            // block rows: particles on level 0, aggregates above
     int bs = 0;                // DOFs per block row: 3 on level 0, 6 above
-    Csr A;                     // operator of the level (constrained level-0 DOFs removed)
-    std::vector<double> Dinv;  // inverse of each bs x bs diagonal block
+    Bsr A;                     // operator of the level; empty on level 0 (the stiffness itself)
+    std::vector<double> Dinv;  // inverse of each bs x bs diagonal block, row-major
     double omega = 1.0;        // smoother damping, 1 / rho(D^-1 A)
-    Csr P, Pt;                 // prolongation from the next level and its transpose
+    Bsr P;                     // prolongation from the next level: bs x 6 blocks
+    Bsr Pt;                    // its transpose (restriction): 6 x bs blocks
 };
 
 struct AmgHierarchy {
     std::vector<AmgLevel> levels;     // finest first; the coarsest operator is coarse_A
-    Csr coarse_A;
-    int coarse_n = 0;
+    Bsr coarse_A;                     // 6 x 6 blocks
+    int coarse_n = 0;                 // scalar size of the coarsest operator
     std::vector<double> coarse_chol;  // dense lower Cholesky factor of coarse_A, row-major
+    std::vector<double> coarse_inv;   // its dense inverse, row-major
 };
 
 // The stiffness in the device's block-CSR layout: block row i holds npad[i]
 // blocks (nconn[i] real ones, then padding) at rowoff[i]; value (r, c) of
 // block b is val[9 * rowoff[i] + (3 r + c) * npad[i] + b]; mask bit d of
-// particle i set = DOF d free.
+// particle i set = DOF d free.  Constrained DOFs are removed (their rows and
+// columns treated as zero).
 struct AmgInput {
     int n = 0;
     const double *xyz = nullptr;      // initial positions, n x 3
@@ -50,6 +54,7 @@ struct AmgOptions {
     double agg_spacing = 0.6;  // edge of a level-0 aggregate box (3 SC spacings at radius 0.1)
     int max_levels = 8;
     int coarse_blocks = 150;   // stop coarsening at this many block rows
+    int power_iters = 15;      // power iterations for rho(D^-1 A)
 };
 
 // Returns the number of levels above the coarsest, or -1 when the coarsest

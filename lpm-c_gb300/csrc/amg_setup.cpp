@@ -1,22 +1,26 @@
 // Host-side build of a smoothed-aggregation multigrid hierarchy for the
-// stiffness (the preconditioner planned to replace block-Jacobi in the PCG).
+// stiffness (the multigrid preconditioner of the PCG, k_amg.cu).
 //
-// Level 0 is the stiffness itself, given in the device block-CSR layout
-// (rows padded to a multiple of 4 blocks, values component-major per row),
-// with the boundary-condition mask (bit d of mask[i] set = DOF d free).
+// Level 0 is the stiffness itself, read in place from the device block-CSR
+// layout (rows padded to a multiple of 4 blocks, values component-major per
+// row) with the boundary-condition mask (bit d of mask[i] set = DOF d free);
+// constrained DOFs are removed, i.e. their rows and columns count as zero.
 // Aggregates are boxes of 3 x 3 x 3 lattice spacings of the initial
 // positions; above level 0, boxes of 3 x 3 x 3 aggregates of the level
-// below.  The tentative prolongator of an aggregate spans the six rigid-body
-// modes of its free DOFs (translations, rotations about the aggregate's
-// centroid), orthonormalised by Householder QR, whose R becomes the
-// near-nullspace of the next level; rank-deficient columns stay zero and the
-// next level decouples them with a unit diagonal.  The prolongator is smoothed
-// by one damped block-Jacobi step, P = (I - 4/3 D^-1 A / rho(D^-1 A)) T, and
-// the coarse operator is the Galerkin product P^T A P.  The coarsest level is
-// factored densely (Cholesky).
+// below.  The tentative prolongator T of an aggregate spans the six
+// rigid-body modes of its free DOFs (translations, rotations about the
+// aggregate's centroid), orthonormalised by Householder QR, whose R becomes
+// the near-nullspace of the next level; rank-deficient columns stay zero and
+// the next level decouples them with a unit diagonal.  The prolongator is
+// smoothed by one damped block-Jacobi step, P = (I - 4/3 D^-1 A / rho) T with
+// rho = rho(D^-1 A) from power iteration, and the coarse operator is the
+// Galerkin product P^T (A P).  The coarsest level is factored densely.
 //
-// Matrices are kept as scalar CSR (double) during the build; the sparse
-// products run row-parallel with a dense accumulator per thread.
+// Everything is kept in blocks (3 x 3 and 3 x 6 on level 0, 6 x 6 above), so
+// the products are small dense block products with compile-time sizes; rows
+// run in parallel with per-thread column markers, and every output is laid
+// out by a counting pass first, so the result does not depend on the thread
+// count.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -29,202 +33,110 @@ namespace lpm {
 
 namespace {
 
-// C = A * B (scalar CSR), rows in parallel: a symbolic pass counts each
-// row's distinct columns, a numeric pass fills them in ascending order.
-Csr spgemm(const Csr &A, const Csr &B)
+// Operator with BS x BS blocks in block-CSR.
+template <int NB>
+struct OpB {
+    const Bsr &A;
+    static constexpr int BS = NB;
+    int nbr() const { return A.nbr; }
+    template <typename F>
+    void row(int I, F f) const
+    {
+        for (long long k = A.ptr[I]; k < A.ptr[I + 1]; k++)
+            f(A.col[k], &A.val[(size_t)k * NB * NB]);
+    }
+};
+
+// The level-0 operator: the stiffness of the device layout with the
+// constrained rows and columns zeroed, as 3 x 3 row-major blocks without the
+// padding.
+Bsr level0(const AmgInput &in)
 {
-    Csr C;
-    C.nrow = A.nrow;
-    C.ncol = B.ncol;
-    C.ptr.assign((size_t)A.nrow + 1, 0);
-    const int nt = omp_get_max_threads();
-    std::vector<std::vector<int>> mark(nt, std::vector<int>(B.ncol, -1));
+    const int n = in.n;
+    Bsr A;
+    A.nbr = A.nbc = n;
+    A.R = A.C = 3;
+    A.ptr.assign((size_t)n + 1, 0);
+    for (int i = 0; i < n; i++)
+        A.ptr[i + 1] = A.ptr[i] + in.nconn[i];
+    A.col.resize((size_t)A.ptr[n]);
+    A.val.resize((size_t)A.ptr[n] * 9);
 #pragma omp parallel for schedule(dynamic, 256)
-    for (int i = 0; i < A.nrow; i++) {
-        std::vector<int> &mk = mark[omp_get_thread_num()];
-        long long cnt = 0;
-        for (long long a = A.ptr[i]; a < A.ptr[i + 1]; a++) {
-            const int k = A.col[a];
-            for (long long b = B.ptr[k]; b < B.ptr[k + 1]; b++) {
-                const int j = B.col[b];
-                if (mk[j] != i) {
-                    mk[j] = i;
-                    cnt++;
-                }
-            }
+    for (int i = 0; i < n; i++) {
+        const long long off = in.rowoff[i];
+        const int np = in.npad[i], nc = in.nconn[i];
+        const unsigned mi = in.mask[i];
+        const double *v = in.val + 9 * off;
+        for (int b = 0; b < nc; b++) {
+            const long long k = A.ptr[i] + b;
+            const int j = in.cols[off + b];
+            const unsigned mj = in.mask[j];
+            A.col[k] = j;
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++)
+                    A.val[(size_t)k * 9 + 3 * r + c] =
+                        (((mi >> r) & (mj >> c)) & 1u) ? v[(size_t)(3 * r + c) * np + b] : 0.0;
         }
-        C.ptr[i + 1] = cnt;
     }
-    for (int i = 0; i < A.nrow; i++)
-        C.ptr[i + 1] += C.ptr[i];
-    C.col.resize((size_t)C.ptr[A.nrow]);
-    C.val.resize((size_t)C.ptr[A.nrow]);
-    std::vector<std::vector<double>> acc(nt, std::vector<double>(B.ncol, 0.0));
-    for (auto &m : mark)
-        std::fill(m.begin(), m.end(), -1);
-#pragma omp parallel for schedule(dynamic, 256)
-    for (int i = 0; i < A.nrow; i++) {
-        const int t = omp_get_thread_num();
-        std::vector<int> &mk = mark[t];
-        std::vector<double> &ac = acc[t];
-        long long p = C.ptr[i];
-        for (long long a = A.ptr[i]; a < A.ptr[i + 1]; a++) {
-            const int k = A.col[a];
-            const double av = A.val[a];
-            for (long long b = B.ptr[k]; b < B.ptr[k + 1]; b++) {
-                const int j = B.col[b];
-                if (mk[j] != i) {
-                    mk[j] = i;
-                    C.col[p++] = j;
-                    ac[j] = 0.0;
-                }
-                ac[j] += av * B.val[b];
-            }
-        }
-        const long long p0 = C.ptr[i];
-        std::sort(C.col.begin() + p0, C.col.begin() + p);
-        for (long long q = p0; q < p; q++)
-            C.val[q] = ac[C.col[q]];
-    }
-    return C;
+    return A;
 }
 
-Csr transpose(const Csr &A)
+// inverse of an n x n matrix (Gauss-Jordan, partial pivoting); rows and
+// columns that are entirely zero are decoupled with a unit diagonal
+template <int N>
+void invert_block(const double *in, double *out)
 {
-    Csr T;
-    T.nrow = A.ncol;
-    T.ncol = A.nrow;
-    T.ptr.assign((size_t)A.ncol + 1, 0);
-    for (long long a = 0; a < A.ptr[A.nrow]; a++)
-        T.ptr[A.col[a] + 1]++;
-    for (int j = 0; j < A.ncol; j++)
-        T.ptr[j + 1] += T.ptr[j];
-    T.col.resize((size_t)T.ptr[A.ncol]);
-    T.val.resize((size_t)T.ptr[A.ncol]);
-    std::vector<long long> fill(T.ptr.begin(), T.ptr.end() - 1);
-    for (int i = 0; i < A.nrow; i++)
-        for (long long a = A.ptr[i]; a < A.ptr[i + 1]; a++) {
-            const long long q = fill[A.col[a]]++;
-            T.col[q] = i;
-            T.val[q] = A.val[a];
-        }
-    return T;
-}
-
-// y = A x
-void spmv(const Csr &A, const std::vector<double> &x, std::vector<double> &y)
-{
-    y.assign(A.nrow, 0.0);
-#pragma omp parallel for schedule(static)
-    for (int i = 0; i < A.nrow; i++) {
-        double s = 0.0;
-        for (long long a = A.ptr[i]; a < A.ptr[i + 1]; a++)
-            s += A.val[a] * x[A.col[a]];
-        y[i] = s;
+    double m[N * N], inv[N * N];
+    std::memcpy(m, in, sizeof(m));
+    for (int r = 0; r < N; r++)
+        for (int c = 0; c < N; c++)
+            inv[r * N + c] = r == c ? 1.0 : 0.0;
+    for (int r = 0; r < N; r++) {
+        bool zero = true;
+        for (int c = 0; c < N; c++)
+            zero = zero && m[r * N + c] == 0.0 && m[c * N + r] == 0.0;
+        if (zero)
+            m[r * N + r] = 1.0;
     }
-}
-
-// Inverse of each bs x bs diagonal block (Gauss-Jordan with partial
-// pivoting); a block row with a zero row/column is decoupled: its inverse
-// has a unit diagonal there.
-std::vector<double> block_diag_inverse(const Csr &A, int bs)
-{
-    const int nb = A.nrow / bs;
-    std::vector<double> out((size_t)nb * bs * bs, 0.0);
-#pragma omp parallel for schedule(static)
-    for (int I = 0; I < nb; I++) {
-        double m[36], inv[36];
-        for (int r = 0; r < bs; r++)
-            for (int c = 0; c < bs; c++) {
-                m[r * bs + c] = 0.0;
-                inv[r * bs + c] = r == c ? 1.0 : 0.0;
+    for (int k = 0; k < N; k++) {
+        int piv = k;
+        for (int r = k + 1; r < N; r++)
+            if (std::fabs(m[r * N + k]) > std::fabs(m[piv * N + k]))
+                piv = r;
+        if (piv != k)
+            for (int c = 0; c < N; c++) {
+                std::swap(m[k * N + c], m[piv * N + c]);
+                std::swap(inv[k * N + c], inv[piv * N + c]);
             }
-        for (int r = 0; r < bs; r++) {
-            const int row = I * bs + r;
-            for (long long a = A.ptr[row]; a < A.ptr[row + 1]; a++) {
-                const int c = A.col[a] - I * bs;
-                if (c >= 0 && c < bs)
-                    m[r * bs + c] = A.val[a];
+        const double d = m[k * N + k];
+        const double id = d != 0.0 ? 1.0 / d : 0.0;
+        for (int c = 0; c < N; c++) {
+            m[k * N + c] *= id;
+            inv[k * N + c] *= id;
+        }
+        for (int r = 0; r < N; r++)
+            if (r != k) {
+                const double f = m[r * N + k];
+                if (f != 0.0)
+                    for (int c = 0; c < N; c++) {
+                        m[r * N + c] -= f * m[k * N + c];
+                        inv[r * N + c] -= f * inv[k * N + c];
+                    }
             }
-        }
-        // decouple empty rows
-        for (int r = 0; r < bs; r++) {
-            bool zero = true;
-            for (int c = 0; c < bs; c++)
-                zero = zero && m[r * bs + c] == 0.0 && m[c * bs + r] == 0.0;
-            if (zero)
-                m[r * bs + r] = 1.0;
-        }
-        for (int k = 0; k < bs; k++) {
-            int piv = k;
-            for (int r = k + 1; r < bs; r++)
-                if (std::fabs(m[r * bs + k]) > std::fabs(m[piv * bs + k]))
-                    piv = r;
-            if (piv != k)
-                for (int c = 0; c < bs; c++) {
-                    std::swap(m[k * bs + c], m[piv * bs + c]);
-                    std::swap(inv[k * bs + c], inv[piv * bs + c]);
-                }
-            const double d = m[k * bs + k];
-            const double id = d != 0.0 ? 1.0 / d : 0.0;
-            for (int c = 0; c < bs; c++) {
-                m[k * bs + c] *= id;
-                inv[k * bs + c] *= id;
-            }
-            for (int r = 0; r < bs; r++)
-                if (r != k) {
-                    const double f = m[r * bs + k];
-                    if (f != 0.0)
-                        for (int c = 0; c < bs; c++) {
-                            m[r * bs + c] -= f * m[k * bs + c];
-                            inv[r * bs + c] -= f * inv[k * bs + c];
-                        }
-                }
-        }
-        std::memcpy(&out[(size_t)I * bs * bs], inv, sizeof(double) * bs * bs);
     }
-    return out;
+    std::memcpy(out, inv, sizeof(inv));
 }
 
-void apply_block_diag(const std::vector<double> &Dinv, int bs, const std::vector<double> &x, std::vector<double> &y)
+// C (R x Q) += A (R x K) * B (K x Q), all row-major
+template <int R, int K, int Q>
+inline void gemm_acc(const double *A, const double *B, double *C)
 {
-    const int nb = (int)(x.size() / bs);
-    y.resize(x.size());
-#pragma omp parallel for schedule(static)
-    for (int I = 0; I < nb; I++)
-        for (int r = 0; r < bs; r++) {
-            double s = 0.0;
-            for (int c = 0; c < bs; c++)
-                s += Dinv[(size_t)I * bs * bs + r * bs + c] * x[(size_t)I * bs + c];
-            y[(size_t)I * bs + r] = s;
+    for (int r = 0; r < R; r++)
+        for (int k = 0; k < K; k++) {
+            const double a = A[r * K + k];
+            for (int q = 0; q < Q; q++)
+                C[r * Q + q] += a * B[k * Q + q];
         }
-}
-
-// rho(D^-1 A) by power iteration from a fixed start vector
-double spectral_radius(const Csr &A, const std::vector<double> &Dinv, int bs)
-{
-    std::vector<double> v(A.nrow), w, z;
-    for (int i = 0; i < A.nrow; i++)
-        v[i] = 1.0 + 0.5 * std::sin(0.731 * i);
-    double lam = 0.0;
-    for (int it = 0; it < 20; it++) {
-        double nv = 0.0;
-        for (double t : v)
-            nv += t * t;
-        nv = std::sqrt(nv);
-        if (!(nv > 0.0))
-            return 1.0;
-        for (double &t : v)
-            t /= nv;
-        spmv(A, v, w);
-        apply_block_diag(Dinv, bs, w, z);
-        double num = 0.0;
-        for (int i = 0; i < A.nrow; i++)
-            num += v[i] * z[i];
-        lam = num;
-        v.swap(z);
-    }
-    return std::max(lam, 1e-300);
 }
 
 // Householder QR of an m x k block (m rows of k columns, row-major): Q
@@ -279,299 +191,492 @@ void small_qr(std::vector<double> B, int m, int k, std::vector<double> &Q, std::
     }
 }
 
+// Per-thread map from column to slot of the current row.
+struct Marker {
+    std::vector<int> slot;
+    std::vector<int> used;
+    explicit Marker(int ncol) : slot(ncol, -1) {}
+    int find_or_add(int c)
+    {
+        int &s = slot[c];
+        if (s < 0) {
+            s = (int)used.size();
+            used.push_back(c);
+        }
+        return s;
+    }
+    void reset()
+    {
+        for (int c : used)
+            slot[c] = -1;
+        used.clear();
+    }
+};
+
+// Exclusive prefix sum of counts into ptr (size n + 1).
+void prefix(const std::vector<long long> &cnt, std::vector<long long> &ptr)
+{
+    ptr.assign(cnt.size() + 1, 0);
+    for (size_t i = 0; i < cnt.size(); i++)
+        ptr[i + 1] = ptr[i] + cnt[i];
+}
+
+// Transpose of a block-CSR matrix; rows of the result list their columns in
+// ascending order.  Per-thread column counts over contiguous row ranges give
+// every block its place, so the fill runs in parallel.
+Bsr transpose(const Bsr &A)
+{
+    Bsr T;
+    T.nbr = A.nbc;
+    T.nbc = A.nbr;
+    T.R = A.C;
+    T.C = A.R;
+    const int nt = omp_get_max_threads();
+    const int bsz = A.R * A.C;
+    std::vector<std::vector<long long>> cnt(nt, std::vector<long long>(A.nbc, 0));
+    std::vector<int> lo(nt + 1);
+    for (int t = 0; t <= nt; t++)
+        lo[t] = (int)((long long)A.nbr * t / nt);
+#pragma omp parallel num_threads(nt)
+    {
+        const int t = omp_get_thread_num();
+        for (int i = lo[t]; i < lo[t + 1]; i++)
+            for (long long k = A.ptr[i]; k < A.ptr[i + 1]; k++)
+                cnt[t][A.col[k]]++;
+    }
+    T.ptr.assign((size_t)A.nbc + 1, 0);
+    for (int c = 0; c < A.nbc; c++) {
+        long long s = 0;
+        for (int t = 0; t < nt; t++)
+            s += cnt[t][c];
+        T.ptr[c + 1] = T.ptr[c] + s;
+    }
+    // per-thread start of each column
+    for (int c = 0; c < A.nbc; c++) {
+        long long p = T.ptr[c];
+        for (int t = 0; t < nt; t++) {
+            const long long k = cnt[t][c];
+            cnt[t][c] = p;
+            p += k;
+        }
+    }
+    T.col.resize((size_t)T.ptr[A.nbc]);
+    T.val.resize((size_t)T.ptr[A.nbc] * bsz);
+#pragma omp parallel num_threads(nt)
+    {
+        const int t = omp_get_thread_num();
+        for (int i = lo[t]; i < lo[t + 1]; i++)
+            for (long long k = A.ptr[i]; k < A.ptr[i + 1]; k++) {
+                const long long q = cnt[t][A.col[k]]++;
+                T.col[q] = i;
+                const double *s = &A.val[(size_t)k * bsz];
+                double *d = &T.val[(size_t)q * bsz];
+                for (int r = 0; r < A.R; r++)
+                    for (int c = 0; c < A.C; c++)
+                        d[c * A.R + r] = s[r * A.C + c];
+            }
+    }
+    return T;
+}
+
+template <class Op>
+std::vector<double> diag_inverse(const Op &A)
+{
+    constexpr int BS = Op::BS;
+    const int nb = A.nbr();
+    std::vector<double> out((size_t)nb * BS * BS);
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int I = 0; I < nb; I++) {
+        double d[BS * BS] = {};
+        A.row(I, [&](int J, const double *blk) {
+            if (J == I)
+                for (int k = 0; k < BS * BS; k++)
+                    d[k] += blk[k];
+        });
+        invert_block<BS>(d, &out[(size_t)I * BS * BS]);
+    }
+    return out;
+}
+
+// rho(D^-1 A) by power iteration from a fixed start vector; the sums run over
+// per-row partials in row order, so the estimate does not depend on the
+// thread count
+template <class Op>
+double spectral_radius(const Op &A, const std::vector<double> &Dinv, int iters)
+{
+    constexpr int BS = Op::BS;
+    const int nb = A.nbr();
+    const size_t nd = (size_t)nb * BS;
+    std::vector<double> v(nd), z(nd), part(nb);
+    for (size_t i = 0; i < nd; i++)
+        v[i] = 1.0 + 0.5 * std::sin(0.731 * (double)i);
+    double lam = 1e-300;
+    for (int it = 0; it < iters; it++) {
+#pragma omp parallel for schedule(static)
+        for (int I = 0; I < nb; I++) {
+            double s = 0.0;
+            for (int r = 0; r < BS; r++)
+                s += v[(size_t)I * BS + r] * v[(size_t)I * BS + r];
+            part[I] = s;
+        }
+        double nv = 0.0;
+        for (int I = 0; I < nb; I++)
+            nv += part[I];
+        nv = std::sqrt(nv);
+        if (!(nv > 0.0))
+            return 1.0;
+#pragma omp parallel for schedule(dynamic, 256)
+        for (int I = 0; I < nb; I++) {
+            double y[BS] = {};
+            A.row(I, [&](int J, const double *blk) {
+                for (int r = 0; r < BS; r++)
+                    for (int c = 0; c < BS; c++)
+                        y[r] += blk[r * BS + c] * v[(size_t)J * BS + c];
+            });
+            const double *D = &Dinv[(size_t)I * BS * BS];
+            double num = 0.0;
+            for (int r = 0; r < BS; r++) {
+                double s = 0.0;
+                for (int c = 0; c < BS; c++)
+                    s += D[r * BS + c] * y[c];
+                z[(size_t)I * BS + r] = s / nv;
+                num += v[(size_t)I * BS + r] * s;
+            }
+            part[I] = num;
+        }
+        double num = 0.0;
+        for (int I = 0; I < nb; I++)
+            num += part[I];
+        lam = num / (nv * nv);
+        v.swap(z);
+    }
+    return std::max(lam, 1e-300);
+}
+
+// One coarsening step from an operator with BS x BS blocks.
+struct CoarseOut {
+    Bsr Ac;
+    std::vector<double> Bc;  // coarse near-nullspace, 6 x 6 per aggregate (row-major)
+    std::vector<int> gidx;   // integer box coordinates of the aggregates
+    std::vector<double> cen; // aggregate centroids
+};
+
+template <class Op>
+bool coarsen(const Op &A, const uint8_t *mask, const std::vector<int> &gidx, const std::vector<double> &pos,
+             const std::vector<double> &Bl, const AmgOptions &opt, AmgLevel &L, CoarseOut &out)
+{
+    constexpr int BS = Op::BS;
+    const int nb = A.nbr();
+    // aggregates: boxes of the integer grid
+    int gmax[3] = {0, 0, 0};
+    for (int I = 0; I < nb; I++)
+        for (int d = 0; d < 3; d++)
+            gmax[d] = std::max(gmax[d], gidx[3 * (size_t)I + d]);
+    std::vector<long long> key(nb);
+    for (int I = 0; I < nb; I++)
+        key[I] = ((long long)gidx[3 * (size_t)I + 2] * (gmax[1] + 1) + gidx[3 * (size_t)I + 1]) * (gmax[0] + 1) +
+                 gidx[3 * (size_t)I];
+    std::vector<long long> uk(key);
+    std::sort(uk.begin(), uk.end());
+    uk.erase(std::unique(uk.begin(), uk.end()), uk.end());
+    const int nagg = (int)uk.size();
+    if (nagg >= nb)
+        return false;
+    std::vector<int> agg(nb);
+#pragma omp parallel for schedule(static)
+    for (int I = 0; I < nb; I++)
+        agg[I] = (int)(std::lower_bound(uk.begin(), uk.end(), key[I]) - uk.begin());
+    std::vector<long long> mcnt(nagg, 0), mptr;
+    for (int I = 0; I < nb; I++)
+        mcnt[agg[I]]++;
+    prefix(mcnt, mptr);
+    std::vector<int> mem(nb);
+    {
+        std::vector<long long> fill(mptr.begin(), mptr.end() - 1);
+        for (int I = 0; I < nb; I++)
+            mem[fill[agg[I]]++] = I;
+    }
+    out.cen.assign(3 * (size_t)nagg, 0.0);
+    for (int a = 0; a < nagg; a++) {
+        for (long long q = mptr[a]; q < mptr[a + 1]; q++)
+            for (int d = 0; d < 3; d++)
+                out.cen[3 * (size_t)a + d] += pos[3 * (size_t)mem[q] + d];
+        for (int d = 0; d < 3; d++)
+            out.cen[3 * (size_t)a + d] /= (double)(mptr[a + 1] - mptr[a]);
+    }
+    // near-nullspace on level 0: translations and rotations about the centroid
+    std::vector<double> B0;
+    const std::vector<double> *B = &Bl;
+    if (mask) {
+        B0.assign((size_t)nb * BS * 6, 0.0);
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < nb; i++) {
+            const double *c = &out.cen[3 * (size_t)agg[i]];
+            const double x = pos[3 * (size_t)i] - c[0], y = pos[3 * (size_t)i + 1] - c[1],
+                         z = pos[3 * (size_t)i + 2] - c[2];
+            const double rot[3][3] = {{-y, 0.0, z}, {x, -z, 0.0}, {0.0, y, -x}};  // rows: x, y, z comps
+            for (int d = 0; d < 3; d++) {
+                if (!((mask[i] >> d) & 1u))
+                    continue;
+                double *row = &B0[((size_t)i * BS + d) * 6];
+                row[d] = 1.0;
+                row[3] = rot[d][0];
+                row[4] = rot[d][1];
+                row[5] = rot[d][2];
+            }
+        }
+        B = &B0;
+    }
+    // tentative prolongator: one BS x 6 block per block row
+    std::vector<double> T((size_t)nb * BS * 6, 0.0);
+    out.Bc.assign((size_t)nagg * 36, 0.0);
+    std::vector<char> dropped((size_t)nagg * 6, 0);
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int a = 0; a < nagg; a++) {
+        const int cnt = (int)(mptr[a + 1] - mptr[a]);
+        const int m = cnt * BS;
+        std::vector<double> Bm((size_t)m * 6), Q, R;
+        for (int q = 0; q < cnt; q++)
+            std::memcpy(&Bm[(size_t)q * BS * 6], &(*B)[(size_t)mem[mptr[a] + q] * BS * 6], sizeof(double) * BS * 6);
+        small_qr(Bm, m, 6, Q, R);
+        double rmax = 0.0;
+        for (double v : R)
+            rmax = std::max(rmax, std::fabs(v));
+        for (int c = 0; c < 6; c++)
+            if (!(std::fabs(R[(size_t)c * 6 + c]) > 1e-10 * std::max(1.0, rmax))) {
+                dropped[(size_t)a * 6 + c] = 1;
+                for (int r = 0; r < m; r++)
+                    Q[(size_t)r * 6 + c] = 0.0;
+                for (int c2 = 0; c2 < 6; c2++)
+                    R[(size_t)c * 6 + c2] = 0.0;
+            }
+        for (int q = 0; q < cnt; q++)
+            std::memcpy(&T[(size_t)mem[mptr[a] + q] * BS * 6], &Q[(size_t)q * BS * 6], sizeof(double) * BS * 6);
+        std::memcpy(&out.Bc[(size_t)a * 36], R.data(), sizeof(double) * 36);
+    }
+    // smoother data
+    L.nblock = nb;
+    L.bs = BS;
+    L.Dinv = diag_inverse(A);
+    const double rho = spectral_radius(A, L.Dinv, opt.power_iters);
+    L.omega = 1.0 / rho;
+    const double wp = 4.0 / 3.0 / rho;
+    // smoothed prolongator P = T - wp D^-1 A T, BS x 6 blocks; the row of a
+    // block row lists the aggregates of its operator row, its own first
+    Bsr &P = L.P;
+    P.nbr = nb;
+    P.nbc = nagg;
+    P.R = BS;
+    P.C = 6;
+    {
+        std::vector<long long> cnt(nb);
+#pragma omp parallel
+        {
+            Marker mk(nagg);
+#pragma omp for schedule(dynamic, 256)
+            for (int I = 0; I < nb; I++) {
+                mk.find_or_add(agg[I]);
+                A.row(I, [&](int J, const double *) { mk.find_or_add(agg[J]); });
+                cnt[I] = (long long)mk.used.size();
+                mk.reset();
+            }
+        }
+        prefix(cnt, P.ptr);
+    }
+    P.col.resize((size_t)P.ptr[nb]);
+    P.val.assign((size_t)P.ptr[nb] * BS * 6, 0.0);
+#pragma omp parallel
+    {
+        Marker mk(nagg);
+        std::vector<double> acc;
+#pragma omp for schedule(dynamic, 256)
+        for (int I = 0; I < nb; I++) {
+            const long long p0 = P.ptr[I];
+            const int ns = (int)(P.ptr[I + 1] - p0);
+            acc.assign((size_t)ns * BS * 6, 0.0);
+            mk.find_or_add(agg[I]);
+            A.row(I, [&](int J, const double *blk) {
+                const int s = mk.find_or_add(agg[J]);
+                gemm_acc<BS, BS, 6>(blk, &T[(size_t)J * BS * 6], &acc[(size_t)s * BS * 6]);
+            });
+            const double *D = &L.Dinv[(size_t)I * BS * BS];
+            for (int s = 0; s < ns; s++) {
+                P.col[p0 + s] = mk.used[s];
+                double *pv = &P.val[(size_t)(p0 + s) * BS * 6];
+                double da[BS * 6] = {};
+                gemm_acc<BS, BS, 6>(D, &acc[(size_t)s * BS * 6], da);
+                for (int k = 0; k < BS * 6; k++)
+                    pv[k] = (s == 0 ? T[(size_t)I * BS * 6 + k] : 0.0) - wp * da[k];
+                if (mask)  // constrained level-0 DOFs stay out of the prolongation
+                    for (int r = 0; r < BS; r++)
+                        if (!((mask[I] >> r) & 1u))
+                            for (int c = 0; c < 6; c++)
+                                pv[r * 6 + c] = 0.0;
+            }
+            mk.reset();
+        }
+    }
+    L.Pt = transpose(P);
+    // W = A P (BS x 6 blocks)
+    Bsr W;
+    W.nbr = nb;
+    W.nbc = nagg;
+    W.R = BS;
+    W.C = 6;
+    {
+        std::vector<long long> cnt(nb);
+#pragma omp parallel
+        {
+            Marker mk(nagg);
+#pragma omp for schedule(dynamic, 256)
+            for (int I = 0; I < nb; I++) {
+                A.row(I, [&](int J, const double *) {
+                    for (long long k = P.ptr[J]; k < P.ptr[J + 1]; k++)
+                        mk.find_or_add(P.col[k]);
+                });
+                cnt[I] = (long long)mk.used.size();
+                mk.reset();
+            }
+        }
+        prefix(cnt, W.ptr);
+    }
+    W.col.resize((size_t)W.ptr[nb]);
+    W.val.assign((size_t)W.ptr[nb] * BS * 6, 0.0);
+#pragma omp parallel
+    {
+        Marker mk(nagg);
+#pragma omp for schedule(dynamic, 256)
+        for (int I = 0; I < nb; I++) {
+            const long long w0 = W.ptr[I];
+            A.row(I, [&](int J, const double *blk) {
+                for (long long k = P.ptr[J]; k < P.ptr[J + 1]; k++) {
+                    const int s = mk.find_or_add(P.col[k]);
+                    gemm_acc<BS, BS, 6>(blk, &P.val[(size_t)k * BS * 6], &W.val[(size_t)(w0 + s) * BS * 6]);
+                }
+            });
+            for (size_t s = 0; s < mk.used.size(); s++)
+                W.col[w0 + s] = mk.used[s];
+            mk.reset();
+        }
+    }
+    // Ac = P^T W (6 x 6 blocks); every row holds its diagonal block
+    Bsr &Ac = out.Ac;
+    Ac.nbr = Ac.nbc = nagg;
+    Ac.R = Ac.C = 6;
+    const Bsr &Pt = L.Pt;
+    {
+        std::vector<long long> cnt(nagg);
+#pragma omp parallel
+        {
+            Marker mk(nagg);
+#pragma omp for schedule(dynamic, 16)
+            for (int a = 0; a < nagg; a++) {
+                mk.find_or_add(a);
+                for (long long k = Pt.ptr[a]; k < Pt.ptr[a + 1]; k++) {
+                    const int I = Pt.col[k];
+                    for (long long q = W.ptr[I]; q < W.ptr[I + 1]; q++)
+                        mk.find_or_add(W.col[q]);
+                }
+                cnt[a] = (long long)mk.used.size();
+                mk.reset();
+            }
+        }
+        prefix(cnt, Ac.ptr);
+    }
+    Ac.col.resize((size_t)Ac.ptr[nagg]);
+    Ac.val.assign((size_t)Ac.ptr[nagg] * 36, 0.0);
+#pragma omp parallel
+    {
+        Marker mk(nagg);
+#pragma omp for schedule(dynamic, 16)
+        for (int a = 0; a < nagg; a++) {
+            const long long a0 = Ac.ptr[a];
+            mk.find_or_add(a);
+            for (long long k = Pt.ptr[a]; k < Pt.ptr[a + 1]; k++) {
+                const int I = Pt.col[k];
+                // Pt block (6 x BS) is the transpose of P's (BS x 6)
+                const double *pt = &Pt.val[(size_t)k * 6 * BS];
+                for (long long q = W.ptr[I]; q < W.ptr[I + 1]; q++) {
+                    const int s = mk.find_or_add(W.col[q]);
+                    gemm_acc<6, BS, 6>(pt, &W.val[(size_t)q * BS * 6], &Ac.val[(size_t)(a0 + s) * 36]);
+                }
+            }
+            for (size_t s = 0; s < mk.used.size(); s++)
+                Ac.col[a0 + s] = mk.used[s];
+            // coarse DOFs without a prolongation column: unit diagonal
+            for (int c = 0; c < 6; c++)
+                if (dropped[(size_t)a * 6 + c])
+                    Ac.val[(size_t)a0 * 36 + c * 6 + c] = 1.0;
+            mk.reset();
+        }
+    }
+    // next level's grid
+    out.gidx.assign(3 * (size_t)nagg, 0);
+    for (int I = 0; I < nb; I++)
+        for (int d = 0; d < 3; d++)
+            out.gidx[3 * (size_t)agg[I] + d] = gidx[3 * (size_t)I + d] / 3;
+    return true;
+}
+
 }  // namespace
 
 int amg_build(const AmgInput &in, AmgHierarchy &H, const AmgOptions &opt)
 {
     H = AmgHierarchy();
     const int n = in.n;
-    // ---- level 0 operator, scalar CSR, constrained rows and columns removed
-    Csr A;
-    A.nrow = A.ncol = 3 * n;
-    A.ptr.assign((size_t)3 * n + 1, 0);
-    auto freedof = [&](int i, int d) { return ((in.mask[i] >> d) & 1u) != 0; };
-    for (int i = 0; i < n; i++)
-        for (int r = 0; r < 3; r++)
-            A.ptr[3 * (size_t)i + r + 1] = freedof(i, r) ? 3LL * in.nconn[i] : 0;
-    for (int k = 0; k < 3 * n; k++)
-        A.ptr[k + 1] += A.ptr[k];
-    A.col.resize((size_t)A.ptr[3 * n]);
-    A.val.resize((size_t)A.ptr[3 * n]);
-#pragma omp parallel for schedule(dynamic, 256)
-    for (int i = 0; i < n; i++) {
-        const long long off = in.rowoff[i];
-        const int np = in.npad[i], nc = in.nconn[i];
-        for (int r = 0; r < 3; r++) {
-            if (!freedof(i, r))
-                continue;
-            long long q = A.ptr[3 * (size_t)i + r];
-            for (int b = 0; b < nc; b++) {
-                const int j = in.cols[off + b];
-                for (int c = 0; c < 3; c++) {
-                    A.col[q] = 3 * j + c;
-                    A.val[q] = freedof(j, c) ? in.val[9 * off + (size_t)(3 * r + c) * np + b] : 0.0;
-                    q++;
-                }
-            }
-        }
-    }
-    // ---- near-nullspace of level 0 and the aggregation grid
     const double h = opt.agg_spacing;
     double lo[3] = {in.xyz[0], in.xyz[1], in.xyz[2]};
     for (int i = 0; i < n; i++)
         for (int d = 0; d < 3; d++)
             lo[d] = std::min(lo[d], in.xyz[3 * (size_t)i + d]);
-    std::vector<int> gidx(3 * (size_t)n);  // integer box coordinates of each block row
+    std::vector<int> gidx(3 * (size_t)n);
     for (int i = 0; i < n; i++)
         for (int d = 0; d < 3; d++)
             gidx[3 * (size_t)i + d] = (int)std::floor((in.xyz[3 * (size_t)i + d] - lo[d]) / h + 1e-9);
-    std::vector<double> pos(in.xyz, in.xyz + 3 * (size_t)n);  // block-row positions
-    int nrow_blocks = n, bs = 3;
-    std::vector<double> Bnull;  // near-nullspace rows (bs * nrow_blocks) x 6
-    for (int lev = 0; lev < opt.max_levels; lev++) {
-        const int nd = nrow_blocks * bs;
-        if (nrow_blocks <= opt.coarse_blocks)
-            break;
-        // aggregates: boxes of the integer grid (coarsened by 3 above level 0)
-        std::vector<long long> key(nrow_blocks);
-        int gmax[3] = {0, 0, 0};
-        for (int I = 0; I < nrow_blocks; I++)
-            for (int d = 0; d < 3; d++)
-                gmax[d] = std::max(gmax[d], gidx[3 * (size_t)I + d]);
-        for (int I = 0; I < nrow_blocks; I++)
-            key[I] = ((long long)gidx[3 * (size_t)I + 2] * (gmax[1] + 1) + gidx[3 * (size_t)I + 1]) * (gmax[0] + 1) +
-                     gidx[3 * (size_t)I];
-        std::vector<long long> uk(key);
-        std::sort(uk.begin(), uk.end());
-        uk.erase(std::unique(uk.begin(), uk.end()), uk.end());
-        const int nagg = (int)uk.size();
-        if (nagg >= nrow_blocks)
-            break;  // no coarsening left
-        std::vector<int> agg(nrow_blocks);
-        for (int I = 0; I < nrow_blocks; I++)
-            agg[I] = (int)(std::lower_bound(uk.begin(), uk.end(), key[I]) - uk.begin());
-        std::vector<double> cen(3 * (size_t)nagg, 0.0);
-        std::vector<int> cnt(nagg, 0);
-        for (int I = 0; I < nrow_blocks; I++) {
-            for (int d = 0; d < 3; d++)
-                cen[3 * (size_t)agg[I] + d] += pos[3 * (size_t)I + d];
-            cnt[agg[I]]++;
-        }
-        for (int a = 0; a < nagg; a++)
-            for (int d = 0; d < 3; d++)
-                cen[3 * (size_t)a + d] /= cnt[a];
-        // near-nullspace of this level's DOFs (zero rows where A has none)
-        std::vector<double> Bl((size_t)nd * 6, 0.0);
-        if (lev == 0) {
-            for (int i = 0; i < n; i++) {
-                const double x = pos[3 * (size_t)i] - cen[3 * (size_t)agg[i]],
-                             y = pos[3 * (size_t)i + 1] - cen[3 * (size_t)agg[i] + 1],
-                             z = pos[3 * (size_t)i + 2] - cen[3 * (size_t)agg[i] + 2];
-                const double rot[3][3] = {{-y, 0.0, z}, {x, -z, 0.0}, {0.0, y, -x}};  // rows: x, y, z comps
-                for (int d = 0; d < 3; d++) {
-                    if (!freedof(i, d))
-                        continue;
-                    double *row = &Bl[(3 * (size_t)i + d) * 6];
-                    row[d] = 1.0;
-                    row[3] = rot[d][0];
-                    row[4] = rot[d][1];
-                    row[5] = rot[d][2];
-                }
-            }
-        } else {
-            Bl = Bnull;
-        }
-        // tentative prolongator T (nd x 6 nagg) and the next near-nullspace
-        std::vector<std::vector<int>> members(nagg);
-        for (int I = 0; I < nrow_blocks; I++)
-            members[agg[I]].push_back(I);
-        Csr T;
-        T.nrow = nd;
-        T.ncol = 6 * nagg;
-        T.ptr.assign((size_t)nd + 1, 0);
-        std::vector<double> Bc((size_t)nagg * 36, 0.0);
-        std::vector<double> tv((size_t)nd * 6, 0.0);
-#pragma omp parallel for schedule(dynamic, 16)
-        for (int a = 0; a < nagg; a++) {
-            const std::vector<int> &mem = members[a];
-            const int m = (int)mem.size() * bs;
-            std::vector<double> B((size_t)m * 6), Q, R;
-            for (size_t q = 0; q < mem.size(); q++)
-                for (int d = 0; d < bs; d++)
-                    for (int c = 0; c < 6; c++)
-                        B[(q * bs + d) * 6 + c] = Bl[((size_t)mem[q] * bs + d) * 6 + c];
-            small_qr(B, m, 6, Q, R);
-            // drop columns the aggregate cannot represent
-            double rmax = 0.0;
-            for (double v : R)
-                rmax = std::max(rmax, std::fabs(v));
-            for (int c = 0; c < 6; c++)
-                if (!(std::fabs(R[(size_t)c * 6 + c]) > 1e-10 * std::max(1.0, rmax))) {
-                    for (int r = 0; r < m; r++)
-                        Q[(size_t)r * 6 + c] = 0.0;
-                    for (int c2 = 0; c2 < 6; c2++)
-                        R[(size_t)c * 6 + c2] = 0.0;
-                }
-            for (size_t q = 0; q < mem.size(); q++)
-                for (int d = 0; d < bs; d++)
-                    for (int c = 0; c < 6; c++)
-                        tv[((size_t)mem[q] * bs + d) * 6 + c] = Q[(q * bs + d) * 6 + c];
-            std::memcpy(&Bc[(size_t)a * 36], R.data(), sizeof(double) * 36);
-        }
-        for (int r = 0; r < nd; r++)
-            T.ptr[r + 1] = T.ptr[r] + 6;
-        T.col.resize((size_t)nd * 6);
-        T.val = tv;
-        for (int r = 0; r < nd; r++)
-            for (int c = 0; c < 6; c++)
-                T.col[(size_t)r * 6 + c] = 6 * agg[r / bs] + c;
-        // smoothed prolongator P = T - omega D^-1 A T
-        const std::vector<double> Dinv = block_diag_inverse(A, bs);
-        const double rho = spectral_radius(A, Dinv, bs);
-        const double omega = 4.0 / 3.0 / rho;
-        Csr AT = spgemm(A, T);
-        // D^-1 (A T): block rows of AT mixed by the bs x bs inverse
-        Csr P;
-        {
-            Csr DAT;
-            DAT.nrow = nd;
-            DAT.ncol = AT.ncol;
-            DAT.ptr.assign((size_t)nd + 1, 0);
-            // the union pattern of the bs rows of a block row, for every row of it
-            std::vector<std::vector<int>> pat(nrow_blocks);
-#pragma omp parallel for schedule(dynamic, 256)
-            for (int I = 0; I < nrow_blocks; I++) {
-                std::vector<int> &pt = pat[I];
-                for (int r = 0; r < bs; r++)
-                    for (long long a2 = AT.ptr[I * bs + r]; a2 < AT.ptr[I * bs + r + 1]; a2++)
-                        pt.push_back(AT.col[a2]);
-                for (int c = 0; c < 6; c++)  // T's own columns too
-                    pt.push_back(6 * agg[I] + c);
-                std::sort(pt.begin(), pt.end());
-                pt.erase(std::unique(pt.begin(), pt.end()), pt.end());
-            }
-            for (int I = 0; I < nrow_blocks; I++)
-                for (int r = 0; r < bs; r++)
-                    DAT.ptr[I * bs + r + 1] = (long long)pat[I].size();
-            for (int k = 0; k < nd; k++)
-                DAT.ptr[k + 1] += DAT.ptr[k];
-            DAT.col.resize((size_t)DAT.ptr[nd]);
-            DAT.val.assign((size_t)DAT.ptr[nd], 0.0);
-#pragma omp parallel for schedule(dynamic, 256)
-            for (int I = 0; I < nrow_blocks; I++) {
-                const std::vector<int> &pt = pat[I];
-                for (int r = 0; r < bs; r++) {
-                    const long long base = DAT.ptr[I * bs + r];
-                    for (size_t q = 0; q < pt.size(); q++)
-                        DAT.col[base + q] = pt[q];
-                    // T part
-                    for (int c = 0; c < 6; c++) {
-                        const size_t q = std::lower_bound(pt.begin(), pt.end(), 6 * agg[I] + c) - pt.begin();
-                        DAT.val[base + q] += tv[((size_t)I * bs + r) * 6 + c];
-                    }
-                    // - omega D^-1 A T part
-                    for (int s = 0; s < bs; s++) {
-                        const double dv = Dinv[(size_t)I * bs * bs + r * bs + s];
-                        if (dv == 0.0)
-                            continue;
-                        for (long long a2 = AT.ptr[I * bs + s]; a2 < AT.ptr[I * bs + s + 1]; a2++) {
-                            const size_t q = std::lower_bound(pt.begin(), pt.end(), AT.col[a2]) - pt.begin();
-                            DAT.val[base + q] -= omega * dv * AT.val[a2];
-                        }
-                    }
-                }
-            }
-            P = std::move(DAT);
-        }
-        // rows of constrained level-0 DOFs stay out of the prolongation
-        if (lev == 0)
-            for (int i = 0; i < n; i++)
-                for (int d = 0; d < 3; d++)
-                    if (!freedof(i, d))
-                        for (long long q = P.ptr[3 * (size_t)i + d]; q < P.ptr[3 * (size_t)i + d + 1]; q++)
-                            P.val[q] = 0.0;
-        Csr Pt = transpose(P);
-        Csr AP = spgemm(A, P);
-        Csr Ac = spgemm(Pt, AP);
-        // decouple coarse DOFs whose prolongation column is empty
-        {
-            std::vector<char> empty(Ac.nrow, 1);
-            for (long long q = 0; q < P.ptr[P.nrow]; q++)
-                if (P.val[q] != 0.0)
-                    empty[P.col[q]] = 0;
-            // rebuild rows of empty DOFs as a unit diagonal
-            Csr B2;
-            B2.nrow = B2.ncol = Ac.nrow;
-            B2.ptr.assign((size_t)Ac.nrow + 1, 0);
-            for (int r = 0; r < Ac.nrow; r++) {
-                long long c = 0;
-                if (empty[r]) {
-                    c = 1;
-                } else {
-                    for (long long q = Ac.ptr[r]; q < Ac.ptr[r + 1]; q++)
-                        c += !empty[Ac.col[q]];
-                }
-                B2.ptr[r + 1] = B2.ptr[r] + c;
-            }
-            B2.col.resize((size_t)B2.ptr[Ac.nrow]);
-            B2.val.resize((size_t)B2.ptr[Ac.nrow]);
-            for (int r = 0; r < Ac.nrow; r++) {
-                long long p = B2.ptr[r];
-                if (empty[r]) {
-                    B2.col[p] = r;
-                    B2.val[p] = 1.0;
-                    continue;
-                }
-                for (long long q = Ac.ptr[r]; q < Ac.ptr[r + 1]; q++)
-                    if (!empty[Ac.col[q]]) {
-                        B2.col[p] = Ac.col[q];
-                        B2.val[p] = Ac.val[q];
-                        p++;
-                    }
-            }
-            Ac = std::move(B2);
-        }
+    std::vector<double> pos(in.xyz, in.xyz + 3 * (size_t)n);
+    Bsr A = level0(in);  // the operator of the level being coarsened
+    std::vector<double> Bnull;
+    if (n > opt.coarse_blocks && opt.max_levels > 0) {
         AmgLevel L;
-        L.nblock = nrow_blocks;
-        L.bs = bs;
-        L.A = std::move(A);
-        L.Dinv = Dinv;
-        L.omega = 1.0 / rho;
-        L.P = std::move(P);
-        L.Pt = std::move(Pt);
-        H.levels.push_back(std::move(L));
-        // next level: aggregates as block rows of 6 DOFs
-        A = std::move(Ac);
-        Bnull = Bc;  // R factors: the coarse near-nullspace, 6 x 6 per aggregate
-        {
-            // Bc is per aggregate 6 x 6 (rows = coarse DOFs of the aggregate)
-            std::vector<double> Bn((size_t)nagg * 6 * 6);
-            for (int a = 0; a < nagg; a++)
-                for (int r = 0; r < 6; r++)
-                    for (int c = 0; c < 6; c++)
-                        Bn[((size_t)a * 6 + r) * 6 + c] = Bc[(size_t)a * 36 + r * 6 + c];
-            Bnull.swap(Bn);
+        CoarseOut co;
+        if (coarsen(OpB<3>{A}, in.mask, gidx, pos, Bnull, opt, L, co)) {
+            H.levels.push_back(std::move(L));
+            A = std::move(co.Ac);
+            Bnull = std::move(co.Bc);
+            gidx = std::move(co.gidx);
+            pos = std::move(co.cen);
         }
-        std::vector<int> g2(3 * (size_t)nagg);
-        for (int I = 0; I < nrow_blocks; I++)
-            for (int d = 0; d < 3; d++)
-                g2[3 * (size_t)agg[I] + d] = gidx[3 * (size_t)I + d] / 3;
-        gidx.swap(g2);
-        pos.swap(cen);
-        nrow_blocks = nagg;
-        bs = 6;
     }
-    // coarsest level: dense Cholesky (lower factor, row-major)
-    const int nc = A.nrow;
+    while (!H.levels.empty() && (int)H.levels.size() < opt.max_levels && A.nbr > opt.coarse_blocks) {
+        AmgLevel L;
+        CoarseOut co;
+        if (!coarsen(OpB<6>{A}, nullptr, gidx, pos, Bnull, opt, L, co))
+            break;
+        L.A = std::move(A);
+        H.levels.push_back(std::move(L));
+        A = std::move(co.Ac);
+        Bnull = std::move(co.Bc);
+        gidx = std::move(co.gidx);
+        pos = std::move(co.cen);
+    }
+    // coarsest level: dense Cholesky (lower factor, row-major) and inverse
+    const int bs = A.R;
+    const int nc = A.nbr * bs;
     H.coarse_n = nc;
     H.coarse_chol.assign((size_t)nc * nc, 0.0);
     std::vector<double> &Lc = H.coarse_chol;
-    for (int r = 0; r < nc; r++)
-        for (long long q = A.ptr[r]; q < A.ptr[r + 1]; q++)
-            Lc[(size_t)r * nc + A.col[q]] = A.val[q];
-    for (int r = 0; r < nc; r++)
-        if (Lc[(size_t)r * nc + r] == 0.0)
-            Lc[(size_t)r * nc + r] = 1.0;  // decoupled DOF
+    for (int I = 0; I < A.nbr; I++)
+        for (long long k = A.ptr[I]; k < A.ptr[I + 1]; k++)
+            for (int r = 0; r < bs; r++)
+                for (int c = 0; c < bs; c++)
+                    Lc[(size_t)(I * bs + r) * nc + A.col[k] * bs + c] += A.val[(size_t)k * bs * bs + r * bs + c];
+    for (int r = 0; r < nc; r++) {
+        bool zero = true;
+        for (int c = 0; c < nc && zero; c++)
+            zero = Lc[(size_t)r * nc + c] == 0.0;
+        if (zero)
+            Lc[(size_t)r * nc + r] = 1.0;  // decoupled (constrained) DOF
+    }
     for (int j = 0; j < nc; j++) {
         double d = Lc[(size_t)j * nc + j];
         for (int k = 0; k < j; k++)
@@ -591,6 +696,29 @@ int amg_build(const AmgInput &in, AmgHierarchy &H, const AmgOptions &opt)
     for (int i = 0; i < nc; i++)
         for (int j = i + 1; j < nc; j++)
             Lc[(size_t)i * nc + j] = 0.0;
+    // inverse: solve L L^T X = I column by column
+    H.coarse_inv.assign((size_t)nc * nc, 0.0);
+#pragma omp parallel
+    {
+        std::vector<double> y(nc);
+#pragma omp for schedule(dynamic, 8)
+        for (int col = 0; col < nc; col++) {
+            for (int i = 0; i < nc; i++) {
+                double s = i == col ? 1.0 : 0.0;
+                for (int k = 0; k < i; k++)
+                    s -= Lc[(size_t)i * nc + k] * y[k];
+                y[i] = s / Lc[(size_t)i * nc + i];
+            }
+            for (int i = nc - 1; i >= 0; i--) {
+                double s = y[i];
+                for (int k = i + 1; k < nc; k++)
+                    s -= Lc[(size_t)k * nc + i] * y[k];
+                y[i] = s / Lc[(size_t)i * nc + i];
+            }
+            for (int i = 0; i < nc; i++)
+                H.coarse_inv[(size_t)i * nc + col] = y[i];
+        }
+    }
     H.coarse_A = std::move(A);
     return (int)H.levels.size();
 }

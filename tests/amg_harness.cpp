@@ -2,6 +2,7 @@
 // block-CSR layout (binary files in a directory) and writes the hierarchy
 // back as binary files, for tests/test_amg_setup.py.
 //   amg_harness DIR AGG_SPACING
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <string>
@@ -29,8 +30,9 @@ static void wr(const std::string &path, const std::vector<T> &v)
     std::fclose(f);
 }
 
-static void wr_csr(const std::string &p, const lpm::Csr &A)
+static void wr_bsr(FILE *f, const std::string &p, const lpm::Bsr &A)
 {
+    std::fprintf(f, " %d %d %d %d", A.nbr, A.nbc, A.R, A.C);
     wr(p + "_ptr.bin", A.ptr);
     wr(p + "_col.bin", A.col);
     wr(p + "_val.bin", A.val);
@@ -67,19 +69,26 @@ int main(int argc, char **argv)
     lpm::AmgOptions opt;
     opt.agg_spacing = std::atof(argv[2]);
     lpm::AmgHierarchy H;
+    const auto t0 = std::chrono::steady_clock::now();
     const int L = lpm::amg_build(in, H, opt);
+    const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::fprintf(stderr, "amg_build %.3f s\n", sec);
     FILE *f = std::fopen((d + "/levels.txt").c_str(), "w");
     std::fprintf(f, "%d %d\n", L, H.coarse_n);
     for (size_t l = 0; l < H.levels.size(); l++) {
         const lpm::AmgLevel &lv = H.levels[l];
-        std::fprintf(f, "%d %d %.17g %d %d\n", lv.nblock, lv.bs, lv.omega, lv.P.nrow, lv.P.ncol);
+        std::fprintf(f, "%d %d %.17g", lv.nblock, lv.bs, lv.omega);
         const std::string p = d + "/L" + std::to_string(l);
-        wr_csr(p + "_A", lv.A);
-        wr_csr(p + "_P", lv.P);
-        wr_csr(p + "_Pt", lv.Pt);
+        wr_bsr(f, p + "_A", lv.A);
+        wr_bsr(f, p + "_P", lv.P);
+        wr_bsr(f, p + "_Pt", lv.Pt);
+        std::fprintf(f, "\n");
         wr(p + "_Dinv.bin", lv.Dinv);
     }
+    wr_bsr(f, d + "/coarse_A", H.coarse_A);
+    std::fprintf(f, "\n");
     std::fclose(f);
     wr(d + "/coarse_chol.bin", H.coarse_chol);
+    wr(d + "/coarse_inv.bin", H.coarse_inv);
     return L >= 0 ? 0 : 1;
 }

@@ -1,9 +1,9 @@
 """The host-side smoothed-aggregation hierarchy (lpm-c_gb300/csrc/amg_setup.cpp)
 on the CPU: built from the oracle's stiffness (the reference's FD matrix with
 the boundary conditions of a load step) in the device block-CSR layout, then
-used as the preconditioner of a CG in numpy (V-cycle: two damped
-block-Jacobi sweeps before and after, Galerkin coarse operators, dense
-Cholesky on the coarsest level).  It must converge to 1e-10 in a small,
+used as the preconditioner of a CG in numpy (V-cycle as the device runs it:
+two damped block-Jacobi sweeps before and after the coarse correction,
+Galerkin coarse operators, the dense inverse on the coarsest level).  It must converge to 1e-10 in a small,
 size-independent number of iterations where block-Jacobi PCG needs hundreds.
 """
 import os
@@ -23,7 +23,7 @@ CSRC = os.path.join(ROOT, "lpm-c_gb300", "csrc")
 @pytest.fixture(scope="module")
 def harness(tmp_path_factory):
     exe = str(tmp_path_factory.mktemp("amg") / "amg_harness")
-    subprocess.check_call(["g++", "-O2", "-std=c++17", "-fopenmp", "-I", CSRC, "-o", exe,
+    subprocess.check_call(["g++", "-O3", "-std=c++17", "-fopenmp", "-I", CSRC, "-o", exe,
                            os.path.join(ROOT, "tests", "amg_harness.cpp"), os.path.join(CSRC, "amg_setup.cpp")])
     return exe
 
@@ -78,33 +78,41 @@ def _device_layout(K, conn, nconn):
 def _load_hierarchy(d):
     lines = open(os.path.join(d, "levels.txt")).read().split("\n")
     L, nc = map(int, lines[0].split())
-    levels = []
     rd = lambda name, dt: np.fromfile(os.path.join(d, name), dtype=dt)  # noqa: E731
+
+    def bsr(p, dims):
+        nbr, nbc, R, C = dims
+        if nbr == 0:
+            return None
+        ptr = rd(f"{p}_ptr.bin", np.int64)
+        return sp.bsr_matrix((rd(f"{p}_val.bin", np.float64).reshape(-1, R, C), rd(f"{p}_col.bin", np.int32), ptr),
+                             shape=(nbr * R, nbc * C)).tocsr()
+    levels = []
     for lev in range(L):
-        nblock, bs, omega, prow, pcol = lines[1 + lev].split()
-        nblock, bs, omega, prow, pcol = int(nblock), int(bs), float(omega), int(prow), int(pcol)
-
-        def csr(p, shape):
-            return sp.csr_matrix((rd(f"{p}_val.bin", np.float64), rd(f"{p}_col.bin", np.int32),
-                                  rd(f"{p}_ptr.bin", np.int64)), shape=shape)
-        nd = nblock * bs
-        levels.append(dict(A=csr(f"L{lev}_A", (nd, nd)), P=csr(f"L{lev}_P", (prow, pcol)),
-                           Pt=csr(f"L{lev}_Pt", (pcol, prow)), bs=bs, omega=omega,
+        f = lines[1 + lev].split()
+        nblock, bs, omega = int(f[0]), int(f[1]), float(f[2])
+        dims = [tuple(map(int, f[3 + 4 * k:7 + 4 * k])) for k in range(3)]
+        levels.append(dict(A=bsr(f"L{lev}_A", dims[0]), P=bsr(f"L{lev}_P", dims[1]),
+                           Pt=bsr(f"L{lev}_Pt", dims[2]), bs=bs, omega=omega,
                            Dinv=rd(f"L{lev}_Dinv.bin", np.float64).reshape(nblock, bs, bs)))
-    chol = rd("coarse_chol.bin", np.float64).reshape(nc, nc)
-    return levels, chol
+    coarse = bsr("coarse_A", tuple(map(int, lines[1 + L].split())))
+    return levels, coarse, rd("coarse_chol.bin", np.float64).reshape(nc, nc), rd("coarse_inv.bin", np.float64).reshape(nc, nc)
 
 
-def _vcycle(levels, chol):
+def _vcycle(levels, cinv):
+    """The V-cycle as the device runs it: on every level one damped
+    block-Jacobi sweep from zero, one more sweep, the residual restricted,
+    the coarse correction prolongated, two sweeps; the coarsest level
+    multiplies by the dense inverse."""
     def smooth(lv, x, b):
         r = (b - lv["A"] @ x).reshape(-1, lv["bs"])
         return x + lv["omega"] * np.einsum("nij,nj->ni", lv["Dinv"], r).ravel()
 
     def V(l, b):
         if l == len(levels):
-            return sla.cho_solve((chol, True), b)
+            return cinv @ b
         lv = levels[l]
-        x = smooth(lv, np.zeros_like(b), b)
+        x = lv["omega"] * np.einsum("nij,nj->ni", lv["Dinv"], b.reshape(-1, lv["bs"])).ravel()
         x = smooth(lv, x, b)
         x = x + lv["P"] @ V(l + 1, lv["Pt"] @ (b - lv["A"] @ x))
         x = smooth(lv, x, b)
@@ -143,17 +151,32 @@ def test_hierarchy_preconditions_cg(oracle_mod, harness, tmp_path, lattice, size
                       ("nconn", nconn.astype(np.int32)), ("cols", cols), ("val", val)):
         np.ascontiguousarray(arr).tofile(os.path.join(d, f"{name}.bin"))
     subprocess.check_call([harness, d, "0.6"])
-    levels, chol = _load_hierarchy(d)
+    levels, coarse, chol, cinv = _load_hierarchy(d)
     assert len(levels) >= 1
-    # the level-0 operator is the stiffness with the constrained DOFs removed
-    free = np.repeat(mask[:, None], 3, axis=1) >> np.arange(3) & 1
-    free = free.ravel().astype(bool)
-    A0 = levels[0]["A"]
-    Kf = K[free][:, free]
-    assert abs(A0[free][:, free] - Kf).max() == 0.0
-    assert A0[~free].nnz == 0 or abs(A0[~free]).max() == 0.0
+    free = (np.repeat(mask[:, None], 3, axis=1) >> np.arange(3) & 1).ravel().astype(bool)
+    # level 0 operates with the stiffness, constrained rows and columns removed
+    dfree = sp.diags(free.astype(float))
+    A0 = (dfree @ K @ dfree).tocsr()
+    levels[0]["A"] = A0
+    for lv in levels[1:]:
+        assert abs(lv["A"] - lv["A"].T).max() <= 1e-9 * abs(lv["A"]).max()
+    # Galerkin products: each coarse operator is P^T A P of the level below
+    ops = [lv["A"] for lv in levels] + [coarse]
+    for l, lv in enumerate(levels):
+        assert abs(lv["Pt"] - lv["P"].T).max() == 0.0
+        G = (lv["Pt"] @ ops[l] @ lv["P"]).toarray()
+        Ac = ops[l + 1].toarray()
+        keep = np.abs(np.diag(G)) > 0  # coarse DOFs with a prolongation column
+        assert np.allclose(Ac[np.ix_(keep, keep)], G[np.ix_(keep, keep)], rtol=1e-10, atol=1e-10 * abs(G).max())
+        assert np.all(np.diag(Ac)[~keep] == 1.0)
+    # constrained DOFs receive no prolongation
+    assert abs(levels[0]["P"][~free]).max() == 0.0
+    # the dense coarse factor and inverse
+    assert np.allclose(chol @ chol.T, coarse.toarray() + np.diag((abs(coarse).sum(1).A1 == 0).astype(float)))
+    assert np.allclose(cinv @ (chol @ chol.T), np.eye(len(cinv)), atol=1e-8)
     b = res * free
-    x, it = _pcg(A0, _vcycle(levels, chol), b)
+    x, it = _pcg(A0, _vcycle(levels, cinv), b)
+    Kf = K[free][:, free]
     assert np.linalg.norm(Kf @ x[free] - b[free]) <= 1e-10 * np.linalg.norm(b)
     # block-Jacobi PCG on the same system for reference
     dinv = levels[0]["Dinv"]
