@@ -20,6 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liblpmgpu.so")
 
 PREC_FP64, PREC_MIXED = 0, 1
+PRECOND_BJ, PRECOND_AMG = 0, 1
 PL_J2, PL_CP, PL_PREDICTOR, PL_ELASTIC = 0, 1, 4, 6
 STATUS_NEWTON_MAXIT, STATUS_CG_MAXIT, STATUS_NAN, STATUS_CP_SINGULAR = 1, 2, 4, 8
 
@@ -55,7 +56,8 @@ class SolverOpts(C.Structure):
     _fields_ = [("precision", C.c_int), ("newton_tol", C.c_double), ("newton_maxiter", C.c_int),
                 ("cg_rtol", C.c_double), ("cg_maxiter", C.c_int), ("inner_rtol", C.c_double),
                 ("refine_maxiter", C.c_int), ("check_every", C.c_int), ("use_graphs", C.c_int),
-                ("mixed_vectors", C.c_int), ("newton_accel", C.c_int), ("cg_forcing", C.c_double)]
+                ("mixed_vectors", C.c_int), ("newton_accel", C.c_int), ("cg_forcing", C.c_double),
+                ("preconditioner", C.c_int), ("amg_spacing", C.c_double), ("amg_rebuild", C.c_double)]
 
 
 class Tuning(C.Structure):
@@ -87,7 +89,10 @@ class StepStats(C.Structure):
                 ("spmv_calls", C.c_int), ("status", C.c_int), ("res0", C.c_double),
                 ("reac0", C.c_double), ("res_final", C.c_double), ("ms_stiffness", C.c_double),
                 ("ms_solve", C.c_double), ("ms_force", C.c_double), ("damage_passes", C.c_int),
-                ("bonds_broken", C.c_int)]
+                ("bonds_broken", C.c_int), ("amg_builds", C.c_int), ("ms_amg_build", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class DamageOpts(C.Structure):

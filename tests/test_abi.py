@@ -58,3 +58,31 @@ def test_legacy_library_exports_header():
     assert not missing, missing
     for g in ("xyz", "K_global", "dLp", "J2_alpha", "residual", "nparticle"):
         assert hasattr(hlib, g), g
+
+
+def test_struct_layouts_match_header(gpu_lib, tmp_path):
+    """The ctypes mirrors of the option and statistics structs have the C
+    header's size and field offsets (a field appended on one side only would
+    shift every later one)."""
+    import subprocess
+    structs = {"lpm_solver_opts": gpu_lib.SolverOpts, "lpm_step_stats": gpu_lib.StepStats,
+               "lpm_damage_opts": gpu_lib.DamageOpts, "lpm_adjoint_opts": gpu_lib.AdjointOpts,
+               "lpm_adjoint_stats": gpu_lib.AdjointStats, "lpm_tuning": gpu_lib.Tuning}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "lpm_gpu.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append('printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f, _ in py._fields_:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (cname, f, cname, f))
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.check_call(["gcc", "-std=c11", "-I", INCLUDE, "-o", str(exe), str(src)])
+    got = dict(l.split() for l in subprocess.check_output([str(exe)], text=True).splitlines())
+    for cname, py in structs.items():
+        if cname not in ("lpm_solver_opts", "lpm_adjoint_opts"):  # returned to callers as dicts
+            d = py().as_dict()
+            assert list(d) == [f for f, _ in py._fields_], cname
+        assert int(got[cname]) == C.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert int(got[f"{cname}.{f}"]) == getattr(py, f).offset, (cname, f)
