@@ -117,7 +117,7 @@ class ClockSampler:
                 "sm_max_mhz": max(smax) if smax else None, "reasons": reasons, "samples": len(rows)}
 
 
-def build_specimen(G, case, precision, stream=None):
+def build_specimen(G, case, precision, stream=None, precond=0):
     s = G.Specimen(0)
     if stream is not None:
         s.set_stream(stream)
@@ -130,7 +130,7 @@ def build_specimen(G, case, precision, stream=None):
     s.set_material(c11 * sc, c12 * sc, c44 * sc, case.sigmay, case.H, 0.0, G.PL_J2)
     s.init_state()
     s.set_solver(precision=precision, newton_tol=case.newton_tol, newton_maxiter=100, cg_rtol=1e-10,
-                 cg_maxiter=200000)
+                 cg_maxiter=200000, preconditioner=precond)
     return s, types
 
 
@@ -157,7 +157,8 @@ def run_ours(args):
     for prec_name, prec in (("mixed", G.PREC_MIXED), ("fp64", G.PREC_FP64)):
         if prec_name == "fp64" and args.no_fp64:
             continue
-        s, types = build_specimen(G, case, prec, stream.cuda_stream)
+        precond = G.PRECOND_AMG if args.precond == "amg" else G.PRECOND_BJ
+        s, types = build_specimen(G, case, prec, stream.cuda_stream, precond)
         tuning = None
         for k in range(W):
             s.load_step(cases.sc_bcs(sched[k]))
@@ -209,6 +210,8 @@ def run_ours(args):
         "config": {"workload": f"SC {args.size}^3 elastoplastic cyclic, load steps {W + 1}-{W + K} of "
                                f"{len(sched)} (first yield near step 12)",
                    "particles": mixed["n"], "nnz_blocks": mixed["nnzb"], "precision": "mixed",
+                   "preconditioner": "smoothed-aggregation multigrid V-cycle" if args.precond == "amg"
+                   else "block-Jacobi",
                    "fp64_steps_per_s": fp64_rate, "mixed_over_fp64": (value / fp64_rate) if fp64_rate else None,
                    "disp_err_mixed_vs_fp64": err, "newton_iters": agg("newton_iters"), "cg_iters": agg("cg_iters"),
                    "reliable_updates": agg("refine_iters"),
@@ -222,7 +225,7 @@ def run_ours(args):
                      "kernel": "k_spmv_f (FP32 block-CSR SpMV)", "peak_source": peak_src,
                      "spmv_launches_sampled": mixed["spmv_cnt"]},
         "clocks": mixed["clocks"],
-        "gpu_launches": gpu_launches(mixed["stats"]),
+        "gpu_launches": gpu_launches(mixed["stats"], amg_levels(mixed["n"]) if args.precond == "amg" else 0),
         "e2e": e2e,
         "cpu_baseline": cpu,
     }
@@ -233,14 +236,28 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def gpu_launches(stats):
+def amg_levels(n, coarse_blocks=150):
+    """Levels above the coarsest of the multigrid hierarchy of a cube of n
+    particles (aggregates of 3 x 3 x 3 block rows per level)."""
+    m, levels = round(n ** (1.0 / 3.0)), 0
+    while m ** 3 > coarse_blocks and levels < 8:
+        m, levels = -(-m // 3), levels + 1
+    return levels
+
+
+def gpu_launches(stats, amg=0):
     """Kernel launches of the timed steps (counted from the solver statistics):
     per step 3 (stiffness) + 2 (BC) + 1 (preconditioner) + 2 (predictor);
     per Newton iteration 2 (force) + 1 (xyz update) + 1 (norm);
-    per PCG iteration 3; per reliable update 3."""
+    per PCG iteration 3 with block-Jacobi, 4 + the V-cycle's 7 per level + 1
+    with the multigrid preconditioner (amg = its levels); per reliable update
+    3 (block-Jacobi) or 3 + the V-cycle."""
+    per_it = 3 if not amg else 4 + 7 * amg + 1
+    per_rel = 3 if not amg else 2 + 7 * amg + 1
     total = 0
     for st in stats:
-        total += 8 + 4 * st["newton_iters"] + 3 * st["cg_iters"] + 3 * st["refine_iters"] + st["newton_iters"]
+        total += 8 + 4 * st["newton_iters"] + per_it * st["cg_iters"] + per_rel * st["refine_iters"] + \
+            st["newton_iters"]
     return total
 
 
@@ -646,6 +663,8 @@ def main():
     ap.add_argument("--adj-forcing", type=float, default=0.0,
                     help="adjoint workload: inexact-Newton forcing cap (opts.cg_forcing; 0 = exact solves)")
     ap.add_argument("--adj-fd", action="store_true")
+    ap.add_argument("--precond", default="bj", choices=["bj", "amg"],
+                    help="sc workload: PCG preconditioner (block-Jacobi or the multigrid V-cycle)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -36,6 +36,8 @@ extern "C" {
 
 #define LPM_PREC_FP64 0  /* FP64 stiffness, SpMV and PCG */
 #define LPM_PREC_MIXED 1 /* FP32 stiffness/SpMV/PCG inside FP64 iterative refinement */
+#define LPM_PRECOND_BJ 0  /* block-Jacobi (3 x 3 diagonal blocks), as solverCG's diagonal preconditioner */
+#define LPM_PRECOND_AMG 1 /* smoothed-aggregation multigrid V-cycle (rigid-body modes, FP64 vectors) */
 
 /* constitutive modes (plmode, src/constitutive.c:88-146) */
 #define LPM_PL_J2 0        /* J2 mixed linear hardening */
@@ -84,6 +86,15 @@ typedef struct {
                            tighter than cg_rtol nor than half the Newton target over |r_k|.  The
                            step converges to the same Newton tolerance with far fewer PCG
                            iterations when modified Newton contracts slowly (plastic range). */
+    int preconditioner; /* LPM_PRECOND_BJ (default) or LPM_PRECOND_AMG.  AMG: the PCG runs with FP64
+                           vectors (FP32 stiffness and FP64 reliable updates under LPM_PREC_MIXED) and
+                           a V-cycle of a smoothed-aggregation hierarchy built on the host at the
+                           first solve; it is rebuilt when the constrained DOFs change or a solve
+                           needs more than amg_rebuild times the iterations of the first solve after
+                           the last build.  Single specimens only (batches use block-Jacobi). */
+    double amg_spacing; /* AMG: edge of a level-0 aggregate box; 0 (default) = 6 particle radii
+                           (3 x 3 x 3 nearest-neighbour spacings) */
+    double amg_rebuild; /* AMG: iteration growth that triggers a rebuild (default 2.5) */
 } lpm_solver_opts;
 
 typedef struct {
@@ -96,6 +107,8 @@ typedef struct {
     double ms_stiffness, ms_solve, ms_force;
     int damage_passes;   /* damage stage: Newton passes of the step (1 + re-solves after breaking) */
     int bonds_broken;    /* damage stage: sum of updateDamageGeneral's return values over the passes */
+    int amg_builds;      /* AMG: hierarchy builds during the step */
+    double ms_amg_build; /* AMG: host time of those builds (stiffness download, setup, upload) */
 } lpm_step_stats;
 
 /* ---- context ------------------------------------------------------------ */

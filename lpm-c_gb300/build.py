@@ -36,6 +36,7 @@ CU_UNITS = [
     ("adjoint.cu", []),
     ("k_noalloc.cu", []),
     ("k_damage.cu", ["-fmad=false"]),
+    ("k_amg.cu", ["-Xcompiler", "-fopenmp"]),
 ]
 CPP_UNITS = [("setup.cpp", ["-ffp-contract=off", "-fopenmp"]), ("output.cpp", ["-ffp-contract=off"]),
              ("amg_setup.cpp", ["-O3", "-fopenmp"])]

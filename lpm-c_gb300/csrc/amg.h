@@ -55,10 +55,12 @@ struct AmgOptions {
     int max_levels = 8;
     int coarse_blocks = 150;   // stop coarsening at this many block rows
     int power_iters = 15;      // power iterations for rho(D^-1 A)
+    int max_coarse_dofs = 6000;  // largest coarsest operator factored densely
 };
 
-// Returns the number of levels above the coarsest, or -1 when the coarsest
-// operator is not positive definite.
+// Returns the number of levels above the coarsest; -1 when the coarsest
+// operator is not positive definite, -2 when the coarsest operator would have
+// more than max_coarse_dofs DOFs (the lattice did not coarsen).
 int amg_build(const AmgInput &in, AmgHierarchy &H, const AmgOptions &opt = AmgOptions());
 
 }  // namespace lpm

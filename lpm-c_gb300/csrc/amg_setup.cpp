@@ -662,6 +662,8 @@ int amg_build(const AmgInput &in, AmgHierarchy &H, const AmgOptions &opt)
     // coarsest level: dense Cholesky (lower factor, row-major) and inverse
     const int bs = A.R;
     const int nc = A.nbr * bs;
+    if (nc > opt.max_coarse_dofs)
+        return -2;  // the lattice did not coarsen (aggregate boxes below the particle spacing)
     H.coarse_n = nc;
     H.coarse_chol.assign((size_t)nc * nc, 0.0);
     std::vector<double> &Lc = H.coarse_chol;

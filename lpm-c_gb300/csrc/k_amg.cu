@@ -1,0 +1,718 @@
+// Smoothed-aggregation multigrid V-cycle as the preconditioner of the PCG
+// that replaces the reference's CG (src/solver.c:188-270), and the PCG steps
+// around it.  The hierarchy is built on the host (amg_setup.cpp) and kept on
+// the device (AmgDev).
+//
+// V-cycle on level l (operator A_l, block-Jacobi inverse D_l^-1, damping
+// omega_l = 1 / rho(D_l^-1 A_l)):
+//     x = omega D^-1 b                      (first sweep from zero)
+//     y = x + omega D^-1 (b - A x)          (second sweep)
+//     x = b - A y                           (residual)
+//     b_{l+1} = P_l^T x                     (restriction)
+//     e = V-cycle_{l+1}(b_{l+1})            (dense inverse on the coarsest level)
+//     y += P_l e                            (prolongation)
+//     x = y + omega D^-1 (b - A y);  y = x + omega D^-1 (b - A x)
+// so the result is in y.  Two Jacobi sweeps before and two after make the
+// cycle a symmetric positive definite operator, as CG needs.  On level 0 the
+// operator is the stiffness (FP64 Kd, or FP32 Kf under mixed precision, with
+// the products in FP32 as in the mixed SpMV), b is the CG residual r, x the
+// scratch vector q (free between the update and the next product) and y the
+// preconditioned residual z; the DOF mask zeroes the constrained DOFs of
+// every level-0 output.
+//
+// PCG iteration: q = K p (with p.q and alpha, k_spmv), x += alpha p and
+// r -= alpha q (k_amg_update, |r|^2 and the convergence test), z = V(r),
+// r.z and beta (k_amg_rz), p = z + beta p (k_cg_p in k_solve.cu).  Every
+// kernel returns at once when the solve is marked done, so a CUDA graph of a
+// whole chunk of iterations stays valid after convergence.  Reductions are
+// deterministic (per-block partials, summed in a fixed order by the last
+// block).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <omp.h>
+#include "amg.h"
+#include "lpm_internal.h"
+
+namespace lpm {
+
+constexpr int ATPB = 256;
+
+__device__ __forceinline__ double amg_warp_sum(double s)
+{
+    for (int o = 16; o > 0; o >>= 1)
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+    return s;
+}
+
+// Block partials of NV values, the last block sums them in block order and
+// calls fin(totals) on its thread 0.  Every thread of the grid calls it.
+template <int NV, typename Fin>
+__device__ void amg_reduce(double (&v)[NV], double *partials, unsigned *counter, Fin fin)
+{
+    __shared__ double red[NV][ATPB / 32];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+        const double s = amg_warp_sum(v[k]);
+        if (lane == 0)
+            red[k][wid] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            double s = 0.0;
+            for (int w = 0; w < ATPB / 32; w++)
+                s += red[k][w];
+            partials[(size_t)k * gridDim.x + blockIdx.x] = s;
+        }
+        __threadfence();
+        last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last)
+        return;
+    __threadfence();
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+        double s = 0.0;
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += ATPB)
+            s += __ldcg(&partials[(size_t)k * gridDim.x + b]);
+        s = amg_warp_sum(s);
+        if (lane == 0)
+            red[k][wid] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tot[NV];
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            double s = 0.0;
+            for (int w = 0; w < ATPB / 32; w++)
+                s += red[k][w];
+            tot[k] = s;
+        }
+        fin(tot);
+        *counter = 0u;
+    }
+}
+
+__device__ __forceinline__ dvec4 amg_mask(dvec4 v, uint8_t m)
+{
+    return make_dvec4((m & 1) ? v.x : 0.0, (m & 2) ? v.y : 0.0, (m & 4) ? v.z : 0.0, 0.0);
+}
+
+// z = P^-1 r with the level-0 3x3 block inverses stored [9][n]
+__device__ __forceinline__ dvec4 amg_pinv(const double *P, int n, int i, dvec4 r)
+{
+    return make_dvec4(P[(size_t)0 * n + i] * r.x + P[(size_t)1 * n + i] * r.y + P[(size_t)2 * n + i] * r.z,
+                      P[(size_t)3 * n + i] * r.x + P[(size_t)4 * n + i] * r.y + P[(size_t)5 * n + i] * r.z,
+                      P[(size_t)6 * n + i] * r.x + P[(size_t)7 * n + i] * r.y + P[(size_t)8 * n + i] * r.z, 0.0);
+}
+
+struct AmgVec {
+    int n;
+    const uint8_t *mask;
+    double *partials;
+    unsigned *counter;
+    CgScalars *sc;
+};
+
+// ---- PCG steps ------------------------------------------------------------------
+
+// x = 0, r = mask(b) * scale, |r|^2, tolerance, counters
+__global__ void __launch_bounds__(ATPB) k_amg_init(AmgVec a, const dvec4 *b, double scale, dvec4 *x, dvec4 *r,
+                                                   double rtol, int maxit, double delta2)
+{
+    double v[1] = {0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
+        dvec4 bb = amg_mask(b[i], a.mask[i]);
+        bb.x *= scale;
+        bb.y *= scale;
+        bb.z *= scale;
+        x[i] = make_dvec4(0.0, 0.0, 0.0, 0.0);
+        r[i] = bb;
+        v[0] += bb.x * bb.x + bb.y * bb.y + bb.z * bb.z;
+    }
+    CgScalars *sc = a.sc;
+    amg_reduce<1>(v, a.partials, a.counter, [sc, rtol, maxit, delta2](const double *t) {
+        sc->rz = 0.0;
+        sc->rz_old = 0.0;
+        sc->rr = t[0];
+        sc->rr_max = t[0];
+        sc->bnorm2 = t[0];
+        sc->tol2 = rtol * rtol * t[0];
+        sc->upd_delta2 = delta2;
+        sc->it = 0;
+        sc->maxit = maxit;
+        sc->done = (t[0] <= sc->tol2 || !(t[0] == t[0])) ? 1 : 0;
+        sc->alpha = 0.0;
+        sc->beta = 0.0;
+        sc->upd_req = 0;
+    });
+}
+
+// x += alpha p, r -= alpha q, |r|^2 and the convergence test
+__global__ void __launch_bounds__(ATPB) k_amg_update(AmgVec a, dvec4 *x, dvec4 *r, const dvec4 *p,
+                                                     const dvec4 *q)
+{
+    CgScalars *sc = a.sc;
+    if (sc->done)
+        return;
+    const double al = sc->alpha;
+    double v[1] = {0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
+        dvec4 xv = x[i], rv = r[i];
+        const dvec4 pv = p[i], qv = q[i];
+        xv.x += al * pv.x;
+        xv.y += al * pv.y;
+        xv.z += al * pv.z;
+        rv.x -= al * qv.x;
+        rv.y -= al * qv.y;
+        rv.z -= al * qv.z;
+        x[i] = xv;
+        r[i] = rv;
+        v[0] += rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
+    }
+    amg_reduce<1>(v, a.partials, a.counter, [sc](const double *t) {
+        sc->rr = t[0];
+        sc->it += 1;
+        if (t[0] <= sc->tol2)
+            sc->done = 1;
+        else if (!(t[0] == t[0]))
+            sc->done = 3;
+        else if (sc->it >= sc->maxit)
+            sc->done = 2;
+        else if (t[0] < sc->upd_delta2 * sc->rr_max)
+            sc->upd_req = 1;  // raised as done = 4 once p is updated (k_cg_p)
+        if (t[0] > sc->rr_max)
+            sc->rr_max = t[0];
+    });
+}
+
+// Reliable update: r = mask(rtrue) (the FP64 true residual in the units of
+// the iteration), |r|^2; the search direction is kept.
+__global__ void __launch_bounds__(ATPB) k_amg_reliable(AmgVec a, const dvec4 *rtrue, dvec4 *r)
+{
+    double v[1] = {0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
+        const dvec4 rv = amg_mask(rtrue[i], a.mask[i]);
+        r[i] = rv;
+        v[0] += rv.x * rv.x + rv.y * rv.y + rv.z * rv.z;
+    }
+    CgScalars *sc = a.sc;
+    amg_reduce<1>(v, a.partials, a.counter, [sc](const double *t) {
+        sc->rr = t[0];
+        sc->rr_max = t[0];
+        sc->done = !(t[0] == t[0]) ? 3 : 0;
+        sc->upd_req = 0;
+    });
+}
+
+enum { RZ_INIT = 0, RZ_ITER = 1, RZ_RELIABLE = 2 };
+
+// r.z after the V-cycle: INIT also sets p = z; ITER sets beta
+template <int MODE>
+__global__ void __launch_bounds__(ATPB) k_amg_rz(AmgVec a, const dvec4 *r, const dvec4 *z, dvec4 *p)
+{
+    CgScalars *sc = a.sc;
+    if (sc->done)
+        return;
+    double v[1] = {0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
+        const dvec4 rv = r[i], zv = z[i];
+        if (MODE == RZ_INIT)
+            p[i] = zv;
+        v[0] += rv.x * zv.x + rv.y * zv.y + rv.z * zv.z;
+    }
+    amg_reduce<1>(v, a.partials, a.counter, [sc](const double *t) {
+        if (MODE == RZ_INIT) {
+            sc->rz = t[0];
+            sc->rz_old = t[0];
+        } else if (MODE == RZ_ITER) {
+            sc->rz_old = sc->rz;
+            sc->rz = t[0];
+            sc->beta = (sc->rz_old != 0.0) ? t[0] / sc->rz_old : 0.0;
+        } else {
+            sc->rz = t[0];
+        }
+    });
+}
+
+// ---- level 0: the stiffness ---------------------------------------------------
+
+constexpr int L0_LANES = 16;  // lanes per block row of the stiffness
+
+enum { SM_SMOOTH = 0, SM_RESID = 1 };
+
+// MODE SM_SMOOTH: out = x + omega Pinv mask(b - K x); SM_RESID: out = mask(b - K x).
+// Half a warp per block row, lanes over the row's blocks (padding included:
+// zero values, column of the row itself); products in V as the SpMV of the
+// same precision, epilogue in FP64.
+template <typename V, int MODE>
+__global__ void __launch_bounds__(ATPB) k_amg_k0(int n, const long long *__restrict__ rowoff,
+                                                 const int *__restrict__ npad, const int *__restrict__ cols,
+                                                 const uint8_t *__restrict__ mask, const V *__restrict__ val,
+                                                 const double *__restrict__ Pinv, double omega,
+                                                 const dvec4 *__restrict__ x, const dvec4 *__restrict__ b,
+                                                 dvec4 *__restrict__ out, const CgScalars *sc)
+{
+    if (sc && sc->done)
+        return;
+    const int sub = threadIdx.x & (L0_LANES - 1);
+    const unsigned gmask = 0xffffu << ((threadIdx.x & 31) & ~(L0_LANES - 1));
+    const int g = (blockIdx.x * blockDim.x + threadIdx.x) / L0_LANES;
+    const int ng = (gridDim.x * blockDim.x) / L0_LANES;
+    for (int row = g; row < n; row += ng) {
+        const long long off = rowoff[row];
+        const int np = npad[row];
+        const V *vr = val + 9 * off;
+        V y0 = 0, y1 = 0, y2 = 0;
+        for (int k = sub; k < np; k += L0_LANES) {
+            const int j = cols[off + k];
+            const dvec4 xv = x[j];
+            const V x0 = (V)xv.x, x1 = (V)xv.y, x2 = (V)xv.z;
+            y0 += vr[(size_t)0 * np + k] * x0 + vr[(size_t)1 * np + k] * x1 + vr[(size_t)2 * np + k] * x2;
+            y1 += vr[(size_t)3 * np + k] * x0 + vr[(size_t)4 * np + k] * x1 + vr[(size_t)5 * np + k] * x2;
+            y2 += vr[(size_t)6 * np + k] * x0 + vr[(size_t)7 * np + k] * x1 + vr[(size_t)8 * np + k] * x2;
+        }
+#pragma unroll
+        for (int o = L0_LANES / 2; o > 0; o >>= 1) {
+            y0 += __shfl_xor_sync(gmask, y0, o);
+            y1 += __shfl_xor_sync(gmask, y1, o);
+            y2 += __shfl_xor_sync(gmask, y2, o);
+        }
+        if (sub == 0) {
+            const uint8_t m = mask[row];
+            const dvec4 bb = b[row];
+            const dvec4 rr = amg_mask(make_dvec4(bb.x - (double)y0, bb.y - (double)y1, bb.z - (double)y2, 0.0), m);
+            if (MODE == SM_RESID) {
+                out[row] = rr;
+            } else {
+                const dvec4 d = amg_pinv(Pinv, n, row, rr);
+                const dvec4 xo = x[row];
+                out[row] = amg_mask(
+                    make_dvec4(xo.x + omega * d.x, xo.y + omega * d.y, xo.z + omega * d.z, 0.0), m);
+            }
+        }
+    }
+}
+
+// out = omega Pinv mask(b): the first sweep from zero on level 0
+__global__ void __launch_bounds__(ATPB) k_amg_jacobi0(int n, const uint8_t *__restrict__ mask,
+                                                      const double *__restrict__ Pinv, double omega,
+                                                      const dvec4 *__restrict__ b, dvec4 *__restrict__ out,
+                                                      const CgScalars *sc)
+{
+    if (sc && sc->done)
+        return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint8_t m = mask[i];
+        const dvec4 d = amg_pinv(Pinv, n, i, amg_mask(b[i], m));
+        out[i] = amg_mask(make_dvec4(omega * d.x, omega * d.y, omega * d.z, 0.0), m);
+    }
+}
+
+// ---- block-CSR levels -------------------------------------------------------------
+
+constexpr int BL_LANES = 8;  // lanes per block row of the coarse-level kernels
+
+enum { BM_SET = 0, BM_ADD = 1, BM_SMOOTH = 2, BM_RESID = 3 };
+
+// y = sum over the row's R x C blocks of blk * x[col] (x: C values of block
+// column j at x[j * SX]); then
+//   BM_SET:    out[row * SY + r] = y_r            (restriction)
+//   BM_ADD:    out[row * SY + r] += y_r           (prolongation)
+//   BM_SMOOTH: out = x_row + omega Dinv (b - y)   (R = C = 6, SX = SY = 6)
+//   BM_RESID:  out = b - y                        (R = C = 6)
+template <int R, int C, int MODE>
+__global__ void __launch_bounds__(ATPB) k_amg_bsr(int nbr, const long long *__restrict__ ptr,
+                                                  const int *__restrict__ col, const double *__restrict__ val,
+                                                  const double *__restrict__ x, int SX, double *__restrict__ out,
+                                                  int SY, const double *__restrict__ b,
+                                                  const double *__restrict__ dinv, double omega,
+                                                  const CgScalars *sc)
+{
+    if (sc && sc->done)
+        return;
+    const int sub = threadIdx.x & (BL_LANES - 1);
+    const unsigned gmask = 0xffu << ((threadIdx.x & 31) & ~(BL_LANES - 1));
+    const int g = (blockIdx.x * blockDim.x + threadIdx.x) / BL_LANES;
+    const int ng = (gridDim.x * blockDim.x) / BL_LANES;
+    for (int row = g; row < nbr; row += ng) {
+        double y[R];
+#pragma unroll
+        for (int r = 0; r < R; r++)
+            y[r] = 0.0;
+        for (long long k = ptr[row] + sub; k < ptr[row + 1]; k += BL_LANES) {
+            const double *blk = val + (size_t)k * (R * C);
+            const double *xc = x + (size_t)col[k] * SX;
+            double xv[C];
+#pragma unroll
+            for (int c = 0; c < C; c++)
+                xv[c] = xc[c];
+#pragma unroll
+            for (int r = 0; r < R; r++)
+#pragma unroll
+                for (int c = 0; c < C; c++)
+                    y[r] += blk[r * C + c] * xv[c];
+        }
+#pragma unroll
+        for (int o = BL_LANES / 2; o > 0; o >>= 1)
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                y[r] += __shfl_xor_sync(gmask, y[r], o);
+        if (sub != 0)
+            continue;
+        double *o = out + (size_t)row * SY;
+        if constexpr (MODE == BM_SET) {
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                o[r] = y[r];
+        } else if constexpr (MODE == BM_ADD) {
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                o[r] += y[r];
+        } else {
+            static_assert(R == 6 && C == 6, "operator rows are 6 x 6");
+            double rr[R];
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                rr[r] = b[(size_t)row * R + r] - y[r];
+            if constexpr (MODE == BM_RESID) {
+#pragma unroll
+                for (int r = 0; r < R; r++)
+                    o[r] = rr[r];
+            } else {
+                const double *D = dinv + (size_t)row * (R * R);
+                const double *xr = x + (size_t)row * SX;
+#pragma unroll
+                for (int r = 0; r < R; r++) {
+                    double s = 0.0;
+#pragma unroll
+                    for (int c = 0; c < R; c++)
+                        s += D[r * R + c] * rr[c];
+                    o[r] = xr[r] + omega * s;
+                }
+            }
+        }
+    }
+}
+
+// out = omega Dinv b on a 6-DOF level: the first sweep from zero
+__global__ void __launch_bounds__(ATPB) k_amg_jacobi6(int nb, const double *__restrict__ dinv, double omega,
+                                                      const double *__restrict__ b, double *__restrict__ out,
+                                                      const CgScalars *sc)
+{
+    if (sc && sc->done)
+        return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += gridDim.x * blockDim.x) {
+        const double *D = dinv + (size_t)i * 36;
+        double bv[6];
+#pragma unroll
+        for (int c = 0; c < 6; c++)
+            bv[c] = b[(size_t)i * 6 + c];
+#pragma unroll
+        for (int r = 0; r < 6; r++) {
+            double s = 0.0;
+#pragma unroll
+            for (int c = 0; c < 6; c++)
+                s += D[r * 6 + c] * bv[c];
+            out[(size_t)i * 6 + r] = omega * s;
+        }
+    }
+}
+
+// Coarsest level: out = Cinv b (dense, nc x nc), one warp per output entry.
+// Entry k of a vector lives at (k / B) * S + k % B (B DOFs per block row,
+// stride S: 6/6 above level 0, 3/4 when level 0 is the coarsest).
+__global__ void __launch_bounds__(ATPB) k_amg_dense(int nc, const double *__restrict__ Cinv,
+                                                    const double *__restrict__ b, double *__restrict__ out, int B,
+                                                    int S, const CgScalars *sc)
+{
+    if (sc && sc->done)
+        return;
+    const int lane = threadIdx.x & 31;
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int k = w; k < nc; k += nw) {
+        const double *row = Cinv + (size_t)k * nc;
+        double s = 0.0;
+        for (int j = lane; j < nc; j += 32)
+            s += row[j] * b[(size_t)(j / B) * S + j % B];
+        s = amg_warp_sum(s);
+        if (lane == 0)
+            out[(size_t)(k / B) * S + k % B] = s;
+    }
+}
+
+// ---- launchers ----------------------------------------------------------------------
+
+static int grid_for(const Ctx &c, long long rows_x_threads)
+{
+    const long long blocks = (rows_x_threads + ATPB - 1) / ATPB;
+    const long long cap = (long long)std::max(1, c.tune.sms) * 16;
+    return (int)std::max(1LL, std::min(blocks, cap));
+}
+
+static AmgVec amg_vec(Ctx &c) { return AmgVec{c.n, c.mask, c.partials, c.counter, c.sc}; }
+
+static void k0_launch(Ctx &c, bool k32, int mode, double omega, const dvec4 *x, const dvec4 *b, dvec4 *out)
+{
+    const int g = grid_for(c, (long long)c.n * L0_LANES);
+    if (k32) {
+        if (mode == SM_SMOOTH)
+            k_amg_k0<float, SM_SMOOTH><<<g, ATPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.mask, c.Kf,
+                                                                 c.Pinv_d, omega, x, b, out, c.sc);
+        else
+            k_amg_k0<float, SM_RESID><<<g, ATPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.mask, c.Kf,
+                                                                c.Pinv_d, omega, x, b, out, c.sc);
+    } else {
+        if (mode == SM_SMOOTH)
+            k_amg_k0<double, SM_SMOOTH><<<g, ATPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.mask, c.Kd,
+                                                                  c.Pinv_d, omega, x, b, out, c.sc);
+        else
+            k_amg_k0<double, SM_RESID><<<g, ATPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.mask, c.Kd,
+                                                                 c.Pinv_d, omega, x, b, out, c.sc);
+    }
+}
+
+template <int R, int C, int MODE>
+static void bsr_launch(Ctx &c, int nbr, const long long *ptr, const int *col, const double *val, const double *x,
+                       int SX, double *out, int SY, const double *b = nullptr, const double *dinv = nullptr,
+                       double omega = 0.0)
+{
+    const int g = grid_for(c, (long long)nbr * BL_LANES);
+    k_amg_bsr<R, C, MODE><<<g, ATPB, 0, c.stream>>>(nbr, ptr, col, val, x, SX, out, SY, b, dinv, omega, c.sc);
+}
+
+void launch_amg_vcycle(Ctx &c, const dvec4 *r, dvec4 *z, dvec4 *tmp, bool k32)
+{
+    AmgDev &H = *c.amg;
+    const int L = (int)H.lv.size();
+    const int gd = grid_for(c, (long long)H.nc * 32);
+    if (L == 0) {
+        // level 0 is the coarsest: z = Cinv r over the 3 DOFs of each particle
+        k_amg_dense<<<gd, ATPB, 0, c.stream>>>(H.nc, H.cinv, (const double *)r, (double *)z, 3, 4, c.sc);
+        return;
+    }
+    // down
+    for (int l = 0; l < L; l++) {
+        AmgDevLevel &v = H.lv[l];
+        double *bnext = (l + 1 < L) ? H.lv[l + 1].b : H.cb;
+        if (l == 0) {
+            k_amg_jacobi0<<<grid_for(c, c.n), ATPB, 0, c.stream>>>(c.n, c.mask, c.Pinv_d, v.omega, r, tmp, c.sc);
+            k0_launch(c, k32, SM_SMOOTH, v.omega, tmp, r, z);
+            k0_launch(c, k32, SM_RESID, v.omega, z, r, tmp);
+            bsr_launch<6, 3, BM_SET>(c, v.nnext, v.pt_ptr, v.pt_col, v.pt_val, (const double *)tmp, 4, bnext, 6);
+        } else {
+            k_amg_jacobi6<<<grid_for(c, v.nb), ATPB, 0, c.stream>>>(v.nb, v.dinv, v.omega, v.b, v.x, c.sc);
+            bsr_launch<6, 6, BM_SMOOTH>(c, v.nb, v.a_ptr, v.a_col, v.a_val, v.x, 6, v.y, 6, v.b, v.dinv, v.omega);
+            bsr_launch<6, 6, BM_RESID>(c, v.nb, v.a_ptr, v.a_col, v.a_val, v.y, 6, v.x, 6, v.b);
+            bsr_launch<6, 6, BM_SET>(c, v.nnext, v.pt_ptr, v.pt_col, v.pt_val, v.x, 6, bnext, 6);
+        }
+    }
+    k_amg_dense<<<gd, ATPB, 0, c.stream>>>(H.nc, H.cinv, H.cb, H.cx, 6, 6, c.sc);
+    // up
+    for (int l = L - 1; l >= 0; l--) {
+        AmgDevLevel &v = H.lv[l];
+        const double *e = (l + 1 < L) ? H.lv[l + 1].y : H.cx;
+        if (l == 0) {
+            bsr_launch<3, 6, BM_ADD>(c, v.nb, v.p_ptr, v.p_col, v.p_val, e, 6, (double *)z, 4);
+            k0_launch(c, k32, SM_SMOOTH, v.omega, z, r, tmp);
+            k0_launch(c, k32, SM_SMOOTH, v.omega, tmp, r, z);
+        } else {
+            bsr_launch<6, 6, BM_ADD>(c, v.nb, v.p_ptr, v.p_col, v.p_val, e, 6, v.y, 6);
+            bsr_launch<6, 6, BM_SMOOTH>(c, v.nb, v.a_ptr, v.a_col, v.a_val, v.y, 6, v.x, 6, v.b, v.dinv, v.omega);
+            bsr_launch<6, 6, BM_SMOOTH>(c, v.nb, v.a_ptr, v.a_col, v.a_val, v.x, 6, v.y, 6, v.b, v.dinv, v.omega);
+        }
+    }
+}
+
+void launch_amg_init(Ctx &c, const dvec4 *b, double scale, double delta2)
+{
+    const bool k32 = c.opts.precision == LPM_PREC_MIXED;
+    k_amg_init<<<red_grid(c), ATPB, 0, c.stream>>>(amg_vec(c), b, scale, c.x_d, c.r_d, solve_rtol(c),
+                                                   c.opts.cg_maxiter, delta2);
+    launch_amg_vcycle(c, c.r_d, c.z_d, c.q_d, k32);
+    k_amg_rz<RZ_INIT><<<red_grid(c), ATPB, 0, c.stream>>>(amg_vec(c), c.r_d, c.z_d, c.p_d);
+}
+
+void launch_amg_iter(Ctx &c, bool k32)
+{
+    if (k32)
+        launch_spmv_fx(c, c.p_d, c.q_d, true, true);
+    else
+        launch_spmv_d(c, c.p_d, c.q_d, true, true);
+    const int g = red_grid(c);
+    k_amg_update<<<g, ATPB, 0, c.stream>>>(amg_vec(c), c.x_d, c.r_d, c.p_d, c.q_d);
+    launch_amg_vcycle(c, c.r_d, c.z_d, c.q_d, k32);
+    k_amg_rz<RZ_ITER><<<g, ATPB, 0, c.stream>>>(amg_vec(c), c.r_d, c.z_d, c.p_d);
+    launch_cg_p_d(c);
+}
+
+void launch_amg_reliable(Ctx &c, const dvec4 *rtrue)
+{
+    const bool k32 = c.opts.precision == LPM_PREC_MIXED;
+    k_amg_reliable<<<red_grid(c), ATPB, 0, c.stream>>>(amg_vec(c), rtrue, c.r_d);
+    launch_amg_vcycle(c, c.r_d, c.z_d, c.q_d, k32);
+    k_amg_rz<RZ_RELIABLE><<<red_grid(c), ATPB, 0, c.stream>>>(amg_vec(c), c.r_d, c.z_d, c.p_d);
+}
+
+// ---- hierarchy on the device -------------------------------------------------------
+
+template <typename T>
+static int amg_alloc_copy(T *&d, const T *h, size_t count)
+{
+    if (count == 0)
+        return LPM_OK;
+    LPM_CUDA(cudaMalloc((void **)&d, sizeof(T) * count));
+    if (h)
+        LPM_CUDA(cudaMemcpy(d, h, sizeof(T) * count, cudaMemcpyHostToDevice));
+    return LPM_OK;
+}
+
+static void amg_free_device(AmgDev &H)
+{
+    for (AmgDevLevel &v : H.lv) {
+        void *ps[] = {v.a_ptr, v.a_col, v.a_val, v.dinv, v.p_ptr, v.p_col, v.p_val,
+                      v.pt_ptr, v.pt_col, v.pt_val, v.b, v.x, v.y};
+        for (void *p : ps)
+            if (p)
+                cudaFree(p);
+    }
+    H.lv.clear();
+    void *ps[] = {H.cinv, H.cb, H.cx};
+    for (void *p : ps)
+        if (p)
+            cudaFree(p);
+    H.cinv = H.cb = H.cx = nullptr;
+    H.nc = H.cbs = 0;
+}
+
+void free_amg(Ctx &c)
+{
+    if (!c.amg)
+        return;
+    amg_free_device(*c.amg);
+    delete c.amg;
+    c.amg = nullptr;
+}
+
+static int amg_upload(AmgDev &H, const AmgHierarchy &h)
+{
+    int rc;
+    const int L = (int)h.levels.size();
+    H.lv.assign(L, AmgDevLevel());
+    for (int l = 0; l < L; l++) {
+        const AmgLevel &s = h.levels[l];
+        AmgDevLevel &v = H.lv[l];
+        v.nb = s.nblock;
+        v.bs = s.bs;
+        v.nnext = s.P.nbc;
+        v.omega = s.omega;
+        if ((rc = amg_alloc_copy(v.p_ptr, s.P.ptr.data(), s.P.ptr.size())) ||
+            (rc = amg_alloc_copy(v.p_col, s.P.col.data(), s.P.col.size())) ||
+            (rc = amg_alloc_copy(v.p_val, s.P.val.data(), s.P.val.size())) ||
+            (rc = amg_alloc_copy(v.pt_ptr, s.Pt.ptr.data(), s.Pt.ptr.size())) ||
+            (rc = amg_alloc_copy(v.pt_col, s.Pt.col.data(), s.Pt.col.size())) ||
+            (rc = amg_alloc_copy(v.pt_val, s.Pt.val.data(), s.Pt.val.size())))
+            return rc;
+        if (l > 0) {
+            if ((rc = amg_alloc_copy(v.a_ptr, s.A.ptr.data(), s.A.ptr.size())) ||
+                (rc = amg_alloc_copy(v.a_col, s.A.col.data(), s.A.col.size())) ||
+                (rc = amg_alloc_copy(v.a_val, s.A.val.data(), s.A.val.size())) ||
+                (rc = amg_alloc_copy(v.dinv, s.Dinv.data(), s.Dinv.size())) ||
+                (rc = amg_alloc_copy<double>(v.b, nullptr, 6 * (size_t)s.nblock)) ||
+                (rc = amg_alloc_copy<double>(v.x, nullptr, 6 * (size_t)s.nblock)) ||
+                (rc = amg_alloc_copy<double>(v.y, nullptr, 6 * (size_t)s.nblock)))
+                return rc;
+        }
+    }
+    H.nc = h.coarse_n;
+    H.cbs = h.coarse_A.R;
+    if ((rc = amg_alloc_copy(H.cinv, h.coarse_inv.data(), h.coarse_inv.size())) ||
+        (rc = amg_alloc_copy<double>(H.cb, nullptr, (size_t)H.nc)) ||
+        (rc = amg_alloc_copy<double>(H.cx, nullptr, (size_t)H.nc)))
+        return rc;
+    return LPM_OK;
+}
+
+int amg_prepare(Ctx &c)
+{
+    const int n = c.n;
+    if (!c.amg)
+        c.amg = new AmgDev();
+    AmgDev &H = *c.amg;
+    std::vector<uint8_t> mask(n);
+    LPM_CUDA(cudaMemcpyAsync(mask.data(), c.mask, n, cudaMemcpyDeviceToHost, c.stream));
+    int rc = sync(c);
+    if (rc)
+        return rc;
+    if (H.builds > 0 && !H.stale && mask == H.mask_h)
+        return LPM_OK;
+    const auto t0 = std::chrono::steady_clock::now();
+    // the current stiffness in FP64 on the host
+    const bool k32 = c.opts.precision == LPM_PREC_MIXED;
+    const size_t nv = 9 * (size_t)c.nblk;
+    hvec<double> val(nv);
+    if (k32) {
+        hvec<float> vf(nv);
+        LPM_CUDA(cudaMemcpyAsync(vf.data(), c.Kf, nv * sizeof(float), cudaMemcpyDeviceToHost, c.stream));
+        if ((rc = sync(c)))
+            return rc;
+#pragma omp parallel for schedule(static)
+        for (long long k = 0; k < (long long)nv; k++)
+            val[k] = (double)vf[k];
+    } else {
+        LPM_CUDA(cudaMemcpyAsync(val.data(), c.Kd, nv * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        if ((rc = sync(c)))
+            return rc;
+    }
+    const HostSetup &hs = c.hs;
+    AmgInput in;
+    in.n = n;
+    in.xyz = hs.xyz.data();
+    in.mask = mask.data();
+    in.rowoff = hs.rowoff.data();
+    in.npad = hs.npad.data();
+    in.nconn = hs.nconn.data();
+    in.cols = hs.cols.data();
+    in.val = val.data();
+    AmgOptions opt;
+    opt.agg_spacing = c.opts.amg_spacing > 0.0 ? c.opts.amg_spacing : 6.0 * hs.radius;
+    AmgHierarchy h;
+    const int nl = amg_build(in, h, opt);
+    if (nl == -2)
+        return fail(LPM_ERR_ARG, "multigrid: the lattice does not coarsen with this aggregate spacing");
+    if (nl < 0)
+        return fail(LPM_ERR_ARG, "multigrid: the coarsest operator is not positive definite (singular stiffness)");
+    // the captured PCG graphs hold the old hierarchy's pointers
+    if (c.graph_fp64) {
+        cudaGraphExecDestroy(c.graph_fp64);
+        c.graph_fp64 = nullptr;
+    }
+    if (c.graph_fp32) {
+        cudaGraphExecDestroy(c.graph_fp32);
+        c.graph_fp32 = nullptr;
+    }
+    amg_free_device(H);
+    if ((rc = amg_upload(H, h))) {
+        amg_free_device(H);
+        H.builds = 0;
+        return rc;
+    }
+    H.mask_h.swap(mask);
+    H.stale = false;
+    H.ref_iters = -1;
+    H.builds++;
+    H.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (c.trace)
+        std::fprintf(stderr, "lpm: multigrid build %d: %d levels + coarsest %d DOFs, %.1f ms\n", H.builds,
+                     (int)H.lv.size(), H.nc, H.build_ms);
+    return LPM_OK;
+}
+
+}  // namespace lpm

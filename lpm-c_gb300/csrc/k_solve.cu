@@ -732,6 +732,12 @@ void launch_cg_iter_d(Ctx &c)
     k_cg_p<double, dvec4><<<g, VTPB, 0, c.stream>>>(c.n, c.sc, c.z_d, c.p_d, c.counter);
 }
 
+// p = z + beta p on the FP64 vectors (the multigrid PCG, k_amg.cu)
+void launch_cg_p_d(Ctx &c)
+{
+    k_cg_p<double, dvec4><<<red_grid(c), VTPB, 0, c.stream>>>(c.n, c.sc, c.z_d, c.p_d, c.counter);
+}
+
 void launch_cg_iter_f(Ctx &c)
 {
     launch_spmv_f(c, c.p_f, c.q_f, true, true);

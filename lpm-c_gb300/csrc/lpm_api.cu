@@ -143,6 +143,7 @@ Ctx::~Ctx()
     free_adjoint(*this);
     free_anderson(*this);
     free_damage(*this);
+    free_amg(*this);
     void **all[] = {(void **)&xyz, (void **)&xyz0, (void **)&xyz_temp, (void **)&Pin, (void **)&Pex,
                     (void **)&res, (void **)&du, (void **)&mask, (void **)&type, (void **)&G, (void **)&sy,
                     (void **)&Hh, (void **)&stress, (void **)&strain, (void **)&dlambda, (void **)&nbr, (void **)&shell,
@@ -394,6 +395,7 @@ static int setup_common(Ctx &c, bool built = false)
     free_adjoint(c);
     free_anderson(c);
     free_damage(c);
+    free_amg(c);
     drop_graphs(c);
     dfree(c.Kf);
     dfree(c.Kd);
@@ -443,6 +445,9 @@ void lpm_default_solver_opts(lpm_solver_opts *o)
     o->mixed_vectors = 32;
     o->newton_accel = 0;
     o->cg_forcing = 0.0;
+    o->preconditioner = LPM_PRECOND_BJ;
+    o->amg_spacing = 0.0;
+    o->amg_rebuild = 2.5;
 }
 
 int lpm_create(lpm_ctx **out, int device)
@@ -507,10 +512,14 @@ int lpm_set_solver(lpm_ctx *ctx, const lpm_solver_opts *o)
     if (o->precision != LPM_PREC_FP64 && o->precision != LPM_PREC_MIXED)
         return fail(LPM_ERR_ARG, "unknown precision");
     if (!(o->cg_rtol > 0) || o->cg_maxiter <= 0 || o->newton_maxiter < 0 || o->check_every <= 0 ||
-        o->newton_accel < 0 || o->newton_accel > 16 || !(o->cg_forcing >= 0.0 && o->cg_forcing < 1.0))
+        o->newton_accel < 0 || o->newton_accel > 16 || !(o->cg_forcing >= 0.0 && o->cg_forcing < 1.0) ||
+        (o->preconditioner != LPM_PRECOND_BJ && o->preconditioner != LPM_PRECOND_AMG) ||
+        !(o->amg_spacing >= 0.0) || !(o->amg_rebuild > 1.0))
         return fail(LPM_ERR_ARG, "invalid solver options");
     Ctx &c = ctx->c;
     const bool prec_change = c.opts.precision != o->precision;
+    if (c.amg && c.opts.amg_spacing != o->amg_spacing)
+        c.amg->stale = true;
     c.opts = *o;
     c.vec64_fallback = false;
     if (prec_change)
@@ -713,7 +722,7 @@ int lpm_init_state(lpm_ctx *ctx)
 
 namespace lpm {
 
-enum PcgMode { PCG_FP64 = 0, PCG_FP32 = 1, PCG_FP32_K_FP64_VEC = 2 };
+enum PcgMode { PCG_FP64 = 0, PCG_FP32 = 1, PCG_FP32_K_FP64_VEC = 2, PCG_AMG_K64 = 3, PCG_AMG_K32 = 4 };
 
 // One chunk of PCG iterations; the first SpMV of the chunk (which always does
 // work: a chunk is only launched while the solve is running) carries the
@@ -726,8 +735,10 @@ static void issue_chunk(Ctx &c, int mode, int chunk)
             launch_cg_iter_d(c);
         else if (mode == PCG_FP32)
             launch_cg_iter_f(c);
-        else
+        else if (mode == PCG_FP32_K_FP64_VEC)
             launch_cg_iter_fx(c);
+        else
+            launch_amg_iter(c, mode == PCG_AMG_K32);
     }
     c.time_this = false;
 }
@@ -737,7 +748,7 @@ static void issue_chunk(Ctx &c, int mode, int chunk)
 static int run_pcg(Ctx &c, int mode, int &iters, int &status)
 {
     const int chunk = c.opts.check_every;
-    cudaGraphExec_t &ge = mode == PCG_FP64 ? c.graph_fp64 : c.graph_fp32;
+    cudaGraphExec_t &ge = mode == PCG_FP32 ? c.graph_fp32 : c.graph_fp64;
     bool use_graph = c.opts.use_graphs != 0;
     if (ge && (c.graph_timed != c.time_spmv || c.graph_chunk != chunk || c.graph_mode != mode)) {
         cudaGraphExecDestroy(ge);
@@ -804,6 +815,74 @@ static int run_pcg(Ctx &c, int mode, int &iters, int &status)
 // true residual b - K32 x64 is recomputed with FP64 products and sums, and
 // replaces the FP32 residual; the search direction is kept, so CG keeps its
 // Krylov history.  Convergence is judged on the FP64 true residual.
+// Multigrid-preconditioned CG (k_amg.cu) with FP64 vectors, the right-hand
+// side normalised by |b| as below.  FP64: the recursive residual decides.
+// Mixed: FP32 stiffness and products; at a reliable-update request or at
+// convergence the true residual s b - K32 x is recomputed with FP64 sums and
+// replaces r (p is kept), and convergence is judged on it.  A solve that
+// needs more iterations per decade of residual reduction than opts.amg_rebuild
+// times those of the first solve after the last build marks the hierarchy
+// for a rebuild before the next solve.
+static int solve_amg(Ctx &c, const dvec4 *b, double bn, lpm_step_stats *st)
+{
+    int rc;
+    const int builds0 = c.amg ? c.amg->builds : 0;
+    if ((rc = amg_prepare(c)))
+        return rc;
+    AmgDev &H = *c.amg;
+    if (st && H.builds != builds0) {
+        st->amg_builds += H.builds - builds0;
+        st->ms_amg_build += H.build_ms;
+    }
+    const bool k32 = c.opts.precision == LPM_PREC_MIXED;
+    const double scale = 1.0 / bn;
+    const double delta = c.opts.inner_rtol;
+    launch_amg_init(c, b, scale, k32 ? delta * delta : 0.0);
+    int sweeps = 0, it = 0, done = 0;
+    double rel = 1.0;
+    for (;;) {
+        if ((rc = run_pcg(c, k32 ? PCG_AMG_K32 : PCG_AMG_K64, it, done)))
+            return rc;
+        if (!k32) {
+            rel = std::sqrt(c.sc_host->rr / std::max(c.sc_host->bnorm2, 1e-300));
+            break;
+        }
+        launch_refine_residual(c, c.x_d, b, c.q_d, scale);
+        LPM_CUDA(cudaMemcpyAsync(c.norms_host, c.norms, 4 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        if ((rc = sync(c)))
+            return rc;
+        rel = std::sqrt(c.norms_host[2]);
+        sweeps++;
+        if (rel <= solve_rtol(c) || done == 2 || done == 3 || !std::isfinite(rel) ||
+            sweeps >= c.opts.refine_maxiter)
+            break;
+        launch_amg_reliable(c, c.q_d);
+    }
+    if (st) {
+        st->cg_iters += it;
+        st->spmv_calls += it + sweeps;
+        st->refine_iters += sweeps;
+        if (done == 2 || (k32 && rel > solve_rtol(c)))
+            st->status |= std::isfinite(rel) ? LPM_STATUS_CG_MAXIT : LPM_STATUS_NAN;
+        if (done == 3)
+            st->status |= LPM_STATUS_NAN;
+    }
+    // iterations per decade of residual reduction against the first solve
+    // after the build
+    if (std::isfinite(rel) && rel > 0.0 && rel < 1.0 && it > 0) {
+        const double per_decade = it / std::max(0.5, -std::log10(rel));
+        if (H.ref_iters < 0)
+            H.ref_iters = std::max(1, (int)std::lround(per_decade * 100.0));
+        else if (per_decade * 100.0 > c.opts.amg_rebuild * H.ref_iters)
+            H.stale = true;
+    }
+    if (c.trace)
+        std::fprintf(stderr, "lpm: solve amg-%s |b| %.6e iters %d sweeps %d rel %.3e end %d%s\n",
+                     k32 ? "fp32K" : "fp64", bn, it, sweeps, rel, done, H.stale ? " (rebuild next)" : "");
+    launch_scale_copy(c, c.du, c.x_d, bn);
+    return LPM_OK;
+}
+
 int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
 {
     int rc;
@@ -818,6 +897,8 @@ int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
             st->status |= LPM_STATUS_NAN;
         return LPM_OK;
     }
+    if (c.opts.preconditioner == LPM_PRECOND_AMG && c.nspec == 0)
+        return solve_amg(c, b, bn, st);
     const double scale = 1.0 / bn;
     const double delta = c.opts.inner_rtol;
     if (c.opts.precision == LPM_PREC_MIXED && (c.opts.mixed_vectors == 64 || c.vec64_fallback)) {

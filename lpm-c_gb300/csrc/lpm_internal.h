@@ -118,6 +118,40 @@ struct CgScalars {
 struct AdjointState;
 struct AsyncWriter;
 
+// One level of the multigrid hierarchy on the device.  Level 0 operates with
+// the stiffness itself (Kd or Kf, its block-Jacobi inverse Pinv_d) on dvec4
+// vectors; the levels above hold 6 DOFs per block row (aggregate), vectors
+// with 6 doubles per row, and their own 6 x 6 block-CSR operator.
+struct AmgDevLevel {
+    int nb = 0, bs = 0;  // block rows, DOFs per block row
+    int nnext = 0;       // block rows of the next level
+    double omega = 1.0;  // smoother damping 1 / rho(D^-1 A)
+    long long *a_ptr = nullptr;   // levels >= 1: operator, 6 x 6 blocks
+    int *a_col = nullptr;
+    double *a_val = nullptr;
+    double *dinv = nullptr;       // levels >= 1: 6 x 6 diagonal-block inverses
+    long long *p_ptr = nullptr;   // prolongation, bs x 6 blocks
+    int *p_col = nullptr;
+    double *p_val = nullptr;
+    long long *pt_ptr = nullptr;  // restriction, 6 x bs blocks
+    int *pt_col = nullptr;
+    double *pt_val = nullptr;
+    double *b = nullptr, *x = nullptr, *y = nullptr;  // levels >= 1: right-hand side, two iterates
+};
+
+struct AmgDev {
+    std::vector<AmgDevLevel> lv;
+    int nc = 0;                    // scalar size of the coarsest operator
+    int cbs = 0;                   // its DOFs per block row (3 when level 0 is the coarsest)
+    double *cinv = nullptr;        // its dense inverse, row-major
+    double *cb = nullptr, *cx = nullptr;
+    std::vector<uint8_t> mask_h;   // DOF mask the hierarchy was built for
+    int ref_iters = -1;            // PCG iterations of the first solve after the build
+    bool stale = false;            // rebuild before the next solve
+    int builds = 0;
+    double build_ms = 0.0;         // host time of the last build (download, setup, upload)
+};
+
 // Per-specimen PCG state of a batch (device pointers, passed by value).
 // done: 0 running, 1 recursive residual met the tolerance, 2 iteration cap,
 // 3 non-finite, 5 specimen inactive (its Newton loop has converged),
@@ -283,6 +317,10 @@ struct Ctx {
         int *count = nullptr, *count_h = nullptr;        // list length (device, pinned)
         std::vector<int> log;                            // broken (particle, partner) pairs, in order
     } dmg;
+    // smoothed-aggregation multigrid preconditioner (opts.preconditioner ==
+    // LPM_PRECOND_AMG): the hierarchy built on the host (amg_setup.cpp) and
+    // kept on the device; null until the first solve that uses it
+    AmgDev *amg = nullptr;
     // Anderson acceleration of the Newton loop (opts.newton_accel)
     struct Anderson {
         int m = 0;
@@ -322,6 +360,14 @@ void launch_crack(Ctx &c);            // updateCrack + updateRR norms
 void launch_tangent_geometry(Ctx &c);
 void launch_assemble(Ctx &c, bool fp32);
 void launch_block_jacobi(Ctx &c, bool fp32);
+// multigrid preconditioner (k_amg.cu): PCG with z = V-cycle(r), FP64
+// vectors; k32 selects the FP32 stiffness (mixed precision)
+void launch_amg_init(Ctx &c, const dvec4 *b, double scale, double delta2);  // x = 0, r, z, p, rz
+void launch_amg_iter(Ctx &c, bool k32);
+void launch_amg_reliable(Ctx &c, const dvec4 *rtrue);  // r = rtrue (masked), z, rz; p kept
+void launch_amg_vcycle(Ctx &c, const dvec4 *r, dvec4 *z, dvec4 *tmp, bool k32);
+int amg_prepare(Ctx &c);  // (re)build the hierarchy when missing, stale or the mask changed
+void free_amg(Ctx &c);
 // solver (k_solve.cu)
 void launch_spmv_d(Ctx &c, const dvec4 *x, dvec4 *y, bool masked, bool dot_pq);
 void launch_spmv_f(Ctx &c, const float4 *x, float4 *y, bool masked, bool dot_pq);
@@ -329,6 +375,7 @@ void launch_refine_residual(Ctx &c, const dvec4 *x, const dvec4 *b, dvec4 *r, do
 void launch_spmv_fx(Ctx &c, const dvec4 *x, dvec4 *y, bool masked, bool dot);
 void launch_cg_init_fx(Ctx &c, const dvec4 *b, double scale, double delta2);
 void launch_cg_iter_fx(Ctx &c);
+void launch_cg_p_d(Ctx &c);  // p = z + beta p (FP64 vectors)
 void launch_reliable_d(Ctx &c, const dvec4 *rtrue);
 void launch_cg_init_d(Ctx &c, const dvec4 *b, double scale);
 void launch_cg_init_f(Ctx &c, const dvec4 *r64, double scale, double rtol, double delta2);
