@@ -3,17 +3,39 @@
 // and checked without a GPU.
 #pragma once
 #include <cstdint>
+#include <memory>
+#include <utility>
 #include <vector>
 
 namespace lpm {
+
+// Allocator whose resize() leaves elements uninitialised, so that the large
+// arrays of the build are first written by the parallel loops that fill
+// them (no serial zero fill, pages touched by the threads that use them).
+template <typename T>
+struct AmgNoInit : std::allocator<T> {
+    template <typename U>
+    struct rebind {
+        typedef AmgNoInit<U> other;
+    };
+    AmgNoInit() = default;
+    template <typename U>
+    AmgNoInit(const AmgNoInit<U> &) noexcept {}
+    template <typename U>
+    void construct(U *p) noexcept { ::new (static_cast<void *>(p)) U; }
+    template <typename U, typename... A>
+    void construct(U *p, A &&...a) { ::new (static_cast<void *>(p)) U(std::forward<A>(a)...); }
+};
+template <typename T>
+using avec = std::vector<T, AmgNoInit<T>>;
 
 // Block-CSR with R x C blocks, 0-based; block k is val[k*R*C ...], row-major.
 struct Bsr {
     int nbr = 0, nbc = 0;  // block rows, block columns
     int R = 0, C = 0;
-    std::vector<long long> ptr;
-    std::vector<int> col;
-    std::vector<double> val;
+    avec<long long> ptr;
+    avec<int> col;
+    avec<double> val;
 };
 
 struct AmgLevel {

@@ -214,7 +214,7 @@ struct Marker {
 };
 
 // Exclusive prefix sum of counts into ptr (size n + 1).
-void prefix(const std::vector<long long> &cnt, std::vector<long long> &ptr)
+void prefix(const std::vector<long long> &cnt, avec<long long> &ptr)
 {
     ptr.assign(cnt.size() + 1, 0);
     for (size_t i = 0; i < cnt.size(); i++)
@@ -386,7 +386,8 @@ bool coarsen(const Op &A, const uint8_t *mask, const std::vector<int> &gidx, con
 #pragma omp parallel for schedule(static)
     for (int I = 0; I < nb; I++)
         agg[I] = (int)(std::lower_bound(uk.begin(), uk.end(), key[I]) - uk.begin());
-    std::vector<long long> mcnt(nagg, 0), mptr;
+    std::vector<long long> mcnt(nagg, 0);
+    avec<long long> mptr;
     for (int I = 0; I < nb; I++)
         mcnt[agg[I]]++;
     prefix(mcnt, mptr);
@@ -484,7 +485,7 @@ bool coarsen(const Op &A, const uint8_t *mask, const std::vector<int> &gidx, con
         prefix(cnt, P.ptr);
     }
     P.col.resize((size_t)P.ptr[nb]);
-    P.val.assign((size_t)P.ptr[nb] * BS * 6, 0.0);
+    P.val.resize((size_t)P.ptr[nb] * BS * 6);  // every value written below
 #pragma omp parallel
     {
         Marker mk(nagg);
@@ -541,13 +542,14 @@ bool coarsen(const Op &A, const uint8_t *mask, const std::vector<int> &gidx, con
         prefix(cnt, W.ptr);
     }
     W.col.resize((size_t)W.ptr[nb]);
-    W.val.assign((size_t)W.ptr[nb] * BS * 6, 0.0);
+    W.val.resize((size_t)W.ptr[nb] * BS * 6);  // zeroed row by row below
 #pragma omp parallel
     {
         Marker mk(nagg);
 #pragma omp for schedule(dynamic, 256)
         for (int I = 0; I < nb; I++) {
             const long long w0 = W.ptr[I];
+            std::fill(W.val.begin() + (size_t)w0 * BS * 6, W.val.begin() + (size_t)W.ptr[I + 1] * BS * 6, 0.0);
             A.row(I, [&](int J, const double *blk) {
                 for (long long k = P.ptr[J]; k < P.ptr[J + 1]; k++) {
                     const int s = mk.find_or_add(P.col[k]);
@@ -584,13 +586,14 @@ bool coarsen(const Op &A, const uint8_t *mask, const std::vector<int> &gidx, con
         prefix(cnt, Ac.ptr);
     }
     Ac.col.resize((size_t)Ac.ptr[nagg]);
-    Ac.val.assign((size_t)Ac.ptr[nagg] * 36, 0.0);
+    Ac.val.resize((size_t)Ac.ptr[nagg] * 36);  // zeroed row by row below
 #pragma omp parallel
     {
         Marker mk(nagg);
 #pragma omp for schedule(dynamic, 16)
         for (int a = 0; a < nagg; a++) {
             const long long a0 = Ac.ptr[a];
+            std::fill(Ac.val.begin() + (size_t)a0 * 36, Ac.val.begin() + (size_t)Ac.ptr[a + 1] * 36, 0.0);
             mk.find_or_add(a);
             for (long long k = Pt.ptr[a]; k < Pt.ptr[a + 1]; k++) {
                 const int I = Pt.col[k];

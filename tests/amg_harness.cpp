@@ -22,11 +22,11 @@ static std::vector<T> rd(const std::string &path, size_t count)
     return v;
 }
 
-template <typename T>
-static void wr(const std::string &path, const std::vector<T> &v)
+template <typename V>
+static void wr(const std::string &path, const V &v)
 {
     FILE *f = std::fopen(path.c_str(), "wb");
-    std::fwrite(v.data(), sizeof(T), v.size(), f);
+    std::fwrite(v.data(), sizeof(v[0]), v.size(), f);
     std::fclose(f);
 }
 
