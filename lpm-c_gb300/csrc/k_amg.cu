@@ -32,6 +32,7 @@
 #include <cmath>
 #include <omp.h>
 #include "amg.h"
+#include "amg_rows.h"
 #include "lpm_internal.h"
 
 namespace lpm {
@@ -102,14 +103,6 @@ __device__ void amg_reduce(double (&v)[NV], double *partials, unsigned *counter,
 __device__ __forceinline__ dvec4 amg_mask(dvec4 v, uint8_t m)
 {
     return make_dvec4((m & 1) ? v.x : 0.0, (m & 2) ? v.y : 0.0, (m & 4) ? v.z : 0.0, 0.0);
-}
-
-// z = P^-1 r with the level-0 3x3 block inverses stored [9][n]
-__device__ __forceinline__ dvec4 amg_pinv(const double *P, int n, int i, dvec4 r)
-{
-    return make_dvec4(P[(size_t)0 * n + i] * r.x + P[(size_t)1 * n + i] * r.y + P[(size_t)2 * n + i] * r.z,
-                      P[(size_t)3 * n + i] * r.x + P[(size_t)4 * n + i] * r.y + P[(size_t)5 * n + i] * r.z,
-                      P[(size_t)6 * n + i] * r.x + P[(size_t)7 * n + i] * r.y + P[(size_t)8 * n + i] * r.z, 0.0);
 }
 
 struct AmgVec {
@@ -245,19 +238,17 @@ __global__ void __launch_bounds__(ATPB) k_amg_rz(AmgVec a, const dvec4 *r, const
 
 constexpr int L0_LANES = 16;  // lanes per block row of the stiffness
 
-enum { SM_SMOOTH = 0, SM_RESID = 1 };
-
 // MODE SM_SMOOTH: out = x + omega Pinv mask(b - K x); SM_RESID: out = mask(b - K x).
 // Half a warp per block row, lanes over the row's blocks (padding included:
 // zero values, column of the row itself); products in V as the SpMV of the
-// same precision, epilogue in FP64.
+// same precision, epilogue in FP64 (amg_rows.h).
 template <typename V, int MODE>
 __global__ void __launch_bounds__(ATPB) k_amg_k0(int n, const long long *__restrict__ rowoff,
                                                  const int *__restrict__ npad, const int *__restrict__ cols,
                                                  const uint8_t *__restrict__ mask, const V *__restrict__ val,
                                                  const double *__restrict__ Pinv, double omega,
-                                                 const dvec4 *__restrict__ x, const dvec4 *__restrict__ b,
-                                                 dvec4 *__restrict__ out, const CgScalars *sc)
+                                                 const double *__restrict__ x, const double *__restrict__ b,
+                                                 double *__restrict__ out, const CgScalars *sc)
 {
     if (sc && sc->done)
         return;
@@ -266,67 +257,38 @@ __global__ void __launch_bounds__(ATPB) k_amg_k0(int n, const long long *__restr
     const int g = (blockIdx.x * blockDim.x + threadIdx.x) / L0_LANES;
     const int ng = (gridDim.x * blockDim.x) / L0_LANES;
     for (int row = g; row < n; row += ng) {
-        const long long off = rowoff[row];
-        const int np = npad[row];
-        const V *vr = val + 9 * off;
         V y0 = 0, y1 = 0, y2 = 0;
-        for (int k = sub; k < np; k += L0_LANES) {
-            const int j = cols[off + k];
-            const dvec4 xv = x[j];
-            const V x0 = (V)xv.x, x1 = (V)xv.y, x2 = (V)xv.z;
-            y0 += vr[(size_t)0 * np + k] * x0 + vr[(size_t)1 * np + k] * x1 + vr[(size_t)2 * np + k] * x2;
-            y1 += vr[(size_t)3 * np + k] * x0 + vr[(size_t)4 * np + k] * x1 + vr[(size_t)5 * np + k] * x2;
-            y2 += vr[(size_t)6 * np + k] * x0 + vr[(size_t)7 * np + k] * x1 + vr[(size_t)8 * np + k] * x2;
-        }
+        k0_row_partial<V>(rowoff, npad, cols, val, x, row, sub, L0_LANES, y0, y1, y2);
 #pragma unroll
         for (int o = L0_LANES / 2; o > 0; o >>= 1) {
             y0 += __shfl_xor_sync(gmask, y0, o);
             y1 += __shfl_xor_sync(gmask, y1, o);
             y2 += __shfl_xor_sync(gmask, y2, o);
         }
-        if (sub == 0) {
-            const uint8_t m = mask[row];
-            const dvec4 bb = b[row];
-            const dvec4 rr = amg_mask(make_dvec4(bb.x - (double)y0, bb.y - (double)y1, bb.z - (double)y2, 0.0), m);
-            if (MODE == SM_RESID) {
-                out[row] = rr;
-            } else {
-                const dvec4 d = amg_pinv(Pinv, n, row, rr);
-                const dvec4 xo = x[row];
-                out[row] = amg_mask(
-                    make_dvec4(xo.x + omega * d.x, xo.y + omega * d.y, xo.z + omega * d.z, 0.0), m);
-            }
-        }
+        if (sub == 0)
+            k0_epilogue(MODE, n, row, mask[row], Pinv, omega, x, b, out, (double)y0, (double)y1, (double)y2);
     }
 }
 
 // out = omega Pinv mask(b): the first sweep from zero on level 0
 __global__ void __launch_bounds__(ATPB) k_amg_jacobi0(int n, const uint8_t *__restrict__ mask,
                                                       const double *__restrict__ Pinv, double omega,
-                                                      const dvec4 *__restrict__ b, dvec4 *__restrict__ out,
+                                                      const double *__restrict__ b, double *__restrict__ out,
                                                       const CgScalars *sc)
 {
     if (sc && sc->done)
         return;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint8_t m = mask[i];
-        const dvec4 d = amg_pinv(Pinv, n, i, amg_mask(b[i], m));
-        out[i] = amg_mask(make_dvec4(omega * d.x, omega * d.y, omega * d.z, 0.0), m);
-    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        jacobi0_row(n, i, mask[i], Pinv, omega, b, out);
 }
 
 // ---- block-CSR levels -------------------------------------------------------------
 
 constexpr int BL_LANES = 8;  // lanes per block row of the coarse-level kernels
 
-enum { BM_SET = 0, BM_ADD = 1, BM_SMOOTH = 2, BM_RESID = 3 };
-
-// y = sum over the row's R x C blocks of blk * x[col] (x: C values of block
-// column j at x[j * SX]); then
-//   BM_SET:    out[row * SY + r] = y_r            (restriction)
-//   BM_ADD:    out[row * SY + r] += y_r           (prolongation)
-//   BM_SMOOTH: out = x_row + omega Dinv (b - y)   (R = C = 6, SX = SY = 6)
-//   BM_RESID:  out = b - y                        (R = C = 6)
+// R x C blocks, 8 lanes per block row, epilogue by MODE (amg_rows.h):
+// restriction (BM_SET), prolongation (BM_ADD), coarse smoothing (BM_SMOOTH)
+// and residual (BM_RESID).
 template <int R, int C, int MODE>
 __global__ void __launch_bounds__(ATPB) k_amg_bsr(int nbr, const long long *__restrict__ ptr,
                                                   const int *__restrict__ col, const double *__restrict__ val,
@@ -335,6 +297,7 @@ __global__ void __launch_bounds__(ATPB) k_amg_bsr(int nbr, const long long *__re
                                                   const double *__restrict__ dinv, double omega,
                                                   const CgScalars *sc)
 {
+    static_assert(MODE == BM_SET || MODE == BM_ADD || (R == 6 && C == 6), "operator rows are 6 x 6");
     if (sc && sc->done)
         return;
     const int sub = threadIdx.x & (BL_LANES - 1);
@@ -346,58 +309,14 @@ __global__ void __launch_bounds__(ATPB) k_amg_bsr(int nbr, const long long *__re
 #pragma unroll
         for (int r = 0; r < R; r++)
             y[r] = 0.0;
-        for (long long k = ptr[row] + sub; k < ptr[row + 1]; k += BL_LANES) {
-            const double *blk = val + (size_t)k * (R * C);
-            const double *xc = x + (size_t)col[k] * SX;
-            double xv[C];
-#pragma unroll
-            for (int c = 0; c < C; c++)
-                xv[c] = xc[c];
-#pragma unroll
-            for (int r = 0; r < R; r++)
-#pragma unroll
-                for (int c = 0; c < C; c++)
-                    y[r] += blk[r * C + c] * xv[c];
-        }
+        bsr_row_partial<R, C>(ptr, col, val, x, SX, row, sub, BL_LANES, y);
 #pragma unroll
         for (int o = BL_LANES / 2; o > 0; o >>= 1)
 #pragma unroll
             for (int r = 0; r < R; r++)
                 y[r] += __shfl_xor_sync(gmask, y[r], o);
-        if (sub != 0)
-            continue;
-        double *o = out + (size_t)row * SY;
-        if constexpr (MODE == BM_SET) {
-#pragma unroll
-            for (int r = 0; r < R; r++)
-                o[r] = y[r];
-        } else if constexpr (MODE == BM_ADD) {
-#pragma unroll
-            for (int r = 0; r < R; r++)
-                o[r] += y[r];
-        } else {
-            static_assert(R == 6 && C == 6, "operator rows are 6 x 6");
-            double rr[R];
-#pragma unroll
-            for (int r = 0; r < R; r++)
-                rr[r] = b[(size_t)row * R + r] - y[r];
-            if constexpr (MODE == BM_RESID) {
-#pragma unroll
-                for (int r = 0; r < R; r++)
-                    o[r] = rr[r];
-            } else {
-                const double *D = dinv + (size_t)row * (R * R);
-                const double *xr = x + (size_t)row * SX;
-#pragma unroll
-                for (int r = 0; r < R; r++) {
-                    double s = 0.0;
-#pragma unroll
-                    for (int c = 0; c < R; c++)
-                        s += D[r * R + c] * rr[c];
-                    o[r] = xr[r] + omega * s;
-                }
-            }
-        }
+        if (sub == 0)
+            bsr_epilogue<R, MODE>(row, y, x, SX, out, SY, b, dinv, omega);
     }
 }
 
@@ -408,21 +327,8 @@ __global__ void __launch_bounds__(ATPB) k_amg_jacobi6(int nb, const double *__re
 {
     if (sc && sc->done)
         return;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += gridDim.x * blockDim.x) {
-        const double *D = dinv + (size_t)i * 36;
-        double bv[6];
-#pragma unroll
-        for (int c = 0; c < 6; c++)
-            bv[c] = b[(size_t)i * 6 + c];
-#pragma unroll
-        for (int r = 0; r < 6; r++) {
-            double s = 0.0;
-#pragma unroll
-            for (int c = 0; c < 6; c++)
-                s += D[r * 6 + c] * bv[c];
-            out[(size_t)i * 6 + r] = omega * s;
-        }
-    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += gridDim.x * blockDim.x)
+        jacobi6_row(i, dinv, omega, b, out);
 }
 
 // Coarsest level: out = Cinv b (dense, nc x nc), one warp per output entry.
@@ -438,11 +344,7 @@ __global__ void __launch_bounds__(ATPB) k_amg_dense(int nc, const double *__rest
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     for (int k = w; k < nc; k += nw) {
-        const double *row = Cinv + (size_t)k * nc;
-        double s = 0.0;
-        for (int j = lane; j < nc; j += 32)
-            s += row[j] * b[(size_t)(j / B) * S + j % B];
-        s = amg_warp_sum(s);
+        const double s = amg_warp_sum(dense_row_partial(nc, Cinv, b, B, S, k, lane, 32));
         if (lane == 0)
             out[(size_t)(k / B) * S + k % B] = s;
     }
@@ -459,9 +361,11 @@ static int grid_for(const Ctx &c, long long rows_x_threads)
 
 static AmgVec amg_vec(Ctx &c) { return AmgVec{c.n, c.mask, c.partials, c.counter, c.sc}; }
 
-static void k0_launch(Ctx &c, bool k32, int mode, double omega, const dvec4 *x, const dvec4 *b, dvec4 *out)
+static void k0_launch(Ctx &c, bool k32, int mode, double omega, const dvec4 *xv, const dvec4 *bv, dvec4 *outv)
 {
     const int g = grid_for(c, (long long)c.n * L0_LANES);
+    const double *x = (const double *)xv, *b = (const double *)bv;
+    double *out = (double *)outv;
     if (k32) {
         if (mode == SM_SMOOTH)
             k_amg_k0<float, SM_SMOOTH><<<g, ATPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.mask, c.Kf,
@@ -503,7 +407,8 @@ void launch_amg_vcycle(Ctx &c, const dvec4 *r, dvec4 *z, dvec4 *tmp, bool k32)
         AmgDevLevel &v = H.lv[l];
         double *bnext = (l + 1 < L) ? H.lv[l + 1].b : H.cb;
         if (l == 0) {
-            k_amg_jacobi0<<<grid_for(c, c.n), ATPB, 0, c.stream>>>(c.n, c.mask, c.Pinv_d, v.omega, r, tmp, c.sc);
+            k_amg_jacobi0<<<grid_for(c, c.n), ATPB, 0, c.stream>>>(c.n, c.mask, c.Pinv_d, v.omega,
+                                                                   (const double *)r, (double *)tmp, c.sc);
             k0_launch(c, k32, SM_SMOOTH, v.omega, tmp, r, z);
             k0_launch(c, k32, SM_RESID, v.omega, z, r, tmp);
             bsr_launch<6, 3, BM_SET>(c, v.nnext, v.pt_ptr, v.pt_col, v.pt_val, (const double *)tmp, 4, bnext, 6);

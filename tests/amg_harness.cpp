@@ -1,6 +1,10 @@
 // Test helper: runs lpm::amg_build on a stiffness given in the device
 // block-CSR layout (binary files in a directory) and writes the hierarchy
-// back as binary files, for tests/test_amg_setup.py.
+// back as binary files, for tests/test_amg_setup.py.  When DIR holds r.bin
+// (a level-0 vector, 4 doubles per particle), it also applies the device's
+// V-cycle to it: the launch sequence of launch_amg_vcycle (k_amg.cu), each
+// kernel's rows computed one after another by the same per-row functions
+// (amg_rows.h), with the stiffness in FP64 (z.bin) and in FP32 (z32.bin).
 //   amg_harness DIR AGG_SPACING
 #include <chrono>
 #include <cstdio>
@@ -8,6 +12,7 @@
 #include <string>
 #include <vector>
 #include "amg.h"
+#include "amg_rows.h"
 
 template <typename T>
 static std::vector<T> rd(const std::string &path, size_t count)
@@ -36,6 +41,91 @@ static void wr_bsr(FILE *f, const std::string &p, const lpm::Bsr &A)
     wr(p + "_ptr.bin", A.ptr);
     wr(p + "_col.bin", A.col);
     wr(p + "_val.bin", A.val);
+}
+
+struct Level0 {
+    int n;
+    const uint8_t *mask;
+    const long long *rowoff;
+    const int *npad, *cols;
+    const double *Pinv;
+};
+
+template <typename V>
+static void k0(const Level0 &z0, const V *val, int mode, double omega, const double *x, const double *b, double *out)
+{
+    for (int row = 0; row < z0.n; row++) {
+        V y0 = 0, y1 = 0, y2 = 0;
+        lpm::k0_row_partial<V>(z0.rowoff, z0.npad, z0.cols, val, x, row, 0, 1, y0, y1, y2);
+        lpm::k0_epilogue(mode, z0.n, row, z0.mask[row], z0.Pinv, omega, x, b, out, y0, y1, y2);
+    }
+}
+
+template <int R, int C, int MODE>
+static void bsr(int nbr, const lpm::Bsr &M, const double *x, int SX, double *out, int SY, const double *b = nullptr,
+                const double *dinv = nullptr, double omega = 0.0)
+{
+    for (int row = 0; row < nbr; row++) {
+        double y[R] = {};
+        lpm::bsr_row_partial<R, C>(M.ptr.data(), M.col.data(), M.val.data(), x, SX, row, 0, 1, y);
+        lpm::bsr_epilogue<R, MODE>(row, y, x, SX, out, SY, b, dinv, omega);
+    }
+}
+
+static void dense(const lpm::AmgHierarchy &H, const double *b, double *out, int B, int S)
+{
+    for (int k = 0; k < H.coarse_n; k++)
+        out[(size_t)(k / B) * S + k % B] = lpm::dense_row_partial(H.coarse_n, H.coarse_inv.data(), b, B, S, k, 0, 1);
+}
+
+// z = V(r), in the order and with the buffers of launch_amg_vcycle
+template <typename V>
+static void vcycle(const lpm::AmgHierarchy &H, const Level0 &z0, const V *val, const double *r, double *z, double *tmp)
+{
+    const int L = (int)H.levels.size();
+    if (L == 0) {
+        dense(H, r, z, 3, 4);
+        return;
+    }
+    std::vector<std::vector<double>> b(L), x(L), y(L);
+    for (int l = 1; l < L; l++) {
+        const size_t m = 6 * (size_t)H.levels[l].nblock;
+        b[l].assign(m, 0.0);
+        x[l].assign(m, 0.0);
+        y[l].assign(m, 0.0);
+    }
+    std::vector<double> cb(H.coarse_n), cx(H.coarse_n);
+    for (int l = 0; l < L; l++) {
+        const lpm::AmgLevel &v = H.levels[l];
+        double *bnext = (l + 1 < L) ? b[l + 1].data() : cb.data();
+        if (l == 0) {
+            for (int i = 0; i < z0.n; i++)
+                lpm::jacobi0_row(z0.n, i, z0.mask[i], z0.Pinv, v.omega, r, tmp);
+            k0<V>(z0, val, lpm::SM_SMOOTH, v.omega, tmp, r, z);
+            k0<V>(z0, val, lpm::SM_RESID, v.omega, z, r, tmp);
+            bsr<6, 3, lpm::BM_SET>(v.P.nbc, v.Pt, tmp, 4, bnext, 6);
+        } else {
+            for (int i = 0; i < v.nblock; i++)
+                lpm::jacobi6_row(i, v.Dinv.data(), v.omega, b[l].data(), x[l].data());
+            bsr<6, 6, lpm::BM_SMOOTH>(v.nblock, v.A, x[l].data(), 6, y[l].data(), 6, b[l].data(), v.Dinv.data(), v.omega);
+            bsr<6, 6, lpm::BM_RESID>(v.nblock, v.A, y[l].data(), 6, x[l].data(), 6, b[l].data());
+            bsr<6, 6, lpm::BM_SET>(v.P.nbc, v.Pt, x[l].data(), 6, bnext, 6);
+        }
+    }
+    dense(H, cb.data(), cx.data(), 6, 6);
+    for (int l = L - 1; l >= 0; l--) {
+        const lpm::AmgLevel &v = H.levels[l];
+        const double *e = (l + 1 < L) ? y[l + 1].data() : cx.data();
+        if (l == 0) {
+            bsr<3, 6, lpm::BM_ADD>(v.nblock, v.P, e, 6, z, 4);
+            k0<V>(z0, val, lpm::SM_SMOOTH, v.omega, z, r, tmp);
+            k0<V>(z0, val, lpm::SM_SMOOTH, v.omega, tmp, r, z);
+        } else {
+            bsr<6, 6, lpm::BM_ADD>(v.nblock, v.P, e, 6, y[l].data(), 6);
+            bsr<6, 6, lpm::BM_SMOOTH>(v.nblock, v.A, y[l].data(), 6, x[l].data(), 6, b[l].data(), v.Dinv.data(), v.omega);
+            bsr<6, 6, lpm::BM_SMOOTH>(v.nblock, v.A, x[l].data(), 6, y[l].data(), 6, b[l].data(), v.Dinv.data(), v.omega);
+        }
+    }
 }
 
 int main(int argc, char **argv)
@@ -90,5 +180,26 @@ int main(int argc, char **argv)
     std::fclose(f);
     wr(d + "/coarse_chol.bin", H.coarse_chol);
     wr(d + "/coarse_inv.bin", H.coarse_inv);
+    if (L >= 0) {
+        FILE *fr = std::fopen((d + "/r.bin").c_str(), "rb");
+        if (fr) {
+            std::fclose(fr);
+            auto r = rd<double>(d + "/r.bin", 4 * (size_t)n);
+            // the block-Jacobi inverse [9][n] as the device keeps it
+            std::vector<double> Pinv(9 * (size_t)n);
+            if (L > 0)
+                for (int i = 0; i < n; i++)
+                    for (int k = 0; k < 9; k++)
+                        Pinv[(size_t)k * n + i] = H.levels[0].Dinv[(size_t)i * 9 + k];
+            const Level0 z0{n, mask.data(), rowoff.data(), npad.data(), cols.data(), Pinv.data()};
+            std::vector<double> z(4 * (size_t)n, 0.0), tmp(4 * (size_t)n, 0.0);
+            vcycle<double>(H, z0, val.data(), r.data(), z.data(), tmp.data());
+            wr(d + "/z.bin", z);
+            std::vector<float> vf(val.begin(), val.end());
+            std::fill(z.begin(), z.end(), 0.0);
+            vcycle<float>(H, z0, vf.data(), r.data(), z.data(), tmp.data());
+            wr(d + "/z32.bin", z);
+        }
+    }
     return L >= 0 ? 0 : 1;
 }

@@ -150,10 +150,14 @@ def test_hierarchy_preconditions_cg(oracle_mod, harness, tmp_path, lattice, size
     for name, arr in (("xyz", xyz), ("mask", mask), ("rowoff", rowoff), ("npad", npad),
                       ("nconn", nconn.astype(np.int32)), ("cols", cols), ("val", val)):
         np.ascontiguousarray(arr).tofile(os.path.join(d, f"{name}.bin"))
+    free = (np.repeat(mask[:, None], 3, axis=1) >> np.arange(3) & 1).ravel().astype(bool)
+    b = res * free
+    r4 = np.zeros((n, 4))
+    r4[:, :3] = b.reshape(n, 3)
+    r4.tofile(os.path.join(d, "r.bin"))  # the harness also applies the device's V-cycle to it
     subprocess.check_call([harness, d, "0.6"])
     levels, coarse, chol, cinv = _load_hierarchy(d)
     assert len(levels) >= 1
-    free = (np.repeat(mask[:, None], 3, axis=1) >> np.arange(3) & 1).ravel().astype(bool)
     # level 0 operates with the stiffness, constrained rows and columns removed
     dfree = sp.diags(free.astype(float))
     A0 = (dfree @ K @ dfree).tocsr()
@@ -174,11 +178,45 @@ def test_hierarchy_preconditions_cg(oracle_mod, harness, tmp_path, lattice, size
     # the dense coarse factor and inverse
     assert np.allclose(chol @ chol.T, coarse.toarray() + np.diag((abs(coarse).sum(1).A1 == 0).astype(float)))
     assert np.allclose(cinv @ (chol @ chol.T), np.eye(len(cinv)), atol=1e-8)
-    b = res * free
-    x, it = _pcg(A0, _vcycle(levels, cinv), b)
+    M = _vcycle(levels, cinv)
+    # the device's launch sequence and per-row arithmetic (emulated on the
+    # host) give the numpy V-cycle's result
+    z = M(b)
+    z64 = np.fromfile(os.path.join(d, "z.bin")).reshape(n, 4)
+    z32 = np.fromfile(os.path.join(d, "z32.bin")).reshape(n, 4)
+    assert np.all(z64[:, 3] == 0.0) and np.all(z64[:, :3].ravel()[~free] == 0.0)
+    assert np.abs(z64[:, :3].ravel() - z).max() <= 1e-10 * np.abs(z).max()
+    assert np.abs(z32[:, :3].ravel() - z).max() <= 1e-4 * np.abs(z).max()
+    x, it = _pcg(A0, M, b)
     Kf = K[free][:, free]
     assert np.linalg.norm(Kf @ x[free] - b[free]) <= 1e-10 * np.linalg.norm(b)
     # block-Jacobi PCG on the same system for reference
     dinv = levels[0]["Dinv"]
     _, it_bj = _pcg(A0, lambda r: np.einsum("nij,nj->ni", dinv, r.reshape(-1, 3)).ravel(), b)
     assert it <= 30 and it * 5 < it_bj, (it, it_bj)
+
+
+def test_single_level_is_the_exact_inverse(oracle_mod, harness, tmp_path):
+    """A lattice of at most 150 particles does not coarsen: the V-cycle is the
+    dense inverse of the stiffness with the constrained DOFs removed."""
+    o, K, res, xyz, mask, conn, nconn = _system(oracle_mod, 2, 4)
+    n = len(nconn)
+    assert n <= 150
+    rowoff, npad, cols, val = _device_layout(K, conn, nconn)
+    d = str(tmp_path)
+    open(os.path.join(d, "n.txt"), "w").write(str(n))
+    for name, arr in (("xyz", xyz), ("mask", mask), ("rowoff", rowoff), ("npad", npad),
+                      ("nconn", nconn.astype(np.int32)), ("cols", cols), ("val", val)):
+        np.ascontiguousarray(arr).tofile(os.path.join(d, f"{name}.bin"))
+    free = (np.repeat(mask[:, None], 3, axis=1) >> np.arange(3) & 1).ravel().astype(bool)
+    b = res * free
+    r4 = np.zeros((n, 4))
+    r4[:, :3] = b.reshape(n, 3)
+    r4.tofile(os.path.join(d, "r.bin"))
+    subprocess.check_call([harness, d, "0.6"])
+    levels, coarse, chol, cinv = _load_hierarchy(d)
+    assert levels == [] and cinv.shape == (3 * n, 3 * n)
+    z = np.fromfile(os.path.join(d, "z.bin")).reshape(n, 4)[:, :3].ravel()
+    x = np.zeros(3 * n)
+    x[free] = np.linalg.solve(K[free][:, free].toarray(), b[free])
+    assert np.abs(z - x).max() <= 1e-9 * np.abs(x).max()
