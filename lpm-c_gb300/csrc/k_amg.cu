@@ -355,7 +355,7 @@ __global__ void __launch_bounds__(ATPB) k_amg_dense(int nc, const double *__rest
 static int grid_for(const Ctx &c, long long rows_x_threads)
 {
     const long long blocks = (rows_x_threads + ATPB - 1) / ATPB;
-    const long long cap = (long long)std::max(1, c.tune.sms) * 16;
+    const long long cap = (long long)(c.tune.sms > 0 ? c.tune.sms : 152) * 16;
     return (int)std::max(1LL, std::min(blocks, cap));
 }
 
