@@ -249,11 +249,12 @@ def gpu_launches(stats, amg=0):
     """Kernel launches of the timed steps (counted from the solver statistics):
     per step 3 (stiffness) + 2 (BC) + 1 (preconditioner) + 2 (predictor);
     per Newton iteration 2 (force) + 1 (xyz update) + 1 (norm);
-    per PCG iteration 3 with block-Jacobi, 4 + the V-cycle's 7 per level + 1
-    with the multigrid preconditioner (amg = its levels); per reliable update
-    3 (block-Jacobi) or 3 + the V-cycle."""
-    per_it = 3 if not amg else 4 + 7 * amg + 1
-    per_rel = 3 if not amg else 2 + 7 * amg + 1
+    per PCG iteration 3 with block-Jacobi, 4 + the V-cycle's 5 per level + 1
+    with the multigrid preconditioner (amg = its levels; one sweep before and
+    after each coarse correction); per reliable update 3 (block-Jacobi) or
+    2 + the V-cycle."""
+    per_it = 3 if not amg else 4 + 5 * amg + 1
+    per_rel = 3 if not amg else 2 + 5 * amg + 1
     total = 0
     for st in stats:
         total += 8 + 4 * st["newton_iters"] + per_it * st["cg_iters"] + per_rel * st["refine_iters"] + \

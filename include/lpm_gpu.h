@@ -95,6 +95,8 @@ typedef struct {
     double amg_spacing; /* AMG: edge of a level-0 aggregate box; 0 (default) = 6 particle radii
                            (3 x 3 x 3 nearest-neighbour spacings) */
     double amg_rebuild; /* AMG: iteration growth that triggers a rebuild (default 2.5) */
+    int amg_sweeps;     /* AMG: damped block-Jacobi sweeps before and after each coarse correction
+                           (1..4, default 1: fewest stiffness passes per solve) */
 } lpm_solver_opts;
 
 typedef struct {

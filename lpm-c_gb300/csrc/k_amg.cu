@@ -4,16 +4,15 @@
 // the device (AmgDev).
 //
 // V-cycle on level l (operator A_l, block-Jacobi inverse D_l^-1, damping
-// omega_l = 1 / rho(D_l^-1 A_l)):
-//     x = omega D^-1 b                      (first sweep from zero)
-//     y = x + omega D^-1 (b - A x)          (second sweep)
-//     x = b - A y                           (residual)
-//     b_{l+1} = P_l^T x                     (restriction)
+// omega_l = 1 / rho(D_l^-1 A_l)), nu = opts.amg_sweeps:
+//     x = omega D^-1 b                      (first sweep, from zero)
+//     nu - 1 sweeps x += omega D^-1 (b - A x)
+//     b_{l+1} = P_l^T (b - A x)             (residual, restriction)
 //     e = V-cycle_{l+1}(b_{l+1})            (dense inverse on the coarsest level)
-//     y += P_l e                            (prolongation)
-//     x = y + omega D^-1 (b - A y);  y = x + omega D^-1 (b - A x)
-// so the result is in y.  Two Jacobi sweeps before and two after make the
-// cycle a symmetric positive definite operator, as CG needs.  On level 0 the
+//     x += P_l e                            (prolongation)
+//     nu sweeps x += omega D^-1 (b - A x)
+// The same number of Jacobi sweeps before and after makes the cycle a
+// symmetric positive definite operator, as CG needs.  On level 0 the
 // operator is the stiffness (FP64 Kd, or FP32 Kf under mixed precision, with
 // the products in FP32 as in the mixed SpMV), b is the CG residual r, x the
 // scratch vector q (free between the update and the next product) and y the
@@ -392,10 +391,15 @@ static void bsr_launch(Ctx &c, int nbr, const long long *ptr, const int *col, co
     k_amg_bsr<R, C, MODE><<<g, ATPB, 0, c.stream>>>(nbr, ptr, col, val, x, SX, out, SY, b, dinv, omega, c.sc);
 }
 
+// With nu sweeps before and after the coarse correction, the iterate starts in
+// the scratch buffer (x, or tmp on level 0) and changes buffer with every
+// sweep but the first (2 nu - 1 times), so it ends in y (z on level 0); the
+// residual goes to the buffer the iterate is not in.
 void launch_amg_vcycle(Ctx &c, const dvec4 *r, dvec4 *z, dvec4 *tmp, bool k32)
 {
     AmgDev &H = *c.amg;
     const int L = (int)H.lv.size();
+    const int nu = std::max(1, c.opts.amg_sweeps);
     const int gd = grid_for(c, (long long)H.nc * 32);
     if (L == 0) {
         // level 0 is the coarsest: z = Cinv r over the 3 DOFs of each particle
@@ -407,31 +411,46 @@ void launch_amg_vcycle(Ctx &c, const dvec4 *r, dvec4 *z, dvec4 *tmp, bool k32)
         AmgDevLevel &v = H.lv[l];
         double *bnext = (l + 1 < L) ? H.lv[l + 1].b : H.cb;
         if (l == 0) {
+            dvec4 *it = tmp, *ot = z;
             k_amg_jacobi0<<<grid_for(c, c.n), ATPB, 0, c.stream>>>(c.n, c.mask, c.Pinv_d, v.omega,
-                                                                   (const double *)r, (double *)tmp, c.sc);
-            k0_launch(c, k32, SM_SMOOTH, v.omega, tmp, r, z);
-            k0_launch(c, k32, SM_RESID, v.omega, z, r, tmp);
-            bsr_launch<6, 3, BM_SET>(c, v.nnext, v.pt_ptr, v.pt_col, v.pt_val, (const double *)tmp, 4, bnext, 6);
+                                                                   (const double *)r, (double *)it, c.sc);
+            for (int s = 1; s < nu; s++) {
+                k0_launch(c, k32, SM_SMOOTH, v.omega, it, r, ot);
+                std::swap(it, ot);
+            }
+            k0_launch(c, k32, SM_RESID, v.omega, it, r, ot);
+            bsr_launch<6, 3, BM_SET>(c, v.nnext, v.pt_ptr, v.pt_col, v.pt_val, (const double *)ot, 4, bnext, 6);
         } else {
-            k_amg_jacobi6<<<grid_for(c, v.nb), ATPB, 0, c.stream>>>(v.nb, v.dinv, v.omega, v.b, v.x, c.sc);
-            bsr_launch<6, 6, BM_SMOOTH>(c, v.nb, v.a_ptr, v.a_col, v.a_val, v.x, 6, v.y, 6, v.b, v.dinv, v.omega);
-            bsr_launch<6, 6, BM_RESID>(c, v.nb, v.a_ptr, v.a_col, v.a_val, v.y, 6, v.x, 6, v.b);
-            bsr_launch<6, 6, BM_SET>(c, v.nnext, v.pt_ptr, v.pt_col, v.pt_val, v.x, 6, bnext, 6);
+            double *it = v.x, *ot = v.y;
+            k_amg_jacobi6<<<grid_for(c, v.nb), ATPB, 0, c.stream>>>(v.nb, v.dinv, v.omega, v.b, it, c.sc);
+            for (int s = 1; s < nu; s++) {
+                bsr_launch<6, 6, BM_SMOOTH>(c, v.nb, v.a_ptr, v.a_col, v.a_val, it, 6, ot, 6, v.b, v.dinv, v.omega);
+                std::swap(it, ot);
+            }
+            bsr_launch<6, 6, BM_RESID>(c, v.nb, v.a_ptr, v.a_col, v.a_val, it, 6, ot, 6, v.b);
+            bsr_launch<6, 6, BM_SET>(c, v.nnext, v.pt_ptr, v.pt_col, v.pt_val, ot, 6, bnext, 6);
         }
     }
     k_amg_dense<<<gd, ATPB, 0, c.stream>>>(H.nc, H.cinv, H.cb, H.cx, 6, 6, c.sc);
-    // up
+    // up: the iterate is where the down sweep left it (x after an even
+    // number of swaps, y after an odd one)
     for (int l = L - 1; l >= 0; l--) {
         AmgDevLevel &v = H.lv[l];
         const double *e = (l + 1 < L) ? H.lv[l + 1].y : H.cx;
         if (l == 0) {
-            bsr_launch<3, 6, BM_ADD>(c, v.nb, v.p_ptr, v.p_col, v.p_val, e, 6, (double *)z, 4);
-            k0_launch(c, k32, SM_SMOOTH, v.omega, z, r, tmp);
-            k0_launch(c, k32, SM_SMOOTH, v.omega, tmp, r, z);
+            dvec4 *it = (nu % 2 == 1) ? tmp : z, *ot = (nu % 2 == 1) ? z : tmp;
+            bsr_launch<3, 6, BM_ADD>(c, v.nb, v.p_ptr, v.p_col, v.p_val, e, 6, (double *)it, 4);
+            for (int s = 0; s < nu; s++) {
+                k0_launch(c, k32, SM_SMOOTH, v.omega, it, r, ot);
+                std::swap(it, ot);
+            }
         } else {
-            bsr_launch<6, 6, BM_ADD>(c, v.nb, v.p_ptr, v.p_col, v.p_val, e, 6, v.y, 6);
-            bsr_launch<6, 6, BM_SMOOTH>(c, v.nb, v.a_ptr, v.a_col, v.a_val, v.y, 6, v.x, 6, v.b, v.dinv, v.omega);
-            bsr_launch<6, 6, BM_SMOOTH>(c, v.nb, v.a_ptr, v.a_col, v.a_val, v.x, 6, v.y, 6, v.b, v.dinv, v.omega);
+            double *it = (nu % 2 == 1) ? v.x : v.y, *ot = (nu % 2 == 1) ? v.y : v.x;
+            bsr_launch<6, 6, BM_ADD>(c, v.nb, v.p_ptr, v.p_col, v.p_val, e, 6, it, 6);
+            for (int s = 0; s < nu; s++) {
+                bsr_launch<6, 6, BM_SMOOTH>(c, v.nb, v.a_ptr, v.a_col, v.a_val, it, 6, ot, 6, v.b, v.dinv, v.omega);
+                std::swap(it, ot);
+            }
         }
     }
 }

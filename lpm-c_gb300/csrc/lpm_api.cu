@@ -448,6 +448,7 @@ void lpm_default_solver_opts(lpm_solver_opts *o)
     o->preconditioner = LPM_PRECOND_BJ;
     o->amg_spacing = 0.0;
     o->amg_rebuild = 2.5;
+    o->amg_sweeps = 1;
 }
 
 int lpm_create(lpm_ctx **out, int device)
@@ -514,7 +515,7 @@ int lpm_set_solver(lpm_ctx *ctx, const lpm_solver_opts *o)
     if (!(o->cg_rtol > 0) || o->cg_maxiter <= 0 || o->newton_maxiter < 0 || o->check_every <= 0 ||
         o->newton_accel < 0 || o->newton_accel > 16 || !(o->cg_forcing >= 0.0 && o->cg_forcing < 1.0) ||
         (o->preconditioner != LPM_PRECOND_BJ && o->preconditioner != LPM_PRECOND_AMG) ||
-        !(o->amg_spacing >= 0.0) || !(o->amg_rebuild > 1.0))
+        !(o->amg_spacing >= 0.0) || !(o->amg_rebuild > 1.0) || o->amg_sweeps < 1 || o->amg_sweeps > 4)
         return fail(LPM_ERR_ARG, "invalid solver options");
     Ctx &c = ctx->c;
     const bool prec_change = c.opts.precision != o->precision;

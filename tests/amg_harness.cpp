@@ -5,7 +5,8 @@
 // V-cycle to it: the launch sequence of launch_amg_vcycle (k_amg.cu), each
 // kernel's rows computed one after another by the same per-row functions
 // (amg_rows.h), with the stiffness in FP64 (z.bin) and in FP32 (z32.bin).
-//   amg_harness DIR AGG_SPACING
+//   amg_harness DIR AGG_SPACING [SWEEPS]
+#include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -78,9 +79,11 @@ static void dense(const lpm::AmgHierarchy &H, const double *b, double *out, int 
         out[(size_t)(k / B) * S + k % B] = lpm::dense_row_partial(H.coarse_n, H.coarse_inv.data(), b, B, S, k, 0, 1);
 }
 
-// z = V(r), in the order and with the buffers of launch_amg_vcycle
+// z = V(r), in the order and with the buffers of launch_amg_vcycle (nu
+// sweeps before and after each coarse correction)
 template <typename V>
-static void vcycle(const lpm::AmgHierarchy &H, const Level0 &z0, const V *val, const double *r, double *z, double *tmp)
+static void vcycle(const lpm::AmgHierarchy &H, const Level0 &z0, const V *val, const double *r, double *z, double *tmp,
+                   int nu)
 {
     const int L = (int)H.levels.size();
     if (L == 0) {
@@ -99,17 +102,25 @@ static void vcycle(const lpm::AmgHierarchy &H, const Level0 &z0, const V *val, c
         const lpm::AmgLevel &v = H.levels[l];
         double *bnext = (l + 1 < L) ? b[l + 1].data() : cb.data();
         if (l == 0) {
+            double *it = tmp, *ot = z;
             for (int i = 0; i < z0.n; i++)
-                lpm::jacobi0_row(z0.n, i, z0.mask[i], z0.Pinv, v.omega, r, tmp);
-            k0<V>(z0, val, lpm::SM_SMOOTH, v.omega, tmp, r, z);
-            k0<V>(z0, val, lpm::SM_RESID, v.omega, z, r, tmp);
-            bsr<6, 3, lpm::BM_SET>(v.P.nbc, v.Pt, tmp, 4, bnext, 6);
+                lpm::jacobi0_row(z0.n, i, z0.mask[i], z0.Pinv, v.omega, r, it);
+            for (int s = 1; s < nu; s++) {
+                k0<V>(z0, val, lpm::SM_SMOOTH, v.omega, it, r, ot);
+                std::swap(it, ot);
+            }
+            k0<V>(z0, val, lpm::SM_RESID, v.omega, it, r, ot);
+            bsr<6, 3, lpm::BM_SET>(v.P.nbc, v.Pt, ot, 4, bnext, 6);
         } else {
+            double *it = x[l].data(), *ot = y[l].data();
             for (int i = 0; i < v.nblock; i++)
-                lpm::jacobi6_row(i, v.Dinv.data(), v.omega, b[l].data(), x[l].data());
-            bsr<6, 6, lpm::BM_SMOOTH>(v.nblock, v.A, x[l].data(), 6, y[l].data(), 6, b[l].data(), v.Dinv.data(), v.omega);
-            bsr<6, 6, lpm::BM_RESID>(v.nblock, v.A, y[l].data(), 6, x[l].data(), 6, b[l].data());
-            bsr<6, 6, lpm::BM_SET>(v.P.nbc, v.Pt, x[l].data(), 6, bnext, 6);
+                lpm::jacobi6_row(i, v.Dinv.data(), v.omega, b[l].data(), it);
+            for (int s = 1; s < nu; s++) {
+                bsr<6, 6, lpm::BM_SMOOTH>(v.nblock, v.A, it, 6, ot, 6, b[l].data(), v.Dinv.data(), v.omega);
+                std::swap(it, ot);
+            }
+            bsr<6, 6, lpm::BM_RESID>(v.nblock, v.A, it, 6, ot, 6, b[l].data());
+            bsr<6, 6, lpm::BM_SET>(v.P.nbc, v.Pt, ot, 6, bnext, 6);
         }
     }
     dense(H, cb.data(), cx.data(), 6, 6);
@@ -117,13 +128,19 @@ static void vcycle(const lpm::AmgHierarchy &H, const Level0 &z0, const V *val, c
         const lpm::AmgLevel &v = H.levels[l];
         const double *e = (l + 1 < L) ? y[l + 1].data() : cx.data();
         if (l == 0) {
-            bsr<3, 6, lpm::BM_ADD>(v.nblock, v.P, e, 6, z, 4);
-            k0<V>(z0, val, lpm::SM_SMOOTH, v.omega, z, r, tmp);
-            k0<V>(z0, val, lpm::SM_SMOOTH, v.omega, tmp, r, z);
+            double *it = (nu % 2 == 1) ? tmp : z, *ot = (nu % 2 == 1) ? z : tmp;
+            bsr<3, 6, lpm::BM_ADD>(v.nblock, v.P, e, 6, it, 4);
+            for (int s = 0; s < nu; s++) {
+                k0<V>(z0, val, lpm::SM_SMOOTH, v.omega, it, r, ot);
+                std::swap(it, ot);
+            }
         } else {
-            bsr<6, 6, lpm::BM_ADD>(v.nblock, v.P, e, 6, y[l].data(), 6);
-            bsr<6, 6, lpm::BM_SMOOTH>(v.nblock, v.A, y[l].data(), 6, x[l].data(), 6, b[l].data(), v.Dinv.data(), v.omega);
-            bsr<6, 6, lpm::BM_SMOOTH>(v.nblock, v.A, x[l].data(), 6, y[l].data(), 6, b[l].data(), v.Dinv.data(), v.omega);
+            double *it = (nu % 2 == 1) ? x[l].data() : y[l].data(), *ot = (nu % 2 == 1) ? y[l].data() : x[l].data();
+            bsr<6, 6, lpm::BM_ADD>(v.nblock, v.P, e, 6, it, 6);
+            for (int s = 0; s < nu; s++) {
+                bsr<6, 6, lpm::BM_SMOOTH>(v.nblock, v.A, it, 6, ot, 6, b[l].data(), v.Dinv.data(), v.omega);
+                std::swap(it, ot);
+            }
         }
     }
 }
@@ -193,11 +210,13 @@ int main(int argc, char **argv)
                         Pinv[(size_t)k * n + i] = H.levels[0].Dinv[(size_t)i * 9 + k];
             const Level0 z0{n, mask.data(), rowoff.data(), npad.data(), cols.data(), Pinv.data()};
             std::vector<double> z(4 * (size_t)n, 0.0), tmp(4 * (size_t)n, 0.0);
-            vcycle<double>(H, z0, val.data(), r.data(), z.data(), tmp.data());
+            const int nu = argc > 3 ? std::atoi(argv[3]) : 1;
+            vcycle<double>(H, z0, val.data(), r.data(), z.data(), tmp.data(), nu);
             wr(d + "/z.bin", z);
             std::vector<float> vf(val.begin(), val.end());
             std::fill(z.begin(), z.end(), 0.0);
-            vcycle<float>(H, z0, vf.data(), r.data(), z.data(), tmp.data());
+            std::fill(tmp.begin(), tmp.end(), 0.0);
+            vcycle<float>(H, z0, vf.data(), r.data(), z.data(), tmp.data(), nu);
             wr(d + "/z32.bin", z);
         }
     }

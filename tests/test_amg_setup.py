@@ -99,11 +99,11 @@ def _load_hierarchy(d):
     return levels, coarse, rd("coarse_chol.bin", np.float64).reshape(nc, nc), rd("coarse_inv.bin", np.float64).reshape(nc, nc)
 
 
-def _vcycle(levels, cinv):
-    """The V-cycle as the device runs it: on every level one damped
-    block-Jacobi sweep from zero, one more sweep, the residual restricted,
-    the coarse correction prolongated, two sweeps; the coarsest level
-    multiplies by the dense inverse."""
+def _vcycle(levels, cinv, nu=1):
+    """The V-cycle as the device runs it: on every level a damped block-Jacobi
+    sweep from zero and nu - 1 more, the residual restricted, the coarse
+    correction prolongated, nu sweeps; the coarsest level multiplies by the
+    dense inverse."""
     def smooth(lv, x, b):
         r = (b - lv["A"] @ x).reshape(-1, lv["bs"])
         return x + lv["omega"] * np.einsum("nij,nj->ni", lv["Dinv"], r).ravel()
@@ -113,10 +113,12 @@ def _vcycle(levels, cinv):
             return cinv @ b
         lv = levels[l]
         x = lv["omega"] * np.einsum("nij,nj->ni", lv["Dinv"], b.reshape(-1, lv["bs"])).ravel()
-        x = smooth(lv, x, b)
+        for _ in range(nu - 1):
+            x = smooth(lv, x, b)
         x = x + lv["P"] @ V(l + 1, lv["Pt"] @ (b - lv["A"] @ x))
-        x = smooth(lv, x, b)
-        return smooth(lv, x, b)
+        for _ in range(nu):
+            x = smooth(lv, x, b)
+        return x
     return lambda r: V(0, r)
 
 
@@ -140,8 +142,8 @@ def _pcg(A, M, b, rtol=1e-10, maxit=5000):
     return x, maxit
 
 
-@pytest.mark.parametrize("lattice,size", [(2, 10), (2, 16), (3, 6)])
-def test_hierarchy_preconditions_cg(oracle_mod, harness, tmp_path, lattice, size):
+@pytest.mark.parametrize("lattice,size,nu", [(2, 10, 1), (2, 16, 1), (2, 16, 2), (3, 6, 1), (3, 6, 3)])
+def test_hierarchy_preconditions_cg(oracle_mod, harness, tmp_path, lattice, size, nu):
     o, K, res, xyz, mask, conn, nconn = _system(oracle_mod, lattice, size)
     n = len(nconn)
     rowoff, npad, cols, val = _device_layout(K, conn, nconn)
@@ -155,7 +157,7 @@ def test_hierarchy_preconditions_cg(oracle_mod, harness, tmp_path, lattice, size
     r4 = np.zeros((n, 4))
     r4[:, :3] = b.reshape(n, 3)
     r4.tofile(os.path.join(d, "r.bin"))  # the harness also applies the device's V-cycle to it
-    subprocess.check_call([harness, d, "0.6"])
+    subprocess.check_call([harness, d, "0.6", str(nu)])
     levels, coarse, chol, cinv = _load_hierarchy(d)
     assert len(levels) >= 1
     # level 0 operates with the stiffness, constrained rows and columns removed
@@ -178,7 +180,7 @@ def test_hierarchy_preconditions_cg(oracle_mod, harness, tmp_path, lattice, size
     # the dense coarse factor and inverse
     assert np.allclose(chol @ chol.T, coarse.toarray() + np.diag((abs(coarse).sum(1).A1 == 0).astype(float)))
     assert np.allclose(cinv @ (chol @ chol.T), np.eye(len(cinv)), atol=1e-8)
-    M = _vcycle(levels, cinv)
+    M = _vcycle(levels, cinv, nu)
     # the device's launch sequence and per-row arithmetic (emulated on the
     # host) give the numpy V-cycle's result
     z = M(b)

@@ -55,6 +55,7 @@ def test_set_solver_defaults_and_preconditioner(fake):
     assert o.preconditioner == G.PRECOND_AMG and o.amg_spacing == 0.5 and o.cg_rtol == 1e-9
     d = G.default_opts()
     assert d.preconditioner == G.PRECOND_BJ and d.amg_spacing == 0.0 and d.amg_rebuild == 2.5
+    assert d.amg_sweeps == 1
     assert d.precision == G.PREC_FP64 and d.cg_forcing == 0.0
     with pytest.raises(KeyError):
         s.set_solver(no_such_option=1)
