@@ -288,8 +288,21 @@ void calcKnTv(void)
     }
     lpm_legacy_reset();
     check(lpm_create(&g_ctx, 0), "lpm_create");
-    if (g_opts_set)
-        check(lpm_set_solver(g_ctx, &g_opts), "lpm_set_solver");
+    {
+        // LPM_PRECOND=amg selects the multigrid preconditioner for an
+        // unmodified reference driver
+        lpm_solver_opts o;
+        if (g_opts_set)
+            o = g_opts;
+        else
+            lpm_default_solver_opts(&o);
+        const char *pc = std::getenv("LPM_PRECOND");
+        const bool amg = pc && std::strcmp(pc, "amg") == 0;
+        if (amg)
+            o.preconditioner = LPM_PRECOND_AMG;
+        if (g_opts_set || amg)
+            check(lpm_set_solver(g_ctx, &o), "lpm_set_solver");
+    }
     const int n = nparticle, nn = nneighbors;
     dvec x0 = flat2(xyz_initial, n, 3);
     check(lpm_setup_particles(g_ctx, lattice, radius, n, x0.data()), "lpm_setup_particles");
