@@ -185,8 +185,9 @@ class SCCase:
 
     def __init__(self, n=10, radius=0.1, E=200e3, nu=0.3, sigmay=250.0, H=2000.0,
                  strain=0.002, steps_per_quarter=20, cycles=2, newton_tol=1e-8,
-                 e_noise=0.0, seed=1):
+                 e_noise=0.0, seed=1, xi=0.0):
         self.n = n
+        self.xi = xi  # kinematic share of the linear hardening (J2_xi)
         self.radius = radius
         self.lattice = 2
         self.box = sc_box(n, n, n, radius)

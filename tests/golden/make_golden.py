@@ -323,11 +323,49 @@ def noise_case(out, tag="sc8_enoise"):
     print(f"{tag}: {n} particles, alpha max {arrs['s_alpha'].max():.3e}", flush=True)
 
 
+def kinematic_case(out, tag="sc6_kinematic"):
+    """Mixed linear hardening (J2_xi = 0.5: half kinematic, half isotropic)
+    over three quarters of a load cycle of SC 6^3 (8 steps per quarter: up to
+    +A, back to 0, on to -A, with reverse yielding): per-step iterations,
+    residuals and top displacement, and the final state with the back
+    stress."""
+    case = cases.SCCase(n=6, sigmay=150.0, xi=0.5, steps_per_quarter=8, cycles=1)
+    n = R.setup(case.lattice, case.radius, case.box)
+    nn = R.gint("nneighbors")
+    xyz0 = R.get_d2("xyz", n, 3)
+    types = cases.sc_types(xyz0, R.get_i1("nb", n), case.radius)
+    R.set_types(types, cases.NTYPE)
+    R.material(case.ce_per_type(), 0, np.full(n, case.sigmay), case.xi, case.H)
+    R.init_state()
+    R.set_cg_tol(1e-20, 0.0)
+    top = types == cases.T_TOP
+    rec = {k: [] for k in ("iters", "nres", "disp_top")}
+    alpha_max = []
+    for s_, stp in enumerate(case.schedule[:24], start=1):
+        with R.quiet():
+            st = R.load_step(cases.sc_bcs(stp), [], case.newton_tol)
+        xyz = R.get_d2("xyz", n, 3)
+        rec["iters"].append(st[0])
+        rec["nres"].append(st[3])
+        rec["disp_top"].append((xyz[top, 2].sum() - xyz0[top, 2].sum()) / top.sum())
+        alpha_max.append(R.get_d2("J2_alpha", n, 3)[:, 1].max())
+    print(f"{tag}: plastic strain max per step {np.array2string(np.array(alpha_max), precision=2)}", flush=True)
+    arrs = {k: np.array(v) for k, v in rec.items()}
+    arrs["types"] = types
+    arrs["s_xyz"] = R.get_d2("xyz", n, 3)
+    arrs["s_alpha"] = R.get_d2("J2_alpha", n, 3)[:, 1]
+    arrs["s_beta"] = R.get_d3("J2_beta", n, 6, 1)
+    arrs["s_F"] = R.get_d2("F", n, nn)
+    np.savez_compressed(os.path.join(out, f"{tag}.npz"), **arrs)
+    print(f"{tag}: {n} particles, {len(rec['iters'])} steps, alpha max {arrs['s_alpha'].max():.3e}, "
+          f"|beta| max {np.abs(arrs['s_beta']).max():.3e}", flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--fcc-steps", type=int, default=12)
-    ap.add_argument("--only", choices=["sc", "fcc", "force", "ductile", "brittle", "enoise"] +
+    ap.add_argument("--only", choices=["sc", "fcc", "force", "ductile", "brittle", "enoise", "kinematic"] +
                     ["setup_" + k for k in cases.SETUP_SHAPES], default=None)
     ap.add_argument("--out", default=HERE)
     args = ap.parse_args()
@@ -340,6 +378,8 @@ def main():
         force_case(args.out)
     elif args.only == "enoise":
         noise_case(args.out)
+    elif args.only == "kinematic":
+        kinematic_case(args.out)
     elif args.only in ("ductile", "brittle"):
         damage_case(args.out, args.only)
     elif args.only and args.only.startswith("setup_"):
@@ -348,7 +388,7 @@ def main():
         sc_case(args.out, args.steps)
     else:
         import subprocess
-        for which in ["sc", "fcc", "force", "ductile", "brittle", "enoise"] + \
+        for which in ["sc", "fcc", "force", "ductile", "brittle", "enoise", "kinematic"] + \
                 ["setup_" + k for k in cases.SETUP_SHAPES]:
             subprocess.check_call([sys.executable, __file__, "--only", which, "--steps", str(args.steps),
                                    "--fcc-steps", str(args.fcc_steps), "--out", args.out])

@@ -13,7 +13,7 @@ def sc_oracle(O, case, threads=4):
     types = cases.sc_types(xyz, nb, case.radius)
     o.set_types(types)
     c11, c12, c44 = material_arrays(case, n)
-    o.set_material(c11, c12, c44, case.sigmay, case.H, 0.0, 0)
+    o.set_material(c11, c12, c44, case.sigmay, case.H, getattr(case, "xi", 0.0), 0)
     o.init_state()
     return o, types
 
@@ -26,7 +26,7 @@ def sc_gpu(G, case, precision=0, **solver):
     types = cases.sc_types(xyz, nb, case.radius)
     s.set_types(types)
     c11, c12, c44 = material_arrays(case, n)
-    s.set_material(c11, c12, c44, case.sigmay, case.H, 0.0, G.PL_J2)
+    s.set_material(c11, c12, c44, case.sigmay, case.H, getattr(case, "xi", 0.0), G.PL_J2)
     s.init_state()
     s.set_solver(precision=precision, newton_tol=case.newton_tol, **solver)
     return s, types

@@ -281,3 +281,29 @@ def test_per_particle_moduli_bit_exact(oracle_mod):
     assert np.array_equal(o.d("alpha1", (n,)), g["s_alpha"])
     assert np.array_equal(o.d("F", (n, nn)), g["s_F"])
     assert g["s_alpha"].max() > 0.0
+
+
+def test_kinematic_hardening_bit_exact(oracle_mod):
+    """Mixed linear hardening (J2_xi = 0.5) over three quarters of a load
+    cycle of SC 6^3 with reverse yielding: per-step Newton iterations,
+    residuals and top displacement, and the final positions, plastic strain,
+    back stress and bond forces equal the reference's
+    (tests/golden/sc6_kinematic.npz)."""
+    case = cases.SCCase(n=6, sigmay=150.0, xi=0.5, steps_per_quarter=8, cycles=1)
+    g = golden("sc6_kinematic.npz")
+    o, types = sc_oracle(oracle_mod, case, threads=1)
+    n, nn = o.n, o.nn
+    assert np.array_equal(types, g["types"])
+    x0 = o.d("xyz_initial", (n, 3))
+    top = types == cases.T_TOP
+    assert len(g["iters"]) == 24
+    for k, stp in enumerate(case.schedule[:24]):
+        st = o.load_step(cases.sc_bcs(stp), [], case.newton_tol, 100, 1e-20, 0.0)
+        assert st[0] == g["iters"][k] and st[3] == g["nres"][k], k
+        xyz = o.d("xyz", (n, 3))
+        assert (xyz[top, 2].sum() - x0[top, 2].sum()) / top.sum() == g["disp_top"][k], k
+    assert np.array_equal(o.d("xyz", (n, 3)), g["s_xyz"])
+    assert np.array_equal(o.d("alpha1", (n,)), g["s_alpha"])
+    assert np.array_equal(o.d("beta1", (n, 6)), g["s_beta"])
+    assert np.array_equal(o.d("F", (n, nn)), g["s_F"])
+    assert np.abs(g["s_beta"]).max() > 0.0
