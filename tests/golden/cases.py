@@ -229,20 +229,29 @@ class FCCCase:
     """FCC single crystal, crystal plasticity, [001] tension (C3 at ncell=80)."""
 
     def __init__(self, ncell=4, radius=0.1, strain=0.02, steps=100, newton_tol=1e-8,
-                 tau0=50.0, h0=500.0, p=20.0, q=1.0, eta=10.0, maxloop=10, dtime=1.0):
+                 tau0=50.0, h0=500.0, p=20.0, q=1.0, eta=10.0, maxloop=10, dtime=1.0, taus=1e30):
         self.lattice = 3
         self.radius = radius
         self.box = fcc_box(ncell, radius)
         # Al constants (examples/FCC_Al_R0.3_001_tension.c:200-202)
         self.C11, self.C12, self.C44 = 107.3e3, 60.8e3, 28.3e3
-        # linear hardening: taus -> infinity makes h = h0 (src/constitutive.c:1125-1126)
-        self.cp = [tau0, 1e30, h0, p, q, eta, maxloop, dtime]
+        # linear hardening by default: taus -> infinity makes h = h0
+        # (src/constitutive.c:1125-1126); a finite taus saturates it
+        self.cp = [tau0, taus, h0, p, q, eta, maxloop, dtime]
         self.height = ncell * 4 * radius / np.sqrt(2.0)
         self.schedule = [strain * self.height / steps] * steps
         self.newton_tol = newton_tol
 
     def ce_per_type(self):
         return np.tile([self.C11, self.C12, self.C44], (NTYPE, 1))
+
+
+# Saturating, latent-hardening, more rate-sensitive crystal plasticity: the
+# hardening modulus h0 / cosh^2(h0 A / (taus - tau0)) of
+# src/constitutive.c:1124-1125 falls from h0 towards zero as the accumulated
+# slip A grows (with taus -> infinity it stays h0), and latent hardening
+# ratio q = 1.4.
+FCC_SAT = dict(tau0=50.0, taus=150.0, h0=500.0, p=20.0, q=1.2)
 
 
 class BatchCase:

@@ -114,9 +114,9 @@ def sc_case(out, nsteps, tag="sc10"):
     np.savez_compressed(os.path.join(out, f"{tag}_cyclic.npz"), **arrs)
 
 
-def fcc_case(out, nsteps, tag="fcc4"):
+def fcc_case(out, nsteps, tag="fcc4", case=None):
     """FCC crystal plasticity (computeBondForceCPMiehe), [001] tension, 4^3 cells."""
-    case = cases.FCCCase(ncell=4)
+    case = case or cases.FCCCase(ncell=4)
     t0 = time.time()
     n = R.setup(case.lattice, case.radius, case.box)
     nn = R.gint("nneighbors")
@@ -365,7 +365,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--fcc-steps", type=int, default=12)
-    ap.add_argument("--only", choices=["sc", "fcc", "force", "ductile", "brittle", "enoise", "kinematic"] +
+    ap.add_argument("--only", choices=["sc", "fcc", "force", "ductile", "brittle", "enoise", "kinematic", "fcc_sat"] +
                     ["setup_" + k for k in cases.SETUP_SHAPES], default=None)
     ap.add_argument("--out", default=HERE)
     args = ap.parse_args()
@@ -380,6 +380,8 @@ def main():
         noise_case(args.out)
     elif args.only == "kinematic":
         kinematic_case(args.out)
+    elif args.only == "fcc_sat":
+        fcc_case(args.out, args.fcc_steps, tag="fcc4_sat", case=cases.FCCCase(ncell=4, **cases.FCC_SAT))
     elif args.only in ("ductile", "brittle"):
         damage_case(args.out, args.only)
     elif args.only and args.only.startswith("setup_"):
@@ -388,7 +390,7 @@ def main():
         sc_case(args.out, args.steps)
     else:
         import subprocess
-        for which in ["sc", "fcc", "force", "ductile", "brittle", "enoise", "kinematic"] + \
+        for which in ["sc", "fcc", "force", "ductile", "brittle", "enoise", "kinematic", "fcc_sat"] + \
                 ["setup_" + k for k in cases.SETUP_SHAPES]:
             subprocess.check_call([sys.executable, __file__, "--only", which, "--steps", str(args.steps),
                                    "--fcc-steps", str(args.fcc_steps), "--out", args.out])

@@ -69,6 +69,32 @@ def test_fcc_cp_steps_match_oracle(oracle_mod, gpu_lib, precision):
     assert np.abs(s.get("cp_gy") - gy_o).max() <= 1e-8 * np.abs(gy_o).max()
 
 
+@pytest.mark.skipif(__import__("os").environ.get("LPM_UNVERIFIED_GPU_TESTS") != "1",
+                    reason="not yet run on a GPU (set LPM_UNVERIFIED_GPU_TESTS=1)")
+def test_fcc_cp_latent_saturating_match_oracle(oracle_mod, gpu_lib):
+    """Latent hardening (q = 1.2) and a finite saturation stress, steps 1-9
+    (the case the oracle matches bit for bit against the reference,
+    tests/golden/fcc4_sat_cp.npz): displacements and slip state agree with the
+    oracle."""
+    case = cases.FCCCase(ncell=4, newton_tol=1e-10, **cases.FCC_SAT)
+    s, _ = fcc_gpu(gpu_lib, case, precision=0, newton_maxiter=300, cg_rtol=1e-11)
+    o, _ = fcc_oracle(oracle_mod, case)
+    n = o.n
+    x0 = o.d("xyz_initial", (n, 3))
+    for k, stp in enumerate(case.schedule[:9]):
+        st = s.load_step(cases.sc_bcs(stp))
+        o.load_step(cases.sc_bcs(stp), [], 1e-10, 300, 1e-22, 0.0)
+        assert st["status"] == 0, (k + 1, st)
+        du_g = s.get("xyz") - x0
+        du_o = o.d("xyz", (n, 3)) - x0
+        assert np.abs(du_g - du_o).max() < 1e-8 * np.abs(du_o).max(), k + 1
+    A_o = o.d("cp_A1", (n,))
+    assert A_o.max() > 0.0
+    assert np.abs(s.get("cp_A") - A_o).max() <= 1e-8 * A_o.max()
+    gy_o = o.d("cp_gy1", (n, 24))
+    assert np.abs(s.get("cp_gy") - gy_o).max() <= 1e-8 * np.abs(gy_o).max()
+
+
 @pytest.mark.parametrize("steps", [0, 3])
 def test_fcc_stiffness_vs_fd(oracle_mod, gpu_lib, steps):
     """Analytic tangent vs the reference's forward-difference K on the FCC

@@ -196,6 +196,37 @@ def test_fcc_cp_bit_exact(oracle_mod):
     assert o.d("cp_A1", (n,)).max() > 0.0
 
 
+def test_fcc_cp_latent_saturating_bit_exact(oracle_mod):
+    """Crystal plasticity with latent hardening (q = 1.2) and a finite
+    saturation stress (taus = 150 MPa), 4^3 cells, 9 steps (the 9th plastic):
+    the oracle reproduces the reference's iterations, residuals,
+    displacements and slip state (tests/golden/fcc4_sat_cp.npz).  Latent
+    hardening changes the plastic step (residual 3.61e-7 against 3.71e-7
+    with q = 1); the reference's modified Newton stops converging from the
+    next step on, so the case ends there."""
+    g = golden("fcc4_sat_cp.npz")
+    case = cases.FCCCase(ncell=4, **cases.FCC_SAT)
+    assert np.array_equal(g["cp"], np.array(case.cp))
+    o, types = fcc_oracle(oracle_mod, case)
+    n, nn = o.n, o.nn
+    ns = 24
+    assert np.array_equal(g["cp_Cab"], o.d("cp_Cab", (n, ns * ns)))
+    x0 = o.d("xyz_initial", (n, 3))
+    top = types == cases.T_TOP
+    for k, stp in enumerate(g["schedule"]):
+        st = o.load_step(cases.sc_bcs(stp), [], case.newton_tol, 100, 1e-20, 0.0)
+        assert st[0] == g["iters"][k] and st[3] == g["nres"][k], k
+        xyz = o.d("xyz", (n, 3))
+        assert (xyz[top, 2].sum() - x0[top, 2].sum()) / top.sum() == g["disp_top"][k]
+    last = len(g["schedule"])
+    assert np.array_equal(g[f"s{last}_xyz"], o.d("xyz", (n, 3)))
+    assert np.array_equal(g[f"s{last}_cp_gy"], o.d("cp_gy1", (n, ns)))
+    assert np.array_equal(g[f"s{last}_cp_A_single"], o.d("cp_As1", (n, ns)))
+    assert np.array_equal(g[f"s{last}_cp_A"], o.d("cp_A1", (n,)))
+    assert np.array_equal(g[f"s{last}_dLp"], o.d("dLp1", (n, nn)))
+    assert o.d("cp_A1", (n,)).max() > 0.0
+
+
 def test_fcc_schmid_factors_001():
     """[001] tension: 8 of the 24 signed {111}<110> systems carry the Schmid
     factor 1/sqrt(6) (both signs of the 4 loaded slip directions... here: the
