@@ -160,8 +160,9 @@ def run_ours(args):
         precond = G.PRECOND_AMG if args.precond == "amg" else G.PRECOND_BJ
         s, types = build_specimen(G, case, prec, stream.cuda_stream, precond)
         tuning = None
+        warm = []
         for k in range(W):
-            s.load_step(cases.sc_bcs(sched[k]))
+            warm.append(s.load_step(cases.sc_bcs(sched[k])))
             if k == 0 and not args.no_autotune:
                 tuning = s.autotune()  # launch shapes from the project's autotuner
         barrier()
@@ -180,7 +181,8 @@ def run_ours(args):
         ck = clocks.stop()
         spmv_ms, spmv_cnt = s.spmv_timing(reset=3)
         ms = max_over_ranks(ms, device="cuda")
-        results[prec_name] = dict(ms=ms, stats=stats, spmv_ms=spmv_ms, spmv_cnt=spmv_cnt, clocks=ck, tuning=tuning,
+        results[prec_name] = dict(ms=ms, stats=stats, warm=warm, spmv_ms=spmv_ms, spmv_cnt=spmv_cnt, clocks=ck,
+                                  tuning=tuning,
                                   spmv_bytes=s.spmv_bytes(prec), xyz=s.get("xyz"), x0=s.get("xyz_initial"),
                                   n=s.n, nnzb=s.sizes()["nnz_blocks"])
         s.close()
@@ -198,10 +200,17 @@ def run_ours(args):
         du_m = mixed["xyz"] - mixed["x0"]
         du_f = f["xyz"] - f["x0"]
         err = float(np.abs(du_m - du_f).max() / np.abs(du_f).max())
+    if args.compare_du:
+        ref = np.load(args.compare_du)
+        du = mixed["xyz"] - mixed["x0"]
+        err = float(np.abs(du - ref).max() / np.abs(ref).max())
     e2e = run_e2e(args, case) if (not args.no_e2e and rank == 0) else None
     counts = step_counts(args.size, W, K, results["fp64"]["stats"] if "fp64" in results else None)
     cpu = run_cpu_baseline(args, case, counts) if (not args.no_cpu and rank == 0) else None
     agg = lambda key: int(sum(st[key] for st in mixed["stats"]))  # noqa: E731
+    amg = None
+    if args.precond == "bj" and not args.no_amg and world == 1:
+        amg = run_amg_side(args, mixed["xyz"] - mixed["x0"], value)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": mixed["ms"] / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -219,6 +228,9 @@ def run_ours(args):
                                      if "fp64" in results else None),
                    "l2": "SpMV stream of 2.4 GB per call > 129 MB L2 (no flush needed)",
                    "tuning": mixed["tuning"],
+                   "amg_build_ms": sum(st["ms_amg_build"] for st in mixed["warm"] + mixed["stats"]),
+                   "amg_builds": sum(st["amg_builds"] for st in mixed["warm"] + mixed["stats"]),
+                   "multigrid": amg,
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
@@ -234,6 +246,40 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def run_amg_side(args, du_bj, bj_value):
+    """The same workload with the multigrid preconditioner, measured in a child
+    process after the block-Jacobi line is complete (a failure there cannot
+    cost the headline): its load steps/s, the ratio to block-Jacobi, PCG
+    iterations, hierarchy build time, and its displacements against
+    block-Jacobi's."""
+    import subprocess
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        ref = os.path.join(d, "du_bj.npy")
+        np.save(ref, du_bj)
+        cmd = [sys.executable, os.path.abspath(__file__), "--precond", "amg", "--no-fp64", "--no-e2e", "--no-cpu",
+               "--no-amg", "--steps", str(args.steps), "--warmup", str(args.warmup), "--size", str(args.size),
+               "--compare-du", ref]
+        if args.no_autotune:
+            cmd.append("--no-autotune")
+        try:
+            out = subprocess.run(cmd, capture_output=True, text=True, timeout=900)
+        except subprocess.TimeoutExpired:
+            return {"error": "timed out after 900 s"}
+        lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
+        if out.returncode != 0 or not lines:
+            tail = (out.stderr or out.stdout).strip().splitlines()[-1:] or [""]
+            return {"error": f"exit {out.returncode}: {tail[0][:300]}"}
+        line = json.loads(lines[-1])
+    c = line["config"]
+    return {"steps_per_s": line["value"], "ms_per_step": line["ms_per_step"],
+            "over_block_jacobi": line["value"] / bj_value if bj_value else None,
+            "cg_iters": c["cg_iters"], "newton_iters": c["newton_iters"], "reliable_updates": c["reliable_updates"],
+            "hierarchy_builds": c["amg_builds"], "hierarchy_build_ms": c["amg_build_ms"],
+            "disp_err_vs_block_jacobi": c["disp_err_mixed_vs_fp64"], "gpu_launches": line["gpu_launches"],
+            "clocks": line.get("clocks")}
 
 
 def amg_levels(n, coarse_blocks=150):
@@ -666,6 +712,9 @@ def main():
     ap.add_argument("--adj-fd", action="store_true")
     ap.add_argument("--precond", default="bj", choices=["bj", "amg"],
                     help="sc workload: PCG preconditioner (block-Jacobi or the multigrid V-cycle)")
+    ap.add_argument("--no-amg", action="store_true",
+                    help="sc workload: skip the side measurement with the multigrid preconditioner")
+    ap.add_argument("--compare-du", default=None, help=argparse.SUPPRESS)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
