@@ -18,9 +18,41 @@ namespace lpm {
 enum { SM_SMOOTH = 0, SM_RESID = 1 };
 enum { BM_SET = 0, BM_ADD = 1, BM_SMOOTH = 2, BM_RESID = 3 };
 
+// Four consecutive values of one stiffness component (16-byte aligned for
+// FP32, 32-byte for FP64: rows start at multiples of 4 blocks and hold a
+// multiple of 4), one vector load on the device.
+AMG_HD void load4(const float *p, float (&v)[4])
+{
+#ifdef __CUDA_ARCH__
+    const float4 t = __ldcs(reinterpret_cast<const float4 *>(p));
+    v[0] = t.x;
+    v[1] = t.y;
+    v[2] = t.z;
+    v[3] = t.w;
+#else
+    for (int j = 0; j < 4; j++)
+        v[j] = p[j];
+#endif
+}
+AMG_HD void load4(const double *p, double (&v)[4])
+{
+#ifdef __CUDA_ARCH__
+    const double2 a = __ldcs(reinterpret_cast<const double2 *>(p));
+    const double2 b = __ldcs(reinterpret_cast<const double2 *>(p) + 1);
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = b.x;
+    v[3] = b.y;
+#else
+    for (int j = 0; j < 4; j++)
+        v[j] = p[j];
+#endif
+}
+
 // Level 0: partial product of block row `row` of the stiffness (device
-// layout: npad[row] blocks at rowoff[row], component-major values) over the
-// blocks k = sub, sub + nl, ...; products in V.
+// layout: npad[row] blocks at rowoff[row], npad a multiple of 4,
+// component-major values) over the groups of 4 consecutive blocks
+// b0 = 4 sub, 4 (sub + nl), ...; products in V.
 template <typename V>
 AMG_HD void k0_row_partial(const long long *rowoff, const int *npad, const int *cols, const V *val,
                            const double *x, int row, int sub, int nl, V &y0, V &y1, V &y2)
@@ -28,12 +60,17 @@ AMG_HD void k0_row_partial(const long long *rowoff, const int *npad, const int *
     const long long off = rowoff[row];
     const int np = npad[row];
     const V *vr = val + 9 * off;
-    for (int k = sub; k < np; k += nl) {
-        const double *xv = x + 4 * (size_t)cols[off + k];
-        const V x0 = (V)xv[0], x1 = (V)xv[1], x2 = (V)xv[2];
-        y0 += vr[(size_t)0 * np + k] * x0 + vr[(size_t)1 * np + k] * x1 + vr[(size_t)2 * np + k] * x2;
-        y1 += vr[(size_t)3 * np + k] * x0 + vr[(size_t)4 * np + k] * x1 + vr[(size_t)5 * np + k] * x2;
-        y2 += vr[(size_t)6 * np + k] * x0 + vr[(size_t)7 * np + k] * x1 + vr[(size_t)8 * np + k] * x2;
+    for (int b0 = 4 * sub; b0 < np; b0 += 4 * nl) {
+        V v[9][4];
+        for (int k = 0; k < 9; k++)
+            load4(vr + (size_t)k * np + b0, v[k]);
+        for (int j = 0; j < 4; j++) {
+            const double *xv = x + 4 * (size_t)cols[off + b0 + j];
+            const V x0 = (V)xv[0], x1 = (V)xv[1], x2 = (V)xv[2];
+            y0 += v[0][j] * x0 + v[1][j] * x1 + v[2][j] * x2;
+            y1 += v[3][j] * x0 + v[4][j] * x1 + v[5][j] * x2;
+            y2 += v[6][j] * x0 + v[7][j] * x1 + v[8][j] * x2;
+        }
     }
 }
 
