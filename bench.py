@@ -633,7 +633,8 @@ def run_fcc(args):
         # FP64 CG vectors with the FP32 stiffness: at 80^3 cells the FCC system
         # is too ill-conditioned for FP32 vectors (their PCG stagnates)
         s.set_solver(precision=prec, newton_tol=case.newton_tol, newton_maxiter=300, cg_rtol=1e-10,
-                     cg_maxiter=40000, mixed_vectors=64)
+                     cg_maxiter=40000, mixed_vectors=64,
+                     preconditioner=G.PRECOND_AMG if args.precond == "amg" else G.PRECOND_BJ)
         setup_s = time.perf_counter() - t0
         for k in range(W):
             s.load_step(cases.sc_bcs(case.schedule[k]))
@@ -661,6 +662,8 @@ def run_fcc(args):
         "dtype": "f32 stiffness and SpMV products, f64 PCG vectors, residual, reliable updates and CP return map",
         "data": "synthetic (FCC lattice)",
         "config": {"workload": f"FCC {args.fcc_cells}^3 cells CP [001] tension, load steps {W + 1}-{W + K} of 100",
+                   "preconditioner": "smoothed-aggregation multigrid V-cycle" if args.precond == "amg"
+                   else "block-Jacobi",
                    "particles": m["n"], "setup_s": m["setup_s"], "fp64_steps_per_s": K / (f["ms"] / 1e3),
                    "mixed_over_fp64": f["ms"] / m["ms"], "disp_err_mixed_vs_fp64": err,
                    "newton_iters": agg(m["stats"], "newton_iters"), "cg_iters": agg(m["stats"], "cg_iters"),
@@ -711,7 +714,7 @@ def main():
                     help="adjoint workload: inexact-Newton forcing cap (opts.cg_forcing; 0 = exact solves)")
     ap.add_argument("--adj-fd", action="store_true")
     ap.add_argument("--precond", default="bj", choices=["bj", "amg"],
-                    help="sc workload: PCG preconditioner (block-Jacobi or the multigrid V-cycle)")
+                    help="sc and fcc workloads: PCG preconditioner (block-Jacobi or the multigrid V-cycle)")
     ap.add_argument("--no-amg", action="store_true",
                     help="sc workload: skip the side measurement with the multigrid preconditioner")
     ap.add_argument("--compare-du", default=None, help=argparse.SUPPRESS)
