@@ -222,8 +222,8 @@ void prefix(const std::vector<long long> &cnt, avec<long long> &ptr)
 }
 
 // Transpose of a block-CSR matrix; rows of the result list their columns in
-// ascending order.  Per-thread column counts over contiguous row ranges give
-// every block its place, so the fill runs in parallel.
+// ascending order.  Column counts per contiguous chunk of rows give every
+// block its place, so the chunks fill in parallel (any number of threads).
 Bsr transpose(const Bsr &A)
 {
     Bsr T;
@@ -237,13 +237,11 @@ Bsr transpose(const Bsr &A)
     std::vector<int> lo(nt + 1);
     for (int t = 0; t <= nt; t++)
         lo[t] = (int)((long long)A.nbr * t / nt);
-#pragma omp parallel num_threads(nt)
-    {
-        const int t = omp_get_thread_num();
+#pragma omp parallel for schedule(static, 1)
+    for (int t = 0; t < nt; t++)
         for (int i = lo[t]; i < lo[t + 1]; i++)
             for (long long k = A.ptr[i]; k < A.ptr[i + 1]; k++)
                 cnt[t][A.col[k]]++;
-    }
     T.ptr.assign((size_t)A.nbc + 1, 0);
     for (int c = 0; c < A.nbc; c++) {
         long long s = 0;
@@ -262,9 +260,8 @@ Bsr transpose(const Bsr &A)
     }
     T.col.resize((size_t)T.ptr[A.nbc]);
     T.val.resize((size_t)T.ptr[A.nbc] * bsz);
-#pragma omp parallel num_threads(nt)
-    {
-        const int t = omp_get_thread_num();
+#pragma omp parallel for schedule(static, 1)
+    for (int t = 0; t < nt; t++)
         for (int i = lo[t]; i < lo[t + 1]; i++)
             for (long long k = A.ptr[i]; k < A.ptr[i + 1]; k++) {
                 const long long q = cnt[t][A.col[k]]++;
@@ -275,7 +272,6 @@ Bsr transpose(const Bsr &A)
                     for (int c = 0; c < A.C; c++)
                         d[c * A.R + r] = s[r * A.C + c];
             }
-    }
     return T;
 }
 
