@@ -222,3 +222,23 @@ def test_single_level_is_the_exact_inverse(oracle_mod, harness, tmp_path):
     x = np.zeros(3 * n)
     x[free] = np.linalg.solve(K[free][:, free].toarray(), b[free])
     assert np.abs(z - x).max() <= 1e-9 * np.abs(x).max()
+
+
+def test_hierarchy_independent_of_thread_count(oracle_mod, harness, tmp_path):
+    """Every output of the build is laid out by counting passes and summed in
+    row order: 1 and 5 threads give the same bytes."""
+    o, K, res, xyz, mask, conn, nconn = _system(oracle_mod, 2, 16)
+    n = len(nconn)
+    rowoff, npad, cols, val = _device_layout(K, conn, nconn)
+    outs = []
+    for threads in (1, 5):
+        d = tmp_path / f"t{threads}"
+        d.mkdir()
+        open(d / "n.txt", "w").write(str(n))
+        for name, arr in (("xyz", xyz), ("mask", mask), ("rowoff", rowoff), ("npad", npad),
+                          ("nconn", nconn.astype(np.int32)), ("cols", cols), ("val", val)):
+            np.ascontiguousarray(arr).tofile(d / f"{name}.bin")
+        subprocess.check_call([harness, str(d), "0.6"], env=dict(os.environ, OMP_NUM_THREADS=str(threads)))
+        outs.append({p.name: p.read_bytes() for p in sorted(d.iterdir()) if p.name.startswith(("L", "coarse"))})
+    assert outs[0].keys() == outs[1].keys() and len(outs[0]) > 5
+    assert all(outs[0][k] == outs[1][k] for k in outs[0])
