@@ -519,7 +519,9 @@ int lpm_set_solver(lpm_ctx *ctx, const lpm_solver_opts *o)
         return fail(LPM_ERR_ARG, "invalid solver options");
     Ctx &c = ctx->c;
     const bool prec_change = c.opts.precision != o->precision;
-    if (c.amg && c.opts.amg_spacing != o->amg_spacing)
+    if (c.amg && o->preconditioner != LPM_PRECOND_AMG)
+        free_amg(c);  // graphs that use it are dropped below
+    else if (c.amg && c.opts.amg_spacing != o->amg_spacing)
         c.amg->stale = true;
     c.opts = *o;
     c.vec64_fallback = false;
