@@ -43,7 +43,7 @@ struct AmgLevel {
     int bs = 0;                // DOFs per block row: 3 on level 0, 6 above
     Bsr A;                     // operator of the level; empty on level 0 (the stiffness itself)
     std::vector<double> Dinv;  // inverse of each bs x bs diagonal block, row-major
-    double omega = 1.0;        // smoother damping, 1 / rho(D^-1 A)
+    double omega = 1.0;        // smoother damping, 4/3 / rho(D^-1 A)
     Bsr P;                     // prolongation from the next level: bs x 6 blocks
     Bsr Pt;                    // its transpose (restriction): 6 x bs blocks
 };

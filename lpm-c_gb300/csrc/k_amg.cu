@@ -4,7 +4,7 @@
 // the device (AmgDev).
 //
 // V-cycle on level l (operator A_l, block-Jacobi inverse D_l^-1, damping
-// omega_l = 1 / rho(D_l^-1 A_l)), nu = opts.amg_sweeps:
+// omega_l = 4/3 / rho(D_l^-1 A_l)), nu = opts.amg_sweeps:
 //     x = omega D^-1 b                      (first sweep, from zero)
 //     nu - 1 sweeps x += omega D^-1 (b - A x)
 //     b_{l+1} = P_l^T (b - A x)             (residual, restriction)

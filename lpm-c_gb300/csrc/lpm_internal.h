@@ -125,7 +125,7 @@ struct AsyncWriter;
 struct AmgDevLevel {
     int nb = 0, bs = 0;  // block rows, DOFs per block row
     int nnext = 0;       // block rows of the next level
-    double omega = 1.0;  // smoother damping 1 / rho(D^-1 A)
+    double omega = 1.0;  // smoother damping 4/3 / rho(D^-1 A)
     long long *a_ptr = nullptr;   // levels >= 1: operator, 6 x 6 blocks
     int *a_col = nullptr;
     double *a_val = nullptr;
