@@ -119,21 +119,23 @@ AMG_HD void jacobi0_row(int n, int i, uint8_t m, const double *Pinv, double omeg
     o[3] = 0.0;
 }
 
-// Block-CSR level: partial y of block row `row` (R x C row-major blocks;
-// block column j of x at x[j * SX]) over the blocks ptr[row] + sub, + nl, ...
-template <int R, int C>
-AMG_HD void bsr_row_partial(const long long *ptr, const int *col, const double *val, const double *x, int SX,
+// Block-CSR level: partial y of block row `row` (R x C row-major blocks of
+// VT, FP64 for the coarse operators, FP32 for the prolongation and
+// restriction; block column j of x at x[j * SX]) over the blocks
+// ptr[row] + sub, + nl, ...; products and sums in FP64.
+template <int R, int C, typename VT>
+AMG_HD void bsr_row_partial(const long long *ptr, const int *col, const VT *val, const double *x, int SX,
                             int row, int sub, int nl, double (&y)[R])
 {
     for (long long k = ptr[row] + sub; k < ptr[row + 1]; k += nl) {
-        const double *blk = val + (size_t)k * (R * C);
+        const VT *blk = val + (size_t)k * (R * C);
         const double *xc = x + (size_t)col[k] * SX;
         double xv[C];
         for (int c = 0; c < C; c++)
             xv[c] = xc[c];
         for (int r = 0; r < R; r++)
             for (int c = 0; c < C; c++)
-                y[r] += blk[r * C + c] * xv[c];
+                y[r] += (double)blk[r * C + c] * xv[c];
     }
 }
 

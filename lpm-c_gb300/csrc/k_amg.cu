@@ -288,9 +288,9 @@ constexpr int BL_LANES = 8;  // lanes per block row of the coarse-level kernels
 // R x C blocks, 8 lanes per block row, epilogue by MODE (amg_rows.h):
 // restriction (BM_SET), prolongation (BM_ADD), coarse smoothing (BM_SMOOTH)
 // and residual (BM_RESID).
-template <int R, int C, int MODE>
+template <int R, int C, int MODE, typename VT>
 __global__ void __launch_bounds__(ATPB) k_amg_bsr(int nbr, const long long *__restrict__ ptr,
-                                                  const int *__restrict__ col, const double *__restrict__ val,
+                                                  const int *__restrict__ col, const VT *__restrict__ val,
                                                   const double *__restrict__ x, int SX, double *__restrict__ out,
                                                   int SY, const double *__restrict__ b,
                                                   const double *__restrict__ dinv, double omega,
@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(ATPB) k_amg_bsr(int nbr, const long long *__re
 #pragma unroll
         for (int r = 0; r < R; r++)
             y[r] = 0.0;
-        bsr_row_partial<R, C>(ptr, col, val, x, SX, row, sub, BL_LANES, y);
+        bsr_row_partial<R, C, VT>(ptr, col, val, x, SX, row, sub, BL_LANES, y);
 #pragma unroll
         for (int o = BL_LANES / 2; o > 0; o >>= 1)
 #pragma unroll
@@ -382,13 +382,13 @@ static void k0_launch(Ctx &c, bool k32, int mode, double omega, const dvec4 *xv,
     }
 }
 
-template <int R, int C, int MODE>
-static void bsr_launch(Ctx &c, int nbr, const long long *ptr, const int *col, const double *val, const double *x,
+template <int R, int C, int MODE, typename VT>
+static void bsr_launch(Ctx &c, int nbr, const long long *ptr, const int *col, const VT *val, const double *x,
                        int SX, double *out, int SY, const double *b = nullptr, const double *dinv = nullptr,
                        double omega = 0.0)
 {
     const int g = grid_for(c, (long long)nbr * BL_LANES);
-    k_amg_bsr<R, C, MODE><<<g, ATPB, 0, c.stream>>>(nbr, ptr, col, val, x, SX, out, SY, b, dinv, omega, c.sc);
+    k_amg_bsr<R, C, MODE, VT><<<g, ATPB, 0, c.stream>>>(nbr, ptr, col, val, x, SX, out, SY, b, dinv, omega, c.sc);
 }
 
 // With nu sweeps before and after the coarse correction, the iterate starts in
@@ -498,6 +498,17 @@ static int amg_alloc_copy(T *&d, const T *h, size_t count)
     return LPM_OK;
 }
 
+// prolongation and restriction values are kept in FP32 on the device: they
+// only shape the preconditioner, and they are read twice per V-cycle
+static std::vector<float> to_float(const avec<double> &v)
+{
+    std::vector<float> f(v.size());
+#pragma omp parallel for schedule(static)
+    for (long long k = 0; k < (long long)v.size(); k++)
+        f[k] = (float)v[k];
+    return f;
+}
+
 static void amg_free_device(AmgDev &H)
 {
     for (AmgDevLevel &v : H.lv) {
@@ -539,10 +550,10 @@ static int amg_upload(AmgDev &H, const AmgHierarchy &h)
         v.omega = s.omega;
         if ((rc = amg_alloc_copy(v.p_ptr, s.P.ptr.data(), s.P.ptr.size())) ||
             (rc = amg_alloc_copy(v.p_col, s.P.col.data(), s.P.col.size())) ||
-            (rc = amg_alloc_copy(v.p_val, s.P.val.data(), s.P.val.size())) ||
+            (rc = amg_alloc_copy(v.p_val, to_float(s.P.val).data(), s.P.val.size())) ||
             (rc = amg_alloc_copy(v.pt_ptr, s.Pt.ptr.data(), s.Pt.ptr.size())) ||
             (rc = amg_alloc_copy(v.pt_col, s.Pt.col.data(), s.Pt.col.size())) ||
-            (rc = amg_alloc_copy(v.pt_val, s.Pt.val.data(), s.Pt.val.size())))
+            (rc = amg_alloc_copy(v.pt_val, to_float(s.Pt.val).data(), s.Pt.val.size())))
             return rc;
         if (l > 0) {
             if ((rc = amg_alloc_copy(v.a_ptr, s.A.ptr.data(), s.A.ptr.size())) ||

@@ -130,12 +130,12 @@ struct AmgDevLevel {
     int *a_col = nullptr;
     double *a_val = nullptr;
     double *dinv = nullptr;       // levels >= 1: 6 x 6 diagonal-block inverses
-    long long *p_ptr = nullptr;   // prolongation, bs x 6 blocks
+    long long *p_ptr = nullptr;   // prolongation, bs x 6 blocks (FP32 values)
     int *p_col = nullptr;
-    double *p_val = nullptr;
-    long long *pt_ptr = nullptr;  // restriction, 6 x bs blocks
+    float *p_val = nullptr;
+    long long *pt_ptr = nullptr;  // restriction, 6 x bs blocks (FP32 values)
     int *pt_col = nullptr;
-    double *pt_val = nullptr;
+    float *pt_val = nullptr;
     double *b = nullptr, *x = nullptr, *y = nullptr;  // levels >= 1: right-hand side, two iterates
 };
 

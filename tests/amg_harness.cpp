@@ -4,7 +4,8 @@
 // (a level-0 vector, 4 doubles per particle), it also applies the device's
 // V-cycle to it: the launch sequence of launch_amg_vcycle (k_amg.cu), each
 // kernel's rows computed one after another by the same per-row functions
-// (amg_rows.h), with the stiffness in FP64 (z.bin) and in FP32 (z32.bin).
+// (amg_rows.h), with the stiffness in FP64 (z.bin) and in FP32 (z32.bin), and
+// the prolongation and restriction in FP32 as the device keeps them.
 //   amg_harness DIR AGG_SPACING [SWEEPS]
 #include <algorithm>
 #include <chrono>
@@ -62,16 +63,20 @@ static void k0(const Level0 &z0, const V *val, int mode, double omega, const dou
     }
 }
 
-template <int R, int C, int MODE>
-static void bsr(int nbr, const lpm::Bsr &M, const double *x, int SX, double *out, int SY, const double *b = nullptr,
-                const double *dinv = nullptr, double omega = 0.0)
+// values: the operator's FP64 ones, or the FP32 copies the device keeps of
+// the prolongation and restriction
+template <int R, int C, int MODE, typename VT>
+static void bsr(int nbr, const lpm::Bsr &M, const VT *val, const double *x, int SX, double *out, int SY,
+                const double *b = nullptr, const double *dinv = nullptr, double omega = 0.0)
 {
     for (int row = 0; row < nbr; row++) {
         double y[R] = {};
-        lpm::bsr_row_partial<R, C>(M.ptr.data(), M.col.data(), M.val.data(), x, SX, row, 0, 1, y);
+        lpm::bsr_row_partial<R, C, VT>(M.ptr.data(), M.col.data(), val, x, SX, row, 0, 1, y);
         lpm::bsr_epilogue<R, MODE>(row, y, x, SX, out, SY, b, dinv, omega);
     }
 }
+
+static std::vector<float> f32(const lpm::Bsr &M) { return std::vector<float>(M.val.begin(), M.val.end()); }
 
 static void dense(const lpm::AmgHierarchy &H, const double *b, double *out, int B, int S)
 {
@@ -98,6 +103,11 @@ static void vcycle(const lpm::AmgHierarchy &H, const Level0 &z0, const V *val, c
         y[l].assign(m, 0.0);
     }
     std::vector<double> cb(H.coarse_n), cx(H.coarse_n);
+    std::vector<std::vector<float>> P32(L), Pt32(L);
+    for (int l = 0; l < L; l++) {
+        P32[l] = f32(H.levels[l].P);
+        Pt32[l] = f32(H.levels[l].Pt);
+    }
     for (int l = 0; l < L; l++) {
         const lpm::AmgLevel &v = H.levels[l];
         double *bnext = (l + 1 < L) ? b[l + 1].data() : cb.data();
@@ -110,17 +120,18 @@ static void vcycle(const lpm::AmgHierarchy &H, const Level0 &z0, const V *val, c
                 std::swap(it, ot);
             }
             k0<V>(z0, val, lpm::SM_RESID, v.omega, it, r, ot);
-            bsr<6, 3, lpm::BM_SET>(v.P.nbc, v.Pt, ot, 4, bnext, 6);
+            bsr<6, 3, lpm::BM_SET>(v.P.nbc, v.Pt, Pt32[l].data(), ot, 4, bnext, 6);
         } else {
             double *it = x[l].data(), *ot = y[l].data();
             for (int i = 0; i < v.nblock; i++)
                 lpm::jacobi6_row(i, v.Dinv.data(), v.omega, b[l].data(), it);
             for (int s = 1; s < nu; s++) {
-                bsr<6, 6, lpm::BM_SMOOTH>(v.nblock, v.A, it, 6, ot, 6, b[l].data(), v.Dinv.data(), v.omega);
+                bsr<6, 6, lpm::BM_SMOOTH>(v.nblock, v.A, v.A.val.data(), it, 6, ot, 6, b[l].data(), v.Dinv.data(),
+                                          v.omega);
                 std::swap(it, ot);
             }
-            bsr<6, 6, lpm::BM_RESID>(v.nblock, v.A, it, 6, ot, 6, b[l].data());
-            bsr<6, 6, lpm::BM_SET>(v.P.nbc, v.Pt, ot, 6, bnext, 6);
+            bsr<6, 6, lpm::BM_RESID>(v.nblock, v.A, v.A.val.data(), it, 6, ot, 6, b[l].data());
+            bsr<6, 6, lpm::BM_SET>(v.P.nbc, v.Pt, Pt32[l].data(), ot, 6, bnext, 6);
         }
     }
     dense(H, cb.data(), cx.data(), 6, 6);
@@ -129,16 +140,17 @@ static void vcycle(const lpm::AmgHierarchy &H, const Level0 &z0, const V *val, c
         const double *e = (l + 1 < L) ? y[l + 1].data() : cx.data();
         if (l == 0) {
             double *it = (nu % 2 == 1) ? tmp : z, *ot = (nu % 2 == 1) ? z : tmp;
-            bsr<3, 6, lpm::BM_ADD>(v.nblock, v.P, e, 6, it, 4);
+            bsr<3, 6, lpm::BM_ADD>(v.nblock, v.P, P32[l].data(), e, 6, it, 4);
             for (int s = 0; s < nu; s++) {
                 k0<V>(z0, val, lpm::SM_SMOOTH, v.omega, it, r, ot);
                 std::swap(it, ot);
             }
         } else {
             double *it = (nu % 2 == 1) ? x[l].data() : y[l].data(), *ot = (nu % 2 == 1) ? y[l].data() : x[l].data();
-            bsr<6, 6, lpm::BM_ADD>(v.nblock, v.P, e, 6, it, 6);
+            bsr<6, 6, lpm::BM_ADD>(v.nblock, v.P, P32[l].data(), e, 6, it, 6);
             for (int s = 0; s < nu; s++) {
-                bsr<6, 6, lpm::BM_SMOOTH>(v.nblock, v.A, it, 6, ot, 6, b[l].data(), v.Dinv.data(), v.omega);
+                bsr<6, 6, lpm::BM_SMOOTH>(v.nblock, v.A, v.A.val.data(), it, 6, ot, 6, b[l].data(), v.Dinv.data(),
+                                          v.omega);
                 std::swap(it, ot);
             }
         }

@@ -182,14 +182,22 @@ def test_hierarchy_preconditions_cg(oracle_mod, harness, tmp_path, lattice, size
     assert np.allclose(cinv @ (chol @ chol.T), np.eye(len(cinv)), atol=1e-8)
     M = _vcycle(levels, cinv, nu)
     # the device's launch sequence and per-row arithmetic (emulated on the
-    # host) give the numpy V-cycle's result
+    # host) give the numpy V-cycle's result; an index error would show as an
+    # O(1) difference
     z = M(b)
     z64 = np.fromfile(os.path.join(d, "z.bin")).reshape(n, 4)
     z32 = np.fromfile(os.path.join(d, "z32.bin")).reshape(n, 4)
     assert np.all(z64[:, 3] == 0.0) and np.all(z64[:, :3].ravel()[~free] == 0.0)
-    assert np.abs(z64[:, :3].ravel() - z).max() <= 1e-10 * np.abs(z).max()
+    # (the device keeps P and P^T in FP32: agreement to FP32 rounding)
+    assert np.abs(z64[:, :3].ravel() - z).max() <= 1e-5 * np.abs(z).max()
     assert np.abs(z32[:, :3].ravel() - z).max() <= 1e-4 * np.abs(z).max()
     x, it = _pcg(A0, M, b)
+    # with P and P^T rounded to FP32 as the device keeps them, the cycle stays
+    # symmetric and converges as fast
+    lv32 = [dict(lv, P=lv["P"].astype(np.float32).astype(np.float64),
+                 Pt=lv["Pt"].astype(np.float32).astype(np.float64)) for lv in levels]
+    _, it32 = _pcg(A0, _vcycle(lv32, cinv, nu), b)
+    assert it32 <= it + 1, (it, it32)
     Kf = K[free][:, free]
     assert np.linalg.norm(Kf @ x[free] - b[free]) <= 1e-10 * np.linalg.norm(b)
     # block-Jacobi PCG on the same system for reference
