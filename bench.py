@@ -548,7 +548,8 @@ def run_adjoint(args):
     plate = cases.NotchedPlate(nx=args.plate_n, ny=10, nz=args.plate_n, notch=max(1, args.plate_n // 5),
                                steps=args.adj_steps, strain=args.adj_strain, corr=10.0)
     solver = dict(precision=G.PREC_FP64, newton_tol=args.adj_newton_tol, newton_maxiter=2000, cg_rtol=1e-12,
-                  cg_maxiter=200000, newton_accel=8, cg_forcing=args.adj_forcing)
+                  cg_maxiter=200000, newton_accel=8, cg_forcing=args.adj_forcing,
+                  preconditioner=G.PRECOND_AMG if args.precond == "amg" else G.PRECOND_BJ)
     bcs = plate.step_bcs()
 
     def specimen():
@@ -714,7 +715,7 @@ def main():
                     help="adjoint workload: inexact-Newton forcing cap (opts.cg_forcing; 0 = exact solves)")
     ap.add_argument("--adj-fd", action="store_true")
     ap.add_argument("--precond", default="bj", choices=["bj", "amg"],
-                    help="sc and fcc workloads: PCG preconditioner (block-Jacobi or the multigrid V-cycle)")
+                    help="sc, fcc and adjoint workloads: PCG preconditioner (block-Jacobi or the multigrid V-cycle)")
     ap.add_argument("--no-amg", action="store_true",
                     help="sc workload: skip the side measurement with the multigrid preconditioner")
     ap.add_argument("--compare-du", default=None, help=argparse.SUPPRESS)
