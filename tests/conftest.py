@@ -14,6 +14,15 @@ GOLDEN = os.path.join(ROOT, "tests", "golden")
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built CUDA library")
+    config.addinivalue_line("markers", "gpu_last: GPU cases that have not run on a GPU yet; collected after "
+                                       "the others, so that a failure among them cannot stop a fail-fast "
+                                       "run before the established tests")
+
+
+def pytest_collection_modifyitems(config, items):
+    late = [i for i in items if i.get_closest_marker("gpu_last")]
+    if late:
+        items[:] = [i for i in items if not i.get_closest_marker("gpu_last")] + late
 
 
 @pytest.fixture(scope="session")

@@ -4,17 +4,13 @@ fewer PCG iterations.  Parity is against the oracle, as for the block-Jacobi
 path (tests/test_gpu_parity.py): both solve every system to the same relative
 tolerance, so the displacements agree to the Newton tolerance's level.  The
 hierarchy itself is checked on the CPU (tests/test_amg_setup.py)."""
-import os
-
 import numpy as np
 import pytest
 
 import cases
 from setup_helpers import sc_gpu, sc_oracle
 
-pytestmark = [pytest.mark.gpu,
-              pytest.mark.skipif(os.environ.get("LPM_UNVERIFIED_GPU_TESTS") != "1",
-                                 reason="not yet run on a GPU (set LPM_UNVERIFIED_GPU_TESTS=1)")]
+pytestmark = [pytest.mark.gpu, pytest.mark.gpu_last]
 
 
 @pytest.mark.parametrize("precision", [0, 1])

@@ -69,8 +69,7 @@ def test_fcc_cp_steps_match_oracle(oracle_mod, gpu_lib, precision):
     assert np.abs(s.get("cp_gy") - gy_o).max() <= 1e-8 * np.abs(gy_o).max()
 
 
-@pytest.mark.skipif(__import__("os").environ.get("LPM_UNVERIFIED_GPU_TESTS") != "1",
-                    reason="not yet run on a GPU (set LPM_UNVERIFIED_GPU_TESTS=1)")
+@pytest.mark.gpu_last
 def test_fcc_cp_latent_saturating_match_oracle(oracle_mod, gpu_lib):
     """Latent hardening (q = 1.2) and a finite saturation stress, steps 1-9
     (the case the oracle matches bit for bit against the reference,
@@ -95,6 +94,7 @@ def test_fcc_cp_latent_saturating_match_oracle(oracle_mod, gpu_lib):
     assert np.abs(s.get("cp_gy") - gy_o).max() <= 1e-8 * np.abs(gy_o).max()
 
 
+@pytest.mark.gpu_last
 @pytest.mark.parametrize("steps", [0, 3])
 def test_fcc_stiffness_vs_fd(oracle_mod, gpu_lib, steps):
     """Analytic tangent vs the reference's forward-difference K on the FCC

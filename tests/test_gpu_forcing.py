@@ -3,16 +3,12 @@ stops at the Eisenstat-Walker forcing tolerance instead of cg_rtol, the step
 still converges to the same Newton tolerance.  Measured with the oracle's
 matrices and numpy PCG on a 20 x 2 x 24 plate (6 plastic steps): 6.4x fewer
 PCG iterations at eta_max = 0.1, displacements within 1e-8 of exact solves."""
-import os
-
 import numpy as np
 import pytest
 
 import cases
 
-pytestmark = [pytest.mark.gpu,
-              pytest.mark.skipif(os.environ.get("LPM_UNVERIFIED_GPU_TESTS") != "1",
-                                 reason="not yet run on a GPU (set LPM_UNVERIFIED_GPU_TESTS=1)")]
+pytestmark = [pytest.mark.gpu, pytest.mark.gpu_last]
 
 
 def _plate_run(G, forcing):

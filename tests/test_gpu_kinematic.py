@@ -3,17 +3,13 @@ matches the reference bit for bit on the same case
 (tests/test_oracle_golden.py::test_kinematic_hardening_bit_exact): 24 steps
 of SC 6^3 with reverse yielding, FP64 and mixed precision, both sides
 converged to 1e-10."""
-import os
-
 import numpy as np
 import pytest
 
 import cases
 from setup_helpers import sc_gpu, sc_oracle
 
-pytestmark = [pytest.mark.gpu,
-              pytest.mark.skipif(os.environ.get("LPM_UNVERIFIED_GPU_TESTS") != "1",
-                                 reason="not yet run on a GPU (set LPM_UNVERIFIED_GPU_TESTS=1)")]
+pytestmark = [pytest.mark.gpu, pytest.mark.gpu_last]
 
 
 @pytest.mark.parametrize("precision", [0, 1])

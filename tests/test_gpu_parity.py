@@ -148,6 +148,7 @@ def test_load_steps_match_oracle(oracle_mod, gpu_lib, precision):
     assert np.abs(s.get("J2_alpha") - o.d("alpha1", (n,))).max() < 1e-10
 
 
+@pytest.mark.gpu_last
 @pytest.mark.parametrize("precision", [0, 1])
 def test_force_bc_steps_match_oracle(oracle_mod, gpu_lib, precision):
     """Force-controlled loading (setForceBC, src/boundary.c:50-70): the top
@@ -174,6 +175,7 @@ def test_force_bc_steps_match_oracle(oracle_mod, gpu_lib, precision):
     assert np.abs(s.get("J2_alpha") - a_o).max() <= 1e-8 * a_o.max()
 
 
+@pytest.mark.gpu_last
 @pytest.mark.parametrize("name", sorted(cases.SETUP_SHAPES))
 def test_setup_shapes_bit_exact(gpu_lib, name):
     """GPU library setup (host cell-list search, device upload) against the
@@ -200,6 +202,7 @@ def test_setup_shapes_bit_exact(gpu_lib, name):
     assert np.array_equal(kp[:, 1], g["K_pointer"][:, 1])
 
 
+@pytest.mark.gpu_last
 @pytest.mark.parametrize("precision", [0, 1])
 def test_per_particle_moduli_match_oracle(oracle_mod, gpu_lib, precision):
     """The C2 material model (E +-5 % per particle) at 8^3: bond Kn/Tv
