@@ -13,8 +13,9 @@
 //     nu sweeps x += omega D^-1 (b - A x)
 // The same number of Jacobi sweeps before and after makes the cycle a
 // symmetric positive definite operator, as CG needs.  On level 0 the
-// operator is the stiffness (FP64 Kd, or FP32 Kf under mixed precision, with
-// the products in FP32 as in the mixed SpMV), b is the CG residual r, x the
+// operator is the stiffness in FP32 (Kf: the assembled one under mixed
+// precision, a copy of the FP64 Kd otherwise; the PCG product keeps Kd),
+// with FP32 products as in the mixed SpMV; b is the CG residual r, x the
 // scratch vector q (free between the update and the next product) and y the
 // preconditioned residual z; the DOF mask zeroes the constrained DOFs of
 // every level-0 output.
@@ -360,26 +361,30 @@ static int grid_for(const Ctx &c, long long rows_x_threads)
 
 static AmgVec amg_vec(Ctx &c) { return AmgVec{c.n, c.mask, c.partials, c.counter, c.sc}; }
 
-static void k0_launch(Ctx &c, bool k32, int mode, double omega, const dvec4 *xv, const dvec4 *bv, dvec4 *outv)
+static void k0_launch(Ctx &c, int mode, double omega, const dvec4 *xv, const dvec4 *bv, dvec4 *outv)
 {
     const int g = grid_for(c, (long long)c.n * L0_LANES);
     const double *x = (const double *)xv, *b = (const double *)bv;
     double *out = (double *)outv;
-    if (k32) {
-        if (mode == SM_SMOOTH)
-            k_amg_k0<float, SM_SMOOTH><<<g, ATPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.mask, c.Kf,
-                                                                 c.Pinv_d, omega, x, b, out, c.sc);
-        else
-            k_amg_k0<float, SM_RESID><<<g, ATPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.mask, c.Kf,
-                                                                c.Pinv_d, omega, x, b, out, c.sc);
-    } else {
-        if (mode == SM_SMOOTH)
-            k_amg_k0<double, SM_SMOOTH><<<g, ATPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.mask, c.Kd,
-                                                                  c.Pinv_d, omega, x, b, out, c.sc);
-        else
-            k_amg_k0<double, SM_RESID><<<g, ATPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.mask, c.Kd,
-                                                                 c.Pinv_d, omega, x, b, out, c.sc);
-    }
+    if (mode == SM_SMOOTH)
+        k_amg_k0<float, SM_SMOOTH><<<g, ATPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.mask, c.Kf, c.Pinv_d,
+                                                             omega, x, b, out, c.sc);
+    else
+        k_amg_k0<float, SM_RESID><<<g, ATPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.mask, c.Kf, c.Pinv_d,
+                                                            omega, x, b, out, c.sc);
+}
+
+__global__ void k_to_float(long long count, const double *__restrict__ in, float *__restrict__ out)
+{
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < count;
+         k += (long long)gridDim.x * blockDim.x)
+        out[k] = (float)in[k];
+}
+
+void launch_amg_stiffness32(Ctx &c)
+{
+    const long long count = 9 * c.nblk;
+    k_to_float<<<grid_for(c, count), ATPB, 0, c.stream>>>(count, c.Kd, c.Kf);
 }
 
 template <int R, int C, int MODE, typename VT>
@@ -395,7 +400,7 @@ static void bsr_launch(Ctx &c, int nbr, const long long *ptr, const int *col, co
 // the scratch buffer (x, or tmp on level 0) and changes buffer with every
 // sweep but the first (2 nu - 1 times), so it ends in y (z on level 0); the
 // residual goes to the buffer the iterate is not in.
-void launch_amg_vcycle(Ctx &c, const dvec4 *r, dvec4 *z, dvec4 *tmp, bool k32)
+void launch_amg_vcycle(Ctx &c, const dvec4 *r, dvec4 *z, dvec4 *tmp)
 {
     AmgDev &H = *c.amg;
     const int L = (int)H.lv.size();
@@ -415,10 +420,10 @@ void launch_amg_vcycle(Ctx &c, const dvec4 *r, dvec4 *z, dvec4 *tmp, bool k32)
             k_amg_jacobi0<<<grid_for(c, c.n), ATPB, 0, c.stream>>>(c.n, c.mask, c.Pinv_d, v.omega,
                                                                    (const double *)r, (double *)it, c.sc);
             for (int s = 1; s < nu; s++) {
-                k0_launch(c, k32, SM_SMOOTH, v.omega, it, r, ot);
+                k0_launch(c, SM_SMOOTH, v.omega, it, r, ot);
                 std::swap(it, ot);
             }
-            k0_launch(c, k32, SM_RESID, v.omega, it, r, ot);
+            k0_launch(c, SM_RESID, v.omega, it, r, ot);
             bsr_launch<6, 3, BM_SET>(c, v.nnext, v.pt_ptr, v.pt_col, v.pt_val, (const double *)ot, 4, bnext, 6);
         } else {
             double *it = v.x, *ot = v.y;
@@ -441,7 +446,7 @@ void launch_amg_vcycle(Ctx &c, const dvec4 *r, dvec4 *z, dvec4 *tmp, bool k32)
             dvec4 *it = (nu % 2 == 1) ? tmp : z, *ot = (nu % 2 == 1) ? z : tmp;
             bsr_launch<3, 6, BM_ADD>(c, v.nb, v.p_ptr, v.p_col, v.p_val, e, 6, (double *)it, 4);
             for (int s = 0; s < nu; s++) {
-                k0_launch(c, k32, SM_SMOOTH, v.omega, it, r, ot);
+                k0_launch(c, SM_SMOOTH, v.omega, it, r, ot);
                 std::swap(it, ot);
             }
         } else {
@@ -457,10 +462,9 @@ void launch_amg_vcycle(Ctx &c, const dvec4 *r, dvec4 *z, dvec4 *tmp, bool k32)
 
 void launch_amg_init(Ctx &c, const dvec4 *b, double scale, double delta2)
 {
-    const bool k32 = c.opts.precision == LPM_PREC_MIXED;
     k_amg_init<<<red_grid(c), ATPB, 0, c.stream>>>(amg_vec(c), b, scale, c.x_d, c.r_d, solve_rtol(c),
                                                    c.opts.cg_maxiter, delta2);
-    launch_amg_vcycle(c, c.r_d, c.z_d, c.q_d, k32);
+    launch_amg_vcycle(c, c.r_d, c.z_d, c.q_d);
     k_amg_rz<RZ_INIT><<<red_grid(c), ATPB, 0, c.stream>>>(amg_vec(c), c.r_d, c.z_d, c.p_d);
 }
 
@@ -472,16 +476,15 @@ void launch_amg_iter(Ctx &c, bool k32)
         launch_spmv_d(c, c.p_d, c.q_d, true, true);
     const int g = red_grid(c);
     k_amg_update<<<g, ATPB, 0, c.stream>>>(amg_vec(c), c.x_d, c.r_d, c.p_d, c.q_d);
-    launch_amg_vcycle(c, c.r_d, c.z_d, c.q_d, k32);
+    launch_amg_vcycle(c, c.r_d, c.z_d, c.q_d);
     k_amg_rz<RZ_ITER><<<g, ATPB, 0, c.stream>>>(amg_vec(c), c.r_d, c.z_d, c.p_d);
     launch_cg_p_d(c);
 }
 
 void launch_amg_reliable(Ctx &c, const dvec4 *rtrue)
 {
-    const bool k32 = c.opts.precision == LPM_PREC_MIXED;
     k_amg_reliable<<<red_grid(c), ATPB, 0, c.stream>>>(amg_vec(c), rtrue, c.r_d);
-    launch_amg_vcycle(c, c.r_d, c.z_d, c.q_d, k32);
+    launch_amg_vcycle(c, c.r_d, c.z_d, c.q_d);
     k_amg_rz<RZ_RELIABLE><<<red_grid(c), ATPB, 0, c.stream>>>(amg_vec(c), c.r_d, c.z_d, c.p_d);
 }
 

@@ -400,6 +400,7 @@ static int setup_common(Ctx &c, bool built = false)
     dfree(c.Kf);
     dfree(c.Kd);
     c.kf_cap = c.kd_cap = 0;
+    c.kf_version = -1;
     c.vec64_fallback = false;
     HostSetup &h = c.hs;
     if (!built) {
@@ -829,6 +830,18 @@ static int run_pcg(Ctx &c, int mode, int &iters, int &status)
 static int solve_amg(Ctx &c, const dvec4 *b, double bn, lpm_step_stats *st)
 {
     int rc;
+    if (c.kf_version != c.k_version) {
+        // FP64 stiffness assembled before the multigrid was switched on: the
+        // smoother's FP32 copy
+        if (!c.Kf || c.kf_cap != c.nblk) {
+            drop_graphs(c);  // captured with the old Kf
+            if ((rc = dalloc(c.Kf, 9 * (size_t)c.nblk)))
+                return rc;
+            c.kf_cap = c.nblk;
+        }
+        launch_amg_stiffness32(c);
+        c.kf_version = c.k_version;
+    }
     const int builds0 = c.amg ? c.amg->builds : 0;
     if ((rc = amg_prepare(c)))
         return rc;
@@ -1011,8 +1024,10 @@ int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
 int assemble(Ctx &c)
 {
     const bool fp32 = c.opts.precision == LPM_PREC_MIXED;
+    // the multigrid smoother reads an FP32 copy of the FP64 stiffness
+    const bool smooth32 = !fp32 && c.opts.preconditioner == LPM_PRECOND_AMG && c.nspec == 0;
     int rc;
-    if (fp32 && (!c.Kf || c.kf_cap != c.nblk)) {
+    if ((fp32 || smooth32) && (!c.Kf || c.kf_cap != c.nblk)) {
         if ((rc = dalloc(c.Kf, 9 * (size_t)c.nblk)))
             return rc;
         c.kf_cap = c.nblk;
@@ -1024,6 +1039,13 @@ int assemble(Ctx &c)
     }
     launch_tangent_geometry(c);
     launch_assemble(c, fp32);
+    c.k_version++;
+    if (fp32)
+        c.kf_version = c.k_version;
+    if (smooth32) {
+        launch_amg_stiffness32(c);
+        c.kf_version = c.k_version;
+    }
     c.have_K = true;
     return LPM_OK;
 }

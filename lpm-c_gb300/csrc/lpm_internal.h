@@ -257,6 +257,8 @@ struct Ctx {
     double *Kd = nullptr;     // FP64 values (9*nblk)
     float *Kf = nullptr;      // FP32 values (9*nblk)
     long long kd_cap = 0, kf_cap = 0;  // blocks Kd / Kf were allocated for
+    long long k_version = 0;   // stiffness assemblies so far
+    long long kf_version = -1; // the assembly Kf holds (FP32 assembly, or the copy of Kd for the smoother)
     double *Pinv_d = nullptr; // block-Jacobi inverse, [9][n]
     float *Pinv_f = nullptr;
     // ---- solver vectors
@@ -361,11 +363,13 @@ void launch_tangent_geometry(Ctx &c);
 void launch_assemble(Ctx &c, bool fp32);
 void launch_block_jacobi(Ctx &c, bool fp32);
 // multigrid preconditioner (k_amg.cu): PCG with z = V-cycle(r), FP64
-// vectors; k32 selects the FP32 stiffness (mixed precision)
+// vectors; k32 selects the FP32 stiffness for the PCG product (mixed
+// precision); the V-cycle smooths with the FP32 stiffness in both precisions
 void launch_amg_init(Ctx &c, const dvec4 *b, double scale, double delta2);  // x = 0, r, z, p, rz
 void launch_amg_iter(Ctx &c, bool k32);
 void launch_amg_reliable(Ctx &c, const dvec4 *rtrue);  // r = rtrue (masked), z, rz; p kept
-void launch_amg_vcycle(Ctx &c, const dvec4 *r, dvec4 *z, dvec4 *tmp, bool k32);
+void launch_amg_vcycle(Ctx &c, const dvec4 *r, dvec4 *z, dvec4 *tmp);  // smoother on the FP32 stiffness Kf
+void launch_amg_stiffness32(Ctx &c);  // Kf = (float) Kd, for the smoother under FP64 precision
 int amg_prepare(Ctx &c);  // (re)build the hierarchy when missing, stale or the mask changed
 void free_amg(Ctx &c);
 // solver (k_solve.cu)
