@@ -729,6 +729,10 @@ static void scatter_block(lpm_oracle *o, int i, int jj, double Kl[3][3])
  * rows i0..i1-1, serially and in order (side effects included). */
 void lo_fd_stiffness_range(lpm_oracle *o, int i0, int i1)
 {
+    if (i0 < 0)
+        i0 = 0;
+    if (i1 > o->n)
+        i1 = o->n;
     int w = o->nafem + 1;
     double h = EPSP * o->radius;
     double *Kloc = DALLOC(3 * w * 3);

@@ -48,3 +48,14 @@ def test_side_run_failure_is_reported(monkeypatch):
         raise subprocess.TimeoutExpired(cmd, 900)
     monkeypatch.setattr(subprocess, "run", timeout)
     assert "timed out" in bench.run_amg_side(_args(), np.ones((8, 3)), 0.2)["error"]
+
+
+def test_reference_arm_small_lattice():
+    """The reference arm (the oracle's C port timed on the host) prints its
+    JSON line for a lattice smaller than its FD-stiffness sample."""
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                          "--warmup", "3", "--size", "8"], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads([l for l in out.stdout.splitlines() if l.startswith("{")][-1])
+    assert line["impl"] == "reference" and line["value"] > 0.0
+    assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
