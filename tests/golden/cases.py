@@ -202,6 +202,11 @@ class SCCase:
         return np.tile(iso_cubic(self.E, self.nu), (NTYPE, 1))
 
 
+def sigmay_field(n, seed=3):
+    """Per-particle yield stress 200 + 200 U[0, 1) MPa (splitmix64, seed 3)."""
+    return 200.0 + 200.0 * splitmix64_uniform(seed, n)
+
+
 def splitmix64_uniform(seed, count):
     """Counter-based uniform doubles in [0,1): splitmix64(seed*2^32 + k) >> 11 * 2^-53."""
     out = np.empty(count, dtype=np.float64)

@@ -361,11 +361,46 @@ def kinematic_case(out, tag="sc6_kinematic"):
           f"|beta| max {np.abs(arrs['s_beta']).max():.3e}", flush=True)
 
 
+def sigmay_case(out, tag="sc8_sigmay"):
+    """Per-particle yield stress (the reference's sigmay[i],
+    src/constitutive.c:591): sigma_y = 200 + 200 U[0, 1) MPa per particle
+    (splitmix64 seed 3), the batch workload's range; 20 cyclic steps of SC 8^3
+    with progressive yielding."""
+    case = cases.SCCase(n=8)
+    n = R.setup(case.lattice, case.radius, case.box)
+    nn = R.gint("nneighbors")
+    xyz0 = R.get_d2("xyz", n, 3)
+    types = cases.sc_types(xyz0, R.get_i1("nb", n), case.radius)
+    R.set_types(types, cases.NTYPE)
+    sy = cases.sigmay_field(n)
+    R.material(case.ce_per_type(), 0, sy, 0.0, case.H)
+    R.init_state()
+    R.set_cg_tol(1e-20, 0.0)
+    top = types == cases.T_TOP
+    rec = {k: [] for k in ("iters", "nres", "disp_top")}
+    for s_, stp in enumerate(case.schedule[:20], start=1):
+        with R.quiet():
+            st = R.load_step(cases.sc_bcs(stp), [], case.newton_tol)
+        xyz = R.get_d2("xyz", n, 3)
+        rec["iters"].append(st[0])
+        rec["nres"].append(st[3])
+        rec["disp_top"].append((xyz[top, 2].sum() - xyz0[top, 2].sum()) / top.sum())
+    arrs = {k: np.array(v) for k, v in rec.items()}
+    arrs["types"] = types
+    arrs["sigmay"] = sy
+    arrs["s_xyz"] = R.get_d2("xyz", n, 3)
+    arrs["s_alpha"] = R.get_d2("J2_alpha", n, 3)[:, 1]
+    arrs["s_F"] = R.get_d2("F", n, nn)
+    np.savez_compressed(os.path.join(out, f"{tag}.npz"), **arrs)
+    print(f"{tag}: {n} particles, yielded {(arrs['s_alpha'] > 0).sum()}, alpha max {arrs['s_alpha'].max():.3e}",
+          flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--fcc-steps", type=int, default=12)
-    ap.add_argument("--only", choices=["sc", "fcc", "force", "ductile", "brittle", "enoise", "kinematic", "fcc_sat"] +
+    ap.add_argument("--only", choices=["sc", "fcc", "force", "ductile", "brittle", "enoise", "kinematic", "fcc_sat", "sigmay"] +
                     ["setup_" + k for k in cases.SETUP_SHAPES], default=None)
     ap.add_argument("--out", default=HERE)
     args = ap.parse_args()
@@ -380,6 +415,8 @@ def main():
         noise_case(args.out)
     elif args.only == "kinematic":
         kinematic_case(args.out)
+    elif args.only == "sigmay":
+        sigmay_case(args.out)
     elif args.only == "fcc_sat":
         fcc_case(args.out, args.fcc_steps, tag="fcc4_sat", case=cases.FCCCase(ncell=4, **cases.FCC_SAT))
     elif args.only in ("ductile", "brittle"):
@@ -390,7 +427,7 @@ def main():
         sc_case(args.out, args.steps)
     else:
         import subprocess
-        for which in ["sc", "fcc", "force", "ductile", "brittle", "enoise", "kinematic", "fcc_sat"] + \
+        for which in ["sc", "fcc", "force", "ductile", "brittle", "enoise", "kinematic", "fcc_sat", "sigmay"] + \
                 ["setup_" + k for k in cases.SETUP_SHAPES]:
             subprocess.check_call([sys.executable, __file__, "--only", which, "--steps", str(args.steps),
                                    "--fcc-steps", str(args.fcc_steps), "--out", args.out])

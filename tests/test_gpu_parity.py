@@ -228,3 +228,40 @@ def test_per_particle_moduli_match_oracle(oracle_mod, gpu_lib, precision):
     a_o = o.d("alpha1", (n,))
     assert a_o.max() > 0.0
     assert np.abs(s.get("J2_alpha") - a_o).max() <= 1e-8 * a_o.max()
+
+
+@pytest.mark.gpu_last
+@pytest.mark.parametrize("precision", [0, 1])
+def test_per_particle_yield_stress_match_oracle(oracle_mod, gpu_lib, precision):
+    """Per-particle yield stress U[200, 400] MPa (the case the oracle matches
+    bit for bit against the reference, tests/golden/sc8_sigmay.npz): 20 cyclic
+    steps of SC 8^3, displacements within 1e-8 of the oracle's and the same
+    plastic strain, both sides converged to 1e-10."""
+    G = gpu_lib
+    case = cases.SCCase(n=8, newton_tol=1e-10)
+    oracle_mod.set_threads(4)
+    o = oracle_mod.Oracle()
+    n = o.setup_lattice(case.lattice, case.radius, case.box)
+    types = cases.sc_types(o.d("xyz", (n, 3)), o.i("nb", (n,)), case.radius)
+    sy = cases.sigmay_field(n)
+    c11, c12, c44 = cases.iso_cubic(case.E, case.nu)
+    o.set_types(types)
+    o.set_material(np.full(n, c11), np.full(n, c12), np.full(n, c44), sy, case.H, 0.0, 0)
+    o.init_state()
+    s = G.Specimen(0)
+    assert s.setup_lattice(case.lattice, case.radius, case.box) == n
+    s.set_types(types)
+    s.set_material(c11, c12, c44, sy, case.H, 0.0, G.PL_J2)
+    s.init_state()
+    s.set_solver(precision=precision, newton_tol=1e-10, newton_maxiter=300, cg_rtol=1e-10)
+    x0 = o.d("xyz_initial", (n, 3))
+    for k, stp in enumerate(case.schedule[:20]):
+        st = s.load_step(cases.sc_bcs(stp))
+        o.load_step(cases.sc_bcs(stp), [], 1e-10, 300, 1e-20, 0.0)
+        assert st["status"] == 0, (k + 1, st)
+        du_g = s.get("xyz") - x0
+        du_o = o.d("xyz", (n, 3)) - x0
+        assert np.abs(du_g - du_o).max() < 1e-8 * np.abs(du_o).max(), k + 1
+    a_o = o.d("alpha1", (n,))
+    assert a_o.max() > 0.0
+    assert np.abs(s.get("J2_alpha") - a_o).max() <= 1e-8 * a_o.max()

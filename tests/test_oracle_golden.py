@@ -338,3 +338,34 @@ def test_kinematic_hardening_bit_exact(oracle_mod):
     assert np.array_equal(o.d("beta1", (n, 6)), g["s_beta"])
     assert np.array_equal(o.d("F", (n, nn)), g["s_F"])
     assert np.abs(g["s_beta"]).max() > 0.0
+
+
+def test_per_particle_yield_stress_bit_exact(oracle_mod):
+    """Per-particle yield stress (sigmay[i], src/constitutive.c:591; U[200,
+    400] MPa as the batch workload draws it), 20 cyclic steps of SC 8^3 with
+    progressive yielding: the oracle equals the reference
+    (tests/golden/sc8_sigmay.npz)."""
+    case = cases.SCCase(n=8)
+    g = golden("sc8_sigmay.npz")
+    oracle_mod.set_threads(1)
+    o = oracle_mod.Oracle()
+    n = o.setup_lattice(case.lattice, case.radius, case.box)
+    nn = o.nn
+    types = cases.sc_types(o.d("xyz", (n, 3)), o.i("nb", (n,)), case.radius)
+    assert np.array_equal(types, g["types"])
+    o.set_types(types)
+    sy = cases.sigmay_field(n)
+    assert np.array_equal(sy, g["sigmay"])
+    c11, c12, c44 = cases.iso_cubic(case.E, case.nu)
+    o.set_material(np.full(n, c11), np.full(n, c12), np.full(n, c44), sy, case.H, 0.0, 0)
+    o.init_state()
+    x0 = o.d("xyz_initial", (n, 3))
+    top = types == cases.T_TOP
+    for k, stp in enumerate(case.schedule[:20]):
+        st = o.load_step(cases.sc_bcs(stp), [], case.newton_tol, 100, 1e-20, 0.0)
+        assert st[0] == g["iters"][k] and st[3] == g["nres"][k], k
+        xyz = o.d("xyz", (n, 3))
+        assert (xyz[top, 2].sum() - x0[top, 2].sum()) / top.sum() == g["disp_top"][k], k
+    assert np.array_equal(o.d("xyz", (n, 3)), g["s_xyz"])
+    assert np.array_equal(o.d("alpha1", (n,)), g["s_alpha"])
+    assert np.array_equal(o.d("F", (n, nn)), g["s_F"])
