@@ -129,8 +129,10 @@ def build_specimen(G, case, precision, stream=None, precond=0):
     sc = 1.0 + case.e_noise * (2.0 * u - 1.0)
     s.set_material(c11 * sc, c12 * sc, c44 * sc, case.sigmay, case.H, 0.0, G.PL_J2)
     s.init_state()
+    # the multigrid PCG needs about 25 iterations per solve: a low cap bounds
+    # the time a misbehaving solve can take
     s.set_solver(precision=precision, newton_tol=case.newton_tol, newton_maxiter=100, cg_rtol=1e-10,
-                 cg_maxiter=200000, preconditioner=precond)
+                 cg_maxiter=2000 if precond else 200000, preconditioner=precond)
     return s, types
 
 
@@ -265,9 +267,9 @@ def run_amg_side(args, du_bj, bj_value):
         if args.no_autotune:
             cmd.append("--no-autotune")
         try:
-            out = subprocess.run(cmd, capture_output=True, text=True, timeout=900)
+            out = subprocess.run(cmd, capture_output=True, text=True, timeout=300)
         except subprocess.TimeoutExpired:
-            return {"error": "timed out after 900 s"}
+            return {"error": "timed out after 300 s"}
         lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
         if out.returncode != 0 or not lines:
             tail = (out.stderr or out.stdout).strip().splitlines()[-1:] or [""]

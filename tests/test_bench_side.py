@@ -45,7 +45,7 @@ def test_side_run_failure_is_reported(monkeypatch):
     assert out == {"error": "exit 1: LPMError: x"}
 
     def timeout(cmd, **kw):
-        raise subprocess.TimeoutExpired(cmd, 900)
+        raise subprocess.TimeoutExpired(cmd, 300)
     monkeypatch.setattr(subprocess, "run", timeout)
     assert "timed out" in bench.run_amg_side(_args(), np.ones((8, 3)), 0.2)["error"]
 
