@@ -11,7 +11,6 @@ import subprocess
 
 import numpy as np
 import pytest
-import scipy.linalg as sla
 import scipy.sparse as sp
 
 import cases

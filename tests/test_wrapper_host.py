@@ -3,7 +3,6 @@ a stand-in library that accepts it (returns 0), so the argument marshalling,
 option handling and result conversion of the methods the tests, the bench
 and smoke() use run on the CPU.  The option defaults come from the real
 library (lpm_default_solver_opts needs no device)."""
-import ctypes as C
 
 import numpy as np
 import pytest
