@@ -259,6 +259,10 @@ class FCCCase:
 FCC_SAT = dict(tau0=50.0, taus=150.0, h0=500.0, p=20.0, q=1.2)
 
 
+# J2 plasticity on the FCC lattice (plmode 0 on lattice 3)
+FCC_J2 = dict(sigmay=100.0, H=1000.0)
+
+
 class BatchCase:
     """Batch of independent SC specimens of uneven size (C4 at nspec=256,
     edges 20..60): each edge drawn independently from U{lo..hi}, per-specimen

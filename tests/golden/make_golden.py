@@ -396,11 +396,45 @@ def sigmay_case(out, tag="sc8_sigmay"):
           flush=True)
 
 
+def fcc_j2_case(out, tag="fcc4_j2"):
+    """J2 plasticity on the FCC lattice (plmode 0 on lattice 3: 12 first- and
+    6 second-shell bonds, the FCC branch of calcKnTv): 4^3 cells with the Al
+    constants, sigma_y = 100 MPa, H = 1000 MPa, [001] tension, 12 steps
+    (yield near step 7)."""
+    case = cases.FCCCase(ncell=4)
+    n = R.setup(case.lattice, case.radius, case.box)
+    nn = R.gint("nneighbors")
+    xyz0 = R.get_d2("xyz", n, 3)
+    types = cases.sc_types(xyz0, R.get_i1("nb", n), case.radius)
+    R.set_types(types, cases.NTYPE)
+    R.material(case.ce_per_type(), 0, np.full(n, cases.FCC_J2["sigmay"]), 0.0, cases.FCC_J2["H"])
+    R.init_state()
+    R.set_cg_tol(1e-20, 0.0)
+    top = types == cases.T_TOP
+    rec = {k: [] for k in ("iters", "nres", "disp_top")}
+    for s_, stp in enumerate(case.schedule[:12], start=1):
+        with R.quiet():
+            st = R.load_step(cases.sc_bcs(stp), [], case.newton_tol)
+        xyz = R.get_d2("xyz", n, 3)
+        rec["iters"].append(st[0])
+        rec["nres"].append(st[3])
+        rec["disp_top"].append((xyz[top, 2].sum() - xyz0[top, 2].sum()) / top.sum())
+    arrs = {k: np.array(v) for k, v in rec.items()}
+    arrs["types"] = types
+    arrs["s_xyz"] = R.get_d2("xyz", n, 3)
+    arrs["s_alpha"] = R.get_d2("J2_alpha", n, 3)[:, 1]
+    arrs["s_dLp"] = R.get_d3("dLp", n, nn, 1)
+    arrs["s_F"] = R.get_d2("F", n, nn)
+    np.savez_compressed(os.path.join(out, f"{tag}.npz"), **arrs)
+    print(f"{tag}: {n} particles, iters {arrs['iters'].astype(int).tolist()}, alpha max {arrs['s_alpha'].max():.3e}",
+          flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--fcc-steps", type=int, default=12)
-    ap.add_argument("--only", choices=["sc", "fcc", "force", "ductile", "brittle", "enoise", "kinematic", "fcc_sat", "sigmay"] +
+    ap.add_argument("--only", choices=["sc", "fcc", "force", "ductile", "brittle", "enoise", "kinematic", "fcc_sat", "sigmay", "fcc_j2"] +
                     ["setup_" + k for k in cases.SETUP_SHAPES], default=None)
     ap.add_argument("--out", default=HERE)
     args = ap.parse_args()
@@ -417,6 +451,8 @@ def main():
         kinematic_case(args.out)
     elif args.only == "sigmay":
         sigmay_case(args.out)
+    elif args.only == "fcc_j2":
+        fcc_j2_case(args.out)
     elif args.only == "fcc_sat":
         fcc_case(args.out, args.fcc_steps, tag="fcc4_sat", case=cases.FCCCase(ncell=4, **cases.FCC_SAT))
     elif args.only in ("ductile", "brittle"):
@@ -427,7 +463,8 @@ def main():
         sc_case(args.out, args.steps)
     else:
         import subprocess
-        for which in ["sc", "fcc", "force", "ductile", "brittle", "enoise", "kinematic", "fcc_sat", "sigmay"] + \
+        for which in ["sc", "fcc", "force", "ductile", "brittle", "enoise", "kinematic", "fcc_sat", "sigmay",
+                      "fcc_j2"] + \
                 ["setup_" + k for k in cases.SETUP_SHAPES]:
             subprocess.check_call([sys.executable, __file__, "--only", which, "--steps", str(args.steps),
                                    "--fcc-steps", str(args.fcc_steps), "--out", args.out])

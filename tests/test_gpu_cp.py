@@ -117,3 +117,38 @@ def test_fcc_stiffness_vs_fd(oracle_mod, gpu_lib, steps):
     rel = np.linalg.norm(K - Kf) / np.linalg.norm(Kf)
     # forward differences with h = 1e-6 r: truncation ~1e-6 relative
     assert rel < 1e-5, rel
+
+
+@pytest.mark.gpu_last
+@pytest.mark.parametrize("precision", [0, 1])
+def test_fcc_j2_match_oracle(oracle_mod, gpu_lib, precision):
+    """J2 plasticity on the FCC lattice (the case the oracle matches bit for
+    bit against the reference, tests/golden/fcc4_j2.npz): 12 steps of [001]
+    tension, displacements and plastic strain against the oracle."""
+    G = gpu_lib
+    case = cases.FCCCase(ncell=4, newton_tol=1e-10)
+    sy, H = cases.FCC_J2["sigmay"], cases.FCC_J2["H"]
+    oracle_mod.set_threads(4)
+    o = oracle_mod.Oracle()
+    n = o.setup_lattice(case.lattice, case.radius, case.box)
+    types = cases.sc_types(o.d("xyz", (n, 3)), o.i("nb", (n,)), case.radius)
+    o.set_types(types)
+    o.set_material(case.C11, case.C12, case.C44, sy, H, 0.0, 0)
+    o.init_state()
+    s = G.Specimen(0)
+    assert s.setup_lattice(case.lattice, case.radius, case.box) == n
+    s.set_types(types)
+    s.set_material(case.C11, case.C12, case.C44, sy, H, 0.0, G.PL_J2)
+    s.init_state()
+    s.set_solver(precision=precision, newton_tol=1e-10, newton_maxiter=300, cg_rtol=1e-11)
+    x0 = o.d("xyz_initial", (n, 3))
+    for k, stp in enumerate(case.schedule[:12]):
+        st = s.load_step(cases.sc_bcs(stp))
+        o.load_step(cases.sc_bcs(stp), [], 1e-10, 300, 1e-22, 0.0)
+        assert st["status"] == 0, (k + 1, st)
+        du_g = s.get("xyz") - x0
+        du_o = o.d("xyz", (n, 3)) - x0
+        assert np.abs(du_g - du_o).max() < 1e-8 * np.abs(du_o).max(), k + 1
+    a_o = o.d("alpha1", (n,))
+    assert a_o.max() > 0.0
+    assert np.abs(s.get("J2_alpha") - a_o).max() <= 1e-8 * a_o.max()

@@ -369,3 +369,32 @@ def test_per_particle_yield_stress_bit_exact(oracle_mod):
     assert np.array_equal(o.d("xyz", (n, 3)), g["s_xyz"])
     assert np.array_equal(o.d("alpha1", (n,)), g["s_alpha"])
     assert np.array_equal(o.d("F", (n, nn)), g["s_F"])
+
+
+def test_fcc_j2_bit_exact(oracle_mod):
+    """J2 plasticity on the FCC lattice (plmode 0 on lattice 3), 4^3 cells,
+    [001] tension, 12 steps with yield from step 8: the oracle equals the
+    reference (tests/golden/fcc4_j2.npz)."""
+    case = cases.FCCCase(ncell=4)
+    g = golden("fcc4_j2.npz")
+    oracle_mod.set_threads(1)
+    o = oracle_mod.Oracle()
+    n = o.setup_lattice(case.lattice, case.radius, case.box)
+    nn = o.nn
+    types = cases.sc_types(o.d("xyz", (n, 3)), o.i("nb", (n,)), case.radius)
+    assert np.array_equal(types, g["types"])
+    o.set_types(types)
+    o.set_material(case.C11, case.C12, case.C44, cases.FCC_J2["sigmay"], cases.FCC_J2["H"], 0.0, 0)
+    o.init_state()
+    x0 = o.d("xyz_initial", (n, 3))
+    top = types == cases.T_TOP
+    for k, stp in enumerate(case.schedule[:12]):
+        st = o.load_step(cases.sc_bcs(stp), [], case.newton_tol, 100, 1e-20, 0.0)
+        assert st[0] == g["iters"][k] and st[3] == g["nres"][k], k
+        xyz = o.d("xyz", (n, 3))
+        assert (xyz[top, 2].sum() - x0[top, 2].sum()) / top.sum() == g["disp_top"][k], k
+    assert np.array_equal(o.d("xyz", (n, 3)), g["s_xyz"])
+    assert np.array_equal(o.d("alpha1", (n,)), g["s_alpha"])
+    assert np.array_equal(o.d("dLp1", (n, nn)), g["s_dLp"])
+    assert np.array_equal(o.d("F", (n, nn)), g["s_F"])
+    assert g["s_alpha"].max() > 0.0
