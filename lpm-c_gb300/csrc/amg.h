@@ -70,6 +70,8 @@ struct AmgInput {
     const int *nconn = nullptr;
     const int *cols = nullptr;
     const double *val = nullptr;
+    const int *group = nullptr;       // specimen of each particle in a batch (null: one specimen);
+                                      // aggregates never span two specimens
 };
 
 struct AmgOptions {

@@ -354,11 +354,13 @@ struct CoarseOut {
     Bsr Ac;
     std::vector<double> Bc;  // coarse near-nullspace, 6 x 6 per aggregate (row-major)
     std::vector<int> gidx;   // integer box coordinates of the aggregates
+    std::vector<int> grp;    // specimen of each aggregate
     std::vector<double> cen; // aggregate centroids
 };
 
 template <class Op>
-bool coarsen(const Op &A, const uint8_t *mask, const std::vector<int> &gidx, const std::vector<double> &pos,
+bool coarsen(const Op &A, const uint8_t *mask, const std::vector<int> &gidx, const std::vector<int> &grp,
+             const std::vector<double> &pos,
              const std::vector<double> &Bl, const AmgOptions &opt, AmgLevel &L, CoarseOut &out)
 {
     constexpr int BS = Op::BS;
@@ -368,9 +370,12 @@ bool coarsen(const Op &A, const uint8_t *mask, const std::vector<int> &gidx, con
     for (int I = 0; I < nb; I++)
         for (int d = 0; d < 3; d++)
             gmax[d] = std::max(gmax[d], gidx[3 * (size_t)I + d]);
+    // boxes never join block rows of different specimens (grp), so every
+    // level stays block-diagonal over the specimens of a batch
     std::vector<long long> key(nb);
     for (int I = 0; I < nb; I++)
-        key[I] = ((long long)gidx[3 * (size_t)I + 2] * (gmax[1] + 1) + gidx[3 * (size_t)I + 1]) * (gmax[0] + 1) +
+        key[I] = (((long long)grp[I] * (gmax[2] + 1) + gidx[3 * (size_t)I + 2]) * (gmax[1] + 1) +
+                  gidx[3 * (size_t)I + 1]) * (gmax[0] + 1) +
                  gidx[3 * (size_t)I];
     std::vector<long long> uk(key);
     std::sort(uk.begin(), uk.end());
@@ -610,6 +615,9 @@ bool coarsen(const Op &A, const uint8_t *mask, const std::vector<int> &gidx, con
         }
     }
     // next level's grid
+    out.grp.assign(nagg, 0);
+    for (int I = 0; I < nb; I++)
+        out.grp[agg[I]] = grp[I];
     out.gidx.assign(3 * (size_t)nagg, 0);
     for (int I = 0; I < nb; I++)
         for (int d = 0; d < 3; d++)
@@ -633,29 +641,34 @@ int amg_build(const AmgInput &in, AmgHierarchy &H, const AmgOptions &opt)
         for (int d = 0; d < 3; d++)
             gidx[3 * (size_t)i + d] = (int)std::floor((in.xyz[3 * (size_t)i + d] - lo[d]) / h + 1e-9);
     std::vector<double> pos(in.xyz, in.xyz + 3 * (size_t)n);
+    std::vector<int> grp(n, 0);
+    if (in.group)
+        grp.assign(in.group, in.group + n);
     Bsr A = level0(in);  // the operator of the level being coarsened
     std::vector<double> Bnull;
     if (n > opt.coarse_blocks && opt.max_levels > 0) {
         AmgLevel L;
         CoarseOut co;
-        if (coarsen(OpB<3>{A}, in.mask, gidx, pos, Bnull, opt, L, co)) {
+        if (coarsen(OpB<3>{A}, in.mask, gidx, grp, pos, Bnull, opt, L, co)) {
             H.levels.push_back(std::move(L));
             A = std::move(co.Ac);
             Bnull = std::move(co.Bc);
             gidx = std::move(co.gidx);
+            grp = std::move(co.grp);
             pos = std::move(co.cen);
         }
     }
     while (!H.levels.empty() && (int)H.levels.size() < opt.max_levels && A.nbr > opt.coarse_blocks) {
         AmgLevel L;
         CoarseOut co;
-        if (!coarsen(OpB<6>{A}, nullptr, gidx, pos, Bnull, opt, L, co))
+        if (!coarsen(OpB<6>{A}, nullptr, gidx, grp, pos, Bnull, opt, L, co))
             break;
         L.A = std::move(A);
         H.levels.push_back(std::move(L));
         A = std::move(co.Ac);
         Bnull = std::move(co.Bc);
         gidx = std::move(co.gidx);
+        grp = std::move(co.grp);
         pos = std::move(co.cen);
     }
     // coarsest level: dense Cholesky (lower factor, row-major) and inverse

@@ -185,6 +185,12 @@ int main(int argc, char **argv)
     in.nconn = nconn.data();
     in.cols = cols.data();
     in.val = val.data();
+    std::vector<int> group;
+    if (FILE *fg = std::fopen((d + "/group.bin").c_str(), "rb")) {
+        std::fclose(fg);
+        group = rd<int>(d + "/group.bin", n);
+        in.group = group.data();
+    }
     lpm::AmgOptions opt;
     opt.agg_spacing = std::atof(argv[2]);
     lpm::AmgHierarchy H;

@@ -249,3 +249,44 @@ def test_hierarchy_independent_of_thread_count(oracle_mod, harness, tmp_path):
         outs.append({p.name: p.read_bytes() for p in sorted(d.iterdir()) if p.name.startswith(("L", "coarse"))})
     assert outs[0].keys() == outs[1].keys() and len(outs[0]) > 5
     assert all(outs[0][k] == outs[1][k] for k in outs[0])
+
+
+def test_batch_groups_keep_specimens_apart(oracle_mod, harness, tmp_path):
+    """Two specimens at the same place in space, as a batch puts them: with a
+    specimen id per particle, no aggregate spans both, every level stays
+    block-diagonal over the specimens (as per-specimen CG scalars need), and
+    the V-cycle PCG converges as for one specimen."""
+    o, K, res, xyz, mask, conn, nconn = _system(oracle_mod, 2, 12)
+    n = len(nconn)
+    rowoff, npad, cols, val = _device_layout(K, conn, nconn)
+    rowoff2 = np.concatenate([rowoff, rowoff[1:] + rowoff[-1]])
+    d = tmp_path
+    open(d / "n.txt", "w").write(str(2 * n))
+    group = np.repeat(np.arange(2, dtype=np.int32), n)
+    for name, arr in (("xyz", np.vstack([xyz, xyz])), ("mask", np.concatenate([mask, mask])),
+                      ("rowoff", rowoff2), ("npad", np.concatenate([npad, npad])),
+                      ("nconn", np.concatenate([nconn, nconn]).astype(np.int32)),
+                      ("cols", np.concatenate([cols, cols + n]).astype(np.int32)),
+                      ("val", np.concatenate([val, val])), ("group", group)):
+        np.ascontiguousarray(arr).tofile(d / f"{name}.bin")
+    subprocess.check_call([harness, str(d), "0.6"])
+    levels, coarse, chol, cinv = _load_hierarchy(str(d))
+    assert len(levels) >= 1
+    g = np.repeat(group, 3)  # specimen of each level-0 DOF
+    for lv in levels:
+        P = lv["P"].tocoo()
+        owner = np.full(P.shape[1], -1)
+        for r, c in zip(P.row, P.col):
+            assert owner[c] in (-1, g[r]), "an aggregate spans two specimens"
+            owner[c] = g[r]
+        g = np.where(owner < 0, 0, owner)  # specimen of each coarse DOF (empty columns: either)
+    # block-diagonal coarsest operator: no entry couples the two specimens
+    C = coarse.tocoo()
+    assert np.all(g[C.row] == g[C.col])
+    free = (np.repeat(np.concatenate([mask, mask])[:, None], 3, axis=1) >> np.arange(3) & 1).ravel().astype(bool)
+    K2 = sp.block_diag([K, K]).tocsr()
+    dfree = sp.diags(free.astype(float))
+    levels[0]["A"] = (dfree @ K2 @ dfree).tocsr()
+    b = np.concatenate([res, 0.5 * res]) * free
+    _, it = _pcg(levels[0]["A"], _vcycle(levels, cinv, 1), b)
+    assert it <= 30, it
