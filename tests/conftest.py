@@ -14,15 +14,28 @@ GOLDEN = os.path.join(ROOT, "tests", "golden")
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built CUDA library")
-    config.addinivalue_line("markers", "gpu_last: GPU cases that have not run on a GPU yet; collected after "
-                                       "the others, so that a failure among them cannot stop a fail-fast "
-                                       "run before the established tests")
+    config.addinivalue_line("markers", "gpu_last: reference-pinned GPU parity cases collected after the "
+                                       "established ones")
+    config.addinivalue_line("markers", "gpu_option: GPU tests of opt-in solver options (multigrid, inexact "
+                                       "and accelerated Newton); collected after every parity test, so "
+                                       "that a failure there cannot stop a fail-fast run before them")
+
+
+def _tier(item):
+    """Collection tier: established tests, then the later reference-pinned
+    parity cases, then the opt-in solver options, then the allocation-free
+    entry point's file (test_zz_*), which always comes last."""
+    if item.fspath.basename.startswith("test_zz_"):
+        return 3
+    if item.get_closest_marker("gpu_option"):
+        return 2
+    if item.get_closest_marker("gpu_last"):
+        return 1
+    return 0
 
 
 def pytest_collection_modifyitems(config, items):
-    late = [i for i in items if i.get_closest_marker("gpu_last")]
-    if late:
-        items[:] = [i for i in items if not i.get_closest_marker("gpu_last")] + late
+    items.sort(key=_tier)  # stable: file order within a tier
 
 
 @pytest.fixture(scope="session")

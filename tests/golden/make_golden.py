@@ -74,7 +74,9 @@ def sc_case(out, nsteps, tag="sc10"):
     sched = case.schedule[:nsteps]
     rec = {k: [] for k in ("iters", "nres0", "nreac0", "nres", "cg", "disp_top", "react_top")}
     snaps = {}
-    snap_steps = {1, 13, 14, 20, 40, len(sched)}
+    # every 20 steps (each quarter cycle's end), so that the whole run can be
+    # replayed in independent segments
+    snap_steps = {1, 13, 14, len(sched)} | set(range(20, len(sched) + 1, 20))
     for s, stp in enumerate(sched, start=1):
         if s == 1 or s == 14:
             # stiffness at the converged state entering this step (FD, upper CSR)
@@ -432,7 +434,7 @@ def fcc_j2_case(out, tag="fcc4_j2"):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--steps", type=int, default=160)
     ap.add_argument("--fcc-steps", type=int, default=12)
     ap.add_argument("--only", choices=["sc", "fcc", "force", "ductile", "brittle", "enoise", "kinematic", "fcc_sat", "sigmay", "fcc_j2"] +
                     ["setup_" + k for k in cases.SETUP_SHAPES], default=None)

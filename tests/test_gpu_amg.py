@@ -10,7 +10,7 @@ import pytest
 import cases
 from setup_helpers import sc_gpu, sc_oracle
 
-pytestmark = [pytest.mark.gpu, pytest.mark.gpu_last]
+pytestmark = [pytest.mark.gpu, pytest.mark.gpu_option]
 
 
 @pytest.mark.parametrize("precision", [0, 1])

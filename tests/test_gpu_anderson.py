@@ -7,7 +7,7 @@ import pytest
 import cases
 from setup_helpers import sc_gpu
 
-pytestmark = pytest.mark.gpu
+pytestmark = [pytest.mark.gpu, pytest.mark.gpu_option]
 
 
 def test_anderson_matches_modified_newton_sc(gpu_lib):

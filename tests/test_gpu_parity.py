@@ -13,6 +13,10 @@ from setup_helpers import sc_gpu, sc_oracle
 
 pytestmark = pytest.mark.gpu
 
+# steps of the per-particle-moduli case (SC 8^3, sigma_y 150 MPa, E +-5 %)
+# on which the reference's modified Newton converges
+ENOISE_CONVERGED_STEPS = 9
+
 
 @pytest.fixture(scope="module")
 def sc10(oracle_mod, gpu_lib):
@@ -206,9 +210,12 @@ def test_setup_shapes_bit_exact(gpu_lib, name):
 @pytest.mark.parametrize("precision", [0, 1])
 def test_per_particle_moduli_match_oracle(oracle_mod, gpu_lib, precision):
     """The C2 material model (E +-5 % per particle) at 8^3: bond Kn/Tv
-    bit-exact with the reference (tests/golden/sc8_enoise.npz), then 14 cyclic
+    bit-exact with the reference (tests/golden/sc8_enoise.npz), then 9 cyclic
     steps into the plastic range within 1e-8 of the oracle, both sides
-    converged to 1e-10."""
+    converged to 1e-10.  Later steps have no converged answer to compare: at
+    the reference's own settings its modified Newton stops at MAXITER on step
+    10 with the residual rising (3e-5, the fixture's nres), and continued past
+    that it reaches NaN at iteration 141 (the oracle, like the reference)."""
     from conftest import golden
     case = cases.SCCase(n=8, sigmay=150.0, e_noise=0.05, seed=1, newton_tol=1e-10)
     g = golden("sc8_enoise.npz")
@@ -217,7 +224,7 @@ def test_per_particle_moduli_match_oracle(oracle_mod, gpu_lib, precision):
     n = o.n
     assert np.array_equal(s.get("Kn"), g["Kn"]) and np.array_equal(s.get("Tv"), g["Tv"])
     x0 = o.d("xyz_initial", (n, 3))
-    for k, stp in enumerate(case.schedule[:14]):
+    for k, stp in enumerate(case.schedule[:ENOISE_CONVERGED_STEPS]):
         st = s.load_step(cases.sc_bcs(stp))
         o.load_step(cases.sc_bcs(stp), [], 1e-10, 300, 1e-20, 0.0)
         assert st["status"] == 0, (k + 1, st)

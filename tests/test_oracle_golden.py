@@ -3,6 +3,8 @@ reference itself (tests/golden/make_golden.py, reference built from its own
 sources).  Everything here is bit-exact: same inputs, same operation order,
 same BLAS/CG shim.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -398,3 +400,50 @@ def test_fcc_j2_bit_exact(oracle_mod):
     assert np.array_equal(o.d("dLp1", (n, nn)), g["s_dLp"])
     assert np.array_equal(o.d("F", (n, nn)), g["s_F"])
     assert g["s_alpha"].max() > 0.0
+
+
+def _cyclic_segment(first):
+    """Steps first+1 .. first+20 of the C1 cyclic case in the oracle, started
+    from the reference's converged state after step `first` (fresh for 0);
+    returns the mismatches against the reference's fixture."""
+    import oracle as O
+    case = cases.SCCase(n=10)
+    o, types = sc_oracle(O, case, threads=1)
+    g = golden("sc10_cyclic.npz")
+    if first:
+        restore(o, g, first)
+    n = o.n
+    x0 = o.d("xyz_initial", (n, 3))
+    top = types == cases.T_TOP
+    bad = []
+    for k in range(first, first + 20):
+        st = o.load_step(cases.sc_bcs(case.schedule[k]), [], case.newton_tol, 100, 1e-20, 0.0)
+        xyz = o.d("xyz", (n, 3))
+        F, csz = o.d("F", (n, 18)), o.d("csz", (n, 18))
+        if not (st[0] == g["iters"][k] and st[3] == g["nres"][k] and
+                (xyz[top, 2].sum() - x0[top, 2].sum()) / top.sum() == g["disp_top"][k] and
+                np.sum(-csz[top] * F[top]) == g["react_top"][k]):
+            bad.append(("step", k + 1))
+    last = first + 20
+    for key in ("xyz", "alpha", "dLp", "stress"):
+        name = {"alpha": "alpha1", "dLp": "dLp1", "stress": "stress_tensor"}.get(key, key)
+        shape = g[f"s{last}_{key}"].shape
+        if not np.array_equal(g[f"s{last}_{key}"], o.d(name, shape)):
+            bad.append((key, last))
+    return bad
+
+
+def test_full_cyclic_run_bit_exact(oracle_mod):
+    """All 160 load steps of the C1 case (two cycles, eight plastic stretches
+    that stop at the reference's MAXITER) against the reference's own run:
+    per-step Newton iterations, final residual, top displacement and reaction,
+    and the converged state every 20 steps, bit for bit.  The run is replayed
+    as eight segments of 20 steps, each started from the reference's state at
+    its first step (the resume itself is pinned above), in parallel."""
+    import multiprocessing as mp
+    g = golden("sc10_cyclic.npz")
+    starts = list(range(0, 160, 20))
+    assert all(s + 20 in set(int(k) for k in g["snap_steps"]) for s in starts)
+    with mp.get_context("spawn").Pool(min(len(starts), max(1, os.cpu_count() or 1))) as pool:
+        results = pool.map(_cyclic_segment, starts)
+    assert all(not r for r in results), results
