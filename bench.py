@@ -7,18 +7,24 @@ cubic lattice 100 x 100 x 100 (1e6 particles, 8.9e6 bonds, 3e6 DOF),
 spacing 0.2 mm, E = 200 GPa with +-5% uniform noise per particle (seed 1),
 nu = 0.3, J2 yield 250 MPa, linear hardening 2 GPa; bottom face fixed in z
 (plus a 3-DOF rigid-body pin), top face displaced along the +-0.2% strain
-cycle, 20 steps per quarter cycle; Newton tolerance 1e-8, block-Jacobi PCG
-to relative residual 1e-10.  The W warm-up steps are the first W steps of
-the schedule; the K timed steps follow them.
+cycle, 20 steps per quarter cycle; Newton tolerance 1e-8 with the
+reference's MAXITER of 100, linear solves to relative residual 1e-10.  The W
+warm-up steps are the first W steps of the schedule; the K timed steps follow
+them (the default 5 + 20 reach through the plastic steps 12-20).
 
-Headline: the mixed-precision path (FP32 stiffness/SpMV/PCG with FP64
-reliable updates, FP64 residuals and return map).  The same steps run on the
-plain FP64 path for the ratio and the displacement error between the two.
-Inputs are resident in HBM (value); `e2e` runs the same steps through the
-reference-named C drop-in (liblpmhost.so + liblpmgpu_legacy.so) with the
-include/lpm.h globals on the host, host<->device copies inside the timed
-region.  The reference arm times the oracle's C port of the reference
-algorithm on the host cores.
+Headline: the mixed-precision path (FP32 stiffness and PCG products in
+difference form, FP64 PCG vectors, reliable updates, residuals and return
+map) with the multigrid-preconditioned PCG.  The same steps run on the plain
+FP64 path for the ratio and the errors between the two.  Inputs are resident
+in HBM (value); `e2e` runs the same steps through the reference-named C
+drop-in (liblpmhost.so + liblpmgpu_legacy.so) with the include/lpm.h globals
+on the host, host<->device copies inside the timed region.  The reference arm
+times the oracle's C port of the reference algorithm on the host cores.
+
+Time budget: the arms run in the order mixed, FP64, e2e, CPU baseline; an arm
+that would not fit the remaining budget (--budget, from process start) is
+skipped and reported as such, and a watchdog prints the line measured so far
+at --budget + --grace seconds, so the run always ends with its JSON line.
 """
 import argparse
 import json
@@ -38,6 +44,8 @@ for _p in (os.path.join(ROOT, "lpm-c_gb300"), os.path.join(ROOT, "oracle"), os.p
         sys.path.insert(0, _p)
 
 import cases  # noqa: E402
+
+T_START = time.time()
 
 METRIC = "load steps/s, 1M-particle SC lattice: mixed vs FP64 GPU @1e-8 err; SpMV GB/s"
 UNIT = "load steps/s"
@@ -129,11 +137,104 @@ def build_specimen(G, case, precision, stream=None, precond=0):
     sc = 1.0 + case.e_noise * (2.0 * u - 1.0)
     s.set_material(c11 * sc, c12 * sc, c44 * sc, case.sigmay, case.H, 0.0, G.PL_J2)
     s.init_state()
-    # the multigrid PCG needs about 25 iterations per solve: a low cap bounds
-    # the time a misbehaving solve can take
-    s.set_solver(precision=precision, newton_tol=case.newton_tol, newton_maxiter=100, cg_rtol=1e-10,
-                 cg_maxiter=2000 if precond else 200000, preconditioner=precond)
+    s.set_solver(**solver_opts(G, case, precision, precond))
     return s, types
+
+
+def solver_opts(G, case, precision, precond):
+    """Newton tolerance 1e-8 and the reference's MAXITER of 100
+    (include/lpm.h:39), linear solves to 1e-10 relative.  The multigrid PCG
+    needs about 40 iterations per solve: its cap of 2000 bounds the time a
+    misbehaving solve can take."""
+    return dict(precision=precision, newton_tol=case.newton_tol, newton_maxiter=100, cg_rtol=1e-10,
+                cg_maxiter=2000 if precond else 200000, preconditioner=precond)
+
+
+class Deadline:
+    """Wall-clock budget of the whole run, counted from process start."""
+
+    def __init__(self, budget_s):
+        self.t_end = T_START + budget_s
+
+    def left(self):
+        return self.t_end - time.time()
+
+
+def run_arm(G, case, prec, precond, W, K, stream, deadline, sync, autotune=True):
+    """One precision on the SC workload: setup, W warm-up load steps, then K
+    timed load steps bracketed by CUDA events on the launching stream.  Stops
+    between steps once the deadline has passed (the arm then reports
+    incomplete, never fewer steps)."""
+    import torch
+    t0 = time.time()
+    s, types = build_specimen(G, case, prec, stream.cuda_stream, precond)
+    setup_s = time.time() - t0
+    sched = case.schedule
+    tuning = None
+    warm = []
+    for k in range(W):
+        if deadline.left() < 0:
+            s.close()
+            return {"incomplete": f"deadline passed in warm-up step {k + 1}"}
+        warm.append(s.load_step(cases.sc_bcs(sched[k])))
+        if k == 0 and autotune:
+            tuning = s.autotune()  # launch shapes from the project's autotuner
+    sync()
+    s.spmv_timing(reset=2)
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stats = []
+    wall = []
+    sync()
+    ev0.record(stream)
+    for k in range(W, W + K):
+        if deadline.left() < 0:
+            ev1.record(stream)
+            sync()
+            clocks.stop()
+            s.close()
+            return {"incomplete": f"deadline passed before timed step {k + 1} ({k - W} of {K} done)",
+                    "stats": stats}
+        t1 = time.time()
+        stats.append(s.load_step(cases.sc_bcs(sched[k])))
+        wall.append(time.time() - t1)
+    ev1.record(stream)
+    sync()
+    ms = ev0.elapsed_time(ev1)
+    ck = clocks.stop()
+    spmv_ms, spmv_cnt = s.spmv_timing(reset=3)
+    out = dict(ms=ms, stats=stats, warm=warm, spmv_ms=spmv_ms, spmv_cnt=spmv_cnt, clocks=ck, tuning=tuning,
+               spmv_bytes=spmv_alg_bytes(s, prec, precond), xyz=s.get("xyz"), x0=s.get("xyz_initial"),
+               alpha=s.get("J2_alpha"), react=reaction(s, types), n=s.n, nnzb=s.sizes()["nnz_blocks"],
+               setup_s=setup_s, step_wall_s=wall)
+    s.close()
+    return out
+
+
+def reaction(s, types):
+    """Reaction of the top face, writeReaction's sum of -cs_z F over the
+    particles of the type (src/data_handler.c:309-335)."""
+    top = types == cases.T_TOP
+    return float(np.sum(-s.get("csz")[top] * s.get("F")[top]))
+
+
+def spmv_alg_bytes(s, prec, precond):
+    """Algorithmic bytes of one launch of the PCG product the arm runs: the
+    stiffness values and column indices of the structural (unpadded) blocks,
+    the row offsets, the input vector read once and the output written once.
+    FP64: 72 B of values per block, FP64 vectors (24 B per particle each way).
+    Mixed with the multigrid: the difference-form FP32 product, 36 B of values
+    per block, the input as two FP32 parts (24 B per particle), the FP64 output
+    (24 B) and the 3 x 3 block row sums (36 B per particle).  Mixed with
+    block-Jacobi: the FP32 SpMV on FP32 vectors (12 B each way)."""
+    z = s.sizes()
+    nnzb, n = z["nnz_blocks"], s.n
+    if prec == 0:
+        return nnzb * (9 * 8 + 4) + 4 * (n + 1) + 2 * 3 * n * 8
+    if precond:
+        return nnzb * (9 * 4 + 4) + 4 * (n + 1) + 3 * n * 8 + 3 * n * 8 + 9 * n * 4
+    return s.spmv_bytes(prec)
 
 
 def run_ours(args):
@@ -145,143 +246,150 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", init_method="env://")
     case = cases.SCCase(n=args.size, e_noise=0.05, seed=1)
-    sched = case.schedule
     W, K = args.warmup, args.steps
     stream = torch.cuda.current_stream()
+    precond = G.PRECOND_AMG if args.precond == "amg" else G.PRECOND_BJ
+    deadline = Deadline(args.budget)
 
-    def barrier():
+    def sync():
         if world > 1:
             import torch.distributed as dist
             dist.barrier()
         torch.cuda.synchronize()
 
-    results = {}
-    for prec_name, prec in (("mixed", G.PREC_MIXED), ("fp64", G.PREC_FP64)):
-        if prec_name == "fp64" and args.no_fp64:
-            continue
-        precond = G.PRECOND_AMG if args.precond == "amg" else G.PRECOND_BJ
-        s, types = build_specimen(G, case, prec, stream.cuda_stream, precond)
-        tuning = None
-        warm = []
-        for k in range(W):
-            warm.append(s.load_step(cases.sc_bcs(sched[k])))
-            if k == 0 and not args.no_autotune:
-                tuning = s.autotune()  # launch shapes from the project's autotuner
-        barrier()
-        s.spmv_timing(reset=2)
-        clocks = ClockSampler(local)
-        clocks.start()
-        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        stats = []
-        barrier()
-        ev0.record(stream)
-        for k in range(W, W + K):
-            stats.append(s.load_step(cases.sc_bcs(sched[k])))
-        ev1.record(stream)
-        barrier()
-        ms = ev0.elapsed_time(ev1)
-        ck = clocks.stop()
-        spmv_ms, spmv_cnt = s.spmv_timing(reset=3)
-        ms = max_over_ranks(ms, device="cuda")
-        results[prec_name] = dict(ms=ms, stats=stats, warm=warm, spmv_ms=spmv_ms, spmv_cnt=spmv_cnt, clocks=ck,
-                                  tuning=tuning,
-                                  spmv_bytes=s.spmv_bytes(prec), xyz=s.get("xyz"), x0=s.get("xyz_initial"),
-                                  n=s.n, nnzb=s.sizes()["nnz_blocks"])
-        s.close()
-        del s
-    mixed = results["mixed"]
-    value = world * K / (mixed["ms"] / 1e3)
-    hbm, peak_src = peaks()
-    achieved = mixed["spmv_bytes"] / (mixed["spmv_ms"] * 1e-3) / 1e9 if mixed["spmv_ms"] > 0 else None
-    traffic = spmv_traffic(mixed["spmv_bytes"])
-    err = None
-    fp64_rate = None
-    if "fp64" in results:
-        f = results["fp64"]
-        fp64_rate = world * K / (f["ms"] / 1e3)
-        du_m = mixed["xyz"] - mixed["x0"]
-        du_f = f["xyz"] - f["x0"]
-        err = float(np.abs(du_m - du_f).max() / np.abs(du_f).max())
-    if args.compare_du:
-        ref = np.load(args.compare_du)
-        du = mixed["xyz"] - mixed["x0"]
-        err = float(np.abs(du - ref).max() / np.abs(ref).max())
-    e2e = run_e2e(args, case) if (not args.no_e2e and rank == 0) else None
-    counts = step_counts(args.size, W, K, results["fp64"]["stats"] if "fp64" in results else None)
-    cpu = run_cpu_baseline(args, case, counts) if (not args.no_cpu and rank == 0) else None
-    agg = lambda key: int(sum(st[key] for st in mixed["stats"]))  # noqa: E731
-    amg = None
-    if args.precond == "bj" and not args.no_amg and world == 1:
-        amg = run_amg_side(args, mixed["xyz"] - mixed["x0"], value)
-    line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
-        "ms_per_step": mixed["ms"] / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 stiffness/SpMV/PCG + f64 residual, refinement and return map",
-        "data": "synthetic (seeded lattice and material noise)",
-        "config": {"workload": f"SC {args.size}^3 elastoplastic cyclic, load steps {W + 1}-{W + K} of "
-                               f"{len(sched)} (first yield near step 12)",
-                   "particles": mixed["n"], "nnz_blocks": mixed["nnzb"], "precision": "mixed",
-                   "preconditioner": "smoothed-aggregation multigrid V-cycle" if args.precond == "amg"
-                   else "block-Jacobi",
-                   "fp64_steps_per_s": fp64_rate, "mixed_over_fp64": (value / fp64_rate) if fp64_rate else None,
-                   "disp_err_mixed_vs_fp64": err, "newton_iters": agg("newton_iters"), "cg_iters": agg("cg_iters"),
-                   "reliable_updates": agg("refine_iters"),
-                   "fp64_cg_iters": (sum(st["cg_iters"] for st in results["fp64"]["stats"])
-                                     if "fp64" in results else None),
-                   "l2": "SpMV stream of 2.4 GB per call > 129 MB L2 (no flush needed)",
-                   "tuning": mixed["tuning"],
-                   "amg_build_ms": sum(st["ms_amg_build"] for st in mixed["warm"] + mixed["stats"]),
-                   "amg_builds": sum(st["amg_builds"] for st in mixed["warm"] + mixed["stats"]),
-                   "multigrid": amg,
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
-                     "kernel": "k_spmv_f (FP32 block-CSR SpMV)", "peak_source": peak_src,
-                     "spmv_launches_sampled": mixed["spmv_cnt"]},
-        "clocks": mixed["clocks"],
-        "gpu_launches": gpu_launches(mixed["stats"], amg_levels(mixed["n"]) if args.precond == "amg" else 0),
-        "e2e": e2e,
-        "cpu_baseline": cpu,
-    }
-    if rank == 0:
-        print(json.dumps(line))
+    state = {"line": None}
+    lock = threading.Lock()
+
+    def emit(line):
+        with lock:
+            if state["line"] is None and rank == 0:
+                state["line"] = line
+                print(json.dumps(line), flush=True)
+
+    # hard stop: print what has been measured and leave before an outer limit
+    # cuts the run off without a line
+    partial = {}
+
+    def watchdog():
+        emit(assemble_line(args, case, partial, world, note="hard time limit reached; unfinished parts are null"))
+        os._exit(0)
+
+    timer = threading.Timer(max(1.0, args.budget + args.grace - (time.time() - T_START)), watchdog)
+    timer.daemon = True
+    timer.start()
+
+    partial["mixed"] = run_arm(G, case, G.PREC_MIXED, precond, W, K, stream, deadline, sync,
+                               autotune=not args.no_autotune)
+    mixed = partial["mixed"]
+    mixed_s = mixed["ms"] / 1e3 if "ms" in mixed else None
+    # the FP64 arm runs the same steps; its FP64 product is about 4x the
+    # mixed one's per PCG iteration, so budget it at 3x the mixed arm
+    if args.no_fp64:
+        partial["fp64"] = {"skipped": "--no-fp64"}
+    elif mixed_s is None:
+        partial["fp64"] = {"skipped": "the mixed arm did not finish"}
+    elif deadline.left() < 3.0 * (mixed_s + mixed["setup_s"]) + 60.0:
+        partial["fp64"] = {"skipped": f"budget: {deadline.left():.0f} s left, about {3.0 * mixed_s:.0f} s needed"}
+    else:
+        partial["fp64"] = run_arm(G, case, G.PREC_FP64, precond, W, K, stream, deadline, sync,
+                                  autotune=not args.no_autotune)
+    if args.no_e2e or rank != 0:
+        partial["e2e"] = None
+    elif mixed_s is None:
+        partial["e2e"] = {"value": None, "unit": UNIT, "skipped": "the mixed arm did not finish"}
+    elif deadline.left() < 2.5 * mixed_s + 60.0:
+        partial["e2e"] = {"value": None, "unit": UNIT,
+                          "skipped": f"budget: {deadline.left():.0f} s left, about {2.5 * mixed_s:.0f} s needed"}
+    else:
+        partial["e2e"] = run_e2e(args, case, precond, deadline)
+    if args.no_cpu or rank != 0:
+        partial["cpu"] = None
+    else:
+        partial["cpu"] = run_cpu_baseline(case, W, K)
+    line = assemble_line(args, case, partial, world)
+    timer.cancel()
+    emit(line)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
 
 
-def run_amg_side(args, du_bj, bj_value):
-    """The same workload with the multigrid preconditioner, measured in a child
-    process after the block-Jacobi line is complete (a failure there cannot
-    cost the headline): its load steps/s, the ratio to block-Jacobi, PCG
-    iterations, hierarchy build time, and its displacements against
-    block-Jacobi's."""
-    import subprocess
-    import tempfile
-    with tempfile.TemporaryDirectory() as d:
-        ref = os.path.join(d, "du_bj.npy")
-        np.save(ref, du_bj)
-        cmd = [sys.executable, os.path.abspath(__file__), "--precond", "amg", "--no-fp64", "--no-e2e", "--no-cpu",
-               "--no-amg", "--steps", str(args.steps), "--warmup", str(args.warmup), "--size", str(args.size),
-               "--compare-du", ref]
-        if args.no_autotune:
-            cmd.append("--no-autotune")
-        try:
-            out = subprocess.run(cmd, capture_output=True, text=True, timeout=300)
-        except subprocess.TimeoutExpired:
-            return {"error": "timed out after 300 s"}
-        lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
-        if out.returncode != 0 or not lines:
-            tail = (out.stderr or out.stdout).strip().splitlines()[-1:] or [""]
-            return {"error": f"exit {out.returncode}: {tail[0][:300]}"}
-        line = json.loads(lines[-1])
-    c = line["config"]
-    return {"steps_per_s": line["value"], "ms_per_step": line["ms_per_step"],
-            "over_block_jacobi": line["value"] / bj_value if bj_value else None,
-            "cg_iters": c["cg_iters"], "newton_iters": c["newton_iters"], "reliable_updates": c["reliable_updates"],
-            "hierarchy_builds": c["amg_builds"], "hierarchy_build_ms": c["amg_build_ms"],
-            "disp_err_vs_block_jacobi": c["disp_err_mixed_vs_fp64"], "gpu_launches": line["gpu_launches"],
-            "clocks": line.get("clocks")}
+def assemble_line(args, case, partial, world, note=None):
+    """The JSON line from whatever the arms have measured so far."""
+    W, K = args.warmup, args.steps
+    mixed = partial.get("mixed") or {}
+    f64 = partial.get("fp64") or {}
+    done = "ms" in mixed
+    value = world * K / (mixed["ms"] / 1e3) if done else None
+    hbm, peak_src = peaks()
+    achieved = (mixed["spmv_bytes"] / (mixed["spmv_ms"] * 1e-3) / 1e9
+                if done and mixed.get("spmv_ms") else None)
+    fp64_rate = world * K / (f64["ms"] / 1e3) if "ms" in f64 else None
+    errs = {}
+    if done and "ms" in f64:
+        du_m, du_f = mixed["xyz"] - mixed["x0"], f64["xyz"] - f64["x0"]
+        errs["disp_err_mixed_vs_fp64"] = float(np.abs(du_m - du_f).max() / np.abs(du_f).max())
+        errs["plastic_strain_err_mixed_vs_fp64"] = float(np.abs(mixed["alpha"] - f64["alpha"]).max() /
+                                                         max(np.abs(f64["alpha"]).max(), 1e-300))
+        errs["reaction_err_mixed_vs_fp64"] = abs(mixed["react"] - f64["react"]) / abs(f64["react"])
+    agg = (lambda arm, key: int(sum(st[key] for st in arm["stats"]))) if True else None  # noqa: E731
+    sched_len = len(case.schedule)
+    precond_name = ("smoothed-aggregation multigrid V-cycle" if args.precond == "amg" else "block-Jacobi")
+    cfg = {"workload": f"SC {args.size}^3 elastoplastic cyclic (E +-5 % per particle), load steps "
+                       f"{W + 1}-{W + K} of {sched_len}: first yield at step 12, steps 15-20 stop at the "
+                       f"reference's 100 Newton iterations",
+           "particles": mixed.get("n"), "nnz_blocks": mixed.get("nnzb"), "precision": "mixed",
+           "preconditioner": precond_name,
+           "newton": "modified Newton with the elastic tangent of the step (src/lpmc_project.c:382-471), "
+                     "tolerance 1e-8, MAXITER 100; linear solves to 1e-10 relative",
+           "fp64_steps_per_s": fp64_rate, "mixed_over_fp64": (value / fp64_rate) if (value and fp64_rate) else None,
+           **errs,
+           "fp64_arm": {k: v for k, v in f64.items() if k in ("skipped", "incomplete")} or None,
+           "newton_iters": agg(mixed, "newton_iters") if done else None,
+           "newton_iters_per_step": [st["newton_iters"] for st in mixed["stats"]] if done else None,
+           "cg_iters": agg(mixed, "cg_iters") if done else None,
+           "reliable_updates": agg(mixed, "refine_iters") if done else None,
+           "fp64_newton_iters": agg(f64, "newton_iters") if "ms" in f64 else None,
+           "fp64_cg_iters": agg(f64, "cg_iters") if "ms" in f64 else None,
+           "step_wall_s": [round(x, 3) for x in mixed["step_wall_s"]] if done else None,
+           "l2": "stiffness stream of 2.4 GB (FP32) per product > 129 MB L2 (no flush needed)",
+           "tuning": mixed.get("tuning"),
+           "amg_build_ms": (sum(st["ms_amg_build"] for st in mixed["warm"] + mixed["stats"]) if done else None),
+           "amg_builds": (sum(st["amg_builds"] for st in mixed["warm"] + mixed["stats"]) if done else None),
+           "setup_s": mixed.get("setup_s"),
+           "parallelism": "replicas" if world > 1 else "single GPU"}
+    if not done:
+        cfg["mixed_arm"] = {k: v for k, v in mixed.items() if k in ("skipped", "incomplete")}
+    if note:
+        cfg["note"] = note
+    kernel = ("k_spmv_diff (difference-form FP32 block-CSR product of the mixed multigrid PCG)"
+              if args.precond == "amg" else "k_spmv<float, float4> (FP32 block-CSR SpMV)")
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": (mixed["ms"] / K) if done else None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 stiffness and PCG products + f64 PCG vectors, residuals, reliable updates and return map",
+        "data": "synthetic (seeded lattice and per-particle material noise)",
+        "config": cfg,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": (achieved / hbm) if achieved else None,
+                     "traffic": (mixed["spmv_bytes"] * SPMV_TRAFFIC_OVER_ALG) if done else None,
+                     "kernel": kernel, "peak_source": peak_src,
+                     "algorithmic_bytes_per_launch": mixed.get("spmv_bytes"),
+                     "launches_sampled": mixed.get("spmv_cnt")},
+        "clocks": mixed.get("clocks"),
+        "gpu_launches": gpu_launches(mixed["stats"], amg_levels(mixed["n"]) if args.precond == "amg" else 0)
+        if done else None,
+        "e2e": partial.get("e2e"),
+        "cpu_baseline": partial.get("cpu"),
+    }
+    return line
+
+
+# DRAM bytes over algorithmic bytes of the PCG product, from the ncu capture
+# summarised in profiles/ (dram__bytes_read.sum + dram__bytes_write.sum of one
+# launch at SC 60^3, scaled by the block count)
+SPMV_TRAFFIC_OVER_ALG = 1.05288
 
 
 def amg_levels(n, coarse_blocks=150):
@@ -310,85 +418,86 @@ def gpu_launches(stats, amg=0):
     return total
 
 
-def run_e2e(args, case):
-    """Same steps through the reference-named C drop-in with host globals."""
+def run_e2e(args, case, precond, deadline):
+    """The same steps through the reference-named C drop-in with the
+    include/lpm.h globals on the host: the C host loop (liblpmhost.so, the
+    src/lpmc_project.c:382-471 sequence) calls calcStiffness3DFiniteDifference,
+    setDispBC, computeBondForceGeneral, updateRR, solverCG and switchStateV of
+    liblpmgpu_legacy.so, which upload what each reads and write back what each
+    writes.  Per-particle E as the reference expresses it: one type per
+    particle with its own Ce row, boundary conditions by BC group."""
     try:
         import torch
         import lpm_gb300 as G
         import lpm_host
+        os.environ["LPM_LEGACY_NO_KEXPORT"] = "1"
         h = lpm_host.HostDriver()
         n = h.setup(case.lattice, case.radius, case.box)
-        # particle types as for the GPU specimen (the legacy ABI selects BCs by
-        # type and takes Ce per type, so this leg runs with uniform E)
         s = G.Specimen(0)
         s.setup_lattice(case.lattice, case.radius, case.box)
-        types = cases.sc_types(h.get("xyz"), s.get("nb"), case.radius)
+        groups = cases.sc_types(h.get("xyz"), s.get("nb"), case.radius)
         s.close()
-        h.set_types(types, cases.NTYPE)
-        h.set_material(np.tile(cases.iso_cubic(case.E, case.nu), (cases.NTYPE, 1)), 0, case.sigmay, 0.0, case.H)
-        h.set_solver(precision=G.PREC_MIXED, cg_rtol=1e-10, cg_maxiter=200000)
+        h.set_types(np.arange(n, dtype=np.int32), n)
+        h.set_bc_groups(groups, cases.NTYPE)
+        c11, c12, c44 = cases.iso_cubic(case.E, case.nu)
+        u = cases.splitmix64_uniform(case.seed, n)
+        sc = 1.0 + case.e_noise * (2.0 * u - 1.0)
+        h.set_material(np.stack([c11 * sc, c12 * sc, c44 * sc], axis=1), 0, case.sigmay, 0.0, case.H)
+        o = solver_opts(G, case, G.PREC_MIXED, precond)
+        o.pop("newton_tol")
+        o.pop("newton_maxiter")
+        h.set_solver(**o)
         h.init()
         W, K = args.warmup, args.steps
         for k in range(W):
-            h.load_step(cases.sc_bcs(case.schedule[k]), newton_tol=case.newton_tol)
+            h.load_step(cases.sc_bcs(case.schedule[k]), newton_tol=case.newton_tol, maxiter=100)
         h.traffic(reset=True)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for k in range(W, W + K):
-            h.load_step(cases.sc_bcs(case.schedule[k]), newton_tol=case.newton_tol)
+            if deadline.left() < 0:
+                return {"value": None, "unit": UNIT, "incomplete": f"deadline passed at step {k + 1}"}
+            h.load_step(cases.sc_bcs(case.schedule[k]), newton_tol=case.newton_tol, maxiter=100)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
         h2d, d2h = h.traffic()
         return {"value": K / dt, "unit": UNIT, "h2d_bytes_per_step": h2d / K, "d2h_bytes_per_step": d2h / K,
                 "path": "C host loop (liblpmhost) -> reference-named drop-in (liblpmgpu_legacy), "
                         "include/lpm.h globals on the host",
-                "note": "uniform E (per-particle E needs one Ce row per particle in the legacy ABI)"}
+                "material": "E +-5 % per particle: one type and Ce row per particle, BCs by BC group",
+                "k_global_export": "off (LPM_LEGACY_NO_KEXPORT=1): the host copy of K_global is not read "
+                                   "by the load-step loop; solverCG uses the device stiffness",
+                "solver": "mixed precision, " + ("multigrid" if precond else "block-Jacobi") + " PCG"}
     except Exception as e:  # report, never fake
         return {"value": None, "unit": UNIT, "error": str(e)[:300]}
 
 
-COUNTS_FILE = os.path.join(ROOT, "profiles", "iteration_counts_sc100.json")
-TRAFFIC_FILE = os.path.join(ROOT, "profiles", "k_spmv_f_traffic.json")
+# Newton iterations per load step of the SC 100^3 cyclic case (E +-5 %,
+# Newton tolerance 1e-8, MAXITER 100), steps 1-25, measured on a GB300 with
+# FP64 multigrid-preconditioned solves to 1e-10; the count is the
+# reference's modified-Newton iteration, independent of the linear solver at
+# that solve accuracy (profiles/sc100_cyclic_steps.md).
+NEWTON_PER_STEP_SC100 = [3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 8, 80, 88, 100, 100, 100, 100, 100, 100, 3, 3, 3, 3, 3]
+# Block-Jacobi PCG iterations per Newton iteration at SC 100^3 (FP64, to
+# 1e-10 relative), measured on a GB300 over steps 4-8: 28,433 iterations in
+# 15 solves (profiles/sc100_cyclic_steps.md).
+CG_PER_NEWTON_SC100 = 1895.5
 
 
-def spmv_traffic(alg_bytes):
-    """DRAM bytes (read + write) per SpMV launch: the ncu capture of a smaller
-    case (dram__bytes_read.sum + dram__bytes_write.sum) scaled to this launch
-    by its algorithmic bytes, which grow with the block count."""
-    try:
-        with open(TRAFFIC_FILE) as f:
-            d = json.load(f)
-        return alg_bytes * d["traffic_over_algorithmic"]
-    except Exception:
-        return None
-
-
-def step_counts(size, W, K, stats=None):
-    """Newton iterations per step and CG iterations per Newton iteration of the
-    timed steps: from this run when available, else from the committed record
-    of an earlier FP64 GPU run of the same steps, else a model."""
-    if stats:
-        newton = sum(st["newton_iters"] for st in stats) / len(stats)
-        cg = sum(st["cg_iters"] for st in stats) / max(1.0, sum(st["newton_iters"] for st in stats))
-        return newton, cg, "this run's FP64 GPU counts"
-    try:
-        with open(COUNTS_FILE) as f:
-            d = json.load(f)
-        # per-step averages over the recorded steps (the elastic steps 4-8
-        # all take 3 Newton iterations), valid for timed runs starting there
-        if d.get("size") == size and d.get("first_step") == W + 1:
-            return d["newton_per_step"], d["cg_per_newton"], "recorded FP64 GPU counts (" + COUNTS_FILE[len(ROOT) + 1:] + ")"
-    except Exception:
-        pass
-    return 2.0, 1800.0, "model: 2 Newton iterations, 1800 CG iterations each"
-
-
-def run_cpu_baseline(args, case, counts):
-    """Per-load-step cost of the reference algorithm (the oracle's C port, all
-    host threads) at full size, from bounded samples of each phase."""
+def run_cpu_baseline(case, W, K):
+    """Per-load-step cost of the reference algorithm at full size on the host
+    cores (the oracle's C port of the reference path), from bounded samples
+    of each phase, with the reference's own thread counts: the finite
+    difference stiffness and the bond forces on nt_force = 3 threads
+    (src/lpmc_project.c:57, :391, :452), the CG on all threads.  Per step:
+    stiffness + Newton iterations x (force + CG iterations x one CG
+    iteration), with the step's Newton count and the block-Jacobi PCG count
+    per solve of the GPU runs (the reference's unpreconditioned CG needs at
+    least as many)."""
     try:
         import oracle as O
         threads = os.cpu_count() or 1
+        nt_force = min(3, threads)
         O.set_threads(threads)
         o = O.Oracle()
         t0 = time.perf_counter()
@@ -401,26 +510,30 @@ def run_cpu_baseline(args, case, counts):
         c11, c12, c44 = cases.iso_cubic(case.E, case.nu)
         o.set_material(c11 * sc, c12 * sc, c44 * sc, case.sigmay, case.H, 0.0, 0)
         o.init_state()
-        rows = min(n, 2000)
-        r0 = min(n // 2, n - rows)  # a sample of interior rows that fits the lattice
-        t0 = time.perf_counter()
-        o.L.lo_fd_stiffness_range(o.h, r0, r0 + rows)  # serial, as the reference's side effects require
-        t_fd = (time.perf_counter() - t0) * n / rows / threads  # the reference runs it OpenMP-parallel
+        O.set_threads(nt_force)
         t0 = time.perf_counter()
         o.force(0)
         t_force = time.perf_counter() - t0
+        O.set_threads(threads)
         nit = 10
         t0 = time.perf_counter()
         o.L.lo_cg_iterations(o.h, nit)
         t_cg = (time.perf_counter() - t0) / nit
-        newton, cgit, src = counts
-        step_s = t_fd + newton * (t_force + cgit * t_cg)
-        return {"value": 1.0 / step_s, "unit": UNIT, "cores": threads, "kind": "port",
-                "sample": (f"oracle C port of the reference path at {n} particles: FD stiffness of {rows} "
-                           f"rows (scaled to all rows and {threads} threads), one J2 force sweep, {nit} "
-                           f"threaded CG iterations on the full upper CSR; per step = FD + {newton:.1f} "
-                           f"Newton x (force + {cgit:.0f} CG iterations) - counts: {src} (the reference's "
-                           f"unpreconditioned CG needs more, so this flatters the CPU)"),
+        rows = min(n, 6000)
+        t_fd = o.L.lo_fd_stiffness_timing(o.h, rows, nt_force) * n / rows  # last: it disturbs the state
+        newton = NEWTON_PER_STEP_SC100[W:W + K] if case.n == 100 and W + K <= len(NEWTON_PER_STEP_SC100) \
+            else [3] * K
+        step_s = [t_fd + nn * (t_force + CG_PER_NEWTON_SC100 * t_cg) for nn in newton]
+        total = sum(step_s)
+        return {"value": K / total, "unit": UNIT, "cores": threads, "kind": "port",
+                "ms_per_step": 1e3 * total / K,
+                "sample": (f"oracle C port of the reference path at {n} particles: finite-difference stiffness "
+                           f"of {rows} rows spread over the lattice on {nt_force} threads (scaled to all rows), "
+                           f"one J2 force sweep on {nt_force} threads, {nit} CG iterations on the full upper "
+                           f"CSR on {threads} threads; per step = stiffness + Newton iterations x (force + "
+                           f"{CG_PER_NEWTON_SC100:.0f} CG iterations), Newton iterations of steps {W + 1}-{W + K} "
+                           f"= {sum(newton)} (measured on the GPU, the same modified-Newton iteration)"),
+                "threads": {"stiffness": nt_force, "force": nt_force, "cg": threads},
                 "phase_s": {"fd_stiffness": t_fd, "force": t_force, "cg_iter": t_cg, "setup": setup_s}}
     except Exception as e:
         return {"value": None, "unit": UNIT, "kind": "port", "error": str(e)[:300]}
@@ -678,24 +791,32 @@ def run_fcc(args):
 
 
 def run_reference(args):
+    """The reference arm: the reference's CPU algorithm (the oracle's C port,
+    bit-identical to the reference on every pinned case) on the host cores,
+    on this arm's workload, metric and unit.  Under torchrun only rank 0
+    measures; the other ranks exit without work."""
     rank, world, local = dist_env()
     if rank != 0:
         return
     case = cases.SCCase(n=args.size, e_noise=0.05, seed=1)
-    cpu = run_cpu_baseline(args, case, step_counts(args.size, args.warmup, args.steps))
-    line = {"metric": METRIC, "impl": "reference", "value": cpu.get("value"), "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "vs_baseline": None,
-            "config": {"workload": f"SC {args.size}^3 elastoplastic cyclic"},
+    cpu = run_cpu_baseline(case, args.warmup, args.steps)
+    v = cpu.get("value")
+    line = {"metric": METRIC, "impl": "reference", "value": v, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": cpu.get("ms_per_step"),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded lattice and per-particle material noise)",
+            "config": {"workload": f"SC {args.size}^3 elastoplastic cyclic (E +-5 % per particle), load steps "
+                                   f"{args.warmup + 1}-{args.warmup + args.steps}"},
             "cpu_baseline": cpu,
-            "e2e": {"value": cpu.get("value"), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=100)
     ap.add_argument("--no-fp64", action="store_true")
@@ -716,11 +837,13 @@ def main():
     ap.add_argument("--adj-forcing", type=float, default=0.0,
                     help="adjoint workload: inexact-Newton forcing cap (opts.cg_forcing; 0 = exact solves)")
     ap.add_argument("--adj-fd", action="store_true")
-    ap.add_argument("--precond", default="bj", choices=["bj", "amg"],
-                    help="sc, fcc and adjoint workloads: PCG preconditioner (block-Jacobi or the multigrid V-cycle)")
-    ap.add_argument("--no-amg", action="store_true",
-                    help="sc workload: skip the side measurement with the multigrid preconditioner")
-    ap.add_argument("--compare-du", default=None, help=argparse.SUPPRESS)
+    ap.add_argument("--precond", default="amg", choices=["bj", "amg"],
+                    help="sc, fcc and adjoint workloads: PCG preconditioner (the multigrid V-cycle or "
+                         "block-Jacobi)")
+    ap.add_argument("--budget", type=float, default=1450.0,
+                    help="sc workload: wall seconds from start within which the arms must fit")
+    ap.add_argument("--grace", type=float, default=200.0,
+                    help="sc workload: the watchdog prints the line measured so far at budget + grace")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

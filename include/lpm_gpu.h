@@ -379,15 +379,19 @@ int lpm_format_strain(const char *path, int t1, int tstep, int n, const int *typ
  * quantities lpm_compute_force reports).  Pin, Pex, dispBC_index and residual
  * are DEVICE arrays of 3n entries on the current device, in the reference's
  * per-particle (x, y, z) order; norms is a host array or NULL.  With norms the
- * call waits for the stream; without, it only enqueues work on it.
+ * call waits for the stream, so norms must be NULL on a stream that is being
+ * captured (the call then returns LPM_ERR_ARG); without norms it only enqueues
+ * work on the stream.
  *
  * Allocates nothing: its only work space is a fixed 256 KB device array in
  * the library (held on every GPU that loads the library until exit), shared by
  * all calls on a device and keeping the last call's contents.  n beyond
  * LPM_NOALLOC_MAX_PARTICLES is rejected with LPM_ERR_ARG.  The first call on
- * each device looks up that array's device address; make that first call
- * before any stream capture.  Calls whose kernels overlap on the GPU race on
- * the shared array: order them on one stream. */
+ * each device looks up that array's device address and keeps it for the
+ * process; make that first call before any stream capture.  A device reset
+ * (cudaDeviceReset) can move the array, so after one the entry point must not
+ * be called again in that process.  Calls whose kernels overlap on the GPU
+ * race on the shared array: order them on one stream. */
 #define LPM_NOALLOC_MAX_PARTICLES 4194304
 int lpm_update_rr_noalloc(int n, const double *Pin, const double *Pex, const int *dispBC_index,
                           double *residual, double norms[2], void *stream);

@@ -1,8 +1,13 @@
 // Per-row arithmetic of the multigrid V-cycle kernels (k_amg.cu), shared
 // with a host emulation of the same launch sequence (tests/amg_harness.cpp),
 // so that the index arithmetic of every kernel is exercised on the CPU.
-// Vectors are plain double arrays: level-0 vectors hold 4 doubles per
-// particle (x, y, z, unused), coarse-level vectors 6 per aggregate.
+// Level-0 vectors hold 4 values per particle (x, y, z, unused), coarse-level
+// vectors 6 per aggregate.  The device instantiates everything with FP32
+// vectors, values and arithmetic (T = float): the V-cycle is the PCG's
+// preconditioner, FP32 costs it nothing in iterations, and FP64 arithmetic
+// is ALU-bound on GB300 (measured: the FP64 products of the prolongation,
+// restriction and coarse operators kept the FP64 pipe 77-86 % busy at 11-34 %
+// of the DRAM bandwidth).  The host emulation also runs them with T = double.
 #pragma once
 #include <cstddef>
 #include <cstdint>
@@ -49,13 +54,60 @@ AMG_HD void load4(const double *p, double (&v)[4])
 #endif
 }
 
+// x, y, z of a level-0 vector entry (4 values per particle): one 16-byte
+// load for FP32 on the device
+template <typename T>
+AMG_HD void load_xyz(const float *p, T &a, T &b, T &c)
+{
+#ifdef __CUDA_ARCH__
+    const float4 t = __ldg(reinterpret_cast<const float4 *>(p));
+    a = (T)t.x;
+    b = (T)t.y;
+    c = (T)t.z;
+#else
+    a = (T)p[0];
+    b = (T)p[1];
+    c = (T)p[2];
+#endif
+}
+template <typename T>
+AMG_HD void load_xyz(const double *p, T &a, T &b, T &c)
+{
+    a = (T)p[0];
+    b = (T)p[1];
+    c = (T)p[2];
+}
+
+// one level-0 entry (x, y, z, 0): a single 16-byte store for FP32 on the
+// device; an FP64 output gets the rounded FP32 values
+template <typename T>
+AMG_HD void store_xyz(float *p, T a, T b, T c)
+{
+#ifdef __CUDA_ARCH__
+    *reinterpret_cast<float4 *>(p) = make_float4((float)a, (float)b, (float)c, 0.f);
+#else
+    p[0] = (float)a;
+    p[1] = (float)b;
+    p[2] = (float)c;
+    p[3] = 0.f;
+#endif
+}
+template <typename T>
+AMG_HD void store_xyz(double *p, T a, T b, T c)
+{
+    p[0] = (double)a;
+    p[1] = (double)b;
+    p[2] = (double)c;
+    p[3] = 0.0;
+}
+
 // Level 0: partial product of block row `row` of the stiffness (device
 // layout: npad[row] blocks at rowoff[row], npad a multiple of 4,
 // component-major values) over the groups of 4 consecutive blocks
 // b0 = 4 sub, 4 (sub + nl), ...; products in V.
-template <typename V>
+template <typename V, typename X>
 AMG_HD void k0_row_partial(const long long *rowoff, const int *npad, const int *cols, const V *val,
-                           const double *x, int row, int sub, int nl, V &y0, V &y1, V &y2)
+                           const X *x, int row, int sub, int nl, V &y0, V &y1, V &y2)
 {
     const long long off = rowoff[row];
     const int np = npad[row];
@@ -65,8 +117,8 @@ AMG_HD void k0_row_partial(const long long *rowoff, const int *npad, const int *
         for (int k = 0; k < 9; k++)
             load4(vr + (size_t)k * np + b0, v[k]);
         for (int j = 0; j < 4; j++) {
-            const double *xv = x + 4 * (size_t)cols[off + b0 + j];
-            const V x0 = (V)xv[0], x1 = (V)xv[1], x2 = (V)xv[2];
+            V x0, x1, x2;
+            load_xyz<V>(x + 4 * (size_t)cols[off + b0 + j], x0, x1, x2);
             y0 += v[0][j] * x0 + v[1][j] * x1 + v[2][j] * x2;
             y1 += v[3][j] * x0 + v[4][j] * x1 + v[5][j] * x2;
             y2 += v[6][j] * x0 + v[7][j] * x1 + v[8][j] * x2;
@@ -75,77 +127,77 @@ AMG_HD void k0_row_partial(const long long *rowoff, const int *npad, const int *
 }
 
 // d = P^-1 r with the 3x3 block inverses stored [9][n]
-AMG_HD void pinv_apply(const double *P, int n, int i, const double (&r)[3], double (&d)[3])
+template <typename T, typename PT>
+AMG_HD void pinv_apply(const PT *P, int n, int i, const T (&r)[3], T (&d)[3])
 {
     for (int a = 0; a < 3; a++)
-        d[a] = P[(size_t)(3 * a) * n + i] * r[0] + P[(size_t)(3 * a + 1) * n + i] * r[1] +
-               P[(size_t)(3 * a + 2) * n + i] * r[2];
+        d[a] = (T)P[(size_t)(3 * a) * n + i] * r[0] + (T)P[(size_t)(3 * a + 1) * n + i] * r[1] +
+               (T)P[(size_t)(3 * a + 2) * n + i] * r[2];
 }
 
 // Level-0 epilogue of row `row` given K x (y): SM_RESID out = mask(b - y);
 // SM_SMOOTH out = mask(x + omega Pinv mask(b - y)).
-AMG_HD void k0_epilogue(int mode, int n, int row, uint8_t m, const double *Pinv, double omega, const double *x,
-                        const double *b, double *out, double y0, double y1, double y2)
+template <typename T, typename PT, typename O>
+AMG_HD void k0_epilogue(int mode, int n, int row, uint8_t m, const PT *Pinv, T omega, const T *x, const T *b,
+                        O *out, T y0, T y1, T y2)
 {
-    const double *bb = b + 4 * (size_t)row;
-    double r[3] = {(m & 1) ? bb[0] - y0 : 0.0, (m & 2) ? bb[1] - y1 : 0.0, (m & 4) ? bb[2] - y2 : 0.0};
-    double *o = out + 4 * (size_t)row;
+    T b0, b1, b2;
+    load_xyz<T>(b + 4 * (size_t)row, b0, b1, b2);
+    T r[3] = {(m & 1) ? b0 - y0 : T(0), (m & 2) ? b1 - y1 : T(0), (m & 4) ? b2 - y2 : T(0)};
+    O *o = out + 4 * (size_t)row;
     if (mode == SM_RESID) {
-        o[0] = r[0];
-        o[1] = r[1];
-        o[2] = r[2];
+        store_xyz<T>(o, r[0], r[1], r[2]);
     } else {
-        double d[3];
-        pinv_apply(Pinv, n, row, r, d);
-        const double *xr = x + 4 * (size_t)row;
-        o[0] = (m & 1) ? xr[0] + omega * d[0] : 0.0;
-        o[1] = (m & 2) ? xr[1] + omega * d[1] : 0.0;
-        o[2] = (m & 4) ? xr[2] + omega * d[2] : 0.0;
+        T d[3];
+        pinv_apply<T, PT>(Pinv, n, row, r, d);
+        T x0, x1, x2;
+        load_xyz<T>(x + 4 * (size_t)row, x0, x1, x2);
+        store_xyz<T>(o, (m & 1) ? x0 + omega * d[0] : T(0), (m & 2) ? x1 + omega * d[1] : T(0),
+                     (m & 4) ? x2 + omega * d[2] : T(0));
     }
-    o[3] = 0.0;
 }
 
-// Level 0, first sweep from zero: out = mask(omega Pinv mask(b))
-AMG_HD void jacobi0_row(int n, int i, uint8_t m, const double *Pinv, double omega, const double *b, double *out)
+// Level 0, first sweep from zero: out = mask(omega Pinv mask(b)), and the
+// right-hand side in the iteration's precision (bt = b)
+template <typename T, typename PT, typename B>
+AMG_HD void jacobi0_row(int n, int i, uint8_t m, const PT *Pinv, T omega, const B *b, T *bt, T *out)
 {
-    const double *bb = b + 4 * (size_t)i;
-    const double r[3] = {(m & 1) ? bb[0] : 0.0, (m & 2) ? bb[1] : 0.0, (m & 4) ? bb[2] : 0.0};
-    double d[3];
-    pinv_apply(Pinv, n, i, r, d);
-    double *o = out + 4 * (size_t)i;
-    o[0] = (m & 1) ? omega * d[0] : 0.0;
-    o[1] = (m & 2) ? omega * d[1] : 0.0;
-    o[2] = (m & 4) ? omega * d[2] : 0.0;
-    o[3] = 0.0;
+    T b0, b1, b2;
+    load_xyz<T>(b + 4 * (size_t)i, b0, b1, b2);
+    const T r[3] = {(m & 1) ? b0 : T(0), (m & 2) ? b1 : T(0), (m & 4) ? b2 : T(0)};
+    store_xyz<T>(bt + 4 * (size_t)i, r[0], r[1], r[2]);
+    T d[3];
+    pinv_apply<T, PT>(Pinv, n, i, r, d);
+    store_xyz<T>(out + 4 * (size_t)i, (m & 1) ? omega * d[0] : T(0), (m & 2) ? omega * d[1] : T(0),
+                 (m & 4) ? omega * d[2] : T(0));
 }
 
 // Block-CSR level: partial y of block row `row` (R x C row-major blocks of
-// VT, FP64 for the coarse operators, FP32 for the prolongation and
-// restriction; block column j of x at x[j * SX]) over the blocks
-// ptr[row] + sub, + nl, ...; products and sums in FP64.
-template <int R, int C, typename VT>
-AMG_HD void bsr_row_partial(const long long *ptr, const int *col, const VT *val, const double *x, int SX,
-                            int row, int sub, int nl, double (&y)[R])
+// T; block column j of x at x[j * SX]) over the blocks ptr[row] + sub,
+// + nl, ...
+template <int R, int C, typename T>
+AMG_HD void bsr_row_partial(const long long *ptr, const int *col, const T *val, const T *x, int SX, int row,
+                            int sub, int nl, T (&y)[R])
 {
     for (long long k = ptr[row] + sub; k < ptr[row + 1]; k += nl) {
-        const VT *blk = val + (size_t)k * (R * C);
-        const double *xc = x + (size_t)col[k] * SX;
-        double xv[C];
+        const T *blk = val + (size_t)k * (R * C);
+        const T *xc = x + (size_t)col[k] * SX;
+        T xv[C];
         for (int c = 0; c < C; c++)
             xv[c] = xc[c];
         for (int r = 0; r < R; r++)
             for (int c = 0; c < C; c++)
-                y[r] += (double)blk[r * C + c] * xv[c];
+                y[r] += blk[r * C + c] * xv[c];
     }
 }
 
 // BM_SET: out[row * SY + r] = y_r; BM_ADD: += y_r; BM_SMOOTH (R = C = 6):
 // out = x_row + omega Dinv (b - y); BM_RESID: out = b - y.
-template <int R, int MODE>
-AMG_HD void bsr_epilogue(int row, const double (&y)[R], const double *x, int SX, double *out, int SY, const double *b,
-                         const double *dinv, double omega)
+template <int R, int MODE, typename T>
+AMG_HD void bsr_epilogue(int row, const T (&y)[R], const T *x, int SX, T *out, int SY, const T *b, const T *dinv,
+                         T omega)
 {
-    double *o = out + (size_t)row * SY;
+    T *o = out + (size_t)row * SY;
     if (MODE == BM_SET) {
         for (int r = 0; r < R; r++)
             o[r] = y[r];
@@ -153,17 +205,17 @@ AMG_HD void bsr_epilogue(int row, const double (&y)[R], const double *x, int SX,
         for (int r = 0; r < R; r++)
             o[r] += y[r];
     } else {
-        double rr[R];
+        T rr[R];
         for (int r = 0; r < R; r++)
             rr[r] = b[(size_t)row * R + r] - y[r];
         if (MODE == BM_RESID) {
             for (int r = 0; r < R; r++)
                 o[r] = rr[r];
         } else {
-            const double *D = dinv + (size_t)row * (R * R);
-            const double *xr = x + (size_t)row * SX;
+            const T *D = dinv + (size_t)row * (R * R);
+            const T *xr = x + (size_t)row * SX;
             for (int r = 0; r < R; r++) {
-                double s = 0.0;
+                T s = 0;
                 for (int c = 0; c < R; c++)
                     s += D[r * R + c] * rr[c];
                 o[r] = xr[r] + omega * s;
@@ -173,11 +225,12 @@ AMG_HD void bsr_epilogue(int row, const double (&y)[R], const double *x, int SX,
 }
 
 // 6-DOF level, first sweep from zero: out = omega Dinv b
-AMG_HD void jacobi6_row(int i, const double *dinv, double omega, const double *b, double *out)
+template <typename T>
+AMG_HD void jacobi6_row(int i, const T *dinv, T omega, const T *b, T *out)
 {
-    const double *D = dinv + (size_t)i * 36;
+    const T *D = dinv + (size_t)i * 36;
     for (int r = 0; r < 6; r++) {
-        double s = 0.0;
+        T s = 0;
         for (int c = 0; c < 6; c++)
             s += D[r * 6 + c] * b[(size_t)i * 6 + c];
         out[(size_t)i * 6 + r] = omega * s;
@@ -185,13 +238,14 @@ AMG_HD void jacobi6_row(int i, const double *dinv, double omega, const double *b
 }
 
 // Coarsest level, entry k of Cinv b over the columns j = sub, sub + nl, ...
-// (entry j of a vector at (j / B) * S + j % B)
-AMG_HD double dense_row_partial(int nc, const double *Cinv, const double *b, int B, int S, int k, int sub, int nl)
+// (entry j of a vector at (j / B) * S + j % B); FP64 sums
+template <typename T>
+AMG_HD double dense_row_partial(int nc, const double *Cinv, const T *b, int B, int S, int k, int sub, int nl)
 {
     const double *row = Cinv + (size_t)k * nc;
     double s = 0.0;
     for (int j = sub; j < nc; j += nl)
-        s += row[j] * b[(size_t)(j / B) * S + j % B];
+        s += row[j] * (double)b[(size_t)(j / B) * S + j % B];
     return s;
 }
 

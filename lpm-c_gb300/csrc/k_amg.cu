@@ -206,9 +206,11 @@ __global__ void __launch_bounds__(ATPB) k_amg_reliable(AmgVec a, const dvec4 *rt
 
 enum { RZ_INIT = 0, RZ_ITER = 1, RZ_RELIABLE = 2 };
 
-// r.z after the V-cycle: INIT also sets p = z; ITER sets beta
+// r.z after the V-cycle: INIT also sets p = z (and its two FP32 parts when
+// hi is given); ITER sets beta
 template <int MODE>
-__global__ void __launch_bounds__(ATPB) k_amg_rz(AmgVec a, const dvec4 *r, const dvec4 *z, dvec4 *p)
+__global__ void __launch_bounds__(ATPB) k_amg_rz(AmgVec a, const dvec4 *r, const dvec4 *z, dvec4 *p,
+                                                 float4 *hi = nullptr, float4 *lo = nullptr)
 {
     CgScalars *sc = a.sc;
     if (sc->done)
@@ -216,8 +218,16 @@ __global__ void __launch_bounds__(ATPB) k_amg_rz(AmgVec a, const dvec4 *r, const
     double v[1] = {0.0};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
         const dvec4 rv = r[i], zv = z[i];
-        if (MODE == RZ_INIT)
+        if (MODE == RZ_INIT) {
             p[i] = zv;
+            if (hi) {
+                const float hx = __double2float_rn(zv.x), hy = __double2float_rn(zv.y),
+                            hz = __double2float_rn(zv.z);
+                hi[i] = make_float4(hx, hy, hz, 0.f);
+                lo[i] = make_float4(__double2float_rn(zv.x - (double)hx), __double2float_rn(zv.y - (double)hy),
+                                    __double2float_rn(zv.z - (double)hz), 0.f);
+            }
+        }
         v[0] += rv.x * zv.x + rv.y * zv.y + rv.z * zv.z;
     }
     amg_reduce<1>(v, a.partials, a.counter, [sc](const double *t) {
@@ -240,15 +250,16 @@ constexpr int L0_LANES = 16;  // lanes per block row of the stiffness
 
 // MODE SM_SMOOTH: out = x + omega Pinv mask(b - K x); SM_RESID: out = mask(b - K x).
 // Half a warp per block row, lanes over the row's blocks (padding included:
-// zero values, column of the row itself); products in V as the SpMV of the
-// same precision, epilogue in FP64 (amg_rows.h).
-template <typename V, int MODE>
+// zero values, column of the row itself); FP32 values, vectors and
+// arithmetic (amg_rows.h).  O: float (an iterate of the cycle) or double
+// (its last sweep, the PCG's z).
+template <int MODE, typename O>
 __global__ void __launch_bounds__(ATPB) k_amg_k0(int n, const long long *__restrict__ rowoff,
                                                  const int *__restrict__ npad, const int *__restrict__ cols,
-                                                 const uint8_t *__restrict__ mask, const V *__restrict__ val,
-                                                 const double *__restrict__ Pinv, double omega,
-                                                 const double *__restrict__ x, const double *__restrict__ b,
-                                                 double *__restrict__ out, const CgScalars *sc)
+                                                 const uint8_t *__restrict__ mask, const float *__restrict__ val,
+                                                 const float *__restrict__ Pinv, float omega,
+                                                 const float *__restrict__ x, const float *__restrict__ b,
+                                                 O *__restrict__ out, const CgScalars *sc)
 {
     if (sc && sc->done)
         return;
@@ -257,8 +268,8 @@ __global__ void __launch_bounds__(ATPB) k_amg_k0(int n, const long long *__restr
     const int g = (blockIdx.x * blockDim.x + threadIdx.x) / L0_LANES;
     const int ng = (gridDim.x * blockDim.x) / L0_LANES;
     for (int row = g; row < n; row += ng) {
-        V y0 = 0, y1 = 0, y2 = 0;
-        k0_row_partial<V>(rowoff, npad, cols, val, x, row, sub, L0_LANES, y0, y1, y2);
+        float y0 = 0.f, y1 = 0.f, y2 = 0.f;
+        k0_row_partial<float, float>(rowoff, npad, cols, val, x, row, sub, L0_LANES, y0, y1, y2);
 #pragma unroll
         for (int o = L0_LANES / 2; o > 0; o >>= 1) {
             y0 += __shfl_xor_sync(gmask, y0, o);
@@ -266,20 +277,21 @@ __global__ void __launch_bounds__(ATPB) k_amg_k0(int n, const long long *__restr
             y2 += __shfl_xor_sync(gmask, y2, o);
         }
         if (sub == 0)
-            k0_epilogue(MODE, n, row, mask[row], Pinv, omega, x, b, out, (double)y0, (double)y1, (double)y2);
+            k0_epilogue<float, float, O>(MODE, n, row, mask[row], Pinv, omega, x, b, out, y0, y1, y2);
     }
 }
 
-// out = omega Pinv mask(b): the first sweep from zero on level 0
+// out = omega Pinv mask(b): the first sweep from zero on level 0; bt = the
+// right-hand side (the PCG residual, FP64) in FP32 for the later sweeps
 __global__ void __launch_bounds__(ATPB) k_amg_jacobi0(int n, const uint8_t *__restrict__ mask,
-                                                      const double *__restrict__ Pinv, double omega,
-                                                      const double *__restrict__ b, double *__restrict__ out,
-                                                      const CgScalars *sc)
+                                                      const float *__restrict__ Pinv, float omega,
+                                                      const double *__restrict__ b, float *__restrict__ bt,
+                                                      float *__restrict__ out, const CgScalars *sc)
 {
     if (sc && sc->done)
         return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        jacobi0_row(n, i, mask[i], Pinv, omega, b, out);
+        jacobi0_row<float, float, double>(n, i, mask[i], Pinv, omega, b, bt, out);
 }
 
 // ---- block-CSR levels -------------------------------------------------------------
@@ -288,13 +300,13 @@ constexpr int BL_LANES = 8;  // lanes per block row of the coarse-level kernels
 
 // R x C blocks, 8 lanes per block row, epilogue by MODE (amg_rows.h):
 // restriction (BM_SET), prolongation (BM_ADD), coarse smoothing (BM_SMOOTH)
-// and residual (BM_RESID).
-template <int R, int C, int MODE, typename VT>
+// and residual (BM_RESID); FP32 throughout.
+template <int R, int C, int MODE>
 __global__ void __launch_bounds__(ATPB) k_amg_bsr(int nbr, const long long *__restrict__ ptr,
-                                                  const int *__restrict__ col, const VT *__restrict__ val,
-                                                  const double *__restrict__ x, int SX, double *__restrict__ out,
-                                                  int SY, const double *__restrict__ b,
-                                                  const double *__restrict__ dinv, double omega,
+                                                  const int *__restrict__ col, const float *__restrict__ val,
+                                                  const float *__restrict__ x, int SX, float *__restrict__ out,
+                                                  int SY, const float *__restrict__ b,
+                                                  const float *__restrict__ dinv, float omega,
                                                   const CgScalars *sc)
 {
     static_assert(MODE == BM_SET || MODE == BM_ADD || (R == 6 && C == 6), "operator rows are 6 x 6");
@@ -305,38 +317,39 @@ __global__ void __launch_bounds__(ATPB) k_amg_bsr(int nbr, const long long *__re
     const int g = (blockIdx.x * blockDim.x + threadIdx.x) / BL_LANES;
     const int ng = (gridDim.x * blockDim.x) / BL_LANES;
     for (int row = g; row < nbr; row += ng) {
-        double y[R];
+        float y[R];
 #pragma unroll
         for (int r = 0; r < R; r++)
-            y[r] = 0.0;
-        bsr_row_partial<R, C, VT>(ptr, col, val, x, SX, row, sub, BL_LANES, y);
+            y[r] = 0.f;
+        bsr_row_partial<R, C, float>(ptr, col, val, x, SX, row, sub, BL_LANES, y);
 #pragma unroll
         for (int o = BL_LANES / 2; o > 0; o >>= 1)
 #pragma unroll
             for (int r = 0; r < R; r++)
                 y[r] += __shfl_xor_sync(gmask, y[r], o);
         if (sub == 0)
-            bsr_epilogue<R, MODE>(row, y, x, SX, out, SY, b, dinv, omega);
+            bsr_epilogue<R, MODE, float>(row, y, x, SX, out, SY, b, dinv, omega);
     }
 }
 
 // out = omega Dinv b on a 6-DOF level: the first sweep from zero
-__global__ void __launch_bounds__(ATPB) k_amg_jacobi6(int nb, const double *__restrict__ dinv, double omega,
-                                                      const double *__restrict__ b, double *__restrict__ out,
+__global__ void __launch_bounds__(ATPB) k_amg_jacobi6(int nb, const float *__restrict__ dinv, float omega,
+                                                      const float *__restrict__ b, float *__restrict__ out,
                                                       const CgScalars *sc)
 {
     if (sc && sc->done)
         return;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += gridDim.x * blockDim.x)
-        jacobi6_row(i, dinv, omega, b, out);
+        jacobi6_row<float>(i, dinv, omega, b, out);
 }
 
-// Coarsest level: out = Cinv b (dense, nc x nc), one warp per output entry.
-// Entry k of a vector lives at (k / B) * S + k % B (B DOFs per block row,
-// stride S: 6/6 above level 0, 3/4 when level 0 is the coarsest).
+// Coarsest level: out = Cinv b (dense, nc x nc, FP64 sums), one warp per
+// output entry.  Entry k of a vector lives at (k / B) * S + k % B (B DOFs per
+// block row, stride S: 6/6 above level 0, 3/4 when level 0 is the coarsest).
+template <typename BT, typename OT>
 __global__ void __launch_bounds__(ATPB) k_amg_dense(int nc, const double *__restrict__ Cinv,
-                                                    const double *__restrict__ b, double *__restrict__ out, int B,
-                                                    int S, const CgScalars *sc)
+                                                    const BT *__restrict__ b, OT *__restrict__ out, int B, int S,
+                                                    const CgScalars *sc)
 {
     if (sc && sc->done)
         return;
@@ -344,9 +357,9 @@ __global__ void __launch_bounds__(ATPB) k_amg_dense(int nc, const double *__rest
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     for (int k = w; k < nc; k += nw) {
-        const double s = amg_warp_sum(dense_row_partial(nc, Cinv, b, B, S, k, lane, 32));
+        const double s = amg_warp_sum(dense_row_partial<BT>(nc, Cinv, b, B, S, k, lane, 32));
         if (lane == 0)
-            out[(size_t)(k / B) * S + k % B] = s;
+            out[(size_t)(k / B) * S + k % B] = (OT)s;
     }
 }
 
@@ -361,17 +374,17 @@ static int grid_for(const Ctx &c, long long rows_x_threads)
 
 static AmgVec amg_vec(Ctx &c) { return AmgVec{c.n, c.mask, c.partials, c.counter, c.sc}; }
 
-static void k0_launch(Ctx &c, int mode, double omega, const dvec4 *xv, const dvec4 *bv, dvec4 *outv)
+template <typename O>
+static void k0_launch(Ctx &c, int mode, float omega, const float4 *xv, const float4 *bv, O *out)
 {
     const int g = grid_for(c, (long long)c.n * L0_LANES);
-    const double *x = (const double *)xv, *b = (const double *)bv;
-    double *out = (double *)outv;
+    const float *x = (const float *)xv, *b = (const float *)bv;
     if (mode == SM_SMOOTH)
-        k_amg_k0<float, SM_SMOOTH><<<g, ATPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.mask, c.Kf, c.Pinv_d,
-                                                             omega, x, b, out, c.sc);
+        k_amg_k0<SM_SMOOTH, O><<<g, ATPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.mask, c.Kf, c.Pinv_f,
+                                                          omega, x, b, out, c.sc);
     else
-        k_amg_k0<float, SM_RESID><<<g, ATPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.mask, c.Kf, c.Pinv_d,
-                                                            omega, x, b, out, c.sc);
+        k_amg_k0<SM_RESID, O><<<g, ATPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.mask, c.Kf, c.Pinv_f,
+                                                         omega, x, b, out, c.sc);
 }
 
 __global__ void k_to_float(long long count, const double *__restrict__ in, float *__restrict__ out)
@@ -387,20 +400,22 @@ void launch_amg_stiffness32(Ctx &c)
     k_to_float<<<grid_for(c, count), ATPB, 0, c.stream>>>(count, c.Kd, c.Kf);
 }
 
-template <int R, int C, int MODE, typename VT>
-static void bsr_launch(Ctx &c, int nbr, const long long *ptr, const int *col, const VT *val, const double *x,
-                       int SX, double *out, int SY, const double *b = nullptr, const double *dinv = nullptr,
-                       double omega = 0.0)
+template <int R, int C, int MODE>
+static void bsr_launch(Ctx &c, int nbr, const long long *ptr, const int *col, const float *val, const float *x,
+                       int SX, float *out, int SY, const float *b = nullptr, const float *dinv = nullptr,
+                       float omega = 0.f)
 {
     const int g = grid_for(c, (long long)nbr * BL_LANES);
-    k_amg_bsr<R, C, MODE, VT><<<g, ATPB, 0, c.stream>>>(nbr, ptr, col, val, x, SX, out, SY, b, dinv, omega, c.sc);
+    k_amg_bsr<R, C, MODE><<<g, ATPB, 0, c.stream>>>(nbr, ptr, col, val, x, SX, out, SY, b, dinv, omega, c.sc);
 }
 
-// With nu sweeps before and after the coarse correction, the iterate starts in
-// the scratch buffer (x, or tmp on level 0) and changes buffer with every
-// sweep but the first (2 nu - 1 times), so it ends in y (z on level 0); the
-// residual goes to the buffer the iterate is not in.
-void launch_amg_vcycle(Ctx &c, const dvec4 *r, dvec4 *z, dvec4 *tmp)
+// FP32 throughout; level 0 works on the float4 buffers r_f (the right-hand
+// side in FP32), x_f and q_f (the iterate and the residual), which the
+// multigrid PCG does not otherwise use, and its last sweep writes z (FP64).
+// With nu sweeps before and after the coarse correction, the iterate starts
+// in one scratch buffer and changes buffer with every sweep but the first
+// (2 nu - 1 times); the residual goes to the buffer the iterate is not in.
+void launch_amg_vcycle(Ctx &c, const dvec4 *r, dvec4 *z)
 {
     AmgDev &H = *c.amg;
     const int L = (int)H.lv.size();
@@ -408,83 +423,92 @@ void launch_amg_vcycle(Ctx &c, const dvec4 *r, dvec4 *z, dvec4 *tmp)
     const int gd = grid_for(c, (long long)H.nc * 32);
     if (L == 0) {
         // level 0 is the coarsest: z = Cinv r over the 3 DOFs of each particle
-        k_amg_dense<<<gd, ATPB, 0, c.stream>>>(H.nc, H.cinv, (const double *)r, (double *)z, 3, 4, c.sc);
+        k_amg_dense<double, double><<<gd, ATPB, 0, c.stream>>>(H.nc, H.cinv, (const double *)r, (double *)z, 3, 4,
+                                                               c.sc);
         return;
     }
+    float4 *bt = c.r_f;
     // down
     for (int l = 0; l < L; l++) {
         AmgDevLevel &v = H.lv[l];
-        double *bnext = (l + 1 < L) ? H.lv[l + 1].b : H.cb;
+        float *bnext = (l + 1 < L) ? H.lv[l + 1].b : H.cb;
+        const float om = (float)v.omega;
         if (l == 0) {
-            dvec4 *it = tmp, *ot = z;
-            k_amg_jacobi0<<<grid_for(c, c.n), ATPB, 0, c.stream>>>(c.n, c.mask, c.Pinv_d, v.omega,
-                                                                   (const double *)r, (double *)it, c.sc);
+            float4 *it = c.x_f, *ot = c.q_f;
+            k_amg_jacobi0<<<grid_for(c, c.n), ATPB, 0, c.stream>>>(c.n, c.mask, c.Pinv_f, om, (const double *)r,
+                                                                   (float *)bt, (float *)it, c.sc);
             for (int s = 1; s < nu; s++) {
-                k0_launch(c, SM_SMOOTH, v.omega, it, r, ot);
+                k0_launch<float>(c, SM_SMOOTH, om, it, bt, (float *)ot);
                 std::swap(it, ot);
             }
-            k0_launch(c, SM_RESID, v.omega, it, r, ot);
-            bsr_launch<6, 3, BM_SET>(c, v.nnext, v.pt_ptr, v.pt_col, v.pt_val, (const double *)ot, 4, bnext, 6);
+            k0_launch<float>(c, SM_RESID, om, it, bt, (float *)ot);
+            bsr_launch<6, 3, BM_SET>(c, v.nnext, v.pt_ptr, v.pt_col, v.pt_val, (const float *)ot, 4, bnext, 6);
         } else {
-            double *it = v.x, *ot = v.y;
-            k_amg_jacobi6<<<grid_for(c, v.nb), ATPB, 0, c.stream>>>(v.nb, v.dinv, v.omega, v.b, it, c.sc);
+            float *it = v.x, *ot = v.y;
+            k_amg_jacobi6<<<grid_for(c, v.nb), ATPB, 0, c.stream>>>(v.nb, v.dinv, om, v.b, it, c.sc);
             for (int s = 1; s < nu; s++) {
-                bsr_launch<6, 6, BM_SMOOTH>(c, v.nb, v.a_ptr, v.a_col, v.a_val, it, 6, ot, 6, v.b, v.dinv, v.omega);
+                bsr_launch<6, 6, BM_SMOOTH>(c, v.nb, v.a_ptr, v.a_col, v.a_val, it, 6, ot, 6, v.b, v.dinv, om);
                 std::swap(it, ot);
             }
             bsr_launch<6, 6, BM_RESID>(c, v.nb, v.a_ptr, v.a_col, v.a_val, it, 6, ot, 6, v.b);
             bsr_launch<6, 6, BM_SET>(c, v.nnext, v.pt_ptr, v.pt_col, v.pt_val, ot, 6, bnext, 6);
         }
     }
-    k_amg_dense<<<gd, ATPB, 0, c.stream>>>(H.nc, H.cinv, H.cb, H.cx, 6, 6, c.sc);
-    // up: the iterate is where the down sweep left it (x after an even
-    // number of swaps, y after an odd one)
+    k_amg_dense<float, float><<<gd, ATPB, 0, c.stream>>>(H.nc, H.cinv, H.cb, H.cx, 6, 6, c.sc);
+    // up: the iterate is where the down sweep left it (the first buffer after
+    // an even number of swaps, the second after an odd one)
     for (int l = L - 1; l >= 0; l--) {
         AmgDevLevel &v = H.lv[l];
-        const double *e = (l + 1 < L) ? H.lv[l + 1].y : H.cx;
+        const float *e = (l + 1 < L) ? H.lv[l + 1].y : H.cx;
+        const float om = (float)v.omega;
         if (l == 0) {
-            dvec4 *it = (nu % 2 == 1) ? tmp : z, *ot = (nu % 2 == 1) ? z : tmp;
-            bsr_launch<3, 6, BM_ADD>(c, v.nb, v.p_ptr, v.p_col, v.p_val, e, 6, (double *)it, 4);
+            float4 *it = (nu % 2 == 1) ? c.x_f : c.q_f, *ot = (nu % 2 == 1) ? c.q_f : c.x_f;
+            bsr_launch<3, 6, BM_ADD>(c, v.nb, v.p_ptr, v.p_col, v.p_val, e, 6, (float *)it, 4);
             for (int s = 0; s < nu; s++) {
-                k0_launch(c, SM_SMOOTH, v.omega, it, r, ot);
-                std::swap(it, ot);
+                if (s == nu - 1) {
+                    k0_launch<double>(c, SM_SMOOTH, om, it, bt, (double *)z);
+                } else {
+                    k0_launch<float>(c, SM_SMOOTH, om, it, bt, (float *)ot);
+                    std::swap(it, ot);
+                }
             }
         } else {
-            double *it = (nu % 2 == 1) ? v.x : v.y, *ot = (nu % 2 == 1) ? v.y : v.x;
+            float *it = (nu % 2 == 1) ? v.x : v.y, *ot = (nu % 2 == 1) ? v.y : v.x;
             bsr_launch<6, 6, BM_ADD>(c, v.nb, v.p_ptr, v.p_col, v.p_val, e, 6, it, 6);
             for (int s = 0; s < nu; s++) {
-                bsr_launch<6, 6, BM_SMOOTH>(c, v.nb, v.a_ptr, v.a_col, v.a_val, it, 6, ot, 6, v.b, v.dinv, v.omega);
+                bsr_launch<6, 6, BM_SMOOTH>(c, v.nb, v.a_ptr, v.a_col, v.a_val, it, 6, ot, 6, v.b, v.dinv, om);
                 std::swap(it, ot);
             }
         }
     }
 }
 
-void launch_amg_init(Ctx &c, const dvec4 *b, double scale, double delta2)
+void launch_amg_init(Ctx &c, const dvec4 *b, double scale, double delta2, bool k32)
 {
     k_amg_init<<<red_grid(c), ATPB, 0, c.stream>>>(amg_vec(c), b, scale, c.x_d, c.r_d, solve_rtol(c),
                                                    c.opts.cg_maxiter, delta2);
-    launch_amg_vcycle(c, c.r_d, c.z_d, c.q_d);
-    k_amg_rz<RZ_INIT><<<red_grid(c), ATPB, 0, c.stream>>>(amg_vec(c), c.r_d, c.z_d, c.p_d);
+    launch_amg_vcycle(c, c.r_d, c.z_d);
+    k_amg_rz<RZ_INIT><<<red_grid(c), ATPB, 0, c.stream>>>(amg_vec(c), c.r_d, c.z_d, c.p_d, k32 ? c.p_hi : nullptr,
+                                                          k32 ? c.p_lo : nullptr);
 }
 
 void launch_amg_iter(Ctx &c, bool k32)
 {
     if (k32)
-        launch_spmv_fx(c, c.p_d, c.q_d, true, true);
+        launch_spmv_diff(c, c.q_d, true);
     else
         launch_spmv_d(c, c.p_d, c.q_d, true, true);
     const int g = red_grid(c);
     k_amg_update<<<g, ATPB, 0, c.stream>>>(amg_vec(c), c.x_d, c.r_d, c.p_d, c.q_d);
-    launch_amg_vcycle(c, c.r_d, c.z_d, c.q_d);
+    launch_amg_vcycle(c, c.r_d, c.z_d);
     k_amg_rz<RZ_ITER><<<g, ATPB, 0, c.stream>>>(amg_vec(c), c.r_d, c.z_d, c.p_d);
-    launch_cg_p_d(c);
+    launch_cg_p_d(c, k32);
 }
 
 void launch_amg_reliable(Ctx &c, const dvec4 *rtrue)
 {
     k_amg_reliable<<<red_grid(c), ATPB, 0, c.stream>>>(amg_vec(c), rtrue, c.r_d);
-    launch_amg_vcycle(c, c.r_d, c.z_d, c.q_d);
+    launch_amg_vcycle(c, c.r_d, c.z_d);
     k_amg_rz<RZ_RELIABLE><<<red_grid(c), ATPB, 0, c.stream>>>(amg_vec(c), c.r_d, c.z_d, c.p_d);
 }
 
@@ -501,9 +525,11 @@ static int amg_alloc_copy(T *&d, const T *h, size_t count)
     return LPM_OK;
 }
 
-// prolongation and restriction values are kept in FP32 on the device: they
-// only shape the preconditioner, and they are read twice per V-cycle
-static std::vector<float> to_float(const avec<double> &v)
+// prolongation, restriction and coarse-operator values are kept in FP32 on
+// the device: they only shape the preconditioner, and FP32 halves their
+// traffic and keeps their products off the FP64 units
+template <typename Vec>
+static std::vector<float> to_float(const Vec &v)
 {
     std::vector<float> f(v.size());
 #pragma omp parallel for schedule(static)
@@ -526,7 +552,8 @@ static void amg_free_device(AmgDev &H)
     for (void *p : ps)
         if (p)
             cudaFree(p);
-    H.cinv = H.cb = H.cx = nullptr;
+    H.cinv = nullptr;
+    H.cb = H.cx = nullptr;
     H.nc = H.cbs = 0;
 }
 
@@ -561,19 +588,19 @@ static int amg_upload(AmgDev &H, const AmgHierarchy &h)
         if (l > 0) {
             if ((rc = amg_alloc_copy(v.a_ptr, s.A.ptr.data(), s.A.ptr.size())) ||
                 (rc = amg_alloc_copy(v.a_col, s.A.col.data(), s.A.col.size())) ||
-                (rc = amg_alloc_copy(v.a_val, s.A.val.data(), s.A.val.size())) ||
-                (rc = amg_alloc_copy(v.dinv, s.Dinv.data(), s.Dinv.size())) ||
-                (rc = amg_alloc_copy<double>(v.b, nullptr, 6 * (size_t)s.nblock)) ||
-                (rc = amg_alloc_copy<double>(v.x, nullptr, 6 * (size_t)s.nblock)) ||
-                (rc = amg_alloc_copy<double>(v.y, nullptr, 6 * (size_t)s.nblock)))
+                (rc = amg_alloc_copy(v.a_val, to_float(s.A.val).data(), s.A.val.size())) ||
+                (rc = amg_alloc_copy(v.dinv, to_float(s.Dinv).data(), s.Dinv.size())) ||
+                (rc = amg_alloc_copy<float>(v.b, nullptr, 6 * (size_t)s.nblock)) ||
+                (rc = amg_alloc_copy<float>(v.x, nullptr, 6 * (size_t)s.nblock)) ||
+                (rc = amg_alloc_copy<float>(v.y, nullptr, 6 * (size_t)s.nblock)))
                 return rc;
         }
     }
     H.nc = h.coarse_n;
     H.cbs = h.coarse_A.R;
     if ((rc = amg_alloc_copy(H.cinv, h.coarse_inv.data(), h.coarse_inv.size())) ||
-        (rc = amg_alloc_copy<double>(H.cb, nullptr, (size_t)H.nc)) ||
-        (rc = amg_alloc_copy<double>(H.cx, nullptr, (size_t)H.nc)))
+        (rc = amg_alloc_copy<float>(H.cb, nullptr, (size_t)H.nc)) ||
+        (rc = amg_alloc_copy<float>(H.cx, nullptr, (size_t)H.nc)))
         return rc;
     return LPM_OK;
 }

@@ -126,6 +126,8 @@ __global__ void __launch_bounds__(RR_TPB) k_update_rr_noalloc(int n, const doubl
 // Device address of the scratch array on the current device.  The first call
 // on a device looks it up (cudaGetSymbolAddress, which may load this
 // library's kernels onto that device); later calls reuse the cached address.
+// A device reset unloads the module and may reload it elsewhere, which is
+// why the header rules out calls after one.
 int rr_scratch_of(double **out)
 {
     int dev = -1;
@@ -169,11 +171,21 @@ extern "C" int lpm_update_rr_noalloc(int n, const double *Pin, const double *Pex
             norms[0] = norms[1] = 0.0;
         return LPM_OK;
     }
+    cudaStream_t s = (cudaStream_t)stream;
+    if (norms) {
+        // reading the norms waits on the stream, which a capture cannot hold
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaError_t ce = cudaStreamIsCapturing(s, &cs);
+        if (ce != cudaSuccess)
+            return fail(LPM_ERR_CUDA, std::string("lpm_update_rr_noalloc: cudaStreamIsCapturing: ") +
+                                          cudaGetErrorString(ce));
+        if (cs != cudaStreamCaptureStatusNone)
+            return fail(LPM_ERR_ARG, "lpm_update_rr_noalloc: norms must be NULL on a stream being captured");
+    }
     double *scratch = nullptr;
     int rc = rr_scratch_of(&scratch);
     if (rc)
         return rc;
-    cudaStream_t s = (cudaStream_t)stream;
     // the last-block counter must start at zero (a call cut short could leave it set)
     cudaError_t e = cudaMemsetAsync(scratch + RR_COUNTER, 0, sizeof(unsigned), s);
     if (e != cudaSuccess)

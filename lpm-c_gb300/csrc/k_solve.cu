@@ -266,6 +266,146 @@ __global__ void __launch_bounds__(VTPB) k_spmv(SpmvArgs a, const V *__restrict__
     }
 }
 
+// ---- difference-form FP32 product ---------------------------------------------
+//
+// The FP32 product K32 x with x rounded to FP32 is accurate only to about
+// 6e-8 |K| |x|.  The stiffness annihilates rigid translations, so on the
+// smooth vectors a multigrid-preconditioned CG works with, |K x| is smaller
+// than |K| |x| by about the condition number and the rounded product loses
+// all accuracy there (measured: the mixed multigrid PCG stagnates at 1M
+// particles).  The difference form
+//     (K32 x)_i = sum_j K32_ij (x_j - x_i) + R_i x_i,   R_i = sum_j K32_ij,
+// is an identity for the FP32 matrix; with x held as two FP32 parts
+// (hi = fl32(x), lo = fl32(x - hi)) the differences
+// (hi_j - hi_i) + (lo_j - lo_i) are formed in FP32 with an error relative to
+// the difference itself, and R_i, zero for the exact tangent (the bond forces
+// depend on relative positions only), is the FP64 row sum of the FP32
+// values.  The product error becomes about 6e-8 sum_j |K_ij| |x_j - x_i|:
+// FP32 arithmetic and an FP32 stiffness stream with the accuracy the CG needs.
+
+__device__ __forceinline__ void split_store(const dvec4 &v, float4 *hi, float4 *lo)
+{
+    const float hx = __double2float_rn(v.x), hy = __double2float_rn(v.y), hz = __double2float_rn(v.z);
+    *hi = make_float4(hx, hy, hz, 0.f);
+    *lo = make_float4(__double2float_rn(v.x - (double)hx), __double2float_rn(v.y - (double)hy),
+                      __double2float_rn(v.z - (double)hz), 0.f);
+}
+
+// Krs[k][row] = sum over the row's blocks of component k of Kf (FP64 sums,
+// rounded once); 16 lanes per block row, four blocks per lane per load.
+__global__ void __launch_bounds__(VTPB) k_row_sums(int n, const long long *__restrict__ rowoff,
+                                                   const int *__restrict__ npad, const float *__restrict__ val,
+                                                   float *__restrict__ out)
+{
+    const int sub = threadIdx.x & 15;
+    const unsigned gmask = 0xffffu << ((threadIdx.x & 31) & ~15);
+    const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 4;
+    const int ng = (gridDim.x * blockDim.x) >> 4;
+    for (int row = g; row < n; row += ng) {
+        const long long off = rowoff[row];
+        const int np = npad[row];
+        const float *vr = val + 9 * off;
+        double s[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++)
+            s[k] = 0.0;
+        for (int b0 = 4 * sub; b0 < np; b0 += 64) {
+#pragma unroll
+            for (int k = 0; k < 9; k++) {
+                const float4 v = __ldcs(reinterpret_cast<const float4 *>(vr + (size_t)k * np + b0));
+                s[k] += ((double)v.x + (double)v.y) + ((double)v.z + (double)v.w);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+#pragma unroll
+            for (int o = 8; o > 0; o >>= 1)
+                s[k] += __shfl_xor_sync(gmask, s[k], o);
+        }
+        if (sub == 0) {
+#pragma unroll
+            for (int k = 0; k < 9; k++)
+                out[(size_t)k * n + row] = (float)s[k];
+        }
+    }
+}
+
+// y = mask(K32 x) in the difference form from x = hi + lo; 16 lanes per
+// block row, four blocks per lane (the layout of k_spmv's default variant).
+// DOT: p.y with p = x64 (FP64) and alpha = rz / (p.y), as k_spmv.
+template <bool DOT>
+__global__ void __launch_bounds__(VTPB) k_spmv_diff(SpmvArgs a, const float *__restrict__ val,
+                                                    const float *__restrict__ rs, const float4 *__restrict__ hi,
+                                                    const float4 *__restrict__ lo, const dvec4 *__restrict__ x64,
+                                                    dvec4 *__restrict__ y)
+{
+    if (DOT && a.sc->done)
+        return;
+    const int sub = threadIdx.x & 15;
+    const unsigned gmask = 0xffffu << ((threadIdx.x & 31) & ~15);
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 4;
+    const int nhw = (gridDim.x * blockDim.x) >> 4;
+    const int n = a.n;
+    double dot = 0.0;
+    for (int row = gw; row < n; row += nhw) {
+        const long long off = a.rowoff[row];
+        const int np = a.npad[row];
+        const float *vr = val + 9 * off;
+        const float4 hi_i = __ldg(hi + row), lo_i = __ldg(lo + row);
+        float y0 = 0.f, y1 = 0.f, y2 = 0.f;
+        for (int b0 = 4 * sub; b0 < np; b0 += 64) {
+            int cc[4];
+            load_cols<4>(a.cols + off + b0, cc);
+            float v[9][4];
+#pragma unroll
+            for (int k = 0; k < 9; k++)
+                unpack<4>(ld_vals(reinterpret_cast<const float4 *>(vr + (size_t)k * np + b0)), v[k]);
+            float d[4][3];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const float4 h = __ldg(hi + cc[j]), l = __ldg(lo + cc[j]);
+                d[j][0] = (h.x - hi_i.x) + (l.x - lo_i.x);
+                d[j][1] = (h.y - hi_i.y) + (l.y - lo_i.y);
+                d[j][2] = (h.z - hi_i.z) + (l.z - lo_i.z);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                y0 += v[0][j] * d[j][0] + v[1][j] * d[j][1] + v[2][j] * d[j][2];
+                y1 += v[3][j] * d[j][0] + v[4][j] * d[j][1] + v[5][j] * d[j][2];
+                y2 += v[6][j] * d[j][0] + v[7][j] * d[j][1] + v[8][j] * d[j][2];
+            }
+        }
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) {
+            y0 += __shfl_xor_sync(gmask, y0, o);
+            y1 += __shfl_xor_sync(gmask, y1, o);
+            y2 += __shfl_xor_sync(gmask, y2, o);
+        }
+        if (sub == 0) {
+            // + R_i x_i (R_i is rounding-sized: hi_i suffices)
+            y0 += rs[(size_t)0 * n + row] * hi_i.x + rs[(size_t)1 * n + row] * hi_i.y + rs[(size_t)2 * n + row] * hi_i.z;
+            y1 += rs[(size_t)3 * n + row] * hi_i.x + rs[(size_t)4 * n + row] * hi_i.y + rs[(size_t)5 * n + row] * hi_i.z;
+            y2 += rs[(size_t)6 * n + row] * hi_i.x + rs[(size_t)7 * n + row] * hi_i.y + rs[(size_t)8 * n + row] * hi_i.z;
+            const uint8_t m = a.mask[row];
+            const double o0 = (m & 1) ? (double)y0 : 0.0, o1 = (m & 2) ? (double)y1 : 0.0,
+                         o2 = (m & 4) ? (double)y2 : 0.0;
+            y[row] = make_dvec4(o0, o1, o2, 0.0);
+            if (DOT) {
+                const dvec4 pv = x64[row];
+                dot += pv.x * o0 + pv.y * o1 + pv.z * o2;
+            }
+        }
+    }
+    if (DOT) {
+        double v[1] = {dot};
+        CgScalars *sc = a.sc;
+        grid_reduce<1>(v, a.partials, a.counter, [sc](const double *t) {
+            sc->pq = t[0];
+            sc->alpha = (t[0] != 0.0) ? sc->rz / t[0] : 0.0;
+        });
+    }
+}
+
 // Refinement residual r = b - K32 x64 with FP64 products and sums (masked),
 // and |r|^2 into norms[slot].  BATCH: only the rows of specimens due for a
 // reliable update (running with a request, or recursively converged).
@@ -455,8 +595,11 @@ __global__ void __launch_bounds__(VTPB) k_cg_update(VecArgs a, const V *P, V4 *x
 
 // p = z + beta p; the last block turns a pending reliable-update request into
 // done = 4, so the host updates only after p belongs to the new iteration.
+// With hi/lo (FP64 vectors only), p is also written as two FP32 parts for
+// the difference-form product (split_store).
 template <typename V, typename V4>
-__global__ void __launch_bounds__(VTPB) k_cg_p(int n, CgScalars *sc, const V4 *z, V4 *p, unsigned *counter)
+__global__ void __launch_bounds__(VTPB) k_cg_p(int n, CgScalars *sc, const V4 *z, V4 *p, unsigned *counter,
+                                               float4 *hi = nullptr, float4 *lo = nullptr)
 {
     if (sc->done)
         return;
@@ -468,6 +611,10 @@ __global__ void __launch_bounds__(VTPB) k_cg_p(int n, CgScalars *sc, const V4 *z
         pv.y = zv.y + be * pv.y;
         pv.z = zv.z + be * pv.z;
         p[i] = pv;
+        if constexpr (sizeof(V) == 8) {
+            if (hi)
+                split_store(pv, hi + i, lo + i);
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -732,10 +879,28 @@ void launch_cg_iter_d(Ctx &c)
     k_cg_p<double, dvec4><<<g, VTPB, 0, c.stream>>>(c.n, c.sc, c.z_d, c.p_d, c.counter);
 }
 
-// p = z + beta p on the FP64 vectors (the multigrid PCG, k_amg.cu)
-void launch_cg_p_d(Ctx &c)
+// p = z + beta p on the FP64 vectors (the multigrid PCG, k_amg.cu); split:
+// also the two FP32 parts of p for the difference-form product
+void launch_cg_p_d(Ctx &c, bool split)
 {
-    k_cg_p<double, dvec4><<<red_grid(c), VTPB, 0, c.stream>>>(c.n, c.sc, c.z_d, c.p_d, c.counter);
+    k_cg_p<double, dvec4><<<red_grid(c), VTPB, 0, c.stream>>>(c.n, c.sc, c.z_d, c.p_d, c.counter,
+                                                              split ? c.p_hi : nullptr, split ? c.p_lo : nullptr);
+}
+
+void launch_row_sums(Ctx &c)
+{
+    k_row_sums<<<spmv_grid(c), VTPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.Kf, c.Krs);
+}
+
+void launch_spmv_diff(Ctx &c, dvec4 *y, bool dot)
+{
+    SpmvArgs a = spmv_args(c);
+    record_timing(c, c.ev_a);
+    if (dot)
+        k_spmv_diff<true><<<spmv_grid(c), VTPB, 0, c.stream>>>(a, c.Kf, c.Krs, c.p_hi, c.p_lo, c.p_d, y);
+    else
+        k_spmv_diff<false><<<spmv_grid(c), VTPB, 0, c.stream>>>(a, c.Kf, c.Krs, c.p_hi, c.p_lo, c.p_d, y);
+    record_timing(c, c.ev_b);
 }
 
 void launch_cg_iter_f(Ctx &c)

@@ -281,6 +281,10 @@ void launch_block_jacobi(Ctx &c, bool fp32)
     } else {
         k_jacobi<double, double><<<g, STPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.nconn_d, c.Kd,
                                                            c.mask, c.Pinv_d);
+        // the multigrid's level-0 smoother works in FP32
+        if (c.opts.preconditioner == LPM_PRECOND_AMG && c.nspec == 0)
+            k_jacobi<double, float><<<g, STPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.nconn_d, c.Kd,
+                                                              c.mask, c.Pinv_f);
     }
 }
 

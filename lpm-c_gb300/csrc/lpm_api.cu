@@ -154,7 +154,7 @@ Ctx::~Ctx()
                     (void **)&rowoff, (void **)&npad, (void **)&cols, (void **)&Kd, (void **)&Kf,
                     (void **)&Pinv_d, (void **)&Pinv_f, (void **)&x_d, (void **)&r_d, (void **)&p_d,
                     (void **)&q_d, (void **)&z_d, (void **)&x_f, (void **)&r_f, (void **)&p_f, (void **)&q_f,
-                    (void **)&z_f, (void **)&pl_flag, (void **)&b_d, (void **)&sc, (void **)&partials, (void **)&counter,
+                    (void **)&z_f, (void **)&p_hi, (void **)&p_lo, (void **)&Krs, (void **)&pl_flag, (void **)&b_d, (void **)&sc, (void **)&partials, (void **)&counter,
                     (void **)&norms, (void **)&status};
     for (void **p : all)
         if (*p) {
@@ -311,6 +311,8 @@ static int alloc_specimen(Ctx &c)
     A_(c.W, 6 * n) A_(c.Pinv_d, 9 * n) A_(c.Pinv_f, 9 * n)
     A_(c.x_d, n) A_(c.r_d, n) A_(c.p_d, n) A_(c.q_d, n) A_(c.z_d, n) A_(c.b_d, n)
     A_(c.x_f, n) A_(c.r_f, n) A_(c.p_f, n) A_(c.q_f, n) A_(c.z_f, n)
+    A_(c.p_hi, n) A_(c.p_lo, n) A_(c.Krs, 9 * n)
+    c.krs_version = -1;
     for (int s = 0; s < 3; s++) {
         A_(c.dLp[s], nb) A_(c.alpha[s], n) A_(c.beta[s], 6 * n)
     }
@@ -858,7 +860,11 @@ static int solve_amg(Ctx &c, const dvec4 *b, double bn, lpm_step_stats *st)
     // 53 iterations); one per three decades keeps the FP32-product drift of
     // the recursive residual far below the tolerance checks on the true one.
     const double delta = std::min(c.opts.inner_rtol, 1e-3);
-    launch_amg_init(c, b, scale, k32 ? delta * delta : 0.0);
+    if (k32 && c.krs_version != c.kf_version) {
+        launch_row_sums(c);  // for the difference-form product
+        c.krs_version = c.kf_version;
+    }
+    launch_amg_init(c, b, scale, k32 ? delta * delta : 0.0, k32);
     int sweeps = 0, it = 0, done = 0;
     double rel = 1.0;
     for (;;) {

@@ -118,33 +118,33 @@ struct CgScalars {
 struct AdjointState;
 struct AsyncWriter;
 
-// One level of the multigrid hierarchy on the device.  Level 0 operates with
-// the stiffness itself (Kd or Kf, its block-Jacobi inverse Pinv_d) on dvec4
-// vectors; the levels above hold 6 DOFs per block row (aggregate), vectors
-// with 6 doubles per row, and their own 6 x 6 block-CSR operator.
+// One level of the multigrid hierarchy on the device, all in FP32.  Level 0
+// operates with the FP32 stiffness Kf and its block-Jacobi inverse Pinv_f on
+// float4 vectors; the levels above hold 6 DOFs per block row (aggregate),
+// vectors with 6 floats per row, and their own 6 x 6 block-CSR operator.
 struct AmgDevLevel {
     int nb = 0, bs = 0;  // block rows, DOFs per block row
     int nnext = 0;       // block rows of the next level
     double omega = 1.0;  // smoother damping 4/3 / rho(D^-1 A)
-    long long *a_ptr = nullptr;   // levels >= 1: operator, 6 x 6 blocks
+    long long *a_ptr = nullptr;   // levels >= 1: operator, 6 x 6 blocks (FP32 values)
     int *a_col = nullptr;
-    double *a_val = nullptr;
-    double *dinv = nullptr;       // levels >= 1: 6 x 6 diagonal-block inverses
+    float *a_val = nullptr;
+    float *dinv = nullptr;        // levels >= 1: 6 x 6 diagonal-block inverses
     long long *p_ptr = nullptr;   // prolongation, bs x 6 blocks (FP32 values)
     int *p_col = nullptr;
     float *p_val = nullptr;
     long long *pt_ptr = nullptr;  // restriction, 6 x bs blocks (FP32 values)
     int *pt_col = nullptr;
     float *pt_val = nullptr;
-    double *b = nullptr, *x = nullptr, *y = nullptr;  // levels >= 1: right-hand side, two iterates
+    float *b = nullptr, *x = nullptr, *y = nullptr;  // levels >= 1: right-hand side, two iterates
 };
 
 struct AmgDev {
     std::vector<AmgDevLevel> lv;
     int nc = 0;                    // scalar size of the coarsest operator
     int cbs = 0;                   // its DOFs per block row (3 when level 0 is the coarsest)
-    double *cinv = nullptr;        // its dense inverse, row-major
-    double *cb = nullptr, *cx = nullptr;
+    double *cinv = nullptr;        // its dense inverse, row-major (FP64)
+    float *cb = nullptr, *cx = nullptr;
     std::vector<uint8_t> mask_h;   // DOF mask the hierarchy was built for
     int ref_iters = -1;            // PCG iterations of the first solve after the build
     bool stale = false;            // rebuild before the next solve
@@ -264,6 +264,12 @@ struct Ctx {
     // ---- solver vectors
     dvec4 *x_d = nullptr, *r_d = nullptr, *p_d = nullptr, *q_d = nullptr, *z_d = nullptr;
     float4 *x_f = nullptr, *r_f = nullptr, *p_f = nullptr, *q_f = nullptr, *z_f = nullptr;
+    // the FP64 search direction split into two FP32 parts (p = hi + lo) for
+    // the difference-form FP32 product, and the FP32 stiffness's block row
+    // sums [9][n] it needs (for the assembly numbered krs_version)
+    float4 *p_hi = nullptr, *p_lo = nullptr;
+    float *Krs = nullptr;
+    long long krs_version = -1;
     dvec4 *b_d = nullptr;
     CgScalars *sc = nullptr;     // device
     CgScalars *sc_host = nullptr; // pinned mirror
@@ -365,10 +371,10 @@ void launch_block_jacobi(Ctx &c, bool fp32);
 // multigrid preconditioner (k_amg.cu): PCG with z = V-cycle(r), FP64
 // vectors; k32 selects the FP32 stiffness for the PCG product (mixed
 // precision); the V-cycle smooths with the FP32 stiffness in both precisions
-void launch_amg_init(Ctx &c, const dvec4 *b, double scale, double delta2);  // x = 0, r, z, p, rz
+void launch_amg_init(Ctx &c, const dvec4 *b, double scale, double delta2, bool k32);  // x = 0, r, z, p, rz
 void launch_amg_iter(Ctx &c, bool k32);
 void launch_amg_reliable(Ctx &c, const dvec4 *rtrue);  // r = rtrue (masked), z, rz; p kept
-void launch_amg_vcycle(Ctx &c, const dvec4 *r, dvec4 *z, dvec4 *tmp);  // smoother on the FP32 stiffness Kf
+void launch_amg_vcycle(Ctx &c, const dvec4 *r, dvec4 *z);  // z = V(r), FP32 inside (Kf, Pinv_f, x_f/q_f/r_f)
 void launch_amg_stiffness32(Ctx &c);  // Kf = (float) Kd, for the smoother under FP64 precision
 int amg_prepare(Ctx &c);  // (re)build the hierarchy when missing, stale or the mask changed
 void free_amg(Ctx &c);
@@ -379,7 +385,10 @@ void launch_refine_residual(Ctx &c, const dvec4 *x, const dvec4 *b, dvec4 *r, do
 void launch_spmv_fx(Ctx &c, const dvec4 *x, dvec4 *y, bool masked, bool dot);
 void launch_cg_init_fx(Ctx &c, const dvec4 *b, double scale, double delta2);
 void launch_cg_iter_fx(Ctx &c);
-void launch_cg_p_d(Ctx &c);  // p = z + beta p (FP64 vectors)
+void launch_cg_p_d(Ctx &c, bool split = false);  // p = z + beta p (FP64 vectors); split: also p_hi/p_lo
+void launch_row_sums(Ctx &c);  // Krs = block row sums of Kf (FP64 sums of the FP32 values)
+// y = K32 p in difference form from p_hi/p_lo and Krs (masked); dot: p.y and alpha
+void launch_spmv_diff(Ctx &c, dvec4 *y, bool dot);
 void launch_reliable_d(Ctx &c, const dvec4 *rtrue);
 void launch_cg_init_d(Ctx &c, const dvec4 *b, double scale);
 void launch_cg_init_f(Ctx &c, const dvec4 *r64, double scale, double rtol, double delta2);

@@ -10,7 +10,17 @@
  * createCuboid / searchNormalNeighbor / searchAFEMNeighbor).
  *
  * Exported for scripting (ctypes): lpmh_setup, lpmh_set_types,
- * lpmh_set_material, lpmh_init, lpmh_load_step, lpmh_get, lpmh_n.
+ * lpmh_set_bc_groups, lpmh_set_material, lpmh_init, lpmh_load_step,
+ * lpmh_get, lpmh_n.
+ *
+ * Per-particle moduli: the reference takes elastic constants per type
+ * (Ce[type[i]], src/stiffness.c:186-200), so a material that varies from
+ * particle to particle gives every particle its own type.  Its boundary
+ * conditions, which setDispBC/setForceBC select by type
+ * (src/boundary.c:12-70), are then given as BC groups: lpmh_set_bc_groups
+ * stores one group label per particle, and each load step hands setDispBC
+ * and setForceBC that label array in place of `type` (the functions
+ * themselves are unchanged).
  */
 #include <math.h>
 #include <stdio.h>
@@ -267,6 +277,36 @@ void lpmh_set_types(const int *t, int nt)
     ntype = nt;
 }
 
+/* BC group label per particle (NULL: boundary conditions select by type) */
+static int *g_bc_group, g_bc_ngroup;
+
+void lpmh_set_bc_groups(const int *g, int ngroup)
+{
+    free(g_bc_group);
+    g_bc_group = NULL;
+    g_bc_ngroup = 0;
+    if (!g)
+        return;
+    g_bc_group = (int *)malloc(sizeof(int) * (size_t)nparticle);
+    memcpy(g_bc_group, g, sizeof(int) * (size_t)nparticle);
+    g_bc_ngroup = ngroup;
+}
+
+/* setDispBC + setForceBC (src/lpmc_project.c:402-403), selecting particles by
+ * BC group when groups are set */
+static void apply_bcs(int nbd, struct dispBCPara *dbp, int nbf, struct forceBCPara *fbp)
+{
+    int *t = type, nt = ntype;
+    if (g_bc_group) {
+        type = g_bc_group;
+        ntype = g_bc_ngroup;
+    }
+    setDispBC(nbd, dbp);
+    setForceBC(nbf, fbp);
+    type = t;
+    ntype = nt;
+}
+
 /* ce: ntype x 3; sy: per particle; cp: tau0, taus, h0, p, q, eta, maxloop, dtime */
 void lpmh_set_material(const double *ce, int pl, const double *sy, double xi, double H, const double *cp)
 {
@@ -340,8 +380,7 @@ int lpmh_load_step(int nbd, struct dispBCPara *dbp, int nbf, struct forceBCPara 
     }
     memcpy(Pex_temp, Pex, sizeof(double) * dim * n);
     calcStiffness3DFiniteDifference(6);
-    setDispBC(nbd, dbp);
-    setForceBC(nbf, fbp);
+    apply_bcs(nbd, dbp, nbf, fbp);
     computeBondForceGeneral(4, 1);
     updateRR();
     int nreact = 0;
@@ -388,6 +427,10 @@ int lpmh_get(const char *name, double *out)
     } else if (!strcmp(name, "csz")) {
         for (int i = 0; i < n; i++)
             memcpy(out + (size_t)i * nn, csz[i], sizeof(double) * nn);
+    } else if (!strcmp(name, "Kn") || !strcmp(name, "Tv")) {
+        double **a = name[0] == 'K' ? Kn : Tv;
+        for (int i = 0; i < n; i++)
+            memcpy(out + (size_t)i * nn, a[i], sizeof(double) * nn);
     } else if (!strcmp(name, "dL")) {
         for (int i = 0; i < n; i++)
             memcpy(out + (size_t)i * nn, dL[i], sizeof(double) * nn);

@@ -22,6 +22,7 @@ class HostDriver:
         dp = C.POINTER(C.c_double)
         self.L.lpmh_setup.argtypes = [C.c_int, C.c_double, dp, C.c_int]
         self.L.lpmh_set_types.argtypes = [C.POINTER(C.c_int), C.c_int]
+        self.L.lpmh_set_bc_groups.argtypes = [C.POINTER(C.c_int), C.c_int]
         self.L.lpmh_set_material.argtypes = [dp, C.c_int, dp, C.c_double, C.c_double, dp]
         self.L.lpmh_load_step.argtypes = [C.c_int, C.POINTER(G.DispBC), C.c_int, C.POINTER(G.ForceBC),
                                           C.c_double, C.c_int, dp]
@@ -40,6 +41,15 @@ class HostDriver:
     def set_types(self, types, ntype):
         t = np.ascontiguousarray(types, dtype=np.int32)
         self.L.lpmh_set_types(t.ctypes.data_as(C.POINTER(C.c_int)), int(ntype))
+
+    def set_bc_groups(self, groups, ngroup):
+        """Boundary conditions select particles by these labels instead of
+        their type (per-particle moduli: one type per particle)."""
+        if groups is None:
+            self.L.lpmh_set_bc_groups(None, 0)
+            return
+        g = np.ascontiguousarray(groups, dtype=np.int32)
+        self.L.lpmh_set_bc_groups(g.ctypes.data_as(C.POINTER(C.c_int)), int(ngroup))
 
     def set_material(self, ce, plmode, sigmay, xi, H, cp=None):
         ce = np.ascontiguousarray(ce, dtype=np.float64).reshape(-1)
@@ -70,7 +80,8 @@ class HostDriver:
 
     def get(self, name):
         shape = {"xyz": (self.n, 3), "xyz_initial": (self.n, 3), "J2_alpha": (self.n,),
-                 "F": (self.n, 18), "csz": (self.n, 18), "dL": (self.n, 18),
+                 "F": (self.n, 18), "csz": (self.n, 18), "dL": (self.n, 18), "Kn": (self.n, 18),
+                 "Tv": (self.n, 18),
                  "strain_tensor": (self.n, 6)}[name]
         out = np.zeros(shape)
         if self.L.lpmh_get(name.encode(), out.ctypes.data_as(C.POINTER(C.c_double))) != 0:

@@ -763,6 +763,57 @@ void lo_fd_stiffness_range(lpm_oracle *o, int i0, int i1)
     free(Kloc);
 }
 
+/* Timing helper for the CPU baseline: calcStiffness3DFiniteDifference's
+ * OpenMP loop over block rows (src/stiffness.c:388-516) on `threads` threads
+ * (the reference's main runs it on nt_force = 3, src/lpmc_project.c:57,391)
+ * for `count` rows spread evenly over the lattice.  Like the reference's
+ * parallel loop, the row bodies write the shared per-particle arrays and the
+ * matrix without synchronisation, so the state is not used afterwards.
+ * Returns the wall time in seconds. */
+double lo_fd_stiffness_timing(lpm_oracle *o, int count, int threads)
+{
+    if (count > o->n)
+        count = o->n;
+    if (count < 1)
+        return 0.0;
+    int w = o->nafem + 1;
+    double h = EPSP * o->radius;
+    long long stride = o->n / count;
+    double t0 = omp_get_wtime();
+#pragma omp parallel num_threads(threads)
+    {
+        double *Kloc = DALLOC(3 * w * 3);
+#pragma omp for schedule(dynamic, 16)
+        for (int k = 0; k < count; k++) {
+            int i = (int)(k * stride);
+            int nc = o->nconn[i];
+            force_elastic_one(o, i);
+            double f0[3] = {o->Pin[3 * i], o->Pin[3 * i + 1], o->Pin[3 * i + 2]};
+            for (int jid = 0; jid < nc; jid++) {
+                int p = o->conn[(size_t)i * w + jid];
+                for (int r = 0; r < 3; r++) {
+                    double xt = o->xyz[3 * p + r];
+                    o->xyz[3 * p + r] = xt + h;
+                    force_elastic_one(o, i);
+                    o->xyz[3 * p + r] = xt;
+                    for (int s2 = 0; s2 < 3; s2++)
+                        Kloc[3 * nc * r + 3 * jid + s2] = (o->Pin[3 * i + s2] - f0[s2]) / EPSP / o->radius;
+                }
+            }
+            for (int jid = 0; jid < nc; jid++) {
+                int jj = o->conn[(size_t)i * w + jid];
+                double Kl[3][3];
+                for (int r = 0; r < 3; r++)
+                    for (int s2 = 0; s2 < 3; s2++)
+                        Kl[r][s2] = Kloc[3 * nc * s2 + 3 * jid + r];
+                scatter_block(o, i, jj, Kl);
+            }
+        }
+        free(Kloc);
+    }
+    return omp_get_wtime() - t0;
+}
+
 void lo_fd_stiffness(lpm_oracle *o)
 {
     memset(o->K, 0, sizeof(double) * o->nnz);

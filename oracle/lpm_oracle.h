@@ -77,6 +77,7 @@ void lo_set_threads(int n);
 void lo_computedL(lpm_oracle *o);
 void lo_fd_stiffness(lpm_oracle *o);
 void lo_fd_stiffness_range(lpm_oracle *o, int i0, int i1);
+double lo_fd_stiffness_timing(lpm_oracle *o, int count, int threads);
 void lo_set_disp_bc(lpm_oracle *o, int n, const lo_disp_bc *d);
 void lo_set_force_bc(lpm_oracle *o, int n, const lo_force_bc *f);
 void lo_bc_stiffness_update(lpm_oracle *o);

@@ -59,6 +59,8 @@ def lib():
             getattr(L, f).argtypes = [vp]
         L.lo_fd_stiffness_range.argtypes = [vp, C.c_int, C.c_int]
         L.lo_cg_iterations.argtypes = [vp, C.c_int]
+        L.lo_fd_stiffness_timing.argtypes = [vp, C.c_int, C.c_int]
+        L.lo_fd_stiffness_timing.restype = C.c_double
         L.lo_set_disp_bc.argtypes = [vp, C.c_int, C.POINTER(DispBC)]
         L.lo_set_force_bc.argtypes = [vp, C.c_int, C.POINTER(ForceBC)]
         L.lo_solver_cg.argtypes = [vp, C.c_double, C.c_double]

@@ -4,8 +4,8 @@
 // (a level-0 vector, 4 doubles per particle), it also applies the device's
 // V-cycle to it: the launch sequence of launch_amg_vcycle (k_amg.cu), each
 // kernel's rows computed one after another by the same per-row functions
-// (amg_rows.h), with the stiffness in FP64 (z.bin) and in FP32 (z32.bin), and
-// the prolongation and restriction in FP32 as the device keeps them.
+// (amg_rows.h), all in FP64 (z.bin) and all in FP32 as the device runs it
+// (z32.bin).
 //   amg_harness DIR AGG_SPACING [SWEEPS]
 #include <algorithm>
 #include <chrono>
@@ -45,112 +45,124 @@ static void wr_bsr(FILE *f, const std::string &p, const lpm::Bsr &A)
     wr(p + "_val.bin", A.val);
 }
 
+template <typename T>
 struct Level0 {
     int n;
     const uint8_t *mask;
     const long long *rowoff;
     const int *npad, *cols;
-    const double *Pinv;
+    const T *Pinv;
 };
 
-template <typename V>
-static void k0(const Level0 &z0, const V *val, int mode, double omega, const double *x, const double *b, double *out)
+// one launch of k_amg_k0, rows one after another (V: stiffness values and
+// products, T: vectors and epilogue)
+template <typename V, typename T, typename O>
+static void k0(const Level0<T> &z0, const V *val, int mode, T omega, const T *x, const T *b, O *out)
 {
     for (int row = 0; row < z0.n; row++) {
         V y0 = 0, y1 = 0, y2 = 0;
-        lpm::k0_row_partial<V>(z0.rowoff, z0.npad, z0.cols, val, x, row, 0, 1, y0, y1, y2);
-        lpm::k0_epilogue(mode, z0.n, row, z0.mask[row], z0.Pinv, omega, x, b, out, y0, y1, y2);
+        lpm::k0_row_partial<V, T>(z0.rowoff, z0.npad, z0.cols, val, x, row, 0, 1, y0, y1, y2);
+        lpm::k0_epilogue<T, T, O>(mode, z0.n, row, z0.mask[row], z0.Pinv, omega, x, b, out, (T)y0, (T)y1, (T)y2);
     }
 }
 
-// values: the operator's FP64 ones, or the FP32 copies the device keeps of
-// the prolongation and restriction
-template <int R, int C, int MODE, typename VT>
-static void bsr(int nbr, const lpm::Bsr &M, const VT *val, const double *x, int SX, double *out, int SY,
-                const double *b = nullptr, const double *dinv = nullptr, double omega = 0.0)
+template <int R, int C, int MODE, typename T>
+static void bsr(int nbr, const lpm::Bsr &M, const T *val, const T *x, int SX, T *out, int SY, const T *b = nullptr,
+                const T *dinv = nullptr, T omega = 0)
 {
     for (int row = 0; row < nbr; row++) {
-        double y[R] = {};
-        lpm::bsr_row_partial<R, C, VT>(M.ptr.data(), M.col.data(), val, x, SX, row, 0, 1, y);
-        lpm::bsr_epilogue<R, MODE>(row, y, x, SX, out, SY, b, dinv, omega);
+        T y[R] = {};
+        lpm::bsr_row_partial<R, C, T>(M.ptr.data(), M.col.data(), val, x, SX, row, 0, 1, y);
+        lpm::bsr_epilogue<R, MODE, T>(row, y, x, SX, out, SY, b, dinv, omega);
     }
 }
 
-static std::vector<float> f32(const lpm::Bsr &M) { return std::vector<float>(M.val.begin(), M.val.end()); }
+template <typename T, typename S>
+static std::vector<T> conv(const S &v) { return std::vector<T>(v.begin(), v.end()); }
 
-static void dense(const lpm::AmgHierarchy &H, const double *b, double *out, int B, int S)
+template <typename BT, typename OT>
+static void dense(const lpm::AmgHierarchy &H, const BT *b, OT *out, int B, int S)
 {
     for (int k = 0; k < H.coarse_n; k++)
-        out[(size_t)(k / B) * S + k % B] = lpm::dense_row_partial(H.coarse_n, H.coarse_inv.data(), b, B, S, k, 0, 1);
+        out[(size_t)(k / B) * S + k % B] = (OT)lpm::dense_row_partial<BT>(H.coarse_n, H.coarse_inv.data(), b, B, S, k,
+                                                                          0, 1);
 }
 
 // z = V(r), in the order and with the buffers of launch_amg_vcycle (nu
-// sweeps before and after each coarse correction)
-template <typename V>
-static void vcycle(const lpm::AmgHierarchy &H, const Level0 &z0, const V *val, const double *r, double *z, double *tmp,
-                   int nu)
+// sweeps before and after each coarse correction); V: stiffness values, T:
+// everything else (the device runs V = T = float)
+template <typename V, typename T>
+static void vcycle(const lpm::AmgHierarchy &H, const Level0<T> &z0, const V *val, const double *r, double *z, int nu)
 {
     const int L = (int)H.levels.size();
     if (L == 0) {
-        dense(H, r, z, 3, 4);
+        dense<double, double>(H, r, z, 3, 4);
         return;
     }
-    std::vector<std::vector<double>> b(L), x(L), y(L);
-    for (int l = 1; l < L; l++) {
-        const size_t m = 6 * (size_t)H.levels[l].nblock;
-        b[l].assign(m, 0.0);
-        x[l].assign(m, 0.0);
-        y[l].assign(m, 0.0);
-    }
-    std::vector<double> cb(H.coarse_n), cx(H.coarse_n);
-    std::vector<std::vector<float>> P32(L), Pt32(L);
-    for (int l = 0; l < L; l++) {
-        P32[l] = f32(H.levels[l].P);
-        Pt32[l] = f32(H.levels[l].Pt);
-    }
+    const size_t n4 = 4 * (size_t)z0.n;
+    std::vector<T> bt(n4, T(0)), xa(n4, T(0)), qa(n4, T(0));
+    std::vector<std::vector<T>> b(L), x(L), y(L), P(L), Pt(L), A(L), D(L);
     for (int l = 0; l < L; l++) {
         const lpm::AmgLevel &v = H.levels[l];
-        double *bnext = (l + 1 < L) ? b[l + 1].data() : cb.data();
-        if (l == 0) {
-            double *it = tmp, *ot = z;
-            for (int i = 0; i < z0.n; i++)
-                lpm::jacobi0_row(z0.n, i, z0.mask[i], z0.Pinv, v.omega, r, it);
-            for (int s = 1; s < nu; s++) {
-                k0<V>(z0, val, lpm::SM_SMOOTH, v.omega, it, r, ot);
-                std::swap(it, ot);
-            }
-            k0<V>(z0, val, lpm::SM_RESID, v.omega, it, r, ot);
-            bsr<6, 3, lpm::BM_SET>(v.P.nbc, v.Pt, Pt32[l].data(), ot, 4, bnext, 6);
-        } else {
-            double *it = x[l].data(), *ot = y[l].data();
-            for (int i = 0; i < v.nblock; i++)
-                lpm::jacobi6_row(i, v.Dinv.data(), v.omega, b[l].data(), it);
-            for (int s = 1; s < nu; s++) {
-                bsr<6, 6, lpm::BM_SMOOTH>(v.nblock, v.A, v.A.val.data(), it, 6, ot, 6, b[l].data(), v.Dinv.data(),
-                                          v.omega);
-                std::swap(it, ot);
-            }
-            bsr<6, 6, lpm::BM_RESID>(v.nblock, v.A, v.A.val.data(), it, 6, ot, 6, b[l].data());
-            bsr<6, 6, lpm::BM_SET>(v.P.nbc, v.Pt, Pt32[l].data(), ot, 6, bnext, 6);
+        P[l] = conv<T>(v.P.val);
+        Pt[l] = conv<T>(v.Pt.val);
+        if (l > 0) {
+            const size_t m = 6 * (size_t)v.nblock;
+            b[l].assign(m, T(0));
+            x[l].assign(m, T(0));
+            y[l].assign(m, T(0));
+            A[l] = conv<T>(v.A.val);
+            D[l] = conv<T>(v.Dinv);
         }
     }
-    dense(H, cb.data(), cx.data(), 6, 6);
-    for (int l = L - 1; l >= 0; l--) {
+    std::vector<T> cb(H.coarse_n), cx(H.coarse_n);
+    for (int l = 0; l < L; l++) {
         const lpm::AmgLevel &v = H.levels[l];
-        const double *e = (l + 1 < L) ? y[l + 1].data() : cx.data();
+        const T om = (T)v.omega;
+        T *bnext = (l + 1 < L) ? b[l + 1].data() : cb.data();
         if (l == 0) {
-            double *it = (nu % 2 == 1) ? tmp : z, *ot = (nu % 2 == 1) ? z : tmp;
-            bsr<3, 6, lpm::BM_ADD>(v.nblock, v.P, P32[l].data(), e, 6, it, 4);
-            for (int s = 0; s < nu; s++) {
-                k0<V>(z0, val, lpm::SM_SMOOTH, v.omega, it, r, ot);
+            T *it = xa.data(), *ot = qa.data();
+            for (int i = 0; i < z0.n; i++)
+                lpm::jacobi0_row<T, T, double>(z0.n, i, z0.mask[i], z0.Pinv, om, r, bt.data(), it);
+            for (int s = 1; s < nu; s++) {
+                k0<V, T, T>(z0, val, lpm::SM_SMOOTH, om, it, bt.data(), ot);
                 std::swap(it, ot);
             }
+            k0<V, T, T>(z0, val, lpm::SM_RESID, om, it, bt.data(), ot);
+            bsr<6, 3, lpm::BM_SET, T>(v.P.nbc, v.Pt, Pt[l].data(), ot, 4, bnext, 6);
         } else {
-            double *it = (nu % 2 == 1) ? x[l].data() : y[l].data(), *ot = (nu % 2 == 1) ? y[l].data() : x[l].data();
-            bsr<6, 6, lpm::BM_ADD>(v.nblock, v.P, P32[l].data(), e, 6, it, 6);
+            T *it = x[l].data(), *ot = y[l].data();
+            for (int i = 0; i < v.nblock; i++)
+                lpm::jacobi6_row<T>(i, D[l].data(), om, b[l].data(), it);
+            for (int s = 1; s < nu; s++) {
+                bsr<6, 6, lpm::BM_SMOOTH, T>(v.nblock, v.A, A[l].data(), it, 6, ot, 6, b[l].data(), D[l].data(), om);
+                std::swap(it, ot);
+            }
+            bsr<6, 6, lpm::BM_RESID, T>(v.nblock, v.A, A[l].data(), it, 6, ot, 6, b[l].data());
+            bsr<6, 6, lpm::BM_SET, T>(v.P.nbc, v.Pt, Pt[l].data(), ot, 6, bnext, 6);
+        }
+    }
+    dense<T, T>(H, cb.data(), cx.data(), 6, 6);
+    for (int l = L - 1; l >= 0; l--) {
+        const lpm::AmgLevel &v = H.levels[l];
+        const T om = (T)v.omega;
+        const T *e = (l + 1 < L) ? y[l + 1].data() : cx.data();
+        if (l == 0) {
+            T *it = (nu % 2 == 1) ? xa.data() : qa.data(), *ot = (nu % 2 == 1) ? qa.data() : xa.data();
+            bsr<3, 6, lpm::BM_ADD, T>(v.nblock, v.P, P[l].data(), e, 6, it, 4);
             for (int s = 0; s < nu; s++) {
-                bsr<6, 6, lpm::BM_SMOOTH>(v.nblock, v.A, v.A.val.data(), it, 6, ot, 6, b[l].data(), v.Dinv.data(),
-                                          v.omega);
+                if (s == nu - 1) {
+                    k0<V, T, double>(z0, val, lpm::SM_SMOOTH, om, it, bt.data(), z);
+                } else {
+                    k0<V, T, T>(z0, val, lpm::SM_SMOOTH, om, it, bt.data(), ot);
+                    std::swap(it, ot);
+                }
+            }
+        } else {
+            T *it = (nu % 2 == 1) ? x[l].data() : y[l].data(), *ot = (nu % 2 == 1) ? y[l].data() : x[l].data();
+            bsr<6, 6, lpm::BM_ADD, T>(v.nblock, v.P, P[l].data(), e, 6, it, 6);
+            for (int s = 0; s < nu; s++) {
+                bsr<6, 6, lpm::BM_SMOOTH, T>(v.nblock, v.A, A[l].data(), it, 6, ot, 6, b[l].data(), D[l].data(), om);
                 std::swap(it, ot);
             }
         }
@@ -226,15 +238,16 @@ int main(int argc, char **argv)
                 for (int i = 0; i < n; i++)
                     for (int k = 0; k < 9; k++)
                         Pinv[(size_t)k * n + i] = H.levels[0].Dinv[(size_t)i * 9 + k];
-            const Level0 z0{n, mask.data(), rowoff.data(), npad.data(), cols.data(), Pinv.data()};
-            std::vector<double> z(4 * (size_t)n, 0.0), tmp(4 * (size_t)n, 0.0);
+            const Level0<double> z0{n, mask.data(), rowoff.data(), npad.data(), cols.data(), Pinv.data()};
+            std::vector<double> z(4 * (size_t)n, 0.0);
             const int nu = argc > 3 ? std::atoi(argv[3]) : 1;
-            vcycle<double>(H, z0, val.data(), r.data(), z.data(), tmp.data(), nu);
+            vcycle<double, double>(H, z0, val.data(), r.data(), z.data(), nu);
             wr(d + "/z.bin", z);
-            std::vector<float> vf(val.begin(), val.end());
+            // as the device runs it: everything in FP32
+            std::vector<float> vf(val.begin(), val.end()), Pf(Pinv.begin(), Pinv.end());
+            const Level0<float> z0f{n, mask.data(), rowoff.data(), npad.data(), cols.data(), Pf.data()};
             std::fill(z.begin(), z.end(), 0.0);
-            std::fill(tmp.begin(), tmp.end(), 0.0);
-            vcycle<float>(H, z0, vf.data(), r.data(), z.data(), tmp.data(), nu);
+            vcycle<float, float>(H, z0f, vf.data(), r.data(), z.data(), nu);
             wr(d + "/z32.bin", z);
         }
     }

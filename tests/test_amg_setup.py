@@ -187,7 +187,8 @@ def test_hierarchy_preconditions_cg(oracle_mod, harness, tmp_path, lattice, size
     z64 = np.fromfile(os.path.join(d, "z.bin")).reshape(n, 4)
     z32 = np.fromfile(os.path.join(d, "z32.bin")).reshape(n, 4)
     assert np.all(z64[:, 3] == 0.0) and np.all(z64[:, :3].ravel()[~free] == 0.0)
-    # (the device keeps P and P^T in FP32: agreement to FP32 rounding)
+    # (z32: the whole cycle in FP32 as the device runs it; agreement to FP32
+    # rounding)
     assert np.abs(z64[:, :3].ravel() - z).max() <= 1e-5 * np.abs(z).max()
     assert np.abs(z32[:, :3].ravel() - z).max() <= 1e-4 * np.abs(z).max()
     x, it = _pcg(A0, M, b)

@@ -33,8 +33,8 @@ def _worker(rank, world, port, q):
         size, warmup, steps = 10, 3, 1
     # the reference arm prints on rank 0 only; skip its (slow) CPU sample here
     orig = bench.run_cpu_baseline
-    bench.run_cpu_baseline = lambda args, case, counts: {"value": 1.0, "unit": "load steps/s", "cores": 1,
-                                                         "kind": "port", "sample": "stub"}
+    bench.run_cpu_baseline = lambda case, W, K: {"value": 1.0, "unit": "load steps/s", "cores": 1,
+                                                 "kind": "port", "sample": "stub"}
     with redirect_stdout(buf):
         bench.run_reference(A)
     bench.run_cpu_baseline = orig
