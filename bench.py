@@ -411,9 +411,12 @@ def gpu_launches(stats, amg=0):
     2 + the V-cycle."""
     per_it = 3 if not amg else 4 + 5 * amg + 1
     per_rel = 3 if not amg else 2 + 5 * amg + 1
+    # multigrid, per step: the FP16 smoother copy (max, conversion), the FP64
+    # copy for the true residual and the row sums of the difference form
+    per_step = 8 if not amg else 12
     total = 0
     for st in stats:
-        total += 8 + 4 * st["newton_iters"] + per_it * st["cg_iters"] + per_rel * st["refine_iters"] + \
+        total += per_step + 4 * st["newton_iters"] + per_it * st["cg_iters"] + per_rel * st["refine_iters"] + \
             st["newton_iters"]
     return total
 

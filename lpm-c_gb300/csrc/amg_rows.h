@@ -54,6 +54,20 @@ AMG_HD void load4(const double *p, double (&v)[4])
 #endif
 }
 
+#ifdef __CUDACC__
+// four FP16 values (the smoother's stiffness copy), one 8-byte load; as float
+__device__ __forceinline__ void load4(const __half *p, float (&v)[4])
+{
+    const uint2 t = __ldcs(reinterpret_cast<const uint2 *>(p));
+    const float2 a = __half22float2(*reinterpret_cast<const __half2 *>(&t.x));
+    const float2 b = __half22float2(*reinterpret_cast<const __half2 *>(&t.y));
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = b.x;
+    v[3] = b.y;
+}
+#endif
+
 // x, y, z of a level-0 vector entry (4 values per particle): one 16-byte
 // load for FP32 on the device
 template <typename T>
@@ -103,22 +117,23 @@ AMG_HD void store_xyz(double *p, T a, T b, T c)
 
 // Level 0: partial product of block row `row` of the stiffness (device
 // layout: npad[row] blocks at rowoff[row], npad a multiple of 4,
-// component-major values) over the groups of 4 consecutive blocks
-// b0 = 4 sub, 4 (sub + nl), ...; products in V.
-template <typename V, typename X>
+// component-major values of type V) over the groups of 4 consecutive blocks
+// b0 = 4 sub, 4 (sub + nl), ...; products in A (the device stores the
+// smoother's stiffness in FP16, scaled, and multiplies in FP32).
+template <typename V, typename X, typename A = V>
 AMG_HD void k0_row_partial(const long long *rowoff, const int *npad, const int *cols, const V *val,
-                           const X *x, int row, int sub, int nl, V &y0, V &y1, V &y2)
+                           const X *x, int row, int sub, int nl, A &y0, A &y1, A &y2)
 {
     const long long off = rowoff[row];
     const int np = npad[row];
     const V *vr = val + 9 * off;
     for (int b0 = 4 * sub; b0 < np; b0 += 4 * nl) {
-        V v[9][4];
+        A v[9][4];
         for (int k = 0; k < 9; k++)
             load4(vr + (size_t)k * np + b0, v[k]);
         for (int j = 0; j < 4; j++) {
-            V x0, x1, x2;
-            load_xyz<V>(x + 4 * (size_t)cols[off + b0 + j], x0, x1, x2);
+            A x0, x1, x2;
+            load_xyz<A>(x + 4 * (size_t)cols[off + b0 + j], x0, x1, x2);
             y0 += v[0][j] * x0 + v[1][j] * x1 + v[2][j] * x2;
             y1 += v[3][j] * x0 + v[4][j] * x1 + v[5][j] * x2;
             y2 += v[6][j] * x0 + v[7][j] * x1 + v[8][j] * x2;

@@ -31,6 +31,7 @@
 #include <chrono>
 #include <cmath>
 #include <omp.h>
+#include <cuda_fp16.h>
 #include "amg.h"
 #include "amg_rows.h"
 #include "lpm_internal.h"
@@ -250,26 +251,32 @@ constexpr int L0_LANES = 16;  // lanes per block row of the stiffness
 
 // MODE SM_SMOOTH: out = x + omega Pinv mask(b - K x); SM_RESID: out = mask(b - K x).
 // Half a warp per block row, lanes over the row's blocks (padding included:
-// zero values, column of the row itself); FP32 values, vectors and
-// arithmetic (amg_rows.h).  O: float (an iterate of the cycle) or double
-// (its last sweep, the PCG's z).
+// zero values, column of the row itself).  The stiffness is the FP16 copy
+// Kh = Kf / s (s in *kscale): products and sums in FP32, the row sums
+// multiplied by s.  FP32 vectors and arithmetic otherwise (amg_rows.h).  O:
+// float (an iterate of the cycle) or double (its last sweep, the PCG's z).
+// The smoother's operator is only the preconditioner's: rounded to FP16 (or
+// even to 8 significand bits) it leaves the PCG iteration counts of the numpy
+// checks unchanged.
 template <int MODE, typename O>
 __global__ void __launch_bounds__(ATPB) k_amg_k0(int n, const long long *__restrict__ rowoff,
                                                  const int *__restrict__ npad, const int *__restrict__ cols,
-                                                 const uint8_t *__restrict__ mask, const float *__restrict__ val,
-                                                 const float *__restrict__ Pinv, float omega,
-                                                 const float *__restrict__ x, const float *__restrict__ b,
-                                                 O *__restrict__ out, const CgScalars *sc)
+                                                 const uint8_t *__restrict__ mask, const __half *__restrict__ val,
+                                                 const float *__restrict__ kscale, const float *__restrict__ Pinv,
+                                                 float omega, const float *__restrict__ x,
+                                                 const float *__restrict__ b, O *__restrict__ out,
+                                                 const CgScalars *sc)
 {
     if (sc && sc->done)
         return;
+    const float s = *kscale;
     const int sub = threadIdx.x & (L0_LANES - 1);
     const unsigned gmask = 0xffffu << ((threadIdx.x & 31) & ~(L0_LANES - 1));
     const int g = (blockIdx.x * blockDim.x + threadIdx.x) / L0_LANES;
     const int ng = (gridDim.x * blockDim.x) / L0_LANES;
     for (int row = g; row < n; row += ng) {
         float y0 = 0.f, y1 = 0.f, y2 = 0.f;
-        k0_row_partial<float, float>(rowoff, npad, cols, val, x, row, sub, L0_LANES, y0, y1, y2);
+        k0_row_partial<__half, float, float>(rowoff, npad, cols, val, x, row, sub, L0_LANES, y0, y1, y2);
 #pragma unroll
         for (int o = L0_LANES / 2; o > 0; o >>= 1) {
             y0 += __shfl_xor_sync(gmask, y0, o);
@@ -277,7 +284,7 @@ __global__ void __launch_bounds__(ATPB) k_amg_k0(int n, const long long *__restr
             y2 += __shfl_xor_sync(gmask, y2, o);
         }
         if (sub == 0)
-            k0_epilogue<float, float, O>(MODE, n, row, mask[row], Pinv, omega, x, b, out, y0, y1, y2);
+            k0_epilogue<float, float, O>(MODE, n, row, mask[row], Pinv, omega, x, b, out, s * y0, s * y1, s * y2);
     }
 }
 
@@ -379,12 +386,13 @@ static void k0_launch(Ctx &c, int mode, float omega, const float4 *xv, const flo
 {
     const int g = grid_for(c, (long long)c.n * L0_LANES);
     const float *x = (const float *)xv, *b = (const float *)bv;
+    const __half *kh = reinterpret_cast<const __half *>(c.Kh);
     if (mode == SM_SMOOTH)
-        k_amg_k0<SM_SMOOTH, O><<<g, ATPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.mask, c.Kf, c.Pinv_f,
-                                                          omega, x, b, out, c.sc);
+        k_amg_k0<SM_SMOOTH, O><<<g, ATPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.mask, kh, c.kh_scale,
+                                                          c.Pinv_f, omega, x, b, out, c.sc);
     else
-        k_amg_k0<SM_RESID, O><<<g, ATPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.mask, c.Kf, c.Pinv_f,
-                                                         omega, x, b, out, c.sc);
+        k_amg_k0<SM_RESID, O><<<g, ATPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.mask, kh, c.kh_scale,
+                                                         c.Pinv_f, omega, x, b, out, c.sc);
 }
 
 __global__ void k_to_float(long long count, const double *__restrict__ in, float *__restrict__ out)
@@ -398,6 +406,56 @@ void launch_amg_stiffness32(Ctx &c)
 {
     const long long count = 9 * c.nblk;
     k_to_float<<<grid_for(c, count), ATPB, 0, c.stream>>>(count, c.Kd, c.Kf);
+}
+
+__global__ void k_to_double(long long count, const float *__restrict__ in, double *__restrict__ out)
+{
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < count;
+         k += (long long)gridDim.x * blockDim.x)
+        out[k] = (double)in[k];
+}
+
+void launch_stiffness64_of32(Ctx &c)
+{
+    const long long count = 9 * c.nblk;
+    k_to_double<<<grid_for(c, count), ATPB, 0, c.stream>>>(count, c.Kf, c.Kd);
+}
+
+// max |v| as the bits of a non-negative float (which order like unsigned ints)
+__global__ void __launch_bounds__(ATPB) k_absmax(long long count, const float *__restrict__ v, unsigned *out)
+{
+    float m = 0.f;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < count;
+         k += (long long)gridDim.x * blockDim.x)
+        m = fmaxf(m, fabsf(v[k]));
+    for (int o = 16; o > 0; o >>= 1)
+        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0)
+        atomicMax(out, __float_as_uint(m));
+}
+
+// Kh = half(Kf / s) with s = max |Kf| / 2^14 (the largest value maps to 16384,
+// well inside FP16's range; values below 2^-24 of the largest underflow)
+__global__ void k_to_half(long long count, const float *__restrict__ in, __half *__restrict__ out,
+                          const unsigned *__restrict__ maxbits, float *__restrict__ scale)
+{
+    const float mx = __uint_as_float(*maxbits);
+    const float s = mx > 0.f ? mx * (1.0f / 16384.0f) : 1.0f;
+    const float inv = 1.0f / s;
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        *scale = s;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < count;
+         k += (long long)gridDim.x * blockDim.x)
+        out[k] = __float2half_rn(in[k] * inv);
+}
+
+void launch_amg_stiffness16(Ctx &c)
+{
+    const long long count = 9 * c.nblk;
+    cudaMemsetAsync(c.kh_max, 0, sizeof(unsigned), c.stream);
+    k_absmax<<<grid_for(c, count), ATPB, 0, c.stream>>>(count, c.Kf, c.kh_max);
+    k_to_half<<<grid_for(c, count), ATPB, 0, c.stream>>>(count, c.Kf, reinterpret_cast<__half *>(c.Kh), c.kh_max,
+                                                         c.kh_scale);
 }
 
 template <int R, int C, int MODE>

@@ -406,11 +406,22 @@ __global__ void __launch_bounds__(VTPB) k_spmv_diff(SpmvArgs a, const float *__r
     }
 }
 
+// two consecutive stiffness values of one component as FP64 (streaming)
+__device__ __forceinline__ double2 ld_pair(const float *p)
+{
+    const float2 v = __ldcs(reinterpret_cast<const float2 *>(p));
+    return make_double2((double)v.x, (double)v.y);
+}
+__device__ __forceinline__ double2 ld_pair(const double *p) { return __ldcs(reinterpret_cast<const double2 *>(p)); }
+
 // Refinement residual r = b - K32 x64 with FP64 products and sums (masked),
-// and |r|^2 into norms[slot].  BATCH: only the rows of specimens due for a
-// reliable update (running with a request, or recursively converged).
-template <bool BATCH = false>
-__global__ void __launch_bounds__(VTPB) k_refine_res(SpmvArgs a, const float *__restrict__ val,
+// and |r|^2 into norms[slot].  The values are the FP32 stiffness (V = float,
+// converted per value) or its exact FP64 copy (V = double: the same
+// arithmetic and result without a conversion per value on the FP64 pipe).
+// BATCH: only the rows of specimens due for a reliable update (running with a
+// request, or recursively converged).
+template <bool BATCH = false, typename V = float>
+__global__ void __launch_bounds__(VTPB) k_refine_res(SpmvArgs a, const V *__restrict__ val,
                                                      const dvec4 *__restrict__ x,
                                                      const dvec4 *__restrict__ bvec,
                                                      dvec4 *__restrict__ r, double *norms, int slot,
@@ -429,21 +440,21 @@ __global__ void __launch_bounds__(VTPB) k_refine_res(SpmvArgs a, const float *__
         }
         const long long off = a.rowoff[row];
         const int np = a.npad[row];
-        const float *vr = val + 9 * off;
+        const V *vr = val + 9 * off;
         double y0 = 0.0, y1 = 0.0, y2 = 0.0;
         for (int b0 = 2 * lane; b0 < np; b0 += 64) {
             const int2 c2 = __ldg(reinterpret_cast<const int2 *>(a.cols + off + b0));
-            float2 v[9];
+            double2 v[9];
 #pragma unroll
             for (int k = 0; k < 9; k++)
-                v[k] = __ldcs(reinterpret_cast<const float2 *>(vr + (size_t)k * np + b0));
+                v[k] = ld_pair(vr + (size_t)k * np + b0);
             const dvec4 xa = x[c2.x], xb = x[c2.y];
-            y0 += (double)v[0].x * xa.x + (double)v[1].x * xa.y + (double)v[2].x * xa.z;
-            y1 += (double)v[3].x * xa.x + (double)v[4].x * xa.y + (double)v[5].x * xa.z;
-            y2 += (double)v[6].x * xa.x + (double)v[7].x * xa.y + (double)v[8].x * xa.z;
-            y0 += (double)v[0].y * xb.x + (double)v[1].y * xb.y + (double)v[2].y * xb.z;
-            y1 += (double)v[3].y * xb.x + (double)v[4].y * xb.y + (double)v[5].y * xb.z;
-            y2 += (double)v[6].y * xb.x + (double)v[7].y * xb.y + (double)v[8].y * xb.z;
+            y0 += v[0].x * xa.x + v[1].x * xa.y + v[2].x * xa.z;
+            y1 += v[3].x * xa.x + v[4].x * xa.y + v[5].x * xa.z;
+            y2 += v[6].x * xa.x + v[7].x * xa.y + v[8].x * xa.z;
+            y0 += v[0].y * xb.x + v[1].y * xb.y + v[2].y * xb.z;
+            y1 += v[3].y * xb.x + v[4].y * xb.y + v[5].y * xb.z;
+            y2 += v[6].y * xb.x + v[7].y * xb.y + v[8].y * xb.z;
         }
         y0 = warp_sum(y0);
         y1 = warp_sum(y1);
@@ -813,7 +824,12 @@ void launch_spmv_batch(Ctx &c, const dvec4 *x, dvec4 *y, bool k32)
 
 void launch_refine_residual(Ctx &c, const dvec4 *x, const dvec4 *b, dvec4 *r, double bscale)
 {
-    k_refine_res<<<red_grid(c), VTPB, 0, c.stream>>>(spmv_args(c), c.Kf, x, b, r, c.norms, 2, bscale);
+    if (c.kd_from_kf >= 0 && c.kd_from_kf == c.kf_version)
+        k_refine_res<false, double><<<red_grid(c), VTPB, 0, c.stream>>>(spmv_args(c), c.Kd, x, b, r, c.norms, 2,
+                                                                        bscale);
+    else
+        k_refine_res<false, float><<<red_grid(c), VTPB, 0, c.stream>>>(spmv_args(c), c.Kf, x, b, r, c.norms, 2,
+                                                                       bscale);
 }
 
 void launch_refine_batch(Ctx &c, const dvec4 *x, const dvec4 *b, dvec4 *r)
@@ -822,7 +838,7 @@ void launch_refine_batch(Ctx &c, const dvec4 *x, const dvec4 *b, dvec4 *r)
     a.row_spec = c.bcg.spec_of;
     a.spec_done = c.bcg.done;
     a.spec_upd = c.bcg.upd;
-    k_refine_res<true><<<red_grid(c), VTPB, 0, c.stream>>>(a, c.Kf, x, b, r, c.norms, 3, 1.0);
+    k_refine_res<true, float><<<red_grid(c), VTPB, 0, c.stream>>>(a, c.Kf, x, b, r, c.norms, 3, 1.0);
 }
 
 // mixed precision with FP64 CG vectors: FP32 stiffness, FP32 products and row

@@ -154,7 +154,7 @@ Ctx::~Ctx()
                     (void **)&rowoff, (void **)&npad, (void **)&cols, (void **)&Kd, (void **)&Kf,
                     (void **)&Pinv_d, (void **)&Pinv_f, (void **)&x_d, (void **)&r_d, (void **)&p_d,
                     (void **)&q_d, (void **)&z_d, (void **)&x_f, (void **)&r_f, (void **)&p_f, (void **)&q_f,
-                    (void **)&z_f, (void **)&p_hi, (void **)&p_lo, (void **)&Krs, (void **)&pl_flag, (void **)&b_d, (void **)&sc, (void **)&partials, (void **)&counter,
+                    (void **)&z_f, (void **)&p_hi, (void **)&p_lo, (void **)&Krs, (void **)&Kh, (void **)&kh_scale, (void **)&kh_max, (void **)&pl_flag, (void **)&b_d, (void **)&sc, (void **)&partials, (void **)&counter,
                     (void **)&norms, (void **)&status};
     for (void **p : all)
         if (*p) {
@@ -311,7 +311,7 @@ static int alloc_specimen(Ctx &c)
     A_(c.W, 6 * n) A_(c.Pinv_d, 9 * n) A_(c.Pinv_f, 9 * n)
     A_(c.x_d, n) A_(c.r_d, n) A_(c.p_d, n) A_(c.q_d, n) A_(c.z_d, n) A_(c.b_d, n)
     A_(c.x_f, n) A_(c.r_f, n) A_(c.p_f, n) A_(c.q_f, n) A_(c.z_f, n)
-    A_(c.p_hi, n) A_(c.p_lo, n) A_(c.Krs, 9 * n)
+    A_(c.p_hi, n) A_(c.p_lo, n) A_(c.Krs, 9 * n) A_(c.kh_scale, 1) A_(c.kh_max, 1)
     c.krs_version = -1;
     for (int s = 0; s < 3; s++) {
         A_(c.dLp[s], nb) A_(c.alpha[s], n) A_(c.beta[s], 6 * n)
@@ -401,12 +401,17 @@ static int setup_common(Ctx &c, bool built = false)
     drop_graphs(c);
     dfree(c.Kf);
     dfree(c.Kd);
-    c.kf_cap = c.kd_cap = 0;
+    dfree(c.Kh);
+    c.kf_cap = c.kd_cap = c.kh_cap = 0;
     c.kf_version = -1;
+    c.kh_version = -1;
+    c.kd_from_kf = -1;
     c.vec64_fallback = false;
     HostSetup &h = c.hs;
     if (!built) {
-        build_neighbors(h);
+        const int brc = build_neighbors(h);
+        if (brc < 0)
+            return brc;
         build_afem(h);
         build_bond_tables(h);
         build_block_pattern(h);
@@ -864,6 +869,29 @@ static int solve_amg(Ctx &c, const dvec4 *b, double bn, lpm_step_stats *st)
         launch_row_sums(c);  // for the difference-form product
         c.krs_version = c.kf_version;
     }
+    if (c.kh_version != c.kf_version) {
+        // the level-0 smoother's FP16 stiffness
+        if (!c.Kh || c.kh_cap != c.nblk) {
+            drop_graphs(c);
+            if ((rc = dalloc(c.Kh, 9 * (size_t)c.nblk)))
+                return rc;
+            c.kh_cap = c.nblk;
+        }
+        launch_amg_stiffness16(c);
+        c.kh_version = c.kf_version;
+    }
+    if (k32 && c.kd_from_kf != c.kf_version) {
+        // the reliable updates' true residual reads an exact FP64 copy of
+        // the FP32 stiffness (FP64 products without per-value conversions)
+        if (!c.Kd || c.kd_cap != c.nblk) {
+            drop_graphs(c);
+            if ((rc = dalloc(c.Kd, 9 * (size_t)c.nblk)))
+                return rc;
+            c.kd_cap = c.nblk;
+        }
+        launch_stiffness64_of32(c);
+        c.kd_from_kf = c.kf_version;
+    }
     launch_amg_init(c, b, scale, k32 ? delta * delta : 0.0, k32);
     int sweeps = 0, it = 0, done = 0;
     double rel = 1.0;
@@ -1043,6 +1071,8 @@ int assemble(Ctx &c)
             return rc;
         c.kd_cap = c.nblk;
     }
+    if (!fp32)
+        c.kd_from_kf = -1;  // Kd is assembled in FP64 now
     launch_tangent_geometry(c);
     launch_assemble(c, fp32);
     c.k_version++;

@@ -94,7 +94,7 @@ struct HostSetup {
 
 int build_lattice(HostSetup &h, int lattice, double radius, const double *box);
 int build_particles(HostSetup &h, int lattice, double radius, int n, const double *xyz);
-void build_neighbors(HostSetup &h);
+int build_neighbors(HostSetup &h);  // LPM_OK, or LPM_ERR_ARG when a particle has too many bonds
 void build_afem(HostSetup &h);
 void build_bond_tables(HostSetup &h);
 void build_block_pattern(HostSetup &h);
@@ -270,6 +270,15 @@ struct Ctx {
     float4 *p_hi = nullptr, *p_lo = nullptr;
     float *Krs = nullptr;
     long long krs_version = -1;
+    // multigrid: FP16 copy of Kf scaled by 1 / kh_scale[0] (device) for the
+    // level-0 smoother, of the assembly numbered kh_version
+    unsigned short *Kh = nullptr;
+    float *kh_scale = nullptr;
+    unsigned *kh_max = nullptr;
+    long long kh_cap = 0, kh_version = -1;
+    // mixed multigrid: Kd holds the exact FP64 copy of Kf of this assembly
+    // (-1: none), read by the reliable updates' true residual
+    long long kd_from_kf = -1;
     dvec4 *b_d = nullptr;
     CgScalars *sc = nullptr;     // device
     CgScalars *sc_host = nullptr; // pinned mirror
@@ -376,6 +385,8 @@ void launch_amg_iter(Ctx &c, bool k32);
 void launch_amg_reliable(Ctx &c, const dvec4 *rtrue);  // r = rtrue (masked), z, rz; p kept
 void launch_amg_vcycle(Ctx &c, const dvec4 *r, dvec4 *z);  // z = V(r), FP32 inside (Kf, Pinv_f, x_f/q_f/r_f)
 void launch_amg_stiffness32(Ctx &c);  // Kf = (float) Kd, for the smoother under FP64 precision
+void launch_amg_stiffness16(Ctx &c);  // Kh = half(Kf / s), s = max |Kf| / 2^14 into kh_scale
+void launch_stiffness64_of32(Ctx &c); // Kd = (double) Kf, exactly
 int amg_prepare(Ctx &c);  // (re)build the hierarchy when missing, stale or the mask changed
 void free_amg(Ctx &c);
 // solver (k_solve.cu)

@@ -103,7 +103,10 @@ int build_particles(HostSetup &h, int lattice, double radius, int n, const doubl
 // searchNormalNeighbor (src/neighbor.c:9-46).  A uniform cell grid replaces
 // the all-pairs loop; every candidate is tested with the reference's
 // distance expression and cut-offs, and bonds are kept in ascending j.
-void build_neighbors(HostSetup &h)
+// A particle with more bonds than the LPM_NN slots (the reference writes past
+// the end of its row then) fails the setup: returns LPM_ERR_ARG with the
+// particle named in the error, LPM_OK otherwise.
+int build_neighbors(HostSetup &h)
 {
     const int n = h.n;
     const double c1 = 1.01 * h.cut1, c2 = 1.01 * h.cut2;
@@ -143,11 +146,13 @@ void build_neighbors(HostSetup &h)
     h.L0.resize((size_t)n * LPM_NN);
     h.cs0.resize((size_t)n * LPM_NN * 3);
     const double *X = h.xyz.data();
-#pragma omp parallel for schedule(dynamic, 512)
+    constexpr int MAXCAND = 96;
+    int over = n;  // lowest particle with too many bonds
+#pragma omp parallel for schedule(dynamic, 512) reduction(min : over)
     for (int i = 0; i < n; i++) {
-        int cand[96];
-        double cd[96];
-        int nc = 0;
+        int cand[MAXCAND];
+        double cd[MAXCAND];
+        int nc = 0, found = 0;
         const int ci = cell[i];
         const int cx = ci % g[0], cy = (ci / g[0]) % g[1], cz = ci / (g[0] * g[1]);
         for (int dz = -1; dz <= 1; dz++)
@@ -162,10 +167,13 @@ void build_neighbors(HostSetup &h)
                         const double ex = X[3 * j] - X[3 * i], ey = X[3 * j + 1] - X[3 * i + 1],
                                      ez = X[3 * j + 2] - X[3 * i + 2];
                         const double dis = std::sqrt(ex * ex + ey * ey + ez * ez);
-                        if ((((dis < c1) && (j != i)) || ((dis > c1) && (dis < c2))) && nc < 96) {
-                            cand[nc] = j;
-                            cd[nc] = dis;
-                            nc++;
+                        if (((dis < c1) && (j != i)) || ((dis > c1) && (dis < c2))) {
+                            found++;
+                            if (nc < MAXCAND) {
+                                cand[nc] = j;
+                                cd[nc] = dis;
+                                nc++;
+                            }
                         }
                     }
                 }
@@ -182,6 +190,8 @@ void build_neighbors(HostSetup &h)
             cand[b + 1] = v;
             cd[b + 1] = dv;
         }
+        if (found > LPM_NN)
+            over = std::min(over, i);
         const int m = std::min(nc, LPM_NN);
         for (int q = 0; q < m; q++) {
             const int j = cand[q];
@@ -203,6 +213,11 @@ void build_neighbors(HostSetup &h)
         }
         h.nb[i] = m;
     }
+    if (over < n)
+        return fail(LPM_ERR_ARG, "setup: particle " + std::to_string(over) + " has more than " +
+                                     std::to_string(LPM_NN) + " bonds within the cut-offs (searchNormalNeighbor "
+                                     "keeps at most nneighbors per particle)");
+    return LPM_OK;
 }
 
 // searchAFEMNeighbor (src/neighbor.c:49-141): conn[i] = sorted unique union,
@@ -413,7 +428,11 @@ int build_batch(HostSetup &dst, int lattice, double radius, int nspec, const dou
             errs[s] = "specimen " + std::to_string(s) + " holds no particle";
             return;
         }
-        build_neighbors(parts[s]);
+        if ((rc = build_neighbors(parts[s])) < 0) {
+            rcs[s] = rc;
+            errs[s] = g_err;
+            return;
+        }
         build_afem(parts[s]);
         build_bond_tables(parts[s]);
         build_block_pattern(parts[s]);

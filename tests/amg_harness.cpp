@@ -5,7 +5,9 @@
 // V-cycle to it: the launch sequence of launch_amg_vcycle (k_amg.cu), each
 // kernel's rows computed one after another by the same per-row functions
 // (amg_rows.h), all in FP64 (z.bin) and all in FP32 as the device runs it
-// (z32.bin).
+// (z32.bin; the device keeps the level-0 smoother's stiffness as scaled FP16
+// values and multiplies them in FP32, which changes the values, not the index
+// arithmetic this emulation checks).
 //   amg_harness DIR AGG_SPACING [SWEEPS]
 #include <algorithm>
 #include <chrono>

@@ -99,3 +99,39 @@ def test_batch_offsets_and_sizes(gpu_lib):
         valid = blk[blk >= 0]
         assert valid.min() >= off[k] and valid.max() < off[k + 1]
     s.close()
+
+
+@pytest.mark.gpu_last
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batch_specimens_match_oracle(oracle_mod, gpu_lib, precision):
+    """Three specimens of a batch (the smallest, a middle one and the
+    largest) against the oracle, the CPU restatement pinned to the reference:
+    6 tension steps into the plastic range, both sides converged to 1e-10,
+    displacements and plastic strain within 1e-8."""
+    G = gpu_lib
+    case = small_case(1e-10)
+    nsteps = 6
+    off, hist, stats, alpha = run_batch(G, case, nsteps, precision=precision)
+    sizes = np.diff(off)
+    picks = sorted({int(np.argmin(sizes)), int(np.argsort(sizes)[len(sizes) // 2]), int(np.argmax(sizes))})
+    oracle_mod.set_threads(4)
+    for k in picks:
+        o = oracle_mod.Oracle()
+        n = o.setup_lattice(case.lattice, case.radius, case.boxes[k])
+        assert n == sizes[k]
+        types = cases.sc_types(o.d("xyz", (n, 3)), o.i("nb", (n,)), case.radius)
+        c11, c12, c44 = cases.iso_cubic(case.E[k], case.nu)
+        o.set_types(types)
+        o.set_material(np.full(n, c11), np.full(n, c12), np.full(n, c44), np.full(n, case.sigmay[k]), case.H,
+                       0.0, 0)
+        o.init_state()
+        x0 = o.d("xyz_initial", (n, 3))
+        sl = slice(off[k], off[k + 1])
+        for j in range(nsteps):
+            so = o.load_step(case.step_bcs()[k], [], 1e-10, 300, 1e-20, 0.0)
+            du_o = o.d("xyz", (n, 3)) - x0
+            err = np.abs(hist[j][sl] - du_o).max() / np.abs(du_o).max()
+            assert err < DISP_RTOL, (k, j + 1, err, so)
+        a_o = o.d("alpha1", (n,))
+        assert np.abs(alpha[sl] - a_o).max() <= DISP_RTOL * max(a_o.max(), 1e-30), k
+    assert alpha.max() > 0.0

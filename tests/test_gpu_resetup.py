@@ -36,3 +36,22 @@ def test_resetup_matches_fresh_context(gpu_lib):
         assert np.array_equal(reused.get("xyz"), fresh.get("xyz"))
     reused.close()
     fresh.close()
+
+
+def test_overfull_neighbourhood_is_an_error(gpu_lib):
+    """A particle with more bonds than the 18 slots fails the setup with
+    LPM_ERR_ARG naming it (the reference writes past its row then), instead of
+    silently dropping bonds; the context stays usable."""
+    G = gpu_lib
+    case = cases.SCCase(n=5)
+    s = G.Specimen(0)
+    n = s.setup_lattice(case.lattice, case.radius, case.box)
+    xyz = s.get("xyz")
+    # a particle at the centre of an interior cell: within the first cut-off
+    # of its 8 corners, which then hold 19 bonds
+    lo = xyz.min(axis=0)
+    centre = lo + 2.0 * case.radius * np.array([1.5, 1.5, 1.5])
+    with pytest.raises(G.LPMError, match="more than 18 bonds"):
+        s.setup_particles(case.lattice, case.radius, np.vstack([xyz, centre]))
+    assert s.setup_particles(case.lattice, case.radius, xyz) == n
+    s.close()
