@@ -278,7 +278,8 @@ def run_ours(args):
     timer.daemon = True
     timer.start()
 
-    partial["mixed"] = run_arm(G, case, G.PREC_MIXED, precond, W, K, stream, deadline, sync,
+    head_prec = G.PREC_FP64 if args.arm_precision == "fp64" else G.PREC_MIXED
+    partial["mixed"] = run_arm(G, case, head_prec, precond, W, K, stream, deadline, sync,
                                autotune=not args.no_autotune)
     mixed = partial["mixed"]
     mixed_s = mixed["ms"] / 1e3 if "ms" in mixed else None
@@ -751,9 +752,10 @@ def run_fcc(args):
         s.init_state()
         # FP64 CG vectors with the FP32 stiffness: at 80^3 cells the FCC system
         # is too ill-conditioned for FP32 vectors (their PCG stagnates)
+        amg = args.precond == "amg"
         s.set_solver(precision=prec, newton_tol=case.newton_tol, newton_maxiter=300, cg_rtol=1e-10,
-                     cg_maxiter=40000, mixed_vectors=64,
-                     preconditioner=G.PRECOND_AMG if args.precond == "amg" else G.PRECOND_BJ)
+                     cg_maxiter=2000 if amg else 40000, mixed_vectors=64,
+                     preconditioner=G.PRECOND_AMG if amg else G.PRECOND_BJ)
         setup_s = time.perf_counter() - t0
         for k in range(W):
             s.load_step(cases.sc_bcs(case.schedule[k]))
@@ -823,6 +825,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=100)
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--arm-precision", default="mixed", choices=["mixed", "fp64"],
+                    help="precision of the first (headline) arm; fp64 with --no-fp64 profiles the comparator "
+                         "alone")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
@@ -830,8 +835,8 @@ def main():
                     help="sc: the 1M-particle SC cyclic case (default); batch: 256 specimens; "
                          "adjoint: gradients on the notched plate; fcc: crystal plasticity")
     ap.add_argument("--fcc-cells", type=int, default=80)
-    ap.add_argument("--fcc-warmup", type=int, default=1,
-                    help="warm-up load steps of the fcc workload (its steps are long)")
+    ap.add_argument("--fcc-warmup", type=int, default=3,
+                    help="warm-up load steps of the fcc workload")
     ap.add_argument("--adj-strain", type=float, default=0.01)
     ap.add_argument("--nspec", type=int, default=256)
     ap.add_argument("--plate-n", type=int, default=200)
