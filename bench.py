@@ -145,9 +145,14 @@ def solver_opts(G, case, precision, precond):
     """Newton tolerance 1e-8 and the reference's MAXITER of 100
     (include/lpm.h:39), linear solves to 1e-10 relative.  The multigrid PCG
     needs about 40 iterations per solve: its cap of 2000 bounds the time a
-    misbehaving solve can take."""
+    misbehaving solve can take.  Each Newton solve of a step starts from the
+    Galerkin combination of the step's last 8 solutions (recycle), in both
+    precisions."""
     return dict(precision=precision, newton_tol=case.newton_tol, newton_maxiter=100, cg_rtol=1e-10,
-                cg_maxiter=2000 if precond else 200000, preconditioner=precond)
+                cg_maxiter=2000 if precond else 200000, preconditioner=precond, recycle=RECYCLE)
+
+
+RECYCLE = 8  # earlier solutions of the load step the Newton solves start from
 
 
 class Deadline:
@@ -342,7 +347,8 @@ def assemble_line(args, case, partial, world, note=None):
            "particles": mixed.get("n"), "nnz_blocks": mixed.get("nnzb"), "precision": "mixed",
            "preconditioner": precond_name,
            "newton": "modified Newton with the elastic tangent of the step (src/lpmc_project.c:382-471), "
-                     "tolerance 1e-8, MAXITER 100; linear solves to 1e-10 relative",
+                     "tolerance 1e-8, MAXITER 100; linear solves to 1e-10 relative, each started from the "
+                     f"Galerkin combination of the step's last {RECYCLE} solutions (both precisions)",
            "fp64_steps_per_s": fp64_rate, "mixed_over_fp64": (value / fp64_rate) if (value and fp64_rate) else None,
            **errs,
            "fp64_arm": {k: v for k, v in f64.items() if k in ("skipped", "incomplete")} or None,

@@ -97,6 +97,14 @@ typedef struct {
     double amg_rebuild; /* AMG: iteration growth that triggers a rebuild (default 2.5) */
     int amg_sweeps;     /* AMG: damped block-Jacobi sweeps before and after each coarse correction
                            (1..4, default 1: fewest stiffness passes per solve) */
+    int recycle;        /* 0 (default): every linear solve starts from zero.  m in 1..8: the
+                           Newton solves of one load step share the stiffness, so each starts
+                           from the Galerkin combination of the step's last m solutions (their
+                           right-hand sides are K times them, so neither the guess nor its
+                           residual needs an extra product beyond one true residual); the solve
+                           still ends at cg_rtol relative to its own right-hand side.  In the
+                           plastic range, where modified Newton contracts slowly, the guess
+                           removes 2 to 4 of the 10 decades a solve must gain. */
 } lpm_solver_opts;
 
 typedef struct {

@@ -187,6 +187,54 @@ AMG_HD void jacobi0_row(int n, int i, uint8_t m, const PT *Pinv, T omega, const 
                  (m & 4) ? omega * d[2] : T(0));
 }
 
+// One R x C block (N = R C values, row-major) into registers: on the device
+// FP32 blocks of 36 values (144 B, 16-byte aligned) load as nine float4, of
+// 18 values (72 B, 8-byte aligned) as nine float2; streaming loads.
+template <int N, typename T>
+AMG_HD void load_block(const T *p, T (&b)[N])
+{
+#ifdef __CUDA_ARCH__
+    if constexpr (sizeof(T) == 4 && N % 4 == 0) {
+        for (int q = 0; q < N / 4; q++) {
+            const float4 v = __ldcs(reinterpret_cast<const float4 *>(p) + q);
+            b[4 * q] = v.x;
+            b[4 * q + 1] = v.y;
+            b[4 * q + 2] = v.z;
+            b[4 * q + 3] = v.w;
+        }
+        return;
+    } else if constexpr (sizeof(T) == 4 && N % 2 == 0) {
+        for (int q = 0; q < N / 2; q++) {
+            const float2 v = __ldcs(reinterpret_cast<const float2 *>(p) + q);
+            b[2 * q] = v.x;
+            b[2 * q + 1] = v.y;
+        }
+        return;
+    }
+#endif
+    for (int q = 0; q < N; q++)
+        b[q] = p[q];
+}
+
+// C consecutive vector entries starting at p (p 8-byte aligned: SX and C
+// even); float2 loads of FP32 on the device
+template <int C, typename T>
+AMG_HD void load_entries(const T *p, T (&v)[C])
+{
+#ifdef __CUDA_ARCH__
+    if constexpr (sizeof(T) == 4 && C % 2 == 0) {
+        for (int q = 0; q < C / 2; q++) {
+            const float2 t = __ldg(reinterpret_cast<const float2 *>(p) + q);
+            v[2 * q] = t.x;
+            v[2 * q + 1] = t.y;
+        }
+        return;
+    }
+#endif
+    for (int c = 0; c < C; c++)
+        v[c] = p[c];
+}
+
 // Block-CSR level: partial y of block row `row` (R x C row-major blocks of
 // T; block column j of x at x[j * SX]) over the blocks ptr[row] + sub,
 // + nl, ...
@@ -195,11 +243,10 @@ AMG_HD void bsr_row_partial(const long long *ptr, const int *col, const T *val, 
                             int sub, int nl, T (&y)[R])
 {
     for (long long k = ptr[row] + sub; k < ptr[row + 1]; k += nl) {
-        const T *blk = val + (size_t)k * (R * C);
-        const T *xc = x + (size_t)col[k] * SX;
+        T blk[R * C];
+        load_block<R * C, T>(val + (size_t)k * (R * C), blk);
         T xv[C];
-        for (int c = 0; c < C; c++)
-            xv[c] = xc[c];
+        load_entries<C, T>(x + (size_t)col[k] * SX, xv);
         for (int r = 0; r < R; r++)
             for (int c = 0; c < C; c++)
                 y[r] += blk[r * C + c] * xv[c];

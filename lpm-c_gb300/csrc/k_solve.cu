@@ -832,6 +832,12 @@ void launch_refine_residual(Ctx &c, const dvec4 *x, const dvec4 *b, dvec4 *r, do
                                                                        bscale);
 }
 
+// r = b - K x with an FP64 matrix (the FP64 stiffness), |r|^2 into norms[2]
+void launch_refine_residual64(Ctx &c, const double *K, const dvec4 *x, const dvec4 *b, dvec4 *r)
+{
+    k_refine_res<false, double><<<red_grid(c), VTPB, 0, c.stream>>>(spmv_args(c), K, x, b, r, c.norms, 2, 1.0);
+}
+
 void launch_refine_batch(Ctx &c, const dvec4 *x, const dvec4 *b, dvec4 *r)
 {
     SpmvArgs a = spmv_args(c);

@@ -113,6 +113,18 @@ static void free_anderson(Ctx &c)
     c.acc = Ctx::Anderson();
 }
 
+static void free_recycle(Ctx &c)
+{
+    dfree(c.rec.du);
+    dfree(c.rec.b);
+    dfree(c.rec.x0);
+    dfree(c.rec.r0);
+    dfree(c.rec.dots);
+    if (c.rec.dots_h)
+        cudaFreeHost(c.rec.dots_h);
+    c.rec = Ctx::Recycle();
+}
+
 static void free_damage(Ctx &c)
 {
     Ctx::Damage &d = c.dmg;
@@ -142,6 +154,7 @@ Ctx::~Ctx()
     free_batch(*this);
     free_adjoint(*this);
     free_anderson(*this);
+    free_recycle(*this);
     free_damage(*this);
     free_amg(*this);
     void **all[] = {(void **)&xyz, (void **)&xyz0, (void **)&xyz_temp, (void **)&Pin, (void **)&Pex,
@@ -396,6 +409,7 @@ static int setup_common(Ctx &c, bool built = false)
     free_writer(c);
     free_adjoint(c);
     free_anderson(c);
+    free_recycle(c);
     free_damage(c);
     free_amg(c);
     drop_graphs(c);
@@ -457,6 +471,7 @@ void lpm_default_solver_opts(lpm_solver_opts *o)
     o->amg_spacing = 0.0;
     o->amg_rebuild = 2.5;
     o->amg_sweeps = 1;
+    o->recycle = 0;
 }
 
 int lpm_create(lpm_ctx **out, int device)
@@ -523,7 +538,8 @@ int lpm_set_solver(lpm_ctx *ctx, const lpm_solver_opts *o)
     if (!(o->cg_rtol > 0) || o->cg_maxiter <= 0 || o->newton_maxiter < 0 || o->check_every <= 0 ||
         o->newton_accel < 0 || o->newton_accel > 16 || !(o->cg_forcing >= 0.0 && o->cg_forcing < 1.0) ||
         (o->preconditioner != LPM_PRECOND_BJ && o->preconditioner != LPM_PRECOND_AMG) ||
-        !(o->amg_spacing >= 0.0) || !(o->amg_rebuild > 1.0) || o->amg_sweeps < 1 || o->amg_sweeps > 4)
+        !(o->amg_spacing >= 0.0) || !(o->amg_rebuild > 1.0) || o->amg_sweeps < 1 || o->amg_sweeps > 4 ||
+        o->recycle < 0 || o->recycle > 8)
         return fail(LPM_ERR_ARG, "invalid solver options");
     Ctx &c = ctx->c;
     const bool prec_change = c.opts.precision != o->precision;
@@ -938,7 +954,7 @@ static int solve_amg(Ctx &c, const dvec4 *b, double bn, lpm_step_stats *st)
     return LPM_OK;
 }
 
-int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
+static int solve_plain(Ctx &c, const dvec4 *b, lpm_step_stats *st)
 {
     int rc;
     launch_norm2(c, b, 2);
@@ -1047,11 +1063,140 @@ int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
         // redo this solve, and the context's later ones, with FP64 vectors
         // (the FP32 stiffness and products stay)
         c.vec64_fallback = true;
-        return solve_device(c, b, st);
+        return solve_plain(c, b, st);
     }
     if (st && rn > solve_rtol(c) * bn)
         st->status |= std::isfinite(rn) ? LPM_STATUS_CG_MAXIT : LPM_STATUS_NAN;
     LPM_CUDA(cudaMemcpyAsync(c.du, c.x_d, sizeof(dvec4) * c.n, cudaMemcpyDeviceToDevice, c.stream));
+    return LPM_OK;
+}
+
+static bool spd_solve(std::vector<double> G, int h, int ld, std::vector<double> &x);
+
+// r = b - K x (masked) in the precision of the solve, |r|^2 into norms[2]:
+// the FP64 stiffness, or the exact FP64 copy of the FP32 one when there is
+// one, else the FP32 values with FP64 products
+static void true_residual(Ctx &c, const dvec4 *x, const dvec4 *b, dvec4 *r)
+{
+    if (c.opts.precision == LPM_PREC_FP64)
+        launch_refine_residual64(c, c.Kd, x, b, r);
+    else
+        launch_refine_residual(c, x, b, r, 1.0);
+}
+
+static int recycle_prepare(Ctx &c, int m)
+{
+    Ctx::Recycle &R = c.rec;
+    if (R.m == m && R.du)
+        return LPM_OK;
+    free_recycle(c);
+    int rc;
+    const size_t n = c.n;
+    if ((rc = dalloc(R.du, (size_t)m * n)) || (rc = dalloc(R.b, (size_t)m * n)) || (rc = dalloc(R.x0, n)) ||
+        (rc = dalloc(R.r0, n)) || (rc = dalloc(R.dots, 16)))
+        return rc;
+    LPM_CUDA(cudaMallocHost((void **)&R.dots_h, 16 * sizeof(double)));
+    R.m = m;
+    R.G.assign((size_t)m * m, 0.0);
+    return LPM_OK;
+}
+
+// dots_h[j] = A_j . w over the stored slots j (in slot order)
+static int recycle_dots(Ctx &c, const dvec4 *const *A, int k, const dvec4 *w)
+{
+    adj_multidot(c, k, A, w, c.rec.dots);
+    LPM_CUDA(cudaMemcpyAsync(c.rec.dots_h, c.rec.dots, k * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    return sync(c);
+}
+
+// Solve K du = b (-> c.du) from the Galerkin combination of the load step's
+// earlier solutions (opts.recycle): with K du_j = b_j, the guess
+// x0 = sum_j c_j du_j with G c = (du_j . b) minimises the energy norm of its
+// error over their span.  One true residual r0 = b - K x0 follows, the
+// solver gains the remaining decades on r0, and (du, b) joins the store.
+int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
+{
+    const int m = std::min(c.opts.recycle, 8);
+    if (m <= 0 || c.nspec != 0)
+        return solve_plain(c, b, st);
+    int rc;
+    if ((rc = recycle_prepare(c, m)))
+        return rc;
+    Ctx::Recycle &R = c.rec;
+    const size_t n = c.n;
+    if (R.k_version != c.k_version) {  // a new stiffness: the stored pairs no longer apply
+        R.count = 0;
+        R.head = 0;
+        R.k_version = c.k_version;
+    }
+    const dvec4 *slots_du[8], *slots_b[8];
+    for (int j = 0; j < R.count; j++) {
+        slots_du[j] = R.du + (size_t)j * n;
+        slots_b[j] = R.b + (size_t)j * n;
+    }
+    bool guessed = false;
+    const double rtol0 = c.cg_rtol_now;
+    if (R.count > 0) {
+        launch_norm2(c, b, 2);
+        LPM_CUDA(cudaMemcpyAsync(c.norms_host, c.norms, 4 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        if ((rc = sync(c)))
+            return rc;
+        const double bn = std::sqrt(c.norms_host[2]);
+        if ((rc = recycle_dots(c, slots_du, R.count, b)))
+            return rc;
+        std::vector<double> coef(R.dots_h, R.dots_h + R.count);
+        if (bn > 0.0 && std::isfinite(bn) && spd_solve(R.G, R.count, R.m, coef)) {
+            adj_axpby(c, coef[0], slots_du[0], 0.0, R.x0);
+            for (int j = 1; j < R.count; j++)
+                adj_axpby(c, coef[j], slots_du[j], 1.0, R.x0);
+            true_residual(c, R.x0, b, R.r0);
+            LPM_CUDA(cudaMemcpyAsync(c.norms_host, c.norms, 4 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+            if ((rc = sync(c)))
+                return rc;
+            const double rn = std::sqrt(c.norms_host[2]);
+            if (c.trace)
+                std::fprintf(stderr, "lpm: recycled guess from %d solutions: |r0| / |b| = %.3e\n", R.count,
+                             rn / bn);
+            if (std::isfinite(rn) && rn < 0.5 * bn) {
+                guessed = true;
+                const double target = solve_rtol(c) * bn;  // the solve's tolerance, relative to |b|
+                if (rn <= target) {
+                    LPM_CUDA(cudaMemcpyAsync(c.du, R.x0, sizeof(dvec4) * n, cudaMemcpyDeviceToDevice, c.stream));
+                } else {
+                    c.cg_rtol_now = target / rn;
+                    rc = solve_plain(c, R.r0, st);
+                    c.cg_rtol_now = rtol0;
+                    if (rc)
+                        return rc;
+                    adj_axpby(c, 1.0, R.x0, 1.0, c.du);
+                }
+            }
+        }
+    }
+    if (!guessed && (rc = solve_plain(c, b, st)))
+        return rc;
+    // store (du, b): the newest pair replaces the oldest
+    const int slot = R.head;
+    dvec4 *du_s = R.du + (size_t)slot * n, *b_s = R.b + (size_t)slot * n;
+    LPM_CUDA(cudaMemcpyAsync(du_s, c.du, sizeof(dvec4) * n, cudaMemcpyDeviceToDevice, c.stream));
+    LPM_CUDA(cudaMemcpyAsync(b_s, b, sizeof(dvec4) * n, cudaMemcpyDeviceToDevice, c.stream));
+    R.count = std::min(R.count + 1, R.m);
+    R.head = (R.head + 1) % R.m;
+    for (int j = 0; j < R.count; j++) {
+        slots_du[j] = R.du + (size_t)j * n;
+        slots_b[j] = R.b + (size_t)j * n;
+    }
+    // G row and column of the new slot: du_slot . b_j and du_j . b_slot, symmetrised
+    if ((rc = recycle_dots(c, slots_b, R.count, du_s)))
+        return rc;
+    std::vector<double> row(R.dots_h, R.dots_h + R.count);
+    if ((rc = recycle_dots(c, slots_du, R.count, b_s)))
+        return rc;
+    for (int j = 0; j < R.count; j++) {
+        const double g = 0.5 * (row[j] + R.dots_h[j]);
+        R.G[(size_t)slot * R.m + j] = g;
+        R.G[(size_t)j * R.m + slot] = g;
+    }
     return LPM_OK;
 }
 

@@ -345,6 +345,16 @@ struct Ctx {
         dvec4 *u_prev = nullptr, *f_prev = nullptr;
         double *dots = nullptr, *dots_h = nullptr;
     } acc;
+    // initial guesses of the Newton solves from the load step's earlier
+    // solutions (opts.recycle): pairs (du_j, b_j) with K du_j = b_j in slots
+    // of a ring, the Galerkin matrix G_ij = du_i . b_j on the host
+    struct Recycle {
+        int m = 0, count = 0, head = 0;
+        dvec4 *du = nullptr, *b = nullptr, *x0 = nullptr, *r0 = nullptr;
+        double *dots = nullptr, *dots_h = nullptr;
+        std::vector<double> G;
+        long long k_version = -1;  // the assembly the stored pairs belong to
+    } rec;
     ~Ctx();
 };
 
@@ -393,6 +403,7 @@ void free_amg(Ctx &c);
 void launch_spmv_d(Ctx &c, const dvec4 *x, dvec4 *y, bool masked, bool dot_pq);
 void launch_spmv_f(Ctx &c, const float4 *x, float4 *y, bool masked, bool dot_pq);
 void launch_refine_residual(Ctx &c, const dvec4 *x, const dvec4 *b, dvec4 *r, double bscale);  // r = s b - K32 x (FP64)
+void launch_refine_residual64(Ctx &c, const double *K, const dvec4 *x, const dvec4 *b, dvec4 *r);  // r = b - K x
 void launch_spmv_fx(Ctx &c, const dvec4 *x, dvec4 *y, bool masked, bool dot);
 void launch_cg_init_fx(Ctx &c, const dvec4 *b, double scale, double delta2);
 void launch_cg_iter_fx(Ctx &c);

@@ -58,7 +58,7 @@ class SolverOpts(C.Structure):
                 ("refine_maxiter", C.c_int), ("check_every", C.c_int), ("use_graphs", C.c_int),
                 ("mixed_vectors", C.c_int), ("newton_accel", C.c_int), ("cg_forcing", C.c_double),
                 ("preconditioner", C.c_int), ("amg_spacing", C.c_double), ("amg_rebuild", C.c_double),
-                ("amg_sweeps", C.c_int)]
+                ("amg_sweeps", C.c_int), ("recycle", C.c_int)]
 
 
 class Tuning(C.Structure):

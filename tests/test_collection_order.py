@@ -8,7 +8,7 @@ import subprocess
 import sys
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-OPTION_FILES = {"test_gpu_amg.py", "test_gpu_forcing.py", "test_gpu_anderson.py"}
+OPTION_FILES = {"test_gpu_amg.py", "test_gpu_forcing.py", "test_gpu_anderson.py", "test_gpu_recycle.py"}
 
 
 def _fname(t):
