@@ -354,6 +354,8 @@ def assemble_line(args, case, partial, world, note=None):
            "fp64_arm": {k: v for k, v in f64.items() if k in ("skipped", "incomplete")} or None,
            "newton_iters": agg(mixed, "newton_iters") if done else None,
            "newton_iters_per_step": [st["newton_iters"] for st in mixed["stats"]] if done else None,
+           "newton_iters_per_warmup_step": [st["newton_iters"] for st in mixed["warm"]] if done else None,
+           "cg_iters_per_step": [st["cg_iters"] for st in mixed["stats"]] if done else None,
            "cg_iters": agg(mixed, "cg_iters") if done else None,
            "reliable_updates": agg(mixed, "refine_iters") if done else None,
            "fp64_newton_iters": agg(f64, "newton_iters") if "ms" in f64 else None,

@@ -208,10 +208,10 @@ __global__ void __launch_bounds__(ATPB) k_amg_reliable(AmgVec a, const dvec4 *rt
 enum { RZ_INIT = 0, RZ_ITER = 1, RZ_RELIABLE = 2 };
 
 // r.z after the V-cycle: INIT also sets p = z (and its two FP32 parts when
-// hi is given); ITER sets beta
+// split is given); ITER sets beta
 template <int MODE>
 __global__ void __launch_bounds__(ATPB) k_amg_rz(AmgVec a, const dvec4 *r, const dvec4 *z, dvec4 *p,
-                                                 float4 *hi = nullptr, float4 *lo = nullptr)
+                                                 float4 *split = nullptr)
 {
     CgScalars *sc = a.sc;
     if (sc->done)
@@ -221,12 +221,13 @@ __global__ void __launch_bounds__(ATPB) k_amg_rz(AmgVec a, const dvec4 *r, const
         const dvec4 rv = r[i], zv = z[i];
         if (MODE == RZ_INIT) {
             p[i] = zv;
-            if (hi) {
+            if (split) {
                 const float hx = __double2float_rn(zv.x), hy = __double2float_rn(zv.y),
                             hz = __double2float_rn(zv.z);
-                hi[i] = make_float4(hx, hy, hz, 0.f);
-                lo[i] = make_float4(__double2float_rn(zv.x - (double)hx), __double2float_rn(zv.y - (double)hy),
-                                    __double2float_rn(zv.z - (double)hz), 0.f);
+                split[2 * (size_t)i] = make_float4(hx, hy, hz, 0.f);
+                split[2 * (size_t)i + 1] =
+                    make_float4(__double2float_rn(zv.x - (double)hx), __double2float_rn(zv.y - (double)hy),
+                                __double2float_rn(zv.z - (double)hz), 0.f);
             }
         }
         v[0] += rv.x * zv.x + rv.y * zv.y + rv.z * zv.z;
@@ -546,8 +547,8 @@ void launch_amg_init(Ctx &c, const dvec4 *b, double scale, double delta2, bool k
     k_amg_init<<<red_grid(c), ATPB, 0, c.stream>>>(amg_vec(c), b, scale, c.x_d, c.r_d, solve_rtol(c),
                                                    c.opts.cg_maxiter, delta2);
     launch_amg_vcycle(c, c.r_d, c.z_d);
-    k_amg_rz<RZ_INIT><<<red_grid(c), ATPB, 0, c.stream>>>(amg_vec(c), c.r_d, c.z_d, c.p_d, k32 ? c.p_hi : nullptr,
-                                                          k32 ? c.p_lo : nullptr);
+    k_amg_rz<RZ_INIT><<<red_grid(c), ATPB, 0, c.stream>>>(amg_vec(c), c.r_d, c.z_d, c.p_d,
+                                                          k32 ? c.p_split : nullptr);
 }
 
 void launch_amg_iter(Ctx &c, bool k32)

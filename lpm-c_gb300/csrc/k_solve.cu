@@ -283,12 +283,20 @@ __global__ void __launch_bounds__(VTPB) k_spmv(SpmvArgs a, const V *__restrict__
 // values.  The product error becomes about 6e-8 sum_j |K_ij| |x_j - x_i|:
 // FP32 arithmetic and an FP32 stiffness stream with the accuracy the CG needs.
 
-__device__ __forceinline__ void split_store(const dvec4 &v, float4 *hi, float4 *lo)
+// the two FP32 parts of one particle's entry, hi then lo, as one 32-byte
+// record (a single sector per neighbour gather)
+struct __align__(32) SplitRec {
+    float4 hi, lo;
+};
+
+__device__ __forceinline__ void split_store(const dvec4 &v, float4 *rec)
 {
     const float hx = __double2float_rn(v.x), hy = __double2float_rn(v.y), hz = __double2float_rn(v.z);
-    *hi = make_float4(hx, hy, hz, 0.f);
-    *lo = make_float4(__double2float_rn(v.x - (double)hx), __double2float_rn(v.y - (double)hy),
-                      __double2float_rn(v.z - (double)hz), 0.f);
+    SplitRec s;
+    s.hi = make_float4(hx, hy, hz, 0.f);
+    s.lo = make_float4(__double2float_rn(v.x - (double)hx), __double2float_rn(v.y - (double)hy),
+                       __double2float_rn(v.z - (double)hz), 0.f);
+    *reinterpret_cast<SplitRec *>(rec) = s;
 }
 
 // Krs[k][row] = sum over the row's blocks of component k of Kf (FP64 sums,
@@ -335,9 +343,9 @@ __global__ void __launch_bounds__(VTPB) k_row_sums(int n, const long long *__res
 // DOT: p.y with p = x64 (FP64) and alpha = rz / (p.y), as k_spmv.
 template <bool DOT>
 __global__ void __launch_bounds__(VTPB) k_spmv_diff(SpmvArgs a, const float *__restrict__ val,
-                                                    const float *__restrict__ rs, const float4 *__restrict__ hi,
-                                                    const float4 *__restrict__ lo, const dvec4 *__restrict__ x64,
-                                                    dvec4 *__restrict__ y)
+                                                    const float *__restrict__ rs,
+                                                    const SplitRec *__restrict__ split,
+                                                    const dvec4 *__restrict__ x64, dvec4 *__restrict__ y)
 {
     if (DOT && a.sc->done)
         return;
@@ -351,7 +359,8 @@ __global__ void __launch_bounds__(VTPB) k_spmv_diff(SpmvArgs a, const float *__r
         const long long off = a.rowoff[row];
         const int np = a.npad[row];
         const float *vr = val + 9 * off;
-        const float4 hi_i = __ldg(hi + row), lo_i = __ldg(lo + row);
+        const SplitRec own = split[row];
+        const float4 hi_i = own.hi, lo_i = own.lo;
         float y0 = 0.f, y1 = 0.f, y2 = 0.f;
         for (int b0 = 4 * sub; b0 < np; b0 += 64) {
             int cc[4];
@@ -363,7 +372,8 @@ __global__ void __launch_bounds__(VTPB) k_spmv_diff(SpmvArgs a, const float *__r
             float d[4][3];
 #pragma unroll
             for (int j = 0; j < 4; j++) {
-                const float4 h = __ldg(hi + cc[j]), l = __ldg(lo + cc[j]);
+                const SplitRec rj = split[cc[j]];
+                const float4 h = rj.hi, l = rj.lo;
                 d[j][0] = (h.x - hi_i.x) + (l.x - lo_i.x);
                 d[j][1] = (h.y - hi_i.y) + (l.y - lo_i.y);
                 d[j][2] = (h.z - hi_i.z) + (l.z - lo_i.z);
@@ -610,7 +620,7 @@ __global__ void __launch_bounds__(VTPB) k_cg_update(VecArgs a, const V *P, V4 *x
 // the difference-form product (split_store).
 template <typename V, typename V4>
 __global__ void __launch_bounds__(VTPB) k_cg_p(int n, CgScalars *sc, const V4 *z, V4 *p, unsigned *counter,
-                                               float4 *hi = nullptr, float4 *lo = nullptr)
+                                               float4 *split = nullptr)
 {
     if (sc->done)
         return;
@@ -623,8 +633,8 @@ __global__ void __launch_bounds__(VTPB) k_cg_p(int n, CgScalars *sc, const V4 *z
         pv.z = zv.z + be * pv.z;
         p[i] = pv;
         if constexpr (sizeof(V) == 8) {
-            if (hi)
-                split_store(pv, hi + i, lo + i);
+            if (split)
+                split_store(pv, split + 2 * (size_t)i);
         }
     }
     __syncthreads();
@@ -906,7 +916,7 @@ void launch_cg_iter_d(Ctx &c)
 void launch_cg_p_d(Ctx &c, bool split)
 {
     k_cg_p<double, dvec4><<<red_grid(c), VTPB, 0, c.stream>>>(c.n, c.sc, c.z_d, c.p_d, c.counter,
-                                                              split ? c.p_hi : nullptr, split ? c.p_lo : nullptr);
+                                                              split ? c.p_split : nullptr);
 }
 
 void launch_row_sums(Ctx &c)
@@ -919,9 +929,9 @@ void launch_spmv_diff(Ctx &c, dvec4 *y, bool dot)
     SpmvArgs a = spmv_args(c);
     record_timing(c, c.ev_a);
     if (dot)
-        k_spmv_diff<true><<<spmv_grid(c), VTPB, 0, c.stream>>>(a, c.Kf, c.Krs, c.p_hi, c.p_lo, c.p_d, y);
+        k_spmv_diff<true><<<spmv_grid(c), VTPB, 0, c.stream>>>(a, c.Kf, c.Krs, reinterpret_cast<const SplitRec *>(c.p_split), c.p_d, y);
     else
-        k_spmv_diff<false><<<spmv_grid(c), VTPB, 0, c.stream>>>(a, c.Kf, c.Krs, c.p_hi, c.p_lo, c.p_d, y);
+        k_spmv_diff<false><<<spmv_grid(c), VTPB, 0, c.stream>>>(a, c.Kf, c.Krs, reinterpret_cast<const SplitRec *>(c.p_split), c.p_d, y);
     record_timing(c, c.ev_b);
 }
 

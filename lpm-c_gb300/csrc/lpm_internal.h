@@ -267,7 +267,7 @@ struct Ctx {
     // the FP64 search direction split into two FP32 parts (p = hi + lo) for
     // the difference-form FP32 product, and the FP32 stiffness's block row
     // sums [9][n] it needs (for the assembly numbered krs_version)
-    float4 *p_hi = nullptr, *p_lo = nullptr;
+    float4 *p_split = nullptr;  // [2 i] = hi, [2 i + 1] = lo: one 32-byte record per particle
     float *Krs = nullptr;
     long long krs_version = -1;
     // multigrid: FP16 copy of Kf scaled by 1 / kh_scale[0] (device) for the
@@ -407,9 +407,9 @@ void launch_refine_residual64(Ctx &c, const double *K, const dvec4 *x, const dve
 void launch_spmv_fx(Ctx &c, const dvec4 *x, dvec4 *y, bool masked, bool dot);
 void launch_cg_init_fx(Ctx &c, const dvec4 *b, double scale, double delta2);
 void launch_cg_iter_fx(Ctx &c);
-void launch_cg_p_d(Ctx &c, bool split = false);  // p = z + beta p (FP64 vectors); split: also p_hi/p_lo
+void launch_cg_p_d(Ctx &c, bool split = false);  // p = z + beta p (FP64 vectors); split: also p_split
 void launch_row_sums(Ctx &c);  // Krs = block row sums of Kf (FP64 sums of the FP32 values)
-// y = K32 p in difference form from p_hi/p_lo and Krs (masked); dot: p.y and alpha
+// y = K32 p in difference form from p_split and Krs (masked); dot: p.y and alpha
 void launch_spmv_diff(Ctx &c, dvec4 *y, bool dot);
 void launch_reliable_d(Ctx &c, const dvec4 *rtrue);
 void launch_cg_init_d(Ctx &c, const dvec4 *b, double scale);

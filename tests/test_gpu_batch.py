@@ -105,15 +105,19 @@ def test_batch_offsets_and_sizes(gpu_lib):
 @pytest.mark.parametrize("precision", [0, 1])
 def test_batch_specimens_match_oracle(oracle_mod, gpu_lib, precision):
     """Three specimens of a batch (the smallest, a middle one and the
-    largest) against the oracle, the CPU restatement pinned to the reference:
-    6 tension steps into the plastic range, both sides converged to 1e-10,
-    displacements and plastic strain within 1e-8."""
+    largest: 140, 168 and 315 particles) against the oracle, the CPU
+    restatement pinned to the reference: 6 tension steps into the plastic
+    range, both sides converged to 1e-10, displacements and plastic strain
+    within 1e-8.  (On specimens 1, 4 and 5 the reference's modified Newton
+    breaks down at this tolerance: its iterates reach NaN in steps 4-6, as on
+    the per-particle-moduli case; at 1e-9 it converges on all seven.)"""
     G = gpu_lib
     case = small_case(1e-10)
     nsteps = 6
     off, hist, stats, alpha = run_batch(G, case, nsteps, precision=precision)
     sizes = np.diff(off)
-    picks = sorted({int(np.argmin(sizes)), int(np.argsort(sizes)[len(sizes) // 2]), int(np.argmax(sizes))})
+    picks = [0, 2, 3]
+    assert sizes[0] == sizes.min() and sizes[3] == sizes.max()
     oracle_mod.set_threads(4)
     for k in picks:
         o = oracle_mod.Oracle()
