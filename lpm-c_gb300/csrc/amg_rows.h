@@ -216,6 +216,34 @@ AMG_HD void load_block(const T *p, T (&b)[N])
         b[q] = p[q];
 }
 
+#ifdef __CUDACC__
+// FP16 blocks (the device's prolongation, restriction and coarse operators)
+// as float: 36 values (72 B, 8-byte aligned) as nine 8-byte loads, 18 values
+// (36 B, 4-byte aligned) as nine half2
+template <int N>
+__device__ __forceinline__ void load_block(const __half *p, float (&b)[N])
+{
+    if constexpr (N % 4 == 0) {
+        for (int q = 0; q < N / 4; q++) {
+            const uint2 t = __ldcs(reinterpret_cast<const uint2 *>(p) + q);
+            const float2 u = __half22float2(*reinterpret_cast<const __half2 *>(&t.x));
+            const float2 w = __half22float2(*reinterpret_cast<const __half2 *>(&t.y));
+            b[4 * q] = u.x;
+            b[4 * q + 1] = u.y;
+            b[4 * q + 2] = w.x;
+            b[4 * q + 3] = w.y;
+        }
+    } else {
+        for (int q = 0; q < N / 2; q++) {
+            const unsigned t = __ldcs(reinterpret_cast<const unsigned *>(p) + q);
+            const float2 u = __half22float2(*reinterpret_cast<const __half2 *>(&t));
+            b[2 * q] = u.x;
+            b[2 * q + 1] = u.y;
+        }
+    }
+}
+#endif
+
 // C consecutive vector entries starting at p (p 8-byte aligned: SX and C
 // even); float2 loads of FP32 on the device
 template <int C, typename T>
@@ -236,15 +264,16 @@ AMG_HD void load_entries(const T *p, T (&v)[C])
 }
 
 // Block-CSR level: partial y of block row `row` (R x C row-major blocks of
-// T; block column j of x at x[j * SX]) over the blocks ptr[row] + sub,
-// + nl, ...
-template <int R, int C, typename T>
-AMG_HD void bsr_row_partial(const long long *ptr, const int *col, const T *val, const T *x, int SX, int row,
+// V; block column j of x at x[j * SX]) over the blocks ptr[row] + sub,
+// + nl, ...; products and sums in T (the device stores FP16 blocks, scaled,
+// and multiplies in FP32; the caller applies the scale to the row sums)
+template <int R, int C, typename T, typename V = T>
+AMG_HD void bsr_row_partial(const long long *ptr, const int *col, const V *val, const T *x, int SX, int row,
                             int sub, int nl, T (&y)[R])
 {
     for (long long k = ptr[row] + sub; k < ptr[row + 1]; k += nl) {
         T blk[R * C];
-        load_block<R * C, T>(val + (size_t)k * (R * C), blk);
+        load_block<R * C>(val + (size_t)k * (R * C), blk);
         T xv[C];
         load_entries<C, T>(x + (size_t)col[k] * SX, xv);
         for (int r = 0; r < R; r++)

@@ -308,12 +308,14 @@ constexpr int BL_LANES = 8;  // lanes per block row of the coarse-level kernels
 
 // R x C blocks, 8 lanes per block row, epilogue by MODE (amg_rows.h):
 // restriction (BM_SET), prolongation (BM_ADD), coarse smoothing (BM_SMOOTH)
-// and residual (BM_RESID); FP32 throughout.
+// and residual (BM_RESID).  Blocks in FP16 times vscale (1 for the
+// prolongation and restriction, whose weights lie well inside FP16's range;
+// max |A| / 2^14 for the coarse operators), FP32 vectors and arithmetic.
 template <int R, int C, int MODE>
 __global__ void __launch_bounds__(ATPB) k_amg_bsr(int nbr, const long long *__restrict__ ptr,
-                                                  const int *__restrict__ col, const float *__restrict__ val,
-                                                  const float *__restrict__ x, int SX, float *__restrict__ out,
-                                                  int SY, const float *__restrict__ b,
+                                                  const int *__restrict__ col, const __half *__restrict__ val,
+                                                  float vscale, const float *__restrict__ x, int SX,
+                                                  float *__restrict__ out, int SY, const float *__restrict__ b,
                                                   const float *__restrict__ dinv, float omega,
                                                   const CgScalars *sc)
 {
@@ -329,14 +331,18 @@ __global__ void __launch_bounds__(ATPB) k_amg_bsr(int nbr, const long long *__re
 #pragma unroll
         for (int r = 0; r < R; r++)
             y[r] = 0.f;
-        bsr_row_partial<R, C, float>(ptr, col, val, x, SX, row, sub, BL_LANES, y);
+        bsr_row_partial<R, C, float, __half>(ptr, col, val, x, SX, row, sub, BL_LANES, y);
 #pragma unroll
         for (int o = BL_LANES / 2; o > 0; o >>= 1)
 #pragma unroll
             for (int r = 0; r < R; r++)
                 y[r] += __shfl_xor_sync(gmask, y[r], o);
-        if (sub == 0)
+        if (sub == 0) {
+#pragma unroll
+            for (int r = 0; r < R; r++)
+                y[r] *= vscale;
             bsr_epilogue<R, MODE, float>(row, y, x, SX, out, SY, b, dinv, omega);
+        }
     }
 }
 
@@ -460,12 +466,13 @@ void launch_amg_stiffness16(Ctx &c)
 }
 
 template <int R, int C, int MODE>
-static void bsr_launch(Ctx &c, int nbr, const long long *ptr, const int *col, const float *val, const float *x,
-                       int SX, float *out, int SY, const float *b = nullptr, const float *dinv = nullptr,
-                       float omega = 0.f)
+static void bsr_launch(Ctx &c, int nbr, const long long *ptr, const int *col, const unsigned short *val,
+                       float vscale, const float *x, int SX, float *out, int SY, const float *b = nullptr,
+                       const float *dinv = nullptr, float omega = 0.f)
 {
     const int g = grid_for(c, (long long)nbr * BL_LANES);
-    k_amg_bsr<R, C, MODE><<<g, ATPB, 0, c.stream>>>(nbr, ptr, col, val, x, SX, out, SY, b, dinv, omega, c.sc);
+    k_amg_bsr<R, C, MODE><<<g, ATPB, 0, c.stream>>>(nbr, ptr, col, reinterpret_cast<const __half *>(val), vscale,
+                                                    x, SX, out, SY, b, dinv, omega, c.sc);
 }
 
 // FP32 throughout; level 0 works on the float4 buffers r_f (the right-hand
@@ -501,16 +508,16 @@ void launch_amg_vcycle(Ctx &c, const dvec4 *r, dvec4 *z)
                 std::swap(it, ot);
             }
             k0_launch<float>(c, SM_RESID, om, it, bt, (float *)ot);
-            bsr_launch<6, 3, BM_SET>(c, v.nnext, v.pt_ptr, v.pt_col, v.pt_val, (const float *)ot, 4, bnext, 6);
+            bsr_launch<6, 3, BM_SET>(c, v.nnext, v.pt_ptr, v.pt_col, v.pt_val, 1.0f, (const float *)ot, 4, bnext, 6);
         } else {
             float *it = v.x, *ot = v.y;
             k_amg_jacobi6<<<grid_for(c, v.nb), ATPB, 0, c.stream>>>(v.nb, v.dinv, om, v.b, it, c.sc);
             for (int s = 1; s < nu; s++) {
-                bsr_launch<6, 6, BM_SMOOTH>(c, v.nb, v.a_ptr, v.a_col, v.a_val, it, 6, ot, 6, v.b, v.dinv, om);
+                bsr_launch<6, 6, BM_SMOOTH>(c, v.nb, v.a_ptr, v.a_col, v.a_val, v.a_scale, it, 6, ot, 6, v.b, v.dinv, om);
                 std::swap(it, ot);
             }
-            bsr_launch<6, 6, BM_RESID>(c, v.nb, v.a_ptr, v.a_col, v.a_val, it, 6, ot, 6, v.b);
-            bsr_launch<6, 6, BM_SET>(c, v.nnext, v.pt_ptr, v.pt_col, v.pt_val, ot, 6, bnext, 6);
+            bsr_launch<6, 6, BM_RESID>(c, v.nb, v.a_ptr, v.a_col, v.a_val, v.a_scale, it, 6, ot, 6, v.b);
+            bsr_launch<6, 6, BM_SET>(c, v.nnext, v.pt_ptr, v.pt_col, v.pt_val, 1.0f, ot, 6, bnext, 6);
         }
     }
     k_amg_dense<float, float><<<gd, ATPB, 0, c.stream>>>(H.nc, H.cinv, H.cb, H.cx, 6, 6, c.sc);
@@ -522,7 +529,7 @@ void launch_amg_vcycle(Ctx &c, const dvec4 *r, dvec4 *z)
         const float om = (float)v.omega;
         if (l == 0) {
             float4 *it = (nu % 2 == 1) ? c.x_f : c.q_f, *ot = (nu % 2 == 1) ? c.q_f : c.x_f;
-            bsr_launch<3, 6, BM_ADD>(c, v.nb, v.p_ptr, v.p_col, v.p_val, e, 6, (float *)it, 4);
+            bsr_launch<3, 6, BM_ADD>(c, v.nb, v.p_ptr, v.p_col, v.p_val, 1.0f, e, 6, (float *)it, 4);
             for (int s = 0; s < nu; s++) {
                 if (s == nu - 1) {
                     k0_launch<double>(c, SM_SMOOTH, om, it, bt, (double *)z);
@@ -533,9 +540,9 @@ void launch_amg_vcycle(Ctx &c, const dvec4 *r, dvec4 *z)
             }
         } else {
             float *it = (nu % 2 == 1) ? v.x : v.y, *ot = (nu % 2 == 1) ? v.y : v.x;
-            bsr_launch<6, 6, BM_ADD>(c, v.nb, v.p_ptr, v.p_col, v.p_val, e, 6, it, 6);
+            bsr_launch<6, 6, BM_ADD>(c, v.nb, v.p_ptr, v.p_col, v.p_val, 1.0f, e, 6, it, 6);
             for (int s = 0; s < nu; s++) {
-                bsr_launch<6, 6, BM_SMOOTH>(c, v.nb, v.a_ptr, v.a_col, v.a_val, it, 6, ot, 6, v.b, v.dinv, om);
+                bsr_launch<6, 6, BM_SMOOTH>(c, v.nb, v.a_ptr, v.a_col, v.a_val, v.a_scale, it, 6, ot, 6, v.b, v.dinv, om);
                 std::swap(it, ot);
             }
         }
@@ -584,9 +591,33 @@ static int amg_alloc_copy(T *&d, const T *h, size_t count)
     return LPM_OK;
 }
 
-// prolongation, restriction and coarse-operator values are kept in FP32 on
-// the device: they only shape the preconditioner, and FP32 halves their
-// traffic and keeps their products off the FP64 units
+// prolongation, restriction and coarse-operator values are kept in FP16 on
+// the device (coarse operators scaled): they only shape the preconditioner,
+// and FP16 quarters their traffic against FP64
+// FP16 copies of block values divided by scale (round to nearest)
+template <typename Vec>
+static std::vector<unsigned short> to_half(const Vec &v, float scale)
+{
+    std::vector<unsigned short> h(v.size());
+    const double inv = 1.0 / scale;
+#pragma omp parallel for schedule(static)
+    for (long long k = 0; k < (long long)v.size(); k++) {
+        const __half x = __double2half(v[k] * inv);
+        h[k] = *reinterpret_cast<const unsigned short *>(&x);
+    }
+    return h;
+}
+
+// max |v| / 2^14: the largest value maps to 16384, inside FP16's range
+template <typename Vec>
+static float half_scale(const Vec &v)
+{
+    double m = 0.0;
+    for (size_t k = 0; k < v.size(); k++)
+        m = std::max(m, std::fabs((double)v[k]));
+    return m > 0.0 ? (float)(m / 16384.0) : 1.0f;
+}
+
 template <typename Vec>
 static std::vector<float> to_float(const Vec &v)
 {
@@ -639,15 +670,16 @@ static int amg_upload(AmgDev &H, const AmgHierarchy &h)
         v.omega = s.omega;
         if ((rc = amg_alloc_copy(v.p_ptr, s.P.ptr.data(), s.P.ptr.size())) ||
             (rc = amg_alloc_copy(v.p_col, s.P.col.data(), s.P.col.size())) ||
-            (rc = amg_alloc_copy(v.p_val, to_float(s.P.val).data(), s.P.val.size())) ||
+            (rc = amg_alloc_copy(v.p_val, to_half(s.P.val, 1.0f).data(), s.P.val.size())) ||
             (rc = amg_alloc_copy(v.pt_ptr, s.Pt.ptr.data(), s.Pt.ptr.size())) ||
             (rc = amg_alloc_copy(v.pt_col, s.Pt.col.data(), s.Pt.col.size())) ||
-            (rc = amg_alloc_copy(v.pt_val, to_float(s.Pt.val).data(), s.Pt.val.size())))
+            (rc = amg_alloc_copy(v.pt_val, to_half(s.Pt.val, 1.0f).data(), s.Pt.val.size())))
             return rc;
         if (l > 0) {
             if ((rc = amg_alloc_copy(v.a_ptr, s.A.ptr.data(), s.A.ptr.size())) ||
                 (rc = amg_alloc_copy(v.a_col, s.A.col.data(), s.A.col.size())) ||
-                (rc = amg_alloc_copy(v.a_val, to_float(s.A.val).data(), s.A.val.size())) ||
+                (v.a_scale = half_scale(s.A.val), false) ||
+                (rc = amg_alloc_copy(v.a_val, to_half(s.A.val, v.a_scale).data(), s.A.val.size())) ||
                 (rc = amg_alloc_copy(v.dinv, to_float(s.Dinv).data(), s.Dinv.size())) ||
                 (rc = amg_alloc_copy<float>(v.b, nullptr, 6 * (size_t)s.nblock)) ||
                 (rc = amg_alloc_copy<float>(v.x, nullptr, 6 * (size_t)s.nblock)) ||

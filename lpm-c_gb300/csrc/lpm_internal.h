@@ -126,16 +126,17 @@ struct AmgDevLevel {
     int nb = 0, bs = 0;  // block rows, DOFs per block row
     int nnext = 0;       // block rows of the next level
     double omega = 1.0;  // smoother damping 4/3 / rho(D^-1 A)
-    long long *a_ptr = nullptr;   // levels >= 1: operator, 6 x 6 blocks (FP32 values)
+    long long *a_ptr = nullptr;   // levels >= 1: operator, 6 x 6 blocks (FP16 values times a_scale)
     int *a_col = nullptr;
-    float *a_val = nullptr;
+    unsigned short *a_val = nullptr;
+    float a_scale = 1.0f;
     float *dinv = nullptr;        // levels >= 1: 6 x 6 diagonal-block inverses
-    long long *p_ptr = nullptr;   // prolongation, bs x 6 blocks (FP32 values)
+    long long *p_ptr = nullptr;   // prolongation, bs x 6 blocks (FP16 values)
     int *p_col = nullptr;
-    float *p_val = nullptr;
-    long long *pt_ptr = nullptr;  // restriction, 6 x bs blocks (FP32 values)
+    unsigned short *p_val = nullptr;
+    long long *pt_ptr = nullptr;  // restriction, 6 x bs blocks (FP16 values)
     int *pt_col = nullptr;
-    float *pt_val = nullptr;
+    unsigned short *pt_val = nullptr;
     float *b = nullptr, *x = nullptr, *y = nullptr;  // levels >= 1: right-hand side, two iterates
 };
 
