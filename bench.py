@@ -763,7 +763,7 @@ def run_fcc(args):
         amg = args.precond == "amg"
         s.set_solver(precision=prec, newton_tol=case.newton_tol, newton_maxiter=300, cg_rtol=1e-10,
                      cg_maxiter=2000 if amg else 40000, mixed_vectors=64,
-                     preconditioner=G.PRECOND_AMG if amg else G.PRECOND_BJ)
+                     preconditioner=G.PRECOND_AMG if amg else G.PRECOND_BJ, recycle=RECYCLE)
         setup_s = time.perf_counter() - t0
         for k in range(W):
             s.load_step(cases.sc_bcs(case.schedule[k]))
@@ -797,7 +797,9 @@ def run_fcc(args):
                    "mixed_over_fp64": f["ms"] / m["ms"], "disp_err_mixed_vs_fp64": err,
                    "newton_iters": agg(m["stats"], "newton_iters"), "cg_iters": agg(m["stats"], "cg_iters"),
                    "fp64_newton_iters": agg(f["stats"], "newton_iters"), "fp64_cg_iters": agg(f["stats"], "cg_iters"),
-                   "max_cp_A": float(m["A"].max())},
+                   "newton_iters_per_step": [st["newton_iters"] for st in m["stats"]],
+                   "cg_iters_per_step": [st["cg_iters"] for st in m["stats"]],
+                   "recycle": RECYCLE, "max_cp_A": float(m["A"].max())},
         "clocks": m["clocks"], "e2e": None, "cpu_baseline": None,
     }
     print(json.dumps(line))
