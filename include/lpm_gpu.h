@@ -269,6 +269,8 @@ typedef struct lpm_tuning {
     int cg_per_sm;
     double spmv_ms;        /* lpm_autotune: time of the chosen SpMV shape */
     double spmv_ms_default;/* lpm_autotune: time of the default shape (0, 8, 8) */
+    int smooth_lanes;      /* output: lanes per block row of the multigrid level-0 smoother (16, 8, 4) */
+    double smooth_ms;      /* lpm_autotune: time of one smoother pass in the chosen shape (0: not tuned) */
 } lpm_tuning;
 /* Time every SpMV shape (and vector-kernel grid) on the context's current
  * stiffness with CUDA events and keep the fastest.  Needs an assembled

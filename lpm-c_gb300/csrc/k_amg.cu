@@ -248,7 +248,6 @@ __global__ void __launch_bounds__(ATPB) k_amg_rz(AmgVec a, const dvec4 *r, const
 
 // ---- level 0: the stiffness ---------------------------------------------------
 
-constexpr int L0_LANES = 16;  // lanes per block row of the stiffness
 
 // MODE SM_SMOOTH: out = x + omega Pinv mask(b - K x); SM_RESID: out = mask(b - K x).
 // Half a warp per block row, lanes over the row's blocks (padding included:
@@ -259,7 +258,7 @@ constexpr int L0_LANES = 16;  // lanes per block row of the stiffness
 // The smoother's operator is only the preconditioner's: rounded to FP16 (or
 // even to 8 significand bits) it leaves the PCG iteration counts of the numpy
 // checks unchanged.
-template <int MODE, typename O>
+template <int MODE, typename O, int L0_LANES = 16>
 __global__ void __launch_bounds__(ATPB) k_amg_k0(int n, const long long *__restrict__ rowoff,
                                                  const int *__restrict__ npad, const int *__restrict__ cols,
                                                  const uint8_t *__restrict__ mask, const __half *__restrict__ val,
@@ -272,7 +271,7 @@ __global__ void __launch_bounds__(ATPB) k_amg_k0(int n, const long long *__restr
         return;
     const float s = *kscale;
     const int sub = threadIdx.x & (L0_LANES - 1);
-    const unsigned gmask = 0xffffu << ((threadIdx.x & 31) & ~(L0_LANES - 1));
+    const unsigned gmask = ((1u << L0_LANES) - 1u) << ((threadIdx.x & 31) & ~(L0_LANES - 1));
     const int g = (blockIdx.x * blockDim.x + threadIdx.x) / L0_LANES;
     const int ng = (gridDim.x * blockDim.x) / L0_LANES;
     for (int row = g; row < n; row += ng) {
@@ -388,18 +387,46 @@ static int grid_for(const Ctx &c, long long rows_x_threads)
 
 static AmgVec amg_vec(Ctx &c) { return AmgVec{c.n, c.mask, c.partials, c.counter, c.sc}; }
 
+template <int MODE, typename O, int L>
+static void k0_launch_l(Ctx &c, float omega, const float *x, const float *b, O *out, const CgScalars *sc)
+{
+    const int g = grid_for(c, (long long)c.n * L);
+    k_amg_k0<MODE, O, L><<<g, ATPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.mask,
+                                                   reinterpret_cast<const __half *>(c.Kh), c.kh_scale, c.Pinv_f,
+                                                   omega, x, b, out, sc);
+}
+
+// level-0 pass with the autotuner's lanes per block row (tune.smooth_variant)
+template <int MODE, typename O>
+static void k0_launch_m(Ctx &c, float omega, const float *x, const float *b, O *out, const CgScalars *sc)
+{
+    switch (c.tune.smooth_variant) {
+    case 1:
+        k0_launch_l<MODE, O, 8>(c, omega, x, b, out, sc);
+        break;
+    case 2:
+        k0_launch_l<MODE, O, 4>(c, omega, x, b, out, sc);
+        break;
+    default:
+        k0_launch_l<MODE, O, 16>(c, omega, x, b, out, sc);
+    }
+}
+
 template <typename O>
 static void k0_launch(Ctx &c, int mode, float omega, const float4 *xv, const float4 *bv, O *out)
 {
-    const int g = grid_for(c, (long long)c.n * L0_LANES);
     const float *x = (const float *)xv, *b = (const float *)bv;
-    const __half *kh = reinterpret_cast<const __half *>(c.Kh);
     if (mode == SM_SMOOTH)
-        k_amg_k0<SM_SMOOTH, O><<<g, ATPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.mask, kh, c.kh_scale,
-                                                          c.Pinv_f, omega, x, b, out, c.sc);
+        k0_launch_m<SM_SMOOTH, O>(c, omega, x, b, out, c.sc);
     else
-        k_amg_k0<SM_RESID, O><<<g, ATPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.mask, kh, c.kh_scale,
-                                                         c.Pinv_f, omega, x, b, out, c.sc);
+        k0_launch_m<SM_RESID, O>(c, omega, x, b, out, c.sc);
+}
+
+// one residual pass on the scratch vectors without the solve's early exit,
+// for the autotuner's timing
+void launch_amg_smoother_pass(Ctx &c)
+{
+    k0_launch_m<SM_RESID, float>(c, 1.0f, (const float *)c.x_f, (const float *)c.r_f, (float *)c.q_f, nullptr);
 }
 
 __global__ void k_to_float(long long count, const double *__restrict__ in, float *__restrict__ out)

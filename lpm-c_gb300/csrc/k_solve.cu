@@ -338,21 +338,23 @@ __global__ void __launch_bounds__(VTPB) k_row_sums(int n, const long long *__res
     }
 }
 
-// y = mask(K32 x) in the difference form from x = hi + lo; 16 lanes per
-// block row, four blocks per lane (the layout of k_spmv's default variant).
-// DOT: p.y with p = x64 (FP64) and alpha = rz / (p.y), as k_spmv.
-template <bool DOT>
+// y = mask(K32 x) in the difference form from x = hi + lo; L lanes per
+// block row, four blocks per lane (the layouts of k_spmv's variants, chosen
+// by the autotuner).  DOT: p.y with p = x64 (FP64) and alpha = rz / (p.y), as
+// k_spmv.
+template <bool DOT, int L = 16>
 __global__ void __launch_bounds__(VTPB) k_spmv_diff(SpmvArgs a, const float *__restrict__ val,
                                                     const float *__restrict__ rs,
                                                     const SplitRec *__restrict__ split,
                                                     const dvec4 *__restrict__ x64, dvec4 *__restrict__ y)
 {
+    static_assert(L == 4 || L == 8 || L == 16, "lanes per row");
     if (DOT && a.sc->done)
         return;
-    const int sub = threadIdx.x & 15;
-    const unsigned gmask = 0xffffu << ((threadIdx.x & 31) & ~15);
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 4;
-    const int nhw = (gridDim.x * blockDim.x) >> 4;
+    const int sub = threadIdx.x & (L - 1);
+    const unsigned gmask = ((1u << L) - 1u) << ((threadIdx.x & 31) & ~(L - 1));
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) / L;
+    const int nhw = (gridDim.x * blockDim.x) / L;
     const int n = a.n;
     double dot = 0.0;
     for (int row = gw; row < n; row += nhw) {
@@ -362,7 +364,7 @@ __global__ void __launch_bounds__(VTPB) k_spmv_diff(SpmvArgs a, const float *__r
         const SplitRec own = split[row];
         const float4 hi_i = own.hi, lo_i = own.lo;
         float y0 = 0.f, y1 = 0.f, y2 = 0.f;
-        for (int b0 = 4 * sub; b0 < np; b0 += 64) {
+        for (int b0 = 4 * sub; b0 < np; b0 += 4 * L) {
             int cc[4];
             load_cols<4>(a.cols + off + b0, cc);
             float v[9][4];
@@ -386,7 +388,7 @@ __global__ void __launch_bounds__(VTPB) k_spmv_diff(SpmvArgs a, const float *__r
             }
         }
 #pragma unroll
-        for (int o = 8; o > 0; o >>= 1) {
+        for (int o = L / 2; o > 0; o >>= 1) {
             y0 += __shfl_xor_sync(gmask, y0, o);
             y1 += __shfl_xor_sync(gmask, y1, o);
             y2 += __shfl_xor_sync(gmask, y2, o);
@@ -924,14 +926,31 @@ void launch_row_sums(Ctx &c)
     k_row_sums<<<spmv_grid(c), VTPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.Kf, c.Krs);
 }
 
+template <bool DOT>
+static void spmv_diff_variant(Ctx &c, const SpmvArgs &a, dvec4 *y)
+{
+    const SplitRec *sp = reinterpret_cast<const SplitRec *>(c.p_split);
+    const int g = spmv_grid(c);
+    switch (c.tune.spmv_variant) {
+    case 1:
+        k_spmv_diff<DOT, 8><<<g, VTPB, 0, c.stream>>>(a, c.Kf, c.Krs, sp, c.p_d, y);
+        break;
+    case 3:
+        k_spmv_diff<DOT, 4><<<g, VTPB, 0, c.stream>>>(a, c.Kf, c.Krs, sp, c.p_d, y);
+        break;
+    default:  // 0, and 2 (whose 32 lanes x 2 blocks has no difference-form counterpart)
+        k_spmv_diff<DOT, 16><<<g, VTPB, 0, c.stream>>>(a, c.Kf, c.Krs, sp, c.p_d, y);
+    }
+}
+
 void launch_spmv_diff(Ctx &c, dvec4 *y, bool dot)
 {
     SpmvArgs a = spmv_args(c);
     record_timing(c, c.ev_a);
     if (dot)
-        k_spmv_diff<true><<<spmv_grid(c), VTPB, 0, c.stream>>>(a, c.Kf, c.Krs, reinterpret_cast<const SplitRec *>(c.p_split), c.p_d, y);
+        spmv_diff_variant<true>(c, a, y);
     else
-        k_spmv_diff<false><<<spmv_grid(c), VTPB, 0, c.stream>>>(a, c.Kf, c.Krs, reinterpret_cast<const SplitRec *>(c.p_split), c.p_d, y);
+        spmv_diff_variant<false>(c, a, y);
     record_timing(c, c.ev_b);
 }
 

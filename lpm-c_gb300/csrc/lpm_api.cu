@@ -2511,6 +2511,8 @@ static void fill_tuning(const Ctx &c, lpm_tuning *t)
     t->spmv_blocks = spmv_variant_blocks(c.tune.spmv_variant);
     t->spmv_per_sm = c.tune.spmv_per_sm;
     t->cg_per_sm = c.tune.vec_per_sm;
+    t->smooth_lanes = c.tune.smooth_variant == 1 ? 8 : (c.tune.smooth_variant == 2 ? 4 : 16);
+    t->smooth_ms = 0.0;
 }
 
 }  // namespace lpm
@@ -2551,9 +2553,16 @@ int lpm_autotune(lpm_ctx *ctx, lpm_tuning *out)
     const bool vec64 = !k32 || c.nspec > 0 || c.opts.mixed_vectors == 64 || c.vec64_fallback;
     const bool timed = c.time_spmv;
     c.time_spmv = false;
+    // the multigrid path's products: the difference form under mixed
+    // precision, and the level-0 smoother in either precision
+    const bool amg = c.opts.preconditioner == LPM_PRECOND_AMG && c.nspec == 0 && c.amg && c.Kh &&
+                     c.kh_version == c.kf_version;
+    const bool diff = amg && k32 && c.krs_version == c.kf_version;
     auto spmv = [&]() {
         if (!k32)
             launch_spmv_d(c, c.p_d, c.q_d, true, false);
+        else if (diff)
+            launch_spmv_diff(c, c.q_d, false);
         else if (vec64)
             launch_spmv_fx(c, c.p_d, c.q_d, true, false);
         else
@@ -2596,6 +2605,20 @@ int lpm_autotune(lpm_ctx *ctx, lpm_tuning *out)
                 best.spmv_per_sm = g;
             }
         }
+    double best_smooth = 0.0;
+    if (amg && !rc) {
+        best_smooth = 1e30;
+        for (int v = 0; v < 3 && !rc; v++) {
+            c.tune.smooth_variant = v;
+            double ms = 0.0;
+            if ((rc = time_it([&]() { launch_amg_smoother_pass(c); }, ms)))
+                break;
+            if (ms < best_smooth) {
+                best_smooth = ms;
+                best.smooth_variant = v;
+            }
+        }
+    }
     double best_vec = 1e30;
     for (int g : grids) {
         if (rc)
@@ -2622,6 +2645,7 @@ int lpm_autotune(lpm_ctx *ctx, lpm_tuning *out)
         fill_tuning(c, out);
         out->spmv_ms = best_ms;
         out->spmv_ms_default = def_ms;
+        out->smooth_ms = best_smooth;
     }
     return sync(c);
 }

@@ -194,6 +194,7 @@ struct BatchHost {
 // spmv_variant: 0 = 16 lanes x 4 blocks per row chunk, 1 = 8 x 4, 2 = 32 x 2,
 // 3 = 4 x 4 (lanes per block row x consecutive blocks per lane).
 struct Tune {
+    int smooth_variant = 0;  // multigrid level-0 smoother: 16 (0), 8 (1) or 4 (2) lanes per block row
     int spmv_variant = 0;
     int spmv_per_sm = 8;  // SpMV thread blocks per SM (grid-stride over rows)
     int vec_per_sm = 8;   // PCG vector-kernel thread blocks per SM
@@ -395,6 +396,7 @@ void launch_amg_init(Ctx &c, const dvec4 *b, double scale, double delta2, bool k
 void launch_amg_iter(Ctx &c, bool k32);
 void launch_amg_reliable(Ctx &c, const dvec4 *rtrue);  // r = rtrue (masked), z, rz; p kept
 void launch_amg_vcycle(Ctx &c, const dvec4 *r, dvec4 *z);  // z = V(r), FP32 inside (Kf, Pinv_f, x_f/q_f/r_f)
+void launch_amg_smoother_pass(Ctx &c);  // one level-0 residual pass on scratch vectors (autotuner timing)
 void launch_amg_stiffness32(Ctx &c);  // Kf = (float) Kd, for the smoother under FP64 precision
 void launch_amg_stiffness16(Ctx &c);  // Kh = half(Kf / s), s = max |Kf| / 2^14 into kh_scale
 void launch_stiffness64_of32(Ctx &c); // Kd = (double) Kf, exactly

@@ -65,7 +65,7 @@ class Tuning(C.Structure):
     """lpm_tuning: launch shapes of the solve (include/lpm_gpu.h)."""
     _fields_ = [("spmv_variant", C.c_int), ("spmv_lanes", C.c_int), ("spmv_blocks", C.c_int),
                 ("spmv_per_sm", C.c_int), ("cg_per_sm", C.c_int), ("spmv_ms", C.c_double),
-                ("spmv_ms_default", C.c_double)]
+                ("spmv_ms_default", C.c_double), ("smooth_lanes", C.c_int), ("smooth_ms", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
