@@ -60,9 +60,10 @@ def test_amg_fewer_iterations_same_answer(gpu_lib, precision):
     assert cg_amg * 5 < cg_bj, (cg_amg, cg_bj)
 
 
-def test_amg_fcc_cp(gpu_lib):
+@pytest.mark.parametrize("precision", [0, 1])
+def test_amg_fcc_cp(gpu_lib, precision):
     """FCC 4^3 cells, crystal plasticity: multigrid and block-Jacobi PCG
-    give the same converged steps."""
+    give the same converged steps, in FP64 and in mixed precision."""
     G = gpu_lib
     case = cases.FCCCase(ncell=4)
     out = []
@@ -73,7 +74,7 @@ def test_amg_fcc_cp(gpu_lib):
         s.set_cp(*case.cp)
         s.set_material(np.full(n, case.C11), np.full(n, case.C12), np.full(n, case.C44), 0.0, 0.0, 0.0, G.PL_CP)
         s.init_state()
-        s.set_solver(precision=0, newton_tol=1e-10, newton_maxiter=300, cg_rtol=1e-10, preconditioner=pc)
+        s.set_solver(precision=precision, newton_tol=1e-10, newton_maxiter=300, cg_rtol=1e-10, preconditioner=pc)
         x0 = s.get("xyz")
         for stp in case.schedule[:4]:
             st = s.load_step(cases.sc_bcs(stp))

@@ -10,20 +10,13 @@ sum runs in a different order and with CUDA's exp).  The order of bonds
 within one brittle pass is not compared: equal-strain bonds swap places there
 under round-off-level differences of the solution, in the reference too.
 """
-import os
-
 import numpy as np
 import pytest
 
 import cases
 from test_oracle_damage import _brittle, _ductile
 
-# These tests have not yet run on a GPU.  Until they have, they run only when
-# LPM_UNVERIFIED_GPU_TESTS=1, so that an unverified test cannot stop a
-# fail-fast GPU run before the parity tests.
-pytestmark = [pytest.mark.gpu,
-              pytest.mark.skipif(os.environ.get("LPM_UNVERIFIED_GPU_TESTS") != "1",
-                                 reason="not yet run on a GPU (set LPM_UNVERIFIED_GPU_TESTS=1)")]
+pytestmark = [pytest.mark.gpu, pytest.mark.gpu_last]
 
 # Both sides converge to 1e-9: the converged displacements are then within
 # 2e-9 of the 1e-10 solution (measured on the oracle), while 1e-10 sits at the

@@ -5,10 +5,12 @@ still converges to the same Newton tolerance.
 How close the two answers can be: both runs stop once the out-of-balance force
 is at most newton_tol times the step's reference norm, so each is off the
 exact equilibrium by up to about newton_tol / (1 - rho) relative, where rho is
-the per-iteration contraction of modified Newton with the elastic tangent.  In
-the plastic range rho is about 0.99 on this plate (the elastic tangent
-overestimates the plastic stiffness a hundredfold), which gives 1e-6 for
-newton_tol = 1e-8.  A GB300 run measured 1.8e-7 at eta_max = 0.1."""
+the per-iteration contraction of modified Newton with the elastic tangent, and
+the two runs by up to twice that.  rho is measured on the exact-solve run
+(the residual drop per Newton iteration of its slowest step): about 0.99 and
+more in the plastic range of this plate, where the elastic tangent
+overestimates the plastic stiffness a hundredfold.  GB300 runs measured
+1.8e-7 at eta_max = 0.1 and 2.1e-6 at eta_max = 0.5."""
 import numpy as np
 import pytest
 
@@ -17,7 +19,6 @@ import cases
 pytestmark = [pytest.mark.gpu, pytest.mark.gpu_option]
 
 NEWTON_TOL = 1e-8
-RHO_PLASTIC = 0.99  # modified-Newton contraction per iteration in the plastic range
 
 
 def _plate_run(G, forcing):
@@ -31,21 +32,29 @@ def _plate_run(G, forcing):
     s.init_state()
     s.set_solver(precision=0, newton_tol=NEWTON_TOL, newton_maxiter=5000, cg_rtol=1e-10, cg_forcing=forcing)
     cg = newton = 0
+    rho = 0.0
     for bcs in plate.step_bcs():
         st = s.load_step(bcs)
         assert st["status"] == 0, st
         cg += st["cg_iters"]
         newton += st["newton_iters"]
-    return s.get("xyz") - s.get("xyz_initial"), cg, newton, s.get("J2_alpha")
+        if st["newton_iters"] > 0 and st["res_final"] > 0.0:
+            rho = max(rho, (st["res_final"] / st["res0"]) ** (1.0 / st["newton_iters"]))
+    out = s.get("xyz") - s.get("xyz_initial"), cg, newton, s.get("J2_alpha"), rho
+    s.close()
+    return out
 
 
 @pytest.mark.parametrize("forcing", [0.1, 0.5])
 def test_forcing_same_answer_fewer_pcg_iterations(gpu_lib, forcing):
-    du0, cg0, nt0, a0 = _plate_run(gpu_lib, 0.0)
-    du1, cg1, nt1, a1 = _plate_run(gpu_lib, forcing)
+    du0, cg0, nt0, a0, rho = _plate_run(gpu_lib, 0.0)
+    du1, cg1, nt1, a1, _ = _plate_run(gpu_lib, forcing)
     assert a0.max() > 0.0  # plastic
+    assert 0.9 < rho < 1.0, rho
     err = np.abs(du1 - du0).max() / np.abs(du0).max()
-    bound = NEWTON_TOL / (1.0 - RHO_PLASTIC)
+    bound = 2.0 * NEWTON_TOL / (1.0 - rho)
+    print(f"\nforcing {forcing}: displacement difference {err:.3e}, bound {bound:.3e} (rho {rho:.4f}), "
+          f"PCG iterations {cg0} -> {cg1}")
     assert err < bound, (err, bound)
     assert np.abs(a1 - a0).max() <= bound * a0.max()
     assert cg1 * 3 < cg0, (cg0, cg1, nt0, nt1)
