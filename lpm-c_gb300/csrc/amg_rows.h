@@ -150,11 +150,19 @@ AMG_HD void pinv_apply(const PT *P, int n, int i, const T (&r)[3], T (&d)[3])
                (T)P[(size_t)(3 * a + 2) * n + i] * r[2];
 }
 
-// Level-0 epilogue of row `row` given K x (y): SM_RESID out = mask(b - y);
-// SM_SMOOTH out = mask(x + omega Pinv mask(b - y)).
-template <typename T, typename PT, typename O>
-AMG_HD void k0_epilogue(int mode, int n, int row, uint8_t m, const PT *Pinv, T omega, const T *x, const T *b,
-                        O *out, T y0, T y1, T y2)
+// d = P r with the row's 3x3 block inverse in registers (row-major)
+template <typename T>
+AMG_HD void pinv_apply9(const T (&P)[9], const T (&r)[3], T (&d)[3])
+{
+    for (int a = 0; a < 3; a++)
+        d[a] = P[3 * a] * r[0] + P[3 * a + 1] * r[1] + P[3 * a + 2] * r[2];
+}
+
+// Level-0 epilogue of row `row` given K x (y) and the row's block inverse P:
+// SM_RESID out = mask(b - y); SM_SMOOTH out = mask(x + omega P mask(b - y)).
+template <typename T, typename O>
+AMG_HD void k0_epilogue(int mode, int row, uint8_t m, const T (&P)[9], T omega, const T *x, const T *b, O *out,
+                        T y0, T y1, T y2)
 {
     T b0, b1, b2;
     load_xyz<T>(b + 4 * (size_t)row, b0, b1, b2);
@@ -164,7 +172,7 @@ AMG_HD void k0_epilogue(int mode, int n, int row, uint8_t m, const PT *Pinv, T o
         store_xyz<T>(o, r[0], r[1], r[2]);
     } else {
         T d[3];
-        pinv_apply<T, PT>(Pinv, n, row, r, d);
+        pinv_apply9<T>(P, r, d);
         T x0, x1, x2;
         load_xyz<T>(x + 4 * (size_t)row, x0, x1, x2);
         store_xyz<T>(o, (m & 1) ? x0 + omega * d[0] : T(0), (m & 2) ? x1 + omega * d[1] : T(0),

@@ -262,7 +262,7 @@ template <int MODE, typename O, int L0_LANES = 16>
 __global__ void __launch_bounds__(ATPB) k_amg_k0(int n, const long long *__restrict__ rowoff,
                                                  const int *__restrict__ npad, const int *__restrict__ cols,
                                                  const uint8_t *__restrict__ mask, const __half *__restrict__ val,
-                                                 const float *__restrict__ kscale, const float *__restrict__ Pinv,
+                                                 const float *__restrict__ kscale, const float *__restrict__ Prow,
                                                  float omega, const float *__restrict__ x,
                                                  const float *__restrict__ b, O *__restrict__ out,
                                                  const CgScalars *sc)
@@ -283,8 +283,21 @@ __global__ void __launch_bounds__(ATPB) k_amg_k0(int n, const long long *__restr
             y1 += __shfl_xor_sync(gmask, y1, o);
             y2 += __shfl_xor_sync(gmask, y2, o);
         }
+        // the row's block inverse ([n][9], 36 contiguous bytes): one value per
+        // lane, then to lane 0
+        float P[9];
+        if constexpr (L0_LANES >= 9) {
+            const float pv = sub < 9 ? Prow[(size_t)row * 9 + sub] : 0.f;
+#pragma unroll
+            for (int k = 0; k < 9; k++)
+                P[k] = __shfl_sync(gmask, pv, k, L0_LANES);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 9; k++)
+                P[k] = Prow[(size_t)row * 9 + k];
+        }
         if (sub == 0)
-            k0_epilogue<float, float, O>(MODE, n, row, mask[row], Pinv, omega, x, b, out, s * y0, s * y1, s * y2);
+            k0_epilogue<float, O>(MODE, row, mask[row], P, omega, x, b, out, s * y0, s * y1, s * y2);
     }
 }
 
@@ -392,7 +405,7 @@ static void k0_launch_l(Ctx &c, float omega, const float *x, const float *b, O *
 {
     const int g = grid_for(c, (long long)c.n * L);
     k_amg_k0<MODE, O, L><<<g, ATPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.mask,
-                                                   reinterpret_cast<const __half *>(c.Kh), c.kh_scale, c.Pinv_f,
+                                                   reinterpret_cast<const __half *>(c.Kh), c.kh_scale, c.Pinv_rf,
                                                    omega, x, b, out, sc);
 }
 

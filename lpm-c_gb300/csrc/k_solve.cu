@@ -299,7 +299,7 @@ __device__ __forceinline__ void split_store(const dvec4 &v, float4 *rec)
     *reinterpret_cast<SplitRec *>(rec) = s;
 }
 
-// Krs[k][row] = sum over the row's blocks of component k of Kf (FP64 sums,
+// Krs[row][k] = sum over the row's blocks of component k of Kf (FP64 sums,
 // rounded once); 16 lanes per block row, four blocks per lane per load.
 __global__ void __launch_bounds__(VTPB) k_row_sums(int n, const long long *__restrict__ rowoff,
                                                    const int *__restrict__ npad, const float *__restrict__ val,
@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(VTPB) k_row_sums(int n, const long long *__res
         if (sub == 0) {
 #pragma unroll
             for (int k = 0; k < 9; k++)
-                out[(size_t)k * n + row] = (float)s[k];
+                out[(size_t)row * 9 + k] = (float)s[k];
         }
     }
 }
@@ -387,6 +387,22 @@ __global__ void __launch_bounds__(VTPB) k_spmv_diff(SpmvArgs a, const float *__r
                 y2 += v[6][j] * d[j][0] + v[7][j] * d[j][1] + v[8][j] * d[j][2];
             }
         }
+        // + R_i x_i (R_i is rounding-sized: hi_i suffices), its 9 values
+        // (36 contiguous bytes) spread over the lanes
+#pragma unroll
+        for (int t = 0; t < (9 + L - 1) / L; t++) {
+            const int k = sub + t * L;
+            if (k < 9) {
+                const int c = k % 3;
+                const float add = rs[(size_t)row * 9 + k] * (c == 0 ? hi_i.x : (c == 1 ? hi_i.y : hi_i.z));
+                if (k < 3)
+                    y0 += add;
+                else if (k < 6)
+                    y1 += add;
+                else
+                    y2 += add;
+            }
+        }
 #pragma unroll
         for (int o = L / 2; o > 0; o >>= 1) {
             y0 += __shfl_xor_sync(gmask, y0, o);
@@ -394,17 +410,14 @@ __global__ void __launch_bounds__(VTPB) k_spmv_diff(SpmvArgs a, const float *__r
             y2 += __shfl_xor_sync(gmask, y2, o);
         }
         if (sub == 0) {
-            // + R_i x_i (R_i is rounding-sized: hi_i suffices)
-            y0 += rs[(size_t)0 * n + row] * hi_i.x + rs[(size_t)1 * n + row] * hi_i.y + rs[(size_t)2 * n + row] * hi_i.z;
-            y1 += rs[(size_t)3 * n + row] * hi_i.x + rs[(size_t)4 * n + row] * hi_i.y + rs[(size_t)5 * n + row] * hi_i.z;
-            y2 += rs[(size_t)6 * n + row] * hi_i.x + rs[(size_t)7 * n + row] * hi_i.y + rs[(size_t)8 * n + row] * hi_i.z;
             const uint8_t m = a.mask[row];
             const double o0 = (m & 1) ? (double)y0 : 0.0, o1 = (m & 2) ? (double)y1 : 0.0,
                          o2 = (m & 4) ? (double)y2 : 0.0;
             y[row] = make_dvec4(o0, o1, o2, 0.0);
             if (DOT) {
-                const dvec4 pv = x64[row];
-                dot += pv.x * o0 + pv.y * o1 + pv.z * o2;
+                // p = hi + lo (the FP64 p to 2^-48): no second read of p
+                dot += ((double)hi_i.x + (double)lo_i.x) * o0 + ((double)hi_i.y + (double)lo_i.y) * o1 +
+                       ((double)hi_i.z + (double)lo_i.z) * o2;
             }
         }
     }

@@ -268,6 +268,16 @@ void launch_assemble(Ctx &c, bool fp32)
         k_assemble<double><<<g, STPB, 0, c.stream>>>(a, c.Kd);
 }
 
+// [9][n] -> [n][9]: the smoother reads one row's inverse as 36 contiguous bytes
+__global__ void k_rows_of(int n, const float *__restrict__ in, float *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    for (int k = 0; k < 9; k++)
+        out[(size_t)i * 9 + k] = in[(size_t)k * n + i];
+}
+
 void launch_block_jacobi(Ctx &c, bool fp32)
 {
     const int g = (c.n + STPB - 1) / STPB;
@@ -286,6 +296,8 @@ void launch_block_jacobi(Ctx &c, bool fp32)
             k_jacobi<double, float><<<g, STPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.cols, c.nconn_d, c.Kd,
                                                               c.mask, c.Pinv_f);
     }
+    if (c.opts.preconditioner == LPM_PRECOND_AMG && c.nspec == 0)
+        k_rows_of<<<g, STPB, 0, c.stream>>>(c.n, c.Pinv_f, c.Pinv_rf);
 }
 
 }  // namespace lpm

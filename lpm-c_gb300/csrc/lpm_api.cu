@@ -167,7 +167,7 @@ Ctx::~Ctx()
                     (void **)&rowoff, (void **)&npad, (void **)&cols, (void **)&Kd, (void **)&Kf,
                     (void **)&Pinv_d, (void **)&Pinv_f, (void **)&x_d, (void **)&r_d, (void **)&p_d,
                     (void **)&q_d, (void **)&z_d, (void **)&x_f, (void **)&r_f, (void **)&p_f, (void **)&q_f,
-                    (void **)&z_f, (void **)&p_split, (void **)&Krs, (void **)&Kh, (void **)&kh_scale, (void **)&kh_max, (void **)&pl_flag, (void **)&b_d, (void **)&sc, (void **)&partials, (void **)&counter,
+                    (void **)&z_f, (void **)&p_split, (void **)&Pinv_rf, (void **)&Krs, (void **)&Kh, (void **)&kh_scale, (void **)&kh_max, (void **)&pl_flag, (void **)&b_d, (void **)&sc, (void **)&partials, (void **)&counter,
                     (void **)&norms, (void **)&status};
     for (void **p : all)
         if (*p) {
@@ -324,7 +324,7 @@ static int alloc_specimen(Ctx &c)
     A_(c.W, 6 * n) A_(c.Pinv_d, 9 * n) A_(c.Pinv_f, 9 * n)
     A_(c.x_d, n) A_(c.r_d, n) A_(c.p_d, n) A_(c.q_d, n) A_(c.z_d, n) A_(c.b_d, n)
     A_(c.x_f, n) A_(c.r_f, n) A_(c.p_f, n) A_(c.q_f, n) A_(c.z_f, n)
-    A_(c.p_split, 2 * n) A_(c.Krs, 9 * n) A_(c.kh_scale, 1) A_(c.kh_max, 1)
+    A_(c.p_split, 2 * n) A_(c.Pinv_rf, 9 * n) A_(c.Krs, 9 * n) A_(c.kh_scale, 1) A_(c.kh_max, 1)
     c.krs_version = -1;
     for (int s = 0; s < 3; s++) {
         A_(c.dLp[s], nb) A_(c.alpha[s], n) A_(c.beta[s], 6 * n)

@@ -263,12 +263,13 @@ struct Ctx {
     long long kf_version = -1; // the assembly Kf holds (FP32 assembly, or the copy of Kd for the smoother)
     double *Pinv_d = nullptr; // block-Jacobi inverse, [9][n]
     float *Pinv_f = nullptr;
+    float *Pinv_rf = nullptr;  // multigrid smoother: the FP32 inverse per row, [n][9]
     // ---- solver vectors
     dvec4 *x_d = nullptr, *r_d = nullptr, *p_d = nullptr, *q_d = nullptr, *z_d = nullptr;
     float4 *x_f = nullptr, *r_f = nullptr, *p_f = nullptr, *q_f = nullptr, *z_f = nullptr;
     // the FP64 search direction split into two FP32 parts (p = hi + lo) for
     // the difference-form FP32 product, and the FP32 stiffness's block row
-    // sums [9][n] it needs (for the assembly numbered krs_version)
+    // sums [n][9] it needs (for the assembly numbered krs_version)
     float4 *p_split = nullptr;  // [2 i] = hi, [2 i + 1] = lo: one 32-byte record per particle
     float *Krs = nullptr;
     long long krs_version = -1;

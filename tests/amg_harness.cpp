@@ -64,7 +64,10 @@ static void k0(const Level0<T> &z0, const V *val, int mode, T omega, const T *x,
     for (int row = 0; row < z0.n; row++) {
         V y0 = 0, y1 = 0, y2 = 0;
         lpm::k0_row_partial<V, T>(z0.rowoff, z0.npad, z0.cols, val, x, row, 0, 1, y0, y1, y2);
-        lpm::k0_epilogue<T, T, O>(mode, z0.n, row, z0.mask[row], z0.Pinv, omega, x, b, out, (T)y0, (T)y1, (T)y2);
+        T P[9];
+        for (int k = 0; k < 9; k++)
+            P[k] = z0.Pinv[(size_t)k * z0.n + row];
+        lpm::k0_epilogue<T, O>(mode, row, z0.mask[row], P, omega, x, b, out, (T)y0, (T)y1, (T)y2);
     }
 }
 
