@@ -148,11 +148,12 @@ def solver_opts(G, case, precision, precond):
     misbehaving solve can take.  Each Newton solve of a step starts from the
     Galerkin combination of the step's last 8 solutions (recycle), in both
     precisions."""
-    return dict(precision=precision, newton_tol=case.newton_tol, newton_maxiter=100, cg_rtol=1e-10,
+    return dict(precision=precision, newton_tol=case.newton_tol, newton_maxiter=100, cg_rtol=CG_RTOL,
                 cg_maxiter=2000 if precond else 200000, preconditioner=precond, recycle=RECYCLE)
 
 
 RECYCLE = 8  # earlier solutions of the load step the Newton solves start from
+CG_RTOL = 1e-10  # relative residual of the SC workload's linear solves (--cg-rtol)
 
 
 class Deadline:
@@ -347,7 +348,7 @@ def assemble_line(args, case, partial, world, note=None):
            "particles": mixed.get("n"), "nnz_blocks": mixed.get("nnzb"), "precision": "mixed",
            "preconditioner": precond_name,
            "newton": "modified Newton with the elastic tangent of the step (src/lpmc_project.c:382-471), "
-                     "tolerance 1e-8, MAXITER 100; linear solves to 1e-10 relative, each started from the "
+                     f"tolerance 1e-8, MAXITER 100; linear solves to {CG_RTOL:g} relative, each started from the "
                      f"Galerkin combination of the step's last {RECYCLE} solutions (both precisions)",
            "fp64_steps_per_s": fp64_rate, "mixed_over_fp64": (value / fp64_rate) if (value and fp64_rate) else None,
            **errs,
@@ -491,8 +492,9 @@ def run_e2e(args, case, precond, deadline):
 # that solve accuracy (profiles/sc100_cyclic_steps.md).
 NEWTON_PER_STEP_SC100 = [3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 8, 80, 88, 100, 100, 100, 100, 100, 100, 3, 3, 3, 3, 3]
 # Block-Jacobi PCG iterations per Newton iteration at SC 100^3 (FP64, to
-# 1e-10 relative), measured on a GB300 over steps 4-8: 28,433 iterations in
-# 15 solves (profiles/sc100_cyclic_steps.md).
+# 1e-8 relative, the tolerance of the reference's solverCG,
+# src/solver.c:221), measured on a GB300 over steps 4-8: 28,433 iterations
+# in 15 solves (profiles/sc100_cyclic_steps.md).
 CG_PER_NEWTON_SC100 = 1895.5
 
 
@@ -862,9 +864,17 @@ def main():
                     help="sc workload: wall seconds from start within which the arms must fit")
     ap.add_argument("--grace", type=float, default=200.0,
                     help="sc workload: the watchdog prints the line measured so far at budget + grace")
+    ap.add_argument("--cg-rtol", type=float, default=CG_RTOL,
+                    help="sc workload: relative residual of the linear solves (the reference's solverCG "
+                         "stops at 1e-8, src/solver.c:221)")
+    ap.add_argument("--recycle", type=int, default=RECYCLE,
+                    help="earlier solutions of the load step each Newton solve starts from (0: from zero, "
+                         "as the reference's solverCG)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    globals()["CG_RTOL"] = args.cg_rtol
+    globals()["RECYCLE"] = args.recycle
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batch":

@@ -33,6 +33,7 @@ extern "C" {
 #define LPM_STATUS_CG_MAXIT 2     /* a linear solve stopped at its iteration cap */
 #define LPM_STATUS_NAN 4          /* a residual norm was not finite */
 #define LPM_STATUS_CP_SINGULAR 8  /* singular slip-system Jacobian (reference exits) */
+#define LPM_STATUS_DEVICE_WAIT 16 /* a bounded device-side wait ran out (streamed product); the solve stopped */
 
 #define LPM_PREC_FP64 0  /* FP64 stiffness, SpMV and PCG */
 #define LPM_PREC_MIXED 1 /* FP32 stiffness/SpMV/PCG inside FP64 iterative refinement */
@@ -207,6 +208,15 @@ int lpm_set_damage(lpm_ctx *ctx, const lpm_damage_opts *opts);
  * reference writes them to its bond file.  pairs may be NULL to query the
  * count; otherwise it holds 2 * capacity ints. */
 int lpm_damage_log(lpm_ctx *ctx, int *pairs, int capacity, int *count);
+/* main's damage stage one function at a time, for the reference-named
+ * drop-in: lpm_damage_update is updateDamageGeneral (src/constitutive.c:149-164)
+ * on the context's current state for its plmode (ductile nonlocal damage for
+ * J2, :1757-1862; brittle bond breaking for elastic bonds, :1437-1527;
+ * nothing for crystal plasticity), *broken its return value, the broken
+ * bonds appended to lpm_damage_log; lpm_damage_crack is updateCrack
+ * (:1399-1434).  Both need the damage stage on (lpm_set_damage). */
+int lpm_damage_update(lpm_ctx *ctx, int *broken);
+int lpm_damage_crack(lpm_ctx *ctx);
 /* The brittle pass's choice (updateBrittleDamage, src/constitutive.c:1471-1520)
  * among k candidate bonds b = slot * n + particle, given in any order with
  * their bond strains: scan order, then, above nbreak candidates, the
@@ -236,8 +246,10 @@ int lpm_begin_step(lpm_ctx *ctx);
  *   dispBC_index (3n, int32), type (n, int32), conn (n x 61, int32), nb_conn (n),
  *   cp_gy (n x nslip), cp_A (n), cp_A_single (n x nslip), J2_dlambda (n);
  *   with the damage stage on: damage_broken, damage_w, damage_D (n x nn,
- *   converged), damage_nonlocal (n, converged), damage_visual (n),
- *   nb_current (n, int32: intact bonds; nb stays nb_initial). */
+ *   converged), damage_D0 (n x nn, current), damage_nonlocal (n, converged),
+ *   damage_nonlocal0 (n, current), damage_visual (n), nb_current (n, int32:
+ *   intact bonds; nb stays nb_initial); damage_visual and nb_current are
+ *   read-only. */
 int lpm_get(lpm_ctx *ctx, const char *name, void *dst, size_t bytes);
 int lpm_set(lpm_ctx *ctx, const char *name, const void *src, size_t bytes);
 int lpm_get_sizes(const lpm_ctx *ctx, int *n, int *nn, int *nslip, long long *nnz_blocks);
@@ -271,6 +283,9 @@ typedef struct lpm_tuning {
     double spmv_ms_default;/* lpm_autotune: time of the default shape (0, 8, 8) */
     int smooth_lanes;      /* output: lanes per block row of the multigrid level-0 smoother (16, 8, 4) */
     double smooth_ms;      /* lpm_autotune: time of one smoother pass in the chosen shape (0: not tuned) */
+    int diff_stream;       /* mixed multigrid PCG: difference-form product fed by registers (0) or
+                              streamed through shared memory by the bulk-copy engine with 1 or 2
+                              thread blocks per SM (1, 2); same arithmetic per row */
 } lpm_tuning;
 /* Time every SpMV shape (and vector-kernel grid) on the context's current
  * stiffness with CUDA events and keep the fastest.  Needs an assembled

@@ -66,14 +66,24 @@ void computeBondForceIncrementalUpdating(int ii);
 /* src/constitutive.c:689, :286: not on the GPU path (exit with a message) */
 void computeBondForceJ2nonlinearIso(int ii);
 void computeBondForceJ2energyReturnMap(int ii, int load_indicator);
-/* src/constitutive.c:149-164, :1399-1862: damage is not modelled on the GPU
- * path; these return 0 broken bonds and leave the state unchanged. */
+/* src/constitutive.c:149-164 (include/constitutive.h:22-27): main's damage
+ * update on the GPU damage stage (lpm_damage_update), which the first damage
+ * call switches on with the globals damage_L, damage_threshold, damagec_A,
+ * critical_bstrain and nbreak: ductile nonlocal damage for plmode 0, brittle
+ * bond breaking for plmode 6 (the global nbreak; a different nbreak argument
+ * of updateBrittleDamage is not applied), 0 for crystal plasticity.  Reads and
+ * writes damage_broken, damage_w, damage_D[.][.][0], damage_nonlocal[.][0];
+ * appends the broken bonds to dataName in the reference's format. */
 int updateDamageGeneral(const char *dataName, int tstep, int plmode);
 int updateBrittleDamage(const char *dataName, int tstep, int nbreak);
+int updateDuctileDamagePwiseNonlocal(const char *dataName, int tstep);
+/* src/constitutive.c:1529-1756: models main does not select; not on the GPU
+ * path (exit with a message) */
 int updateDuctileDamageBwiseLocal(const char *dataName, int tstep);
 int updateDuctileDamagePwiseLocal(const char *dataName, int tstep);
 int updateDuctileDamageBwiseNonlocal(const char *dataName, int tstep);
-int updateDuctileDamagePwiseNonlocal(const char *dataName, int tstep);
+/* src/constitutive.c:1399-1434 (include/constitutive.h:29): F scaled by
+ * damage_w, Pin, nb, damage_visual, fix_index of particles without bonds */
 void updateCrack(void);
 
 /* src/boundary.c:12, :48 (include/boundary.h:13-14) */

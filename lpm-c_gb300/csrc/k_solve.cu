@@ -431,6 +431,256 @@ __global__ void __launch_bounds__(VTPB) k_spmv_diff(SpmvArgs a, const float *__r
     }
 }
 
+// ---- streamed difference-form product ---------------------------------------
+// The product of k_spmv_diff<DOT, 16> (the same lanes, blocks and arithmetic
+// per row) with the stiffness stream decoupled from the gathers.  One CTA
+// per SM (or two) walks tiles of STREAM_ROWS consecutive rows, whose row
+// offsets, column indices and values are contiguous in the block-CSR arrays.
+// Thread 0 copies a tile into a ring of shared-memory stages with
+// cp.async.bulk, completing on the stage's mbarrier by byte count, up to
+// stages - 1 tiles ahead of the computation; every warp computes two rows of
+// the tile from shared memory (a half-warp per row) and gathers the split x
+// from L2.  The copy engine keeps the DRAM stream deep with no registers
+// held, where the register-fed kernel is limited to the loads its resident
+// warps have issued.
+//
+// Every mbarrier wait is bounded (STREAM_WAIT_CYCLES, about a second); one
+// that runs out sets LPM_STATUS_DEVICE_WAIT in the status word and ends the
+// kernel once the copies it issued have landed (again with bounded waits);
+// the CG stops (done = 3) after the kernel's dot product.
+constexpr int STREAM_ROWS = 16;  // 8 warps x 2 half-warps
+constexpr long long STREAM_WAIT_CYCLES = 2000000000LL;
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// wait for the completion of the barrier's phase of the given parity;
+// false after STREAM_WAIT_CYCLES
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity)
+{
+    const unsigned a = smem_u32(bar);
+    const long long t0 = clock64();
+    for (;;) {
+        unsigned ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (ok)
+            return true;
+        if (clock64() - t0 > STREAM_WAIT_CYCLES)
+            return false;
+    }
+}
+
+// global -> shared copy by the bulk-copy engine, completing on bar (both
+// addresses 16-byte aligned, size a multiple of 16)
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// A stage: the tile's 18 row offsets (144 B, rows r0 .. r0 + 17; the row
+// offset array is padded so the last tile's copy stays inside it), its
+// column indices at cols_off and its values at vals_off.
+struct StreamLayout {
+    int stages, stage_bytes, cols_off, vals_off;
+};
+
+template <bool DOT>
+__global__ void __launch_bounds__(VTPB, 1)
+    k_spmv_diff_stream(SpmvArgs a, StreamLayout lay, const float *__restrict__ val, const float *__restrict__ rs,
+                       const SplitRec *__restrict__ split, dvec4 *__restrict__ y, int *status)
+{
+    extern __shared__ __align__(128) unsigned char stage_mem[];
+    __shared__ unsigned long long full[STREAM_MAX_STAGES], empty[STREAM_MAX_STAGES];
+    __shared__ volatile int abort_k;
+    if (DOT && a.sc->done)
+        return;
+    const int n = a.n, S = lay.stages;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int sub = lane & 15, rl = 2 * wid + (lane >> 4);  // row of the tile
+    const unsigned gmask = 0xffffu << (lane & 16);
+    const int ntiles = (n + STREAM_ROWS - 1) / STREAM_ROWS;
+    const int mine = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < S; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], VTPB / 32);
+        }
+        abort_k = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    auto first_row = [&](int i) { return ((int)blockIdx.x + i * (int)gridDim.x) * STREAM_ROWS; };
+    auto fail = [&]() {
+        atomicOr(status, LPM_STATUS_DEVICE_WAIT);
+        abort_k = 1;
+    };
+    // warp 0 issues the copies; its lanes hold the block range [pb0, pb1) of
+    // the tiles jb + lane, loaded 32 tiles at a time
+    int issued = 0, jb = -32;
+    long long pb0 = 0, pb1 = 0;
+    auto issue_next = [&]() -> bool {  // warp 0, warp-uniform
+        const int j = issued, s = j % S;
+        if (j - jb >= 32) {
+            jb += 32;
+            if (jb + lane < mine) {
+                const int r0 = first_row(jb + lane);
+                pb0 = a.rowoff[r0];
+                pb1 = a.rowoff[min(r0 + STREAM_ROWS, n)];
+            }
+        }
+        const long long b0 = __shfl_sync(0xffffffffu, pb0, j - jb);
+        const long long b1 = __shfl_sync(0xffffffffu, pb1, j - jb);
+        if (j >= S && !mbar_wait(&empty[s], (unsigned)((j / S) - 1) & 1u))
+            return false;
+        if (lane == 0) {
+            unsigned char *st = stage_mem + (size_t)s * lay.stage_bytes;
+            const unsigned nb = (unsigned)(b1 - b0);
+            mbar_expect_tx(&full[s], 144u + 40u * nb);
+            bulk_g2s(st, a.rowoff + first_row(j), 144u, &full[s]);
+            if (nb) {
+                bulk_g2s(st + lay.cols_off, a.cols + b0, 4u * nb, &full[s]);
+                bulk_g2s(st + lay.vals_off, val + 9 * b0, 36u * nb, &full[s]);
+            }
+        }
+        __syncwarp();
+        issued++;
+        return true;
+    };
+    if (wid == 0) {
+        while (issued < mine && issued < S - 1)
+            issue_next();
+    }
+    double dot = 0.0;
+    int i = 0;
+    for (; i < mine; i++) {
+        if (abort_k)
+            break;
+        if (wid == 0 && issued < mine && !issue_next()) {
+            fail();
+            break;
+        }
+        const int s = i % S;
+        const int row = first_row(i) + rl;
+        // the row's own entries, ahead of the stage wait
+        SplitRec own = {};
+        float rsv = 0.f;
+        uint8_t m = 0;
+        if (row < n) {
+            own = split[row];
+            if (sub < 9)
+                rsv = rs[(size_t)row * 9 + sub];
+            if (sub == 0)
+                m = a.mask[row];
+        }
+        if (!mbar_wait(&full[s], (unsigned)(i / S) & 1u)) {
+            fail();
+            break;
+        }
+        if (row < n) {
+            const unsigned char *st = stage_mem + (size_t)s * lay.stage_bytes;
+            const long long *ro = reinterpret_cast<const long long *>(st);
+            const int o = (int)(ro[rl] - ro[0]), np = (int)(ro[rl + 1] - ro[rl]);
+            const int *cs = reinterpret_cast<const int *>(st + lay.cols_off) + o;
+            const float *vr = reinterpret_cast<const float *>(st + lay.vals_off) + 9 * (size_t)o;
+            const float4 hi_i = own.hi, lo_i = own.lo;
+            float y0 = 0.f, y1 = 0.f, y2 = 0.f;
+            for (int b0 = 4 * sub; b0 < np; b0 += 64) {
+                const int4 c4 = *reinterpret_cast<const int4 *>(cs + b0);
+                const int cc[4] = {c4.x, c4.y, c4.z, c4.w};
+                float d[4][3];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const SplitRec rj = split[cc[j]];
+                    const float4 h = rj.hi, l = rj.lo;
+                    d[j][0] = (h.x - hi_i.x) + (l.x - lo_i.x);
+                    d[j][1] = (h.y - hi_i.y) + (l.y - lo_i.y);
+                    d[j][2] = (h.z - hi_i.z) + (l.z - lo_i.z);
+                }
+                float v[9][4];
+#pragma unroll
+                for (int k = 0; k < 9; k++)
+                    unpack<4>(*reinterpret_cast<const float4 *>(vr + (size_t)k * np + b0), v[k]);
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    y0 += v[0][j] * d[j][0] + v[1][j] * d[j][1] + v[2][j] * d[j][2];
+                    y1 += v[3][j] * d[j][0] + v[4][j] * d[j][1] + v[5][j] * d[j][2];
+                    y2 += v[6][j] * d[j][0] + v[7][j] * d[j][1] + v[8][j] * d[j][2];
+                }
+            }
+            if (sub < 9) {
+                const int c = sub % 3;
+                const float add = rsv * (c == 0 ? hi_i.x : (c == 1 ? hi_i.y : hi_i.z));
+                if (sub < 3)
+                    y0 += add;
+                else if (sub < 6)
+                    y1 += add;
+                else
+                    y2 += add;
+            }
+#pragma unroll
+            for (int off = 8; off > 0; off >>= 1) {
+                y0 += __shfl_xor_sync(gmask, y0, off);
+                y1 += __shfl_xor_sync(gmask, y1, off);
+                y2 += __shfl_xor_sync(gmask, y2, off);
+            }
+            if (sub == 0) {
+                const double o0 = (m & 1) ? (double)y0 : 0.0, o1 = (m & 2) ? (double)y1 : 0.0,
+                             o2 = (m & 4) ? (double)y2 : 0.0;
+                y[row] = make_dvec4(o0, o1, o2, 0.0);
+                if (DOT)
+                    dot += ((double)hi_i.x + (double)lo_i.x) * o0 + ((double)hi_i.y + (double)lo_i.y) * o1 +
+                           ((double)hi_i.z + (double)lo_i.z) * o2;
+            }
+        }
+        __syncwarp();
+        if (lane == 0)
+            mbar_arrive(&empty[s]);
+    }
+    // after a failed wait: let the copies issued past the last consumed tile land
+    if (wid == 0) {
+        for (int k = i; k < issued; k++)
+            if (!mbar_wait(&full[k % S], (unsigned)(k / S) & 1u))
+                break;
+    }
+    if (DOT) {
+        double v[1] = {dot};
+        CgScalars *sc = a.sc;
+        grid_reduce<1>(v, a.partials, a.counter, [sc](const double *t) {
+            sc->pq = t[0];
+            sc->alpha = (t[0] != 0.0) ? sc->rz / t[0] : 0.0;
+        });
+        // stop the CG after a failed wait (every block of this persistent
+        // grid read done at its start, and all of them took part in the sum)
+        __syncthreads();
+        if (threadIdx.x == 0 && abort_k)
+            a.sc->done = 3;
+    }
+}
+
 // two consecutive stiffness values of one component as FP64 (streaming)
 __device__ __forceinline__ double2 ld_pair(const float *p)
 {
@@ -939,10 +1189,44 @@ void launch_row_sums(Ctx &c)
     k_row_sums<<<spmv_grid(c), VTPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.Kf, c.Krs);
 }
 
+// Stage layout of the streamed product for rows of at most max_npad blocks,
+// and the stage count with one and with two CTAs per SM (0 where fewer than
+// two stages fit).  Also lifts the kernels' dynamic shared-memory limit.
+void init_stream_product(Ctx &c, int max_npad)
+{
+    auto up = [](int v, int a) { return (v + a - 1) / a * a; };
+    c.stream_cols_off = 256;  // after the 144 bytes of row offsets
+    c.stream_vals_off = c.stream_cols_off + up(STREAM_ROWS * max_npad * 4, 128);
+    c.stream_stage_bytes = c.stream_vals_off + up(STREAM_ROWS * max_npad * 36, 128);
+    int optin = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device);
+    cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c.device);
+    const int reserve = 2048;  // static shared memory and the per-block reservation
+    const int avail[2] = {std::min(optin, per_sm) - reserve, per_sm / 2 - reserve};
+    for (int k = 0; k < 2; k++) {
+        const int st = avail[k] > 0 ? std::min(STREAM_MAX_STAGES, avail[k] / c.stream_stage_bytes) : 0;
+        c.stream_stages[k] = st >= 2 ? st : 0;
+    }
+    const int bytes = c.stream_stages[0] * c.stream_stage_bytes;
+    if (bytes > 0) {
+        cudaFuncSetAttribute(k_spmv_diff_stream<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        cudaFuncSetAttribute(k_spmv_diff_stream<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    }
+    cudaGetLastError();
+}
+
 template <bool DOT>
 static void spmv_diff_variant(Ctx &c, const SpmvArgs &a, dvec4 *y)
 {
     const SplitRec *sp = reinterpret_cast<const SplitRec *>(c.p_split);
+    const int ds = c.tune.diff_stream;
+    if (ds >= 1 && ds <= 2 && c.stream_stages[ds - 1] >= 2) {
+        const StreamLayout lay = {c.stream_stages[ds - 1], c.stream_stage_bytes, c.stream_cols_off,
+                                  c.stream_vals_off};
+        k_spmv_diff_stream<DOT><<<sm_count(c) * ds, VTPB, (size_t)lay.stages * lay.stage_bytes, c.stream>>>(
+            a, lay, c.Kf, c.Krs, sp, y, c.status);
+        return;
+    }
     const int g = spmv_grid(c);
     switch (c.tune.spmv_variant) {
     case 1:

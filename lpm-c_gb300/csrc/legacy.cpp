@@ -18,16 +18,16 @@
 // Globals of include/lpm.h:55-81 used by the solve path (defined by the host
 // program, as src/lpmc_project.c:19-45 does).
 extern "C" {
-extern int nparticle, nneighbors, dim, lattice, plmode, ntype, nslipSys;
+extern int nparticle, nneighbors, dim, lattice, plmode, ntype, nslipSys, nbreak;
 extern int *IK, *JK, *type, *dispBC_index, *fix_index, *nb, *nb_initial, *nb_conn;
 extern int **neighbors, **K_pointer, **conn, **nsign;
 extern double radius, particle_volume, J2_H, J2_xi, cp_tau0[3], cp_taus[3], cp_eta, cp_p, cp_h0, cp_q,
-    cp_maxloop, dtime;
+    cp_maxloop, dtime, damage_L, damage_threshold, damagec_A, critical_bstrain;
 extern double *K_global, *residual, *Pin, *Pex, *disp, *sigmay, *reaction_force;
-extern double *J2_dlambda, *J2_stresseq, *J2_stressm, *J2_triaxiality;
+extern double *J2_dlambda, *J2_stresseq, *J2_stressm, *J2_triaxiality, *damage_visual;
 extern double **xyz, **xyz_initial, **xyz_temp, **F, **F_temp, **csx, **csy, **csz, **Ce, **dL, **Kn, **Tv;
 extern double **stress_tensor, **bond_stress, **J2_alpha, **J2_beta_eq, **cp_A, **cp_Cab;
-extern double **damage_local, **damage_nonlocal, **strain_tensor;
+extern double **damage_local, **damage_nonlocal, **strain_tensor, **damage_broken, **damage_w;
 extern double ***dLp, ***J2_beta, ***cp_gy, ***cp_A_single, ***damage_D;
 }
 
@@ -54,6 +54,8 @@ bool g_opts_set = false;
 int g_status = 0;
 long long g_h2d = 0, g_d2h = 0;
 int g_plmode_dev = -1;
+bool g_damage_on = false;  // the context's damage stage is on (first damage call)
+int g_log_written = 0;     // broken bonds of lpm_damage_log already in the bond file
 
 [[noreturn]] void die(const char *what)
 {
@@ -245,6 +247,38 @@ void device_force(int pl, bool stress_outputs)
     }
 }
 
+// The context's damage stage with main's parameters (src/lpmc_project.c:239-244
+// set them as globals), switched on by the first damage call.
+void ensure_damage()
+{
+    if (g_damage_on)
+        return;
+    lpm_damage_opts o;
+    lpm_default_damage_opts(&o);
+    o.enabled = 1;
+    o.length = damage_L;
+    o.threshold = damage_threshold;
+    o.triax_coeff = damagec_A;
+    o.critical_bstrain = critical_bstrain;
+    o.nbreak = nbreak;
+    check(lpm_set_damage(ctx(), &o), "damage stage");
+    g_damage_on = true;
+    g_log_written = 0;
+}
+
+// Upload the damage state the damage functions read (current slots).
+void put_damage()
+{
+    const int n = nparticle, nn = nneighbors;
+    put("damage_broken", flat2(damage_broken, n, nn));
+    put("damage_w", flat2(damage_w, n, nn));
+    put("damage_D0", flat3(damage_D, n, nn, 0));
+    dvec a(n);
+    for (int i = 0; i < n; i++)
+        a[i] = damage_nonlocal[i][0];
+    put("damage_nonlocal0", a);
+}
+
 }  // namespace
 
 extern "C" {
@@ -287,6 +321,7 @@ void calcKnTv(void)
         std::exit(5);
     }
     lpm_legacy_reset();
+    g_damage_on = false;
     check(lpm_create(&g_ctx, 0), "lpm_create");
     {
         // LPM_PRECOND=amg selects the multigrid preconditioner for an
@@ -358,7 +393,12 @@ void calcStiffness2DFiniteDifference(int)
     std::exit(5);
 }
 
-// src/stiffness.c:384-516
+// src/stiffness.c:384-516.  The reference's finite-difference sweep leaves
+// the elastic-law bond forces of the current configuration in F and Pin
+// (:390-418, computeBondForceElastic per particle).  Where a caller reads them
+// before the next force evaluation - main's re-entry after broken bonds
+// (src/lpmc_project.c:528-546 -> updateRR) - they are needed: with the damage
+// stage on, the elastic forces are computed and written back here as well.
 void calcStiffness3DFiniteDifference(int)
 {
     const int n = nparticle, nn = nneighbors;
@@ -370,6 +410,8 @@ void calcStiffness3DFiniteDifference(int)
         check(lpm_export_upper_csr(ctx(), K_global, IK, JK, &nnz), "K export");
         g_d2h += nnz * 12;
     }
+    if (g_damage_on)
+        device_force(6, false);
 }
 
 // src/stiffness.c:519-534
@@ -468,13 +510,116 @@ void computeBondForceJ2energyReturnMap(int, int)
     std::exit(5);
 }
 
-int updateDamageGeneral(const char *, int, int) { return 0; }
-int updateBrittleDamage(const char *, int, int) { return 0; }
-int updateDuctileDamageBwiseLocal(const char *, int) { return 0; }
-int updateDuctileDamagePwiseLocal(const char *, int) { return 0; }
-int updateDuctileDamageBwiseNonlocal(const char *, int) { return 0; }
-int updateDuctileDamagePwiseNonlocal(const char *, int) { return 0; }
-void updateCrack(void) {}
+// src/constitutive.c:149-164 on the GPU damage stage: the ductile nonlocal
+// update for J2 (plmode 0, updateDuctileDamagePwiseNonlocal, :1757-1862), the
+// brittle one for elastic bonds (plmode 6, updateBrittleDamage with the global
+// nbreak, :1437-1527), nothing for crystal plasticity.  Uploads the damage
+// state and the update's input (J2_dlambda, or dL), writes back the damage
+// state and appends the step's broken bonds to dataName as the reference
+// does ("TIMESTEP t", then "i j " per bond).
+int updateDamageGeneral(const char *dataName, int tstep, int pl)
+{
+    if (pl == 5) {
+        std::printf("LPM GPU drop-in: bond-wise local ductile damage (plmode 5) is not on the GPU path\n");
+        std::exit(5);
+    }
+    if (pl != 0 && pl != 6)
+        return 0;
+    if (pl != g_plmode_dev) {
+        std::printf("LPM GPU drop-in: damage for plmode %d requested but the specimen was built for %d\n", pl,
+                    g_plmode_dev);
+        std::exit(5);
+    }
+    ensure_damage();
+    const int n = nparticle, nn = nneighbors;
+    const size_t nb = (size_t)n * nn;
+    put_damage();
+    if (pl == 0)
+        put("J2_dlambda", dvec(J2_dlambda, J2_dlambda + n));
+    else
+        put("dL", flat2(dL, n, nn));
+    int broken = 0;
+    check(lpm_damage_update(ctx(), &broken), "updateDamageGeneral");
+    scatter2(damage_broken, get("damage_broken", nb), n, nn);
+    scatter2(damage_w, get("damage_w", nb), n, nn);
+    scatter3(damage_D, get("damage_D0", nb), n, nn, 0);
+    if (pl == 0) {
+        const dvec a = get("damage_nonlocal0", n);
+        for (int i = 0; i < n; i++)
+            damage_nonlocal[i][0] = a[i];
+    }
+    int total = 0;
+    check(lpm_damage_log(ctx(), nullptr, 0, &total), "damage log");
+    std::vector<int> pairs(2 * (size_t)total + 2);
+    if (total > 0)
+        check(lpm_damage_log(ctx(), pairs.data(), total, &total), "damage log");
+    if (FILE *f = dataName ? std::fopen(dataName, "a+") : nullptr) {
+        std::fprintf(f, "TIMESTEP %d\n", tstep);
+        for (int k = g_log_written; k < total; k++)
+            std::fprintf(f, "%d %d \n", pairs[2 * (size_t)k], pairs[2 * (size_t)k + 1]);
+        std::fclose(f);
+    }
+    g_log_written = total;
+    return broken;
+}
+
+int updateBrittleDamage(const char *dataName, int tstep, int)
+{
+    return updateDamageGeneral(dataName, tstep, 6);
+}
+
+int updateDuctileDamagePwiseNonlocal(const char *dataName, int tstep)
+{
+    return updateDamageGeneral(dataName, tstep, 0);
+}
+
+int updateDuctileDamageBwiseLocal(const char *, int)
+{
+    std::printf("LPM GPU drop-in: updateDuctileDamageBwiseLocal is not on the GPU path\n");
+    std::exit(5);
+}
+
+int updateDuctileDamagePwiseLocal(const char *, int)
+{
+    std::printf("LPM GPU drop-in: updateDuctileDamagePwiseLocal is not on the GPU path\n");
+    std::exit(5);
+}
+
+int updateDuctileDamageBwiseNonlocal(const char *, int)
+{
+    std::printf("LPM GPU drop-in: updateDuctileDamageBwiseNonlocal is not on the GPU path\n");
+    std::exit(5);
+}
+
+// src/constitutive.c:1399-1434: bond forces scaled by damage_w, internal
+// forces, intact-bond counts nb, damage_visual, and fix_index cleared for
+// particles left without bonds.
+void updateCrack(void)
+{
+    ensure_damage();
+    const int n = nparticle, nn = nneighbors;
+    const size_t nb3 = (size_t)n * nn;
+    put_damage();
+    put("F", flat2(F, n, nn));
+    put("csx", flat2(csx, n, nn));
+    put("csy", flat2(csy, n, nn));
+    put("csz", flat2(csz, n, nn));
+    check(lpm_damage_crack(ctx()), "updateCrack");
+    scatter2(F, get("F", nb3), n, nn);
+    const dvec pin = get("Pin", 3 * (size_t)n);
+    std::memcpy(Pin, pin.data(), pin.size() * sizeof(double));
+    const dvec vis = get("damage_visual", n);
+    std::memcpy(damage_visual, vis.data(), vis.size() * sizeof(double));
+    std::vector<int> cnt(n);
+    check(lpm_get(ctx(), "nb_current", cnt.data(), cnt.size() * sizeof(int)), "nb_current");
+    g_d2h += (long long)(cnt.size() * sizeof(int));
+    for (int i = 0; i < n; i++) {
+        nb[i] = cnt[i];
+        if (nb[i] < 1)
+            for (int k = 0; k < dim; k++)
+                fix_index[dim * i + k] = 0;
+    }
+}
 
 // src/boundary.c:12-45
 void setDispBC(int nbd, struct dispBCPara *d)

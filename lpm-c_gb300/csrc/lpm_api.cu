@@ -341,9 +341,20 @@ static int alloc_specimen(Ctx &c)
     c.nblk_real = 0;
     for (int i = 0; i < c.n; i++)
         c.nblk_real += h.nconn[i];
-    A_(c.rowoff, n + 1) A_(c.npad, n) A_(c.cols, (size_t)c.nblk)
+    // row offsets padded past n + 1 with the total (empty rows): the streamed
+    // product copies 18 offsets per tile of 16 rows
+    const size_t nro = (n + 15) / 16 * 16 + 2;
+    A_(c.rowoff, nro) A_(c.npad, n) A_(c.cols, (size_t)c.nblk)
 #undef A_
-    LPM_CUDA(cudaMemcpy(c.rowoff, h.rowoff.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice));
+    {
+        std::vector<long long> ro(h.rowoff.begin(), h.rowoff.begin() + n + 1);
+        ro.resize(nro, h.rowoff[n]);
+        LPM_CUDA(cudaMemcpy(c.rowoff, ro.data(), sizeof(long long) * nro, cudaMemcpyHostToDevice));
+        int max_npad = 0;
+        for (size_t i = 0; i < n; i++)
+            max_npad = std::max(max_npad, h.npad[i]);
+        init_stream_product(c, max_npad);
+    }
     LPM_CUDA(cudaMemcpy(c.npad, h.npad.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     LPM_CUDA(cudaMemcpy(c.cols, h.cols.data(), sizeof(int) * c.nblk, cudaMemcpyHostToDevice));
     if (!c.sc_host) {
@@ -1288,12 +1299,12 @@ static int apply_bc(Ctx &c, int nbd, const lpm_disp_bc *dbc, int nbf, const lpm_
     return LPM_OK;
 }
 
-// The damage stage after a converged Newton pass (src/lpmc_project.c:466-469):
-// updateDamageGeneral for the model (src/constitutive.c:149-164), then
-// updateCrack (:1399-1434) and the stress weights of the intact bonds.
-// `broken` is updateDamageGeneral's return value.  Broken bonds are logged as
-// (particle, partner) in the order the reference writes its bond file.
-static int damage_pass(Ctx &c, int &broken)
+// updateDamageGeneral for the context's model (src/constitutive.c:149-164):
+// ductile nonlocal damage for J2, brittle bond breaking for elastic bonds,
+// nothing for crystal plasticity.  `broken` is its return value.  Broken
+// bonds are logged as (particle, partner) in the order the reference writes
+// its bond file.
+static int damage_update(Ctx &c, int &broken)
 {
     Ctx::Damage &d = c.dmg;
     const int n = c.n;
@@ -1354,9 +1365,24 @@ static int damage_pass(Ctx &c, int &broken)
         }
         broken = k;
     }
+    return sync(c);
+}
+
+// updateCrack (src/constitutive.c:1399-1434): bond forces scaled by
+// damage_w, internal forces and residual, intact-bond counts, visual damage;
+// then the stress weights of the intact bonds.
+static int damage_crack(Ctx &c)
+{
     launch_crack(c);
     launch_dmg_oppv(c);
     return sync(c);
+}
+
+// The damage stage after a converged Newton pass (src/lpmc_project.c:466-470).
+static int damage_pass(Ctx &c, int &broken)
+{
+    int rc = damage_update(c, broken);
+    return rc ? rc : damage_crack(c);
 }
 
 struct Timer {
@@ -1540,6 +1566,27 @@ int lpm_damage_log(lpm_ctx *ctx, int *pairs, int capacity, int *count)
         std::memcpy(pairs, c.dmg.log.data(), sizeof(int) * 2 * (size_t)k);
     }
     return LPM_OK;
+}
+
+int lpm_damage_update(lpm_ctx *ctx, int *broken)
+{
+    if (!ctx || !broken)
+        return fail(LPM_ERR_ARG, "null argument");
+    Ctx &c = ctx->c;
+    if (!c.dmg.on)
+        return fail(LPM_ERR_ARG, "lpm_damage_update: the damage stage is off (lpm_set_damage)");
+    *broken = 0;
+    return damage_update(c, *broken);
+}
+
+int lpm_damage_crack(lpm_ctx *ctx)
+{
+    if (!ctx)
+        return fail(LPM_ERR_ARG, "null argument");
+    Ctx &c = ctx->c;
+    if (!c.dmg.on)
+        return fail(LPM_ERR_ARG, "lpm_damage_crack: the damage stage is off (lpm_set_damage)");
+    return damage_crack(c);
 }
 
 int lpm_damage_brittle_select(const int *bonds, const double *strain, int k, int n, int nbreak, int *chosen,
@@ -2337,13 +2384,15 @@ int lpm_get(lpm_ctx *ctx, const char *name, void *dst, size_t bytes)
         return LPM_OK;
     }
     if (nm == "damage_broken" || nm == "damage_w" || nm == "damage_D" || nm == "damage_nonlocal" ||
-        nm == "damage_visual" || nm == "nb_current") {
+        nm == "damage_D0" || nm == "damage_nonlocal0" || nm == "damage_visual" || nm == "nb_current") {
         if (!c.dmg.on)
             return fail(LPM_ERR_ARG, nm + ": the damage stage is off (lpm_set_damage)");
         if (nm == "damage_broken") return bond_d(c.dmg.brk);
         if (nm == "damage_w") return bond_d(c.dmg.dw);
         if (nm == "damage_D") return bond_d(c.dmg.D[1]);
+        if (nm == "damage_D0") return bond_d(c.dmg.D[0]);
         if (nm == "damage_nonlocal") return rows_d(c.dmg.dnl[1], 1);
+        if (nm == "damage_nonlocal0") return rows_d(c.dmg.dnl[0], 1);
         if (nm == "damage_visual") return rows_d(c.dmg.dvis, 1);
         if (!need(n * sizeof(int)))
             return fail(LPM_ERR_ARG, nm + ": buffer too small");
@@ -2409,6 +2458,18 @@ int lpm_set(lpm_ctx *ctx, const char *name, const void *src, size_t bytes)
     if ((nm == "cp_gy" || nm == "cp_gy1") && c.nslip) return rows_d(c.gy[1], c.nslip);
     if ((nm == "cp_A_single" || nm == "cp_A_single1") && c.nslip) return rows_d(c.As[1], c.nslip);
     if ((nm == "cp_A" || nm == "cp_A1") && c.nslip) return rows_d(c.A[1], 1);
+    if (nm == "J2_dlambda") return rows_d(c.dlambda, 1);
+    if (nm == "damage_broken" || nm == "damage_w" || nm == "damage_D" || nm == "damage_D0" ||
+        nm == "damage_nonlocal" || nm == "damage_nonlocal0") {
+        if (!c.dmg.on)
+            return fail(LPM_ERR_ARG, nm + ": the damage stage is off (lpm_set_damage)");
+        if (nm == "damage_broken") return bond_d(c.dmg.brk);
+        if (nm == "damage_w") return bond_d(c.dmg.dw);
+        if (nm == "damage_D") return bond_d(c.dmg.D[1]);
+        if (nm == "damage_D0") return bond_d(c.dmg.D[0]);
+        if (nm == "damage_nonlocal") return rows_d(c.dmg.dnl[1], 1);
+        return rows_d(c.dmg.dnl[0], 1);
+    }
     if (nm == "dispBC_index") {
         if (bytes < 3 * (size_t)n * sizeof(int))
             return fail(LPM_ERR_ARG, nm + ": buffer too small");
@@ -2513,6 +2574,7 @@ static void fill_tuning(const Ctx &c, lpm_tuning *t)
     t->cg_per_sm = c.tune.vec_per_sm;
     t->smooth_lanes = c.tune.smooth_variant == 1 ? 8 : (c.tune.smooth_variant == 2 ? 4 : 16);
     t->smooth_ms = 0.0;
+    t->diff_stream = c.tune.diff_stream;
 }
 
 }  // namespace lpm
@@ -2533,10 +2595,14 @@ int lpm_set_tuning(lpm_ctx *ctx, const lpm_tuning *t)
     if (!ctx || !t)
         return fail(LPM_ERR_ARG, "null argument");
     auto ok_grid = [](int v) { return v >= 1 && v <= TUNE_MAX_PER_SM; };
-    if (t->spmv_variant < 0 || t->spmv_variant > 3 || !ok_grid(t->spmv_per_sm) || !ok_grid(t->cg_per_sm))
+    if (t->spmv_variant < 0 || t->spmv_variant > 3 || !ok_grid(t->spmv_per_sm) || !ok_grid(t->cg_per_sm) ||
+        t->diff_stream < 0 || t->diff_stream > 2)
         return fail(LPM_ERR_ARG, "lpm_set_tuning: variant 0..3, blocks per SM 1.." +
-                                     std::to_string(TUNE_MAX_PER_SM));
+                                     std::to_string(TUNE_MAX_PER_SM) + ", diff_stream 0..2");
     Ctx &c = ctx->c;
+    if (t->diff_stream > 0 && c.stream_stages[t->diff_stream - 1] < 2)
+        return fail(LPM_ERR_ARG, "lpm_set_tuning: the streamed product's stages do not fit in shared memory");
+    c.tune.diff_stream = t->diff_stream;
     c.tune.spmv_variant = t->spmv_variant;
     c.tune.spmv_per_sm = t->spmv_per_sm;
     c.tune.vec_per_sm = t->cg_per_sm;
@@ -2590,6 +2656,7 @@ int lpm_autotune(lpm_ctx *ctx, lpm_tuning *out)
     Tune best = keep;
     double best_ms = 1e30, def_ms = 0.0;
     int rc = LPM_OK;
+    c.tune.diff_stream = 0;
     for (int v = 0; v < 4 && !rc; v++)
         for (int g : grids) {
             c.tune.spmv_variant = v;
@@ -2605,6 +2672,28 @@ int lpm_autotune(lpm_ctx *ctx, lpm_tuning *out)
                 best.spmv_per_sm = g;
             }
         }
+    // the streamed difference-form product with 1 and 2 CTAs per SM
+    best.diff_stream = 0;
+    if (diff && !rc) {
+        for (int ds = 1; ds <= 2 && !rc; ds++) {
+            if (c.stream_stages[ds - 1] < 2)
+                continue;
+            c.tune.diff_stream = ds;
+            double ms = 0.0;
+            if ((rc = time_it(spmv, ms)))
+                break;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best.diff_stream = ds;
+            }
+        }
+        c.tune.diff_stream = 0;
+        if (!rc) {
+            LPM_CUDA(cudaMemcpyAsync(c.status_host, c.status, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+            if (!(rc = sync(c)) && (*c.status_host & LPM_STATUS_DEVICE_WAIT))
+                rc = fail(LPM_ERR_DEVICE, "lpm_autotune: a wait of the streamed product ran out");
+        }
+    }
     double best_smooth = 0.0;
     if (amg && !rc) {
         best_smooth = 1e30;

@@ -195,12 +195,14 @@ struct BatchHost {
 // 3 = 4 x 4 (lanes per block row x consecutive blocks per lane).
 struct Tune {
     int smooth_variant = 0;  // multigrid level-0 smoother: 16 (0), 8 (1) or 4 (2) lanes per block row
+    int diff_stream = 0;     // difference-form product: register-fed (0) or streamed, 1 or 2 CTAs per SM
     int spmv_variant = 0;
     int spmv_per_sm = 8;  // SpMV thread blocks per SM (grid-stride over rows)
     int vec_per_sm = 8;   // PCG vector-kernel thread blocks per SM
     int sms = 0;          // SM count of the device
 };
 constexpr int TUNE_MAX_PER_SM = 16;
+constexpr int STREAM_MAX_STAGES = 8;  // shared-memory stages of the streamed product
 
 struct Ctx {
     int device = 0;
@@ -277,6 +279,10 @@ struct Ctx {
     // level-0 smoother, of the assembly numbered kh_version
     unsigned short *Kh = nullptr;
     float *kh_scale = nullptr;
+    // streamed difference-form product: stages per CTA with 1 and 2 CTAs per
+    // SM (0: does not fit), bytes per stage and the offsets within a stage
+    int stream_stages[2] = {0, 0};
+    int stream_stage_bytes = 0, stream_cols_off = 0, stream_vals_off = 0;
     unsigned *kh_max = nullptr;
     long long kh_cap = 0, kh_version = -1;
     // mixed multigrid: Kd holds the exact FP64 copy of Kf of this assembly
@@ -399,6 +405,7 @@ void launch_amg_reliable(Ctx &c, const dvec4 *rtrue);  // r = rtrue (masked), z,
 void launch_amg_vcycle(Ctx &c, const dvec4 *r, dvec4 *z);  // z = V(r), FP32 inside (Kf, Pinv_f, x_f/q_f/r_f)
 void launch_amg_smoother_pass(Ctx &c);  // one level-0 residual pass on scratch vectors (autotuner timing)
 void launch_amg_stiffness32(Ctx &c);  // Kf = (float) Kd, for the smoother under FP64 precision
+void init_stream_product(Ctx &c, int max_npad);  // layouts of the streamed product for the pattern
 void launch_amg_stiffness16(Ctx &c);  // Kh = half(Kf / s), s = max |Kf| / 2^14 into kh_scale
 void launch_stiffness64_of32(Ctx &c); // Kd = (double) Kf, exactly
 int amg_prepare(Ctx &c);  // (re)build the hierarchy when missing, stale or the mask changed

@@ -10,8 +10,8 @@
  * createCuboid / searchNormalNeighbor / searchAFEMNeighbor).
  *
  * Exported for scripting (ctypes): lpmh_setup, lpmh_set_types,
- * lpmh_set_bc_groups, lpmh_set_material, lpmh_init, lpmh_load_step,
- * lpmh_get, lpmh_n.
+ * lpmh_set_bc_groups, lpmh_set_material, lpmh_set_damage, lpmh_init,
+ * lpmh_load_step, lpmh_get, lpmh_n.
  *
  * Per-particle moduli: the reference takes elastic constants per type
  * (Ce[type[i]], src/stiffness.c:186-200), so a material that varies from
@@ -70,6 +70,11 @@ double **cp_Cab, **strain_tensor, **dL_ave, **ddL_total, **TddL_total, **F_temp,
 double **dL, **ddL, **bond_stress, **damage_broken, **damage_w, **bond_stretch, **bond_vector, **bond_force;
 double **Kn, **Tv, **J2_alpha, **damage_local, **damage_nonlocal, **cp_A, **cp_dgy, **cp_dA_single, **J2_beta_eq;
 double ***slip_vector, ***dLp, ***J2_beta, ***damage_D, ***cp_gy, ***cp_A_single;
+
+/* main's damage stage (src/lpmc_project.c:239-244 parameters, :466-470 and
+ * :528-546 per load step): off unless lpmh_set_damage is called */
+static int g_damage = 0, g_max_passes = 1000, g_step = 0;
+static char g_bondfile[1024];
 
 /* ---- allocation helpers (src/lpm_basic.c:361-445 semantics) ---------------- */
 static double *d1(int n, double v)
@@ -196,6 +201,8 @@ static lpm_ctx *g_setup = NULL;
 /* Lattice + bond lists + AFEM connectivity into the globals.  Returns n. */
 int lpmh_setup(int lat, double rad, const double *bx, int nslip)
 {
+    g_damage = 0;
+    g_step = 0;
     lattice = lat;
     dim = 3;
     radius = rad;
@@ -366,14 +373,31 @@ void lpmh_init(void)
         computeCab();
 }
 
+void lpmh_set_damage(double L, double threshold, double cA, double crit, int nbr, const char *bondfile,
+                     int max_passes)
+{
+    damage_L = L;
+    damage_threshold = threshold;
+    damagec_A = cA;
+    critical_bstrain = crit;
+    nbreak = nbr;
+    snprintf(g_bondfile, sizeof g_bondfile, "%s", bondfile ? bondfile : "result_brokenbonds.txt");
+    g_max_passes = max_passes > 0 ? max_passes : 1000;
+    g_damage = 1;
+}
+
 /*
- * One load step, src/lpmc_project.c:385-471 (damage skipped: the GPU path
- * has none).  stats: Newton iterations, |r0|, |reaction0|, |r| final.
+ * One load step, src/lpmc_project.c:385-471, and with the damage stage on
+ * :466-470 and the re-entry after broken bonds (:528-546: new stiffness, then
+ * label_broken_bond).  computeStrain and the output writers are left out.
+ * stats (7 values): Newton iterations, |r0|, |reaction0|, |r| final, 0,
+ * Newton passes, sum of updateDamageGeneral's return values.
  */
 int lpmh_load_step(int nbd, struct dispBCPara *dbp, int nbf, struct forceBCPara *fbp, double newton_tol,
                    int maxiter, double *stats)
 {
     int n = nparticle;
+    g_step++;
     for (int i = 0; i < n; i++) {
         memcpy(xyz_temp[i], xyz[i], sizeof(double) * NDIM);
         memcpy(F_temp[i], F[i], sizeof(double) * nneighbors);
@@ -382,30 +406,54 @@ int lpmh_load_step(int nbd, struct dispBCPara *dbp, int nbf, struct forceBCPara 
     calcStiffness3DFiniteDifference(6);
     apply_bcs(nbd, dbp, nbf, fbp);
     computeBondForceGeneral(4, 1);
-    updateRR();
-    int nreact = 0;
-    for (int k = 0; k < n * dim; k++)
-        nreact += (dispBC_index[k] != 1);
-    double nr = dnrm2(dim * n, residual), nreac = dnrm2(nreact, reaction_force);
-    double tolm = MAXV(nr, nreac), nr0 = nr;
-    int ni = 0;
-    while (nr > newton_tol * tolm && ni < maxiter) {
-        switchStateV(0);
-        setDispBC_stiffnessUpdate3D();
-        solverCG();
-        computeBondForceGeneral(plmode, 1);
-        updateRR();
-        ni++;
+    double nr = 0.0, nr0 = 0.0, nreac0 = 0.0;
+    int ni_tot = 0, passes = 0, broken_tot = 0;
+    for (;;) {
+        updateRR(); /* label_broken_bond */
+        int nreact = 0;
+        for (int k = 0; k < n * dim; k++)
+            nreact += (dispBC_index[k] != 1);
         nr = dnrm2(dim * n, residual);
+        double nreac = dnrm2(nreact, reaction_force);
+        double tolm = MAXV(nr, nreac);
+        if (passes == 0) {
+            nr0 = nr;
+            nreac0 = nreac;
+        }
+        int ni = 0;
+        while (nr > newton_tol * tolm && ni < maxiter) {
+            switchStateV(0);
+            setDispBC_stiffnessUpdate3D();
+            solverCG();
+            computeBondForceGeneral(plmode, 1);
+            updateRR();
+            ni++;
+            nr = dnrm2(dim * n, residual);
+        }
+        ni_tot += ni;
+        passes++;
+        if (!g_damage) {
+            switchStateV(1);
+            break;
+        }
+        int broken = updateDamageGeneral(g_bondfile, g_step, plmode);
+        updateCrack();
+        switchStateV(1);
+        broken_tot += broken;
+        if (broken <= 0 || passes >= g_max_passes)
+            break;
+        calcStiffness3DFiniteDifference(6);
     }
-    switchStateV(1);
     if (stats) {
-        stats[0] = ni;
+        stats[0] = ni_tot;
         stats[1] = nr0;
-        stats[2] = nreac;
+        stats[2] = nreac0;
         stats[3] = nr;
+        stats[4] = 0.0;
+        stats[5] = passes;
+        stats[6] = broken_tot;
     }
-    return ni;
+    return ni_tot;
 }
 
 /* flat copies of a few globals (row-major) */
@@ -434,6 +482,16 @@ int lpmh_get(const char *name, double *out)
     } else if (!strcmp(name, "dL")) {
         for (int i = 0; i < n; i++)
             memcpy(out + (size_t)i * nn, dL[i], sizeof(double) * nn);
+    } else if (!strcmp(name, "damage_broken") || !strcmp(name, "damage_w")) {
+        double **a = name[7] == 'b' ? damage_broken : damage_w;
+        for (int i = 0; i < n; i++)
+            memcpy(out + (size_t)i * nn, a[i], sizeof(double) * nn);
+    } else if (!strcmp(name, "damage_nonlocal")) {
+        for (int i = 0; i < n; i++)
+            out[i] = damage_nonlocal[i][1];
+    } else if (!strcmp(name, "nb")) {
+        for (int i = 0; i < n; i++)
+            out[i] = nb[i];
     } else if (!strcmp(name, "strain_tensor")) {
         for (int i = 0; i < n; i++)
             memcpy(out + 6 * (size_t)i, strain_tensor[i], sizeof(double) * 6);

@@ -38,6 +38,7 @@ EXPORTED = [
     "lpm_format_dump", "lpm_format_disp", "lpm_format_reaction", "lpm_format_stress",
     "lpm_compute_strain", "lpm_write_strain", "lpm_format_strain",
     "lpm_default_damage_opts", "lpm_set_damage", "lpm_damage_log", "lpm_damage_brittle_select",
+    "lpm_damage_update", "lpm_damage_crack",
 ]
 
 
@@ -65,7 +66,8 @@ class Tuning(C.Structure):
     """lpm_tuning: launch shapes of the solve (include/lpm_gpu.h)."""
     _fields_ = [("spmv_variant", C.c_int), ("spmv_lanes", C.c_int), ("spmv_blocks", C.c_int),
                 ("spmv_per_sm", C.c_int), ("cg_per_sm", C.c_int), ("spmv_ms", C.c_double),
-                ("spmv_ms_default", C.c_double), ("smooth_lanes", C.c_int), ("smooth_ms", C.c_double)]
+                ("spmv_ms_default", C.c_double), ("smooth_lanes", C.c_int), ("smooth_ms", C.c_double),
+                ("diff_stream", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -181,6 +183,8 @@ def load(path=LIB_PATH):
         "lpm_default_damage_opts": ([C.POINTER(DamageOpts)], None),
         "lpm_set_damage": ([vp, C.POINTER(DamageOpts)], C.c_int),
         "lpm_damage_log": ([vp, ip, C.c_int, ip], C.c_int),
+        "lpm_damage_update": ([vp, ip], C.c_int),
+        "lpm_damage_crack": ([vp], C.c_int),
         "lpm_damage_brittle_select": ([ip, dp, C.c_int, C.c_int, C.c_int, ip, ip], C.c_int),
     }
     for name, (args, res) in sig.items():
@@ -293,8 +297,9 @@ class Specimen:
         self._check(self.L.lpm_autotune(self.h, C.byref(t)))
         return t.as_dict()
 
-    def set_tuning(self, spmv_variant=0, spmv_per_sm=8, cg_per_sm=8):
-        t = Tuning(spmv_variant=spmv_variant, spmv_per_sm=spmv_per_sm, cg_per_sm=cg_per_sm)
+    def set_tuning(self, spmv_variant=0, spmv_per_sm=8, cg_per_sm=8, diff_stream=0):
+        t = Tuning(spmv_variant=spmv_variant, spmv_per_sm=spmv_per_sm, cg_per_sm=cg_per_sm,
+                   diff_stream=diff_stream)
         self._check(self.L.lpm_set_tuning(self.h, C.byref(t)))
 
     def get_tuning(self):

@@ -27,6 +27,8 @@ class HostDriver:
         self.L.lpmh_load_step.argtypes = [C.c_int, C.POINTER(G.DispBC), C.c_int, C.POINTER(G.ForceBC),
                                           C.c_double, C.c_int, dp]
         self.L.lpmh_get.argtypes = [C.c_char_p, dp]
+        self.L.lpmh_set_damage.argtypes = [C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, C.c_char_p,
+                                           C.c_int]
         self.L.lpm_legacy_set_solver.argtypes = [C.c_void_p]
         self.L.lpm_legacy_traffic.argtypes = [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.c_int]
         self.n = 0
@@ -68,12 +70,22 @@ class HostDriver:
         if rc < 0:
             raise G.LPMError("legacy solver options rejected")
 
+    def set_damage(self, bondfile, length=0.5, threshold=0.9, triax_coeff=0.0, critical_bstrain=1e-2, nbreak=20,
+                   max_passes=1000):
+        """main's damage stage in every load step: updateDamageGeneral,
+        updateCrack and the re-solves after broken bonds; broken bonds are
+        appended to bondfile."""
+        self.L.lpmh_set_damage(float(length), float(threshold), float(triax_coeff), float(critical_bstrain),
+                               int(nbreak), os.fsencode(bondfile), int(max_passes))
+
     def init(self):
         self.L.lpmh_init()
 
     def load_step(self, disp_bcs, force_bcs=(), newton_tol=1e-8, maxiter=100):
+        """Returns Newton iterations, |r0|, |reaction0|, |r|, 0, Newton
+        passes, bonds broken (the last two with the damage stage on)."""
         nd, darr, nf, farr = G.bc_arrays(disp_bcs, list(force_bcs))
-        st = np.zeros(4)
+        st = np.zeros(7)
         self.L.lpmh_load_step(nd, darr, nf, farr, float(newton_tol), int(maxiter),
                               st.ctypes.data_as(C.POINTER(C.c_double)))
         return st
@@ -81,7 +93,8 @@ class HostDriver:
     def get(self, name):
         shape = {"xyz": (self.n, 3), "xyz_initial": (self.n, 3), "J2_alpha": (self.n,),
                  "F": (self.n, 18), "csz": (self.n, 18), "dL": (self.n, 18), "Kn": (self.n, 18),
-                 "Tv": (self.n, 18),
+                 "Tv": (self.n, 18), "damage_broken": (self.n, 18), "damage_w": (self.n, 18),
+                 "damage_nonlocal": (self.n,), "nb": (self.n,),
                  "strain_tensor": (self.n, 6)}[name]
         out = np.zeros(shape)
         if self.L.lpmh_get(name.encode(), out.ctypes.data_as(C.POINTER(C.c_double))) != 0:

@@ -8,7 +8,8 @@ import subprocess
 import sys
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-OPTION_FILES = {"test_gpu_amg.py", "test_gpu_forcing.py", "test_gpu_anderson.py", "test_gpu_recycle.py"}
+OPTION_FILES = {"test_gpu_amg.py", "test_gpu_forcing.py", "test_gpu_anderson.py", "test_gpu_recycle.py",
+                "test_gpu_stream.py"}
 
 
 def _fname(t):

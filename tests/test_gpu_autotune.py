@@ -62,29 +62,3 @@ def test_batch_with_other_shape(gpu_lib):
     assert np.abs(da - db).max() <= 1e-9 * np.abs(da).max()
     a.close()
     b.close()
-
-
-@pytest.mark.gpu_last
-@pytest.mark.parametrize("precision", [0, 1])
-def test_autotune_multigrid_then_solve(gpu_lib, precision):
-    """With the multigrid preconditioner the tuner also picks the lanes per
-    block row of the difference-form product (mixed) and of the level-0
-    smoother; later load steps follow the untuned run."""
-    G = gpu_lib
-    case = cases.SCCase(n=12, e_noise=0.05, newton_tol=1e-10)
-    opts = dict(precision=precision, newton_maxiter=300, cg_rtol=1e-11, preconditioner=G.PRECOND_AMG,
-                cg_maxiter=2000)
-    ref, _ = sc_gpu(G, case, **opts)
-    tun, _ = sc_gpu(G, case, **opts)
-    x0 = ref.get("xyz_initial")
-    for k, stp in enumerate(case.schedule[:14]):
-        a = ref.load_step(cases.sc_bcs(stp))
-        b = tun.load_step(cases.sc_bcs(stp))
-        if k == 0:
-            t = tun.autotune()
-            assert t["smooth_lanes"] in (4, 8, 16) and t["smooth_ms"] > 0.0
-        assert a["status"] == 0 and b["status"] == 0
-        da, db = ref.get("xyz") - x0, tun.get("xyz") - x0
-        assert np.abs(da - db).max() <= 1e-9 * np.abs(da).max()
-    ref.close()
-    tun.close()

@@ -1,0 +1,69 @@
+"""The multigrid PCG's launch shapes: the streamed difference-form product
+(tiles of 16 rows copied into shared-memory stages by the bulk-copy engine)
+computes every row as the register-fed product does, and the autotuner's
+choice among the product and smoother shapes leaves later load steps where
+the untuned run puts them."""
+import numpy as np
+import pytest
+
+import cases
+from setup_helpers import sc_gpu
+
+pytestmark = [pytest.mark.gpu, pytest.mark.gpu_option]
+
+
+def _opts(G, precision):
+    return dict(precision=precision, newton_maxiter=300, cg_rtol=1e-11, preconditioner=G.PRECOND_AMG,
+                cg_maxiter=2000)
+
+
+@pytest.mark.parametrize("edge,diff_stream", [(12, 1), (30, 1), (30, 2)])
+def test_streamed_product_follows_register_fed(gpu_lib, edge, diff_stream):
+    """SC 12^3: 108 tiles, fewer than thread blocks (most blocks get none).
+    SC 30^3: 1,688 tiles, the last one partial, and more tiles per thread
+    block than the ring has stages (the stage barriers change phase)."""
+    G = gpu_lib
+    case = cases.SCCase(n=edge, e_noise=0.05, newton_tol=1e-10)
+    ref, _ = sc_gpu(G, case, **_opts(G, G.PREC_MIXED))
+    st, _ = sc_gpu(G, case, **_opts(G, G.PREC_MIXED))
+    st.set_tuning(diff_stream=diff_stream)
+    assert st.get_tuning()["diff_stream"] == diff_stream
+    x0 = ref.get("xyz_initial")
+    worst = 0.0
+    for stp in case.schedule[:8]:
+        a = ref.load_step(cases.sc_bcs(stp))
+        b = st.load_step(cases.sc_bcs(stp))
+        assert a["status"] == 0 and b["status"] == 0, (a["status"], b["status"])
+        assert abs(a["cg_iters"] - b["cg_iters"]) <= 2 + a["cg_iters"] // 20
+        da, db = ref.get("xyz") - x0, st.get("xyz") - x0
+        err = float(np.abs(da - db).max() / np.abs(da).max())
+        worst = max(worst, err)
+        assert err <= 1e-9
+    print(f"\nSC {edge}^3, {diff_stream} block(s) per SM: displacements within {worst:.2e} of the register-fed "
+          f"product")
+    ref.close()
+    st.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_autotune_multigrid_then_solve(gpu_lib, precision):
+    """With the multigrid preconditioner the tuner also picks the lanes per
+    block row of the difference-form product or its streamed form (mixed)
+    and of the level-0 smoother; later load steps follow the untuned run."""
+    G = gpu_lib
+    case = cases.SCCase(n=12, e_noise=0.05, newton_tol=1e-10)
+    ref, _ = sc_gpu(G, case, **_opts(G, precision))
+    tun, _ = sc_gpu(G, case, **_opts(G, precision))
+    x0 = ref.get("xyz_initial")
+    for k, stp in enumerate(case.schedule[:14]):
+        a = ref.load_step(cases.sc_bcs(stp))
+        b = tun.load_step(cases.sc_bcs(stp))
+        if k == 0:
+            t = tun.autotune()
+            assert t["smooth_lanes"] in (4, 8, 16) and t["smooth_ms"] > 0.0
+            assert t["diff_stream"] in ((0, 1, 2) if precision == G.PREC_MIXED else (0,))
+        assert a["status"] == 0 and b["status"] == 0
+        da, db = ref.get("xyz") - x0, tun.get("xyz") - x0
+        assert np.abs(da - db).max() <= 1e-9 * np.abs(da).max()
+    ref.close()
+    tun.close()
