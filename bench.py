@@ -154,6 +154,8 @@ def solver_opts(G, case, precision, precond):
 
 RECYCLE = 8  # earlier solutions of the load step the Newton solves start from
 CG_RTOL = 1e-10  # relative residual of the SC workload's linear solves (--cg-rtol)
+DIFF_STREAM = -1  # form of the mixed multigrid product (--diff-stream; -1: the autotuner's choice)
+SMOOTH_STREAM = -1  # form of the multigrid level-0 smoother (--smooth-stream; -1: the autotuner's choice)
 
 
 class Deadline:
@@ -185,6 +187,13 @@ def run_arm(G, case, prec, precond, W, K, stream, deadline, sync, autotune=True)
         warm.append(s.load_step(cases.sc_bcs(sched[k])))
         if k == 0 and autotune:
             tuning = s.autotune()  # launch shapes from the project's autotuner
+        if k == 0 and precond and (DIFF_STREAM >= 0 or SMOOTH_STREAM >= 0):
+            t = s.get_tuning()
+            ds = DIFF_STREAM if (DIFF_STREAM >= 0 and prec == G.PREC_MIXED) else t["diff_stream"]
+            ss = SMOOTH_STREAM if SMOOTH_STREAM >= 0 else t["smooth_stream"]
+            s.set_tuning(spmv_variant=t["spmv_variant"], spmv_per_sm=t["spmv_per_sm"], cg_per_sm=t["cg_per_sm"],
+                         diff_stream=ds, smooth_stream=ss)
+            tuning = dict(tuning or {}, diff_stream=ds, smooth_stream=ss, set_by="--diff-stream/--smooth-stream")
     sync()
     s.spmv_timing(reset=2)
     clocks = ClockSampler(torch.cuda.current_device())
@@ -867,6 +876,12 @@ def main():
     ap.add_argument("--cg-rtol", type=float, default=CG_RTOL,
                     help="sc workload: relative residual of the linear solves (the reference's solverCG "
                          "stops at 1e-8, src/solver.c:221)")
+    ap.add_argument("--diff-stream", type=int, default=DIFF_STREAM, choices=[-1, 0, 1, 2],
+                    help="sc workload, mixed multigrid: difference-form product fed by registers (0) or streamed "
+                         "through shared memory with 1 or 2 thread blocks per SM; -1 keeps the autotuner's choice")
+    ap.add_argument("--smooth-stream", type=int, default=SMOOTH_STREAM, choices=[-1, 0, 1, 2],
+                    help="sc workload, multigrid: level-0 smoother fed by registers (0) or streamed through shared "
+                         "memory with 1 or 2 thread blocks per SM; -1 keeps the autotuner's choice")
     ap.add_argument("--recycle", type=int, default=RECYCLE,
                     help="earlier solutions of the load step each Newton solve starts from (0: from zero, "
                          "as the reference's solverCG)")
@@ -875,6 +890,8 @@ def main():
         args.warmup = 3
     globals()["CG_RTOL"] = args.cg_rtol
     globals()["RECYCLE"] = args.recycle
+    globals()["DIFF_STREAM"] = args.diff_stream
+    globals()["SMOOTH_STREAM"] = args.smooth_stream
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batch":

@@ -286,6 +286,8 @@ typedef struct lpm_tuning {
     int diff_stream;       /* mixed multigrid PCG: difference-form product fed by registers (0) or
                               streamed through shared memory by the bulk-copy engine with 1 or 2
                               thread blocks per SM (1, 2); same arithmetic per row */
+    int smooth_stream;     /* multigrid level-0 smoother: register-fed (0, smooth_lanes per row) or
+                              streamed as diff_stream (1, 2; 16 lanes per row) */
 } lpm_tuning;
 /* Time every SpMV shape (and vector-kernel grid) on the context's current
  * stiffness with CUDA events and keep the fastest.  Needs an assembled

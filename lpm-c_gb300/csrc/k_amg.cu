@@ -35,6 +35,7 @@
 #include "amg.h"
 #include "amg_rows.h"
 #include "lpm_internal.h"
+#include "stream_pipe.h"
 
 namespace lpm {
 
@@ -301,6 +302,180 @@ __global__ void __launch_bounds__(ATPB) k_amg_k0(int n, const long long *__restr
     }
 }
 
+// k_amg_k0 (16 lanes per block row, the same arithmetic per row) with the
+// FP16 stiffness streamed through a ring of shared-memory stages by the
+// bulk-copy engine (stream_pipe.h).  A tile's FP16 values start 8 bytes off a
+// 16-byte boundary for half of the tiles (18 bytes per block, rows start at
+// multiples of 4 blocks): the copy starts at the boundary below and ends at
+// the one above (the value array is padded by 16 bytes), and the rows index
+// from the offset.  The row's own entries (block inverse, mask, b, x) are
+// loaded ahead of the stage wait.
+template <int MODE, typename O>
+__global__ void __launch_bounds__(ATPB, 1)
+    k_amg_k0_stream(int n, const long long *__restrict__ rowoff, const int *__restrict__ cols,
+                    const uint8_t *__restrict__ mask, const __half *__restrict__ val, const float *__restrict__ kscale,
+                    const float *__restrict__ Prow, float omega, const float *__restrict__ x,
+                    const float *__restrict__ b, O *__restrict__ out, const CgScalars *sc, StreamLayout lay,
+                    int *status)
+{
+    extern __shared__ __align__(128) unsigned char stage_mem[];
+    __shared__ unsigned long long full[STREAM_MAX_STAGES], empty[STREAM_MAX_STAGES];
+    __shared__ volatile int abort_k;
+    if (sc && sc->done)
+        return;
+    const float s = *kscale;
+    const int S = lay.stages;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int sub = lane & 15, rl = 2 * wid + (lane >> 4);
+    const unsigned gmask = 0xffffu << (lane & 16);
+    const int ntiles = (n + STREAM_ROWS - 1) / STREAM_ROWS;
+    const int mine = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < S; k++) {
+            mbar_init(&full[k], 1);
+            mbar_init(&empty[k], ATPB / 32);
+        }
+        abort_k = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    auto first_row = [&](int i) { return ((int)blockIdx.x + i * (int)gridDim.x) * STREAM_ROWS; };
+    auto fail = [&]() {
+        atomicOr(status, LPM_STATUS_DEVICE_WAIT);
+        abort_k = 1;
+    };
+    int issued = 0, jb = -32;
+    long long pb0 = 0, pb1 = 0;
+    auto issue_next = [&]() -> bool {  // warp 0, warp-uniform
+        const int j = issued, st_i = j % S;
+        if (j - jb >= 32) {
+            jb += 32;
+            if (jb + lane < mine) {
+                const int r0 = first_row(jb + lane);
+                pb0 = rowoff[r0];
+                pb1 = rowoff[min(r0 + STREAM_ROWS, n)];
+            }
+        }
+        const long long b0 = __shfl_sync(0xffffffffu, pb0, j - jb);
+        const long long b1 = __shfl_sync(0xffffffffu, pb1, j - jb);
+        if (j >= S && !warp_mbar_wait(&empty[st_i], (unsigned)((j / S) - 1) & 1u))
+            return false;
+        if (lane == 0) {
+            unsigned char *st = stage_mem + (size_t)st_i * lay.stage_bytes;
+            const unsigned nb = (unsigned)(b1 - b0);
+            const long long v0 = (18 * b0) & ~15LL, v1 = (18 * b1 + 15) & ~15LL;
+            const unsigned vb = nb ? (unsigned)(v1 - v0) : 0u;
+            mbar_expect_tx(&full[st_i], 144u + 4u * nb + vb);
+            bulk_g2s(st, rowoff + first_row(j), 144u, &full[st_i]);
+            if (nb) {
+                bulk_g2s(st + lay.cols_off, cols + b0, 4u * nb, &full[st_i]);
+                bulk_g2s(st + lay.vals_off, reinterpret_cast<const unsigned char *>(val) + v0, vb, &full[st_i]);
+            }
+        }
+        __syncwarp();
+        issued++;
+        return true;
+    };
+    if (wid == 0) {
+        while (issued < mine && issued < S - 1)
+            issue_next();
+    }
+    int i = 0;
+    for (; i < mine; i++) {
+        if (__any_sync(0xffffffffu, abort_k != 0))
+            break;
+        if (wid == 0 && issued < mine && !issue_next()) {
+            fail();
+            break;
+        }
+        const int st_i = i % S;
+        const int row = first_row(i) + rl;
+        float pv = 0.f;
+        uint8_t m = 0;
+        float4 bq = make_float4(0.f, 0.f, 0.f, 0.f), xq = bq;
+        if (row < n) {
+            if (sub < 9)
+                pv = Prow[(size_t)row * 9 + sub];
+            if (sub == 0) {
+                m = mask[row];
+                bq = __ldg(reinterpret_cast<const float4 *>(b) + row);
+                if (MODE == SM_SMOOTH)
+                    xq = __ldg(reinterpret_cast<const float4 *>(x) + row);
+            }
+        }
+        if (!warp_mbar_wait(&full[st_i], (unsigned)(i / S) & 1u)) {
+            fail();
+            break;
+        }
+        if (row < n) {
+            const unsigned char *st = stage_mem + (size_t)st_i * lay.stage_bytes;
+            const long long *ro = reinterpret_cast<const long long *>(st);
+            const int o = (int)(ro[rl] - ro[0]), np = (int)(ro[rl + 1] - ro[rl]);
+            const int *cs = reinterpret_cast<const int *>(st + lay.cols_off) + o;
+            const __half *vr = reinterpret_cast<const __half *>(st + lay.vals_off + ((18 * ro[0]) & 15)) +
+                               9 * (size_t)o;
+            float y0 = 0.f, y1 = 0.f, y2 = 0.f;
+            for (int b0 = 4 * sub; b0 < np; b0 += 64) {
+                const int4 c4 = *reinterpret_cast<const int4 *>(cs + b0);
+                const int cc[4] = {c4.x, c4.y, c4.z, c4.w};
+                float v[9][4];
+#pragma unroll
+                for (int k = 0; k < 9; k++) {
+                    const uint2 t = *reinterpret_cast<const uint2 *>(vr + (size_t)k * np + b0);
+                    const float2 lo = __half22float2(*reinterpret_cast<const __half2 *>(&t.x));
+                    const float2 hi = __half22float2(*reinterpret_cast<const __half2 *>(&t.y));
+                    v[k][0] = lo.x;
+                    v[k][1] = lo.y;
+                    v[k][2] = hi.x;
+                    v[k][3] = hi.y;
+                }
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    float x0, x1, x2;
+                    load_xyz<float>(x + 4 * (size_t)cc[j], x0, x1, x2);
+                    y0 += v[0][j] * x0 + v[1][j] * x1 + v[2][j] * x2;
+                    y1 += v[3][j] * x0 + v[4][j] * x1 + v[5][j] * x2;
+                    y2 += v[6][j] * x0 + v[7][j] * x1 + v[8][j] * x2;
+                }
+            }
+#pragma unroll
+            for (int off = 8; off > 0; off >>= 1) {
+                y0 += __shfl_xor_sync(gmask, y0, off);
+                y1 += __shfl_xor_sync(gmask, y1, off);
+                y2 += __shfl_xor_sync(gmask, y2, off);
+            }
+            float P[9];
+#pragma unroll
+            for (int k = 0; k < 9; k++)
+                P[k] = __shfl_sync(gmask, pv, k, 16);
+            if (sub == 0) {
+                y0 *= s;
+                y1 *= s;
+                y2 *= s;
+                const float r[3] = {(m & 1) ? bq.x - y0 : 0.f, (m & 2) ? bq.y - y1 : 0.f,
+                                    (m & 4) ? bq.z - y2 : 0.f};
+                O *po = out + 4 * (size_t)row;
+                if (MODE == SM_RESID) {
+                    store_xyz<float>(po, r[0], r[1], r[2]);
+                } else {
+                    float d[3];
+                    pinv_apply9<float>(P, r, d);
+                    store_xyz<float>(po, (m & 1) ? xq.x + omega * d[0] : 0.f, (m & 2) ? xq.y + omega * d[1] : 0.f,
+                                     (m & 4) ? xq.z + omega * d[2] : 0.f);
+                }
+            }
+        }
+        __syncwarp();
+        if (lane == 0)
+            mbar_arrive(&empty[st_i]);
+    }
+    if (wid == 0) {
+        for (int k = i; k < issued; k++)
+            if (!warp_mbar_wait(&full[k % S], (unsigned)(k / S) & 1u))
+                break;
+    }
+}
+
 // out = omega Pinv mask(b): the first sweep from zero on level 0; bt = the
 // right-hand side (the PCG residual, FP64) in FP32 for the later sweeps
 __global__ void __launch_bounds__(ATPB) k_amg_jacobi0(int n, const uint8_t *__restrict__ mask,
@@ -409,10 +584,51 @@ static void k0_launch_l(Ctx &c, float omega, const float *x, const float *b, O *
                                                    omega, x, b, out, sc);
 }
 
-// level-0 pass with the autotuner's lanes per block row (tune.smooth_variant)
+// Stage layout of the streamed smoother for rows of at most max_npad blocks
+// (FP16 values: 18 bytes per block plus 16 for the aligned copy), the stage
+// counts with one and two CTAs per SM (0 where fewer than two stages fit),
+// and the kernels' dynamic shared-memory limit.
+void init_stream_smoother(Ctx &c, int max_npad)
+{
+    auto up = [](int v, int a) { return (v + a - 1) / a * a; };
+    c.smooth_cols_off = 256;
+    c.smooth_vals_off = c.smooth_cols_off + up(STREAM_ROWS * max_npad * 4, 128);
+    c.smooth_stage_bytes = c.smooth_vals_off + up(STREAM_ROWS * max_npad * 18 + 16, 128);
+    int optin = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device);
+    cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c.device);
+    const int reserve = 2048;
+    const int avail[2] = {std::min(optin, per_sm) - reserve, per_sm / 2 - reserve};
+    for (int k = 0; k < 2; k++) {
+        const int st = avail[k] > 0 ? std::min(STREAM_MAX_STAGES, avail[k] / c.smooth_stage_bytes) : 0;
+        c.smooth_stages[k] = st >= 2 ? st : 0;
+    }
+    const int bytes = c.smooth_stages[0] * c.smooth_stage_bytes;
+    if (bytes > 0) {
+        cudaFuncSetAttribute(k_amg_k0_stream<SM_SMOOTH, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        cudaFuncSetAttribute(k_amg_k0_stream<SM_SMOOTH, double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             bytes);
+        cudaFuncSetAttribute(k_amg_k0_stream<SM_RESID, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        cudaFuncSetAttribute(k_amg_k0_stream<SM_RESID, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    }
+    cudaGetLastError();
+}
+
+// level-0 pass with the autotuner's shape: streamed (tune.smooth_stream) or
+// register-fed with tune.smooth_variant's lanes per block row
 template <int MODE, typename O>
 static void k0_launch_m(Ctx &c, float omega, const float *x, const float *b, O *out, const CgScalars *sc)
 {
+    const int ss = c.tune.smooth_stream;
+    if (ss >= 1 && ss <= 2 && c.smooth_stages[ss - 1] >= 2) {
+        const StreamLayout lay = {c.smooth_stages[ss - 1], c.smooth_stage_bytes, c.smooth_cols_off,
+                                  c.smooth_vals_off};
+        const int g = (c.tune.sms > 0 ? c.tune.sms : 152) * ss;
+        k_amg_k0_stream<MODE, O><<<g, ATPB, (size_t)lay.stages * lay.stage_bytes, c.stream>>>(
+            c.n, c.rowoff, c.cols, c.mask, reinterpret_cast<const __half *>(c.Kh), c.kh_scale, c.Pinv_rf, omega,
+            x, b, out, sc, lay, c.status);
+        return;
+    }
     switch (c.tune.smooth_variant) {
     case 1:
         k0_launch_l<MODE, O, 8>(c, omega, x, b, out, sc);

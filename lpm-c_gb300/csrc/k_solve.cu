@@ -16,6 +16,7 @@
 // Reductions are deterministic: per-block partial sums, then the last block
 // adds them in a fixed order and updates the CG scalars.
 #include "lpm_internal.h"
+#include "stream_pipe.h"
 
 namespace lpm {
 
@@ -448,66 +449,6 @@ __global__ void __launch_bounds__(VTPB) k_spmv_diff(SpmvArgs a, const float *__r
 // that runs out sets LPM_STATUS_DEVICE_WAIT in the status word and ends the
 // kernel once the copies it issued have landed (again with bounded waits);
 // the CG stops (done = 3) after the kernel's dot product.
-constexpr int STREAM_ROWS = 16;  // 8 warps x 2 half-warps
-constexpr long long STREAM_WAIT_CYCLES = 2000000000LL;
-
-__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(unsigned long long *bar)
-{
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-
-// wait for the completion of the barrier's phase of the given parity;
-// false after STREAM_WAIT_CYCLES
-__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity)
-{
-    const unsigned a = smem_u32(bar);
-    const long long t0 = clock64();
-    for (;;) {
-        unsigned ok;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(ok)
-            : "r"(a), "r"(parity)
-            : "memory");
-        if (ok)
-            return true;
-        if (clock64() - t0 > STREAM_WAIT_CYCLES)
-            return false;
-    }
-}
-
-// global -> shared copy by the bulk-copy engine, completing on bar (both
-// addresses 16-byte aligned, size a multiple of 16)
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar)
-{
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
-}
-
-// A stage: the tile's 18 row offsets (144 B, rows r0 .. r0 + 17; the row
-// offset array is padded so the last tile's copy stays inside it), its
-// column indices at cols_off and its values at vals_off.
-struct StreamLayout {
-    int stages, stage_bytes, cols_off, vals_off;
-};
-
 template <bool DOT>
 __global__ void __launch_bounds__(VTPB, 1)
     k_spmv_diff_stream(SpmvArgs a, StreamLayout lay, const float *__restrict__ val, const float *__restrict__ rs,
@@ -554,7 +495,7 @@ __global__ void __launch_bounds__(VTPB, 1)
         }
         const long long b0 = __shfl_sync(0xffffffffu, pb0, j - jb);
         const long long b1 = __shfl_sync(0xffffffffu, pb1, j - jb);
-        if (j >= S && !mbar_wait(&empty[s], (unsigned)((j / S) - 1) & 1u))
+        if (j >= S && !warp_mbar_wait(&empty[s], (unsigned)((j / S) - 1) & 1u))
             return false;
         if (lane == 0) {
             unsigned char *st = stage_mem + (size_t)s * lay.stage_bytes;
@@ -577,7 +518,7 @@ __global__ void __launch_bounds__(VTPB, 1)
     double dot = 0.0;
     int i = 0;
     for (; i < mine; i++) {
-        if (abort_k)
+        if (__any_sync(0xffffffffu, abort_k != 0))
             break;
         if (wid == 0 && issued < mine && !issue_next()) {
             fail();
@@ -596,7 +537,7 @@ __global__ void __launch_bounds__(VTPB, 1)
             if (sub == 0)
                 m = a.mask[row];
         }
-        if (!mbar_wait(&full[s], (unsigned)(i / S) & 1u)) {
+        if (!warp_mbar_wait(&full[s], (unsigned)(i / S) & 1u)) {
             fail();
             break;
         }
@@ -663,7 +604,7 @@ __global__ void __launch_bounds__(VTPB, 1)
     // after a failed wait: let the copies issued past the last consumed tile land
     if (wid == 0) {
         for (int k = i; k < issued; k++)
-            if (!mbar_wait(&full[k % S], (unsigned)(k / S) & 1u))
+            if (!warp_mbar_wait(&full[k % S], (unsigned)(k / S) & 1u))
                 break;
     }
     if (DOT) {

@@ -354,6 +354,7 @@ static int alloc_specimen(Ctx &c)
         for (size_t i = 0; i < n; i++)
             max_npad = std::max(max_npad, h.npad[i]);
         init_stream_product(c, max_npad);
+        init_stream_smoother(c, max_npad);
     }
     LPM_CUDA(cudaMemcpy(c.npad, h.npad.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     LPM_CUDA(cudaMemcpy(c.cols, h.cols.data(), sizeof(int) * c.nblk, cudaMemcpyHostToDevice));
@@ -900,7 +901,8 @@ static int solve_amg(Ctx &c, const dvec4 *b, double bn, lpm_step_stats *st)
         // the level-0 smoother's FP16 stiffness
         if (!c.Kh || c.kh_cap != c.nblk) {
             drop_graphs(c);
-            if ((rc = dalloc(c.Kh, 9 * (size_t)c.nblk)))
+            // + 8 values: the streamed smoother copies whole 16-byte units
+            if ((rc = dalloc(c.Kh, 9 * (size_t)c.nblk + 8)))
                 return rc;
             c.kh_cap = c.nblk;
         }
@@ -1213,9 +1215,16 @@ int solve_device(Ctx &c, const dvec4 *b, lpm_step_stats *st)
 
 int assemble(Ctx &c)
 {
-    const bool fp32 = c.opts.precision == LPM_PREC_MIXED;
-    // the multigrid smoother reads an FP32 copy of the FP64 stiffness
-    const bool smooth32 = !fp32 && c.opts.preconditioner == LPM_PRECOND_AMG && c.nspec == 0;
+    const bool amg = c.opts.preconditioner == LPM_PRECOND_AMG && c.nspec == 0;
+    // FP32 assembly accumulates a block's contributions in FP32, so a block
+    // and its transpose, summed in different rows, differ by rounding.  The
+    // multigrid PCG needs a symmetric operator: there the FP32 stiffness is
+    // the rounding of the FP64 assembly (one rounding per value, and K_ij,
+    // K_ji agree to FP64 rounding before it), as it is for the FP64 path's
+    // smoother.  The FP64 values are then replaced by an exact copy of the
+    // FP32 ones for the reliable updates (solve_amg).
+    const bool fp32 = c.opts.precision == LPM_PREC_MIXED && !amg;
+    const bool smooth32 = amg;
     int rc;
     if ((fp32 || smooth32) && (!c.Kf || c.kf_cap != c.nblk)) {
         if ((rc = dalloc(c.Kf, 9 * (size_t)c.nblk)))
@@ -2572,9 +2581,11 @@ static void fill_tuning(const Ctx &c, lpm_tuning *t)
     t->spmv_blocks = spmv_variant_blocks(c.tune.spmv_variant);
     t->spmv_per_sm = c.tune.spmv_per_sm;
     t->cg_per_sm = c.tune.vec_per_sm;
-    t->smooth_lanes = c.tune.smooth_variant == 1 ? 8 : (c.tune.smooth_variant == 2 ? 4 : 16);
+    t->smooth_lanes =
+        c.tune.smooth_stream ? 16 : (c.tune.smooth_variant == 1 ? 8 : (c.tune.smooth_variant == 2 ? 4 : 16));
     t->smooth_ms = 0.0;
     t->diff_stream = c.tune.diff_stream;
+    t->smooth_stream = c.tune.smooth_stream;
 }
 
 }  // namespace lpm
@@ -2600,9 +2611,14 @@ int lpm_set_tuning(lpm_ctx *ctx, const lpm_tuning *t)
         return fail(LPM_ERR_ARG, "lpm_set_tuning: variant 0..3, blocks per SM 1.." +
                                      std::to_string(TUNE_MAX_PER_SM) + ", diff_stream 0..2");
     Ctx &c = ctx->c;
+    if (t->smooth_stream < 0 || t->smooth_stream > 2)
+        return fail(LPM_ERR_ARG, "lpm_set_tuning: smooth_stream 0..2");
     if (t->diff_stream > 0 && c.stream_stages[t->diff_stream - 1] < 2)
         return fail(LPM_ERR_ARG, "lpm_set_tuning: the streamed product's stages do not fit in shared memory");
+    if (t->smooth_stream > 0 && c.smooth_stages[t->smooth_stream - 1] < 2)
+        return fail(LPM_ERR_ARG, "lpm_set_tuning: the streamed smoother's stages do not fit in shared memory");
     c.tune.diff_stream = t->diff_stream;
+    c.tune.smooth_stream = t->smooth_stream;
     c.tune.spmv_variant = t->spmv_variant;
     c.tune.spmv_per_sm = t->spmv_per_sm;
     c.tune.vec_per_sm = t->cg_per_sm;
@@ -2682,6 +2698,10 @@ int lpm_autotune(lpm_ctx *ctx, lpm_tuning *out)
             double ms = 0.0;
             if ((rc = time_it(spmv, ms)))
                 break;
+            if (c.trace)
+                std::fprintf(stderr, "lpm: autotune streamed product, %d block(s) per SM, %d stages: %.4f ms "
+                                     "(best register-fed %.4f ms)\n",
+                             ds, c.stream_stages[ds - 1], ms, best_ms);
             if (ms < best_ms) {
                 best_ms = ms;
                 best.diff_stream = ds;
@@ -2697,6 +2717,7 @@ int lpm_autotune(lpm_ctx *ctx, lpm_tuning *out)
     double best_smooth = 0.0;
     if (amg && !rc) {
         best_smooth = 1e30;
+        c.tune.smooth_stream = 0;
         for (int v = 0; v < 3 && !rc; v++) {
             c.tune.smooth_variant = v;
             double ms = 0.0;
@@ -2706,6 +2727,30 @@ int lpm_autotune(lpm_ctx *ctx, lpm_tuning *out)
                 best_smooth = ms;
                 best.smooth_variant = v;
             }
+        }
+        // the streamed smoother with 1 and 2 CTAs per SM
+        best.smooth_stream = 0;
+        for (int ss = 1; ss <= 2 && !rc; ss++) {
+            if (c.smooth_stages[ss - 1] < 2)
+                continue;
+            c.tune.smooth_stream = ss;
+            double ms = 0.0;
+            if ((rc = time_it([&]() { launch_amg_smoother_pass(c); }, ms)))
+                break;
+            if (c.trace)
+                std::fprintf(stderr, "lpm: autotune streamed smoother, %d block(s) per SM, %d stages: %.4f ms "
+                                     "(best register-fed %.4f ms)\n",
+                             ss, c.smooth_stages[ss - 1], ms, best_smooth);
+            if (ms < best_smooth) {
+                best_smooth = ms;
+                best.smooth_stream = ss;
+            }
+        }
+        c.tune.smooth_stream = 0;
+        if (!rc) {
+            LPM_CUDA(cudaMemcpyAsync(c.status_host, c.status, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+            if (!(rc = sync(c)) && (*c.status_host & LPM_STATUS_DEVICE_WAIT))
+                rc = fail(LPM_ERR_DEVICE, "lpm_autotune: a wait of the streamed smoother ran out");
         }
     }
     double best_vec = 1e30;

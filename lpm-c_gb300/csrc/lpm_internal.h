@@ -196,6 +196,7 @@ struct BatchHost {
 struct Tune {
     int smooth_variant = 0;  // multigrid level-0 smoother: 16 (0), 8 (1) or 4 (2) lanes per block row
     int diff_stream = 0;     // difference-form product: register-fed (0) or streamed, 1 or 2 CTAs per SM
+    int smooth_stream = 0;   // multigrid level-0 smoother: register-fed (0) or streamed, 1 or 2 CTAs per SM
     int spmv_variant = 0;
     int spmv_per_sm = 8;  // SpMV thread blocks per SM (grid-stride over rows)
     int vec_per_sm = 8;   // PCG vector-kernel thread blocks per SM
@@ -283,6 +284,9 @@ struct Ctx {
     // SM (0: does not fit), bytes per stage and the offsets within a stage
     int stream_stages[2] = {0, 0};
     int stream_stage_bytes = 0, stream_cols_off = 0, stream_vals_off = 0;
+    // the same for the streamed level-0 smoother (FP16 values)
+    int smooth_stages[2] = {0, 0};
+    int smooth_stage_bytes = 0, smooth_cols_off = 0, smooth_vals_off = 0;
     unsigned *kh_max = nullptr;
     long long kh_cap = 0, kh_version = -1;
     // mixed multigrid: Kd holds the exact FP64 copy of Kf of this assembly
@@ -406,6 +410,7 @@ void launch_amg_vcycle(Ctx &c, const dvec4 *r, dvec4 *z);  // z = V(r), FP32 ins
 void launch_amg_smoother_pass(Ctx &c);  // one level-0 residual pass on scratch vectors (autotuner timing)
 void launch_amg_stiffness32(Ctx &c);  // Kf = (float) Kd, for the smoother under FP64 precision
 void init_stream_product(Ctx &c, int max_npad);  // layouts of the streamed product for the pattern
+void init_stream_smoother(Ctx &c, int max_npad); // and of the streamed level-0 smoother
 void launch_amg_stiffness16(Ctx &c);  // Kh = half(Kf / s), s = max |Kf| / 2^14 into kh_scale
 void launch_stiffness64_of32(Ctx &c); // Kd = (double) Kf, exactly
 int amg_prepare(Ctx &c);  // (re)build the hierarchy when missing, stale or the mask changed

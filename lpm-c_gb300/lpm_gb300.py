@@ -67,7 +67,7 @@ class Tuning(C.Structure):
     _fields_ = [("spmv_variant", C.c_int), ("spmv_lanes", C.c_int), ("spmv_blocks", C.c_int),
                 ("spmv_per_sm", C.c_int), ("cg_per_sm", C.c_int), ("spmv_ms", C.c_double),
                 ("spmv_ms_default", C.c_double), ("smooth_lanes", C.c_int), ("smooth_ms", C.c_double),
-                ("diff_stream", C.c_int)]
+                ("diff_stream", C.c_int), ("smooth_stream", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -297,9 +297,9 @@ class Specimen:
         self._check(self.L.lpm_autotune(self.h, C.byref(t)))
         return t.as_dict()
 
-    def set_tuning(self, spmv_variant=0, spmv_per_sm=8, cg_per_sm=8, diff_stream=0):
+    def set_tuning(self, spmv_variant=0, spmv_per_sm=8, cg_per_sm=8, diff_stream=0, smooth_stream=0):
         t = Tuning(spmv_variant=spmv_variant, spmv_per_sm=spmv_per_sm, cg_per_sm=cg_per_sm,
-                   diff_stream=diff_stream)
+                   diff_stream=diff_stream, smooth_stream=smooth_stream)
         self._check(self.L.lpm_set_tuning(self.h, C.byref(t)))
 
     def get_tuning(self):

@@ -1,8 +1,8 @@
 """The multigrid PCG's launch shapes: the streamed difference-form product
-(tiles of 16 rows copied into shared-memory stages by the bulk-copy engine)
-computes every row as the register-fed product does, and the autotuner's
-choice among the product and smoother shapes leaves later load steps where
-the untuned run puts them."""
+and the streamed level-0 smoother (tiles of 16 rows copied into
+shared-memory stages by the bulk-copy engine) compute every row as the
+register-fed kernels do, and the autotuner's choice among the product and
+smoother shapes leaves later load steps where the untuned run puts them."""
 import numpy as np
 import pytest
 
@@ -17,17 +17,23 @@ def _opts(G, precision):
                 cg_maxiter=2000)
 
 
-@pytest.mark.parametrize("edge,diff_stream", [(12, 1), (30, 1), (30, 2)])
-def test_streamed_product_follows_register_fed(gpu_lib, edge, diff_stream):
-    """SC 12^3: 108 tiles, fewer than thread blocks (most blocks get none).
-    SC 30^3: 1,688 tiles, the last one partial, and more tiles per thread
-    block than the ring has stages (the stage barriers change phase)."""
+@pytest.mark.parametrize("edge,precision,diff_stream,smooth_stream",
+                         [(12, 1, 1, 0), (30, 1, 1, 0), (30, 1, 2, 0), (12, 0, 0, 1), (30, 0, 0, 1), (30, 0, 0, 2),
+                          (30, 1, 1, 1)])
+def test_streamed_kernels_follow_register_fed(gpu_lib, edge, precision, diff_stream, smooth_stream):
+    """The streamed product (mixed) and the streamed level-0 smoother (both
+    precisions), alone and together.  SC 12^3: 108 tiles, fewer than thread
+    blocks (most blocks get none).  SC 30^3: 1,688 tiles, the last one
+    partial, and more tiles per thread block than the ring has stages (the
+    stage barriers change phase); the FP16 values of half of the tiles start
+    8 bytes off a 16-byte boundary."""
     G = gpu_lib
     case = cases.SCCase(n=edge, e_noise=0.05, newton_tol=1e-10)
-    ref, _ = sc_gpu(G, case, **_opts(G, G.PREC_MIXED))
-    st, _ = sc_gpu(G, case, **_opts(G, G.PREC_MIXED))
-    st.set_tuning(diff_stream=diff_stream)
-    assert st.get_tuning()["diff_stream"] == diff_stream
+    ref, _ = sc_gpu(G, case, **_opts(G, precision))
+    st, _ = sc_gpu(G, case, **_opts(G, precision))
+    st.set_tuning(diff_stream=diff_stream, smooth_stream=smooth_stream)
+    t = st.get_tuning()
+    assert t["diff_stream"] == diff_stream and t["smooth_stream"] == smooth_stream
     x0 = ref.get("xyz_initial")
     worst = 0.0
     for stp in case.schedule[:8]:
@@ -39,8 +45,8 @@ def test_streamed_product_follows_register_fed(gpu_lib, edge, diff_stream):
         err = float(np.abs(da - db).max() / np.abs(da).max())
         worst = max(worst, err)
         assert err <= 1e-9
-    print(f"\nSC {edge}^3, {diff_stream} block(s) per SM: displacements within {worst:.2e} of the register-fed "
-          f"product")
+    print(f"\nSC {edge}^3, precision {precision}, streamed product {diff_stream} / smoother {smooth_stream} "
+          f"block(s) per SM: displacements within {worst:.2e} of the register-fed kernels")
     ref.close()
     st.close()
 
@@ -62,6 +68,7 @@ def test_autotune_multigrid_then_solve(gpu_lib, precision):
             t = tun.autotune()
             assert t["smooth_lanes"] in (4, 8, 16) and t["smooth_ms"] > 0.0
             assert t["diff_stream"] in ((0, 1, 2) if precision == G.PREC_MIXED else (0,))
+            assert t["smooth_stream"] in (0, 1, 2)
         assert a["status"] == 0 and b["status"] == 0
         da, db = ref.get("xyz") - x0, tun.get("xyz") - x0
         assert np.abs(da - db).max() <= 1e-9 * np.abs(da).max()
