@@ -406,9 +406,10 @@ def assemble_line(args, case, partial, world, note=None):
 
 
 # DRAM bytes over algorithmic bytes of the PCG product, from the ncu capture
-# summarised in profiles/ (dram__bytes_read.sum + dram__bytes_write.sum of one
-# launch at SC 60^3, scaled by the block count)
-SPMV_TRAFFIC_OVER_ALG = 1.05288
+# of k_spmv_diff at SC 60^3 (dram__bytes_read.sum + dram__bytes_write.sum of
+# one launch, 547.11 MB over 519.69 MB; profiles/k_spmv_diff_sc60_full.md),
+# applied to the 1M-particle launch
+SPMV_TRAFFIC_OVER_ALG = 1.0528
 
 
 def amg_levels(n, coarse_blocks=150):
@@ -776,8 +777,9 @@ def run_fcc(args):
                      cg_maxiter=2000 if amg else 40000, mixed_vectors=64,
                      preconditioner=G.PRECOND_AMG if amg else G.PRECOND_BJ, recycle=RECYCLE)
         setup_s = time.perf_counter() - t0
+        warm = []
         for k in range(W):
-            s.load_step(cases.sc_bcs(case.schedule[k]))
+            warm.append(s.load_step(cases.sc_bcs(case.schedule[k])))
             if k == 0:
                 s.autotune()
         torch.cuda.synchronize()
@@ -788,7 +790,7 @@ def run_fcc(args):
         stats = [s.load_step(cases.sc_bcs(case.schedule[k])) for k in range(W, W + K)]
         ev1.record(stream)
         torch.cuda.synchronize()
-        out[name] = dict(ms=ev0.elapsed_time(ev1), stats=stats, clocks=clocks.stop(), n=n, setup_s=setup_s,
+        out[name] = dict(ms=ev0.elapsed_time(ev1), stats=stats, warm=warm, clocks=clocks.stop(), n=n, setup_s=setup_s,
                          du=s.get("xyz") - s.get("xyz_initial"), A=s.get("cp_A"))
         s.close()
     m, f = out["mixed"], out["fp64"]
@@ -810,7 +812,10 @@ def run_fcc(args):
                    "fp64_newton_iters": agg(f["stats"], "newton_iters"), "fp64_cg_iters": agg(f["stats"], "cg_iters"),
                    "newton_iters_per_step": [st["newton_iters"] for st in m["stats"]],
                    "cg_iters_per_step": [st["cg_iters"] for st in m["stats"]],
-                   "recycle": RECYCLE, "max_cp_A": float(m["A"].max())},
+                   "recycle": RECYCLE, "max_cp_A": float(m["A"].max()),
+                   "fp64_fallbacks": agg(m["stats"], "fp64_fallbacks") + agg(m.get("warm", []), "fp64_fallbacks"),
+                   "fp64_fallback_note": "mixed solves that failed with FP32 products and were redone with FP64 "
+                                         "ones (the context keeps FP64 products from then on)"},
         "clocks": m["clocks"], "e2e": None, "cpu_baseline": None,
     }
     print(json.dumps(line))
@@ -856,8 +861,8 @@ def main():
                     help="sc: the 1M-particle SC cyclic case (default); batch: 256 specimens; "
                          "adjoint: gradients on the notched plate; fcc: crystal plasticity")
     ap.add_argument("--fcc-cells", type=int, default=80)
-    ap.add_argument("--fcc-warmup", type=int, default=3,
-                    help="warm-up load steps of the fcc workload")
+    ap.add_argument("--fcc-warmup", type=int, default=10,
+                    help="warm-up load steps of the fcc workload (the crystal yields in step 10 or 11)")
     ap.add_argument("--adj-strain", type=float, default=0.01)
     ap.add_argument("--nspec", type=int, default=256)
     ap.add_argument("--plate-n", type=int, default=200)

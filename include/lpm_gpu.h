@@ -120,6 +120,8 @@ typedef struct {
     int bonds_broken;    /* damage stage: sum of updateDamageGeneral's return values over the passes */
     int amg_builds;      /* AMG: hierarchy builds during the step */
     double ms_amg_build; /* AMG: host time of those builds (stiffness download, setup, upload) */
+    int fp64_fallbacks;  /* mixed multigrid: solves that failed with FP32 products and were redone
+                            with FP64 ones (the context keeps FP64 products from then on) */
 } lpm_step_stats;
 
 /* ---- context ------------------------------------------------------------ */

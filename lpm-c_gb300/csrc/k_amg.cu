@@ -681,7 +681,7 @@ __global__ void k_to_double(long long count, const float *__restrict__ in, doubl
 void launch_stiffness64_of32(Ctx &c)
 {
     const long long count = 9 * c.nblk;
-    k_to_double<<<grid_for(c, count), ATPB, 0, c.stream>>>(count, c.Kf, c.Kd);
+    k_to_double<<<grid_for(c, count), ATPB, 0, c.stream>>>(count, c.Kf, c.Kc);
 }
 
 // max |v| as the bits of a non-negative float (which order like unsigned ints)

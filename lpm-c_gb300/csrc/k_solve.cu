@@ -1040,8 +1040,8 @@ void launch_spmv_batch(Ctx &c, const dvec4 *x, dvec4 *y, bool k32)
 
 void launch_refine_residual(Ctx &c, const dvec4 *x, const dvec4 *b, dvec4 *r, double bscale)
 {
-    if (c.kd_from_kf >= 0 && c.kd_from_kf == c.kf_version)
-        k_refine_res<false, double><<<red_grid(c), VTPB, 0, c.stream>>>(spmv_args(c), c.Kd, x, b, r, c.norms, 2,
+    if (c.kc_version >= 0 && c.kc_version == c.kf_version)
+        k_refine_res<false, double><<<red_grid(c), VTPB, 0, c.stream>>>(spmv_args(c), c.Kc, x, b, r, c.norms, 2,
                                                                         bscale);
     else
         k_refine_res<false, float><<<red_grid(c), VTPB, 0, c.stream>>>(spmv_args(c), c.Kf, x, b, r, c.norms, 2,

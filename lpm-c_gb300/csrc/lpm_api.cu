@@ -428,11 +428,13 @@ static int setup_common(Ctx &c, bool built = false)
     dfree(c.Kf);
     dfree(c.Kd);
     dfree(c.Kh);
-    c.kf_cap = c.kd_cap = c.kh_cap = 0;
+    dfree(c.Kc);
+    c.kf_cap = c.kd_cap = c.kh_cap = c.kc_cap = 0;
     c.kf_version = -1;
     c.kh_version = -1;
-    c.kd_from_kf = -1;
+    c.kc_version = -1;
     c.vec64_fallback = false;
+    c.amg_k64 = false;
     HostSetup &h = c.hs;
     if (!built) {
         const int brc = build_neighbors(h);
@@ -561,6 +563,7 @@ int lpm_set_solver(lpm_ctx *ctx, const lpm_solver_opts *o)
         c.amg->stale = true;
     c.opts = *o;
     c.vec64_fallback = false;
+    c.amg_k64 = false;
     if (prec_change)
         c.have_K = false;
     if (c.graph_fp64) {
@@ -885,7 +888,7 @@ static int solve_amg(Ctx &c, const dvec4 *b, double bn, lpm_step_stats *st)
         st->amg_builds += H.builds - builds0;
         st->ms_amg_build += H.build_ms;
     }
-    const bool k32 = c.opts.precision == LPM_PREC_MIXED;
+    const bool k32 = c.opts.precision == LPM_PREC_MIXED && !c.amg_k64;
     const double scale = 1.0 / bn;
     // The multigrid PCG gains a decade every one or two iterations, so a
     // reliable update per decade (inner_rtol 0.1) would cost a host round trip
@@ -909,17 +912,17 @@ static int solve_amg(Ctx &c, const dvec4 *b, double bn, lpm_step_stats *st)
         launch_amg_stiffness16(c);
         c.kh_version = c.kf_version;
     }
-    if (k32 && c.kd_from_kf != c.kf_version) {
+    if (k32 && c.kc_version != c.kf_version) {
         // the reliable updates' true residual reads an exact FP64 copy of
         // the FP32 stiffness (FP64 products without per-value conversions)
-        if (!c.Kd || c.kd_cap != c.nblk) {
+        if (!c.Kc || c.kc_cap != c.nblk) {
             drop_graphs(c);
-            if ((rc = dalloc(c.Kd, 9 * (size_t)c.nblk)))
+            if ((rc = dalloc(c.Kc, 9 * (size_t)c.nblk)))
                 return rc;
-            c.kd_cap = c.nblk;
+            c.kc_cap = c.nblk;
         }
         launch_stiffness64_of32(c);
-        c.kd_from_kf = c.kf_version;
+        c.kc_version = c.kf_version;
     }
     launch_amg_init(c, b, scale, k32 ? delta * delta : 0.0, k32);
     int sweeps = 0, it = 0, done = 0;
@@ -941,6 +944,25 @@ static int solve_amg(Ctx &c, const dvec4 *b, double bn, lpm_step_stats *st)
             sweeps >= c.opts.refine_maxiter)
             break;
         launch_amg_reliable(c, c.q_d);
+    }
+    if (k32 && (done == 2 || done == 3 || !std::isfinite(rel))) {
+        // FP32 products failed on this system (the FP32 rounding of an
+        // ill-conditioned stiffness moves its smallest eigenvalues by as much
+        // as they are): solve it again with the FP64 products of the FP64
+        // assembly (Kd), and keep those for the rest of the context
+        c.amg_k64 = true;
+        if (c.trace)
+            std::fprintf(stderr, "lpm: solve amg-fp32K failed (end %d, rel %.3e after %d iterations): FP64 "
+                                 "products from now on\n",
+                         done, rel, it);
+        if (st) {
+            st->cg_iters += it;
+            st->spmv_calls += it + sweeps;
+            st->refine_iters += sweeps;
+            st->fp64_fallbacks++;
+        }
+        drop_graphs(c);
+        return solve_amg(c, b, bn, st);
     }
     if (st) {
         st->cg_iters += it;
@@ -1091,7 +1113,7 @@ static bool spd_solve(std::vector<double> G, int h, int ld, std::vector<double> 
 // one, else the FP32 values with FP64 products
 static void true_residual(Ctx &c, const dvec4 *x, const dvec4 *b, dvec4 *r)
 {
-    if (c.opts.precision == LPM_PREC_FP64)
+    if (c.opts.precision == LPM_PREC_FP64 || c.amg_k64)
         launch_refine_residual64(c, c.Kd, x, b, r);
     else
         launch_refine_residual(c, x, b, r, 1.0);
@@ -1236,8 +1258,6 @@ int assemble(Ctx &c)
             return rc;
         c.kd_cap = c.nblk;
     }
-    if (!fp32)
-        c.kd_from_kf = -1;  // Kd is assembled in FP64 now
     launch_tangent_geometry(c);
     launch_assemble(c, fp32);
     c.k_version++;

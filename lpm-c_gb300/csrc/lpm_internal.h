@@ -289,9 +289,13 @@ struct Ctx {
     int smooth_stage_bytes = 0, smooth_cols_off = 0, smooth_vals_off = 0;
     unsigned *kh_max = nullptr;
     long long kh_cap = 0, kh_version = -1;
-    // mixed multigrid: Kd holds the exact FP64 copy of Kf of this assembly
-    // (-1: none), read by the reliable updates' true residual
-    long long kd_from_kf = -1;
+    // mixed multigrid: Kc is the exact FP64 copy of Kf of assembly kc_version
+    // (-1: none), read by the reliable updates' true residual; Kd keeps the
+    // FP64 assembly, for the FP64-product fallback (amg_k64: a mixed solve
+    // failed with FP32 products, and the context solves with FP64 ones since)
+    double *Kc = nullptr;
+    long long kc_cap = 0, kc_version = -1;
+    bool amg_k64 = false;
     dvec4 *b_d = nullptr;
     CgScalars *sc = nullptr;     // device
     CgScalars *sc_host = nullptr; // pinned mirror
@@ -412,7 +416,7 @@ void launch_amg_stiffness32(Ctx &c);  // Kf = (float) Kd, for the smoother under
 void init_stream_product(Ctx &c, int max_npad);  // layouts of the streamed product for the pattern
 void init_stream_smoother(Ctx &c, int max_npad); // and of the streamed level-0 smoother
 void launch_amg_stiffness16(Ctx &c);  // Kh = half(Kf / s), s = max |Kf| / 2^14 into kh_scale
-void launch_stiffness64_of32(Ctx &c); // Kd = (double) Kf, exactly
+void launch_stiffness64_of32(Ctx &c); // Kc = (double) Kf, exactly
 int amg_prepare(Ctx &c);  // (re)build the hierarchy when missing, stale or the mask changed
 void free_amg(Ctx &c);
 // solver (k_solve.cu)

@@ -75,6 +75,8 @@ double ***slip_vector, ***dLp, ***J2_beta, ***damage_D, ***cp_gy, ***cp_A_single
  * :528-546 per load step): off unless lpmh_set_damage is called */
 static int g_damage = 0, g_max_passes = 1000, g_step = 0;
 static char g_bondfile[1024];
+/* BC group per particle (lpmh_set_bc_groups); NULL: BCs select by type */
+static int *g_bc_group, g_bc_ngroup;
 
 /* ---- allocation helpers (src/lpm_basic.c:361-445 semantics) ---------------- */
 static double *d1(int n, double v)
@@ -203,6 +205,9 @@ int lpmh_setup(int lat, double rad, const double *bx, int nslip)
 {
     g_damage = 0;
     g_step = 0;
+    free(g_bc_group); /* a new specimen: BCs select by type until groups are set again */
+    g_bc_group = NULL;
+    g_bc_ngroup = 0;
     lattice = lat;
     dim = 3;
     radius = rad;
@@ -285,7 +290,6 @@ void lpmh_set_types(const int *t, int nt)
 }
 
 /* BC group label per particle (NULL: boundary conditions select by type) */
-static int *g_bc_group, g_bc_ngroup;
 
 void lpmh_set_bc_groups(const int *g, int ngroup)
 {

@@ -92,7 +92,8 @@ class StepStats(C.Structure):
                 ("spmv_calls", C.c_int), ("status", C.c_int), ("res0", C.c_double),
                 ("reac0", C.c_double), ("res_final", C.c_double), ("ms_stiffness", C.c_double),
                 ("ms_solve", C.c_double), ("ms_force", C.c_double), ("damage_passes", C.c_int),
-                ("bonds_broken", C.c_int), ("amg_builds", C.c_int), ("ms_amg_build", C.c_double)]
+                ("bonds_broken", C.c_int), ("amg_builds", C.c_int), ("ms_amg_build", C.c_double),
+                ("fp64_fallbacks", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
