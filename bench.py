@@ -381,8 +381,15 @@ def assemble_line(args, case, partial, world, note=None):
         cfg["mixed_arm"] = {k: v for k, v in mixed.items() if k in ("skipped", "incomplete")}
     if note:
         cfg["note"] = note
-    kernel = ("k_spmv_diff (difference-form FP32 block-CSR product of the mixed multigrid PCG)"
-              if args.precond == "amg" else "k_spmv<float, float4> (FP32 block-CSR SpMV)")
+    streamed = bool((mixed.get("tuning") or {}).get("diff_stream", 0)) and args.precond == "amg"
+    if streamed:
+        kernel = ("k_spmv_diff_stream (difference-form FP32 block-CSR product of the mixed multigrid PCG, "
+                  "stiffness streamed into shared memory by the bulk-copy engine)")
+    elif args.precond == "amg":
+        kernel = "k_spmv_diff (difference-form FP32 block-CSR product of the mixed multigrid PCG)"
+    else:
+        kernel = "k_spmv<float, float4> (FP32 block-CSR SpMV)"
+    traffic_ratio = SPMV_STREAM_TRAFFIC_OVER_ALG if streamed else SPMV_TRAFFIC_OVER_ALG
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": (mixed["ms"] / K) if done else None, "higher_is_better": True, "scaling": "weak",
@@ -392,7 +399,7 @@ def assemble_line(args, case, partial, world, note=None):
         "config": cfg,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": (achieved / hbm) if achieved else None,
-                     "traffic": (mixed["spmv_bytes"] * SPMV_TRAFFIC_OVER_ALG) if done else None,
+                     "traffic": (mixed["spmv_bytes"] * traffic_ratio) if done else None,
                      "kernel": kernel, "peak_source": peak_src,
                      "algorithmic_bytes_per_launch": mixed.get("spmv_bytes"),
                      "launches_sampled": mixed.get("spmv_cnt")},
@@ -410,6 +417,8 @@ def assemble_line(args, case, partial, world, note=None):
 # one launch, 547.11 MB over 519.69 MB; profiles/k_spmv_diff_sc60_full.md),
 # applied to the 1M-particle launch
 SPMV_TRAFFIC_OVER_ALG = 1.0528
+# the same for k_spmv_diff_stream (549.34 MB over 519.69 MB; profiles/k_spmv_diff_stream_sc60_full.md)
+SPMV_STREAM_TRAFFIC_OVER_ALG = 1.0571
 
 
 def amg_levels(n, coarse_blocks=150):
