@@ -890,12 +890,13 @@ def main():
     ap.add_argument("--cg-rtol", type=float, default=CG_RTOL,
                     help="sc workload: relative residual of the linear solves (the reference's solverCG "
                          "stops at 1e-8, src/solver.c:221)")
-    ap.add_argument("--diff-stream", type=int, default=DIFF_STREAM, choices=[-1, 0, 1, 2],
+    ap.add_argument("--diff-stream", type=int, default=DIFF_STREAM, choices=[-1, 0, 1, 2, 3],
                     help="sc workload, mixed multigrid: difference-form product fed by registers (0) or streamed "
-                         "through shared memory with 1 or 2 thread blocks per SM; -1 keeps the autotuner's choice")
-    ap.add_argument("--smooth-stream", type=int, default=SMOOTH_STREAM, choices=[-1, 0, 1, 2],
+                         "through shared memory (1, 2: tiles of 16 rows, 1 or 2 thread blocks per SM; 3: tiles of "
+                         "8 rows, 5 per SM); -1 keeps the autotuner's choice")
+    ap.add_argument("--smooth-stream", type=int, default=SMOOTH_STREAM, choices=[-1, 0, 1, 2, 3],
                     help="sc workload, multigrid: level-0 smoother fed by registers (0) or streamed through shared "
-                         "memory with 1 or 2 thread blocks per SM; -1 keeps the autotuner's choice")
+                         "memory (as --diff-stream; 3: 6 thread blocks per SM); -1 keeps the autotuner's choice")
     ap.add_argument("--recycle", type=int, default=RECYCLE,
                     help="earlier solutions of the load step each Newton solve starts from (0: from zero, "
                          "as the reference's solverCG)")

@@ -286,10 +286,12 @@ typedef struct lpm_tuning {
     int smooth_lanes;      /* output: lanes per block row of the multigrid level-0 smoother (16, 8, 4) */
     double smooth_ms;      /* lpm_autotune: time of one smoother pass in the chosen shape (0: not tuned) */
     int diff_stream;       /* mixed multigrid PCG: difference-form product fed by registers (0) or
-                              streamed through shared memory by the bulk-copy engine with 1 or 2
-                              thread blocks per SM (1, 2); same arithmetic per row */
+                              streamed through shared memory by the bulk-copy engine: tiles of 16
+                              rows with 1 or 2 thread blocks per SM (1, 2), tiles of 8 rows with 5
+                              (3); same arithmetic per row */
     int smooth_stream;     /* multigrid level-0 smoother: register-fed (0, smooth_lanes per row) or
-                              streamed as diff_stream (1, 2; 16 lanes per row) */
+                              streamed as diff_stream (1, 2; 3: tiles of 8 rows, 6 thread blocks per
+                              SM; 16 lanes per row) */
 } lpm_tuning;
 /* Time every SpMV shape (and vector-kernel grid) on the context's current
  * stiffness with CUDA events and keep the fastest.  Needs an assembled

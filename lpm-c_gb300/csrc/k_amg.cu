@@ -310,14 +310,18 @@ __global__ void __launch_bounds__(ATPB) k_amg_k0(int n, const long long *__restr
 // the one above (the value array is padded by 16 bytes), and the rows index
 // from the offset.  The row's own entries (block inverse, mask, b, x) are
 // loaded ahead of the stage wait.
-template <int MODE, typename O>
-__global__ void __launch_bounds__(ATPB, 1)
+// ROWS rows per tile, a half-warp per row: 16 (256 threads) or 8 (128
+// threads, six CTAs per SM)
+template <int MODE, typename O, int ROWS>
+__global__ void __launch_bounds__(ROWS * 16, ROWS == 16 ? 1 : 6)
     k_amg_k0_stream(int n, const long long *__restrict__ rowoff, const int *__restrict__ cols,
                     const uint8_t *__restrict__ mask, const __half *__restrict__ val, const float *__restrict__ kscale,
                     const float *__restrict__ Prow, float omega, const float *__restrict__ x,
                     const float *__restrict__ b, O *__restrict__ out, const CgScalars *sc, StreamLayout lay,
                     int *status)
 {
+    constexpr int NT = ROWS * 16;
+    constexpr unsigned RO_BYTES = (ROWS + 2) * 8;
     extern __shared__ __align__(128) unsigned char stage_mem[];
     __shared__ unsigned long long full[STREAM_MAX_STAGES], empty[STREAM_MAX_STAGES];
     __shared__ volatile int abort_k;
@@ -328,18 +332,18 @@ __global__ void __launch_bounds__(ATPB, 1)
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int sub = lane & 15, rl = 2 * wid + (lane >> 4);
     const unsigned gmask = 0xffffu << (lane & 16);
-    const int ntiles = (n + STREAM_ROWS - 1) / STREAM_ROWS;
+    const int ntiles = (n + ROWS - 1) / ROWS;
     const int mine = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     if (threadIdx.x == 0) {
         for (int k = 0; k < S; k++) {
             mbar_init(&full[k], 1);
-            mbar_init(&empty[k], ATPB / 32);
+            mbar_init(&empty[k], NT / 32);
         }
         abort_k = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    auto first_row = [&](int i) { return ((int)blockIdx.x + i * (int)gridDim.x) * STREAM_ROWS; };
+    auto first_row = [&](int i) { return ((int)blockIdx.x + i * (int)gridDim.x) * ROWS; };
     auto fail = [&]() {
         atomicOr(status, LPM_STATUS_DEVICE_WAIT);
         abort_k = 1;
@@ -353,7 +357,7 @@ __global__ void __launch_bounds__(ATPB, 1)
             if (jb + lane < mine) {
                 const int r0 = first_row(jb + lane);
                 pb0 = rowoff[r0];
-                pb1 = rowoff[min(r0 + STREAM_ROWS, n)];
+                pb1 = rowoff[min(r0 + ROWS, n)];
             }
         }
         const long long b0 = __shfl_sync(0xffffffffu, pb0, j - jb);
@@ -365,8 +369,8 @@ __global__ void __launch_bounds__(ATPB, 1)
             const unsigned nb = (unsigned)(b1 - b0);
             const long long v0 = (18 * b0) & ~15LL, v1 = (18 * b1 + 15) & ~15LL;
             const unsigned vb = nb ? (unsigned)(v1 - v0) : 0u;
-            mbar_expect_tx(&full[st_i], 144u + 4u * nb + vb);
-            bulk_g2s(st, rowoff + first_row(j), 144u, &full[st_i]);
+            mbar_expect_tx(&full[st_i], RO_BYTES + 4u * nb + vb);
+            bulk_g2s(st, rowoff + first_row(j), RO_BYTES, &full[st_i]);
             if (nb) {
                 bulk_g2s(st + lay.cols_off, cols + b0, 4u * nb, &full[st_i]);
                 bulk_g2s(st + lay.vals_off, reinterpret_cast<const unsigned char *>(val) + v0, vb, &full[st_i]);
@@ -584,32 +588,44 @@ static void k0_launch_l(Ctx &c, float omega, const float *x, const float *b, O *
                                                    omega, x, b, out, sc);
 }
 
-// Stage layout of the streamed smoother for rows of at most max_npad blocks
-// (FP16 values: 18 bytes per block plus 16 for the aligned copy), the stage
-// counts with one and two CTAs per SM (0 where fewer than two stages fit),
-// and the kernels' dynamic shared-memory limit.
+// Stage layouts of the streamed smoother's variants for rows of at most
+// max_npad blocks (FP16 values: 18 bytes per block plus 16 for the aligned
+// copy): tiles of 16 rows with one or two CTAs per SM, tiles of 8 rows with
+// six; 0 stages where fewer than two fit.  Also lifts the kernels' dynamic
+// shared-memory limit.
+template <int ROWS>
+static void stream_smoother_limit(int bytes)
+{
+    cudaFuncSetAttribute(k_amg_k0_stream<SM_SMOOTH, float, ROWS>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_amg_k0_stream<SM_SMOOTH, double, ROWS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         bytes);
+    cudaFuncSetAttribute(k_amg_k0_stream<SM_RESID, float, ROWS>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_amg_k0_stream<SM_RESID, double, ROWS>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
 void init_stream_smoother(Ctx &c, int max_npad)
 {
     auto up = [](int v, int a) { return (v + a - 1) / a * a; };
-    c.smooth_cols_off = 256;
-    c.smooth_vals_off = c.smooth_cols_off + up(STREAM_ROWS * max_npad * 4, 128);
-    c.smooth_stage_bytes = c.smooth_vals_off + up(STREAM_ROWS * max_npad * 18 + 16, 128);
     int optin = 0, per_sm = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device);
     cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c.device);
-    const int reserve = 2048;
-    const int avail[2] = {std::min(optin, per_sm) - reserve, per_sm / 2 - reserve};
-    for (int k = 0; k < 2; k++) {
-        const int st = avail[k] > 0 ? std::min(STREAM_MAX_STAGES, avail[k] / c.smooth_stage_bytes) : 0;
+    const int rows[3] = {16, 16, 8}, ctas[3] = {1, 2, 6};
+    for (int k = 0; k < 3; k++) {
+        c.smooth_cols_off[k] = up((rows[k] + 2) * 8, 128);
+        c.smooth_vals_off[k] = c.smooth_cols_off[k] + up(rows[k] * max_npad * 4, 128);
+        c.smooth_stage_bytes[k] = c.smooth_vals_off[k] + up(rows[k] * max_npad * 18 + 16, 128);
+        const int avail = std::min(optin, per_sm / ctas[k]) - 2048;
+        const int st = avail > 0 ? std::min(STREAM_MAX_STAGES, avail / c.smooth_stage_bytes[k]) : 0;
         c.smooth_stages[k] = st >= 2 ? st : 0;
     }
-    const int bytes = c.smooth_stages[0] * c.smooth_stage_bytes;
-    if (bytes > 0) {
-        cudaFuncSetAttribute(k_amg_k0_stream<SM_SMOOTH, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-        cudaFuncSetAttribute(k_amg_k0_stream<SM_SMOOTH, double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             bytes);
-        cudaFuncSetAttribute(k_amg_k0_stream<SM_RESID, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-        cudaFuncSetAttribute(k_amg_k0_stream<SM_RESID, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    for (int k = 0; k < 3; k++) {
+        const int bytes = c.smooth_stages[k] * c.smooth_stage_bytes[k];
+        if (bytes <= 0)
+            continue;
+        if (rows[k] == 16)
+            stream_smoother_limit<16>(bytes);
+        else
+            stream_smoother_limit<8>(bytes);
     }
     cudaGetLastError();
 }
@@ -620,13 +636,19 @@ template <int MODE, typename O>
 static void k0_launch_m(Ctx &c, float omega, const float *x, const float *b, O *out, const CgScalars *sc)
 {
     const int ss = c.tune.smooth_stream;
-    if (ss >= 1 && ss <= 2 && c.smooth_stages[ss - 1] >= 2) {
-        const StreamLayout lay = {c.smooth_stages[ss - 1], c.smooth_stage_bytes, c.smooth_cols_off,
-                                  c.smooth_vals_off};
-        const int g = (c.tune.sms > 0 ? c.tune.sms : 152) * ss;
-        k_amg_k0_stream<MODE, O><<<g, ATPB, (size_t)lay.stages * lay.stage_bytes, c.stream>>>(
-            c.n, c.rowoff, c.cols, c.mask, reinterpret_cast<const __half *>(c.Kh), c.kh_scale, c.Pinv_rf, omega,
-            x, b, out, sc, lay, c.status);
+    if (ss >= 1 && ss <= 3 && c.smooth_stages[ss - 1] >= 2) {
+        const int k = ss - 1;
+        const StreamLayout lay = {c.smooth_stages[k], c.smooth_stage_bytes[k], c.smooth_cols_off[k],
+                                  c.smooth_vals_off[k]};
+        const size_t smem = (size_t)lay.stages * lay.stage_bytes;
+        const int sms = c.tune.sms > 0 ? c.tune.sms : 152;
+        const __half *kh = reinterpret_cast<const __half *>(c.Kh);
+        if (ss == 3)
+            k_amg_k0_stream<MODE, O, 8><<<sms * 6, 128, smem, c.stream>>>(
+                c.n, c.rowoff, c.cols, c.mask, kh, c.kh_scale, c.Pinv_rf, omega, x, b, out, sc, lay, c.status);
+        else
+            k_amg_k0_stream<MODE, O, 16><<<sms * ss, 256, smem, c.stream>>>(
+                c.n, c.rowoff, c.cols, c.mask, kh, c.kh_scale, c.Pinv_rf, omega, x, b, out, sc, lay, c.status);
         return;
     }
     switch (c.tune.smooth_variant) {

@@ -31,10 +31,10 @@ __device__ __forceinline__ double warp_sum(double s)
 
 // Block partial of NV values -> partials; last block reduces, then calls
 // fin(total) on thread 0.  All threads of the grid must call it.
-template <int NV, typename Fin>
+template <int NV, int NT = VTPB, typename Fin>
 __device__ void grid_reduce(double (&v)[NV], double *partials, unsigned *counter, Fin fin)
 {
-    __shared__ double red[NV][VTPB / 32];
+    __shared__ double red[NV][NT / 32];
     __shared__ bool last;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
@@ -48,7 +48,7 @@ __device__ void grid_reduce(double (&v)[NV], double *partials, unsigned *counter
 #pragma unroll
         for (int k = 0; k < NV; k++) {
             double s = 0.0;
-            for (int w = 0; w < VTPB / 32; w++)
+            for (int w = 0; w < NT / 32; w++)
                 s += red[k][w];
             partials[(size_t)k * gridDim.x + blockIdx.x] = s;
         }
@@ -62,7 +62,7 @@ __device__ void grid_reduce(double (&v)[NV], double *partials, unsigned *counter
 #pragma unroll
     for (int k = 0; k < NV; k++) {
         double s = 0.0;
-        for (unsigned b = threadIdx.x; b < gridDim.x; b += VTPB)
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += NT)
             s += __ldcg(&partials[(size_t)k * gridDim.x + b]);
         s = warp_sum(s);
         if (lane == 0)
@@ -74,7 +74,7 @@ __device__ void grid_reduce(double (&v)[NV], double *partials, unsigned *counter
 #pragma unroll
         for (int k = 0; k < NV; k++) {
             double s = 0.0;
-            for (int w = 0; w < VTPB / 32; w++)
+            for (int w = 0; w < NT / 32; w++)
                 s += red[k][w];
             tot[k] = s;
         }
@@ -435,7 +435,7 @@ __global__ void __launch_bounds__(VTPB) k_spmv_diff(SpmvArgs a, const float *__r
 // ---- streamed difference-form product ---------------------------------------
 // The product of k_spmv_diff<DOT, 16> (the same lanes, blocks and arithmetic
 // per row) with the stiffness stream decoupled from the gathers.  One CTA
-// per SM (or two) walks tiles of STREAM_ROWS consecutive rows, whose row
+// per SM (or several) walks tiles of consecutive rows, whose row
 // offsets, column indices and values are contiguous in the block-CSR arrays.
 // Thread 0 copies a tile into a ring of shared-memory stages with
 // cp.async.bulk, completing on the stage's mbarrier by byte count, up to
@@ -449,11 +449,16 @@ __global__ void __launch_bounds__(VTPB) k_spmv_diff(SpmvArgs a, const float *__r
 // that runs out sets LPM_STATUS_DEVICE_WAIT in the status word and ends the
 // kernel once the copies it issued have landed (again with bounded waits);
 // the CG stops (done = 3) after the kernel's dot product.
-template <bool DOT>
-__global__ void __launch_bounds__(VTPB, 1)
+// ROWS rows per tile, a half-warp per row: ROWS = 16 (256 threads, one or
+// two CTAs per SM) or 8 (128 threads, five CTAs per SM: more rows in
+// computation per SM for the same shared memory)
+template <bool DOT, int ROWS>
+__global__ void __launch_bounds__(ROWS * 16, ROWS == 16 ? 1 : 5)
     k_spmv_diff_stream(SpmvArgs a, StreamLayout lay, const float *__restrict__ val, const float *__restrict__ rs,
                        const SplitRec *__restrict__ split, dvec4 *__restrict__ y, int *status)
 {
+    constexpr int NT = ROWS * 16;
+    constexpr unsigned RO_BYTES = (ROWS + 2) * 8;  // the tile's row offsets, r0 .. r0 + ROWS + 1
     extern __shared__ __align__(128) unsigned char stage_mem[];
     __shared__ unsigned long long full[STREAM_MAX_STAGES], empty[STREAM_MAX_STAGES];
     __shared__ volatile int abort_k;
@@ -463,18 +468,18 @@ __global__ void __launch_bounds__(VTPB, 1)
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int sub = lane & 15, rl = 2 * wid + (lane >> 4);  // row of the tile
     const unsigned gmask = 0xffffu << (lane & 16);
-    const int ntiles = (n + STREAM_ROWS - 1) / STREAM_ROWS;
+    const int ntiles = (n + ROWS - 1) / ROWS;
     const int mine = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     if (threadIdx.x == 0) {
         for (int s = 0; s < S; s++) {
             mbar_init(&full[s], 1);
-            mbar_init(&empty[s], VTPB / 32);
+            mbar_init(&empty[s], NT / 32);
         }
         abort_k = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    auto first_row = [&](int i) { return ((int)blockIdx.x + i * (int)gridDim.x) * STREAM_ROWS; };
+    auto first_row = [&](int i) { return ((int)blockIdx.x + i * (int)gridDim.x) * ROWS; };
     auto fail = [&]() {
         atomicOr(status, LPM_STATUS_DEVICE_WAIT);
         abort_k = 1;
@@ -490,7 +495,7 @@ __global__ void __launch_bounds__(VTPB, 1)
             if (jb + lane < mine) {
                 const int r0 = first_row(jb + lane);
                 pb0 = a.rowoff[r0];
-                pb1 = a.rowoff[min(r0 + STREAM_ROWS, n)];
+                pb1 = a.rowoff[min(r0 + ROWS, n)];
             }
         }
         const long long b0 = __shfl_sync(0xffffffffu, pb0, j - jb);
@@ -500,8 +505,8 @@ __global__ void __launch_bounds__(VTPB, 1)
         if (lane == 0) {
             unsigned char *st = stage_mem + (size_t)s * lay.stage_bytes;
             const unsigned nb = (unsigned)(b1 - b0);
-            mbar_expect_tx(&full[s], 144u + 40u * nb);
-            bulk_g2s(st, a.rowoff + first_row(j), 144u, &full[s]);
+            mbar_expect_tx(&full[s], RO_BYTES + 40u * nb);
+            bulk_g2s(st, a.rowoff + first_row(j), RO_BYTES, &full[s]);
             if (nb) {
                 bulk_g2s(st + lay.cols_off, a.cols + b0, 4u * nb, &full[s]);
                 bulk_g2s(st + lay.vals_off, val + 9 * b0, 36u * nb, &full[s]);
@@ -610,7 +615,7 @@ __global__ void __launch_bounds__(VTPB, 1)
     if (DOT) {
         double v[1] = {dot};
         CgScalars *sc = a.sc;
-        grid_reduce<1>(v, a.partials, a.counter, [sc](const double *t) {
+        grid_reduce<1, NT>(v, a.partials, a.counter, [sc](const double *t) {
             sc->pq = t[0];
             sc->alpha = (t[0] != 0.0) ? sc->rz / t[0] : 0.0;
         });
@@ -1130,28 +1135,37 @@ void launch_row_sums(Ctx &c)
     k_row_sums<<<spmv_grid(c), VTPB, 0, c.stream>>>(c.n, c.rowoff, c.npad, c.Kf, c.Krs);
 }
 
-// Stage layout of the streamed product for rows of at most max_npad blocks,
-// and the stage count with one and with two CTAs per SM (0 where fewer than
-// two stages fit).  Also lifts the kernels' dynamic shared-memory limit.
+// Stage layouts of the streamed product's variants for rows of at most
+// max_npad blocks: tiles of 16 rows with one or two CTAs per SM, tiles of 8
+// rows with five; a variant gets 0 stages where fewer than two fit in its
+// share of shared memory.  Also lifts the kernels' dynamic shared-memory
+// limit.
 void init_stream_product(Ctx &c, int max_npad)
 {
     auto up = [](int v, int a) { return (v + a - 1) / a * a; };
-    c.stream_cols_off = 256;  // after the 144 bytes of row offsets
-    c.stream_vals_off = c.stream_cols_off + up(STREAM_ROWS * max_npad * 4, 128);
-    c.stream_stage_bytes = c.stream_vals_off + up(STREAM_ROWS * max_npad * 36, 128);
     int optin = 0, per_sm = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device);
     cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c.device);
-    const int reserve = 2048;  // static shared memory and the per-block reservation
-    const int avail[2] = {std::min(optin, per_sm) - reserve, per_sm / 2 - reserve};
-    for (int k = 0; k < 2; k++) {
-        const int st = avail[k] > 0 ? std::min(STREAM_MAX_STAGES, avail[k] / c.stream_stage_bytes) : 0;
+    const int rows[3] = {16, 16, 8}, ctas[3] = {1, 2, 5};
+    for (int k = 0; k < 3; k++) {
+        c.stream_cols_off[k] = up((rows[k] + 2) * 8, 128);
+        c.stream_vals_off[k] = c.stream_cols_off[k] + up(rows[k] * max_npad * 4, 128);
+        c.stream_stage_bytes[k] = c.stream_vals_off[k] + up(rows[k] * max_npad * 36, 128);
+        const int avail = std::min(optin, per_sm / ctas[k]) - 2048;  // static memory, per-block reservation
+        const int st = avail > 0 ? std::min(STREAM_MAX_STAGES, avail / c.stream_stage_bytes[k]) : 0;
         c.stream_stages[k] = st >= 2 ? st : 0;
     }
-    const int bytes = c.stream_stages[0] * c.stream_stage_bytes;
-    if (bytes > 0) {
-        cudaFuncSetAttribute(k_spmv_diff_stream<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-        cudaFuncSetAttribute(k_spmv_diff_stream<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    for (int k = 0; k < 3; k++) {
+        const int bytes = c.stream_stages[k] * c.stream_stage_bytes[k];
+        if (bytes <= 0)
+            continue;
+        if (rows[k] == 16) {
+            cudaFuncSetAttribute(k_spmv_diff_stream<true, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+            cudaFuncSetAttribute(k_spmv_diff_stream<false, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        } else {
+            cudaFuncSetAttribute(k_spmv_diff_stream<true, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+            cudaFuncSetAttribute(k_spmv_diff_stream<false, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        }
     }
     cudaGetLastError();
 }
@@ -1161,11 +1175,17 @@ static void spmv_diff_variant(Ctx &c, const SpmvArgs &a, dvec4 *y)
 {
     const SplitRec *sp = reinterpret_cast<const SplitRec *>(c.p_split);
     const int ds = c.tune.diff_stream;
-    if (ds >= 1 && ds <= 2 && c.stream_stages[ds - 1] >= 2) {
-        const StreamLayout lay = {c.stream_stages[ds - 1], c.stream_stage_bytes, c.stream_cols_off,
-                                  c.stream_vals_off};
-        k_spmv_diff_stream<DOT><<<sm_count(c) * ds, VTPB, (size_t)lay.stages * lay.stage_bytes, c.stream>>>(
-            a, lay, c.Kf, c.Krs, sp, y, c.status);
+    if (ds >= 1 && ds <= 3 && c.stream_stages[ds - 1] >= 2) {
+        const int k = ds - 1;
+        const StreamLayout lay = {c.stream_stages[k], c.stream_stage_bytes[k], c.stream_cols_off[k],
+                                  c.stream_vals_off[k]};
+        const size_t smem = (size_t)lay.stages * lay.stage_bytes;
+        if (ds == 3)
+            k_spmv_diff_stream<DOT, 8><<<sm_count(c) * 5, 128, smem, c.stream>>>(a, lay, c.Kf, c.Krs, sp, y,
+                                                                                c.status);
+        else
+            k_spmv_diff_stream<DOT, 16><<<sm_count(c) * ds, 256, smem, c.stream>>>(a, lay, c.Kf, c.Krs, sp, y,
+                                                                                  c.status);
         return;
     }
     const int g = spmv_grid(c);

@@ -2627,12 +2627,12 @@ int lpm_set_tuning(lpm_ctx *ctx, const lpm_tuning *t)
         return fail(LPM_ERR_ARG, "null argument");
     auto ok_grid = [](int v) { return v >= 1 && v <= TUNE_MAX_PER_SM; };
     if (t->spmv_variant < 0 || t->spmv_variant > 3 || !ok_grid(t->spmv_per_sm) || !ok_grid(t->cg_per_sm) ||
-        t->diff_stream < 0 || t->diff_stream > 2)
+        t->diff_stream < 0 || t->diff_stream > 3)
         return fail(LPM_ERR_ARG, "lpm_set_tuning: variant 0..3, blocks per SM 1.." +
-                                     std::to_string(TUNE_MAX_PER_SM) + ", diff_stream 0..2");
+                                     std::to_string(TUNE_MAX_PER_SM) + ", diff_stream 0..3");
     Ctx &c = ctx->c;
-    if (t->smooth_stream < 0 || t->smooth_stream > 2)
-        return fail(LPM_ERR_ARG, "lpm_set_tuning: smooth_stream 0..2");
+    if (t->smooth_stream < 0 || t->smooth_stream > 3)
+        return fail(LPM_ERR_ARG, "lpm_set_tuning: smooth_stream 0..3");
     if (t->diff_stream > 0 && c.stream_stages[t->diff_stream - 1] < 2)
         return fail(LPM_ERR_ARG, "lpm_set_tuning: the streamed product's stages do not fit in shared memory");
     if (t->smooth_stream > 0 && c.smooth_stages[t->smooth_stream - 1] < 2)
@@ -2711,7 +2711,7 @@ int lpm_autotune(lpm_ctx *ctx, lpm_tuning *out)
     // the streamed difference-form product with 1 and 2 CTAs per SM
     best.diff_stream = 0;
     if (diff && !rc) {
-        for (int ds = 1; ds <= 2 && !rc; ds++) {
+        for (int ds = 1; ds <= 3 && !rc; ds++) {
             if (c.stream_stages[ds - 1] < 2)
                 continue;
             c.tune.diff_stream = ds;
@@ -2719,8 +2719,8 @@ int lpm_autotune(lpm_ctx *ctx, lpm_tuning *out)
             if ((rc = time_it(spmv, ms)))
                 break;
             if (c.trace)
-                std::fprintf(stderr, "lpm: autotune streamed product, %d block(s) per SM, %d stages: %.4f ms "
-                                     "(best register-fed %.4f ms)\n",
+                std::fprintf(stderr, "lpm: autotune streamed product, variant %d, %d stages: %.4f ms "
+                                     "(best so far %.4f ms)\n",
                              ds, c.stream_stages[ds - 1], ms, best_ms);
             if (ms < best_ms) {
                 best_ms = ms;
@@ -2750,7 +2750,7 @@ int lpm_autotune(lpm_ctx *ctx, lpm_tuning *out)
         }
         // the streamed smoother with 1 and 2 CTAs per SM
         best.smooth_stream = 0;
-        for (int ss = 1; ss <= 2 && !rc; ss++) {
+        for (int ss = 1; ss <= 3 && !rc; ss++) {
             if (c.smooth_stages[ss - 1] < 2)
                 continue;
             c.tune.smooth_stream = ss;
@@ -2758,8 +2758,8 @@ int lpm_autotune(lpm_ctx *ctx, lpm_tuning *out)
             if ((rc = time_it([&]() { launch_amg_smoother_pass(c); }, ms)))
                 break;
             if (c.trace)
-                std::fprintf(stderr, "lpm: autotune streamed smoother, %d block(s) per SM, %d stages: %.4f ms "
-                                     "(best register-fed %.4f ms)\n",
+                std::fprintf(stderr, "lpm: autotune streamed smoother, variant %d, %d stages: %.4f ms "
+                                     "(best so far %.4f ms)\n",
                              ss, c.smooth_stages[ss - 1], ms, best_smooth);
             if (ms < best_smooth) {
                 best_smooth = ms;

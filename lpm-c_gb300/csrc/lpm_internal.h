@@ -195,8 +195,8 @@ struct BatchHost {
 // 3 = 4 x 4 (lanes per block row x consecutive blocks per lane).
 struct Tune {
     int smooth_variant = 0;  // multigrid level-0 smoother: 16 (0), 8 (1) or 4 (2) lanes per block row
-    int diff_stream = 0;     // difference-form product: register-fed (0) or streamed, 1 or 2 CTAs per SM
-    int smooth_stream = 0;   // multigrid level-0 smoother: register-fed (0) or streamed, 1 or 2 CTAs per SM
+    int diff_stream = 0;     // difference-form product: register-fed (0) or streamed (1..3)
+    int smooth_stream = 0;   // multigrid level-0 smoother: register-fed (0) or streamed (1..3)
     int spmv_variant = 0;
     int spmv_per_sm = 8;  // SpMV thread blocks per SM (grid-stride over rows)
     int vec_per_sm = 8;   // PCG vector-kernel thread blocks per SM
@@ -280,13 +280,15 @@ struct Ctx {
     // level-0 smoother, of the assembly numbered kh_version
     unsigned short *Kh = nullptr;
     float *kh_scale = nullptr;
-    // streamed difference-form product: stages per CTA with 1 and 2 CTAs per
-    // SM (0: does not fit), bytes per stage and the offsets within a stage
-    int stream_stages[2] = {0, 0};
-    int stream_stage_bytes = 0, stream_cols_off = 0, stream_vals_off = 0;
-    // the same for the streamed level-0 smoother (FP16 values)
-    int smooth_stages[2] = {0, 0};
-    int smooth_stage_bytes = 0, smooth_cols_off = 0, smooth_vals_off = 0;
+    // streamed difference-form product, per variant (tune.diff_stream - 1:
+    // tiles of 16 rows with 1 or 2 CTAs per SM, tiles of 8 rows with 5):
+    // stages per CTA (0: does not fit), bytes per stage, offsets in a stage
+    int stream_stages[3] = {0, 0, 0};
+    int stream_stage_bytes[3] = {0, 0, 0}, stream_cols_off[3] = {0, 0, 0}, stream_vals_off[3] = {0, 0, 0};
+    // the same for the streamed level-0 smoother (FP16 values; variant 3:
+    // tiles of 8 rows with 6 CTAs per SM)
+    int smooth_stages[3] = {0, 0, 0};
+    int smooth_stage_bytes[3] = {0, 0, 0}, smooth_cols_off[3] = {0, 0, 0}, smooth_vals_off[3] = {0, 0, 0};
     unsigned *kh_max = nullptr;
     long long kh_cap = 0, kh_version = -1;
     // mixed multigrid: Kc is the exact FP64 copy of Kf of assembly kc_version

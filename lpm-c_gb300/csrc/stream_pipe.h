@@ -1,7 +1,7 @@
 // Shared-memory stage ring fed by the bulk-copy engine, for the kernels that
 // stream the block-CSR stiffness (the difference-form product in k_solve.cu,
 // the multigrid level-0 smoother in k_amg.cu).  A persistent CTA walks tiles
-// of STREAM_ROWS consecutive rows, whose row offsets, column indices and
+// of consecutive rows (16 or 8), whose row offsets, column indices and
 // values are contiguous in the block-CSR arrays; one thread copies a tile
 // into a stage with cp.async.bulk, completing on the stage's "full" mbarrier
 // by byte count, up to stages - 1 tiles ahead, and the warps release a stage
@@ -12,7 +12,6 @@
 
 namespace lpm {
 
-constexpr int STREAM_ROWS = 16;  // 8 warps x 2 half-warps
 constexpr long long STREAM_WAIT_CYCLES = 2000000000LL;
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }

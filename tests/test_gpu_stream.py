@@ -18,12 +18,14 @@ def _opts(G, precision):
 
 
 @pytest.mark.parametrize("edge,precision,diff_stream,smooth_stream",
-                         [(12, 1, 1, 0), (30, 1, 1, 0), (30, 1, 2, 0), (12, 0, 0, 1), (30, 0, 0, 1), (30, 0, 0, 2),
-                          (30, 1, 1, 1)])
+                         [(12, 1, 1, 0), (30, 1, 1, 0), (30, 1, 2, 0), (30, 1, 3, 0), (12, 0, 0, 1), (30, 0, 0, 1),
+                          (30, 0, 0, 2), (30, 0, 0, 3), (30, 1, 1, 1), (12, 1, 3, 3)])
 def test_streamed_kernels_follow_register_fed(gpu_lib, edge, precision, diff_stream, smooth_stream):
     """The streamed product (mixed) and the streamed level-0 smoother (both
-    precisions), alone and together.  SC 12^3: 108 tiles, fewer than thread
-    blocks (most blocks get none).  SC 30^3: 1,688 tiles, the last one
+    precisions), alone and together; variants 1 and 2 walk tiles of 16 rows
+    with 1 or 2 thread blocks per SM, variant 3 tiles of 8 rows with 5
+    (product) or 6 (smoother).  SC 12^3: 108 tiles of 16 rows, fewer than
+    thread blocks (most blocks get none).  SC 30^3: 1,688 tiles, the last one
     partial, and more tiles per thread block than the ring has stages (the
     stage barriers change phase); the FP16 values of half of the tiles start
     8 bytes off a 16-byte boundary."""
@@ -67,8 +69,8 @@ def test_autotune_multigrid_then_solve(gpu_lib, precision):
         if k == 0:
             t = tun.autotune()
             assert t["smooth_lanes"] in (4, 8, 16) and t["smooth_ms"] > 0.0
-            assert t["diff_stream"] in ((0, 1, 2) if precision == G.PREC_MIXED else (0,))
-            assert t["smooth_stream"] in (0, 1, 2)
+            assert t["diff_stream"] in ((0, 1, 2, 3) if precision == G.PREC_MIXED else (0,))
+            assert t["smooth_stream"] in (0, 1, 2, 3)
         assert a["status"] == 0 and b["status"] == 0
         da, db = ref.get("xyz") - x0, tun.get("xyz") - x0
         assert np.abs(da - db).max() <= 1e-9 * np.abs(da).max()
