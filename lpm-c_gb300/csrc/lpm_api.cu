@@ -2660,12 +2660,22 @@ int lpm_autotune(lpm_ctx *ctx, lpm_tuning *out)
     const bool amg = c.opts.preconditioner == LPM_PRECOND_AMG && c.nspec == 0 && c.amg && c.Kh &&
                      c.kh_version == c.kf_version;
     const bool diff = amg && k32 && c.krs_version == c.kf_version;
+    // the difference-form product is timed in the form the PCG launches (with
+    // p.q), on scratch CG scalars whose solve is never done
+    CgScalars *sc_run = c.sc, *sc_tune = nullptr;
+    if (diff) {
+        int arc = dalloc(sc_tune, 1);
+        if (arc)
+            return arc;
+    }
     auto spmv = [&]() {
-        if (!k32)
+        if (!k32) {
             launch_spmv_d(c, c.p_d, c.q_d, true, false);
-        else if (diff)
-            launch_spmv_diff(c, c.q_d, false);
-        else if (vec64)
+        } else if (diff) {
+            c.sc = sc_tune;
+            launch_spmv_diff(c, c.q_d, true);
+            c.sc = sc_run;
+        } else if (vec64)
             launch_spmv_fx(c, c.p_d, c.q_d, true, false);
         else
             launch_spmv_f(c, c.p_f, c.q_f, true, false);
@@ -2789,6 +2799,10 @@ int lpm_autotune(lpm_ctx *ctx, lpm_tuning *out)
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     c.time_spmv = timed;
+    if (sc_tune) {
+        cudaStreamSynchronize(c.stream);
+        dfree(sc_tune);
+    }
     if (rc) {
         c.tune = keep;
         return rc;
