@@ -618,15 +618,17 @@ void init_stream_smoother(Ctx &c, int max_npad)
         const int st = avail > 0 ? std::min(STREAM_MAX_STAGES, avail / c.smooth_stage_bytes[k]) : 0;
         c.smooth_stages[k] = st >= 2 ? st : 0;
     }
+    // one limit per kernel instantiation: the largest of the variants using it
+    int max16 = 0, max8 = 0;
     for (int k = 0; k < 3; k++) {
         const int bytes = c.smooth_stages[k] * c.smooth_stage_bytes[k];
-        if (bytes <= 0)
-            continue;
-        if (rows[k] == 16)
-            stream_smoother_limit<16>(bytes);
-        else
-            stream_smoother_limit<8>(bytes);
+        int &m = rows[k] == 16 ? max16 : max8;
+        m = std::max(m, bytes);
     }
+    if (max16 > 0)
+        stream_smoother_limit<16>(max16);
+    if (max8 > 0)
+        stream_smoother_limit<8>(max8);
     cudaGetLastError();
 }
 

@@ -1155,17 +1155,20 @@ void init_stream_product(Ctx &c, int max_npad)
         const int st = avail > 0 ? std::min(STREAM_MAX_STAGES, avail / c.stream_stage_bytes[k]) : 0;
         c.stream_stages[k] = st >= 2 ? st : 0;
     }
+    // one limit per kernel instantiation: the largest of the variants using it
+    int max16 = 0, max8 = 0;
     for (int k = 0; k < 3; k++) {
         const int bytes = c.stream_stages[k] * c.stream_stage_bytes[k];
-        if (bytes <= 0)
-            continue;
-        if (rows[k] == 16) {
-            cudaFuncSetAttribute(k_spmv_diff_stream<true, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-            cudaFuncSetAttribute(k_spmv_diff_stream<false, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-        } else {
-            cudaFuncSetAttribute(k_spmv_diff_stream<true, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-            cudaFuncSetAttribute(k_spmv_diff_stream<false, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-        }
+        int &m = rows[k] == 16 ? max16 : max8;
+        m = std::max(m, bytes);
+    }
+    if (max16 > 0) {
+        cudaFuncSetAttribute(k_spmv_diff_stream<true, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, max16);
+        cudaFuncSetAttribute(k_spmv_diff_stream<false, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, max16);
+    }
+    if (max8 > 0) {
+        cudaFuncSetAttribute(k_spmv_diff_stream<true, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, max8);
+        cudaFuncSetAttribute(k_spmv_diff_stream<false, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, max8);
     }
     cudaGetLastError();
 }
