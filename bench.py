@@ -870,8 +870,9 @@ def main():
                     help="sc: the 1M-particle SC cyclic case (default); batch: 256 specimens; "
                          "adjoint: gradients on the notched plate; fcc: crystal plasticity")
     ap.add_argument("--fcc-cells", type=int, default=80)
-    ap.add_argument("--fcc-warmup", type=int, default=10,
-                    help="warm-up load steps of the fcc workload (the crystal yields in step 10 or 11)")
+    ap.add_argument("--fcc-warmup", type=int, default=7,
+                    help="warm-up load steps of the fcc workload (at 80^3 cells the crystal first slips in "
+                         "step 8; time it with --steps 1)")
     ap.add_argument("--adj-strain", type=float, default=0.01)
     ap.add_argument("--nspec", type=int, default=256)
     ap.add_argument("--plate-n", type=int, default=200)
