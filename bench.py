@@ -417,8 +417,9 @@ def assemble_line(args, case, partial, world, note=None):
 # one launch, 547.11 MB over 519.69 MB; profiles/k_spmv_diff_sc60_full.md),
 # applied to the 1M-particle launch
 SPMV_TRAFFIC_OVER_ALG = 1.0528
-# the same for k_spmv_diff_stream (549.34 MB over 519.69 MB; profiles/k_spmv_diff_stream_sc60_full.md)
-SPMV_STREAM_TRAFFIC_OVER_ALG = 1.0571
+# the same for k_spmv_diff_stream in the autotuner's 8-row shape (549.56 MB over
+# 519.69 MB; profiles/k_spmv_diff_stream_sc60_full.md)
+SPMV_STREAM_TRAFFIC_OVER_ALG = 1.0575
 
 
 def amg_levels(n, coarse_blocks=150):
