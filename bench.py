@@ -414,11 +414,11 @@ def assemble_line(args, case, partial, world, note=None):
 
 # DRAM bytes over algorithmic bytes of the PCG product, from the ncu capture
 # of k_spmv_diff at SC 60^3 (dram__bytes_read.sum + dram__bytes_write.sum of
-# one launch, 547.11 MB over 519.69 MB; profiles/k_spmv_diff_sc60_full.md),
+# one launch, 547.11 MB over 519.69 MB; the ncu summary of k_spmv_diff under profiles/),
 # applied to the 1M-particle launch
 SPMV_TRAFFIC_OVER_ALG = 1.0528
 # the same for k_spmv_diff_stream in the autotuner's 8-row shape (549.56 MB over
-# 519.69 MB; profiles/k_spmv_diff_stream_sc60_full.md)
+# 519.69 MB; the ncu summary of k_spmv_diff_stream under profiles/)
 SPMV_STREAM_TRAFFIC_OVER_ALG = 1.0575
 
 
@@ -509,12 +509,12 @@ def run_e2e(args, case, precond, deadline):
 # Newton tolerance 1e-8, MAXITER 100), steps 1-25, measured on a GB300 with
 # FP64 multigrid-preconditioned solves to 1e-10; the count is the
 # reference's modified-Newton iteration, independent of the linear solver at
-# that solve accuracy (profiles/sc100_cyclic_steps.md).
+# that solve accuracy (the per-step counts are summarised under profiles/).
 NEWTON_PER_STEP_SC100 = [3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 8, 80, 88, 100, 100, 100, 100, 100, 100, 3, 3, 3, 3, 3]
 # Block-Jacobi PCG iterations per Newton iteration at SC 100^3 (FP64, to
 # 1e-8 relative, the tolerance of the reference's solverCG,
 # src/solver.c:221), measured on a GB300 over steps 4-8: 28,433 iterations
-# in 15 solves (profiles/sc100_cyclic_steps.md).
+# in 15 solves (summarised under profiles/ with the per-step counts).
 CG_PER_NEWTON_SC100 = 1895.5
 
 
