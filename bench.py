@@ -513,9 +513,10 @@ def run_e2e(args, case, precond, deadline):
 NEWTON_PER_STEP_SC100 = [3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 3, 8, 80, 88, 100, 100, 100, 100, 100, 100, 3, 3, 3, 3, 3]
 # Block-Jacobi PCG iterations per Newton iteration at SC 100^3 (FP64, to
 # 1e-8 relative, the tolerance of the reference's solverCG,
-# src/solver.c:221), measured on a GB300 over steps 4-8: 28,433 iterations
-# in 15 solves (summarised under profiles/ with the per-step counts).
-CG_PER_NEWTON_SC100 = 1895.5
+# src/solver.c:221, each solve from zero), measured on a GB300 over steps 4-8:
+# 26,016 iterations in 15 solves (summarised under profiles/ with the
+# per-step counts).
+CG_PER_NEWTON_SC100 = 1734.4
 
 
 def run_cpu_baseline(case, W, K):
