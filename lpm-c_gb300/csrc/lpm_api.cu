@@ -167,7 +167,7 @@ Ctx::~Ctx()
                     (void **)&rowoff, (void **)&npad, (void **)&cols, (void **)&Kd, (void **)&Kf,
                     (void **)&Pinv_d, (void **)&Pinv_f, (void **)&x_d, (void **)&r_d, (void **)&p_d,
                     (void **)&q_d, (void **)&z_d, (void **)&x_f, (void **)&r_f, (void **)&p_f, (void **)&q_f,
-                    (void **)&z_f, (void **)&p_split, (void **)&Pinv_rf, (void **)&Krs, (void **)&Kh, (void **)&kh_scale, (void **)&kh_max, (void **)&pl_flag, (void **)&b_d, (void **)&sc, (void **)&partials, (void **)&counter,
+                    (void **)&z_f, (void **)&p_split, (void **)&Pinv_rf, (void **)&Krs, (void **)&Kh, (void **)&Kc, (void **)&kh_scale, (void **)&kh_max, (void **)&pl_flag, (void **)&b_d, (void **)&sc, (void **)&partials, (void **)&counter,
                     (void **)&norms, (void **)&status};
     for (void **p : all)
         if (*p) {
