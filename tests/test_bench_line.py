@@ -49,6 +49,22 @@ def test_line_complete():
     json.dumps(line)
 
 
+def test_line_names_the_streamed_product():
+    """With the autotuner's streamed product the roofline names that kernel
+    and scales its own measured traffic ratio."""
+    c = cases.SCCase(n=10)
+    mixed = _arm(1000.0)
+    mixed["tuning"] = {"diff_stream": 3, "smooth_stream": 3}
+    line = bench.assemble_line(_args(), c, {"mixed": mixed, "fp64": _arm(2000.0), "e2e": None, "cpu": None}, 1)
+    rl = line["roofline"]
+    assert rl["kernel"].startswith("k_spmv_diff_stream")
+    assert abs(rl["traffic"] - 2.4e9 * bench.SPMV_STREAM_TRAFFIC_OVER_ALG) < 1.0
+    line = bench.assemble_line(_args(), c, {"mixed": _arm(1000.0), "fp64": _arm(2000.0), "e2e": None, "cpu": None},
+                               1)
+    assert line["roofline"]["kernel"].startswith("k_spmv_diff (")
+    assert abs(line["roofline"]["traffic"] - 2.4e9 * bench.SPMV_TRAFFIC_OVER_ALG) < 1.0
+
+
 def test_line_with_skipped_arms():
     c = cases.SCCase(n=10)
     line = bench.assemble_line(_args(), c, {"mixed": _arm(1000.0), "fp64": {"skipped": "budget: 10 s left"},
