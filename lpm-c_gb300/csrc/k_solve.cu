@@ -434,24 +434,22 @@ __global__ void __launch_bounds__(VTPB) k_spmv_diff(SpmvArgs a, const float *__r
 
 // ---- streamed difference-form product ---------------------------------------
 // The product of k_spmv_diff<DOT, 16> (the same lanes, blocks and arithmetic
-// per row) with the stiffness stream decoupled from the gathers.  One CTA
-// per SM (or several) walks tiles of consecutive rows, whose row
-// offsets, column indices and values are contiguous in the block-CSR arrays.
-// Thread 0 copies a tile into a ring of shared-memory stages with
-// cp.async.bulk, completing on the stage's mbarrier by byte count, up to
-// stages - 1 tiles ahead of the computation; every warp computes two rows of
-// the tile from shared memory (a half-warp per row) and gathers the split x
-// from L2.  The copy engine keeps the DRAM stream deep with no registers
-// held, where the register-fed kernel is limited to the loads its resident
-// warps have issued.
+// per row) with the stiffness stream decoupled from the gathers.  Persistent
+// CTAs walk tiles of ROWS consecutive rows, whose row offsets, column
+// indices and values are contiguous in the block-CSR arrays.  Thread 0
+// copies a tile into a ring of shared-memory stages with cp.async.bulk,
+// completing on the stage's mbarrier by byte count, up to stages - 1 tiles
+// ahead of the computation; every warp computes two rows of the tile from
+// shared memory (a half-warp per row) and gathers the split x from L2.  The
+// copy engine keeps the DRAM stream deep with no registers held, where the
+// register-fed kernel is limited to the loads its resident warps have issued.
+// ROWS = 16 (256 threads, one or two CTAs per SM) or 8 (128 threads, five
+// CTAs per SM: more rows in computation per SM for the same shared memory).
 //
 // Every mbarrier wait is bounded (STREAM_WAIT_CYCLES, about a second); one
 // that runs out sets LPM_STATUS_DEVICE_WAIT in the status word and ends the
 // kernel once the copies it issued have landed (again with bounded waits);
 // the CG stops (done = 3) after the kernel's dot product.
-// ROWS rows per tile, a half-warp per row: ROWS = 16 (256 threads, one or
-// two CTAs per SM) or 8 (128 threads, five CTAs per SM: more rows in
-// computation per SM for the same shared memory)
 template <bool DOT, int ROWS>
 __global__ void __launch_bounds__(ROWS * 16, ROWS == 16 ? 1 : 5)
     k_spmv_diff_stream(SpmvArgs a, StreamLayout lay, const float *__restrict__ val, const float *__restrict__ rs,

@@ -72,9 +72,10 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
                  : "memory");
 }
 
-// A stage: the tile's 18 row offsets (144 B, rows r0 .. r0 + 17; the row
-// offset array is padded so the last tile's copy stays inside it), its
-// column indices at cols_off and its values at vals_off.
+// A stage: the tile's ROWS + 2 row offsets (rows r0 .. r0 + ROWS + 1, a
+// multiple of 16 bytes; the row-offset array is padded so the last tile's
+// copy stays inside it), its column indices at cols_off and its values at
+// vals_off.
 struct StreamLayout {
     int stages, stage_bytes, cols_off, vals_off;
 };
